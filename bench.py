@@ -1,0 +1,267 @@
+"""Benchmark of the parallel-tempering hot path on GB300 (one JSON line on rank 0).
+
+Workload (default, the reference's published CE configuration): fcc Ni/Pt, 8x8x8 conventional cells = 2,048
+sites, synthetic per-orbit ECIs (cutoffs 8/6/5 A), int8 occupancy 50/50, R = 32 replicas on a geometric
+300-1400 K ladder, replica exchange every 5,000 steps, 200,000 steps per replica.  A bench "step" is one
+chunk of 5,000 MC steps for all 32 replicas followed by the on-device exchange (160,000 swap attempts);
+the whole job is 40 such steps.  Proposals come from the device Philox stream.
+
+  value     swap attempts/s with the state resident in HBM, CUDA events around each chunk on its stream,
+            L2 flushed (256 MB write) between timed chunks outside the events
+  e2e       the same chunks through nce_ce_run_chunk_host: pinned host buffers in and out every chunk
+  roofline  dominant kernel ce_pt_chunk_kernel; algorithmic bytes per attempt = 14,996 B of int8
+            member-occupancy reads (2 x 7,498 member slots of the rows of both sites)
+  cpu_baseline  the oracle's C restatement on the host cores (bounded sample, all threads)
+--impl reference times the oracle port on the host cores (the reference's own CPU paths, JAX and icet,
+are not installed on this image) with the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MC swap attempts/s (CE, NCE) vs plain FP64 form; p50/p99 PT-job latency"
+H100_PUBLISHED = 1_231_993.0          # reference CE PT, 2,048 sites, R=32, H100 (results/bench_stage/gpu_icet_*H100*.json)
+B_GATHER = 14_996                     # bytes of member occupancy per attempt, config-0 cluster set
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
+    ap.add_argument("--warps", type=int, default=0)
+    ap.add_argument("--L", type=int, default=8)
+    ap.add_argument("--R", type=int, default=32)
+    ap.add_argument("--chunk", type=int, default=5000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0")); world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index; self.p = None; self.path = None
+
+    def start(self):
+        import tempfile
+        fd, self.path = tempfile.mkstemp(suffix=".csv"); os.close(fd)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.strip()]
+        os.unlink(self.path)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1])); mx = max(mx, float(r[2]))
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                pass
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_oracle_rate(L, R, target_s=10.0, threads=None):
+    """attempts/s of the C oracle on the host cores for the same workload (bounded sample)."""
+    from neuralce_gb300.workloads import ce_config, ladder, replica_configs
+    from oracle.ce_oracle import OracleCE, new_state
+    threads = threads or os.cpu_count() or 1
+    gce, sig = ce_config(L, seed=0)
+    orc = OracleCE(gce.info)
+    sig_r = replica_configs(sig, R, 1)
+    _, beta = ladder(R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    st = new_state(sig_r, E0, beta)
+    t = time.perf_counter(); orc.run(st, 20, 0, seed=7, n_threads=threads); dt = time.perf_counter() - t
+    steps = max(20, int(20 * target_s / max(dt, 1e-6)))
+    t = time.perf_counter(); orc.run(st, steps, 20, seed=7, n_threads=threads); dt = time.perf_counter() - t
+    return R * steps / dt, threads, f"{R} replicas x {steps} steps of the {gce.n_atoms}-site job ({dt:.1f} s)"
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from neuralce_gb300.workloads import ce_config, ladder, replica_configs
+    from oracle.ce_oracle import OracleCE, new_state
+    threads = os.cpu_count() or 1
+    gce, sig = ce_config(args.L, seed=0)
+    orc = OracleCE(gce.info)
+    sig_r = replica_configs(sig, args.R, 1)
+    _, beta = ladder(args.R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    st = new_state(sig_r, E0, beta)
+    t = time.perf_counter(); orc.run(st, 10, 0, seed=7, n_threads=threads); dt = time.perf_counter() - t
+    per = max(10, int(10 * 2.0 / max(dt, 1e-6)))          # ~2 s per bench step
+    step0 = 10
+    for _ in range(args.warmup):
+        orc.run(st, per, step0, seed=7, n_threads=threads); step0 += per
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter(); orc.run(st, per, step0, seed=7, n_threads=threads, do_exchange=True)
+        times.append(time.perf_counter() - t); step0 += per
+    tot = sum(times); value = args.R * per * args.steps / tot
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "swap attempts/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args, gce),
+            "cpu_baseline": {"value": value, "unit": "swap attempts/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.R} replicas x {per} steps per bench step of the {gce.n_atoms}-site job; "
+                                       "C restatement of the reference delta path (JAX/icet CPU paths not installed)"},
+            "e2e": {"value": value, "unit": "swap attempts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, gce):
+    return {"workload": f"CE parallel tempering fp{args.precision}: fcc Ni/Pt {args.L}x{args.L}x{args.L} conventional "
+                        f"({gce.n_atoms} sites), R={args.R} replicas 300-1400 K, exchange every {args.chunk} steps, "
+                        f"{args.chunk * args.steps} steps per replica timed",
+            "sites": gce.n_atoms, "replicas": args.R, "steps_per_chunk": args.chunk, "cluster_set": "8/6/5 A (37 orbits)",
+            "proposals": "device Philox4x32-10", "l2": "flushed between timed chunks (256 MB write)",
+            "parallelism": f"replicas only: {args.gpus} independent job(s), one per GPU"}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.pt import PTState, run_chunk, make_chunk
+    from neuralce_gb300.workloads import ce_config, ladder, replica_configs
+    _lib.lib()
+    gce, sig = ce_config(args.L, seed=rank)
+    R, T = args.R, args.chunk
+    sig_r = replica_configs(sig, R, 1 + rank)
+    _, beta = ladder(R)
+    E0 = gce.batched_energy(torch.as_tensor(sig_r).cuda()).cpu().numpy()
+    st = PTState(sig_r, E0, beta, np.zeros(R, np.int32))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    step = 0
+    for _ in range(args.warmup):
+        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, 1, None, True); step += T
+    torch.cuda.synchronize()
+    clk = Clocks(local); clk.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, 1, None, True)
+        ev[k][1].record(stream)
+        step += T
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = clk.stop()
+    per_ms = [a.elapsed_time(b) for a, b in ev]
+    tot_s = sum(per_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([tot_s], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX); tot_s = float(t.item())
+    attempts = R * T * args.steps * world
+    value = attempts / tot_s
+    # e2e: same chunks with host buffers through the C-ABI (pinned host memory)
+    e2e = None
+    if not args.no_e2e:
+        import ctypes as C
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        h_sig = pin(st.sigma.cpu().numpy()); h_E = pin(st.E.cpu().numpy()); h_b = pin(beta)
+        h_ros = pin(st.rep_of_slot.cpu().numpy()); h_sor = pin(st.slot_of_rep.cpu().numpy()); h_lid = pin(np.zeros(R, np.int32))
+        h_emr = pin(st.E_min_rep.cpu().numpy()); h_nacc = pin(st.n_acc.cpu().numpy()); h_nex = pin(st.n_ex.cpu().numpy())
+        h_samp = pin(np.zeros((1, R)))
+        torch.cuda.synchronize()
+        ck = make_chunk(T, step, 42 + rank, args.precision, args.warps, None, T, None, True)
+        def host_call():
+            _lib.check(_lib.lib().nce_ce_run_chunk_host(gce.handle, R, h_sig.data_ptr(), h_E.data_ptr(), h_b.data_ptr(),
+                                                        h_ros.data_ptr(), h_sor.data_ptr(), h_lid.data_ptr(), h_emr.data_ptr(),
+                                                        h_nacc.data_ptr(), h_nex.data_ptr(), C.byref(ck), h_samp.data_ptr()),
+                       "nce_ce_run_chunk_host")
+        host_call(); ck.step0 += T      # warm the staging buffers
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            host_call(); ck.step0 += T
+        e2e_s = time.perf_counter() - t0
+        h2d = R * gce.n_atoms + R * (8 + 4 + 4 + 4 + 4 + 8 + 8) + 8
+        d2h = R * gce.n_atoms + R * (8 + 4 + 4 + 8 + 8) + 8 + 8 * R
+        e2e = {"value": R * T * args.steps * world / e2e_s, "unit": "swap attempts/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "api": "nce_ce_run_chunk_host"}
+    hbm, src = peaks()
+    ms_chunk = float(np.mean(per_ms))
+    achieved = R * T * B_GATHER / (ms_chunk / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+            "kernel": "ce_pt_chunk_kernel", "peak_source": src,
+            "algorithmic_bytes_per_launch": R * T * B_GATHER}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, cores, sample = cpu_oracle_rate(args.L, R)
+        cpu = {"value": v, "unit": "swap attempts/s", "cores": cores, "kind": "port", "sample": sample}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "swap attempts/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_chunk, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": value / H100_PUBLISHED if (args.L == 8 and args.R == 32) else None,
+                "dtype": "f64" if args.precision == 64 else "f32", "data": "synthetic (seeded lattice, random-normal ECIs)",
+                "config": workload_config(args, gce), "clocks": clocks, "e2e": e2e, "gpu_launches": 2 * args.steps,
+                "roofline": roof, "cpu_baseline": cpu,
+                "accept_rate": float(st.n_acc.sum().item()) / max(1, R * step)}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

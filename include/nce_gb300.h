@@ -1,0 +1,155 @@
+/* nce_gb300.h -- C ABI of libnce_gb300.so, the GB300 (sm_103a) engine for neuralce's parallel-tempering
+ * Monte Carlo hot path.
+ *
+ * Plain C types only: pointers, sizes, status codes.  Device pointers are CUDA global-memory addresses
+ * (a caller typically takes them from torch tensors); "stream" is a cudaStream_t passed as void*
+ * (NULL = legacy default stream).  Every function returns 0 (NCE_OK) or a negative NCE_ERR_* code;
+ * nce_last_error() gives the message of the calling thread's last failure.
+ *
+ * Threading: a handle may be used from one host thread at a time; calls are asynchronous on the given
+ * stream unless stated otherwise.  Table inputs are host pointers and are copied during *_create; the
+ * caller keeps ownership.
+ *
+ * Reference interfaces replaced (paths inside the neuralce project):
+ *   nce_ce_create        GPUClusterExpansion(..., table_mode='implicit')      neuralce/ce/classical_ce_gpu.py:496-535
+ *                        build_ce_gpu_implicit tables                         neuralce/ce/ce_gpu_implicit.py:50-126
+ *   nce_ce_energy        GPUClusterExpansion.energy_a / energy               neuralce/ce/ce_gpu_implicit.py:147-163
+ *   nce_ce_delta         GPUClusterExpansion.delta_energy_a                  neuralce/ce/ce_gpu_implicit.py:181-191
+ *   nce_ce_run_chunk     run_chunk = scan(micro) + exchange_slots            neuralce/ce/pt_mcmc_ce.py:748-818
+ *                        (mc_step delta branch                               neuralce/ce/pt_mcmc_ce.py:558-566,
+ *                         make_fast_swap_implicit proposal                   neuralce/ce/ce_gpu_implicit.py:194-211)
+ *   nce_ce_run_batch     vmap over independent jobs of run_chunk             neuralce/ce/pt_mcmc_ce.py:733,765-818
+ *   nce_ce_run_chunk_host  same as nce_ce_run_chunk with host buffers (the e2e call of a host-side driver)
+ *   nce_philox4x32       counter-based RNG used on the device (replaces jax.random keys in micro, pt_mcmc_ce.py:773-774)
+ */
+#ifndef NCE_GB300_H
+#define NCE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NCE_OK                 0
+#define NCE_ERR_INVALID       -1   /* bad argument (size, pointer, range) */
+#define NCE_ERR_CUDA          -2   /* a CUDA call failed */
+#define NCE_ERR_UNSUPPORTED   -3   /* valid but not supported by this build (e.g. cluster order > 8) */
+#define NCE_ERR_TIMEOUT       -4   /* a bounded device wait gave up */
+#define NCE_ERR_NOMEM         -5   /* device allocation failed / admission refused */
+
+int nce_version(void);
+/* Copies the calling thread's last error message into buf (NUL-terminated); returns its full length. */
+int nce_last_error(char *buf, size_t len);
+
+/* ── cluster expansion (orthonormal, template-only tables) ──────────────────────────────────────── */
+
+typedef struct {
+    int32_t nB;            /* basis sites of the primitive */
+    int32_t J;             /* reverse rows per basis site (padded) */
+    int32_t mo;            /* maximum cluster order (members per row), 1..8 */
+    int32_t n_nbr;         /* neighbourhood entries per basis site (entry 0 = the site itself) */
+    int32_t n_pfc;         /* point-function columns = n_sublattices * (max_bf + 1) */
+    int32_t max_sp;        /* species per site, maximum over sublattices */
+    int64_t d[3];          /* Smith-normal-form diagonal of the supercell */
+    int64_t n_cells;       /* primitive cells in the supercell = d0*d1*d2 */
+    double zerolet;        /* constant term (already multiplied by energy_scale) */
+    const int32_t *Rv_len; /* (nB) valid reverse rows per basis site */
+    const uint16_t *Rv_loc;/* (nB, J, mo) neighbourhood index of each row member */
+    const uint8_t *Rv_pfc; /* (nB, J, mo) point-function column of each row member */
+    const double *Rv_eci;  /* (nB, J) eci per row = eci * scale / (instances * n_cells); padded rows 0 */
+    const int32_t *nb_b;   /* (nB, n_nbr) basis of each neighbourhood entry */
+    const int32_t *nb_uo;  /* (nB, n_nbr, 3) U*offset mod d of each neighbourhood entry */
+    int32_t Rt;            /* template rows (full energy) */
+    const int32_t *T_b;    /* (Rt, mo) */
+    const int32_t *T_uo;   /* (Rt, mo, 3) */
+    const uint8_t *T_pfc;  /* (Rt, mo) */
+    const double *T_eci;   /* (Rt) */
+    const double *pf;      /* (n_pfc, max_sp) point-function values */
+    int32_t n_groups;      /* active sublattices (swap groups) */
+    int32_t max_gb;        /* basis sites per group, maximum */
+    const int32_t *act_b;  /* (n_groups, max_gb) basis sites of each group */
+    const int32_t *act_nb; /* (n_groups) */
+    const uint64_t *grp_cum; /* (n_groups) cumulative choice thresholds in units of 2^-32 (last = 2^32) */
+} nce_ce_tables;
+
+typedef struct nce_ce_model *nce_ce_handle;
+
+/* Copy the tables to the current device.  Replaces GPUClusterExpansion(table_mode='implicit'). */
+int nce_ce_create(const nce_ce_tables *tables, nce_ce_handle *out);
+int nce_ce_destroy(nce_ce_handle h);
+
+/* Full energy of R configurations sigma (R, N) int8 (device) -> E (R) float64 (device).
+ * precision: 64 = float64 tables and products, 32 = float32 products with float64 accumulation. */
+int nce_ce_energy(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t precision, double *E, void *stream);
+
+/* n independent swap energy differences on device data: for query q, configuration rep[q] of sigma (R,N),
+ * E(after sigma[ia]=sa_new, sigma[ib]=sb_new) - E(before) -> out[q] (float64).  Replaces delta_energy_a. */
+int nce_ce_delta(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t n, const int32_t *rep,
+                 const int64_t *ia, const int64_t *ib, const int8_t *sa_new, const int8_t *sb_new,
+                 int32_t precision, int32_t warps, double *out, void *stream);
+
+/* Parallel-tempering state of one job, all device pointers. */
+typedef struct {
+    int32_t R;             /* replicas = temperature slots */
+    int64_t N;             /* sites per replica */
+    int8_t *sigma;         /* (R, N) species index, canonical site order; replica r's row */
+    double *E;             /* (R) carried energy per replica */
+    const float *beta_slot;/* (R) 1/(kB T) of each temperature slot (float32, as the reference) */
+    int32_t *rep_of_slot;  /* (R) replica holding slot t */
+    int32_t *slot_of_rep;  /* (R) inverse */
+    const int32_t *ladder_id; /* (R) ladder of each slot (exchange only within a ladder) */
+    double *E_min_rep;     /* (R) running minimum of E per replica */
+    int64_t *n_acc;        /* (R) accepted swaps per replica (accumulated) */
+    int64_t *n_ex;         /* (1) accepted exchanges (accumulated) */
+} nce_pt_state;
+
+/* One chunk of steps.  Proposals: host-supplied stream (prop_a/prop_b/prop_u device arrays indexed
+ * [step][slot]) or, when prop_a is NULL, Philox4x32-10 keyed by seed with counter (global step, slot). */
+typedef struct {
+    int64_t n_steps;       /* steps in this chunk */
+    int64_t step0;         /* global index of the chunk's first step */
+    const int32_t *prop_a; /* (n_steps, R) or NULL */
+    const int32_t *prop_b;
+    const double *prop_u;  /* (n_steps, R) uniforms in (0,1] */
+    uint64_t seed;
+    int64_t sample_interval;   /* record E every sample_interval steps (slot order) */
+    double *E_samples;         /* (n_steps/sample_interval, R) device, or NULL */
+    int32_t do_exchange;       /* chunk ends on an exchange step */
+    int32_t ex_parity;         /* used when ex_u != NULL */
+    const double *ex_u;        /* (ceil((R-1)/2)) device uniforms, or NULL -> Philox */
+    int32_t precision;         /* 64 or 32 */
+    int32_t warps;             /* warps per replica (0 = default) */
+} nce_pt_chunk;
+
+int nce_ce_run_chunk(nce_ce_handle h, const nce_pt_state *st, const nce_pt_chunk *ck, void *stream);
+
+/* Independent jobs (different cells, ladders, tables) in one launch; n_jobs <= 64 per call.
+ * Every chunk in the batch must use the same precision and warps. */
+int nce_ce_run_batch(int32_t n_jobs, const nce_ce_handle *h, const nce_pt_state *st, const nce_pt_chunk *ck,
+                     void *stream);
+
+/* e2e form: the same chunk with HOST buffers.  sigma_host (R,N), E_host (R) and the permutations are read
+ * and written back; prop_* are host arrays (or NULL for Philox); E_samples_host (n_steps/si, R) receives
+ * the samples.  Synchronous.  Replaces a host driver's call of run_chunk on host arrays. */
+int nce_ce_run_chunk_host(nce_ce_handle h, int32_t R, int8_t *sigma_host, double *E_host, const float *beta_slot_host,
+                          int32_t *rep_of_slot_host, int32_t *slot_of_rep_host, const int32_t *ladder_id_host,
+                          double *E_min_rep_host, int64_t *n_acc_host, int64_t *n_ex_host,
+                          const nce_pt_chunk *ck_host_pointers, double *E_samples_host);
+
+/* chunk epilogue: global running minimum and the replica index of the lowest current energy.
+ * out (device): out_min[0] = min_r E_min_rep[r], out_arg[0] = argmin_r E[r] (first on ties). */
+int nce_pt_minimum(const nce_pt_state *st, double *out_min, int32_t *out_arg, void *stream);
+
+/* Reads and clears the handle's device error word (synchronous).  Bit 0: a proposal index was outside
+ * [0, N) (that step was rejected instead of read). */
+int nce_ce_errors(nce_ce_handle h, int32_t *flags);
+
+/* Philox4x32-10 on the host (same function the kernels use), for tests and host drivers. */
+void nce_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NCE_GB300_H */

@@ -1,0 +1,108 @@
+"""ctypes binding of libnce_gb300.so (declared in include/nce_gb300.h).
+
+The library is built in-tree by ``neuralce_gb300.build``; ``lib()`` loads it and raises if it is missing, so
+no code path silently falls back to a CPU implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libnce_gb300.so")
+
+i32, i64, u64, f64, f32 = C.c_int32, C.c_int64, C.c_uint64, C.c_double, C.c_float
+P = C.POINTER
+vp = C.c_void_p
+
+
+class NceCeTables(C.Structure):
+    _fields_ = [("nB", i32), ("J", i32), ("mo", i32), ("n_nbr", i32), ("n_pfc", i32), ("max_sp", i32),
+                ("d", i64 * 3), ("n_cells", i64), ("zerolet", f64),
+                ("Rv_len", vp), ("Rv_loc", vp), ("Rv_pfc", vp), ("Rv_eci", vp), ("nb_b", vp), ("nb_uo", vp),
+                ("Rt", i32), ("T_b", vp), ("T_uo", vp), ("T_pfc", vp), ("T_eci", vp), ("pf", vp),
+                ("n_groups", i32), ("max_gb", i32), ("act_b", vp), ("act_nb", vp), ("grp_cum", vp)]
+
+
+class NcePtState(C.Structure):
+    _fields_ = [("R", i32), ("N", i64), ("sigma", vp), ("E", vp), ("beta_slot", vp), ("rep_of_slot", vp),
+                ("slot_of_rep", vp), ("ladder_id", vp), ("E_min_rep", vp), ("n_acc", vp), ("n_ex", vp)]
+
+
+class NcePtChunk(C.Structure):
+    _fields_ = [("n_steps", i64), ("step0", i64), ("prop_a", vp), ("prop_b", vp), ("prop_u", vp), ("seed", u64),
+                ("sample_interval", i64), ("E_samples", vp), ("do_exchange", i32), ("ex_parity", i32),
+                ("ex_u", vp), ("precision", i32), ("warps", i32)]
+
+
+_lock = threading.Lock()
+_lib = None
+
+SIGNATURES = {
+    "nce_version": (i32, []),
+    "nce_last_error": (i32, [C.c_char_p, C.c_size_t]),
+    "nce_ce_create": (i32, [P(NceCeTables), P(vp)]),
+    "nce_ce_destroy": (i32, [vp]),
+    "nce_ce_energy": (i32, [vp, vp, i32, i32, vp, vp]),
+    "nce_ce_delta": (i32, [vp, vp, i32, i32, vp, vp, vp, vp, vp, i32, i32, vp, vp]),
+    "nce_ce_run_chunk": (i32, [vp, P(NcePtState), P(NcePtChunk), vp]),
+    "nce_ce_run_batch": (i32, [i32, P(vp), P(NcePtState), P(NcePtChunk), vp]),
+    "nce_ce_run_chunk_host": (i32, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, P(NcePtChunk), vp]),
+    "nce_ce_errors": (i32, [vp, P(i32)]),
+    "nce_pt_minimum": (i32, [P(NcePtState), vp, vp, vp]),
+    "nce_philox4x32": (None, [P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)]),
+}
+
+
+def lib():
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m neuralce_gb300.build` "
+                                   "(this package has no CPU fallback)")
+            L = C.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+class NceError(RuntimeError):
+    pass
+
+
+def check(rc, what=""):
+    if rc != 0:
+        buf = C.create_string_buffer(2048)
+        lib().nce_last_error(buf, len(buf))
+        raise NceError(f"{what}: status {rc}: {buf.value.decode(errors='replace')}")
+
+
+def ptr(x):
+    """device/host address of a torch tensor or numpy array (None -> NULL)."""
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if hasattr(x, "ctypes"):
+        return x.ctypes.data
+    raise TypeError(type(x))
+
+
+def stream_ptr(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def philox4x32(ctr, key):
+    c = (C.c_uint32 * 4)(*[int(x) & 0xFFFFFFFF for x in ctr])
+    k = (C.c_uint32 * 2)(*[int(x) & 0xFFFFFFFF for x in key])
+    o = (C.c_uint32 * 4)()
+    lib().nce_philox4x32(c, k, o)
+    return [int(x) for x in o]

@@ -1,0 +1,843 @@
+// Cluster-expansion parallel-tempering engine for GB300 (sm_103a).
+//
+// Kernels
+//   ce_pt_chunk_kernel  one CTA per replica (of one or many jobs): for every step of a chunk it draws or
+//                       reads the swap proposal, gathers the occupancy of the two sites' neighbourhoods
+//                       (n_nbr entries each, integer lattice arithmetic on the SNF coordinates), evaluates
+//                       every reverse row of both sites with warp-parallel products of point functions,
+//                       reduces dE with warp shuffles, applies the Metropolis rule and writes the two sites.
+//                       Row tables are staged in shared memory once per chunk.
+//   ce_exchange_kernel  chunk-end replica exchange of temperature slots (one CTA per job).
+//   ce_energy_kernel    full energy: cells x template rows, per-block float64 partials, fixed-order sum.
+//   ce_delta_kernel     batched swap dE queries through the same block routine as the chunk kernel.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace nce {
+
+constexpr int kMaxJobs = 64;
+
+struct CEJob {
+    // tables (device)
+    const uint16_t *loc;   // (nB, J, mo)
+    const uint8_t *pfc;    // (nB, J, mo)
+    const void *eci;       // (nB, J) double or float
+    const int32_t *rv_len; // (nB)
+    const int32_t *nb_b;   // (nB, n_nbr)
+    const int32_t *nb_uo;  // (nB, n_nbr, 3)
+    const void *pf;        // (n_pfc, max_sp) double or float
+    const int32_t *act_b;  // (n_groups, max_gb)
+    const int32_t *act_nb; // (n_groups)
+    const uint64_t *grp_cum;
+    int32_t nB, J, n_nbr, n_pfc, max_sp, n_groups, max_gb;
+    int32_t d0, d1, d2;
+    int64_t n_cells, N;
+    // state
+    int8_t *sigma; double *E; const float *beta_slot; const int32_t *slot_of_rep;
+    double *E_min_rep; int64_t *n_acc;
+    int32_t R;
+    // chunk
+    int64_t n_steps, step0;
+    const int32_t *prop_a, *prop_b; const double *prop_u;
+    uint64_t seed;
+    int64_t sample_interval; double *E_samples;
+    int32_t cta_base;      // first CTA of this job
+    int32_t *err;          // device error word
+};
+
+struct CEBatch {
+    int32_t n_jobs;
+    int32_t tables_in_smem;
+    CEJob job[kMaxJobs];
+};
+
+struct CEShared {          // per-step control block (shared memory)
+    int64_t ia, ib;
+    double u;
+    int32_t valid, near, b_a, b_b;
+    int32_t ka[3], kb[3];
+    int32_t sa, sb;
+};
+
+template <typename Real>
+struct Layout {            // offsets of the dynamic shared-memory regions
+    size_t loc, pfc, eci, vals, hit, red, total;
+    __host__ __device__ static Layout make(int nB, int J, int mo, int n_nbr, int n_pfc, int nwarps, bool tables) {
+        Layout L; size_t o = 0;
+        auto al = [](size_t x, size_t a) { return (x + a - 1) / a * a; };
+        if (tables) {
+            L.loc = o; o = al(o + sizeof(uint16_t) * (size_t)nB * J * mo, 16);
+            L.pfc = o; o = al(o + (size_t)nB * J * mo, 16);
+            L.eci = o; o = al(o + sizeof(Real) * (size_t)nB * J, 16);
+        } else {
+            L.loc = L.pfc = L.eci = 0;
+        }
+        L.vals = o; o = al(o + sizeof(Real) * 4 * (size_t)n_pfc * n_nbr, 16);
+        L.hit = o; o = al(o + (size_t)n_nbr, 16);
+        L.red = o; o = al(o + sizeof(Real) * 32, 16);
+        L.total = o;
+        return L;
+    }
+};
+
+__device__ __forceinline__ int32_t wrap_add(int32_t k, int32_t u, int32_t d) {
+    int32_t q = k + u;
+    return q >= d ? q - d : q;
+}
+
+__device__ __forceinline__ void site_coords(const CEJob &jb, int64_t i, int32_t &b, int32_t k[3]) {
+    b = (int32_t)(i % jb.nB);
+    int64_t c = i / jb.nB;
+    int64_t d12 = (int64_t)jb.d1 * jb.d2;
+    k[0] = (int32_t)(c / d12);
+    k[1] = (int32_t)((c / jb.d2) % jb.d1);
+    k[2] = (int32_t)(c % jb.d2);
+}
+
+template <typename Real>
+__device__ __forceinline__ Real warp_sum(Real v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Gathers both neighbourhoods into shared value tables, then sums the reverse rows of both sites.
+// Must be called by all threads of the block with cs (ia, ib, sa, sb, b_a, b_b, ka, kb, valid) set.
+// Returns dE in thread 0 (other threads: undefined).  Contains three __syncthreads.
+template <typename Real, int MO>
+__device__ Real block_delta(const CEJob &jb, const int8_t *__restrict__ sig, CEShared &cs, unsigned char *smem,
+                            const Layout<Real> &L, const uint16_t *tloc, const uint8_t *tpfc, const Real *teci) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc, max_sp = jb.max_sp;
+    Real *vals = reinterpret_cast<Real *>(smem + L.vals);     // [side][old/new][pfc][n_nbr]
+    uint8_t *hit = smem + L.hit;
+    Real *red = reinterpret_cast<Real *>(smem + L.red);
+    const Real *pf = reinterpret_cast<const Real *>(jb.pf);
+    const int64_t ia = cs.ia, ib = cs.ib;
+    const int sa_new = cs.sb, sb_new = cs.sa;
+    // 1. neighbourhood gather
+    int near_local = 0;
+    for (int t = tid; t < 2 * n_nbr; t += nt) {
+        const int side = t >= n_nbr, n = side ? t - n_nbr : t;
+        const int b0 = side ? cs.b_b : cs.b_a;
+        const int32_t *k = side ? cs.kb : cs.ka;
+        const int e = b0 * n_nbr + n;
+        const int32_t *uo = jb.nb_uo + 3 * e;
+        int32_t q0 = wrap_add(k[0], __ldg(uo + 0), jb.d0);
+        int32_t q1 = wrap_add(k[1], __ldg(uo + 1), jb.d1);
+        int32_t q2 = wrap_add(k[2], __ldg(uo + 2), jb.d2);
+        int64_t s = (((int64_t)q0 * jb.d1 + q1) * jb.d2 + q2) * jb.nB + __ldg(jb.nb_b + e);
+        int so = sig[s];
+        int sn = (s == ia) ? sa_new : ((s == ib) ? sb_new : so);
+        Real *vo = vals + (size_t)(2 * side) * n_pfc * n_nbr;
+        Real *vn = vo + (size_t)n_pfc * n_nbr;
+        for (int c = 0; c < n_pfc; ++c) {
+            vo[c * n_nbr + n] = pf[c * max_sp + so];
+            vn[c * n_nbr + n] = pf[c * max_sp + sn];
+        }
+        if (side) { hit[n] = (s == ia); near_local |= (s == ia); }
+    }
+    const int near = __syncthreads_or(near_local);
+    // 2. rows
+    Real acc = Real(0);
+    const int Ja = __ldg(jb.rv_len + cs.b_a), Jb = __ldg(jb.rv_len + cs.b_b);
+    for (int side = 0; side < 2; ++side) {
+        const int b0 = side ? cs.b_b : cs.b_a;
+        const int Jn = side ? Jb : Ja;
+        const uint16_t *loc = tloc + (size_t)b0 * jb.J * MO;
+        const uint8_t *pfc = tpfc + (size_t)b0 * jb.J * MO;
+        const Real *eci = teci + (size_t)b0 * jb.J;
+        const Real *vo = vals + (size_t)(2 * side) * n_pfc * n_nbr;
+        const Real *vn = vo + (size_t)n_pfc * n_nbr;
+        const bool check = side && near;
+        for (int r = tid; r < Jn; r += nt) {
+            Real po = Real(1), pn = Real(1);
+            bool skip = false;
+#pragma unroll
+            for (int m = 0; m < MO; ++m) {
+                const int l = loc[(size_t)r * MO + m];
+                const int c = pfc[(size_t)r * MO + m];
+                po *= vo[c * n_nbr + l];
+                pn *= vn[c * n_nbr + l];
+                if (check) skip |= hit[l] != 0;
+            }
+            if (!skip) acc += eci[r] * (pn - po);
+        }
+    }
+    acc = warp_sum(acc);
+    if ((tid & 31) == 0) red[tid >> 5] = acc;
+    __syncthreads();
+    Real dE = Real(0);
+    if (tid == 0) {
+        const int nw = (nt + 31) >> 5;
+        for (int w = 0; w < nw; ++w) dE += red[w];
+    }
+    return dE;
+}
+
+// Stage (or point at) the job's row tables.
+template <typename Real>
+__device__ void stage_tables(const CEJob &jb, bool in_smem, unsigned char *smem, const Layout<Real> &L, int MO,
+                             const uint16_t *&tloc, const uint8_t *&tpfc, const Real *&teci) {
+    const size_t nl = (size_t)jb.nB * jb.J * MO, ne = (size_t)jb.nB * jb.J;
+    if (!in_smem) {
+        tloc = jb.loc; tpfc = jb.pfc; teci = reinterpret_cast<const Real *>(jb.eci);
+        return;
+    }
+    uint16_t *sl = reinterpret_cast<uint16_t *>(smem + L.loc);
+    uint8_t *sp = smem + L.pfc;
+    Real *se = reinterpret_cast<Real *>(smem + L.eci);
+    for (size_t i = threadIdx.x; i < nl; i += blockDim.x) { sl[i] = __ldg(jb.loc + i); sp[i] = __ldg(jb.pfc + i); }
+    const Real *ge = reinterpret_cast<const Real *>(jb.eci);
+    for (size_t i = threadIdx.x; i < ne; i += blockDim.x) se[i] = ge[i];
+    tloc = sl; tpfc = sp; teci = se;
+    __syncthreads();
+}
+
+__device__ __forceinline__ int find_job(const CEBatch &bt, int cta) {
+    int j = 0;
+    while (j + 1 < bt.n_jobs && cta >= bt.job[j + 1].cta_base) ++j;
+    return j;
+}
+
+// proposal of slot t at global step g (same layout as the C oracle)
+__device__ __forceinline__ void propose(const CEJob &jb, int64_t g, int32_t t, int64_t &ia, int64_t &ib, double &u) {
+    const uint32_t k0 = (uint32_t)jb.seed, k1 = (uint32_t)(jb.seed >> 32);
+    const uint32_t c0 = (uint32_t)g, c1 = (uint32_t)((uint64_t)g >> 32);
+    u32x4 x = philox4x32(c0, c1, (uint32_t)t, 0u, k0, k1);
+    int grp = 0; uint32_t ba = 0, bb = 0;
+    if (jb.n_groups > 1 || __ldg(jb.act_nb) > 1) {
+        u32x4 y = philox4x32(c0, c1, (uint32_t)t, 1u, k0, k1);
+        if (jb.n_groups > 1)
+            while (grp < jb.n_groups - 1 && (uint64_t)y.x >= __ldg(jb.grp_cum + grp)) ++grp;
+        const uint32_t nb = (uint32_t)__ldg(jb.act_nb + grp);
+        ba = draw_index(y.y, nb); bb = draw_index(y.z, nb);
+    }
+    const uint32_t nc = (uint32_t)jb.n_cells;
+    ia = (int64_t)draw_index(x.x, nc) * jb.nB + __ldg(jb.act_b + grp * jb.max_gb + ba);
+    ib = (int64_t)draw_index(x.y, nc) * jb.nB + __ldg(jb.act_b + grp * jb.max_gb + bb);
+    u = draw_u01(x.z, x.w);
+}
+
+template <typename Real, int MO>
+__global__ void __launch_bounds__(1024) ce_pt_chunk_kernel(const __grid_constant__ CEBatch bt) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ CEShared cs;
+    const int j = find_job(bt, blockIdx.x);
+    const CEJob &jb = bt.job[j];
+    const int r = blockIdx.x - jb.cta_base;
+    if (r >= jb.R) return;
+    const Layout<Real> L = Layout<Real>::make(jb.nB, jb.J, MO, jb.n_nbr, jb.n_pfc, blockDim.x >> 5, bt.tables_in_smem);
+    const uint16_t *tloc; const uint8_t *tpfc; const Real *teci;
+    stage_tables<Real>(jb, bt.tables_in_smem, smem, L, MO, tloc, tpfc, teci);
+    int8_t *sig = jb.sigma + (int64_t)r * jb.N;
+    const int32_t t = jb.slot_of_rep[r];
+    const double beta = (double)jb.beta_slot[t];
+    double E = jb.E[r], Emin = jb.E_min_rep[r];
+    int64_t nacc = 0;
+    const int R = jb.R;
+    for (int64_t s = 0; s < jb.n_steps; ++s) {
+        if (threadIdx.x == 0) {
+            int64_t ia, ib; double u;
+            if (jb.prop_a) {
+                ia = jb.prop_a[s * R + t]; ib = jb.prop_b[s * R + t]; u = jb.prop_u[s * R + t];
+            } else {
+                propose(jb, jb.step0 + s, t, ia, ib, u);
+            }
+            int valid = 0;
+            if (ia < 0 || ib < 0 || ia >= jb.N || ib >= jb.N) {
+                atomicOr(jb.err, 1);                 // out-of-range proposal: rejected, flagged
+            } else {
+                cs.sa = sig[ia]; cs.sb = sig[ib];
+                valid = cs.sa != cs.sb;
+            }
+            cs.ia = ia; cs.ib = ib; cs.u = u; cs.valid = valid;
+            if (valid) { site_coords(jb, ia, cs.b_a, cs.ka); site_coords(jb, ib, cs.b_b, cs.kb); }
+        }
+        __syncthreads();
+        if (cs.valid) {
+            Real dE = block_delta<Real, MO>(jb, sig, cs, smem, L, tloc, tpfc, teci);
+            if (threadIdx.x == 0) {
+                const double dEd = (double)dE;
+                if (log(cs.u) < -beta * dEd) {
+                    sig[cs.ia] = (int8_t)cs.sb; sig[cs.ib] = (int8_t)cs.sa;
+                    E += dEd; ++nacc;
+                }
+            }
+        }
+        if (threadIdx.x == 0) {
+            Emin = fmin(Emin, E);
+            if (jb.E_samples && (s + 1) % jb.sample_interval == 0)
+                jb.E_samples[((s + 1) / jb.sample_interval - 1) * R + t] = E;
+        }
+    }
+    if (threadIdx.x == 0) { jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc; }
+}
+
+// chunk-end exchange of temperature slots, one CTA (thread 0) per job
+struct CEExJob {
+    int32_t R; double *E; const float *beta_slot; int32_t *rep_of_slot, *slot_of_rep; const int32_t *ladder_id;
+    int64_t *n_ex; uint64_t seed; int64_t g_end; int32_t parity; const double *ex_u;
+    double *E_samples; int64_t last_row; int32_t do_exchange;
+};
+struct CEExBatch { int32_t n_jobs; CEExJob job[kMaxJobs]; };
+
+__global__ void ce_exchange_kernel(const __grid_constant__ CEExBatch bt) {
+    extern __shared__ int32_t xsm[];
+    const int j = blockIdx.x;
+    if (j >= bt.n_jobs || threadIdx.x != 0) return;
+    const CEExJob &x = bt.job[j];
+    if (!x.do_exchange || x.R < 2) return;
+    int32_t *perm = xsm;
+    int32_t *ros = perm + x.R;
+    const int R = x.R;
+    const uint32_t k0 = (uint32_t)x.seed, k1 = (uint32_t)(x.seed >> 32);
+    const uint32_t c0 = (uint32_t)x.g_end, c1 = (uint32_t)((uint64_t)x.g_end >> 32);
+    int parity = x.ex_u ? x.parity : (int)(philox4x32(c0, c1, 0xFFFFFFFFu, 0u, k0, k1).x & 1u);
+    for (int i = 0; i < R; ++i) perm[i] = i;
+    int64_t nswap = 0;
+    for (int k = 0; 2 * k < R - 1; ++k) {
+        const int a = 2 * k + parity, b = a + 1;
+        if (b >= R) continue;
+        if (x.ladder_id[a] != x.ladder_id[b]) continue;
+        const double Ea = x.E[x.rep_of_slot[a]], Eb = x.E[x.rep_of_slot[b]];
+        const double log_acc = ((double)x.beta_slot[b] - (double)x.beta_slot[a]) * (Eb - Ea);
+        double u;
+        if (x.ex_u) u = x.ex_u[k];
+        else { u32x4 w = philox4x32(c0, c1, 0xFFFFFFFEu, (uint32_t)k, k0, k1); u = draw_u01(w.x, w.y); }
+        if (log(u) < log_acc) { perm[a] = b; perm[b] = a; ++nswap; }
+    }
+    for (int t = 0; t < R; ++t) ros[t] = x.rep_of_slot[perm[t]];
+    for (int t = 0; t < R; ++t) { x.rep_of_slot[t] = ros[t]; x.slot_of_rep[ros[t]] = t; }
+    *x.n_ex += nswap;
+    if (x.E_samples && x.last_row >= 0)
+        for (int t = 0; t < R; ++t) x.E_samples[x.last_row * R + t] = x.E[x.rep_of_slot[t]];
+}
+
+// full energy: grid (blocks_per_rep, R); per-block float64 partial -> partial[r * nblk + bx]
+template <typename Real>
+__global__ void __launch_bounds__(256) ce_energy_kernel(const int8_t *__restrict__ sigma, int64_t N, int64_t n_cells,
+                                                        int32_t nB, int32_t d0, int32_t d1, int32_t d2, int32_t Rt, int32_t mo,
+                                                        const int32_t *__restrict__ T_b, const int32_t *__restrict__ T_uo,
+                                                        const uint8_t *__restrict__ T_pfc, const Real *__restrict__ T_eci,
+                                                        const Real *__restrict__ pf, int32_t max_sp, double *partial) {
+    __shared__ double red[32];
+    const int r = blockIdx.y;
+    const int8_t *sig = sigma + (int64_t)r * N;
+    double acc = 0.0;
+    const int64_t d12 = (int64_t)d1 * d2;
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n_cells; c += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t k0 = (int32_t)(c / d12), k1 = (int32_t)((c / d2) % d1), k2 = (int32_t)(c % d2);
+        Real cell_sum = Real(0);
+        for (int row = 0; row < Rt; ++row) {
+            Real pr = Real(1);
+            for (int m = 0; m < mo; ++m) {
+                const int e = row * mo + m;
+                const int32_t q0 = wrap_add(k0, __ldg(T_uo + 3 * e), d0);
+                const int32_t q1 = wrap_add(k1, __ldg(T_uo + 3 * e + 1), d1);
+                const int32_t q2 = wrap_add(k2, __ldg(T_uo + 3 * e + 2), d2);
+                const int64_t s = (((int64_t)q0 * d1 + q1) * d2 + q2) * nB + __ldg(T_b + e);
+                pr *= pf[(int)__ldg(T_pfc + e) * max_sp + sig[s]];
+            }
+            cell_sum += __ldg(T_eci + row) * pr;
+        }
+        acc += (double)cell_sum;
+    }
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+        partial[(int64_t)r * gridDim.x + blockIdx.x] = s;
+    }
+}
+
+__global__ void ce_energy_finish(const double *partial, int32_t nblk, int32_t R, double zerolet, double *E) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    double s = 0.0;
+    for (int b = 0; b < nblk; ++b) s += partial[(int64_t)r * nblk + b];
+    E[r] = zerolet + s;
+}
+
+// batched dE queries: one CTA per query
+template <typename Real, int MO>
+__global__ void __launch_bounds__(1024) ce_delta_kernel(const __grid_constant__ CEJob jb, int32_t n, const int32_t *rep,
+                                                        const int64_t *qa, const int64_t *qb, const int8_t *qsa,
+                                                        const int8_t *qsb, double *out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ CEShared cs;
+    const int q = blockIdx.x;
+    if (q >= n) return;
+    // uniform per block: every thread reads the same query, so an invalid one returns the whole block
+    if (rep[q] < 0 || rep[q] >= jb.R || qa[q] < 0 || qa[q] >= jb.N || qb[q] < 0 || qb[q] >= jb.N ||
+        qsa[q] < 0 || qsa[q] >= jb.max_sp || qsb[q] < 0 || qsb[q] >= jb.max_sp) {
+        if (threadIdx.x == 0) { out[q] = __longlong_as_double(0x7ff8000000000000ll); atomicOr(jb.err, 2); }
+        return;
+    }
+    const Layout<Real> L = Layout<Real>::make(jb.nB, jb.J, MO, jb.n_nbr, jb.n_pfc, blockDim.x >> 5, false);
+    const int8_t *sig = jb.sigma + (int64_t)rep[q] * jb.N;
+    if (threadIdx.x == 0) {
+        cs.ia = qa[q]; cs.ib = qb[q];
+        // the swap writes sa_new at ia and sb_new at ib: block_delta takes the new species as (cs.sb, cs.sa)
+        cs.sb = qsa[q]; cs.sa = qsb[q];
+        site_coords(jb, cs.ia, cs.b_a, cs.ka); site_coords(jb, cs.ib, cs.b_b, cs.kb);
+    }
+    __syncthreads();
+    Real dE = block_delta<Real, MO>(jb, sig, cs, smem, L, jb.loc, jb.pfc, reinterpret_cast<const Real *>(jb.eci));
+    if (threadIdx.x == 0) out[q] = (double)dE;
+}
+
+// chunk-end minimum: out_min = min_r E_min_rep, out_arg = argmin_r E (first)
+__global__ void pt_minimum_kernel(const double *E, const double *Emin, int32_t R, double *out_min, int32_t *out_arg) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double m = Emin[0]; int a = 0; double be = E[0];
+    for (int r = 1; r < R; ++r) {
+        m = fmin(m, Emin[r]);
+        if (E[r] < be) { be = E[r]; a = r; }
+    }
+    *out_min = m; *out_arg = a;
+}
+
+}  // namespace nce
+
+// ───────────────────────────── host side ──────────────────────────────────────────────────────
+
+struct nce_ce_model {
+    int32_t nB, J, mo, n_nbr, n_pfc, max_sp, n_groups, max_gb, Rt;
+    int64_t d[3], n_cells, N;
+    double zerolet;
+    uint16_t *loc = nullptr; uint8_t *pfc = nullptr; double *eci64 = nullptr; float *eci32 = nullptr;
+    int32_t *rv_len = nullptr, *nb_b = nullptr, *nb_uo = nullptr;
+    double *pf64 = nullptr; float *pf32 = nullptr;
+    int32_t *act_b = nullptr, *act_nb = nullptr; uint64_t *grp_cum = nullptr;
+    int32_t *T_b = nullptr, *T_uo = nullptr; uint8_t *T_pfc = nullptr; double *T_eci64 = nullptr; float *T_eci32 = nullptr;
+    int32_t *err = nullptr;                  // device error word
+    double *energy_partial = nullptr; size_t energy_partial_n = 0;
+    int device = 0;
+    std::mutex mu;
+    // staging for the host-buffer entry point
+    std::vector<void *> staging; size_t staging_bytes = 0; void *staging_base = nullptr;
+};
+
+namespace nce {
+
+template <typename T>
+static int upload(T *&dst, const T *src, size_t n) {
+    if (n == 0) { dst = nullptr; return NCE_OK; }
+    NCE_CUDA(cudaMalloc((void **)&dst, sizeof(T) * n));
+    NCE_CUDA(cudaMemcpy(dst, src, sizeof(T) * n, cudaMemcpyHostToDevice));
+    return NCE_OK;
+}
+
+static int free_model(nce_ce_model *m) {
+    void *ptrs[] = {m->loc, m->pfc, m->eci64, m->eci32, m->rv_len, m->nb_b, m->nb_uo, m->pf64, m->pf32, m->act_b,
+                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err,
+                    m->energy_partial, m->staging_base};
+    for (void *p : ptrs) if (p) cudaFree(p);
+    delete m;
+    return NCE_OK;
+}
+
+template <typename Real>
+static bool tables_fit(const nce_ce_model *m, int warps, size_t *bytes_out) {
+    const Layout<Real> L1 = Layout<Real>::make(m->nB, m->J, m->mo, m->n_nbr, m->n_pfc, warps, true);
+    const Layout<Real> L0 = Layout<Real>::make(m->nB, m->J, m->mo, m->n_nbr, m->n_pfc, warps, false);
+    const size_t limit = 200 * 1024;
+    if (L1.total <= limit) { *bytes_out = L1.total; return true; }
+    *bytes_out = L0.total;
+    return false;
+}
+
+static CEJob make_job(const nce_ce_model *m, const nce_pt_state *st, const nce_pt_chunk *ck, int cta_base) {
+    CEJob j;
+    std::memset(&j, 0, sizeof(j));
+    const bool p64 = ck ? ck->precision != 32 : true;
+    j.loc = m->loc; j.pfc = m->pfc; j.eci = p64 ? (const void *)m->eci64 : (const void *)m->eci32;
+    j.rv_len = m->rv_len; j.nb_b = m->nb_b; j.nb_uo = m->nb_uo; j.pf = p64 ? (const void *)m->pf64 : (const void *)m->pf32;
+    j.act_b = m->act_b; j.act_nb = m->act_nb; j.grp_cum = m->grp_cum;
+    j.nB = m->nB; j.J = m->J; j.n_nbr = m->n_nbr; j.n_pfc = m->n_pfc; j.max_sp = m->max_sp;
+    j.n_groups = m->n_groups; j.max_gb = m->max_gb;
+    j.d0 = (int32_t)m->d[0]; j.d1 = (int32_t)m->d[1]; j.d2 = (int32_t)m->d[2];
+    j.n_cells = m->n_cells; j.N = m->N; j.err = m->err;
+    if (st) {
+        j.sigma = st->sigma; j.E = st->E; j.beta_slot = st->beta_slot; j.slot_of_rep = st->slot_of_rep;
+        j.E_min_rep = st->E_min_rep; j.n_acc = st->n_acc; j.R = st->R;
+    }
+    if (ck) {
+        j.n_steps = ck->n_steps; j.step0 = ck->step0; j.prop_a = ck->prop_a; j.prop_b = ck->prop_b; j.prop_u = ck->prop_u;
+        j.seed = ck->seed; j.sample_interval = ck->sample_interval > 0 ? ck->sample_interval : 1;
+        j.E_samples = ck->E_samples;
+    }
+    j.cta_base = cta_base;
+    return j;
+}
+
+template <typename Real, int MO>
+static int launch_chunk_mo(const CEBatch &bt, int total, int warps, size_t smem, cudaStream_t s) {
+    auto kern = ce_pt_chunk_kernel<Real, MO>;
+    NCE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<total, warps * 32, smem, s>>>(bt);
+    NCE_CUDA(cudaGetLastError());
+    return NCE_OK;
+}
+
+template <typename Real>
+static int launch_chunk(const CEBatch &bt, int mo, int total, int warps, size_t smem, cudaStream_t s) {
+    switch (mo) {
+        case 1: return launch_chunk_mo<Real, 1>(bt, total, warps, smem, s);
+        case 2: return launch_chunk_mo<Real, 2>(bt, total, warps, smem, s);
+        case 3: return launch_chunk_mo<Real, 3>(bt, total, warps, smem, s);
+        case 4: return launch_chunk_mo<Real, 4>(bt, total, warps, smem, s);
+        case 5: return launch_chunk_mo<Real, 5>(bt, total, warps, smem, s);
+        case 6: return launch_chunk_mo<Real, 6>(bt, total, warps, smem, s);
+        case 7: return launch_chunk_mo<Real, 7>(bt, total, warps, smem, s);
+        case 8: return launch_chunk_mo<Real, 8>(bt, total, warps, smem, s);
+        default: return fail(NCE_ERR_UNSUPPORTED, "cluster order %d > 8", mo);
+    }
+}
+
+static int check_state(const nce_ce_model *m, const nce_pt_state *st) {
+    NCE_CHECK(st && st->R >= 1, "state: R must be >= 1");
+    NCE_CHECK(st->N == m->N, "state: N=%lld but the tables are for %lld sites", (long long)st->N, (long long)m->N);
+    NCE_CHECK(st->sigma && st->E && st->beta_slot && st->rep_of_slot && st->slot_of_rep && st->ladder_id &&
+              st->E_min_rep && st->n_acc && st->n_ex, "state: null device pointer");
+    return NCE_OK;
+}
+
+static int check_chunk(const nce_pt_state *st, const nce_pt_chunk *ck) {
+    NCE_CHECK(ck, "chunk: null");
+    NCE_CHECK(ck->n_steps >= 0, "chunk: n_steps < 0");
+    NCE_CHECK(ck->precision == 64 || ck->precision == 32, "chunk: precision must be 64 or 32");
+    NCE_CHECK((ck->prop_a == nullptr) == (ck->prop_b == nullptr) && (ck->prop_a == nullptr) == (ck->prop_u == nullptr),
+              "chunk: prop_a/prop_b/prop_u must be all set or all NULL");
+    NCE_CHECK(!ck->E_samples || ck->sample_interval > 0, "chunk: sample_interval must be > 0 with E_samples");
+    NCE_CHECK(ck->warps >= 0 && ck->warps <= 32, "chunk: warps must be 0..32");
+    NCE_CHECK(!ck->do_exchange || !ck->ex_u || (ck->ex_parity == 0 || ck->ex_parity == 1), "chunk: ex_parity must be 0/1");
+    (void)st;
+    return NCE_OK;
+}
+
+static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *sts, const nce_pt_chunk *cks, cudaStream_t s) {
+    NCE_CHECK(n_jobs >= 1 && n_jobs <= kMaxJobs, "batch: n_jobs must be 1..%d", kMaxJobs);
+    const int precision = cks[0].precision;
+    const int warps = cks[0].warps > 0 ? cks[0].warps : 8;
+    int mo = 0, total = 0, max_R = 0;
+    for (int j = 0; j < n_jobs; ++j) {
+        NCE_CHECK(hs[j], "batch: null handle");
+        int rc = check_state(hs[j], &sts[j]); if (rc) return rc;
+        rc = check_chunk(&sts[j], &cks[j]); if (rc) return rc;
+        NCE_CHECK(cks[j].precision == precision, "batch: all chunks must use the same precision");
+        NCE_CHECK((cks[j].warps > 0 ? cks[j].warps : 8) == warps, "batch: all chunks must use the same warps");
+        mo = std::max(mo, hs[j]->mo);
+        total += sts[j].R; max_R = std::max(max_R, sts[j].R);
+    }
+    for (int j = 0; j < n_jobs; ++j)
+        NCE_CHECK(hs[j]->mo == mo, "batch: all jobs must have the same maximum cluster order");
+    CEBatch bt; std::memset(&bt, 0, sizeof(bt));
+    bt.n_jobs = n_jobs;
+    size_t smem = 0; bool all_fit = true;
+    for (int j = 0; j < n_jobs; ++j) {
+        size_t b; bool fit = precision == 64 ? tables_fit<double>(hs[j], warps, &b) : tables_fit<float>(hs[j], warps, &b);
+        all_fit = all_fit && fit;
+    }
+    for (int j = 0; j < n_jobs; ++j) {
+        size_t b;
+        if (precision == 64) {
+            b = Layout<double>::make(hs[j]->nB, hs[j]->J, mo, hs[j]->n_nbr, hs[j]->n_pfc, warps, all_fit).total;
+        } else {
+            b = Layout<float>::make(hs[j]->nB, hs[j]->J, mo, hs[j]->n_nbr, hs[j]->n_pfc, warps, all_fit).total;
+        }
+        smem = std::max(smem, b);
+    }
+    bt.tables_in_smem = all_fit ? 1 : 0;
+    int base = 0;
+    for (int j = 0; j < n_jobs; ++j) {
+        bt.job[j] = make_job(hs[j], &sts[j], &cks[j], base);
+        base += sts[j].R;
+    }
+    int64_t max_steps = 0;
+    for (int j = 0; j < n_jobs; ++j) max_steps = std::max(max_steps, cks[j].n_steps);
+    if (max_steps > 0) {
+        int rc = precision == 64 ? launch_chunk<double>(bt, mo, total, warps, smem, s)
+                                 : launch_chunk<float>(bt, mo, total, warps, smem, s);
+        if (rc) return rc;
+    }
+    // exchange
+    CEExBatch ex; std::memset(&ex, 0, sizeof(ex));
+    ex.n_jobs = n_jobs;
+    bool any = false;
+    for (int j = 0; j < n_jobs; ++j) {
+        const nce_pt_state &st = sts[j]; const nce_pt_chunk &ck = cks[j];
+        CEExJob &x = ex.job[j];
+        x.R = st.R; x.E = st.E; x.beta_slot = st.beta_slot; x.rep_of_slot = st.rep_of_slot; x.slot_of_rep = st.slot_of_rep;
+        x.ladder_id = st.ladder_id; x.n_ex = st.n_ex; x.seed = ck.seed; x.g_end = ck.step0 + ck.n_steps;
+        x.parity = ck.ex_parity; x.ex_u = ck.ex_u; x.E_samples = ck.E_samples;
+        x.last_row = (ck.E_samples && ck.n_steps > 0 && ck.n_steps % ck.sample_interval == 0) ? ck.n_steps / ck.sample_interval - 1 : -1;
+        x.do_exchange = ck.do_exchange && st.R > 1;
+        any = any || x.do_exchange;
+    }
+    if (any) {
+        const size_t xs = sizeof(int32_t) * 2 * (size_t)max_R;
+        NCE_CHECK(xs <= 200 * 1024, "batch: %d replicas per job exceed the exchange kernel's shared memory", max_R);
+        NCE_CUDA(cudaFuncSetAttribute(ce_exchange_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
+        ce_exchange_kernel<<<n_jobs, 32, xs, s>>>(ex);
+        NCE_CUDA(cudaGetLastError());
+    }
+    return NCE_OK;
+}
+
+template <typename Real, int MO>
+static int launch_delta_mo(const CEJob &jb, int n, const int32_t *rep, const int64_t *ia, const int64_t *ib,
+                           const int8_t *sa, const int8_t *sb, double *out, int warps, cudaStream_t s) {
+    const size_t smem = Layout<Real>::make(jb.nB, jb.J, MO, jb.n_nbr, jb.n_pfc, warps, false).total;
+    auto kern = ce_delta_kernel<Real, MO>;
+    NCE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<n, warps * 32, smem, s>>>(jb, n, rep, ia, ib, sa, sb, out);
+    NCE_CUDA(cudaGetLastError());
+    return NCE_OK;
+}
+
+template <typename Real>
+static int launch_delta(const CEJob &jb, int mo, int n, const int32_t *rep, const int64_t *ia, const int64_t *ib,
+                        const int8_t *sa, const int8_t *sb, double *out, int warps, cudaStream_t s) {
+    switch (mo) {
+#define NCE_MO_CASE(M) case M: return launch_delta_mo<Real, M>(jb, n, rep, ia, ib, sa, sb, out, warps, s);
+        NCE_MO_CASE(1) NCE_MO_CASE(2) NCE_MO_CASE(3) NCE_MO_CASE(4) NCE_MO_CASE(5) NCE_MO_CASE(6) NCE_MO_CASE(7) NCE_MO_CASE(8)
+#undef NCE_MO_CASE
+        default: return fail(NCE_ERR_UNSUPPORTED, "cluster order %d > 8", mo);
+    }
+}
+
+}  // namespace nce
+
+using namespace nce;
+
+extern "C" {
+
+int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
+    NCE_CHECK(t && out, "nce_ce_create: null argument");
+    NCE_CHECK(t->nB >= 1 && t->J >= 1 && t->mo >= 1 && t->mo <= 8, "nce_ce_create: nB/J/mo out of range (mo 1..8)");
+    NCE_CHECK(t->n_nbr >= 1 && t->n_nbr <= 65535, "nce_ce_create: n_nbr out of range");
+    NCE_CHECK(t->n_pfc >= 1 && t->n_pfc <= 255 && t->max_sp >= 1 && t->max_sp <= 127, "nce_ce_create: n_pfc/max_sp out of range");
+    NCE_CHECK(t->d[0] >= 1 && t->d[1] >= 1 && t->d[2] >= 1 && t->d[0] < (1 << 30) && t->d[1] < (1 << 30) && t->d[2] < (1 << 30),
+              "nce_ce_create: bad SNF diagonal");
+    NCE_CHECK(t->n_cells == t->d[0] * t->d[1] * t->d[2], "nce_ce_create: n_cells != d0*d1*d2");
+    NCE_CHECK(t->n_cells <= 0xFFFFFFFFll, "nce_ce_create: more than 2^32 cells");
+    NCE_CHECK(t->n_groups >= 1 && t->max_gb >= 1, "nce_ce_create: no active sublattice");
+    NCE_CHECK(t->Rv_len && t->Rv_loc && t->Rv_pfc && t->Rv_eci && t->nb_b && t->nb_uo && t->pf && t->act_b && t->act_nb &&
+              t->grp_cum && t->T_b && t->T_uo && t->T_pfc && t->T_eci, "nce_ce_create: null table pointer");
+    const size_t nl = (size_t)t->nB * t->J * t->mo;
+    for (size_t i = 0; i < nl; ++i) {
+        NCE_CHECK(t->Rv_loc[i] < t->n_nbr, "nce_ce_create: Rv_loc[%zu]=%d >= n_nbr", i, (int)t->Rv_loc[i]);
+        NCE_CHECK(t->Rv_pfc[i] < t->n_pfc, "nce_ce_create: Rv_pfc[%zu] >= n_pfc", i);
+    }
+    for (int b = 0; b < t->nB; ++b) NCE_CHECK(t->Rv_len[b] >= 0 && t->Rv_len[b] <= t->J, "nce_ce_create: Rv_len out of range");
+    for (size_t i = 0; i < (size_t)t->nB * t->n_nbr; ++i) {
+        NCE_CHECK(t->nb_b[i] >= 0 && t->nb_b[i] < t->nB, "nce_ce_create: nb_b out of range");
+        for (int c = 0; c < 3; ++c)
+            NCE_CHECK(t->nb_uo[3 * i + c] >= 0 && t->nb_uo[3 * i + c] < t->d[c], "nce_ce_create: nb_uo out of [0,d)");
+    }
+    for (size_t i = 0; i < (size_t)t->Rt * t->mo; ++i) {
+        NCE_CHECK(t->T_b[i] >= 0 && t->T_b[i] < t->nB && t->T_pfc[i] < t->n_pfc, "nce_ce_create: template row out of range");
+        for (int c = 0; c < 3; ++c) NCE_CHECK(t->T_uo[3 * i + c] >= 0 && t->T_uo[3 * i + c] < t->d[c], "nce_ce_create: T_uo out of [0,d)");
+    }
+    for (int g = 0; g < t->n_groups; ++g) {
+        NCE_CHECK(t->act_nb[g] >= 1 && t->act_nb[g] <= t->max_gb, "nce_ce_create: act_nb out of range");
+        for (int q = 0; q < t->act_nb[g]; ++q)
+            NCE_CHECK(t->act_b[g * t->max_gb + q] >= 0 && t->act_b[g * t->max_gb + q] < t->nB, "nce_ce_create: act_b out of range");
+    }
+    nce_ce_model *m = new nce_ce_model();
+    m->nB = t->nB; m->J = t->J; m->mo = t->mo; m->n_nbr = t->n_nbr; m->n_pfc = t->n_pfc; m->max_sp = t->max_sp;
+    m->n_groups = t->n_groups; m->max_gb = t->max_gb; m->Rt = t->Rt;
+    for (int c = 0; c < 3; ++c) m->d[c] = t->d[c];
+    m->n_cells = t->n_cells; m->N = t->n_cells * t->nB; m->zerolet = t->zerolet;
+    cudaGetDevice(&m->device);
+    std::vector<float> e32((size_t)t->nB * t->J), p32((size_t)t->n_pfc * t->max_sp), te32(t->Rt);
+    for (size_t i = 0; i < e32.size(); ++i) e32[i] = (float)t->Rv_eci[i];
+    for (size_t i = 0; i < p32.size(); ++i) p32[i] = (float)t->pf[i];
+    for (int i = 0; i < t->Rt; ++i) te32[i] = (float)t->T_eci[i];
+    int rc = NCE_OK;
+    if (!rc) rc = upload(m->loc, t->Rv_loc, nl);
+    if (!rc) rc = upload(m->pfc, t->Rv_pfc, nl);
+    if (!rc) rc = upload(m->eci64, t->Rv_eci, e32.size());
+    if (!rc) rc = upload(m->eci32, e32.data(), e32.size());
+    if (!rc) rc = upload(m->rv_len, t->Rv_len, (size_t)t->nB);
+    if (!rc) rc = upload(m->nb_b, t->nb_b, (size_t)t->nB * t->n_nbr);
+    if (!rc) rc = upload(m->nb_uo, t->nb_uo, (size_t)t->nB * t->n_nbr * 3);
+    if (!rc) rc = upload(m->pf64, t->pf, p32.size());
+    if (!rc) rc = upload(m->pf32, p32.data(), p32.size());
+    if (!rc) rc = upload(m->act_b, t->act_b, (size_t)t->n_groups * t->max_gb);
+    if (!rc) rc = upload(m->act_nb, t->act_nb, (size_t)t->n_groups);
+    if (!rc) rc = upload(m->grp_cum, t->grp_cum, (size_t)t->n_groups);
+    if (!rc) rc = upload(m->T_b, t->T_b, (size_t)t->Rt * t->mo);
+    if (!rc) rc = upload(m->T_uo, t->T_uo, (size_t)t->Rt * t->mo * 3);
+    if (!rc) rc = upload(m->T_pfc, t->T_pfc, (size_t)t->Rt * t->mo);
+    if (!rc) rc = upload(m->T_eci64, t->T_eci, (size_t)t->Rt);
+    if (!rc) rc = upload(m->T_eci32, te32.data(), (size_t)t->Rt);
+    if (!rc) {
+        cudaError_t e = cudaMalloc((void **)&m->err, sizeof(int32_t));
+        if (e == cudaSuccess) e = cudaMemset(m->err, 0, sizeof(int32_t));
+        if (e != cudaSuccess) rc = fail(NCE_ERR_CUDA, "nce_ce_create: %s", cudaGetErrorString(e));
+    }
+    if (rc) { free_model(m); return rc; }
+    *out = m;
+    return NCE_OK;
+}
+
+int nce_ce_destroy(nce_ce_handle h) {
+    if (!h) return NCE_OK;
+    cudaDeviceSynchronize();
+    return free_model(h);
+}
+
+int nce_ce_energy(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t precision, double *E, void *stream) {
+    NCE_CHECK(h && sigma && E && R >= 1, "nce_ce_energy: bad argument");
+    NCE_CHECK(precision == 64 || precision == 32, "nce_ce_energy: precision must be 64 or 32");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaStream_t s = (cudaStream_t)stream;
+    const int threads = 256;
+    int nblk = (int)std::min<int64_t>((h->n_cells + threads - 1) / threads, 1184);
+    nblk = std::max(nblk, 1);
+    const size_t need = (size_t)nblk * R;
+    if (need > h->energy_partial_n) {
+        if (h->energy_partial) { cudaStreamSynchronize(s); cudaFree(h->energy_partial); }
+        h->energy_partial = nullptr; h->energy_partial_n = 0;
+        NCE_CUDA(cudaMalloc((void **)&h->energy_partial, sizeof(double) * need));
+        h->energy_partial_n = need;
+    }
+    dim3 grid(nblk, R);
+    if (precision == 64)
+        ce_energy_kernel<double><<<grid, threads, 0, s>>>(sigma, h->N, h->n_cells, h->nB, (int)h->d[0], (int)h->d[1], (int)h->d[2],
+                                                          h->Rt, h->mo, h->T_b, h->T_uo, h->T_pfc, h->T_eci64, h->pf64, h->max_sp,
+                                                          h->energy_partial);
+    else
+        ce_energy_kernel<float><<<grid, threads, 0, s>>>(sigma, h->N, h->n_cells, h->nB, (int)h->d[0], (int)h->d[1], (int)h->d[2],
+                                                         h->Rt, h->mo, h->T_b, h->T_uo, h->T_pfc, h->T_eci32, h->pf32, h->max_sp,
+                                                         h->energy_partial);
+    NCE_CUDA(cudaGetLastError());
+    ce_energy_finish<<<(R + 127) / 128, 128, 0, s>>>(h->energy_partial, nblk, R, h->zerolet, E);
+    NCE_CUDA(cudaGetLastError());
+    return NCE_OK;
+}
+
+int nce_ce_delta(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t n, const int32_t *rep, const int64_t *ia,
+                 const int64_t *ib, const int8_t *sa_new, const int8_t *sb_new, int32_t precision, int32_t warps,
+                 double *out, void *stream) {
+    NCE_CHECK(h && sigma && R >= 1 && n >= 0, "nce_ce_delta: bad argument");
+    if (n == 0) return NCE_OK;
+    NCE_CHECK(rep && ia && ib && sa_new && sb_new && out, "nce_ce_delta: null pointer");
+    NCE_CHECK(precision == 64 || precision == 32, "nce_ce_delta: precision must be 64 or 32");
+    if (warps <= 0) warps = 8;
+    NCE_CHECK(warps <= 32, "nce_ce_delta: warps must be <= 32");
+    nce_pt_state st; std::memset(&st, 0, sizeof(st));
+    st.R = R; st.N = h->N; st.sigma = const_cast<int8_t *>(sigma);
+    nce_pt_chunk ck; std::memset(&ck, 0, sizeof(ck)); ck.precision = precision;
+    CEJob jb = make_job(h, &st, &ck, 0);
+    cudaStream_t s = (cudaStream_t)stream;
+    return precision == 64 ? launch_delta<double>(jb, h->mo, n, rep, ia, ib, sa_new, sb_new, out, warps, s)
+                           : launch_delta<float>(jb, h->mo, n, rep, ia, ib, sa_new, sb_new, out, warps, s);
+}
+
+int nce_ce_run_chunk(nce_ce_handle h, const nce_pt_state *st, const nce_pt_chunk *ck, void *stream) {
+    NCE_CHECK(h && st && ck, "nce_ce_run_chunk: null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    return run_batch(1, &h, st, ck, (cudaStream_t)stream);
+}
+
+int nce_ce_run_batch(int32_t n_jobs, const nce_ce_handle *hs, const nce_pt_state *st, const nce_pt_chunk *ck, void *stream) {
+    NCE_CHECK(hs && st && ck, "nce_ce_run_batch: null argument");
+    return run_batch(n_jobs, hs, st, ck, (cudaStream_t)stream);
+}
+
+int nce_pt_minimum(const nce_pt_state *st, double *out_min, int32_t *out_arg, void *stream) {
+    NCE_CHECK(st && st->E && st->E_min_rep && out_min && out_arg && st->R >= 1, "nce_pt_minimum: bad argument");
+    pt_minimum_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(st->E, st->E_min_rep, st->R, out_min, out_arg);
+    NCE_CUDA(cudaGetLastError());
+    return NCE_OK;
+}
+
+int nce_ce_run_chunk_host(nce_ce_handle h, int32_t R, int8_t *sigma_host, double *E_host, const float *beta_slot_host,
+                          int32_t *rep_of_slot_host, int32_t *slot_of_rep_host, const int32_t *ladder_id_host,
+                          double *E_min_rep_host, int64_t *n_acc_host, int64_t *n_ex_host, const nce_pt_chunk *ckh,
+                          double *E_samples_host) {
+    NCE_CHECK(h && R >= 1 && sigma_host && E_host && beta_slot_host && rep_of_slot_host && slot_of_rep_host && ladder_id_host &&
+              E_min_rep_host && n_acc_host && n_ex_host && ckh, "nce_ce_run_chunk_host: null argument");
+    int rc = check_chunk(nullptr, ckh); if (rc) return rc;
+    std::lock_guard<std::mutex> lk(h->mu);
+    const int64_t N = h->N, T = ckh->n_steps;
+    const bool props = ckh->prop_a != nullptr;
+    const int64_t nsamp = (E_samples_host && ckh->sample_interval > 0) ? T / ckh->sample_interval : 0;
+    const int64_t nexu = ckh->ex_u ? (R - 1 + 1) / 2 : 0;
+    auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+    size_t off[16]; size_t o = 0; int k = 0;
+    const size_t sizes[] = {(size_t)R * N, sizeof(double) * R, sizeof(float) * R, sizeof(int32_t) * R, sizeof(int32_t) * R,
+                            sizeof(int32_t) * R, sizeof(double) * R, sizeof(int64_t) * R, sizeof(int64_t),
+                            props ? sizeof(int32_t) * T * R : 0, props ? sizeof(int32_t) * T * R : 0,
+                            props ? sizeof(double) * T * R : 0, sizeof(double) * nsamp * R, sizeof(double) * nexu};
+    for (size_t sz : sizes) { off[k++] = o; o = al(o + sz); }
+    if (o > h->staging_bytes) {
+        if (h->staging_base) cudaFree(h->staging_base);
+        h->staging_base = nullptr; h->staging_bytes = 0;
+        NCE_CUDA(cudaMalloc(&h->staging_base, o));
+        h->staging_bytes = o;
+    }
+    char *b = (char *)h->staging_base;
+    nce_pt_state st;
+    st.R = R; st.N = N; st.sigma = (int8_t *)(b + off[0]); st.E = (double *)(b + off[1]); st.beta_slot = (float *)(b + off[2]);
+    st.rep_of_slot = (int32_t *)(b + off[3]); st.slot_of_rep = (int32_t *)(b + off[4]); st.ladder_id = (int32_t *)(b + off[5]);
+    st.E_min_rep = (double *)(b + off[6]); st.n_acc = (int64_t *)(b + off[7]); st.n_ex = (int64_t *)(b + off[8]);
+    nce_pt_chunk ck = *ckh;
+    cudaStream_t s = 0;
+    NCE_CUDA(cudaMemcpyAsync(st.sigma, sigma_host, (size_t)R * N, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync(st.E, E_host, sizeof(double) * R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync((void *)st.beta_slot, beta_slot_host, sizeof(float) * R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync(st.rep_of_slot, rep_of_slot_host, sizeof(int32_t) * R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync(st.slot_of_rep, slot_of_rep_host, sizeof(int32_t) * R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync((void *)st.ladder_id, ladder_id_host, sizeof(int32_t) * R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync(st.E_min_rep, E_min_rep_host, sizeof(double) * R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync(st.n_acc, n_acc_host, sizeof(int64_t) * R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync(st.n_ex, n_ex_host, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    if (props) {
+        ck.prop_a = (int32_t *)(b + off[9]); ck.prop_b = (int32_t *)(b + off[10]); ck.prop_u = (double *)(b + off[11]);
+        NCE_CUDA(cudaMemcpyAsync((void *)ck.prop_a, ckh->prop_a, sizeof(int32_t) * T * R, cudaMemcpyHostToDevice, s));
+        NCE_CUDA(cudaMemcpyAsync((void *)ck.prop_b, ckh->prop_b, sizeof(int32_t) * T * R, cudaMemcpyHostToDevice, s));
+        NCE_CUDA(cudaMemcpyAsync((void *)ck.prop_u, ckh->prop_u, sizeof(double) * T * R, cudaMemcpyHostToDevice, s));
+    }
+    ck.E_samples = nsamp ? (double *)(b + off[12]) : nullptr;
+    if (nexu) {
+        ck.ex_u = (double *)(b + off[13]);
+        NCE_CUDA(cudaMemcpyAsync((void *)ck.ex_u, ckh->ex_u, sizeof(double) * nexu, cudaMemcpyHostToDevice, s));
+    }
+    rc = run_batch(1, &h, &st, &ck, s);
+    if (rc) return rc;
+    NCE_CUDA(cudaMemcpyAsync(sigma_host, st.sigma, (size_t)R * N, cudaMemcpyDeviceToHost, s));
+    NCE_CUDA(cudaMemcpyAsync(E_host, st.E, sizeof(double) * R, cudaMemcpyDeviceToHost, s));
+    NCE_CUDA(cudaMemcpyAsync(rep_of_slot_host, st.rep_of_slot, sizeof(int32_t) * R, cudaMemcpyDeviceToHost, s));
+    NCE_CUDA(cudaMemcpyAsync(slot_of_rep_host, st.slot_of_rep, sizeof(int32_t) * R, cudaMemcpyDeviceToHost, s));
+    NCE_CUDA(cudaMemcpyAsync(E_min_rep_host, st.E_min_rep, sizeof(double) * R, cudaMemcpyDeviceToHost, s));
+    NCE_CUDA(cudaMemcpyAsync(n_acc_host, st.n_acc, sizeof(int64_t) * R, cudaMemcpyDeviceToHost, s));
+    NCE_CUDA(cudaMemcpyAsync(n_ex_host, st.n_ex, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    if (nsamp) NCE_CUDA(cudaMemcpyAsync(E_samples_host, ck.E_samples, sizeof(double) * nsamp * R, cudaMemcpyDeviceToHost, s));
+    NCE_CUDA(cudaStreamSynchronize(s));
+    return NCE_OK;
+}
+
+int nce_ce_errors(nce_ce_handle h, int32_t *flags) {
+    NCE_CHECK(h && flags, "nce_ce_errors: null argument");
+    NCE_CUDA(cudaMemcpy(flags, h->err, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    NCE_CUDA(cudaMemset(h->err, 0, sizeof(int32_t)));
+    return NCE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,58 @@
+"""Synthetic, seeded workloads of the benchmark configurations (no dataset is involved).
+
+ce_config(L):  fcc Ni/Pt, a = 3.924 A, 4-site conventional cell repeated L x L x L (L = 8: 2,048 sites),
+               cluster set cut at pairs 8 A / triplets 6 A / quadruplets 5 A (the shipped PtNi .ce's cutoffs),
+               one ECI per orbit ~ N(0, (0.05 eV / k)^2) with k the 1-based rank of the orbit (order, radius),
+               zerolet 0.  ECIs are per-atom energies; the cell's total energy uses energy_scale = N, as the
+               shipped .ce does for its 256-site base cell.  Occupancy int8, exactly N/2 Pt by a seeded
+               permutation (numpy default_rng).
+ladder(R):     geometric 300-1400 K, beta = 1/(kB T) in float32 (``neuralce/ce/pt_mcmc_ce.py:223-229``).
+"""
+from __future__ import annotations
+
+import functools
+
+import numpy as np
+
+from .ce_tables import ClusterSpace, synthetic_eci
+from .io import Z_OF, fcc_conventional, fcc_primitive
+
+A_FCC = 3.924
+CUTOFFS = (8.0, 6.0, 5.0)
+
+
+@functools.lru_cache(maxsize=4)
+def cluster_space(cutoffs=CUTOFFS):
+    return ClusterSpace.build(fcc_primitive(A_FCC), list(cutoffs))
+
+
+def ce_structure(L, seed=0, x_pt=0.5):
+    s = fcc_conventional(A_FCC, (L, L, L))
+    N = len(s)
+    rng = np.random.default_rng(seed)
+    n_pt = int(round(x_pt * N))
+    z = np.full(N, Z_OF["Ni"], np.int64)
+    z[rng.permutation(N)[:n_pt]] = Z_OF["Pt"]
+    s.numbers = z
+    return s
+
+
+def ce_config(L=8, seed=0, x_pt=0.5, eci_seed=0):
+    """(GPUClusterExpansion, canonical sigma) of the synthetic CE workload on an L^3 conventional fcc cell."""
+    from .ce import GPUClusterExpansion
+    cs = cluster_space()
+    eci = synthetic_eci(cs, eci_seed)
+    s = ce_structure(L, seed, x_pt)
+    gce = GPUClusterExpansion((cs, eci), s, energy_scale=len(s))
+    return gce, gce.encode(s)
+
+
+def ladder(R, T_min=300.0, T_max=1400.0):
+    temps = np.geomspace(T_min, T_max, R) if R > 1 else np.array([T_min])
+    return temps, (1.0 / (8.617333e-5 * temps)).astype(np.float32)
+
+
+def replica_configs(sigma, R, seed):
+    """R independent shuffles of sigma (same composition), one per replica."""
+    rng = np.random.default_rng(seed)
+    return np.stack([sigma[rng.permutation(len(sigma))] for _ in range(R)]).astype(np.int8)

@@ -1,0 +1,192 @@
+"""GPU parity of the CE engine against the C oracle (float64), through the C-ABI.
+
+Tolerances: float64 kernel dE within 1e-10 eV of the oracle (only the summation order differs); float32
+kernel dE within 1e-6 eV (spec bound).  Occupancy trajectories on a seeded stream are bit-exact;
+steps whose Metropolis margin |beta*dE + ln u| is below 1e-9 (fp64) / 1e-5 (fp32) would be allowed to differ
+and are counted -- none occur for these seeds.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(L, seed=0, R=4):
+    from neuralce_gb300.workloads import ce_config, ladder, replica_configs
+    from oracle.ce_oracle import OracleCE
+    gce, sig = ce_config(L, seed=seed)
+    orc = OracleCE(gce.info)
+    sig_r = replica_configs(sig, R, seed + 1)
+    _, beta = ladder(R)
+    return gce, orc, sig_r, beta
+
+
+@pytest.mark.parametrize("L", [2, 3, 8])
+def test_energy_matches_oracle(cuda, L):
+    torch = cuda
+    gce, orc, sig_r, _ = _setup(L)
+    E = gce.batched_energy(torch.as_tensor(sig_r).cuda()).cpu().numpy()
+    E32 = gce.batched_energy(torch.as_tensor(sig_r).cuda(), precision=32).cpu().numpy()
+    for r in range(len(sig_r)):
+        e = orc.energy(sig_r[r])
+        assert abs(E[r] - e) < 1e-10 * max(1.0, abs(e)), (E[r], e)
+        assert abs(E32[r] - e) < 1e-5, (E32[r], e)
+
+
+@pytest.mark.parametrize("L,warps", [(2, 8), (3, 4), (8, 8), (8, 32)])
+def test_delta_matches_oracle(cuda, L, warps):
+    """Random swaps (L=2: the 8 A pair shell wraps onto periodic images of the 16-site cell)."""
+    torch = cuda
+    gce, orc, sig_r, _ = _setup(L)
+    rng = np.random.default_rng(L * 100 + warps)
+    N = gce.n_atoms
+    q = []
+    while len(q) < 200:
+        r = int(rng.integers(0, len(sig_r))); ia, ib = (int(x) for x in rng.integers(0, N, 2))
+        if sig_r[r, ia] != sig_r[r, ib]:
+            q.append((r, ia, ib))
+    rep, ia, ib = (np.array(x) for x in zip(*q))
+    sa_new = sig_r[rep, ib]; sb_new = sig_r[rep, ia]
+    sd = torch.as_tensor(sig_r).cuda()
+    d64 = gce.delta_energy_batch(sd, rep, ia, ib, sa_new, sb_new, precision=64, warps=warps).cpu().numpy()
+    d32 = gce.delta_energy_batch(sd, rep, ia, ib, sa_new, sb_new, precision=32, warps=warps).cpu().numpy()
+    want = np.array([orc.delta(sig_r[r], a, b, sa, sb) for r, a, b, sa, sb in zip(rep, ia, ib, sa_new, sb_new)])
+    assert np.abs(d64 - want).max() < 1e-10
+    assert np.abs(d32 - want).max() < 1e-6
+
+
+def _engine_state(sig_r, E, beta):
+    from neuralce_gb300.pt import PTState
+    return PTState(sig_r, E, beta, np.zeros(len(beta), np.int32))
+
+
+def _compare(st, ref, E_tol):
+    assert np.array_equal(st.sigma.cpu().numpy(), ref["sigma"])
+    assert np.abs(st.E.cpu().numpy() - ref["E"]).max() < E_tol
+    assert np.array_equal(st.n_acc.cpu().numpy(), ref["n_acc"])
+    assert np.array_equal(st.rep_of_slot.cpu().numpy(), ref["rep_of_slot"])
+    assert np.array_equal(st.slot_of_rep.cpu().numpy(), ref["slot_of_rep"])
+    assert int(st.n_ex.item()) == int(ref["n_ex"][0])
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_trajectory_host_stream(cuda, precision):
+    """Seeded host proposal stream + exchange uniforms: bit-exact occupancy trajectory, energies, acceptance,
+    slot permutation and slot-ordered samples vs the oracle."""
+    torch = cuda
+    from neuralce_gb300.ce import proposal_stream
+    from neuralce_gb300.pt import run_chunk
+    from oracle.ce_oracle import new_state
+    R, T, si = 8, 1500, 50
+    gce, orc, sig_r, beta = _setup(8, seed=3, R=R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    st = _engine_state(sig_r, E0, beta)
+    ref = new_state(sig_r, E0, beta)
+    step = 0
+    for chunk in range(2):
+        pa, pb, pu = proposal_stream(gce, R, T, seed=10 + chunk)
+        exu = np.random.default_rng(50 + chunk).random((R - 1 + 1) // 2)
+        exu = 1.0 - exu
+        par = chunk % 2
+        Es = torch.zeros((T // si, R), dtype=torch.float64, device="cuda")
+        dev = tuple(torch.as_tensor(x).cuda() for x in (pa, pb, pu))
+        run_chunk(gce, st, T, step, 0, precision, 8, dev, si, Es, True, par, torch.as_tensor(exu).cuda())
+        Es_ref = np.zeros((T // si, R))
+        orc.run(ref, T, step, 0, (pa, pb, pu), si, Es_ref, True, par, exu, n_threads=4)
+        torch.cuda.synchronize()
+        tol = 1e-9 if precision == 64 else 1e-4
+        _compare(st, ref, tol)
+        assert np.abs(Es.cpu().numpy() - Es_ref).max() < tol
+        step += T
+    assert int(st.n_acc.sum()) > 0
+
+
+def test_trajectory_philox_multichunk(cuda):
+    """Device Philox stream, 3 chunks with exchanges: equals the oracle's Philox restatement."""
+    torch = cuda
+    from neuralce_gb300.pt import run_chunk
+    from oracle.ce_oracle import new_state
+    R, T = 16, 1000
+    gce, orc, sig_r, beta = _setup(4, seed=5, R=R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    st = _engine_state(sig_r, E0, beta); ref = new_state(sig_r, E0, beta)
+    for c in range(3):
+        Es = torch.zeros((T // 100, R), dtype=torch.float64, device="cuda")
+        Es_ref = np.zeros((T // 100, R))
+        run_chunk(gce, st, T, c * T, 1234, 64, 4, None, 100, Es, True)
+        orc.run(ref, T, c * T, 1234, None, 100, Es_ref, True, n_threads=4)
+        torch.cuda.synchronize()
+        _compare(st, ref, 1e-9)
+        assert np.abs(Es.cpu().numpy() - Es_ref).max() < 1e-9
+    # running energies equal full recomputes
+    Ef = gce.batched_energy(st.sigma).cpu().numpy()
+    assert np.abs(Ef - st.E.cpu().numpy()).max() < 1e-9
+
+
+def test_batch_equals_alone(cuda):
+    """Jobs with different cells and replica counts in one launch give the same results as alone."""
+    torch = cuda
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.pt import make_chunk
+    jobs = []
+    for k, (L, R) in enumerate([(3, 2), (4, 5), (5, 3)]):
+        gce, orc, sig_r, beta = _setup(L, seed=20 + k, R=R)
+        E0 = np.array([orc.energy(x) for x in sig_r])
+        jobs.append((gce, sig_r, E0, beta))
+    T = 700
+    alone = []
+    for k, (gce, sig_r, E0, beta) in enumerate(jobs):
+        st = _engine_state(sig_r, E0, beta)
+        ck = make_chunk(T, 0, 77 + k, 64, 4, None, 1, None, True)
+        _lib.check(_lib.lib().nce_ce_run_chunk(gce.handle, C.byref(st.struct()), C.byref(ck), _lib.stream_ptr()), "alone")
+        alone.append(st)
+    sts = [_engine_state(sig_r, E0, beta) for (_, sig_r, E0, beta) in jobs]
+    hs = (C.c_void_p * 3)(*[j[0].handle.value for j in jobs])
+    ss = (_lib.NcePtState * 3)(*[s.struct() for s in sts])
+    cks = (_lib.NcePtChunk * 3)(*[make_chunk(T, 0, 77 + k, 64, 4, None, 1, None, True) for k in range(3)])
+    _lib.check(_lib.lib().nce_ce_run_batch(3, hs, ss, cks, _lib.stream_ptr()), "batch")
+    torch.cuda.synchronize()
+    for a, b in zip(alone, sts):
+        assert torch.equal(a.sigma, b.sigma) and torch.equal(a.E, b.E) and torch.equal(a.rep_of_slot, b.rep_of_slot)
+
+
+def test_host_buffer_entry_point(cuda):
+    """nce_ce_run_chunk_host (host buffers, copies inside) equals the device-pointer call."""
+    torch = cuda
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.pt import make_chunk, run_chunk
+    R, T = 4, 600
+    gce, orc, sig_r, beta = _setup(3, seed=8, R=R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    st = _engine_state(sig_r, E0, beta)
+    run_chunk(gce, st, T, 0, 5, 64, 4, None, 100, None, True)
+    h_sig = sig_r.copy(); h_E = E0.copy(); ros = np.arange(R, dtype=np.int32); sor = ros.copy()
+    lid = np.zeros(R, np.int32); emr = np.full(R, np.inf); emr[0] = E0[0]; nacc = np.zeros(R, np.int64); nex = np.zeros(1, np.int64)
+    samples = np.zeros((T // 100, R))
+    ck = make_chunk(T, 0, 5, 64, 4, None, 100, None, True)
+    p = _lib.ptr
+    _lib.check(_lib.lib().nce_ce_run_chunk_host(gce.handle, R, p(h_sig), p(h_E), p(beta), p(ros), p(sor), p(lid), p(emr),
+                                                p(nacc), p(nex), C.byref(ck), p(samples)), "host")
+    torch.cuda.synchronize()
+    assert np.array_equal(h_sig, st.sigma.cpu().numpy()) and np.array_equal(h_E, st.E.cpu().numpy())
+    assert np.array_equal(ros, st.rep_of_slot.cpu().numpy()) and np.array_equal(nacc, st.n_acc.cpu().numpy())
+
+
+def test_out_of_range_proposal_is_flagged(cuda):
+    """A proposal index outside [0, N) is rejected by the kernel's bounds check and reported, not read."""
+    torch = cuda
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.pt import run_chunk
+    R, T = 2, 10
+    gce, orc, sig_r, beta = _setup(3, R=R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    st = _engine_state(sig_r, E0, beta)
+    pa = np.zeros((T, R), np.int32); pb = np.ones((T, R), np.int32); pu = np.full((T, R), 0.5)
+    pa[3, 1] = gce.n_atoms + 5
+    dev = tuple(torch.as_tensor(x).cuda() for x in (pa, pb, pu))
+    run_chunk(gce, st, T, 0, 0, 64, 4, dev)
+    flags = _lib.i32()
+    _lib.check(_lib.lib().nce_ce_errors(gce.handle, C.byref(flags)), "errors")
+    assert flags.value & 1
