@@ -146,6 +146,81 @@ int nce_pt_minimum(const nce_pt_state *st, double *out_min, int32_t *out_arg, vo
  * [0, N) (that step was rejected instead of read). */
 int nce_ce_errors(nce_ce_handle h, int32_t *flags);
 
+/* ── NeuralCE receptive-field update ─────────────────────────────────────────────────────────────
+ * Reference interfaces replaced:
+ *   nce_nce_create      setup / setup_implicit geometry + expand_params      neuralce/nce/mc_model.py:60-111,175-228
+ *                       (build_geometry                                      neuralce/nce/gpu_layer0_implicit.py:17-118)
+ *   nce_nce_full_cache  full_cache + energy_of (h0 cache mode)               neuralce/nce/local_update_implicit.py:89-112
+ *   nce_nce_run_chunk   scan(step): propose, local_delta, accept, commit    neuralce/nce/mcmc.py:130-199,
+ *                                                                            neuralce/nce/local_update_implicit.py:117-194
+ *                       + neighbour exchange rounds at the chunk end         neuralce/nce/mcmc.py:370-384
+ */
+typedef struct {
+    int32_t nB, J, mo, P, W, depth, C0, D, maxM, maxP, wL;
+    int64_t d[3];
+    int64_t n_cells;
+    const int32_t *Rv_b;   /* (nB, J, mo) member basis of the reverse rows */
+    const int32_t *Rv_uo;  /* (nB, J, mo, 3) */
+    const int32_t *Rv_p;   /* (nB, J, mo) point-function index */
+    const int32_t *Rv_col; /* (nB, J) cluster-vector column (channel = col + 1) */
+    const uint8_t *Rv_m;   /* (nB, J, mo) member mask */
+    const double *Rv_w;    /* (nB, J) nA / (order * count * n_cells * sd[col+1]); 0 for padded rows */
+    const int32_t *Mb;     /* (nB) species per basis site */
+    const double *theta;   /* (maxM+1, maxP, maxM) point functions */
+    const int32_t *Sh_b;   /* (nB, P, W) shell partners */
+    const int32_t *Sh_uo;  /* (nB, P, W, 3) */
+    const uint8_t *Sh_m;   /* (nB, P, W) */
+    const float *Sh_inv;   /* (nB, P) 1 / max(partners, 1) */
+    const int32_t *ball_b; /* (nB, wL) receptive-field offsets, ordered by the level where they first appear */
+    const int32_t *ball_uo;/* (nB, wL, 3) */
+    const int32_t *ball_end; /* (nB, depth+1) end of each level in the ball lists */
+    const float *lin;      /* (C0) layer-0 linear readout */
+    const float *head_w;   /* (D) */
+    double head_b;
+    const float *W_cat[4]; /* per layer ((1+P)*Cin, D): [W_self; W_shell[0]; ...] */
+    const float *bias[4];  /* (D) */
+    const float *G_cat[4]; /* per layer (P*Cin, D) sigmoid-gate weights, or NULL */
+    const float *gate_b[4];
+    const float *mu, *sd;  /* (C0) standardisation of layer 0 */
+    int32_t act;           /* 0 tanh (reference model), 1 SiLU */
+    int32_t gate;          /* layers carry a sigmoid gate */
+    double norm;           /* energy = sum(e) / norm + head_b: nA (site mean) or 1 (sum) */
+    double scale_eV;       /* dE in eV = dE * scale_eV (ys * N for model.pkl, 1 for eV-valued models) */
+    int32_t n_groups, max_gb;
+    const int32_t *act_b, *act_nb; const uint64_t *grp_cum;   /* swap groups, as in nce_ce_tables */
+} nce_nce_desc;
+
+typedef struct nce_nce_model *nce_nce_handle;
+
+typedef struct {
+    int32_t R; int64_t N;
+    int8_t *sigma;         /* (R, N) */
+    float *h0;             /* (R, N, C0) standardised layer 0 */
+    float *hmid;           /* (depth-1, R, N, D) hidden layers 1..depth-1, or NULL for depth < 2 */
+    float *e;              /* (R, N) per-site energy */
+    double *E;             /* (R) energy: sum(e)/norm + head_b */
+    const float *beta_slot; int32_t *rep_of_slot, *slot_of_rep; const int32_t *ladder_id;
+    int64_t *n_acc, *n_ex;
+} nce_nce_state;
+
+typedef struct {
+    int64_t n_steps, step0;
+    const int32_t *prop_a, *prop_b; const double *prop_u; /* (n_steps, R) or NULL -> Philox */
+    uint64_t seed;
+    int64_t sample_interval; double *E_samples;           /* (n_steps/si, R) or NULL */
+    double *dE_out;        /* (n_steps, R) dE of every step (0 for same-species draws), or NULL */
+    int32_t force;         /* 0 Metropolis, 1 accept every move, -1 reject every move */
+    int32_t exchange_rounds; /* neighbour-slot exchange rounds at the chunk end (0 = none) */
+    int32_t ex_parity; const double *ex_u; /* host-supplied exchange randoms: (rounds) parities packed in bits,
+                                              ex_u (rounds, ceil((R-1)/2)); NULL -> Philox */
+} nce_nce_chunk;
+
+int nce_nce_create(const nce_nce_desc *desc, nce_nce_handle *out);
+int nce_nce_destroy(nce_nce_handle h);
+int nce_nce_full_cache(nce_nce_handle h, const nce_nce_state *st, void *stream);
+int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_chunk *ck, void *stream);
+int nce_nce_errors(nce_nce_handle h, int32_t *flags);
+
 /* Philox4x32-10 on the host (same function the kernels use), for tests and host drivers. */
 void nce_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

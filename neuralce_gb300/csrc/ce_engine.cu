@@ -288,6 +288,7 @@ struct CEExJob {
     int32_t R; double *E; const float *beta_slot; int32_t *rep_of_slot, *slot_of_rep; const int32_t *ladder_id;
     int64_t *n_ex; uint64_t seed; int64_t g_end; int32_t parity; const double *ex_u;
     double *E_samples; int64_t last_row; int32_t do_exchange;
+    double E_scale; int32_t rounds;          // energies in eV = E * E_scale; exchange rounds back to back
 };
 struct CEExBatch { int32_t n_jobs; CEExJob job[kMaxJobs]; };
 
@@ -302,22 +303,26 @@ __global__ void ce_exchange_kernel(const __grid_constant__ CEExBatch bt) {
     const int R = x.R;
     const uint32_t k0 = (uint32_t)x.seed, k1 = (uint32_t)(x.seed >> 32);
     const uint32_t c0 = (uint32_t)x.g_end, c1 = (uint32_t)((uint64_t)x.g_end >> 32);
-    int parity = x.ex_u ? x.parity : (int)(philox4x32(c0, c1, 0xFFFFFFFFu, 0u, k0, k1).x & 1u);
-    for (int i = 0; i < R; ++i) perm[i] = i;
+    const int npair = R / 2;                 // ceil((R-1)/2)
     int64_t nswap = 0;
-    for (int k = 0; 2 * k < R - 1; ++k) {
-        const int a = 2 * k + parity, b = a + 1;
-        if (b >= R) continue;
-        if (x.ladder_id[a] != x.ladder_id[b]) continue;
-        const double Ea = x.E[x.rep_of_slot[a]], Eb = x.E[x.rep_of_slot[b]];
-        const double log_acc = ((double)x.beta_slot[b] - (double)x.beta_slot[a]) * (Eb - Ea);
-        double u;
-        if (x.ex_u) u = x.ex_u[k];
-        else { u32x4 w = philox4x32(c0, c1, 0xFFFFFFFEu, (uint32_t)k, k0, k1); u = draw_u01(w.x, w.y); }
-        if (log(u) < log_acc) { perm[a] = b; perm[b] = a; ++nswap; }
+    for (int q = 0; q < max(x.rounds, 1); ++q) {
+        const uint32_t cq = 0xFFFFFFFFu - 2u * (uint32_t)q;
+        const int parity = x.ex_u ? ((x.parity >> q) & 1) : (int)(philox4x32(c0, c1, cq, 0u, k0, k1).x & 1u);
+        for (int i = 0; i < R; ++i) perm[i] = i;
+        for (int k = 0; 2 * k < R - 1; ++k) {
+            const int a = 2 * k + parity, b = a + 1;
+            if (b >= R) continue;
+            if (x.ladder_id[a] != x.ladder_id[b]) continue;
+            const double Ea = x.E[x.rep_of_slot[a]] * x.E_scale, Eb = x.E[x.rep_of_slot[b]] * x.E_scale;
+            const double log_acc = ((double)x.beta_slot[b] - (double)x.beta_slot[a]) * (Eb - Ea);
+            double u;
+            if (x.ex_u) u = x.ex_u[(size_t)q * npair + k];
+            else { u32x4 w = philox4x32(c0, c1, cq - 1u, (uint32_t)k, k0, k1); u = draw_u01(w.x, w.y); }
+            if (log(u) < log_acc) { perm[a] = b; perm[b] = a; ++nswap; }
+        }
+        for (int t = 0; t < R; ++t) ros[t] = x.rep_of_slot[perm[t]];
+        for (int t = 0; t < R; ++t) { x.rep_of_slot[t] = ros[t]; x.slot_of_rep[ros[t]] = t; }
     }
-    for (int t = 0; t < R; ++t) ros[t] = x.rep_of_slot[perm[t]];
-    for (int t = 0; t < R; ++t) { x.rep_of_slot[t] = ros[t]; x.slot_of_rep[ros[t]] = t; }
     *x.n_ex += nswap;
     if (x.E_samples && x.last_row >= 0)
         for (int t = 0; t < R; ++t) x.E_samples[x.last_row * R + t] = x.E[x.rep_of_slot[t]];
@@ -585,6 +590,7 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
         x.parity = ck.ex_parity; x.ex_u = ck.ex_u; x.E_samples = ck.E_samples;
         x.last_row = (ck.E_samples && ck.n_steps > 0 && ck.n_steps % ck.sample_interval == 0) ? ck.n_steps / ck.sample_interval - 1 : -1;
         x.do_exchange = ck.do_exchange && st.R > 1;
+        x.E_scale = 1.0; x.rounds = 1;
         any = any || x.do_exchange;
     }
     if (any) {
@@ -594,6 +600,25 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
         ce_exchange_kernel<<<n_jobs, 32, xs, s>>>(ex);
         NCE_CUDA(cudaGetLastError());
     }
+    return NCE_OK;
+}
+
+// chunk-end slot exchange of one job (used by the NCE engine)
+int launch_exchange(int32_t R, double *E, double E_scale, const float *beta_slot, int32_t *ros, int32_t *sor, const int32_t *lid,
+                    int64_t *n_ex, uint64_t seed, int64_t g_end, int32_t parity_bits, const double *ex_u, int32_t rounds,
+                    cudaStream_t s) {
+    if (R < 2 || rounds < 1) return NCE_OK;
+    CEExBatch ex; std::memset(&ex, 0, sizeof(ex));
+    ex.n_jobs = 1;
+    CEExJob &x = ex.job[0];
+    x.R = R; x.E = E; x.beta_slot = beta_slot; x.rep_of_slot = ros; x.slot_of_rep = sor; x.ladder_id = lid; x.n_ex = n_ex;
+    x.seed = seed; x.g_end = g_end; x.parity = parity_bits; x.ex_u = ex_u; x.E_samples = nullptr; x.last_row = -1;
+    x.do_exchange = 1; x.E_scale = E_scale; x.rounds = rounds;
+    const size_t xs = sizeof(int32_t) * 2 * (size_t)R;
+    NCE_CHECK(xs <= 200 * 1024, "exchange: %d replicas exceed the exchange kernel's shared memory", R);
+    NCE_CUDA(cudaFuncSetAttribute(ce_exchange_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
+    ce_exchange_kernel<<<1, 32, xs, s>>>(ex);
+    NCE_CUDA(cudaGetLastError());
     return NCE_OK;
 }
 

@@ -1,0 +1,760 @@
+// NeuralCE receptive-field local update on GB300 (sm_103a).
+//
+// One CTA per replica runs every step of a chunk:
+//   1. proposal (i, j) from Philox or a host stream; same species -> accepted no-op (reference rule dE = 0 <= 0)
+//   2. nested unique receptive field: the ball offsets of i and j are enumerated level by level and claimed in
+//      a per-replica slot map, so positions [0, n_l) of the site list are exactly ball_l(i) U ball_l(j)
+//   3. layer-0 change: the reverse rows of both flips (the second with the first applied) push
+//      dPi * nA / (order * norm * sd) onto every member; sums are int64 fixed point (2^-40) in shared memory,
+//      so the result does not depend on the order of the atomic adds
+//   4. layer l+1 on positions [0, n_{l+1}): gather [h, masked shell means] of the patched level-l values into a
+//      shared tile, FP32 FMA against [W_self; W_shell] (+ sigmoid gate), tanh or SiLU
+//   5. dE = sum over the last level of (e_new - e) (fixed point), Metropolis rule of the reference's NCE driver
+//      (dE_eV <= 0 or u < exp(-beta dE_eV)), commit of h0 / hidden / e rows on accept, slot map cleared.
+// Full cache (h0 pull over reverse rows, layers on all sites, per-site e) and the energy are separate kernels.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <climits>
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+
+namespace nce {
+
+int launch_exchange(int32_t R, double *E, double E_scale, const float *beta_slot, int32_t *ros, int32_t *sor, const int32_t *lid,
+                    int64_t *n_ex, uint64_t seed, int64_t g_end, int32_t parity_bits, const double *ex_u, int32_t rounds,
+                    cudaStream_t s);
+
+constexpr int kMaxLayers = 4;
+constexpr int kTM = 16;                 // sites per GEMM tile
+constexpr double kFix = 1099511627776.0;      // 2^40
+constexpr double kInvFix = 1.0 / 1099511627776.0;
+
+struct NceDev {
+    int32_t nB, J, mo, P, W, depth, C0, D, maxM, maxP;
+    int32_t d0, d1, d2;
+    int64_t N, n_cells;
+    int32_t wL;                           // ball offsets per basis (last level)
+    const int32_t *Rv_b, *Rv_uo, *Rv_p, *Rv_col; const uint8_t *Rv_m; const double *Rv_w;   // (nB,J,mo[,3]), (nB,J)
+    const int32_t *Mb; const double *theta;                                                  // (nB), (maxM+1,maxP,maxM)
+    const int32_t *Sh_b, *Sh_uo; const uint8_t *Sh_m; const float *Sh_inv;                  // (nB,P,W[,3]), (nB,P)
+    const int32_t *ball_b, *ball_uo, *ball_end;                                              // (nB,wL[,3]), (nB,depth+1)
+    const float *lin, *head_w; float head_b;
+    const float *Wc[kMaxLayers], *bias[kMaxLayers], *G[kMaxLayers], *gb[kMaxLayers];
+    const float *mu, *sd;
+    int32_t act, gate; double norm, scale_eV;
+    int32_t n0max, nmax;
+    int32_t n_groups, max_gb; const int32_t *act_b, *act_nb; const uint64_t *grp_cum;
+};
+
+struct NceJob {
+    NceDev m;
+    // state
+    int8_t *sigma; float *h0; float *hmid; float *e; double *E;
+    const float *beta_slot; const int32_t *slot_of_rep; int64_t *n_acc;
+    int32_t R;
+    // scratch (per replica stride)
+    int32_t *slot; int32_t *list; float *newbuf; float *e_new; int64_t scratch_stride;   // floats per replica in newbuf
+    // chunk
+    int64_t n_steps, step0; const int32_t *prop_a, *prop_b; const double *prop_u; uint64_t seed;
+    int64_t sample_interval; double *E_samples; double *dE_out; int32_t force;   // force: 0 Metropolis, 1 accept, -1 reject
+    int32_t *err;
+};
+
+__device__ __forceinline__ int32_t wadd(int32_t k, int32_t u, int32_t d) { int32_t q = k + u; return q >= d ? q - d : q; }
+
+__device__ __forceinline__ void coords(const NceDev &m, int64_t i, int32_t &b, int32_t k[3]) {
+    b = (int32_t)(i % m.nB);
+    int64_t c = i / m.nB;
+    k[0] = (int32_t)(c / ((int64_t)m.d1 * m.d2)); k[1] = (int32_t)((c / m.d2) % m.d1); k[2] = (int32_t)(c % m.d2);
+}
+
+__device__ __forceinline__ int64_t site_at(const NceDev &m, const int32_t k[3], const int32_t *uo, int32_t b) {
+    return (((int64_t)wadd(k[0], uo[0], m.d0) * m.d1 + wadd(k[1], uo[1], m.d1)) * m.d2 + wadd(k[2], uo[2], m.d2)) * m.nB + b;
+}
+
+__device__ __forceinline__ float act_fn(int act, float x) {
+    return act == 0 ? tanhf(x) : x / (1.0f + expf(-x));
+}
+
+// newbuf layout per replica: level 0 block (n0max x C0), then level l (1..depth-1) blocks (nmax x D)
+__device__ __forceinline__ float *level_buf(const NceJob &jb, float *base, int lvl) {
+    if (lvl == 0) return base;
+    return base + (size_t)jb.m.n0max * jb.m.C0 + (size_t)(lvl - 1) * jb.m.nmax * jb.m.D;
+}
+
+struct NceCtl {
+    int64_t si, sj; double u; int32_t same, bi, bj, ki[3], kj[3], ssi, ssj;
+    int32_t cnt; int32_t nl[kMaxLayers + 1];
+    unsigned long long dacc;
+};
+
+// value of level lvl at site q (patched by the step's new values), channel c
+__device__ __forceinline__ float patched(const NceJob &jb, int lvl, const float *cache, const float *newl, const int32_t *slot,
+                                         int32_t nlev, int64_t q, int c, int Cin) {
+    const int32_t p = slot[q];
+    if (p >= 0 && p < nlev) return newl[(size_t)p * Cin + c];
+    return cache[(size_t)q * Cin + c];
+}
+
+// Evaluate one layer for the sites list[pos0 .. pos0+cnt).  Inputs come from level lvl (cache patched with the step's
+// values, or unpatched when slot == nullptr).  Output per (m, n) delivered to `sink`.
+template <typename Sink>
+__device__ void layer_tiles(const NceJob &jb, int lvl, const float *cache, const float *newl, const int32_t *slot, int32_t nlev,
+                            const int32_t *list, int64_t pos0, int64_t cnt, const int64_t *direct0, float *X, int32_t *src,
+                            Sink sink) {
+    const NceDev &m = jb.m;
+    const int Cin = lvl == 0 ? m.C0 : m.D, D = m.D, P = m.P, W = m.W;
+    const int Kin = (1 + P) * Cin;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const float *Wc = m.Wc[lvl], *bias = m.bias[lvl], *G = m.gate ? m.G[lvl] : nullptr, *gb = m.gate ? m.gb[lvl] : nullptr;
+    const int mrow = tid / 16, ng = tid % 16;                         // 16 x 16 thread grid over (site, column group)
+    const int ncol = D / 16;
+    for (int64_t t0 = 0; t0 < cnt; t0 += kTM) {
+        const int tm = (int)min((int64_t)kTM, cnt - t0);
+        // gather: 1) source row of the site and of every shell partner (patched rows >= 0, cache rows -(q+1),
+        //            masked partner INT_MIN); 2) values and masked shell means
+        const int PW = 1 + P * W;
+        for (int idx = tid; idx < tm * PW; idx += nt) {
+            const int mm = idx / PW, q = idx % PW;
+            const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
+            int64_t site = s;
+            if (q > 0) {
+                int32_t b, k[3]; coords(m, s, b, k);
+                const int e0 = b * P * W + (q - 1);
+                site = m.Sh_m[e0] ? site_at(m, k, m.Sh_uo + 3 * e0, m.Sh_b[e0]) : -1;
+            }
+            int32_t code = INT_MIN;
+            if (site >= 0) {
+                const int32_t p = slot ? slot[site] : -1;
+                code = (p >= 0 && p < nlev) ? p : -(int32_t)(site + 1);
+            }
+            src[idx] = code;
+        }
+        __syncthreads();
+        for (int idx = tid; idx < tm * Cin; idx += nt) {
+            const int mm = idx / Cin, c = idx % Cin;
+            const int32_t *sr = src + mm * PW;
+            float *xr = X + (size_t)mm * Kin;
+            auto val = [&](int32_t code) {
+                return code >= 0 ? newl[(size_t)code * Cin + c] : cache[(size_t)(-(int64_t)code - 1) * Cin + c];
+            };
+            xr[c] = val(sr[0]);
+            int32_t b = 0;
+            {
+                const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
+                b = (int32_t)(s % m.nB);
+            }
+            for (int p = 0; p < P; ++p) {
+                float acc = 0.f;
+                for (int w = 0; w < W; ++w) {
+                    const int32_t code = sr[1 + p * W + w];
+                    if (code != INT_MIN) acc += val(code);
+                }
+                xr[Cin + p * Cin + c] = acc * m.Sh_inv[b * P + p];
+            }
+        }
+        __syncthreads();
+        if (mrow < tm) {
+            float o[8], g[8];
+            for (int j = 0; j < ncol; ++j) { o[j] = __ldg(bias + ng + 16 * j); g[j] = gb ? __ldg(gb + ng + 16 * j) : 0.f; }
+            const float *xr = X + (size_t)mrow * Kin;
+            for (int kk = 0; kk < Kin; ++kk) {
+                const float xv = xr[kk];
+                const float *wr = Wc + (size_t)kk * D + ng;
+#pragma unroll 8
+                for (int j = 0; j < 8; ++j) if (j < ncol) o[j] = fmaf(xv, __ldg(wr + 16 * j), o[j]);
+                if (G && kk >= Cin) {
+                    const float *gr = G + (size_t)(kk - Cin) * D + ng;
+#pragma unroll 8
+                    for (int j = 0; j < 8; ++j) if (j < ncol) g[j] = fmaf(xv, __ldg(gr + 16 * j), g[j]);
+                }
+            }
+            for (int j = 0; j < ncol; ++j) {
+                float v = act_fn(m.act, o[j]);
+                if (G) v *= 1.0f / (1.0f + expf(-g[j]));
+                o[j] = v;
+            }
+            sink(t0 + mrow, ng, o, ncol);
+        } else {
+            sink(-1, ng, nullptr, 0);
+        }
+        __syncthreads();
+    }
+}
+
+// reduce over the 16 threads of a row group (same half warp)
+__device__ __forceinline__ float row16_sum(float v) {
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, 16);
+    return v;
+}
+
+// One MC step of one replica (all threads of the block).  Returns through ctl (thread 0 reads dE).
+__device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &ctl, unsigned long long *dh, float *X,
+                         int32_t *src, double &E, int64_t &nacc) {
+    const NceDev &m = jb.m;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int64_t N = m.N;
+    int8_t *sig = jb.sigma + (int64_t)r * N;
+    float *h0 = jb.h0 + (size_t)r * N * m.C0;
+    float *e = jb.e + (size_t)r * N;
+    int32_t *slot = jb.slot + (size_t)r * N;
+    int32_t *list = jb.list + (size_t)r * m.nmax;
+    float *nb = jb.newbuf + (size_t)r * jb.scratch_stride;
+    float *en = jb.e_new + (size_t)r * m.nmax;
+    const int L = m.depth;
+    if (tid == 0) {
+        int64_t i, j; double u;
+        if (jb.prop_a) { i = jb.prop_a[s_idx * jb.R + t]; j = jb.prop_b[s_idx * jb.R + t]; u = jb.prop_u[s_idx * jb.R + t]; }
+        else {
+            const uint32_t k0 = (uint32_t)jb.seed, k1 = (uint32_t)(jb.seed >> 32);
+            const int64_t g = jb.step0 + s_idx;
+            const uint32_t c0 = (uint32_t)g, c1 = (uint32_t)((uint64_t)g >> 32);
+            u32x4 x = philox4x32(c0, c1, (uint32_t)t, 0u, k0, k1);
+            int grp = 0; uint32_t ba = 0, bb = 0;
+            if (m.n_groups > 1 || m.act_nb[0] > 1) {
+                u32x4 y = philox4x32(c0, c1, (uint32_t)t, 1u, k0, k1);
+                if (m.n_groups > 1)
+                    while (grp < m.n_groups - 1 && (uint64_t)y.x >= m.grp_cum[grp]) ++grp;
+                ba = draw_index(y.y, (uint32_t)m.act_nb[grp]); bb = draw_index(y.z, (uint32_t)m.act_nb[grp]);
+            }
+            const uint32_t nc = (uint32_t)m.n_cells;
+            i = (int64_t)draw_index(x.x, nc) * m.nB + m.act_b[grp * m.max_gb + ba];
+            j = (int64_t)draw_index(x.y, nc) * m.nB + m.act_b[grp * m.max_gb + bb];
+            u = draw_u01(x.z, x.w);
+        }
+        int same = 1;
+        if (i < 0 || j < 0 || i >= N || j >= N) { atomicOr(jb.err, 1); }
+        else { ctl.ssi = sig[i]; ctl.ssj = sig[j]; same = ctl.ssi == ctl.ssj; }
+        ctl.si = i; ctl.sj = j; ctl.u = u; ctl.same = same; ctl.cnt = 0; ctl.dacc = 0ull;
+        if (!same) { coords(m, i, ctl.bi, ctl.ki); coords(m, j, ctl.bj, ctl.kj); }
+    }
+    __syncthreads();
+    if (ctl.same) {
+        if (tid == 0) { ++nacc; if (jb.dE_out) jb.dE_out[s_idx * jb.R + t] = 0.0; }
+        return;
+    }
+    // 2. nested unique receptive field
+    for (int lvl = 0; lvl <= L; ++lvl) {
+        for (int f = 0; f < 2; ++f) {
+            const int b = f ? ctl.bj : ctl.bi;
+            const int32_t *k = f ? ctl.kj : ctl.ki;
+            const int q0 = lvl ? m.ball_end[b * (L + 1) + lvl - 1] : 0, q1 = m.ball_end[b * (L + 1) + lvl];
+            for (int q = q0 + tid; q < q1; q += nt) {
+                const int e0 = b * m.wL + q;
+                const int64_t s = site_at(m, k, m.ball_uo + 3 * e0, m.ball_b[e0]);
+                if (atomicCAS(&slot[s], -1, -2) == -1) {
+                    const int p = atomicAdd(&ctl.cnt, 1);
+                    list[p] = (int32_t)s; slot[s] = p;
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == 0) ctl.nl[lvl] = ctl.cnt;
+        __syncthreads();
+    }
+    const int n0 = ctl.nl[0];
+    if (n0 > m.n0max || ctl.nl[L] > m.nmax) {         // cannot happen for consistent tables; refuse instead of overflow
+        if (tid == 0) atomicOr(jb.err, 4);
+        for (int p = tid; p < min(ctl.nl[L], m.nmax); p += nt) slot[list[p]] = -1;
+        __syncthreads();
+        return;
+    }
+    // 3. layer-0 change (fixed point)
+    for (int idx = tid; idx < n0 * m.C0; idx += nt) dh[idx] = 0ull;
+    __syncthreads();
+    const int Jt = 2 * m.J;
+    for (int rr = tid; rr < Jt; rr += nt) {
+        const int f = rr >= m.J, jr = f ? rr - m.J : rr;
+        const int b = f ? ctl.bj : ctl.bi;
+        const int32_t *k = f ? ctl.kj : ctl.ki;
+        const int e = b * m.J + jr;
+        const double w = m.Rv_w[e];
+        if (w == 0.0) continue;
+        double po = 1.0, pn = 1.0;
+        int64_t ms[8];
+        for (int mm = 0; mm < m.mo; ++mm) {
+            const int em = e * m.mo + mm;
+            const int64_t s = site_at(m, k, m.Rv_uo + 3 * em, m.Rv_b[em]);
+            ms[mm] = s;
+            if (!m.Rv_m[em]) continue;
+            int so = sig[s], sn = so;
+            // flip 0: i -> ssj ; flip 1 (f = 1) evaluated on the configuration after flip 0
+            if (f == 0) { if (s == ctl.si) sn = ctl.ssj; }
+            else {
+                if (s == ctl.si) { so = ctl.ssj; sn = ctl.ssj; }
+                if (s == ctl.sj) sn = ctl.ssi;
+            }
+            const int M = m.Mb[m.Rv_b[em]], pi = m.Rv_p[em];
+            const double *th = m.theta + ((size_t)M * m.maxP + pi) * m.maxM;
+            po *= th[so]; pn *= th[sn];
+        }
+        const double val = (pn - po) * w;
+        if (val == 0.0) continue;
+        const long long fx = llrint(val * kFix);
+        const int ch = m.Rv_col[e] + 1;
+        for (int mm = 0; mm < m.mo; ++mm) {
+            if (!m.Rv_m[e * m.mo + mm]) continue;
+            const int p = slot[ms[mm]];
+            if (p < 0 || p >= n0) { atomicOr(jb.err, 8); continue; }
+            atomicAdd(&dh[(size_t)p * m.C0 + ch], (unsigned long long)fx);
+        }
+    }
+    __syncthreads();
+    float *nb0 = level_buf(jb, nb, 0);
+    for (int idx = tid; idx < n0 * m.C0; idx += nt) {
+        const int p = idx / m.C0, c = idx % m.C0;
+        const int64_t s = list[p];
+        nb0[idx] = h0[(size_t)s * m.C0 + c] + (float)((double)(long long)dh[idx] * kInvFix);
+    }
+    __syncthreads();
+    // 4. layers
+    for (int lvl = 0; lvl < L; ++lvl) {
+        const int Cin = lvl == 0 ? m.C0 : m.D;
+        const float *cache = lvl == 0 ? h0 : jb.hmid + ((size_t)(lvl - 1) * jb.R + r) * N * m.D;
+        const float *newl = level_buf(jb, nb, lvl);
+        const int nout = ctl.nl[lvl + 1];
+        if (lvl + 1 < L) {
+            float *outb = level_buf(jb, nb, lvl + 1);
+            const int D = m.D;
+            layer_tiles(jb, lvl, cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
+                        [&](int64_t pos, int ng, const float *o, int ncol) {
+                            if (pos < 0) return;
+                            for (int jj = 0; jj < ncol; ++jj) outb[(size_t)pos * D + ng + 16 * jj] = o[jj];
+                        });
+        } else {
+            const int D = m.D;
+            layer_tiles(jb, lvl, cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
+                        [&](int64_t pos, int ng, const float *o, int ncol) {
+                            float part = 0.f;
+                            if (pos >= 0) for (int jj = 0; jj < ncol; ++jj) part = fmaf(o[jj], __ldg(m.head_w + ng + 16 * jj), part);
+                            part = row16_sum(part);
+                            if (pos >= 0 && ng == 0) {
+                                const int64_t s = list[pos];
+                                // h0 (patched) . lin
+                                float l0 = 0.f;
+                                const int p0 = slot[s];
+                                const float *hr = (p0 >= 0 && p0 < n0) ? nb0 + (size_t)p0 * m.C0 : h0 + (size_t)s * m.C0;
+                                for (int c = 0; c < m.C0; ++c) l0 = fmaf(hr[c], __ldg(m.lin + c), l0);
+                                const bool active = m.Mb[s % m.nB] > 1;
+                                const float ev = active ? l0 + part : 0.f;
+                                en[pos] = ev;
+                                atomicAdd(&ctl.dacc, (unsigned long long)llrint(((double)ev - (double)e[s]) * kFix));
+                            }
+                            (void)D;
+                        });
+        }
+    }
+    if (L == 0) {
+        for (int p = tid; p < n0; p += nt) {
+            const int64_t s = list[p];
+            float l0 = 0.f;
+            for (int c = 0; c < m.C0; ++c) l0 = fmaf(nb0[(size_t)p * m.C0 + c], __ldg(m.lin + c), l0);
+            const float ev = m.Mb[s % m.nB] > 1 ? l0 : 0.f;
+            en[p] = ev;
+            atomicAdd(&ctl.dacc, (unsigned long long)llrint(((double)ev - (double)e[s]) * kFix));
+        }
+    }
+    __syncthreads();
+    // 5. accept
+    __shared__ int acc_flag;
+    if (tid == 0) {
+        const double dE = (double)(long long)ctl.dacc * kInvFix / m.norm;
+        const double dEeV = dE * m.scale_eV;
+        const double beta = (double)jb.beta_slot[t];
+        int a;
+        if (jb.force > 0) a = 1;
+        else if (jb.force < 0) a = 0;
+        else a = (dEeV <= 0.0) || (ctl.u < exp(-beta * dEeV));
+        acc_flag = a;
+        if (jb.dE_out) jb.dE_out[s_idx * jb.R + t] = dE;
+        if (a) { sig[ctl.si] = (int8_t)ctl.ssj; sig[ctl.sj] = (int8_t)ctl.ssi; E += dE; ++nacc; }
+    }
+    __syncthreads();
+    const int nL = ctl.nl[L];
+    if (acc_flag) {
+        for (int idx = tid; idx < n0 * m.C0; idx += nt) {
+            const int p = idx / m.C0, c = idx % m.C0;
+            h0[(size_t)list[p] * m.C0 + c] = nb0[idx];
+        }
+        for (int lvl = 1; lvl < L; ++lvl) {
+            float *hm = jb.hmid + ((size_t)(lvl - 1) * jb.R + r) * N * m.D;
+            const float *src = level_buf(jb, nb, lvl);
+            const int nl = ctl.nl[lvl];
+            for (int idx = tid; idx < nl * m.D; idx += nt) {
+                const int p = idx / m.D, c = idx % m.D;
+                hm[(size_t)list[p] * m.D + c] = src[idx];
+            }
+        }
+        for (int p = tid; p < nL; p += nt) e[list[p]] = en[p];
+    }
+    for (int p = tid; p < nL; p += nt) slot[list[p]] = -1;
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) nce_chunk_kernel(const __grid_constant__ NceJob jb) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ NceCtl ctl;
+    const int r = blockIdx.x;
+    if (r >= jb.R) return;
+    unsigned long long *dh = reinterpret_cast<unsigned long long *>(smem);
+    float *X = reinterpret_cast<float *>(smem + sizeof(unsigned long long) * (size_t)jb.m.n0max * jb.m.C0);
+    int32_t *src = reinterpret_cast<int32_t *>(X + (size_t)kTM * (1 + jb.m.P) * max(jb.m.C0, jb.m.D));
+    const int t = jb.slot_of_rep[r];
+    double E = jb.E[r];
+    int64_t nacc = 0;
+    for (int64_t s = 0; s < jb.n_steps; ++s) {
+        nce_step(jb, r, t, s, ctl, dh, X, src, E, nacc);
+        if (threadIdx.x == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
+            jb.E_samples[((s + 1) / jb.sample_interval - 1) * jb.R + t] = E;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { jb.E[r] = E; jb.n_acc[r] += nacc; }
+}
+
+// ── full cache ─────────────────────────────────────────────────────────────────────────────────────
+// h0 by pulling every reverse row of each site (deterministic), standardised, float32
+__global__ void nce_h0_kernel(NceDev m, const int8_t *sigma, int32_t R, float *h0) {
+    const int64_t total = (int64_t)R * m.N;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = idx / m.N, s = idx % m.N;
+        const int8_t *sig = sigma + r * m.N;
+        int32_t b, k[3]; coords(m, s, b, k);
+        float *out = h0 + (size_t)idx * m.C0;
+        const bool active = m.Mb[b] > 1;
+        double acc[64];
+        for (int c = 0; c < m.C0; ++c) acc[c] = 0.0;
+        for (int jr = 0; jr < m.J; ++jr) {
+            const int e = b * m.J + jr;
+            const double w = m.Rv_w[e];
+            if (w == 0.0) continue;
+            double pr = 1.0;
+            for (int mm = 0; mm < m.mo; ++mm) {
+                const int em = e * m.mo + mm;
+                if (!m.Rv_m[em]) continue;
+                const int64_t q = site_at(m, k, m.Rv_uo + 3 * em, m.Rv_b[em]);
+                const double *th = m.theta + ((size_t)m.Mb[m.Rv_b[em]] * m.maxP + m.Rv_p[em]) * m.maxM;
+                pr *= th[sig[q]];
+            }
+            acc[m.Rv_col[e] + 1] += pr * w;      // Rv_w already carries 1/sd of the column
+        }
+        if (!active) { for (int c = 0; c < m.C0; ++c) out[c] = 0.f; continue; }
+        // channel 0: the active indicator, standardised; columns: standardised sums (mu/sd folded: acc already / sd)
+        out[0] = (float)((1.0 - (double)m.mu[0]) / (double)m.sd[0]);
+        for (int c = 1; c < m.C0; ++c) out[c] = (float)(acc[c] - (double)m.mu[c] / (double)m.sd[c]);
+    }
+}
+
+// one layer on all sites: out = layer(in); e accumulation on the last layer
+__global__ void __launch_bounds__(256) nce_layer_all_kernel(NceJob jb, int lvl, int32_t r, const float *in, float *out,
+                                                             float *e_out, int64_t chunk0, int64_t chunk_n) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float *X = reinterpret_cast<float *>(smem);
+    int32_t *src = reinterpret_cast<int32_t *>(X + (size_t)kTM * (1 + jb.m.P) * max(jb.m.C0, jb.m.D));
+    const NceDev &m = jb.m;
+    const int64_t per = (chunk_n + gridDim.x - 1) / gridDim.x;
+    const int64_t a = chunk0 + (int64_t)blockIdx.x * per, cnt = max((int64_t)0, min(per, chunk0 + chunk_n - a));
+    if (cnt <= 0) return;
+    const float *h0 = jb.h0 + (size_t)r * m.N * m.C0;
+    const int D = m.D;
+    if (out) {
+        layer_tiles(jb, lvl, in, nullptr, nullptr, 0, nullptr, 0, cnt, &a, X, src, [&](int64_t pos, int ng, const float *o, int ncol) {
+            if (pos < 0) return;
+            for (int jj = 0; jj < ncol; ++jj) out[(size_t)(a + pos) * D + ng + 16 * jj] = o[jj];
+        });
+    } else {
+        layer_tiles(jb, lvl, in, nullptr, nullptr, 0, nullptr, 0, cnt, &a, X, src, [&](int64_t pos, int ng, const float *o, int ncol) {
+            float part = 0.f;
+            if (pos >= 0) for (int jj = 0; jj < ncol; ++jj) part = fmaf(o[jj], __ldg(m.head_w + ng + 16 * jj), part);
+            part = row16_sum(part);
+            if (pos >= 0 && ng == 0) {
+                const int64_t s = a + pos;
+                float l0 = 0.f;
+                for (int c = 0; c < m.C0; ++c) l0 = fmaf(h0[(size_t)s * m.C0 + c], __ldg(m.lin + c), l0);
+                e_out[s] = (m.Mb[s % m.nB] > 1) ? l0 + part : 0.f;
+            }
+        });
+    }
+}
+
+__global__ void nce_e0_kernel(NceDev m, const float *h0, int64_t n, float *e) {
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t site = s % m.N;
+        float l0 = 0.f;
+        for (int c = 0; c < m.C0; ++c) l0 = fmaf(h0[(size_t)s * m.C0 + c], __ldg(m.lin + c), l0);
+        e[s] = m.Mb[site % m.nB] > 1 ? l0 : 0.f;
+    }
+}
+
+// E[r] = sum_s e[r, s] / norm + head_b, fixed point (order independent)
+__global__ void nce_energy_kernel(NceDev m, const float *e, int32_t R, double *E, unsigned long long *acc) {
+    const int r = blockIdx.y;
+    unsigned long long local = 0ull;
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m.N; s += (int64_t)gridDim.x * blockDim.x)
+        local += (unsigned long long)llrint((double)e[(size_t)r * m.N + s] * kFix);
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&acc[r], local);
+}
+
+__global__ void nce_energy_finish(NceDev m, const unsigned long long *acc, int32_t R, double *E) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < R) E[r] = (double)(long long)acc[r] * kInvFix / m.norm + (double)m.head_b;
+}
+
+}  // namespace nce
+
+// ───────────────────────────── host side ──────────────────────────────────────────────────────
+
+struct nce_nce_model {
+    nce::NceDev dev;
+    std::vector<void *> allocs;
+    std::mutex mu;
+    int32_t *err = nullptr;
+    // scratch for R replicas
+    int32_t *slot = nullptr, *list = nullptr; float *newbuf = nullptr, *e_new = nullptr; int64_t stride = 0; int32_t R_alloc = 0;
+    unsigned long long *eacc = nullptr; int32_t eacc_n = 0;
+};
+
+namespace nce {
+
+template <typename T>
+static int dup(nce_nce_model *h, const T *src, size_t n, const T *&dst) {
+    dst = nullptr;
+    if (!n || !src) return NCE_OK;
+    void *p = nullptr;
+    NCE_CUDA(cudaMalloc(&p, sizeof(T) * n));
+    h->allocs.push_back(p);
+    NCE_CUDA(cudaMemcpy(p, src, sizeof(T) * n, cudaMemcpyHostToDevice));
+    dst = (const T *)p;
+    return NCE_OK;
+}
+
+static size_t tile_smem(const NceDev &m) {
+    const int Kin = (1 + m.P) * std::max(m.C0, m.D);
+    return sizeof(float) * (size_t)kTM * Kin + sizeof(int32_t) * (size_t)kTM * (1 + m.P * m.W);
+}
+
+static size_t step_smem(const NceDev &m) {
+    return sizeof(unsigned long long) * (size_t)m.n0max * m.C0 + tile_smem(m);
+}
+
+static int ensure_scratch(nce_nce_model *h, int32_t R) {
+    if (h->R_alloc >= R) return NCE_OK;
+    for (void *p : {(void *)h->slot, (void *)h->list, (void *)h->newbuf, (void *)h->e_new}) if (p) cudaFree(p);
+    const NceDev &m = h->dev;
+    h->stride = (int64_t)m.n0max * m.C0 + (int64_t)std::max(0, m.depth - 1) * m.nmax * m.D;
+    NCE_CUDA(cudaMalloc((void **)&h->slot, sizeof(int32_t) * (size_t)R * m.N));
+    NCE_CUDA(cudaMemset(h->slot, 0xFF, sizeof(int32_t) * (size_t)R * m.N));
+    NCE_CUDA(cudaMalloc((void **)&h->list, sizeof(int32_t) * (size_t)R * m.nmax));
+    NCE_CUDA(cudaMalloc((void **)&h->newbuf, sizeof(float) * (size_t)R * std::max<int64_t>(h->stride, 1)));
+    NCE_CUDA(cudaMalloc((void **)&h->e_new, sizeof(float) * (size_t)R * m.nmax));
+    h->R_alloc = R;
+    return NCE_OK;
+}
+
+static NceJob make_nce_job(nce_nce_model *h, const nce_nce_state *st) {
+    NceJob j; std::memset(&j, 0, sizeof(j));
+    j.m = h->dev;
+    j.sigma = st->sigma; j.h0 = st->h0; j.hmid = st->hmid; j.e = st->e; j.E = st->E; j.beta_slot = st->beta_slot;
+    j.slot_of_rep = st->slot_of_rep; j.n_acc = st->n_acc; j.R = st->R;
+    j.slot = h->slot; j.list = h->list; j.newbuf = h->newbuf; j.e_new = h->e_new; j.scratch_stride = h->stride;
+    j.err = h->err; j.sample_interval = 1;
+    return j;
+}
+
+}  // namespace nce
+
+using namespace nce;
+
+extern "C" {
+
+int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
+    NCE_CHECK(d && out, "nce_nce_create: null argument");
+    NCE_CHECK(d->depth >= 0 && d->depth <= kMaxLayers, "nce_nce_create: depth must be 0..%d", kMaxLayers);
+    NCE_CHECK(d->C0 >= 1 && d->C0 <= 64, "nce_nce_create: layer-0 channels must be 1..64");
+    NCE_CHECK(d->depth == 0 || (d->D % 16 == 0 && d->D >= 16 && d->D <= 128), "nce_nce_create: width must be 16..128, multiple of 16");
+    NCE_CHECK(d->mo >= 1 && d->mo <= 8 && d->P >= 1 && d->P <= 8 && d->W >= 1, "nce_nce_create: mo/P/W out of range");
+    NCE_CHECK(d->nB >= 1 && d->J >= 1 && d->n_cells == d->d[0] * d->d[1] * d->d[2] && d->n_cells <= 0xFFFFFFFFll,
+              "nce_nce_create: bad lattice");
+    NCE_CHECK(d->act == 0 || d->act == 1, "nce_nce_create: act must be 0 (tanh) or 1 (silu)");
+    NCE_CHECK(d->norm > 0.0, "nce_nce_create: norm must be > 0");
+    const int64_t N = d->n_cells * d->nB;
+    NCE_CHECK(N < (1ll << 31) - 1, "nce_nce_create: more than 2^31 sites");
+    NCE_CHECK(d->n_groups >= 1 && d->max_gb >= 1 && d->act_b && d->act_nb && d->grp_cum, "nce_nce_create: no swap group");
+    for (int g = 0; g < d->n_groups; ++g) {
+        NCE_CHECK(d->act_nb[g] >= 1 && d->act_nb[g] <= d->max_gb, "nce_nce_create: act_nb out of range");
+        for (int q = 0; q < d->act_nb[g]; ++q)
+            NCE_CHECK(d->act_b[g * d->max_gb + q] >= 0 && d->act_b[g * d->max_gb + q] < d->nB, "nce_nce_create: act_b out of range");
+    }
+    NCE_CHECK(d->maxM >= 1 && d->maxP >= 1, "nce_nce_create: maxM/maxP must be >= 1");
+    for (int b = 0; b < d->nB; ++b) NCE_CHECK(d->Mb[b] >= 1 && d->Mb[b] <= d->maxM, "nce_nce_create: Mb out of range");
+    // host-side range checks of every table index
+    const size_t nr = (size_t)d->nB * d->J * d->mo;
+    for (size_t i = 0; i < nr; ++i) {
+        NCE_CHECK(d->Rv_b[i] >= 0 && d->Rv_b[i] < d->nB && d->Rv_p[i] >= 0 && d->Rv_p[i] < d->maxP, "nce_nce_create: Rv_b/Rv_p out of range");
+        NCE_CHECK(d->Mb[d->Rv_b[i]] >= 1 && d->Mb[d->Rv_b[i]] <= d->maxM, "nce_nce_create: Mb out of range");
+        for (int c = 0; c < 3; ++c) NCE_CHECK(d->Rv_uo[3 * i + c] >= 0 && d->Rv_uo[3 * i + c] < d->d[c], "nce_nce_create: Rv_uo out of [0,d)");
+    }
+    for (size_t i = 0; i < (size_t)d->nB * d->J; ++i)
+        NCE_CHECK(d->Rv_col[i] >= 0 && d->Rv_col[i] + 1 < d->C0, "nce_nce_create: Rv_col out of range");
+    const size_t ns = (size_t)d->nB * d->P * d->W;
+    for (size_t i = 0; i < ns; ++i) {
+        NCE_CHECK(d->Sh_b[i] >= 0 && d->Sh_b[i] < d->nB, "nce_nce_create: Sh_b out of range");
+        for (int c = 0; c < 3; ++c) NCE_CHECK(d->Sh_uo[3 * i + c] >= 0 && d->Sh_uo[3 * i + c] < d->d[c], "nce_nce_create: Sh_uo out of [0,d)");
+    }
+    const size_t nbl = (size_t)d->nB * d->wL;
+    for (size_t i = 0; i < nbl; ++i) {
+        NCE_CHECK(d->ball_b[i] >= 0 && d->ball_b[i] < d->nB, "nce_nce_create: ball_b out of range");
+        for (int c = 0; c < 3; ++c) NCE_CHECK(d->ball_uo[3 * i + c] >= 0 && d->ball_uo[3 * i + c] < d->d[c], "nce_nce_create: ball_uo out of [0,d)");
+    }
+    int n0max = 0, nLmax = 0;
+    for (int b = 0; b < d->nB; ++b) {
+        for (int l = 0; l <= d->depth; ++l) {
+            const int e1 = d->ball_end[b * (d->depth + 1) + l], e0 = l ? d->ball_end[b * (d->depth + 1) + l - 1] : 0;
+            NCE_CHECK(e0 <= e1 && e1 <= d->wL, "nce_nce_create: ball_end not monotone within [0, wL]");
+        }
+        n0max = std::max(n0max, d->ball_end[b * (d->depth + 1)]);
+        nLmax = std::max(nLmax, d->ball_end[b * (d->depth + 1) + d->depth]);
+    }
+    nce_nce_model *h = new nce_nce_model();
+    NceDev &m = h->dev;
+    std::memset(&m, 0, sizeof(m));
+    m.nB = d->nB; m.J = d->J; m.mo = d->mo; m.P = d->P; m.W = d->W; m.depth = d->depth; m.C0 = d->C0; m.D = d->D;
+    m.maxM = d->maxM; m.maxP = d->maxP; m.d0 = (int32_t)d->d[0]; m.d1 = (int32_t)d->d[1]; m.d2 = (int32_t)d->d[2];
+    m.N = N; m.n_cells = d->n_cells; m.wL = d->wL; m.act = d->act; m.gate = d->gate; m.norm = d->norm; m.scale_eV = d->scale_eV;
+    m.head_b = (float)d->head_b;
+    m.n0max = 2 * n0max; m.nmax = 2 * nLmax;
+    int rc = NCE_OK;
+    auto chk = [&](int x) { if (!rc) rc = x; };
+    chk(dup(h, d->Rv_b, nr, m.Rv_b)); chk(dup(h, d->Rv_uo, nr * 3, m.Rv_uo)); chk(dup(h, d->Rv_p, nr, m.Rv_p));
+    chk(dup(h, d->Rv_m, nr, m.Rv_m)); chk(dup(h, d->Rv_col, (size_t)d->nB * d->J, m.Rv_col)); chk(dup(h, d->Rv_w, (size_t)d->nB * d->J, m.Rv_w));
+    chk(dup(h, d->Mb, (size_t)d->nB, m.Mb)); chk(dup(h, d->theta, (size_t)(d->maxM + 1) * d->maxP * d->maxM, m.theta));
+    chk(dup(h, d->Sh_b, ns, m.Sh_b)); chk(dup(h, d->Sh_uo, ns * 3, m.Sh_uo)); chk(dup(h, d->Sh_m, ns, m.Sh_m));
+    chk(dup(h, d->Sh_inv, (size_t)d->nB * d->P, m.Sh_inv));
+    chk(dup(h, d->ball_b, nbl, m.ball_b)); chk(dup(h, d->ball_uo, nbl * 3, m.ball_uo));
+    chk(dup(h, d->ball_end, (size_t)d->nB * (d->depth + 1), m.ball_end));
+    chk(dup(h, d->lin, (size_t)d->C0, m.lin)); chk(dup(h, d->head_w, (size_t)std::max(d->D, 1), m.head_w));
+    chk(dup(h, d->mu, (size_t)d->C0, m.mu)); chk(dup(h, d->sd, (size_t)d->C0, m.sd));
+    m.n_groups = d->n_groups; m.max_gb = d->max_gb;
+    chk(dup(h, d->act_b, (size_t)d->n_groups * d->max_gb, m.act_b)); chk(dup(h, d->act_nb, (size_t)d->n_groups, m.act_nb));
+    chk(dup(h, d->grp_cum, (size_t)d->n_groups, m.grp_cum));
+    for (int l = 0; l < d->depth; ++l) {
+        const int Cin = l == 0 ? d->C0 : d->D;
+        chk(dup(h, d->W_cat[l], (size_t)(1 + d->P) * Cin * d->D, m.Wc[l]));
+        chk(dup(h, d->bias[l], (size_t)d->D, m.bias[l]));
+        if (d->gate) { chk(dup(h, d->G_cat[l], (size_t)d->P * Cin * d->D, m.G[l])); chk(dup(h, d->gate_b[l], (size_t)d->D, m.gb[l])); }
+    }
+    if (!rc) {
+        cudaError_t e = cudaMalloc((void **)&h->err, sizeof(int32_t));
+        if (e == cudaSuccess) e = cudaMemset(h->err, 0, sizeof(int32_t));
+        if (e != cudaSuccess) rc = fail(NCE_ERR_CUDA, "nce_nce_create: %s", cudaGetErrorString(e));
+    }
+    if (!rc && step_smem(m) > 220 * 1024) rc = fail(NCE_ERR_UNSUPPORTED, "nce_nce_create: receptive field too large for shared memory");
+    if (rc) {
+        for (void *p : h->allocs) cudaFree(p);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return NCE_OK;
+}
+
+int nce_nce_destroy(nce_nce_handle h) {
+    if (!h) return NCE_OK;
+    cudaDeviceSynchronize();
+    for (void *p : h->allocs) cudaFree(p);
+    for (void *p : {(void *)h->slot, (void *)h->list, (void *)h->newbuf, (void *)h->e_new, (void *)h->err, (void *)h->eacc}) if (p) cudaFree(p);
+    delete h;
+    return NCE_OK;
+}
+
+int nce_nce_full_cache(nce_nce_handle h, const nce_nce_state *st, void *stream) {
+    NCE_CHECK(h && st && st->sigma && st->h0 && st->e && st->E && st->R >= 1, "nce_nce_full_cache: bad argument");
+    NCE_CHECK(st->N == h->dev.N, "nce_nce_full_cache: N mismatch");
+    NCE_CHECK(h->dev.depth < 2 || st->hmid, "nce_nce_full_cache: hmid required for depth >= 2");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaStream_t s = (cudaStream_t)stream;
+    const NceDev &m = h->dev;
+    const int64_t tot = (int64_t)st->R * m.N;
+    nce_h0_kernel<<<(int)std::min<int64_t>((tot + 127) / 128, 65535), 128, 0, s>>>(m, st->sigma, st->R, st->h0);
+    NCE_CUDA(cudaGetLastError());
+    NceJob jb = make_nce_job(h, st);
+    const size_t xs = tile_smem(m);
+    NCE_CUDA(cudaFuncSetAttribute(nce_layer_all_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
+    const int blocks = (int)std::min<int64_t>((m.N + kTM - 1) / kTM, 1216);
+    if (m.depth == 0) {
+        nce_e0_kernel<<<(int)std::min<int64_t>((tot + 255) / 256, 65535), 256, 0, s>>>(m, st->h0, tot, st->e);
+        NCE_CUDA(cudaGetLastError());
+    }
+    // hidden layers: hmid[l-1] for l = 1..depth-1, then the last layer into e
+    for (int32_t r = 0; r < st->R && m.depth > 0; ++r) {
+        for (int l = 0; l < m.depth; ++l) {
+            const float *in = l == 0 ? st->h0 + (size_t)r * m.N * m.C0 : st->hmid + ((size_t)(l - 1) * st->R + r) * m.N * m.D;
+            if (l + 1 < m.depth) {
+                float *outp = st->hmid + ((size_t)l * st->R + r) * m.N * m.D;
+                nce_layer_all_kernel<<<blocks, 256, xs, s>>>(jb, l, r, in, outp, nullptr, 0, m.N);
+            } else {
+                nce_layer_all_kernel<<<blocks, 256, xs, s>>>(jb, l, r, in, nullptr, st->e + (size_t)r * m.N, 0, m.N);
+            }
+            NCE_CUDA(cudaGetLastError());
+        }
+    }
+    if (h->eacc_n < st->R) {
+        if (h->eacc) { cudaStreamSynchronize(s); cudaFree(h->eacc); }
+        h->eacc = nullptr; h->eacc_n = 0;
+        NCE_CUDA(cudaMalloc((void **)&h->eacc, sizeof(unsigned long long) * st->R));
+        h->eacc_n = st->R;
+    }
+    NCE_CUDA(cudaMemsetAsync(h->eacc, 0, sizeof(unsigned long long) * st->R, s));
+    dim3 g((unsigned)std::min<int64_t>((m.N + 255) / 256, 1024), st->R);
+    nce_energy_kernel<<<g, 256, 0, s>>>(m, st->e, st->R, st->E, h->eacc);
+    NCE_CUDA(cudaGetLastError());
+    nce_energy_finish<<<(st->R + 127) / 128, 128, 0, s>>>(m, h->eacc, st->R, st->E);
+    NCE_CUDA(cudaGetLastError());
+    return NCE_OK;
+}
+
+int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_chunk *ck, void *stream) {
+    NCE_CHECK(h && st && ck, "nce_nce_run_chunk: null argument");
+    NCE_CHECK(st->N == h->dev.N && st->R >= 1, "nce_nce_run_chunk: state size mismatch");
+    NCE_CHECK(st->sigma && st->h0 && st->e && st->E && st->beta_slot && st->slot_of_rep && st->n_acc, "nce_nce_run_chunk: null state pointer");
+    NCE_CHECK(h->dev.depth < 2 || st->hmid, "nce_nce_run_chunk: hmid required for depth >= 2");
+    NCE_CHECK((ck->prop_a == nullptr) == (ck->prop_b == nullptr) && (ck->prop_a == nullptr) == (ck->prop_u == nullptr),
+              "nce_nce_run_chunk: prop_a/prop_b/prop_u must be all set or all NULL");
+    NCE_CHECK(!ck->E_samples || ck->sample_interval > 0, "nce_nce_run_chunk: sample_interval must be > 0");
+    NCE_CHECK(ck->n_steps >= 0 && ck->force >= -1 && ck->force <= 1, "nce_nce_run_chunk: bad n_steps/force");
+    std::lock_guard<std::mutex> lk(h->mu);
+    int rc = ensure_scratch(h, st->R); if (rc) return rc;
+    NceJob jb = make_nce_job(h, st);
+    jb.n_steps = ck->n_steps; jb.step0 = ck->step0; jb.prop_a = ck->prop_a; jb.prop_b = ck->prop_b; jb.prop_u = ck->prop_u;
+    jb.seed = ck->seed; jb.sample_interval = ck->sample_interval > 0 ? ck->sample_interval : 1; jb.E_samples = ck->E_samples;
+    jb.dE_out = ck->dE_out; jb.force = ck->force;
+    if (ck->n_steps == 0) return NCE_OK;
+    const size_t sm = step_smem(h->dev);
+    NCE_CUDA(cudaFuncSetAttribute(nce_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    nce_chunk_kernel<<<st->R, 256, sm, (cudaStream_t)stream>>>(jb);
+    NCE_CUDA(cudaGetLastError());
+    if (ck->exchange_rounds > 0 && st->R > 1) {
+        NCE_CHECK(st->rep_of_slot && st->ladder_id && st->n_ex, "nce_nce_run_chunk: exchange needs rep_of_slot/ladder_id/n_ex");
+        rc = launch_exchange(st->R, st->E, h->dev.scale_eV, st->beta_slot, st->rep_of_slot, st->slot_of_rep, st->ladder_id,
+                             st->n_ex, ck->seed, ck->step0 + ck->n_steps, ck->ex_parity, ck->ex_u, ck->exchange_rounds,
+                             (cudaStream_t)stream);
+        if (rc) return rc;
+    }
+    return NCE_OK;
+}
+
+int nce_nce_errors(nce_nce_handle h, int32_t *flags) {
+    NCE_CHECK(h && flags, "nce_nce_errors: null argument");
+    NCE_CUDA(cudaMemcpy(flags, h->err, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    NCE_CUDA(cudaMemset(h->err, 0, sizeof(int32_t)));
+    return NCE_OK;
+}
+
+}  // extern "C"
