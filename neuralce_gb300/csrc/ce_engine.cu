@@ -858,6 +858,69 @@ int nce_ce_run_chunk_host(nce_ce_handle h, int32_t R, int8_t *sigma_host, double
     return NCE_OK;
 }
 
+}  // extern "C"
+
+// ── full energy without any allocation ─────────────────────────────────────────────────────────────
+// Some callers cannot allocate device memory once they are running: a process whose device memory is all
+// reserved up front by its own pool (so a library cudaMalloc would fail or fragment it), or a latency-bound
+// loop where cudaMalloc/cudaFree would add an implicit device synchronisation.  nce_ce_energy_noalloc serves
+// them: the per-block float64 partials of ce_energy_kernel live in the fixed array below, which the CUDA driver
+// places in device memory with the rest of this library's image on each device the library is used on, and
+// which stays there until the process exits.  Every call on a device shares this one array; calls that overlap
+// on the GPU (two streams at once) race on it.  Each launch writes every partial it later reads, so nothing
+// has to be cleared between calls.
+namespace nce {
+constexpr int64_t kNoAllocPartials = 65536;                                    // 512 KiB of float64 partials
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocPartials];
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_ptr[256];                                             // per device ordinal
+
+// Device address of the array on the current device (host code must not use the symbol itself as a pointer).
+static int noalloc_partials(double **out) {
+    int dev = 0;
+    NCE_CUDA(cudaGetDevice(&dev));
+    NCE_CHECK(dev >= 0 && dev < 256, "nce_ce_energy_noalloc: device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        NCE_CUDA(cudaGetSymbolAddress(&p, g_noalloc_partials));
+        g_noalloc_ptr[dev] = (double *)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return NCE_OK;
+}
+}  // namespace nce
+
+extern "C" {
+
+int nce_ce_energy_noalloc(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t precision, double *E, void *stream) {
+    NCE_CHECK(h && sigma && E && R >= 1, "nce_ce_energy_noalloc: bad argument");
+    NCE_CHECK(precision == 64 || precision == 32, "nce_ce_energy_noalloc: precision must be 64 or 32");
+    NCE_CHECK(R <= kNoAllocPartials, "nce_ce_energy_noalloc: %d configurations exceed the limit of %lld per call", R,
+              (long long)kNoAllocPartials);
+    double *partial = nullptr;
+    int rc = noalloc_partials(&partial);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int threads = 256;
+    // same blocks per configuration as nce_ce_energy, reduced so that R x blocks fits the fixed array
+    int64_t nblk = std::min<int64_t>((h->n_cells + threads - 1) / threads, 1184);
+    nblk = std::max<int64_t>(1, std::min<int64_t>(nblk, kNoAllocPartials / R));
+    dim3 grid((unsigned)nblk, R);
+    if (precision == 64)
+        ce_energy_kernel<double><<<grid, threads, 0, s>>>(sigma, h->N, h->n_cells, h->nB, (int)h->d[0], (int)h->d[1], (int)h->d[2],
+                                                          h->Rt, h->mo, h->T_b, h->T_uo, h->T_pfc, h->T_eci64, h->pf64, h->max_sp,
+                                                          partial);
+    else
+        ce_energy_kernel<float><<<grid, threads, 0, s>>>(sigma, h->N, h->n_cells, h->nB, (int)h->d[0], (int)h->d[1], (int)h->d[2],
+                                                         h->Rt, h->mo, h->T_b, h->T_uo, h->T_pfc, h->T_eci32, h->pf32, h->max_sp,
+                                                         partial);
+    NCE_CUDA(cudaGetLastError());
+    ce_energy_finish<<<(R + 127) / 128, 128, 0, s>>>(partial, (int32_t)nblk, R, h->zerolet, E);
+    NCE_CUDA(cudaGetLastError());
+    return NCE_OK;
+}
+
 int nce_ce_errors(nce_ce_handle h, int32_t *flags) {
     NCE_CHECK(h && flags, "nce_ce_errors: null argument");
     NCE_CUDA(cudaMemcpy(flags, h->err, sizeof(int32_t), cudaMemcpyDeviceToHost));
