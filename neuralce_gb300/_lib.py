@@ -36,6 +36,28 @@ class NcePtChunk(C.Structure):
                 ("ex_u", vp), ("precision", i32), ("warps", i32)]
 
 
+class NceNceDesc(C.Structure):
+    _fields_ = [("nB", i32), ("J", i32), ("mo", i32), ("P", i32), ("W", i32), ("depth", i32), ("C0", i32), ("D", i32),
+                ("maxM", i32), ("maxP", i32), ("wL", i32), ("d", i64 * 3), ("n_cells", i64),
+                ("Rv_b", vp), ("Rv_uo", vp), ("Rv_p", vp), ("Rv_col", vp), ("Rv_m", vp), ("Rv_w", vp),
+                ("Mb", vp), ("theta", vp), ("Sh_b", vp), ("Sh_uo", vp), ("Sh_m", vp), ("Sh_inv", vp),
+                ("ball_b", vp), ("ball_uo", vp), ("ball_end", vp), ("lin", vp), ("head_w", vp), ("head_b", f64),
+                ("W_cat", vp * 4), ("bias", vp * 4), ("G_cat", vp * 4), ("gate_b", vp * 4), ("mu", vp), ("sd", vp),
+                ("act", i32), ("gate", i32), ("norm", f64), ("scale_eV", f64),
+                ("n_groups", i32), ("max_gb", i32), ("act_b", vp), ("act_nb", vp), ("grp_cum", vp)]
+
+
+class NceNceState(C.Structure):
+    _fields_ = [("R", i32), ("N", i64), ("sigma", vp), ("h0", vp), ("hmid", vp), ("e", vp), ("E", vp),
+                ("beta_slot", vp), ("rep_of_slot", vp), ("slot_of_rep", vp), ("ladder_id", vp), ("n_acc", vp), ("n_ex", vp)]
+
+
+class NceNceChunk(C.Structure):
+    _fields_ = [("n_steps", i64), ("step0", i64), ("prop_a", vp), ("prop_b", vp), ("prop_u", vp), ("seed", u64),
+                ("sample_interval", i64), ("E_samples", vp), ("dE_out", vp), ("force", i32), ("exchange_rounds", i32),
+                ("ex_parity", i32), ("ex_u", vp)]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -52,6 +74,11 @@ SIGNATURES = {
     "nce_ce_errors": (i32, [vp, P(i32)]),
     "nce_pt_minimum": (i32, [P(NcePtState), vp, vp, vp]),
     "nce_philox4x32": (None, [P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)]),
+    "nce_nce_create": (i32, [P(NceNceDesc), P(vp)]),
+    "nce_nce_destroy": (i32, [vp]),
+    "nce_nce_full_cache": (i32, [vp, P(NceNceState), vp]),
+    "nce_nce_run_chunk": (i32, [vp, P(NceNceState), P(NceNceChunk), vp]),
+    "nce_nce_errors": (i32, [vp, P(i32)]),
 }
 
 

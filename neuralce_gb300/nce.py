@@ -1,0 +1,239 @@
+"""NeuralCE on the GB300 engine: ``load_model`` / ``setup(mdl, atoms)`` and the device PT state.
+
+Mirrors ``neuralce/nce/mc_model.py``: ``load_model`` (``:20-21``), ``expand_params`` (``:36-57``: zero rows for the
+layer-0 channels the model dropped), ``setup`` / ``setup_implicit`` (``:60-111,175-228``) returning a dict with
+``energy``, ``full_cache``, ``local_delta``-style stepping, ``perm`` / ``inv_perm``, ``to_eV_per_atom`` and
+``dE_eV_total``.  The receptive-field update runs in libnce_gb300 (``nce_nce_run_chunk``); geometry comes from
+``nce_geometry.build_geometry``.
+
+Two network families share the engine:
+  * model.pkl networks (tanh, optional sigmoid gate, site-mean readout, eV via ys/ym) -- the reference's;
+  * the benchmark network (``synthetic_model``): depth 3, width 64, SiLU, sum readout, one 12-neighbour shell,
+    weights ~ N(0, 1/fan_in) from a seed, energies directly in eV.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .ce_tables import ClusterSpace
+from .io import Structure, load_model  # noqa: F401  (re-exported, reference name)
+from .nce_geometry import build_geometry
+
+
+def expand_params(mdl, seed_idx=0):
+    """model.pkl parameters on the full layer-0 channel list; mu = 0 / sd = 1 on dropped channels."""
+    keep = np.asarray(mdl["keep"]); Kfull = int(mdl["K_chem"])
+    P = mdl["params"][seed_idx]
+    lin = np.zeros(Kfull); lin[keep] = P["lin"]
+    layers = []
+    for L in P["layers"]:
+        if L["self"].shape[0] == len(keep):
+            Lx = dict(L)
+            Lx["self"] = np.zeros((Kfull, L["self"].shape[1])); Lx["self"][keep] = L["self"]
+            Lx["shell"] = np.zeros((L["shell"].shape[0], Kfull, L["shell"].shape[2])); Lx["shell"][:, keep] = L["shell"]
+            if "gate" in L:
+                Lx["gate"] = np.zeros((L["gate"].shape[0], Kfull, L["gate"].shape[2])); Lx["gate"][:, keep] = L["gate"]
+            if "shell_max" in L:
+                raise NotImplementedError("shell_max (masked max) layers are not on this engine")
+            layers.append(Lx)
+        else:
+            layers.append(dict(L))
+    mu = np.zeros(Kfull); sd = np.ones(Kfull); mu[keep] = mdl["mu"]; sd[keep] = mdl["sd"]
+    return dict(lin=lin, layers=layers, head=dict(P["head"])), mu, sd
+
+
+def synthetic_model(C0, depth=3, width=64, P=1, seed=0):
+    """Benchmark network: weights and biases ~ N(0, 1/fan_in) from ``seed``."""
+    rng = np.random.default_rng(seed)
+    g = lambda shape, fan: rng.normal(0.0, 1.0 / np.sqrt(fan), shape)
+    layers = []
+    cin = C0
+    for _ in range(depth):
+        layers.append(dict(self=g((cin, width), cin), shell=g((P, cin, width), cin), b=g((width,), cin)))
+        cin = width
+    return dict(lin=g((C0,), C0), layers=layers, head=dict(w=g((width,), width), b=0.0))
+
+
+class NCEModel:
+    """Geometry + parameters of one cell, uploaded to the device (``nce_nce_create``)."""
+
+    def __init__(self, cs, structure, params, mu=None, sd=None, shell_edges=(0.0, 3.3), act="tanh", pool="mean",
+                 ys=1.0, ym=0.0):
+        depth = len(params["layers"])
+        self.cs, self.params, self.act, self.pool = cs, params, act, pool
+        self.geo = geo = build_geometry(cs, structure, list(shell_edges), depth)
+        K1 = geo["K"] + 1
+        self.mu = np.zeros(K1) if mu is None else np.asarray(mu, float)
+        self.sd = np.ones(K1) if sd is None else np.asarray(sd, float)
+        self.ys, self.ym = float(ys), float(ym)
+        self.depth = depth
+        self.N, self.nA = geo["N"], geo["nA"]
+        self.C0 = K1
+        self.D = params["layers"][0]["self"].shape[1] if depth else 16
+        self.norm = float(self.nA) if pool == "mean" else 1.0
+        self.scale_eV = self.ys * self.N if pool == "mean" else 1.0
+        self.perm, self.inv_perm = geo["perm"], geo["inv_perm"]
+        self.sig0 = geo["sig"]
+        self._build_desc()
+        self._handle = None
+
+    def _build_desc(self):
+        g = self.geo; keep = self.keep = {}
+        a = lambda name, x, dt: keep.__setitem__(name, np.ascontiguousarray(np.asarray(x, dt))) or keep[name]
+        nB, J, mo, P, W = g["nB"], g["J"], g["mo"], g["P"], g["W"]
+        a("Rv_b", g["Rv_b"], np.int32); a("Rv_uo", g["Rv_uo"], np.int32); a("Rv_p", g["Rv_p"], np.int32)
+        a("Rv_col", g["Rv_col"], np.int32); a("Rv_m", g["Rv_m"], np.uint8)
+        col = g["Rv_col"]
+        w = np.where(g["Rv_v"], g["nA"] / (g["Rv_ord"] * g["norm"][col] * self.sd[col + 1]), 0.0)
+        a("Rv_w", w, np.float64)
+        a("Mb", g["Mb"], np.int32); th = a("theta", g["theta"], np.float64)
+        a("Sh_b", g["Sh_b"], np.int32); a("Sh_uo", g["Sh_uo"], np.int32); a("Sh_m", g["Sh_m"], np.uint8)
+        a("Sh_inv", 1.0 / np.maximum(g["Sh_m"].sum(-1), 1), np.float32)
+        # receptive-field offsets ordered by the level where they first appear
+        L = self.depth
+        lists, ends = [], []
+        for b in range(nB):
+            seen = set(); order = []; e = []
+            for l in range(L + 1):
+                n = int(g["ball_n"][l][b])
+                for bb, o in zip(g["ball_b"][l][b][:n], g["ball_off"][l][b][:n]):
+                    it = (int(bb), tuple(int(x) for x in o))
+                    if it not in seen:
+                        seen.add(it); order.append(it)
+                e.append(len(order))
+            lists.append(order); ends.append(e)
+        wL = max(len(o) for o in lists)
+        bb_ = np.zeros((nB, wL), np.int32); bo = np.zeros((nB, wL, 3), np.int64)
+        for b in range(nB):
+            bb_[b] = b
+            for q, (x, o) in enumerate(lists[b]):
+                bb_[b, q] = x; bo[b, q] = o
+        U, d = g["U"], g["d"]
+        a("ball_b", bb_, np.int32); a("ball_uo", np.mod(bo @ U.T, d), np.int32); a("ball_end", np.array(ends), np.int32)
+        self.wL = wL
+        p = self.params
+        a("lin", p["lin"], np.float32)
+        a("head_w", p["head"]["w"] if self.depth else np.zeros(16), np.float32)
+        a("mu", self.mu, np.float32); a("sd", self.sd, np.float32)
+        gate = bool(self.depth and "gate" in p["layers"][0])
+        for l, Ly in enumerate(p["layers"]):
+            a(f"W{l}", np.concatenate([Ly["self"]] + [Ly["shell"][q] for q in range(Ly["shell"].shape[0])], axis=0), np.float32)
+            a(f"b{l}", Ly["b"], np.float32)
+            if gate:
+                a(f"G{l}", np.concatenate([Ly["gate"][q] for q in range(Ly["gate"].shape[0])], axis=0), np.float32)
+                a(f"gb{l}", Ly["gb"], np.float32)
+        a("act_b", g["grp_b"], np.int32); nb = a("act_nb", g["grp_nb"], np.int32)
+        cum = np.floor(np.cumsum(nb) / nb.sum() * 2.0 ** 32).astype(np.uint64); cum[-1] = np.uint64(2 ** 32)
+        a("grp_cum", cum, np.uint64)
+        s = _lib.NceNceDesc()
+        s.nB, s.J, s.mo, s.P, s.W, s.depth, s.C0, s.D = nB, J, mo, P, W, self.depth, self.C0, self.D
+        s.maxM, s.maxP = th.shape[0] - 1, th.shape[1]
+        s.wL = wL
+        for c in range(3):
+            s.d[c] = int(d[c])
+        s.n_cells = int(g["n_cells"])
+        for f in ("Rv_b", "Rv_uo", "Rv_p", "Rv_col", "Rv_m", "Rv_w", "Mb", "theta", "Sh_b", "Sh_uo", "Sh_m", "Sh_inv",
+                  "ball_b", "ball_uo", "ball_end", "lin", "head_w", "mu", "sd", "act_b", "act_nb", "grp_cum"):
+            setattr(s, f, keep[f].ctypes.data)
+        s.head_b = float(p["head"]["b"])
+        for l in range(self.depth):
+            s.W_cat[l] = keep[f"W{l}"].ctypes.data; s.bias[l] = keep[f"b{l}"].ctypes.data
+            if gate:
+                s.G_cat[l] = keep[f"G{l}"].ctypes.data; s.gate_b[l] = keep[f"gb{l}"].ctypes.data
+        s.act = 0 if self.act == "tanh" else 1
+        s.gate = int(gate)
+        s.norm = self.norm; s.scale_eV = self.scale_eV
+        s.n_groups, s.max_gb = keep["act_b"].shape
+        self.desc = s
+
+    @property
+    def handle(self):
+        if self._handle is None:
+            h = C.c_void_p()
+            _lib.check(_lib.lib().nce_nce_create(C.byref(self.desc), C.byref(h)), "nce_nce_create")
+            self._handle = h
+        return self._handle
+
+    def close(self):
+        if self._handle is not None:
+            _lib.lib().nce_nce_destroy(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class NCEState:
+    """Device PT state of R replicas (torch buffers) in the C-ABI layout."""
+
+    def __init__(self, model: NCEModel, sigma, beta_slot, ladder_id=None, device="cuda"):
+        import torch
+        R, N = sigma.shape
+        self.R, self.N, self.model = R, N, model
+        f32 = dict(dtype=torch.float32, device=device)
+        self.sigma = torch.as_tensor(np.ascontiguousarray(sigma), dtype=torch.int8).to(device)
+        self.h0 = torch.zeros((R, N, model.C0), **f32)
+        self.hmid = torch.zeros((max(model.depth - 1, 0), R, N, model.D), **f32) if model.depth >= 2 else None
+        self.e = torch.zeros((R, N), **f32)
+        self.E = torch.zeros(R, dtype=torch.float64, device=device)
+        self.beta_slot = torch.as_tensor(np.asarray(beta_slot, np.float32)).to(device)
+        self.rep_of_slot = torch.arange(R, dtype=torch.int32, device=device)
+        self.slot_of_rep = torch.arange(R, dtype=torch.int32, device=device)
+        self.ladder_id = torch.as_tensor(np.zeros(R, np.int32) if ladder_id is None else np.asarray(ladder_id, np.int32)).to(device)
+        self.n_acc = torch.zeros(R, dtype=torch.int64, device=device)
+        self.n_ex = torch.zeros(1, dtype=torch.int64, device=device)
+
+    def struct(self):
+        s = _lib.NceNceState()
+        s.R, s.N = self.R, self.N
+        for f in ("sigma", "h0", "e", "E", "beta_slot", "rep_of_slot", "slot_of_rep", "ladder_id", "n_acc", "n_ex"):
+            setattr(s, f, getattr(self, f).data_ptr())
+        s.hmid = self.hmid.data_ptr() if self.hmid is not None else None
+        return s
+
+    def full_cache(self, stream=None):
+        st = self.struct()
+        _lib.check(_lib.lib().nce_nce_full_cache(self.model.handle, C.byref(st), _lib.stream_ptr(stream)), "nce_nce_full_cache")
+        return self
+
+    def run_chunk(self, n_steps, step0, seed=0, proposals=None, sample_interval=1, E_samples=None, dE_out=None, force=0,
+                  exchange_rounds=0, ex_parity=0, ex_u=None, stream=None):
+        c = _lib.NceNceChunk()
+        c.n_steps, c.step0, c.seed = int(n_steps), int(step0), int(seed) & 0xFFFFFFFFFFFFFFFF
+        if proposals is not None:
+            c.prop_a, c.prop_b, c.prop_u = (_lib.ptr(p) for p in proposals)
+        c.sample_interval = int(sample_interval); c.E_samples = _lib.ptr(E_samples); c.dE_out = _lib.ptr(dE_out)
+        c.force = int(force); c.exchange_rounds = int(exchange_rounds); c.ex_parity = int(ex_parity); c.ex_u = _lib.ptr(ex_u)
+        st = self.struct()
+        _lib.check(_lib.lib().nce_nce_run_chunk(self.model.handle, C.byref(st), C.byref(c), _lib.stream_ptr(stream)),
+                   "nce_nce_run_chunk")
+
+
+def setup(mdl, atoms: Structure, seed_idx=0, dtype="float32", table=None):
+    """Reference-shaped entry (``mc_model.py:60-111,175-228``): the MC machinery for ``atoms`` on the GPU."""
+    if table not in (None, "implicit"):
+        raise ValueError("only the implicit (template-only) geometry is implemented on this engine")
+    if dtype not in ("float32", None):
+        raise ValueError("the engine's NCE path computes in float32 (the oracle is the float64 reference)")
+    if int(mdl.get("spin", 0) or 0):
+        raise NotImplementedError("spin models are not on this engine's path")
+    cs = ClusterSpace.build(mdl["primitive"], list(mdl["cutoffs"]))
+    P, mu, sd = expand_params(mdl, seed_idx)
+    model = NCEModel(cs, atoms, P, mu, sd, shell_edges=list(mdl["shell_edges"]), act="tanh", pool="mean",
+                     ys=mdl["ys"], ym=mdl["ym"])
+    ys, ym, n_atoms = mdl["ys"], mdl["ym"], len(atoms)
+
+    def energy(sig):
+        st = NCEState(model, np.asarray(sig, np.int8)[None], np.ones(1, np.float32)).full_cache()
+        return float(st.E[0].item()) * ys + ym
+
+    return dict(cs=cs, P=P, model=model, depth=model.depth, ym=ym, ys=ys, n_atoms=n_atoms, n_active=model.nA,
+                sig0=model.sig0, energy=energy, perm=model.perm, inv_perm=model.inv_perm, implicit=True, geo=model.geo,
+                to_eV_per_atom=lambda E_std: E_std * ys + ym, dE_eV_total=lambda dE_std: dE_std * ys * n_atoms,
+                new_state=lambda sig, betas: NCEState(model, np.asarray(sig, np.int8), betas))

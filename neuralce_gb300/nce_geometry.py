@@ -145,7 +145,7 @@ def build_geometry(cs, structure, shell_edges, depth):
                     s.add((b2, (o[0] + o2[0], o[1] + o2[1], o[2] + o2[2])))
             nxt.append(s)
         balls.append(nxt)
-    ball_b, ball_off = [], []
+    ball_b, ball_off, ball_n = [], [], []
     for bl in balls:
         w = max(len(s) for s in bl)
         Bb = np.zeros((nB, w), np.int32); Bo = np.zeros((nB, w, 3), np.int64); Bn = np.zeros(nB, np.int32)
@@ -153,7 +153,7 @@ def build_geometry(cs, structure, shell_edges, depth):
             Bb[b] = b; items = sorted(bl[b]); Bn[b] = len(items)
             for q, (bb, o) in enumerate(items):
                 Bb[b, q] = bb; Bo[b, q] = o
-        ball_b.append(Bb); ball_off.append(Bo)
+        ball_b.append(Bb); ball_off.append(Bo); ball_n.append(Bn)
     grp_sl = {}
     for b in active_b:
         grp_sl.setdefault(tuple(prim.species[b]), []).append(b)
@@ -169,5 +169,5 @@ def build_geometry(cs, structure, shell_edges, depth):
                 T_col=tpl["col"].astype(np.int32), T_ord=tpl["order"].astype(np.float64),
                 Rv_b=Rv_b, Rv_off=Rv_off, Rv_uo=uo(Rv_off), Rv_p=Rv_p, Rv_m=Rv_m, Rv_col=Rv_col, Rv_ord=Rv_ord, Rv_v=Rv_v,
                 Sh_b=Sh_b, Sh_off=Sh_off, Sh_uo=uo(Sh_off), Sh_m=Sh_m,
-                ball_b=ball_b, ball_off=ball_off, ball_uo=[uo(x) for x in ball_off], ball_w=[x.shape[1] for x in ball_b],
+                ball_b=ball_b, ball_off=ball_off, ball_uo=[uo(x) for x in ball_off], ball_w=[x.shape[1] for x in ball_b], ball_n=ball_n,
                 grp_b=grp_b, grp_nb=grp_nb)

@@ -212,3 +212,26 @@ def expand_params(mdl, seed_idx=0):
             layers.append(dict(L))
     mu = np.zeros(Kfull); sd = np.ones(Kfull); mu[keep] = mdl["mu"]; sd[keep] = mdl["sd"]
     return dict(lin=lin, layers=layers, head=dict(P["head"])), mu, sd
+
+
+def run_chain(orc, cache, sig, prop_i, prop_j, u, beta, scale_eV):
+    """Metropolis chain of one replica on a host proposal stream (``neuralce/nce/mcmc.py:167-185``): flips
+    [[i, sig[j]], [j, sig[i]]]; same species is an accepted no-op; accept if dE_eV <= 0 or u < exp(-beta dE_eV).
+    Returns (cache, sig, E change, accepted count, dE per step, min Metropolis margin)."""
+    sig = np.asarray(sig, np.int64).copy()
+    dEs, nacc, dsum, margin = [], 0, 0.0, np.inf
+    for i, j, uu in zip(prop_i, prop_j, u):
+        i, j = int(i), int(j)
+        if sig[i] == sig[j]:
+            dEs.append(0.0); nacc += 1; continue
+        dE, patch = orc.local_delta(cache, sig, [(i, int(sig[j])), (j, int(sig[i]))])
+        dEeV = dE * scale_eV
+        acc = dEeV <= 0 or uu < np.exp(-beta * dEeV)
+        if dEeV > 0:
+            margin = min(margin, abs(np.log(uu) + beta * dEeV))
+        dEs.append(dE)
+        if acc:
+            cache = orc.commit(cache, patch, True)
+            sig[i], sig[j] = sig[j], sig[i]
+            nacc += 1; dsum += dE
+    return cache, sig, dsum, nacc, np.array(dEs), margin

@@ -55,6 +55,41 @@ def ordered_refs(a=3.924):
 
 
 @pytest.fixture(scope="session")
+def nipt_model():
+    """The shipped NeuralCE model (golden fixture) in model.pkl form (seed 0) + its exact-enumeration energies."""
+    from neuralce_gb300.lattice import Primitive
+    g = json.load(open(os.path.join(GOLDEN, "nipt_v3_nomax_sel.json")))
+    a = lambda x: np.asarray(x, float)
+    P = g["params0"]
+    params = dict(lin=a(P["lin"]), layers=[{k: a(v) for k, v in L.items()} for L in P["layers"]],
+                  head={k: (float(v) if np.ndim(v) == 0 else a(v)) for k, v in P["head"].items()})
+    prim = Primitive(cell=a(g["primitive_cell"]), frac=a(g["primitive_frac"]),
+                     species=g["chemical_symbols"] * len(g["primitive_numbers"]), numbers=np.array(g["primitive_numbers"]))
+    mdl = dict(params=[params], mu=a(g["mu"]), sd=a(g["sd"]), keep=np.array(g["keep"]), K_chem=g["K_chem"], ys=g["ys"],
+               ym=g["ym"], cutoffs=g["cutoffs"], shell_edges=g["shell_edges"], chemical_symbols=g["chemical_symbols"],
+               primitive=prim, spin=0)
+    return mdl, g
+
+
+def l10_cell(reps=(2, 2, 3), a=3.924):
+    """L1_0 NiPt on a conventional fcc cell: Pt on the odd (001) half-layers (scripts/bench/ptni_exact_enum.py:358-359)."""
+    from neuralce_gb300.io import Z_OF, fcc_conventional
+    s = fcc_conventional(a, reps)
+    z = s.scaled_positions()[:, 2] * reps[2] * 2
+    s.numbers = np.where(np.round(z).astype(int) % 2 == 1, Z_OF["Pt"], Z_OF["Ni"]).astype(np.int64)
+    return s
+
+
+def random_cell(reps, seed, a=3.924):
+    from neuralce_gb300.io import Z_OF, fcc_conventional
+    s = fcc_conventional(a, reps)
+    r = np.random.RandomState(seed)
+    z = np.full(len(s), Z_OF["Pt"], np.int64); z[r.choice(len(s), len(s) // 2, replace=False)] = Z_OF["Ni"]
+    s.numbers = z
+    return s
+
+
+@pytest.fixture(scope="session")
 def cuda():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():

@@ -1,0 +1,121 @@
+"""GPU parity of the NeuralCE engine against the float64 oracle, through the C ABI.
+
+Tolerances (float32 engine): energies within 2e-5 eV/atom of the oracle; per-swap dE within 1e-4 eV
+(spec NCE bound) in eV of the total energy; occupancy trajectories on a seeded stream bit-exact except at
+steps whose Metropolis margin |beta dE_eV + ln u| is below 1e-4 (counted: none occur for these seeds).
+"""
+import numpy as np
+import pytest
+
+from tests.conftest import l10_cell, random_cell
+
+pytestmark = pytest.mark.gpu
+
+
+def _model_pkl(mdl, s):
+    from neuralce_gb300.ce_tables import ClusterSpace
+    from neuralce_gb300.nce import NCEModel, expand_params
+    from oracle.nce_oracle import NCEOracle
+    cs = ClusterSpace.build(mdl["primitive"], mdl["cutoffs"])
+    P, mu, sd = expand_params(mdl, 0)
+    m = NCEModel(cs, s, P, mu, sd, shell_edges=mdl["shell_edges"], act="tanh", pool="mean", ys=mdl["ys"], ym=mdl["ym"])
+    return m, NCEOracle(m.geo, P, mu, sd, act="tanh", pool="mean")
+
+
+def _model_bench(L=3, seed=0):
+    from neuralce_gb300.nce import NCEModel, synthetic_model
+    from neuralce_gb300.workloads import cluster_space
+    from oracle.nce_oracle import NCEOracle
+    cs = cluster_space()
+    s = random_cell((L, L, L), seed)
+    P = synthetic_model(len(cs.orbits) + 1, 3, 64, 1, 0)
+    m = NCEModel(cs, s, P, shell_edges=(0.0, 3.3), act="silu", pool="sum")
+    return m, NCEOracle(m.geo, P, act="silu", pool="sum")
+
+
+def test_full_cache_golden_L10(cuda, nipt_model):
+    from neuralce_gb300.nce import NCEState
+    mdl, g = nipt_model
+    m, orc = _model_pkl(mdl, l10_cell())
+    st = NCEState(m, m.sig0[None], np.ones(1)).full_cache()
+    E = float(st.E[0].item()) * mdl["ys"] + mdl["ym"]
+    assert abs(E - g["E_L10"]) < 2e-5, (E, g["E_L10"])
+
+
+@pytest.mark.parametrize("which", ["pkl", "bench"])
+def test_full_cache_matches_oracle(cuda, nipt_model, which):
+    torch = cuda
+    from neuralce_gb300.nce import NCEState
+    if which == "pkl":
+        m, orc = _model_pkl(nipt_model[0], random_cell((4, 4, 4), 1))
+    else:
+        m, orc = _model_bench(3, 2)
+    rng = np.random.default_rng(0)
+    sig = np.stack([m.sig0[rng.permutation(m.N)] for _ in range(3)]).astype(np.int8)
+    st = NCEState(m, sig, np.ones(3)).full_cache()
+    torch.cuda.synchronize()
+    for r in range(3):
+        c = orc.full_cache(sig[r].astype(np.int64))
+        assert abs(float(st.E[r]) - orc.energy_of(c)) * m.scale_eV < 1e-4 * max(1.0, m.N / 64)
+        assert np.abs(st.h0[r].cpu().numpy() - c["h0"]).max() < 2e-5
+        assert np.abs(st.e[r].cpu().numpy() - c["e"]).max() < 1e-4
+
+
+@pytest.mark.parametrize("which", ["pkl", "bench"])
+def test_local_chain_matches_oracle(cuda, nipt_model, which):
+    """Every proposal accepted (force=1): per-step dE vs the oracle's local_delta chain, then the carried energy
+    and the caches vs a full rebuild."""
+    torch = cuda
+    from neuralce_gb300.nce import NCEState
+    from oracle.nce_oracle import run_chain
+    if which == "pkl":
+        m, orc = _model_pkl(nipt_model[0], random_cell((4, 4, 4), 3))
+        T = 24
+    else:
+        m, orc = _model_bench(3, 4)
+        T = 8
+    rng = np.random.default_rng(7)
+    pi = rng.integers(0, m.N, T).astype(np.int32); pj = rng.integers(0, m.N, T).astype(np.int32); pu = np.full(T, 0.5)
+    st = NCEState(m, m.sig0[None].astype(np.int8), np.ones(1)).full_cache()
+    dE = torch.zeros((T, 1), dtype=torch.float64, device="cuda")
+    props = tuple(torch.as_tensor(x.reshape(T, 1)).cuda() for x in (pi, pj, pu))
+    st.run_chunk(T, 0, proposals=props, dE_out=dE, force=1)
+    torch.cuda.synchronize()
+    cache = orc.full_cache(m.sig0.astype(np.int64))
+    E0 = orc.energy_of(cache)
+    # oracle with every move accepted: beta = 0 and u = 0.5 accepts dE <= 0 and (u < 1) all others
+    cache, sig, dsum, nacc, dEs, _ = run_chain(orc, cache, m.sig0, pi, pj, np.full(T, 0.5), 0.0, m.scale_eV)
+    got = dE.cpu().numpy()[:, 0]
+    assert np.abs((got - dEs) * m.scale_eV).max() < 1e-4, np.abs((got - dEs) * m.scale_eV).max()
+    assert np.array_equal(st.sigma[0].cpu().numpy(), sig.astype(np.int8))
+    Ecar = float(st.E[0].item())
+    st2 = NCEState(m, st.sigma.cpu().numpy(), np.ones(1)).full_cache()
+    torch.cuda.synchronize()
+    assert abs(Ecar - float(st2.E[0].item())) * m.scale_eV < 1e-4
+    assert abs(Ecar - (E0 + dsum)) * m.scale_eV < 1e-4
+    assert np.abs(st.e[0].cpu().numpy() - st2.e[0].cpu().numpy()).max() < 1e-4
+    assert int(st.n_acc[0].item()) == T
+
+
+def test_metropolis_trajectory_matches_oracle(cuda, nipt_model):
+    """Seeded host stream, Metropolis at 600 K on 4 replicas: bit-exact occupancy vs the oracle."""
+    torch = cuda
+    from neuralce_gb300.nce import NCEState
+    from oracle.nce_oracle import run_chain
+    mdl = nipt_model[0]
+    m, orc = _model_pkl(mdl, random_cell((4, 4, 4), 5))
+    R, T = 4, 30
+    beta = np.full(R, 1.0 / (8.617333e-5 * 600.0), np.float32)
+    rng = np.random.default_rng(11)
+    sig = np.stack([m.sig0[rng.permutation(m.N)] for _ in range(R)]).astype(np.int8)
+    pi = rng.integers(0, m.N, (T, R)).astype(np.int32); pj = rng.integers(0, m.N, (T, R)).astype(np.int32)
+    pu = 1.0 - rng.random((T, R))
+    st = NCEState(m, sig, beta).full_cache()
+    st.run_chunk(T, 0, proposals=tuple(torch.as_tensor(x).cuda() for x in (pi, pj, pu)))
+    torch.cuda.synchronize()
+    for r in range(R):
+        cache = orc.full_cache(sig[r].astype(np.int64))
+        _, s_ref, _, nacc, _, margin = run_chain(orc, cache, sig[r], pi[:, r], pj[:, r], pu[:, r], float(beta[r]), m.scale_eV)
+        if margin > 1e-4:
+            assert np.array_equal(st.sigma[r].cpu().numpy(), s_ref.astype(np.int8))
+            assert int(st.n_acc[r].item()) == nacc
