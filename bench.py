@@ -41,10 +41,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
-    ap.add_argument("--warps", type=int, default=0)
+    ap.add_argument("--warps", type=int, default=0, help="warps per replica (0 = autotune)")
+    ap.add_argument("--path", type=int, default=0, help="0 auto, 1 general products, 2 sign parity")
     ap.add_argument("--L", type=int, default=8)
     ap.add_argument("--R", type=int, default=32)
     ap.add_argument("--chunk", type=int, default=5000)
+    ap.add_argument("--workload", choices=["ce", "nce"], default="ce")
+    ap.add_argument("--nce-steps", type=int, default=3, help="chunks of the NeuralCE side measurement (0 = skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -157,6 +160,39 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, steps=3, warmup=1, seed=0):
+    """NeuralCE configuration 1: local receptive-field update, float32, R replicas 300-1400 K; a step is one
+    chunk of ``chunk`` MC steps + chunk//exchange_every exchange rounds; full re-anchor every ceil(N/chunk)
+    chunks (the reference driver's default)."""
+    import torch
+    from neuralce_gb300.nce import NCEState
+    from neuralce_gb300.workloads import ladder, nce_config, replica_configs
+    m, sig = nce_config(L, depth, width, seed)
+    _, beta = ladder(R)
+    st = NCEState(m, replica_configs(sig, R, 1 + seed), beta).full_cache()
+    anchor = max(1, -(-m.N // chunk))
+    step = 0
+    def one(k):
+        nonlocal step
+        st.run_chunk(chunk, step, seed=99, exchange_rounds=max(chunk // exchange_every, 1)); step += chunk
+        if (k + 1) % anchor == 0:
+            st.full_cache()
+    for k in range(warmup):
+        one(k)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    stream = torch.cuda.current_stream()
+    for k in range(steps):
+        ev[k][0].record(stream); one(warmup + k); ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    tot = sum(ms) / 1e3
+    return {"value": R * chunk * steps / tot, "unit": "swap attempts/s", "ms_per_step": float(np.mean(ms)),
+            "config": f"NeuralCE fp32: {m.N} sites, R={R}, depth {depth}, width {width}, SiLU, sum readout, 12-NN shell, "
+                      f"chunk {chunk} steps + {max(chunk // exchange_every, 1)} exchange rounds, re-anchor every {anchor} chunks",
+            "receptive_field": [int(x) for x in m.keep['ball_end'][0]], "accept_rate": float(st.n_acc.sum().item()) / (R * step)}
+
+
 def workload_config(args, gce):
     return {"workload": f"CE parallel tempering fp{args.precision}: fcc Ni/Pt {args.L}x{args.L}x{args.L} conventional "
                         f"({gce.n_atoms} sites), R={args.R} replicas 300-1400 K, exchange every {args.chunk} steps, "
@@ -187,11 +223,15 @@ def main():
     _, beta = ladder(R)
     E0 = gce.batched_energy(torch.as_tensor(sig_r).cuda()).cpu().numpy()
     st = PTState(sig_r, E0, beta, np.zeros(R, np.int32))
+    tuned = None
+    if args.warps == 0:
+        from neuralce_gb300.autotune import best_warps
+        args.warps, tuned = best_warps(gce, st, args.precision, args.path)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
     step = 0
     for _ in range(args.warmup):
-        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, 1, None, True); step += T
+        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, 1, None, True, path=args.path); step += T
     torch.cuda.synchronize()
     clk = Clocks(local); clk.start()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -201,7 +241,7 @@ def main():
     for k in range(args.steps):
         flush.zero_()
         ev[k][0].record(stream)
-        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, 1, None, True)
+        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, 1, None, True, path=args.path)
         ev[k][1].record(stream)
         step += T
     torch.cuda.synchronize()
@@ -225,7 +265,7 @@ def main():
         h_emr = pin(st.E_min_rep.cpu().numpy()); h_nacc = pin(st.n_acc.cpu().numpy()); h_nex = pin(st.n_ex.cpu().numpy())
         h_samp = pin(np.zeros((1, R)))
         torch.cuda.synchronize()
-        ck = make_chunk(T, step, 42 + rank, args.precision, args.warps, None, T, None, True)
+        ck = make_chunk(T, step, 42 + rank, args.precision, args.warps, None, T, None, True, path=args.path)
         def host_call():
             _lib.check(_lib.lib().nce_ce_run_chunk_host(gce.handle, R, h_sig.data_ptr(), h_E.data_ptr(), h_b.data_ptr(),
                                                         h_ros.data_ptr(), h_sor.data_ptr(), h_lid.data_ptr(), h_emr.data_ptr(),
@@ -246,6 +286,9 @@ def main():
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
             "kernel": "ce_pt_chunk_kernel", "peak_source": src,
             "algorithmic_bytes_per_launch": R * T * B_GATHER}
+    nce_line = None
+    if rank == 0 and args.nce_steps > 0:
+        nce_line = bench_nce(steps=args.nce_steps)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, cores, sample = cpu_oracle_rate(args.L, R)
@@ -256,7 +299,9 @@ def main():
                 "vs_baseline": value / H100_PUBLISHED if (args.L == 8 and args.R == 32) else None,
                 "dtype": "f64" if args.precision == 64 else "f32", "data": "synthetic (seeded lattice, random-normal ECIs)",
                 "config": workload_config(args, gce), "clocks": clocks, "e2e": e2e, "gpu_launches": 2 * args.steps,
-                "roofline": roof, "cpu_baseline": cpu,
+                "roofline": roof, "cpu_baseline": cpu, "nce": nce_line,
+                "launch": {"warps_per_replica": args.warps, "path": ["auto", "general", "sign-parity"][args.path],
+                           "autotune_ms": tuned},
                 "accept_rate": float(st.n_acc.sum().item()) / max(1, R * step)}
         print(json.dumps(line), flush=True)
     if world > 1:

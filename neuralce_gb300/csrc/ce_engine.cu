@@ -52,6 +52,7 @@ struct CEJob {
     int64_t sample_interval; double *E_samples;
     int32_t cta_base;      // first CTA of this job
     int32_t *err;          // device error word
+    const uint8_t *sbits;  // (n_pfc, 4) sign bit of each point-function value (sign-parity kernel)
 };
 
 struct CEBatch {
@@ -283,6 +284,174 @@ __global__ void __launch_bounds__(1024) ce_pt_chunk_kernel(const __grid_constant
     if (threadIdx.x == 0) { jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc; }
 }
 
+// ── sign-parity kernel for point functions in {-1, +1} ───────────────────────────────────────────────
+// Binary orthonormal point functions take the values -1 / +1 (and 1 for padded members), so every row product
+// is a sign: Pi = (-1)^p with p the XOR of one bit per member.  Per neighbourhood entry the kernel keeps, for each
+// point-function column, the bit of the old species (bit 0), of the new species (bit 1) and, for the second
+// site, whether the entry is the first site (bit 2).  A row then needs its member bytes XOR-ed (parities) and
+// OR-ed (contains the first site); dPi = (-1)^p_new - (-1)^p_old is 0 or +-2 exactly, so each row whose parity
+// changes adds -+2 eci: the same numbers as the product form, with one add per changed row.
+struct BinProp {
+    int64_t ia, ib; double logu;
+    int32_t ka[3], kb[3], ba, bb;
+};
+
+struct BinLayout {
+    size_t loc, pfc, eci, sig, bits, red, total;
+    __host__ __device__ static BinLayout make(int nB, int J, int mo, int n_nbr, int n_pfc, size_t acc_bytes, int64_t N,
+                                                bool tables, bool sig_smem) {
+        BinLayout L; size_t o = 0;
+        auto al = [](size_t x, size_t a) { return (x + a - 1) / a * a; };
+        if (tables) {
+            L.loc = o; o = al(o + sizeof(uint16_t) * (size_t)nB * J * mo, 16);
+            L.pfc = o; o = al(o + (size_t)nB * J * mo, 16);
+            L.eci = o; o = al(o + acc_bytes * (size_t)nB * J, 16);
+        } else {
+            L.loc = L.pfc = L.eci = 0;
+        }
+        if (sig_smem) { L.sig = o; o = al(o + (size_t)N, 16); } else { L.sig = 0; }
+        L.bits = o; o = al(o + 2 * (size_t)n_pfc * n_nbr, 16);
+        L.red = o; o = al(o + acc_bytes * 32, 16);
+        L.total = o;
+        return L;
+    }
+};
+
+__device__ __forceinline__ void bin_propose(const CEJob &jb, int64_t s, int32_t t, BinProp &P) {
+    int64_t ia, ib; double u;
+    if (jb.prop_a) {
+        ia = jb.prop_a[s * jb.R + t]; ib = jb.prop_b[s * jb.R + t]; u = jb.prop_u[s * jb.R + t];
+    } else {
+        propose(jb, jb.step0 + s, t, ia, ib, u);
+    }
+    if (ia < 0 || ib < 0 || ia >= jb.N || ib >= jb.N) {
+        atomicOr(jb.err, 1);
+        ia = ib = 0;                                   // same site -> same species -> rejected step
+    }
+    P.ia = ia; P.ib = ib; P.logu = log(u);
+    site_coords(jb, ia, P.ba, P.ka); site_coords(jb, ib, P.bb, P.kb);
+}
+
+template <typename Acc, int MO>
+__global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constant__ CEBatch bt, int32_t sig_smem) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ BinProp prop[2];
+    __shared__ int32_t ctl_valid, ctl_sa, ctl_sb;
+    const int j = find_job(bt, blockIdx.x);
+    const CEJob &jb = bt.job[j];
+    const int r = blockIdx.x - jb.cta_base;
+    if (r >= jb.R) return;
+    const int tid = threadIdx.x, nt = blockDim.x, nw = nt >> 5;
+    const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc;
+    const BinLayout L = BinLayout::make(jb.nB, jb.J, MO, n_nbr, n_pfc, sizeof(Acc), jb.N, bt.tables_in_smem, sig_smem);
+    // stage tables (eci doubled once)
+    const uint16_t *tloc; const uint8_t *tpfc; const Acc *teci2;
+    const size_t nl = (size_t)jb.nB * jb.J * MO, ne = (size_t)jb.nB * jb.J;
+    const Acc *geci2 = reinterpret_cast<const Acc *>(jb.eci);      // host passes 2*eci for this kernel
+    if (bt.tables_in_smem) {
+        uint16_t *sl = reinterpret_cast<uint16_t *>(smem + L.loc); uint8_t *sp = smem + L.pfc; Acc *se = reinterpret_cast<Acc *>(smem + L.eci);
+        for (size_t i = tid; i < nl; i += nt) { sl[i] = __ldg(jb.loc + i); sp[i] = __ldg(jb.pfc + i); }
+        for (size_t i = tid; i < ne; i += nt) se[i] = geci2[i];
+        tloc = sl; tpfc = sp; teci2 = se;
+    } else {
+        tloc = jb.loc; tpfc = jb.pfc; teci2 = geci2;
+    }
+    int8_t *gsig = jb.sigma + (int64_t)r * jb.N;
+    int8_t *sig = sig_smem ? reinterpret_cast<int8_t *>(smem + L.sig) : gsig;
+    if (sig_smem) {
+        for (int64_t i = tid; i < jb.N; i += nt) sig[i] = gsig[i];
+    }
+    uint8_t *bits = smem + L.bits;                         // [side][pfc][n_nbr]
+    Acc *red = reinterpret_cast<Acc *>(smem + L.red);
+    const uint8_t *sbits = jb.sbits;                     // [pfc][species < 4] -> sign bit
+    const int32_t t = jb.slot_of_rep[r];
+    const double beta = (double)jb.beta_slot[t];
+    double E = jb.E[r], Emin = jb.E_min_rep[r];
+    int64_t nacc = 0;
+    const int R = jb.R;
+    if (tid == 0 && jb.n_steps > 0) bin_propose(jb, 0, t, prop[0]);
+    __syncthreads();
+    for (int64_t s = 0; s < jb.n_steps; ++s) {
+        const BinProp &P = prop[s & 1];
+        if (tid == 0) {
+            ctl_sa = sig[P.ia]; ctl_sb = sig[P.ib];
+            ctl_valid = ctl_sa != ctl_sb;
+        }
+        __syncthreads();
+        const bool prop_lane = (tid == nt - 32) && (s + 1 < jb.n_steps);   // lane 0 of the last warp draws the next proposal
+        if (ctl_valid) {
+            const int64_t ia = P.ia, ib = P.ib;
+            const int sa_new = ctl_sb, sb_new = ctl_sa;
+            int near_local = 0;
+            for (int q = tid; q < 2 * n_nbr; q += nt) {
+                const int side = q >= n_nbr, n = side ? q - n_nbr : q;
+                const int b0 = side ? P.bb : P.ba;
+                const int32_t *k = side ? P.kb : P.ka;
+                const int e = b0 * n_nbr + n;
+                const int32_t *uo = jb.nb_uo + 3 * e;
+                const int64_t st = (((int64_t)wrap_add(k[0], __ldg(uo), jb.d0) * jb.d1 + wrap_add(k[1], __ldg(uo + 1), jb.d1)) * jb.d2 +
+                                    wrap_add(k[2], __ldg(uo + 2), jb.d2)) * jb.nB + __ldg(jb.nb_b + e);
+                const int so = sig[st];
+                const int sn = (st == ia) ? sa_new : ((st == ib) ? sb_new : so);
+                const int isa = side && (st == ia);
+                near_local |= isa;
+                uint8_t *bs = bits + (size_t)side * n_pfc * n_nbr;
+                for (int c = 0; c < n_pfc; ++c)
+                    bs[c * n_nbr + n] = (uint8_t)(sbits[c * 4 + so] | (sbits[c * 4 + sn] << 1) | (isa << 2));
+            }
+            const int near = __syncthreads_or(near_local);
+            if (prop_lane) bin_propose(jb, s + 1, t, prop[(s + 1) & 1]);
+            Acc acc = Acc(0);
+            for (int side = 0; side < 2; ++side) {
+                const int b0 = side ? P.bb : P.ba;
+                const int Jn = __ldg(jb.rv_len + b0);
+                const uint16_t *loc = tloc + (size_t)b0 * jb.J * MO;
+                const uint8_t *pfc = tpfc + (size_t)b0 * jb.J * MO;
+                const Acc *e2 = teci2 + (size_t)b0 * jb.J;
+                const uint8_t *bs = bits + (size_t)side * n_pfc * n_nbr;
+                const bool check = side && near;
+                for (int rr = tid; rr < Jn; rr += nt) {
+                    unsigned x = 0, y = 0;
+#pragma unroll
+                    for (int m = 0; m < MO; ++m) {
+                        const unsigned v = bs[pfc[(size_t)rr * MO + m] * n_nbr + loc[(size_t)rr * MO + m]];
+                        x ^= v; y |= v;
+                    }
+                    const bool skip = check && (y & 4u);
+                    if (!skip && ((x ^ (x >> 1)) & 1u)) {        // parity changed
+                        const Acc v2 = e2[rr];
+                        acc += (x & 1u) ? v2 : -v2;             // old parity odd: Pi -1 -> +1 (+2 eci); even: -2 eci
+                    }
+                }
+            }
+            acc = warp_sum(acc);
+            if ((tid & 31) == 0) red[tid >> 5] = acc;
+            __syncthreads();
+            if (tid == 0) {
+                Acc dE = Acc(0);
+                for (int w = 0; w < nw; ++w) dE += red[w];
+                const double dEd = (double)dE;
+                if (P.logu < -beta * dEd) {
+                    sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new;
+                    E += dEd; ++nacc;
+                }
+            }
+        } else if (prop_lane) {
+            bin_propose(jb, s + 1, t, prop[(s + 1) & 1]);
+        }
+        if (tid == 0) {
+            Emin = fmin(Emin, E);
+            if (jb.E_samples && (s + 1) % jb.sample_interval == 0)
+                jb.E_samples[((s + 1) / jb.sample_interval - 1) * R + t] = E;
+        }
+        __syncthreads();
+    }
+    if (sig_smem) {
+        for (int64_t i = tid; i < jb.N; i += nt) gsig[i] = sig[i];
+    }
+    if (tid == 0) { jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc; }
+}
+
 // chunk-end exchange of temperature slots, one CTA (thread 0) per job
 struct CEExJob {
     int32_t R; double *E; const float *beta_slot; int32_t *rep_of_slot, *slot_of_rep; const int32_t *ladder_id;
@@ -428,6 +597,8 @@ struct nce_ce_model {
     int32_t *act_b = nullptr, *act_nb = nullptr; uint64_t *grp_cum = nullptr;
     int32_t *T_b = nullptr, *T_uo = nullptr; uint8_t *T_pfc = nullptr; double *T_eci64 = nullptr; float *T_eci32 = nullptr;
     int32_t *err = nullptr;                  // device error word
+    bool binary = false;                     // every point-function value is -1 or +1 (sign-parity kernel applies)
+    uint8_t *sbits = nullptr; double *eci2_64 = nullptr; float *eci2_32 = nullptr;
     double *energy_partial = nullptr; size_t energy_partial_n = 0;
     int device = 0;
     std::mutex mu;
@@ -447,7 +618,7 @@ static int upload(T *&dst, const T *src, size_t n) {
 
 static int free_model(nce_ce_model *m) {
     void *ptrs[] = {m->loc, m->pfc, m->eci64, m->eci32, m->rv_len, m->nb_b, m->nb_uo, m->pf64, m->pf32, m->act_b,
-                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err,
+                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->eci2_64, m->eci2_32,
                     m->energy_partial, m->staging_base};
     for (void *p : ptrs) if (p) cudaFree(p);
     delete m;
@@ -464,11 +635,13 @@ static bool tables_fit(const nce_ce_model *m, int warps, size_t *bytes_out) {
     return false;
 }
 
-static CEJob make_job(const nce_ce_model *m, const nce_pt_state *st, const nce_pt_chunk *ck, int cta_base) {
+static CEJob make_job(const nce_ce_model *m, const nce_pt_state *st, const nce_pt_chunk *ck, int cta_base, bool bin = false) {
     CEJob j;
     std::memset(&j, 0, sizeof(j));
     const bool p64 = ck ? ck->precision != 32 : true;
     j.loc = m->loc; j.pfc = m->pfc; j.eci = p64 ? (const void *)m->eci64 : (const void *)m->eci32;
+    if (bin) j.eci = p64 ? (const void *)m->eci2_64 : (const void *)m->eci2_32;
+    j.sbits = m->sbits;
     j.rv_len = m->rv_len; j.nb_b = m->nb_b; j.nb_uo = m->nb_uo; j.pf = p64 ? (const void *)m->pf64 : (const void *)m->pf32;
     j.act_b = m->act_b; j.act_nb = m->act_nb; j.grp_cum = m->grp_cum;
     j.nB = m->nB; j.J = m->J; j.n_nbr = m->n_nbr; j.n_pfc = m->n_pfc; j.max_sp = m->max_sp;
@@ -495,6 +668,25 @@ static int launch_chunk_mo(const CEBatch &bt, int total, int warps, size_t smem,
     kern<<<total, warps * 32, smem, s>>>(bt);
     NCE_CUDA(cudaGetLastError());
     return NCE_OK;
+}
+
+template <typename Acc, int MO>
+static int launch_bin_mo(const CEBatch &bt, int total, int warps, size_t smem, int sig_smem, cudaStream_t s) {
+    auto kern = ce_bin_chunk_kernel<Acc, MO>;
+    NCE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<total, warps * 32, smem, s>>>(bt, sig_smem);
+    NCE_CUDA(cudaGetLastError());
+    return NCE_OK;
+}
+
+template <typename Acc>
+static int launch_bin(const CEBatch &bt, int mo, int total, int warps, size_t smem, int sig_smem, cudaStream_t s) {
+    switch (mo) {
+#define NCE_BIN_CASE(M) case M: return launch_bin_mo<Acc, M>(bt, total, warps, smem, sig_smem, s);
+        NCE_BIN_CASE(1) NCE_BIN_CASE(2) NCE_BIN_CASE(3) NCE_BIN_CASE(4) NCE_BIN_CASE(5) NCE_BIN_CASE(6) NCE_BIN_CASE(7) NCE_BIN_CASE(8)
+#undef NCE_BIN_CASE
+        default: return fail(NCE_ERR_UNSUPPORTED, "cluster order %d > 8", mo);
+    }
 }
 
 template <typename Real>
@@ -549,32 +741,63 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
     }
     for (int j = 0; j < n_jobs; ++j)
         NCE_CHECK(hs[j]->mo == mo, "batch: all jobs must have the same maximum cluster order");
+    const int path = cks[0].path;
+    bool all_bin = true;
+    for (int j = 0; j < n_jobs; ++j) {
+        NCE_CHECK(cks[j].path == path, "batch: all chunks must use the same path");
+        all_bin = all_bin && hs[j]->binary;
+    }
+    NCE_CHECK(path >= 0 && path <= 2, "chunk: path must be 0 (auto), 1 (general) or 2 (sign parity)");
+    NCE_CHECK(path != 2 || all_bin, "chunk: the sign-parity path needs point functions in {-1, +1}");
+    const bool use_bin = (path == 2) || (path == 0 && all_bin);
     CEBatch bt; std::memset(&bt, 0, sizeof(bt));
     bt.n_jobs = n_jobs;
     size_t smem = 0; bool all_fit = true;
-    for (int j = 0; j < n_jobs; ++j) {
-        size_t b; bool fit = precision == 64 ? tables_fit<double>(hs[j], warps, &b) : tables_fit<float>(hs[j], warps, &b);
-        all_fit = all_fit && fit;
-    }
-    for (int j = 0; j < n_jobs; ++j) {
-        size_t b;
-        if (precision == 64) {
-            b = Layout<double>::make(hs[j]->nB, hs[j]->J, mo, hs[j]->n_nbr, hs[j]->n_pfc, warps, all_fit).total;
-        } else {
-            b = Layout<float>::make(hs[j]->nB, hs[j]->J, mo, hs[j]->n_nbr, hs[j]->n_pfc, warps, all_fit).total;
+    int sig_smem = 0;
+    if (use_bin) {
+        const size_t accb = precision == 64 ? 8 : 4;
+        size_t t_on = 0, t_off = 0; int64_t maxN = 0;
+        for (int j = 0; j < n_jobs; ++j) {
+            const nce_ce_model *m = hs[j];
+            t_on = std::max(t_on, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, accb, 0, true, false).total);
+            t_off = std::max(t_off, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, accb, 0, false, false).total);
+            maxN = std::max(maxN, m->N);
         }
-        smem = std::max(smem, b);
+        const size_t limit = 200 * 1024, sigb = (size_t)((maxN + 15) / 16 * 16);
+        all_fit = t_on <= limit;
+        const size_t base = all_fit ? t_on : t_off;
+        sig_smem = base + sigb <= limit ? 1 : 0;
+        smem = base + (sig_smem ? sigb : 0);
+    } else {
+        for (int j = 0; j < n_jobs; ++j) {
+            size_t b; bool fit = precision == 64 ? tables_fit<double>(hs[j], warps, &b) : tables_fit<float>(hs[j], warps, &b);
+            all_fit = all_fit && fit;
+        }
+        for (int j = 0; j < n_jobs; ++j) {
+            size_t b;
+            if (precision == 64) {
+                b = Layout<double>::make(hs[j]->nB, hs[j]->J, mo, hs[j]->n_nbr, hs[j]->n_pfc, warps, all_fit).total;
+            } else {
+                b = Layout<float>::make(hs[j]->nB, hs[j]->J, mo, hs[j]->n_nbr, hs[j]->n_pfc, warps, all_fit).total;
+            }
+            smem = std::max(smem, b);
+        }
     }
     bt.tables_in_smem = all_fit ? 1 : 0;
     int base = 0;
     for (int j = 0; j < n_jobs; ++j) {
-        bt.job[j] = make_job(hs[j], &sts[j], &cks[j], base);
+        bt.job[j] = make_job(hs[j], &sts[j], &cks[j], base, use_bin);
         base += sts[j].R;
     }
     int64_t max_steps = 0;
     for (int j = 0; j < n_jobs; ++j) max_steps = std::max(max_steps, cks[j].n_steps);
     if (max_steps > 0) {
-        int rc = precision == 64 ? launch_chunk<double>(bt, mo, total, warps, smem, s)
+        int rc;
+        if (use_bin)
+            rc = precision == 64 ? launch_bin<double>(bt, mo, total, warps, smem, sig_smem, s)
+                                 : launch_bin<float>(bt, mo, total, warps, smem, sig_smem, s);
+        else
+            rc = precision == 64 ? launch_chunk<double>(bt, mo, total, warps, smem, s)
                                  : launch_chunk<float>(bt, mo, total, warps, smem, s);
         if (rc) return rc;
     }
@@ -714,6 +937,24 @@ int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
         cudaError_t e = cudaMalloc((void **)&m->err, sizeof(int32_t));
         if (e == cudaSuccess) e = cudaMemset(m->err, 0, sizeof(int32_t));
         if (e != cudaSuccess) rc = fail(NCE_ERR_CUDA, "nce_ce_create: %s", cudaGetErrorString(e));
+    }
+    // sign-parity eligibility: every point-function value is exactly -1 or +1, at most 4 species
+    bool bin = t->max_sp <= 4;
+    std::vector<uint8_t> sb((size_t)t->n_pfc * 4, 0);
+    for (int c = 0; c < t->n_pfc && bin; ++c)
+        for (int q = 0; q < t->max_sp; ++q) {
+            const double v = t->pf[(size_t)c * t->max_sp + q];
+            if (v == 1.0) sb[(size_t)c * 4 + q] = 0;
+            else if (v == -1.0) sb[(size_t)c * 4 + q] = 1;
+            else bin = false;
+        }
+    if (!rc && bin) {
+        std::vector<double> e2((size_t)t->nB * t->J); std::vector<float> f2(e2.size());
+        for (size_t i = 0; i < e2.size(); ++i) { e2[i] = 2.0 * t->Rv_eci[i]; f2[i] = 2.0f * (float)t->Rv_eci[i]; }
+        rc = upload(m->sbits, sb.data(), sb.size());
+        if (!rc) rc = upload(m->eci2_64, e2.data(), e2.size());
+        if (!rc) rc = upload(m->eci2_32, f2.data(), f2.size());
+        m->binary = !rc;
     }
     if (rc) { free_model(m); return rc; }
     *out = m;

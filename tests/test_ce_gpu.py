@@ -71,8 +71,8 @@ def _compare(st, ref, E_tol):
     assert int(st.n_ex.item()) == int(ref["n_ex"][0])
 
 
-@pytest.mark.parametrize("precision", [64, 32])
-def test_trajectory_host_stream(cuda, precision):
+@pytest.mark.parametrize("precision,path,warps", [(64, 1, 8), (32, 1, 8), (64, 2, 8), (32, 2, 4), (64, 2, 1)])
+def test_trajectory_host_stream(cuda, precision, path, warps):
     """Seeded host proposal stream + exchange uniforms: bit-exact occupancy trajectory, energies, acceptance,
     slot permutation and slot-ordered samples vs the oracle."""
     torch = cuda
@@ -92,7 +92,7 @@ def test_trajectory_host_stream(cuda, precision):
         par = chunk % 2
         Es = torch.zeros((T // si, R), dtype=torch.float64, device="cuda")
         dev = tuple(torch.as_tensor(x).cuda() for x in (pa, pb, pu))
-        run_chunk(gce, st, T, step, 0, precision, 8, dev, si, Es, True, par, torch.as_tensor(exu).cuda())
+        run_chunk(gce, st, T, step, 0, precision, warps, dev, si, Es, True, par, torch.as_tensor(exu).cuda(), path=path)
         Es_ref = np.zeros((T // si, R))
         orc.run(ref, T, step, 0, (pa, pb, pu), si, Es_ref, True, par, exu, n_threads=4)
         torch.cuda.synchronize()
@@ -103,7 +103,8 @@ def test_trajectory_host_stream(cuda, precision):
     assert int(st.n_acc.sum()) > 0
 
 
-def test_trajectory_philox_multichunk(cuda):
+@pytest.mark.parametrize("path", [1, 2])
+def test_trajectory_philox_multichunk(cuda, path):
     """Device Philox stream, 3 chunks with exchanges: equals the oracle's Philox restatement."""
     torch = cuda
     from neuralce_gb300.pt import run_chunk
@@ -115,7 +116,7 @@ def test_trajectory_philox_multichunk(cuda):
     for c in range(3):
         Es = torch.zeros((T // 100, R), dtype=torch.float64, device="cuda")
         Es_ref = np.zeros((T // 100, R))
-        run_chunk(gce, st, T, c * T, 1234, 64, 4, None, 100, Es, True)
+        run_chunk(gce, st, T, c * T, 1234, 64, 4, None, 100, Es, True, path=path)
         orc.run(ref, T, c * T, 1234, None, 100, Es_ref, True, n_threads=4)
         torch.cuda.synchronize()
         _compare(st, ref, 1e-9)
@@ -172,6 +173,23 @@ def test_host_buffer_entry_point(cuda):
     torch.cuda.synchronize()
     assert np.array_equal(h_sig, st.sigma.cpu().numpy()) and np.array_equal(h_E, st.E.cpu().numpy())
     assert np.array_equal(ros, st.rep_of_slot.cpu().numpy()) and np.array_equal(nacc, st.n_acc.cpu().numpy())
+
+
+@pytest.mark.parametrize("L", [2, 3])
+def test_sign_parity_small_cells(cuda, L):
+    """Tiny periodic cells (neighbourhood entries alias onto the same sites): sign-parity == general == oracle."""
+    torch = cuda
+    from neuralce_gb300.pt import run_chunk
+    from oracle.ce_oracle import new_state
+    R, T = 4, 400
+    gce, orc, sig_r, beta = _setup(L, seed=9, R=R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    a = _engine_state(sig_r, E0, beta); b = _engine_state(sig_r, E0, beta); ref = new_state(sig_r, E0, beta)
+    run_chunk(gce, a, T, 0, 31, 64, 2, None, 1, None, True, path=1)
+    run_chunk(gce, b, T, 0, 31, 64, 2, None, 1, None, True, path=2)
+    orc.run(ref, T, 0, 31, None, 1, None, True)
+    torch.cuda.synchronize()
+    _compare(a, ref, 1e-9); _compare(b, ref, 1e-9)
 
 
 def test_out_of_range_proposal_is_flagged(cuda):
