@@ -72,6 +72,8 @@ typedef struct {
     const int32_t *act_b;  /* (n_groups, max_gb) basis sites of each group */
     const int32_t *act_nb; /* (n_groups) */
     const uint64_t *grp_cum; /* (n_groups) cumulative choice thresholds in units of 2^-32 (last = 2^32) */
+    const int32_t *Rv_col; /* (nB, J) cluster-vector column of each reverse row (non-decreasing within a site), or NULL */
+    int32_t n_cols;        /* columns (<= 255 for the sign-parity kernel) */
 } nce_ce_tables;
 
 typedef struct nce_ce_model *nce_ce_handle;

@@ -22,7 +22,8 @@ class NceCeTables(C.Structure):
                 ("d", i64 * 3), ("n_cells", i64), ("zerolet", f64),
                 ("Rv_len", vp), ("Rv_loc", vp), ("Rv_pfc", vp), ("Rv_eci", vp), ("nb_b", vp), ("nb_uo", vp),
                 ("Rt", i32), ("T_b", vp), ("T_uo", vp), ("T_pfc", vp), ("T_eci", vp), ("pf", vp),
-                ("n_groups", i32), ("max_gb", i32), ("act_b", vp), ("act_nb", vp), ("grp_cum", vp)]
+                ("n_groups", i32), ("max_gb", i32), ("act_b", vp), ("act_nb", vp), ("grp_cum", vp),
+                ("Rv_col", vp), ("n_cols", i32)]
 
 
 class NcePtState(C.Structure):

@@ -53,6 +53,10 @@ struct CEJob {
     int32_t cta_base;      // first CTA of this job
     int32_t *err;          // device error word
     const uint8_t *sbits;  // (n_pfc, 4) sign bit of each point-function value (sign-parity kernel)
+    const uint16_t *bix;   // (nB, J, mo) pfc * n_nbr + loc of each member (sign-parity kernel)
+    const uint8_t *rcol;   // (nB, J) cluster-vector column of each reverse row
+    const void *ecol2;     // (n_cols) 2 * eci of each column, double or float
+    int32_t n_cols;
 };
 
 struct CEBatch {
@@ -288,34 +292,47 @@ __global__ void __launch_bounds__(1024) ce_pt_chunk_kernel(const __grid_constant
 // Binary orthonormal point functions take the values -1 / +1 (and 1 for padded members), so every row product
 // is a sign: Pi = (-1)^p with p the XOR of one bit per member.  Per neighbourhood entry the kernel keeps, for each
 // point-function column, the bit of the old species (bit 0), of the new species (bit 1) and, for the second
-// site, whether the entry is the first site (bit 2).  A row then needs its member bytes XOR-ed (parities) and
-// OR-ed (contains the first site); dPi = (-1)^p_new - (-1)^p_old is 0 or +-2 exactly, so each row whose parity
-// changes adds -+2 eci: the same numbers as the product form, with one add per changed row.
+// site, whether the entry is the first site (bit 2).  A row's member bytes are XOR-ed (parities) and OR-ed
+// (contains the first site); dPi = (-1)^p_new - (-1)^p_old is 0 or +-2 exactly.  All rows of one cluster-vector
+// column share one eci, so dE = sum over columns of 2 eci_c * n_c with n_c the exact integer sum of the rows'
+// +-1 parity changes; the reverse rows of a site are ordered by column, so each warp folds its 32 consecutive
+// rows with a segmented scan and adds one integer per column run.  Products and the column sum run in the
+// kernel's precision (float64 or float32); the counts are exact.
 struct BinProp {
     int64_t ia, ib; double logu;
     int32_t ka[3], kb[3], ba, bb;
 };
 
 struct BinLayout {
-    size_t loc, pfc, eci, sig, bits, red, total;
-    __host__ __device__ static BinLayout make(int nB, int J, int mo, int n_nbr, int n_pfc, size_t acc_bytes, int64_t N,
+    size_t bix, rcol, ecol, sig, bits, cnt, total;
+    __host__ __device__ static BinLayout make(int nB, int J, int mo, int n_nbr, int n_pfc, int n_cols, size_t acc_bytes, int64_t N,
                                                 bool tables, bool sig_smem) {
         BinLayout L; size_t o = 0;
         auto al = [](size_t x, size_t a) { return (x + a - 1) / a * a; };
         if (tables) {
-            L.loc = o; o = al(o + sizeof(uint16_t) * (size_t)nB * J * mo, 16);
-            L.pfc = o; o = al(o + (size_t)nB * J * mo, 16);
-            L.eci = o; o = al(o + acc_bytes * (size_t)nB * J, 16);
+            L.bix = o; o = al(o + sizeof(uint16_t) * (size_t)nB * J * mo, 16);
+            L.rcol = o; o = al(o + (size_t)nB * J, 16);
         } else {
-            L.loc = L.pfc = L.eci = 0;
+            L.bix = L.rcol = 0;
         }
+        L.ecol = o; o = al(o + acc_bytes * (size_t)n_cols, 16);
         if (sig_smem) { L.sig = o; o = al(o + (size_t)N, 16); } else { L.sig = 0; }
         L.bits = o; o = al(o + 2 * (size_t)n_pfc * n_nbr, 16);
-        L.red = o; o = al(o + acc_bytes * 32, 16);
+        L.cnt = o; o = al(o + sizeof(int32_t) * (size_t)n_cols, 16);
         L.total = o;
         return L;
     }
 };
+
+__device__ __forceinline__ void site_coords32(const CEJob &jb, int64_t i, int32_t &b, int32_t k[3]) {
+    const uint32_t ii = (uint32_t)i, nB = (uint32_t)jb.nB, d1 = (uint32_t)jb.d1, d2 = (uint32_t)jb.d2;
+    const uint32_t c = ii / nB;
+    b = (int32_t)(ii - c * nB);
+    const uint32_t c12 = c / d2;
+    k[2] = (int32_t)(c - c12 * d2);
+    k[0] = (int32_t)(c12 / d1);
+    k[1] = (int32_t)(c12 - (uint32_t)k[0] * d1);
+}
 
 __device__ __forceinline__ void bin_propose(const CEJob &jb, int64_t s, int32_t t, BinProp &P) {
     int64_t ia, ib; double u;
@@ -329,126 +346,153 @@ __device__ __forceinline__ void bin_propose(const CEJob &jb, int64_t s, int32_t 
         ia = ib = 0;                                   // same site -> same species -> rejected step
     }
     P.ia = ia; P.ib = ib; P.logu = log(u);
-    site_coords(jb, ia, P.ba, P.ka); site_coords(jb, ib, P.bb, P.kb);
+    site_coords32(jb, ia, P.ba, P.ka); site_coords32(jb, ib, P.bb, P.kb);
 }
 
 template <typename Acc, int MO>
 __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constant__ CEBatch bt, int32_t sig_smem) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ BinProp prop[2];
-    __shared__ int32_t ctl_valid, ctl_sa, ctl_sb;
+    __shared__ int32_t near_flag;
     const int j = find_job(bt, blockIdx.x);
     const CEJob &jb = bt.job[j];
     const int r = blockIdx.x - jb.cta_base;
     if (r >= jb.R) return;
-    const int tid = threadIdx.x, nt = blockDim.x, nw = nt >> 5;
-    const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc;
-    const BinLayout L = BinLayout::make(jb.nB, jb.J, MO, n_nbr, n_pfc, sizeof(Acc), jb.N, bt.tables_in_smem, sig_smem);
-    // stage tables (eci doubled once)
-    const uint16_t *tloc; const uint8_t *tpfc; const Acc *teci2;
+    const int tid = threadIdx.x, nt = blockDim.x, nw = nt >> 5, lane = tid & 31, warp = tid >> 5;
+    const int ncons = nw > 1 ? nw - 1 : 1;            // consumer warps; the last warp (when there are two or more) draws proposals
+    const bool producer = nw > 1 ? (warp == nw - 1) : (tid == 0);
+    const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc, n_cols = jb.n_cols;
+    const BinLayout L = BinLayout::make(jb.nB, jb.J, MO, n_nbr, n_pfc, n_cols, sizeof(Acc), jb.N, bt.tables_in_smem, sig_smem);
+    const uint16_t *tbix; const uint8_t *trcol;
     const size_t nl = (size_t)jb.nB * jb.J * MO, ne = (size_t)jb.nB * jb.J;
-    const Acc *geci2 = reinterpret_cast<const Acc *>(jb.eci);      // host passes 2*eci for this kernel
     if (bt.tables_in_smem) {
-        uint16_t *sl = reinterpret_cast<uint16_t *>(smem + L.loc); uint8_t *sp = smem + L.pfc; Acc *se = reinterpret_cast<Acc *>(smem + L.eci);
-        for (size_t i = tid; i < nl; i += nt) { sl[i] = __ldg(jb.loc + i); sp[i] = __ldg(jb.pfc + i); }
-        for (size_t i = tid; i < ne; i += nt) se[i] = geci2[i];
-        tloc = sl; tpfc = sp; teci2 = se;
+        uint16_t *sb = reinterpret_cast<uint16_t *>(smem + L.bix); uint8_t *sc = smem + L.rcol;
+        for (size_t i = tid; i < nl; i += nt) sb[i] = __ldg(jb.bix + i);
+        for (size_t i = tid; i < ne; i += nt) sc[i] = __ldg(jb.rcol + i);
+        tbix = sb; trcol = sc;
     } else {
-        tloc = jb.loc; tpfc = jb.pfc; teci2 = geci2;
+        tbix = jb.bix; trcol = jb.rcol;
     }
+    Acc *ecol = reinterpret_cast<Acc *>(smem + L.ecol);
+    const Acc *gecol = reinterpret_cast<const Acc *>(jb.ecol2);
+    int32_t *cnt = reinterpret_cast<int32_t *>(smem + L.cnt);
+    for (int c = tid; c < n_cols; c += nt) { ecol[c] = gecol[c]; cnt[c] = 0; }
     int8_t *gsig = jb.sigma + (int64_t)r * jb.N;
     int8_t *sig = sig_smem ? reinterpret_cast<int8_t *>(smem + L.sig) : gsig;
-    if (sig_smem) {
+    if (sig_smem)
         for (int64_t i = tid; i < jb.N; i += nt) sig[i] = gsig[i];
-    }
     uint8_t *bits = smem + L.bits;                         // [side][pfc][n_nbr]
-    Acc *red = reinterpret_cast<Acc *>(smem + L.red);
-    const uint8_t *sbits = jb.sbits;                     // [pfc][species < 4] -> sign bit
+    const uint8_t *sbits = jb.sbits;                       // [pfc][species < 4] -> sign bit
     const int32_t t = jb.slot_of_rep[r];
     const double beta = (double)jb.beta_slot[t];
     double E = jb.E[r], Emin = jb.E_min_rep[r];
     int64_t nacc = 0;
     const int R = jb.R;
-    if (tid == 0 && jb.n_steps > 0) bin_propose(jb, 0, t, prop[0]);
+    if (tid == 0) { near_flag = 0; if (jb.n_steps > 0) bin_propose(jb, 0, t, prop[0]); }
     __syncthreads();
     for (int64_t s = 0; s < jb.n_steps; ++s) {
         const BinProp &P = prop[s & 1];
-        if (tid == 0) {
-            ctl_sa = sig[P.ia]; ctl_sb = sig[P.ib];
-            ctl_valid = ctl_sa != ctl_sb;
-        }
-        __syncthreads();
-        const bool prop_lane = (tid == nt - 32) && (s + 1 < jb.n_steps);   // lane 0 of the last warp draws the next proposal
-        if (ctl_valid) {
-            const int64_t ia = P.ia, ib = P.ib;
-            const int sa_new = ctl_sb, sb_new = ctl_sa;
-            int near_local = 0;
-            for (int q = tid; q < 2 * n_nbr; q += nt) {
+        const int64_t ia = P.ia, ib = P.ib;
+        const int sa = sig[ia], sb = sig[ib];
+        const bool next = (s + 1 < jb.n_steps);
+        if (sa != sb) {
+            const int sa_new = sb, sb_new = sa;
+            // 1. neighbourhood bits (consumer threads); near_flag was cleared before the previous barrier
+            const int ct = ncons * 32;
+            for (int q = tid; q < 2 * n_nbr && tid < ct; q += ct) {
                 const int side = q >= n_nbr, n = side ? q - n_nbr : q;
                 const int b0 = side ? P.bb : P.ba;
                 const int32_t *k = side ? P.kb : P.ka;
                 const int e = b0 * n_nbr + n;
                 const int32_t *uo = jb.nb_uo + 3 * e;
-                const int64_t st = (((int64_t)wrap_add(k[0], __ldg(uo), jb.d0) * jb.d1 + wrap_add(k[1], __ldg(uo + 1), jb.d1)) * jb.d2 +
-                                    wrap_add(k[2], __ldg(uo + 2), jb.d2)) * jb.nB + __ldg(jb.nb_b + e);
+                const uint32_t st = ((((uint32_t)wrap_add(k[0], __ldg(uo), jb.d0) * (uint32_t)jb.d1 + (uint32_t)wrap_add(k[1], __ldg(uo + 1), jb.d1)) *
+                                      (uint32_t)jb.d2 + (uint32_t)wrap_add(k[2], __ldg(uo + 2), jb.d2)) * (uint32_t)jb.nB + (uint32_t)__ldg(jb.nb_b + e));
                 const int so = sig[st];
-                const int sn = (st == ia) ? sa_new : ((st == ib) ? sb_new : so);
-                const int isa = side && (st == ia);
-                near_local |= isa;
+                const int sn = (st == (uint32_t)ia) ? sa_new : ((st == (uint32_t)ib) ? sb_new : so);
+                const int isa = side && (st == (uint32_t)ia);
+                if (isa) near_flag = 1;
                 uint8_t *bs = bits + (size_t)side * n_pfc * n_nbr;
                 for (int c = 0; c < n_pfc; ++c)
                     bs[c * n_nbr + n] = (uint8_t)(sbits[c * 4 + so] | (sbits[c * 4 + sn] << 1) | (isa << 2));
             }
-            const int near = __syncthreads_or(near_local);
-            if (prop_lane) bin_propose(jb, s + 1, t, prop[(s + 1) & 1]);
-            Acc acc = Acc(0);
-            for (int side = 0; side < 2; ++side) {
-                const int b0 = side ? P.bb : P.ba;
-                const int Jn = __ldg(jb.rv_len + b0);
-                const uint16_t *loc = tloc + (size_t)b0 * jb.J * MO;
-                const uint8_t *pfc = tpfc + (size_t)b0 * jb.J * MO;
-                const Acc *e2 = teci2 + (size_t)b0 * jb.J;
-                const uint8_t *bs = bits + (size_t)side * n_pfc * n_nbr;
-                const bool check = side && near;
-                for (int rr = tid; rr < Jn; rr += nt) {
-                    unsigned x = 0, y = 0;
-#pragma unroll
-                    for (int m = 0; m < MO; ++m) {
-                        const unsigned v = bs[pfc[(size_t)rr * MO + m] * n_nbr + loc[(size_t)rr * MO + m]];
-                        x ^= v; y |= v;
-                    }
-                    const bool skip = check && (y & 4u);
-                    if (!skip && ((x ^ (x >> 1)) & 1u)) {        // parity changed
-                        const Acc v2 = e2[rr];
-                        acc += (x & 1u) ? v2 : -v2;             // old parity odd: Pi -1 -> +1 (+2 eci); even: -2 eci
-                    }
-                }
-            }
-            acc = warp_sum(acc);
-            if ((tid & 31) == 0) red[tid >> 5] = acc;
             __syncthreads();
-            if (tid == 0) {
-                Acc dE = Acc(0);
-                for (int w = 0; w < nw; ++w) dE += red[w];
-                const double dEd = (double)dE;
-                if (P.logu < -beta * dEd) {
-                    sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new;
-                    E += dEd; ++nacc;
+            if (producer) {
+                if (lane == 0 && next) bin_propose(jb, s + 1, t, prop[(s + 1) & 1]);
+            }
+            if (!producer || nw == 1) {
+                // 2. rows: warp-contiguous blocks of 32 rows, exact integer parity counts per column run
+                const int Ja = __ldg(jb.rv_len + P.ba), Jb = __ldg(jb.rv_len + P.bb);
+                const int Jt = Ja + Jb;
+                const bool near = near_flag != 0;
+                const int cw = nw > 1 ? warp : 0;
+                for (int base = cw * 32; base < Jt; base += ncons * 32) {
+                    const int v = base + lane;
+                    int sgn = 0, col = 0x7fffffff;
+                    if (v < Jt) {
+                        const int side = v >= Ja, rr = side ? v - Ja : v;
+                        const int b0 = side ? P.bb : P.ba;
+                        const uint16_t *bx = tbix + ((size_t)b0 * jb.J + rr) * MO;
+                        const uint8_t *bs = bits + (size_t)side * n_pfc * n_nbr;
+                        unsigned x = 0, y = 0;
+                        if (MO == 4) {
+                            const uint2 w = *reinterpret_cast<const uint2 *>(bx);
+                            const unsigned v0 = bs[w.x & 0xffffu], v1 = bs[w.x >> 16], v2 = bs[w.y & 0xffffu], v3 = bs[w.y >> 16];
+                            x = v0 ^ v1 ^ v2 ^ v3; y = v0 | v1 | v2 | v3;
+                        } else {
+#pragma unroll
+                            for (int m = 0; m < MO; ++m) { const unsigned vv = bs[bx[m]]; x ^= vv; y |= vv; }
+                        }
+                        col = trcol[(size_t)b0 * jb.J + rr] + (side ? 0x10000 : 0);   // runs never join across the two sites
+                        const bool skip = side && near && (y & 4u);
+                        if (!skip && ((x ^ (x >> 1)) & 1u)) sgn = (x & 1u) ? 1 : -1;  // odd old parity: Pi -1 -> +1
+                    }
+                    // segmented sum over runs of equal col within the warp
+                    int pre = sgn;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int up = __shfl_up_sync(0xffffffffu, pre, o);
+                        if (lane >= o) pre += up;
+                    }
+                    const int prev_col = __shfl_up_sync(0xffffffffu, col, 1);
+                    const int next_col = __shfl_down_sync(0xffffffffu, col, 1);
+                    const bool head = lane == 0 || prev_col != col;
+                    const bool tail = lane == 31 || next_col != col;
+                    const unsigned heads = __ballot_sync(0xffffffffu, head);
+                    const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+                    const int before = __shfl_sync(0xffffffffu, pre, start > 0 ? start - 1 : 0);
+                    if (tail && col != 0x7fffffff) {
+                        const int run = pre - (start > 0 ? before : 0);
+                        if (run) atomicAdd(&cnt[col & 0xffff], run);
+                    }
                 }
             }
-        } else if (prop_lane) {
+            __syncthreads();
+            // 3. dE = sum_c 2 eci_c n_c (warp 0, fixed order), accept, write
+            if (warp == 0) {
+                Acc part = Acc(0);
+                for (int c = lane; c < n_cols; c += 32) { const int n = cnt[c]; if (n) { part += ecol[c] * (Acc)n; cnt[c] = 0; } }
+                part = warp_sum(part);
+                if (lane == 0) {
+                    const double dEd = (double)part;
+                    if (P.logu < -beta * dEd) {
+                        sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new;
+                        E += dEd; ++nacc;
+                    }
+                }
+            }
+        } else if (producer && lane == 0 && next) {
             bin_propose(jb, s + 1, t, prop[(s + 1) & 1]);
         }
         if (tid == 0) {
+            near_flag = 0;
             Emin = fmin(Emin, E);
             if (jb.E_samples && (s + 1) % jb.sample_interval == 0)
                 jb.E_samples[((s + 1) / jb.sample_interval - 1) * R + t] = E;
         }
         __syncthreads();
     }
-    if (sig_smem) {
+    if (sig_smem)
         for (int64_t i = tid; i < jb.N; i += nt) gsig[i] = sig[i];
-    }
     if (tid == 0) { jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc; }
 }
 
@@ -598,7 +642,8 @@ struct nce_ce_model {
     int32_t *T_b = nullptr, *T_uo = nullptr; uint8_t *T_pfc = nullptr; double *T_eci64 = nullptr; float *T_eci32 = nullptr;
     int32_t *err = nullptr;                  // device error word
     bool binary = false;                     // every point-function value is -1 or +1 (sign-parity kernel applies)
-    uint8_t *sbits = nullptr; double *eci2_64 = nullptr; float *eci2_32 = nullptr;
+    uint8_t *sbits = nullptr; uint16_t *bix = nullptr; uint8_t *rcol = nullptr; double *ecol2_64 = nullptr; float *ecol2_32 = nullptr;
+    int32_t n_cols = 0;
     double *energy_partial = nullptr; size_t energy_partial_n = 0;
     int device = 0;
     std::mutex mu;
@@ -618,7 +663,7 @@ static int upload(T *&dst, const T *src, size_t n) {
 
 static int free_model(nce_ce_model *m) {
     void *ptrs[] = {m->loc, m->pfc, m->eci64, m->eci32, m->rv_len, m->nb_b, m->nb_uo, m->pf64, m->pf32, m->act_b,
-                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->eci2_64, m->eci2_32,
+                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->bix, m->rcol, m->ecol2_64, m->ecol2_32,
                     m->energy_partial, m->staging_base};
     for (void *p : ptrs) if (p) cudaFree(p);
     delete m;
@@ -640,8 +685,9 @@ static CEJob make_job(const nce_ce_model *m, const nce_pt_state *st, const nce_p
     std::memset(&j, 0, sizeof(j));
     const bool p64 = ck ? ck->precision != 32 : true;
     j.loc = m->loc; j.pfc = m->pfc; j.eci = p64 ? (const void *)m->eci64 : (const void *)m->eci32;
-    if (bin) j.eci = p64 ? (const void *)m->eci2_64 : (const void *)m->eci2_32;
-    j.sbits = m->sbits;
+    j.sbits = m->sbits; j.bix = m->bix; j.rcol = m->rcol; j.n_cols = m->n_cols;
+    j.ecol2 = p64 ? (const void *)m->ecol2_64 : (const void *)m->ecol2_32;
+    (void)bin;
     j.rv_len = m->rv_len; j.nb_b = m->nb_b; j.nb_uo = m->nb_uo; j.pf = p64 ? (const void *)m->pf64 : (const void *)m->pf32;
     j.act_b = m->act_b; j.act_nb = m->act_nb; j.grp_cum = m->grp_cum;
     j.nB = m->nB; j.J = m->J; j.n_nbr = m->n_nbr; j.n_pfc = m->n_pfc; j.max_sp = m->max_sp;
@@ -759,8 +805,8 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
         size_t t_on = 0, t_off = 0; int64_t maxN = 0;
         for (int j = 0; j < n_jobs; ++j) {
             const nce_ce_model *m = hs[j];
-            t_on = std::max(t_on, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, accb, 0, true, false).total);
-            t_off = std::max(t_off, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, accb, 0, false, false).total);
+            t_on = std::max(t_on, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, m->n_cols, accb, 0, true, false).total);
+            t_off = std::max(t_off, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, m->n_cols, accb, 0, false, false).total);
             maxN = std::max(maxN, m->N);
         }
         const size_t limit = 200 * 1024, sigb = (size_t)((maxN + 15) / 16 * 16);
@@ -948,13 +994,32 @@ int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
             else if (v == -1.0) sb[(size_t)c * 4 + q] = 1;
             else bin = false;
         }
-    if (!rc && bin) {
-        std::vector<double> e2((size_t)t->nB * t->J); std::vector<float> f2(e2.size());
-        for (size_t i = 0; i < e2.size(); ++i) { e2[i] = 2.0 * t->Rv_eci[i]; f2[i] = 2.0f * (float)t->Rv_eci[i]; }
-        rc = upload(m->sbits, sb.data(), sb.size());
-        if (!rc) rc = upload(m->eci2_64, e2.data(), e2.size());
-        if (!rc) rc = upload(m->eci2_32, f2.data(), f2.size());
-        m->binary = !rc;
+    // column eci: every reverse row of one cluster-vector column must carry the same eci
+    if (bin && t->Rv_col && t->n_cols >= 1 && t->n_cols <= 255 && (int64_t)t->n_pfc * t->n_nbr <= 65535) {
+        std::vector<double> ec((size_t)t->n_cols, 0.0); std::vector<char> seen((size_t)t->n_cols, 0);
+        for (int b = 0; b < t->nB && bin; ++b)
+            for (int q = 0; q < t->Rv_len[b]; ++q) {
+                const int c = t->Rv_col[(size_t)b * t->J + q];
+                const double v = t->Rv_eci[(size_t)b * t->J + q];
+                if (c < 0 || c >= t->n_cols) { bin = false; break; }
+                if (!seen[c]) { seen[c] = 1; ec[c] = v; }
+                else if (ec[c] != v) { bin = false; break; }
+                if (q > 0 && c < t->Rv_col[(size_t)b * t->J + q - 1]) { bin = false; break; }   // rows sorted by column
+            }
+        if (bin && !rc) {
+            std::vector<double> e2(ec.size()); std::vector<float> f2(ec.size());
+            for (size_t i = 0; i < ec.size(); ++i) { e2[i] = 2.0 * ec[i]; f2[i] = 2.0f * (float)ec[i]; }
+            std::vector<uint16_t> bx(nl); std::vector<uint8_t> rc8((size_t)t->nB * t->J);
+            for (size_t i = 0; i < nl; ++i) bx[i] = (uint16_t)(t->Rv_pfc[i] * t->n_nbr + t->Rv_loc[i]);
+            for (size_t i = 0; i < rc8.size(); ++i) rc8[i] = (uint8_t)std::max(0, std::min(254, t->Rv_col[i]));
+            rc = upload(m->sbits, sb.data(), sb.size());
+            if (!rc) rc = upload(m->bix, bx.data(), bx.size());
+            if (!rc) rc = upload(m->rcol, rc8.data(), rc8.size());
+            if (!rc) rc = upload(m->ecol2_64, e2.data(), e2.size());
+            if (!rc) rc = upload(m->ecol2_32, f2.data(), f2.size());
+            m->n_cols = t->n_cols;
+            m->binary = !rc;
+        }
     }
     if (rc) { free_model(m); return rc; }
     *out = m;
