@@ -9,7 +9,7 @@ from __future__ import annotations
 _cache = {}
 
 
-def best_warps(gce, st, precision=64, path=0, candidates=(1, 2, 4, 8, 16), steps=300, seed=12345):
+def best_warps(gce, st, precision=64, path=0, candidates=(2, 4, 8, 16, 32), steps=300, seed=12345):
     import torch
     from .pt import PTState, run_chunk
     key = (id(gce), st.R, precision, path)

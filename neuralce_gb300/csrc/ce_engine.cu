@@ -57,6 +57,9 @@ struct CEJob {
     const uint8_t *rcol;   // (nB, J) cluster-vector column of each reverse row
     const void *ecol2;     // (n_cols) 2 * eci of each column, double or float
     int32_t n_cols;
+    const uint32_t *chunks;// (nB, max_chunks) column-aligned row chunks: col | start << 8 | len << 24
+    const int32_t *n_chunks; // (nB)
+    int32_t max_chunks;
 };
 
 struct CEBatch {
@@ -304,9 +307,9 @@ struct BinProp {
 };
 
 struct BinLayout {
-    size_t bix, rcol, ecol, sig, bits, cnt, total;
-    __host__ __device__ static BinLayout make(int nB, int J, int mo, int n_nbr, int n_pfc, int n_cols, size_t acc_bytes, int64_t N,
-                                                bool tables, bool sig_smem) {
+    size_t bix, rcol, chunk, nb, ecol, sig, bits, cnt, total;
+    __host__ __device__ static BinLayout make(int nB, int J, int mo, int n_nbr, int n_pfc, int n_cols, int max_chunks, size_t acc_bytes,
+                                                int64_t N, bool tables, bool sig_smem) {
         BinLayout L; size_t o = 0;
         auto al = [](size_t x, size_t a) { return (x + a - 1) / a * a; };
         if (tables) {
@@ -315,6 +318,8 @@ struct BinLayout {
         } else {
             L.bix = L.rcol = 0;
         }
+        L.chunk = o; o = al(o + sizeof(uint32_t) * (size_t)nB * max_chunks, 16);
+        L.nb = o; o = al(o + sizeof(int32_t) * 4 * (size_t)nB * n_nbr, 16);
         L.ecol = o; o = al(o + acc_bytes * (size_t)n_cols, 16);
         if (sig_smem) { L.sig = o; o = al(o + (size_t)N, 16); } else { L.sig = 0; }
         L.bits = o; o = al(o + 2 * (size_t)n_pfc * n_nbr, 16);
@@ -362,7 +367,7 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     const int ncons = nw > 1 ? nw - 1 : 1;            // consumer warps; the last warp (when there are two or more) draws proposals
     const bool producer = nw > 1 ? (warp == nw - 1) : (tid == 0);
     const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc, n_cols = jb.n_cols;
-    const BinLayout L = BinLayout::make(jb.nB, jb.J, MO, n_nbr, n_pfc, n_cols, sizeof(Acc), jb.N, bt.tables_in_smem, sig_smem);
+    const BinLayout L = BinLayout::make(jb.nB, jb.J, MO, n_nbr, n_pfc, n_cols, jb.max_chunks, sizeof(Acc), jb.N, bt.tables_in_smem, sig_smem);
     const uint16_t *tbix; const uint8_t *trcol;
     const size_t nl = (size_t)jb.nB * jb.J * MO, ne = (size_t)jb.nB * jb.J;
     if (bt.tables_in_smem) {
@@ -373,6 +378,11 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     } else {
         tbix = jb.bix; trcol = jb.rcol;
     }
+    uint32_t *chunks = reinterpret_cast<uint32_t *>(smem + L.chunk);        // [basis][k]: col | start << 8 | len << 24
+    for (int i = tid; i < jb.nB * jb.max_chunks; i += nt) chunks[i] = __ldg(jb.chunks + i);
+    int4 *nbt = reinterpret_cast<int4 *>(smem + L.nb);                          // [basis][n]: (uo0, uo1, uo2, basis)
+    for (int i = tid; i < jb.nB * n_nbr; i += nt) nbt[i] = make_int4(__ldg(jb.nb_uo + 3 * i), __ldg(jb.nb_uo + 3 * i + 1),
+                                                                      __ldg(jb.nb_uo + 3 * i + 2), __ldg(jb.nb_b + i));
     Acc *ecol = reinterpret_cast<Acc *>(smem + L.ecol);
     const Acc *gecol = reinterpret_cast<const Acc *>(jb.ecol2);
     int32_t *cnt = reinterpret_cast<int32_t *>(smem + L.cnt);
@@ -403,10 +413,9 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                 const int side = q >= n_nbr, n = side ? q - n_nbr : q;
                 const int b0 = side ? P.bb : P.ba;
                 const int32_t *k = side ? P.kb : P.ka;
-                const int e = b0 * n_nbr + n;
-                const int32_t *uo = jb.nb_uo + 3 * e;
-                const uint32_t st = ((((uint32_t)wrap_add(k[0], __ldg(uo), jb.d0) * (uint32_t)jb.d1 + (uint32_t)wrap_add(k[1], __ldg(uo + 1), jb.d1)) *
-                                      (uint32_t)jb.d2 + (uint32_t)wrap_add(k[2], __ldg(uo + 2), jb.d2)) * (uint32_t)jb.nB + (uint32_t)__ldg(jb.nb_b + e));
+                const int4 nbe = nbt[b0 * n_nbr + n];
+                const uint32_t st = ((((uint32_t)wrap_add(k[0], nbe.x, jb.d0) * (uint32_t)jb.d1 + (uint32_t)wrap_add(k[1], nbe.y, jb.d1)) *
+                                      (uint32_t)jb.d2 + (uint32_t)wrap_add(k[2], nbe.z, jb.d2)) * (uint32_t)jb.nB + (uint32_t)nbe.w);
                 const int so = sig[st];
                 const int sn = (st == (uint32_t)ia) ? sa_new : ((st == (uint32_t)ib) ? sb_new : so);
                 const int isa = side && (st == (uint32_t)ia);
@@ -420,17 +429,20 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                 if (lane == 0 && next) bin_propose(jb, s + 1, t, prop[(s + 1) & 1]);
             }
             if (!producer || nw == 1) {
-                // 2. rows: warp-contiguous blocks of 32 rows, exact integer parity counts per column run
-                const int Ja = __ldg(jb.rv_len + P.ba), Jb = __ldg(jb.rv_len + P.bb);
-                const int Jt = Ja + Jb;
+                // 2. rows: column-aligned chunks of <= 32 rows (one lane per row); one integer reduction per chunk
+                const int nca = __ldg(jb.n_chunks + P.ba), ncb = __ldg(jb.n_chunks + P.bb);
+                const int total = nca + ncb;
                 const bool near = near_flag != 0;
                 const int cw = nw > 1 ? warp : 0;
-                for (int base = cw * 32; base < Jt; base += ncons * 32) {
-                    const int v = base + lane;
-                    int sgn = 0, col = 0x7fffffff;
-                    if (v < Jt) {
-                        const int side = v >= Ja, rr = side ? v - Ja : v;
-                        const int b0 = side ? P.bb : P.ba;
+                auto chunk_count = [&](int k, int &col) -> int {
+                    const int side = k >= nca, kk = side ? k - nca : k;
+                    const int b0 = side ? P.bb : P.ba;
+                    const uint32_t d = chunks[b0 * jb.max_chunks + kk];
+                    col = (int)(d & 0xffu);
+                    const int start = (int)((d >> 8) & 0xffffu), len = (int)(d >> 24);
+                    int sgn = 0;
+                    if (lane < len) {
+                        const int rr = start + lane;
                         const uint16_t *bx = tbix + ((size_t)b0 * jb.J + rr) * MO;
                         const uint8_t *bs = bits + (size_t)side * n_pfc * n_nbr;
                         unsigned x = 0, y = 0;
@@ -442,27 +454,21 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
 #pragma unroll
                             for (int m = 0; m < MO; ++m) { const unsigned vv = bs[bx[m]]; x ^= vv; y |= vv; }
                         }
-                        col = trcol[(size_t)b0 * jb.J + rr] + (side ? 0x10000 : 0);   // runs never join across the two sites
                         const bool skip = side && near && (y & 4u);
-                        if (!skip && ((x ^ (x >> 1)) & 1u)) sgn = (x & 1u) ? 1 : -1;  // odd old parity: Pi -1 -> +1
+                        if (!skip && ((x ^ (x >> 1)) & 1u)) sgn = (x & 1u) ? 1 : -1;   // odd old parity: Pi -1 -> +1
                     }
-                    // segmented sum over runs of equal col within the warp
-                    int pre = sgn;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int up = __shfl_up_sync(0xffffffffu, pre, o);
-                        if (lane >= o) pre += up;
-                    }
-                    const int prev_col = __shfl_up_sync(0xffffffffu, col, 1);
-                    const int next_col = __shfl_down_sync(0xffffffffu, col, 1);
-                    const bool head = lane == 0 || prev_col != col;
-                    const bool tail = lane == 31 || next_col != col;
-                    const unsigned heads = __ballot_sync(0xffffffffu, head);
-                    const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
-                    const int before = __shfl_sync(0xffffffffu, pre, start > 0 ? start - 1 : 0);
-                    if (tail && col != 0x7fffffff) {
-                        const int run = pre - (start > 0 ? before : 0);
-                        if (run) atomicAdd(&cnt[col & 0xffff], run);
+                    return sgn;
+                };
+                for (int k = cw; k < total; k += 2 * ncons) {
+                    const int k2 = k + ncons;
+                    int c1 = 0, c2 = 0;
+                    const int s1 = chunk_count(k, c1);
+                    const int s2 = k2 < total ? chunk_count(k2, c2) : 0;
+                    const int n1 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s1);
+                    const int n2 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s2);
+                    if (lane == 0) {
+                        if (n1) atomicAdd(&cnt[c1], n1);
+                        if (n2) atomicAdd(&cnt[c2], n2);
                     }
                 }
             }
@@ -644,6 +650,7 @@ struct nce_ce_model {
     bool binary = false;                     // every point-function value is -1 or +1 (sign-parity kernel applies)
     uint8_t *sbits = nullptr; uint16_t *bix = nullptr; uint8_t *rcol = nullptr; double *ecol2_64 = nullptr; float *ecol2_32 = nullptr;
     int32_t n_cols = 0;
+    uint32_t *chunks = nullptr; int32_t *n_chunks = nullptr; int32_t max_chunks = 0;
     double *energy_partial = nullptr; size_t energy_partial_n = 0;
     int device = 0;
     std::mutex mu;
@@ -663,7 +670,7 @@ static int upload(T *&dst, const T *src, size_t n) {
 
 static int free_model(nce_ce_model *m) {
     void *ptrs[] = {m->loc, m->pfc, m->eci64, m->eci32, m->rv_len, m->nb_b, m->nb_uo, m->pf64, m->pf32, m->act_b,
-                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->bix, m->rcol, m->ecol2_64, m->ecol2_32,
+                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->bix, m->rcol, m->ecol2_64, m->ecol2_32, m->chunks, m->n_chunks,
                     m->energy_partial, m->staging_base};
     for (void *p : ptrs) if (p) cudaFree(p);
     delete m;
@@ -687,6 +694,7 @@ static CEJob make_job(const nce_ce_model *m, const nce_pt_state *st, const nce_p
     j.loc = m->loc; j.pfc = m->pfc; j.eci = p64 ? (const void *)m->eci64 : (const void *)m->eci32;
     j.sbits = m->sbits; j.bix = m->bix; j.rcol = m->rcol; j.n_cols = m->n_cols;
     j.ecol2 = p64 ? (const void *)m->ecol2_64 : (const void *)m->ecol2_32;
+    j.chunks = m->chunks; j.n_chunks = m->n_chunks; j.max_chunks = m->max_chunks;
     (void)bin;
     j.rv_len = m->rv_len; j.nb_b = m->nb_b; j.nb_uo = m->nb_uo; j.pf = p64 ? (const void *)m->pf64 : (const void *)m->pf32;
     j.act_b = m->act_b; j.act_nb = m->act_nb; j.grp_cum = m->grp_cum;
@@ -805,8 +813,8 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
         size_t t_on = 0, t_off = 0; int64_t maxN = 0;
         for (int j = 0; j < n_jobs; ++j) {
             const nce_ce_model *m = hs[j];
-            t_on = std::max(t_on, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, m->n_cols, accb, 0, true, false).total);
-            t_off = std::max(t_off, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, m->n_cols, accb, 0, false, false).total);
+            t_on = std::max(t_on, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, m->n_cols, m->max_chunks, accb, 0, true, false).total);
+            t_off = std::max(t_off, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, m->n_cols, m->max_chunks, accb, 0, false, false).total);
             maxN = std::max(maxN, m->N);
         }
         const size_t limit = 200 * 1024, sigb = (size_t)((maxN + 15) / 16 * 16);
@@ -995,7 +1003,7 @@ int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
             else bin = false;
         }
     // column eci: every reverse row of one cluster-vector column must carry the same eci
-    if (bin && t->Rv_col && t->n_cols >= 1 && t->n_cols <= 255 && (int64_t)t->n_pfc * t->n_nbr <= 65535) {
+    if (bin && t->Rv_col && t->n_cols >= 1 && t->n_cols <= 255 && (int64_t)t->n_pfc * t->n_nbr <= 65535 && t->J <= 65535) {
         std::vector<double> ec((size_t)t->n_cols, 0.0); std::vector<char> seen((size_t)t->n_cols, 0);
         for (int b = 0; b < t->nB && bin; ++b)
             for (int q = 0; q < t->Rv_len[b]; ++q) {
@@ -1017,6 +1025,26 @@ int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
             if (!rc) rc = upload(m->rcol, rc8.data(), rc8.size());
             if (!rc) rc = upload(m->ecol2_64, e2.data(), e2.size());
             if (!rc) rc = upload(m->ecol2_32, f2.data(), f2.size());
+            // column-aligned chunks of at most 32 consecutive rows
+            std::vector<std::vector<uint32_t>> ch(t->nB);
+            for (int b = 0; b < t->nB; ++b) {
+                int q = 0;
+                const int Jb = t->Rv_len[b];
+                while (q < Jb) {
+                    const int c = t->Rv_col[(size_t)b * t->J + q];
+                    int e = q;
+                    while (e < Jb && e - q < 32 && t->Rv_col[(size_t)b * t->J + e] == c) ++e;
+                    ch[b].push_back((uint32_t)c | ((uint32_t)q << 8) | ((uint32_t)(e - q) << 24));
+                    q = e;
+                }
+            }
+            size_t mx = 1;
+            for (auto &v : ch) mx = std::max(mx, v.size());
+            std::vector<uint32_t> flat((size_t)t->nB * mx, 0u); std::vector<int32_t> nch(t->nB);
+            for (int b = 0; b < t->nB; ++b) { nch[b] = (int32_t)ch[b].size(); std::copy(ch[b].begin(), ch[b].end(), flat.begin() + (size_t)b * mx); }
+            if (!rc) rc = upload(m->chunks, flat.data(), flat.size());
+            if (!rc) rc = upload(m->n_chunks, nch.data(), nch.size());
+            m->max_chunks = (int32_t)mx;
             m->n_cols = t->n_cols;
             m->binary = !rc;
         }
