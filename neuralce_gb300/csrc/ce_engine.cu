@@ -357,7 +357,7 @@ __device__ __forceinline__ void bin_propose(const CEJob &jb, int64_t s, int32_t 
 template <typename Acc, int MO>
 __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constant__ CEBatch bt, int32_t sig_smem) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ BinProp prop[2];
+    __shared__ BinProp prop[64];                      // ring of two batches of 32 proposals
     __shared__ int32_t near_flag;
     const int j = find_job(bt, blockIdx.x);
     const CEJob &jb = bt.job[j];
@@ -398,13 +398,18 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     double E = jb.E[r], Emin = jb.E_min_rep[r];
     int64_t nacc = 0;
     const int R = jb.R;
-    if (tid == 0) { near_flag = 0; if (jb.n_steps > 0) bin_propose(jb, 0, t, prop[0]); }
+    // proposals are drawn 32 at a time (one per lane of the producer warp), one batch ahead of their use
+    if (tid == 0) near_flag = 0;
+    if (warp == 0 && lane < jb.n_steps) bin_propose(jb, lane, t, prop[lane]);
     __syncthreads();
     for (int64_t s = 0; s < jb.n_steps; ++s) {
-        const BinProp &P = prop[s & 1];
+        const BinProp &P = prop[s & 63];
         const int64_t ia = P.ia, ib = P.ib;
+        if ((s & 31) == 0 && (nw == 1 ? true : warp == nw - 1)) {     // draw the next batch (steps s+32 .. s+63)
+            const int64_t q = s + 32 + lane;
+            if (q < jb.n_steps) bin_propose(jb, q, t, prop[q & 63]);
+        }
         const int sa = sig[ia], sb = sig[ib];
-        const bool next = (s + 1 < jb.n_steps);
         if (sa != sb) {
             const int sa_new = sb, sb_new = sa;
             // 1. neighbourhood bits (consumer threads); near_flag was cleared before the previous barrier
@@ -425,9 +430,6 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                     bs[c * n_nbr + n] = (uint8_t)(sbits[c * 4 + so] | (sbits[c * 4 + sn] << 1) | (isa << 2));
             }
             __syncthreads();
-            if (producer) {
-                if (lane == 0 && next) bin_propose(jb, s + 1, t, prop[(s + 1) & 1]);
-            }
             if (!producer || nw == 1) {
                 // 2. rows: column-aligned chunks of <= 32 rows (one lane per row); one integer reduction per chunk
                 const int nca = __ldg(jb.n_chunks + P.ba), ncb = __ldg(jb.n_chunks + P.bb);
@@ -486,8 +488,6 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                     }
                 }
             }
-        } else if (producer && lane == 0 && next) {
-            bin_propose(jb, s + 1, t, prop[(s + 1) & 1]);
         }
         if (tid == 0) {
             near_flag = 0;
