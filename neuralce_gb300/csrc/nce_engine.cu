@@ -31,7 +31,6 @@ int launch_exchange(int32_t R, double *E, double E_scale, const float *beta_slot
                     cudaStream_t s);
 
 constexpr int kMaxLayers = 4;
-constexpr int kTM = 16;                 // sites per GEMM tile
 constexpr double kFix = 1099511627776.0;      // 2^40
 constexpr double kInvFix = 1.0 / 1099511627776.0;
 
@@ -102,24 +101,32 @@ __device__ __forceinline__ float patched(const NceJob &jb, int lvl, const float 
     return cache[(size_t)q * Cin + c];
 }
 
-// Evaluate one layer for the sites list[pos0 .. pos0+cnt).  Inputs come from level lvl (cache patched with the step's
-// values, or unpatched when slot == nullptr).  Output per (m, n) delivered to `sink`.
+// Tile geometry of the layer GEMM: D/4 column groups of 4 outputs, 256/(D/4) site groups, TM sites per tile,
+// MS sites per thread (register micro-tile MS x 4).  D in {16, 32, 64, 128}.
+__host__ __device__ __forceinline__ int tile_tm(int D) { return D == 16 ? 64 : 32; }
+__host__ __device__ __forceinline__ int tile_kin(int P, int C0, int D) { return (1 + P) * (C0 > D ? C0 : D); }
+
+struct LayerW {            // weights of one layer as seen by the kernel (shared or global memory)
+    const float *W, *b, *G, *gb;
+};
+
+// Evaluate one layer for the sites list[pos0 .. pos0+cnt) (or direct0 + 0..cnt-1).  Inputs come from level lvl
+// (cache patched with the step's values, or unpatched when slot == nullptr).  For every site and group of 4
+// consecutive output columns, `sink(pos, col0, v[4])` receives the activated outputs (pos < 0: padding lane).
 template <typename Sink>
-__device__ void layer_tiles(const NceJob &jb, int lvl, const float *cache, const float *newl, const int32_t *slot, int32_t nlev,
-                            const int32_t *list, int64_t pos0, int64_t cnt, const int64_t *direct0, float *X, int32_t *src,
-                            Sink sink) {
+__device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const float *cache, const float *newl, const int32_t *slot,
+                            int32_t nlev, const int32_t *list, int64_t pos0, int64_t cnt, const int64_t *direct0, float *X,
+                            int32_t *src, Sink sink) {
     const NceDev &m = jb.m;
     const int Cin = lvl == 0 ? m.C0 : m.D, D = m.D, P = m.P, W = m.W;
-    const int Kin = (1 + P) * Cin;
+    const int Kin = (1 + P) * Cin, XS = Kin + 1;
     const int tid = threadIdx.x, nt = blockDim.x;
-    const float *Wc = m.Wc[lvl], *bias = m.bias[lvl], *G = m.gate ? m.G[lvl] : nullptr, *gb = m.gate ? m.gb[lvl] : nullptr;
-    const int mrow = tid / 16, ng = tid % 16;                         // 16 x 16 thread grid over (site, column group)
-    const int ncol = D / 16;
-    for (int64_t t0 = 0; t0 < cnt; t0 += kTM) {
-        const int tm = (int)min((int64_t)kTM, cnt - t0);
-        // gather: 1) source row of the site and of every shell partner (patched rows >= 0, cache rows -(q+1),
-        //            masked partner INT_MIN); 2) values and masked shell means
-        const int PW = 1 + P * W;
+    const int ncg = D / 4, SG = 256 / ncg, TM = tile_tm(D), MS = TM / SG;
+    const int cg = tid % ncg, sg = tid / ncg;
+    const int PW = 1 + P * W;
+    for (int64_t t0 = 0; t0 < cnt; t0 += TM) {
+        const int tm = (int)min((int64_t)TM, cnt - t0);
+        // 1) source row of each site and shell partner: patched rows >= 0, cache rows -(q+1), masked partner INT_MIN
         for (int idx = tid; idx < tm * PW; idx += nt) {
             const int mm = idx / PW, q = idx % PW;
             const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
@@ -137,19 +144,17 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const float *cache, const
             src[idx] = code;
         }
         __syncthreads();
+        // 2) X = [h | masked shell means] of the tile's sites
         for (int idx = tid; idx < tm * Cin; idx += nt) {
             const int mm = idx / Cin, c = idx % Cin;
             const int32_t *sr = src + mm * PW;
-            float *xr = X + (size_t)mm * Kin;
+            float *xr = X + (size_t)mm * XS;
             auto val = [&](int32_t code) {
                 return code >= 0 ? newl[(size_t)code * Cin + c] : cache[(size_t)(-(int64_t)code - 1) * Cin + c];
             };
             xr[c] = val(sr[0]);
-            int32_t b = 0;
-            {
-                const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
-                b = (int32_t)(s % m.nB);
-            }
+            const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
+            const int32_t b = (int32_t)(s % m.nB);
             for (int p = 0; p < P; ++p) {
                 float acc = 0.f;
                 for (int w = 0; w < W; ++w) {
@@ -160,44 +165,64 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const float *cache, const
             }
         }
         __syncthreads();
-        if (mrow < tm) {
-            float o[8], g[8];
-            for (int j = 0; j < ncol; ++j) { o[j] = __ldg(bias + ng + 16 * j); g[j] = gb ? __ldg(gb + ng + 16 * j) : 0.f; }
-            const float *xr = X + (size_t)mrow * Kin;
-            for (int kk = 0; kk < Kin; ++kk) {
-                const float xv = xr[kk];
-                const float *wr = Wc + (size_t)kk * D + ng;
-#pragma unroll 8
-                for (int j = 0; j < 8; ++j) if (j < ncol) o[j] = fmaf(xv, __ldg(wr + 16 * j), o[j]);
-                if (G && kk >= Cin) {
-                    const float *gr = G + (size_t)(kk - Cin) * D + ng;
-#pragma unroll 8
-                    for (int j = 0; j < 8; ++j) if (j < ncol) g[j] = fmaf(xv, __ldg(gr + 16 * j), g[j]);
+        // 3) register micro-tile GEMM: MS sites x 4 columns per thread
+        float o[4][4], g[4][4];
+        const float4 b4 = *reinterpret_cast<const float4 *>(LW.b + cg * 4);
+        const float4 gb4 = LW.G ? *reinterpret_cast<const float4 *>(LW.gb + cg * 4) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            o[i][0] = b4.x; o[i][1] = b4.y; o[i][2] = b4.z; o[i][3] = b4.w;
+            g[i][0] = gb4.x; g[i][1] = gb4.y; g[i][2] = gb4.z; g[i][3] = gb4.w;
+        }
+        for (int kk = 0; kk < Kin; ++kk) {
+            const float4 w4 = *reinterpret_cast<const float4 *>(LW.W + (size_t)kk * D + cg * 4);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                if (i < MS) {
+                    const float xv = X[(size_t)(sg + i * SG) * XS + kk];
+                    o[i][0] = fmaf(xv, w4.x, o[i][0]); o[i][1] = fmaf(xv, w4.y, o[i][1]);
+                    o[i][2] = fmaf(xv, w4.z, o[i][2]); o[i][3] = fmaf(xv, w4.w, o[i][3]);
                 }
             }
-            for (int j = 0; j < ncol; ++j) {
-                float v = act_fn(m.act, o[j]);
-                if (G) v *= 1.0f / (1.0f + expf(-g[j]));
-                o[j] = v;
+            if (LW.G && kk >= Cin) {
+                const float4 g4 = *reinterpret_cast<const float4 *>(LW.G + (size_t)(kk - Cin) * D + cg * 4);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    if (i < MS) {
+                        const float xv = X[(size_t)(sg + i * SG) * XS + kk];
+                        g[i][0] = fmaf(xv, g4.x, g[i][0]); g[i][1] = fmaf(xv, g4.y, g[i][1]);
+                        g[i][2] = fmaf(xv, g4.z, g[i][2]); g[i][3] = fmaf(xv, g4.w, g[i][3]);
+                    }
+                }
             }
-            sink(t0 + mrow, ng, o, ncol);
-        } else {
-            sink(-1, ng, nullptr, 0);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (i < MS) {
+                const int mm = sg + i * SG;
+                float v[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    float a = act_fn(m.act, o[i][q]);
+                    if (LW.G) a *= 1.0f / (1.0f + expf(-g[i][q]));
+                    v[q] = a;
+                }
+                sink(mm < tm ? t0 + mm : -1, cg * 4, v);
+            }
         }
         __syncthreads();
     }
 }
 
-// reduce over the 16 threads of a row group (same half warp)
-__device__ __forceinline__ float row16_sum(float v) {
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, 16);
+// sum over the D/4 lanes of one site (consecutive lanes of one warp)
+__device__ __forceinline__ float group_sum(float v, int ncg) {
+    for (int o = ncg >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, ncg);
     return v;
 }
 
 // One MC step of one replica (all threads of the block).  Returns through ctl (thread 0 reads dE).
 __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &ctl, unsigned long long *dh, float *X,
-                         int32_t *src, double &E, int64_t &nacc) {
+                         int32_t *src, const LayerW *LWs, const float *lin, const float *hw, double &E, int64_t &nacc) {
     const NceDev &m = jb.m;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int64_t N = m.N;
@@ -315,39 +340,35 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
     }
     __syncthreads();
     // 4. layers
+    const int ncg = m.D / 4;
     for (int lvl = 0; lvl < L; ++lvl) {
-        const int Cin = lvl == 0 ? m.C0 : m.D;
         const float *cache = lvl == 0 ? h0 : jb.hmid + ((size_t)(lvl - 1) * jb.R + r) * N * m.D;
         const float *newl = level_buf(jb, nb, lvl);
         const int nout = ctl.nl[lvl + 1];
         if (lvl + 1 < L) {
             float *outb = level_buf(jb, nb, lvl + 1);
             const int D = m.D;
-            layer_tiles(jb, lvl, cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
-                        [&](int64_t pos, int ng, const float *o, int ncol) {
-                            if (pos < 0) return;
-                            for (int jj = 0; jj < ncol; ++jj) outb[(size_t)pos * D + ng + 16 * jj] = o[jj];
+            layer_tiles(jb, lvl, LWs[lvl], cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
+                        [&](int64_t pos, int c0, const float *v) {
+                            if (pos >= 0) *reinterpret_cast<float4 *>(outb + (size_t)pos * D + c0) = make_float4(v[0], v[1], v[2], v[3]);
                         });
         } else {
-            const int D = m.D;
-            layer_tiles(jb, lvl, cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
-                        [&](int64_t pos, int ng, const float *o, int ncol) {
+            layer_tiles(jb, lvl, LWs[lvl], cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
+                        [&](int64_t pos, int c0, const float *v) {
                             float part = 0.f;
-                            if (pos >= 0) for (int jj = 0; jj < ncol; ++jj) part = fmaf(o[jj], __ldg(m.head_w + ng + 16 * jj), part);
-                            part = row16_sum(part);
-                            if (pos >= 0 && ng == 0) {
-                                const int64_t s = list[pos];
-                                // h0 (patched) . lin
+                            for (int q = 0; q < 4; ++q) part = fmaf(v[q], hw[c0 + q], part);
+                            part = group_sum(part, ncg);
+                            if (pos >= 0 && c0 == 0) {
+                                const int64_t st = list[pos];
                                 float l0 = 0.f;
-                                const int p0 = slot[s];
-                                const float *hr = (p0 >= 0 && p0 < n0) ? nb0 + (size_t)p0 * m.C0 : h0 + (size_t)s * m.C0;
-                                for (int c = 0; c < m.C0; ++c) l0 = fmaf(hr[c], __ldg(m.lin + c), l0);
-                                const bool active = m.Mb[s % m.nB] > 1;
+                                const int p0 = slot[st];
+                                const float *hr = (p0 >= 0 && p0 < n0) ? nb0 + (size_t)p0 * m.C0 : h0 + (size_t)st * m.C0;
+                                for (int c = 0; c < m.C0; ++c) l0 = fmaf(hr[c], lin[c], l0);
+                                const bool active = m.Mb[st % m.nB] > 1;
                                 const float ev = active ? l0 + part : 0.f;
                                 en[pos] = ev;
-                                atomicAdd(&ctl.dacc, (unsigned long long)llrint(((double)ev - (double)e[s]) * kFix));
+                                atomicAdd(&ctl.dacc, (unsigned long long)llrint(((double)ev - (double)e[st]) * kFix));
                             }
-                            (void)D;
                         });
         }
     }
@@ -355,7 +376,7 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         for (int p = tid; p < n0; p += nt) {
             const int64_t s = list[p];
             float l0 = 0.f;
-            for (int c = 0; c < m.C0; ++c) l0 = fmaf(nb0[(size_t)p * m.C0 + c], __ldg(m.lin + c), l0);
+            for (int c = 0; c < m.C0; ++c) l0 = fmaf(nb0[(size_t)p * m.C0 + c], lin[c], l0);
             const float ev = m.Mb[s % m.nB] > 1 ? l0 : 0.f;
             en[p] = ev;
             atomicAdd(&ctl.dacc, (unsigned long long)llrint(((double)ev - (double)e[s]) * kFix));
@@ -398,19 +419,77 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(256) nce_chunk_kernel(const __grid_constant__ NceJob jb) {
+// weights of all layers staged in shared memory when they fit (w_smem), else read from global memory
+__device__ void stage_weights(const NceDev &m, bool w_smem, float *wbuf, LayerW *LWs, const float *&lin, const float *&hw) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    size_t o = 0;
+    auto put = [&](const float *g, size_t n) -> const float * {
+        if (!g) return nullptr;
+        if (!w_smem) return g;
+        float *d = wbuf + o;
+        for (size_t i = tid; i < n; i += nt) d[i] = __ldg(g + i);
+        o += (n + 3) & ~(size_t)3;
+        return d;
+    };
+    for (int l = 0; l < m.depth; ++l) {
+        const int Cin = l == 0 ? m.C0 : m.D;
+        LWs[l].W = put(m.Wc[l], (size_t)(1 + m.P) * Cin * m.D);
+        LWs[l].b = put(m.bias[l], (size_t)m.D);
+        LWs[l].G = m.gate ? put(m.G[l], (size_t)m.P * Cin * m.D) : nullptr;
+        LWs[l].gb = m.gate ? put(m.gb[l], (size_t)m.D) : nullptr;
+    }
+    lin = put(m.lin, (size_t)m.C0);
+    hw = put(m.head_w, (size_t)(m.depth ? m.D : 4));
+    __syncthreads();
+}
+
+__host__ __device__ inline size_t weight_floats(int depth, int P, int C0, int D, int gate) {
+    size_t o = 0;
+    auto add = [&](size_t n) { o += (n + 3) & ~(size_t)3; };
+    for (int l = 0; l < depth; ++l) {
+        const int Cin = l == 0 ? C0 : D;
+        add((size_t)(1 + P) * Cin * D); add((size_t)D);
+        if (gate) { add((size_t)P * Cin * D); add((size_t)D); }
+    }
+    add((size_t)C0); add((size_t)(depth ? D : 4));
+    return o;
+}
+
+// shared-memory plan of the step kernel (byte offsets, 16-byte aligned): dh | X tile | partner codes | weights
+struct SmemPlan {
+    size_t dh, X, src, w, dh_bytes, tile_end, total_w;
+    __host__ __device__ static SmemPlan make(const NceDev &m) {
+        auto al = [](size_t x) { return (x + 15) / 16 * 16; };
+        SmemPlan p;
+        const int TM = tile_tm(m.D), Kmax = tile_kin(m.P, m.C0, m.D);
+        p.dh = 0; p.dh_bytes = al(sizeof(unsigned long long) * (size_t)m.n0max * m.C0);
+        p.X = p.dh_bytes;
+        p.src = al(p.X + sizeof(float) * (size_t)TM * (Kmax + 1));
+        p.tile_end = al(p.src + sizeof(int32_t) * (size_t)TM * (1 + m.P * m.W));
+        p.w = p.tile_end;
+        p.total_w = al(p.w + sizeof(float) * weight_floats(m.depth, m.P, m.C0, m.D, m.gate));
+        return p;
+    }
+};
+
+__global__ void __launch_bounds__(256) nce_chunk_kernel(const __grid_constant__ NceJob jb, int32_t w_smem) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ NceCtl ctl;
     const int r = blockIdx.x;
     if (r >= jb.R) return;
-    unsigned long long *dh = reinterpret_cast<unsigned long long *>(smem);
-    float *X = reinterpret_cast<float *>(smem + sizeof(unsigned long long) * (size_t)jb.m.n0max * jb.m.C0);
-    int32_t *src = reinterpret_cast<int32_t *>(X + (size_t)kTM * (1 + jb.m.P) * max(jb.m.C0, jb.m.D));
+    const NceDev &m = jb.m;
+    const SmemPlan sp = SmemPlan::make(m);
+    unsigned long long *dh = reinterpret_cast<unsigned long long *>(smem + sp.dh);
+    float *X = reinterpret_cast<float *>(smem + sp.X);
+    int32_t *src = reinterpret_cast<int32_t *>(smem + sp.src);
+    float *wbuf = reinterpret_cast<float *>(smem + sp.w);
+    LayerW lw[kMaxLayers]; const float *lin, *hw;
+    stage_weights(m, w_smem != 0, wbuf, lw, lin, hw);
     const int t = jb.slot_of_rep[r];
     double E = jb.E[r];
     int64_t nacc = 0;
     for (int64_t s = 0; s < jb.n_steps; ++s) {
-        nce_step(jb, r, t, s, ctl, dh, X, src, E, nacc);
+        nce_step(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, E, nacc);
         if (threadIdx.x == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
             jb.E_samples[((s + 1) / jb.sample_interval - 1) * jb.R + t] = E;
         __syncthreads();
@@ -451,33 +530,35 @@ __global__ void nce_h0_kernel(NceDev m, const int8_t *sigma, int32_t R, float *h
     }
 }
 
-// one layer on all sites: out = layer(in); e accumulation on the last layer
+// one layer on all sites: out = layer(in); e accumulation on the last layer (weights read from global memory)
 __global__ void __launch_bounds__(256) nce_layer_all_kernel(NceJob jb, int lvl, int32_t r, const float *in, float *out,
                                                              float *e_out, int64_t chunk0, int64_t chunk_n) {
     extern __shared__ __align__(16) unsigned char smem[];
-    float *X = reinterpret_cast<float *>(smem);
-    int32_t *src = reinterpret_cast<int32_t *>(X + (size_t)kTM * (1 + jb.m.P) * max(jb.m.C0, jb.m.D));
     const NceDev &m = jb.m;
-    const int64_t per = (chunk_n + gridDim.x - 1) / gridDim.x;
+    const int TM = tile_tm(m.D);
+    const SmemPlan sp = SmemPlan::make(m);
+    float *X = reinterpret_cast<float *>(smem + sp.X - sp.dh_bytes);
+    int32_t *src = reinterpret_cast<int32_t *>(smem + sp.src - sp.dh_bytes);
+    const int64_t per = ((chunk_n + gridDim.x - 1) / gridDim.x + TM - 1) / TM * TM;
     const int64_t a = chunk0 + (int64_t)blockIdx.x * per, cnt = max((int64_t)0, min(per, chunk0 + chunk_n - a));
     if (cnt <= 0) return;
     const float *h0 = jb.h0 + (size_t)r * m.N * m.C0;
-    const int D = m.D;
+    const int D = m.D, ncg = D / 4;
+    LayerW LW; LW.W = m.Wc[lvl]; LW.b = m.bias[lvl]; LW.G = m.gate ? m.G[lvl] : nullptr; LW.gb = m.gate ? m.gb[lvl] : nullptr;
     if (out) {
-        layer_tiles(jb, lvl, in, nullptr, nullptr, 0, nullptr, 0, cnt, &a, X, src, [&](int64_t pos, int ng, const float *o, int ncol) {
-            if (pos < 0) return;
-            for (int jj = 0; jj < ncol; ++jj) out[(size_t)(a + pos) * D + ng + 16 * jj] = o[jj];
+        layer_tiles(jb, lvl, LW, in, nullptr, nullptr, 0, nullptr, 0, cnt, &a, X, src, [&](int64_t pos, int c0, const float *v) {
+            if (pos >= 0) *reinterpret_cast<float4 *>(out + (size_t)(a + pos) * D + c0) = make_float4(v[0], v[1], v[2], v[3]);
         });
     } else {
-        layer_tiles(jb, lvl, in, nullptr, nullptr, 0, nullptr, 0, cnt, &a, X, src, [&](int64_t pos, int ng, const float *o, int ncol) {
+        layer_tiles(jb, lvl, LW, in, nullptr, nullptr, 0, nullptr, 0, cnt, &a, X, src, [&](int64_t pos, int c0, const float *v) {
             float part = 0.f;
-            if (pos >= 0) for (int jj = 0; jj < ncol; ++jj) part = fmaf(o[jj], __ldg(m.head_w + ng + 16 * jj), part);
-            part = row16_sum(part);
-            if (pos >= 0 && ng == 0) {
-                const int64_t s = a + pos;
+            for (int q = 0; q < 4; ++q) part = fmaf(v[q], __ldg(m.head_w + c0 + q), part);
+            part = group_sum(part, ncg);
+            if (pos >= 0 && c0 == 0) {
+                const int64_t st = a + pos;
                 float l0 = 0.f;
-                for (int c = 0; c < m.C0; ++c) l0 = fmaf(h0[(size_t)s * m.C0 + c], __ldg(m.lin + c), l0);
-                e_out[s] = (m.Mb[s % m.nB] > 1) ? l0 + part : 0.f;
+                for (int c = 0; c < m.C0; ++c) l0 = fmaf(h0[(size_t)st * m.C0 + c], __ldg(m.lin + c), l0);
+                e_out[st] = (m.Mb[st % m.nB] > 1) ? l0 + part : 0.f;
             }
         });
     }
@@ -536,12 +617,13 @@ static int dup(nce_nce_model *h, const T *src, size_t n, const T *&dst) {
 }
 
 static size_t tile_smem(const NceDev &m) {
-    const int Kin = (1 + m.P) * std::max(m.C0, m.D);
-    return sizeof(float) * (size_t)kTM * Kin + sizeof(int32_t) * (size_t)kTM * (1 + m.P * m.W);
+    const SmemPlan p = SmemPlan::make(m);
+    return p.tile_end - p.dh_bytes;
 }
 
-static size_t step_smem(const NceDev &m) {
-    return sizeof(unsigned long long) * (size_t)m.n0max * m.C0 + tile_smem(m);
+static size_t step_smem(const NceDev &m, bool w_smem) {
+    const SmemPlan p = SmemPlan::make(m);
+    return w_smem ? p.total_w : p.tile_end;
 }
 
 static int ensure_scratch(nce_nce_model *h, int32_t R) {
@@ -578,7 +660,7 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
     NCE_CHECK(d && out, "nce_nce_create: null argument");
     NCE_CHECK(d->depth >= 0 && d->depth <= kMaxLayers, "nce_nce_create: depth must be 0..%d", kMaxLayers);
     NCE_CHECK(d->C0 >= 1 && d->C0 <= 64, "nce_nce_create: layer-0 channels must be 1..64");
-    NCE_CHECK(d->depth == 0 || (d->D % 16 == 0 && d->D >= 16 && d->D <= 128), "nce_nce_create: width must be 16..128, multiple of 16");
+    NCE_CHECK(d->depth == 0 || d->D == 16 || d->D == 32 || d->D == 64 || d->D == 128, "nce_nce_create: width must be 16, 32, 64 or 128");
     NCE_CHECK(d->mo >= 1 && d->mo <= 8 && d->P >= 1 && d->P <= 8 && d->W >= 1, "nce_nce_create: mo/P/W out of range");
     NCE_CHECK(d->nB >= 1 && d->J >= 1 && d->n_cells == d->d[0] * d->d[1] * d->d[2] && d->n_cells <= 0xFFFFFFFFll,
               "nce_nce_create: bad lattice");
@@ -655,7 +737,7 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
         if (e == cudaSuccess) e = cudaMemset(h->err, 0, sizeof(int32_t));
         if (e != cudaSuccess) rc = fail(NCE_ERR_CUDA, "nce_nce_create: %s", cudaGetErrorString(e));
     }
-    if (!rc && step_smem(m) > 220 * 1024) rc = fail(NCE_ERR_UNSUPPORTED, "nce_nce_create: receptive field too large for shared memory");
+    if (!rc && step_smem(m, false) > 220 * 1024) rc = fail(NCE_ERR_UNSUPPORTED, "nce_nce_create: receptive field too large for shared memory");
     if (rc) {
         for (void *p : h->allocs) cudaFree(p);
         delete h;
@@ -687,7 +769,7 @@ int nce_nce_full_cache(nce_nce_handle h, const nce_nce_state *st, void *stream) 
     NceJob jb = make_nce_job(h, st);
     const size_t xs = tile_smem(m);
     NCE_CUDA(cudaFuncSetAttribute(nce_layer_all_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
-    const int blocks = (int)std::min<int64_t>((m.N + kTM - 1) / kTM, 1216);
+    const int blocks = (int)std::min<int64_t>((m.N + tile_tm(m.D) - 1) / tile_tm(m.D), 1216);
     if (m.depth == 0) {
         nce_e0_kernel<<<(int)std::min<int64_t>((tot + 255) / 256, 65535), 256, 0, s>>>(m, st->h0, tot, st->e);
         NCE_CUDA(cudaGetLastError());
@@ -736,9 +818,10 @@ int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_c
     jb.seed = ck->seed; jb.sample_interval = ck->sample_interval > 0 ? ck->sample_interval : 1; jb.E_samples = ck->E_samples;
     jb.dE_out = ck->dE_out; jb.force = ck->force;
     if (ck->n_steps == 0) return NCE_OK;
-    const size_t sm = step_smem(h->dev);
+    const bool w_smem = step_smem(h->dev, true) <= 220 * 1024;
+    const size_t sm = step_smem(h->dev, w_smem);
     NCE_CUDA(cudaFuncSetAttribute(nce_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    nce_chunk_kernel<<<st->R, 256, sm, (cudaStream_t)stream>>>(jb);
+    nce_chunk_kernel<<<st->R, 256, sm, (cudaStream_t)stream>>>(jb, w_smem ? 1 : 0);
     NCE_CUDA(cudaGetLastError());
     if (ck->exchange_rounds > 0 && st->R > 1) {
         NCE_CHECK(st->rep_of_slot && st->ladder_id && st->n_ex, "nce_nce_run_chunk: exchange needs rep_of_slot/ladder_id/n_ex");
