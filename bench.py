@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--chunk", type=int, default=5000)
     ap.add_argument("--workload", choices=["ce", "nce"], default="ce")
     ap.add_argument("--nce-steps", type=int, default=3, help="chunks of the NeuralCE side measurement (0 = skip)")
+    ap.add_argument("--nce-chunk", type=int, default=1000, help="MC steps per NeuralCE chunk")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -161,6 +162,7 @@ def run_reference(args, rank, world):
 
 
 def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, steps=3, warmup=1, seed=0):
+    exchange_every = min(exchange_every, chunk)
     """NeuralCE configuration 1: local receptive-field update, float32, R replicas 300-1400 K; a step is one
     chunk of ``chunk`` MC steps + chunk//exchange_every exchange rounds; full re-anchor every ceil(N/chunk)
     chunks (the reference driver's default)."""
@@ -210,6 +212,16 @@ def main():
         return
     import torch
     torch.cuda.set_device(local)
+    if args.workload == "nce":
+        from neuralce_gb300 import _lib
+        _lib.lib()
+        r = bench_nce(L=args.L, R=args.R, chunk=args.nce_chunk, steps=args.steps, warmup=args.warmup, seed=rank)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": r["value"], "unit": "swap attempts/s", "n_gpus": world, "steps": args.steps,
+                              "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                              "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": {"workload": r["config"]},
+                              "nce": r}), flush=True)
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")

@@ -199,6 +199,7 @@ typedef struct {
     double scale_eV;       /* dE in eV = dE * scale_eV (ys * N for model.pkl, 1 for eV-valued models) */
     int32_t n_groups, max_gb;
     const int32_t *act_b, *act_nb; const uint64_t *grp_cum;   /* swap groups, as in nce_ce_tables */
+    const uint16_t *Rv_loc;/* (nB, J, mo) index of each masked row member in its site's ball-0 list (ball_b/ball_uo order) */
 } nce_nce_desc;
 
 typedef struct nce_nce_model *nce_nce_handle;

@@ -49,6 +49,8 @@ struct NceDev {
     int32_t act, gate; double norm, scale_eV;
     int32_t n0max, nmax;
     int32_t n_groups, max_gb; const int32_t *act_b, *act_nb; const uint64_t *grp_cum;
+    const uint16_t *Rv_loc;                   // (nB, J, mo) index of each row member in its site's ball-0 list
+    int32_t w0max;                            // ball-0 entries per basis, maximum
 };
 
 struct NceJob {
@@ -68,9 +70,13 @@ struct NceJob {
 __device__ __forceinline__ int32_t wadd(int32_t k, int32_t u, int32_t d) { int32_t q = k + u; return q >= d ? q - d : q; }
 
 __device__ __forceinline__ void coords(const NceDev &m, int64_t i, int32_t &b, int32_t k[3]) {
-    b = (int32_t)(i % m.nB);
-    int64_t c = i / m.nB;
-    k[0] = (int32_t)(c / ((int64_t)m.d1 * m.d2)); k[1] = (int32_t)((c / m.d2) % m.d1); k[2] = (int32_t)(c % m.d2);
+    const uint32_t ii = (uint32_t)i, nB = (uint32_t)m.nB, d1 = (uint32_t)m.d1, d2 = (uint32_t)m.d2;   // N < 2^31
+    const uint32_t c = ii / nB;
+    b = (int32_t)(ii - c * nB);
+    const uint32_t c12 = c / d2;
+    k[2] = (int32_t)(c - c12 * d2);
+    k[0] = (int32_t)(c12 / d1);
+    k[1] = (int32_t)(c12 - (uint32_t)k[0] * d1);
 }
 
 __device__ __forceinline__ int64_t site_at(const NceDev &m, const int32_t k[3], const int32_t *uo, int32_t b) {
@@ -144,24 +150,34 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
             src[idx] = code;
         }
         __syncthreads();
-        // 2) X = [h | masked shell means] of the tile's sites
-        for (int idx = tid; idx < tm * Cin; idx += nt) {
-            const int mm = idx / Cin, c = idx % Cin;
-            const int32_t *sr = src + mm * PW;
-            float *xr = X + (size_t)mm * XS;
-            auto val = [&](int32_t code) {
-                return code >= 0 ? newl[(size_t)code * Cin + c] : cache[(size_t)(-(int64_t)code - 1) * Cin + c];
-            };
-            xr[c] = val(sr[0]);
-            const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
-            const int32_t b = (int32_t)(s % m.nB);
-            for (int p = 0; p < P; ++p) {
-                float acc = 0.f;
-                for (int w = 0; w < W; ++w) {
-                    const int32_t code = sr[1 + p * W + w];
-                    if (code != INT_MIN) acc += val(code);
+        // 2) X = [h | masked shell means] of the tile's sites: one warp per site, lanes over channels (coalesced rows)
+        {
+            const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+            for (int mm = warp; mm < tm; mm += nwarp) {
+                const int32_t *sr = src + mm * PW;
+                float *xr = X + (size_t)mm * XS;
+                const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
+                const int32_t b = (int32_t)((uint32_t)s % (uint32_t)m.nB);
+                for (int c = lane; c < Cin; c += 32) {
+                    auto val = [&](int32_t code) {
+                        return code >= 0 ? newl[(size_t)code * Cin + c] : cache[(size_t)(-(int64_t)code - 1) * Cin + c];
+                    };
+                    xr[c] = val(sr[0]);
+                    for (int p = 0; p < P; ++p) {
+                        const int32_t *pc = sr + 1 + p * W;
+                        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+                        int w = 0;
+                        for (; w + 4 <= W; w += 4) {
+                            const int32_t q0 = pc[w], q1 = pc[w + 1], q2 = pc[w + 2], q3 = pc[w + 3];
+                            if (q0 != INT_MIN) a0 += val(q0);
+                            if (q1 != INT_MIN) a1 += val(q1);
+                            if (q2 != INT_MIN) a2 += val(q2);
+                            if (q3 != INT_MIN) a3 += val(q3);
+                        }
+                        for (; w < W; ++w) { const int32_t q = pc[w]; if (q != INT_MIN) a0 += val(q); }
+                        xr[Cin + p * Cin + c] = ((a0 + a1) + (a2 + a3)) * m.Sh_inv[b * P + p];
+                    }
                 }
-                xr[Cin + p * Cin + c] = acc * m.Sh_inv[b * P + p];
             }
         }
         __syncthreads();
@@ -222,7 +238,8 @@ __device__ __forceinline__ float group_sum(float v, int ncg) {
 
 // One MC step of one replica (all threads of the block).  Returns through ctl (thread 0 reads dE).
 __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &ctl, unsigned long long *dh, float *X,
-                         int32_t *src, const LayerW *LWs, const float *lin, const float *hw, double &E, int64_t &nacc) {
+                         int32_t *src, const LayerW *LWs, const float *lin, const float *hw, int32_t *ent_site, int32_t *ent_pos,
+                         int8_t *ent_sig, double &E, int64_t &nacc) {
     const NceDev &m = jb.m;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int64_t N = m.N;
@@ -274,6 +291,7 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
             for (int q = q0 + tid; q < q1; q += nt) {
                 const int e0 = b * m.wL + q;
                 const int64_t s = site_at(m, k, m.ball_uo + 3 * e0, m.ball_b[e0]);
+                if (lvl == 0) ent_site[f * m.w0max + q] = (int32_t)s;
                 if (atomicCAS(&slot[s], -1, -2) == -1) {
                     const int p = atomicAdd(&ctl.cnt, 1);
                     list[p] = (int32_t)s; slot[s] = p;
@@ -291,6 +309,16 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         __syncthreads();
         return;
     }
+    // ball-0 entries of both flips: list position and occupancy (read once, reused by every row member)
+    for (int f = 0; f < 2; ++f) {
+        const int b = f ? ctl.bj : ctl.bi;
+        const int q1 = m.ball_end[b * (L + 1)];
+        for (int q = tid; q < q1; q += nt) {
+            const int32_t st = ent_site[f * m.w0max + q];
+            ent_pos[f * m.w0max + q] = slot[st];
+            ent_sig[f * m.w0max + q] = sig[st];
+        }
+    }
     // 3. layer-0 change (fixed point)
     for (int idx = tid; idx < n0 * m.C0; idx += nt) dh[idx] = 0ull;
     __syncthreads();
@@ -298,23 +326,24 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
     for (int rr = tid; rr < Jt; rr += nt) {
         const int f = rr >= m.J, jr = f ? rr - m.J : rr;
         const int b = f ? ctl.bj : ctl.bi;
-        const int32_t *k = f ? ctl.kj : ctl.ki;
         const int e = b * m.J + jr;
         const double w = m.Rv_w[e];
         if (w == 0.0) continue;
         double po = 1.0, pn = 1.0;
-        int64_t ms[8];
+        int32_t pos[8];
+        const int32_t *es = ent_site + f * m.w0max;
         for (int mm = 0; mm < m.mo; ++mm) {
             const int em = e * m.mo + mm;
-            const int64_t s = site_at(m, k, m.Rv_uo + 3 * em, m.Rv_b[em]);
-            ms[mm] = s;
             if (!m.Rv_m[em]) continue;
-            int so = sig[s], sn = so;
+            const int q = m.Rv_loc[em];
+            const int32_t st = es[q];
+            pos[mm] = ent_pos[f * m.w0max + q];
+            int so = ent_sig[f * m.w0max + q], sn = so;
             // flip 0: i -> ssj ; flip 1 (f = 1) evaluated on the configuration after flip 0
-            if (f == 0) { if (s == ctl.si) sn = ctl.ssj; }
+            if (f == 0) { if (st == (int32_t)ctl.si) sn = ctl.ssj; }
             else {
-                if (s == ctl.si) { so = ctl.ssj; sn = ctl.ssj; }
-                if (s == ctl.sj) sn = ctl.ssi;
+                if (st == (int32_t)ctl.si) { so = ctl.ssj; sn = ctl.ssj; }
+                if (st == (int32_t)ctl.sj) sn = ctl.ssi;
             }
             const int M = m.Mb[m.Rv_b[em]], pi = m.Rv_p[em];
             const double *th = m.theta + ((size_t)M * m.maxP + pi) * m.maxM;
@@ -326,7 +355,7 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         const int ch = m.Rv_col[e] + 1;
         for (int mm = 0; mm < m.mo; ++mm) {
             if (!m.Rv_m[e * m.mo + mm]) continue;
-            const int p = slot[ms[mm]];
+            const int p = pos[mm];
             if (p < 0 || p >= n0) { atomicOr(jb.err, 8); continue; }
             atomicAdd(&dh[(size_t)p * m.C0 + ch], (unsigned long long)fx);
         }
@@ -457,7 +486,7 @@ __host__ __device__ inline size_t weight_floats(int depth, int P, int C0, int D,
 
 // shared-memory plan of the step kernel (byte offsets, 16-byte aligned): dh | X tile | partner codes | weights
 struct SmemPlan {
-    size_t dh, X, src, w, dh_bytes, tile_end, total_w;
+    size_t dh, X, src, ent, w, dh_bytes, tile_end, total_w;
     __host__ __device__ static SmemPlan make(const NceDev &m) {
         auto al = [](size_t x) { return (x + 15) / 16 * 16; };
         SmemPlan p;
@@ -466,7 +495,8 @@ struct SmemPlan {
         p.X = p.dh_bytes;
         p.src = al(p.X + sizeof(float) * (size_t)TM * (Kmax + 1));
         p.tile_end = al(p.src + sizeof(int32_t) * (size_t)TM * (1 + m.P * m.W));
-        p.w = p.tile_end;
+        p.ent = p.tile_end;
+        p.w = al(p.ent + (sizeof(int32_t) * 2 + 1) * 2 * (size_t)m.w0max);
         p.total_w = al(p.w + sizeof(float) * weight_floats(m.depth, m.P, m.C0, m.D, m.gate));
         return p;
     }
@@ -483,13 +513,16 @@ __global__ void __launch_bounds__(256) nce_chunk_kernel(const __grid_constant__ 
     float *X = reinterpret_cast<float *>(smem + sp.X);
     int32_t *src = reinterpret_cast<int32_t *>(smem + sp.src);
     float *wbuf = reinterpret_cast<float *>(smem + sp.w);
+    int32_t *ent_site = reinterpret_cast<int32_t *>(smem + sp.ent);
+    int32_t *ent_pos = ent_site + 2 * m.w0max;
+    int8_t *ent_sig = reinterpret_cast<int8_t *>(ent_pos + 2 * m.w0max);
     LayerW lw[kMaxLayers]; const float *lin, *hw;
     stage_weights(m, w_smem != 0, wbuf, lw, lin, hw);
     const int t = jb.slot_of_rep[r];
     double E = jb.E[r];
     int64_t nacc = 0;
     for (int64_t s = 0; s < jb.n_steps; ++s) {
-        nce_step(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, E, nacc);
+        nce_step(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, ent_site, ent_pos, ent_sig, E, nacc);
         if (threadIdx.x == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
             jb.E_samples[((s + 1) / jb.sample_interval - 1) * jb.R + t] = E;
         __syncthreads();
@@ -623,7 +656,7 @@ static size_t tile_smem(const NceDev &m) {
 
 static size_t step_smem(const NceDev &m, bool w_smem) {
     const SmemPlan p = SmemPlan::make(m);
-    return w_smem ? p.total_w : p.tile_end;
+    return w_smem ? p.total_w : p.w;
 }
 
 static int ensure_scratch(nce_nce_model *h, int32_t R) {
@@ -711,11 +744,17 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
     m.maxM = d->maxM; m.maxP = d->maxP; m.d0 = (int32_t)d->d[0]; m.d1 = (int32_t)d->d[1]; m.d2 = (int32_t)d->d[2];
     m.N = N; m.n_cells = d->n_cells; m.wL = d->wL; m.act = d->act; m.gate = d->gate; m.norm = d->norm; m.scale_eV = d->scale_eV;
     m.head_b = (float)d->head_b;
-    m.n0max = 2 * n0max; m.nmax = 2 * nLmax;
+    m.n0max = 2 * n0max; m.nmax = 2 * nLmax; m.w0max = n0max;
+    NCE_CHECK(d->Rv_loc, "nce_nce_create: Rv_loc required");
+    for (size_t i = 0; i < nr; ++i)
+        if (d->Rv_m[i]) {
+            const int b = (int)(i / ((size_t)d->J * d->mo));
+            NCE_CHECK(d->Rv_loc[i] < d->ball_end[b * (d->depth + 1)], "nce_nce_create: Rv_loc outside ball 0");
+        }
     int rc = NCE_OK;
     auto chk = [&](int x) { if (!rc) rc = x; };
     chk(dup(h, d->Rv_b, nr, m.Rv_b)); chk(dup(h, d->Rv_uo, nr * 3, m.Rv_uo)); chk(dup(h, d->Rv_p, nr, m.Rv_p));
-    chk(dup(h, d->Rv_m, nr, m.Rv_m)); chk(dup(h, d->Rv_col, (size_t)d->nB * d->J, m.Rv_col)); chk(dup(h, d->Rv_w, (size_t)d->nB * d->J, m.Rv_w));
+    chk(dup(h, d->Rv_m, nr, m.Rv_m)); chk(dup(h, d->Rv_loc, nr, m.Rv_loc)); chk(dup(h, d->Rv_col, (size_t)d->nB * d->J, m.Rv_col)); chk(dup(h, d->Rv_w, (size_t)d->nB * d->J, m.Rv_w));
     chk(dup(h, d->Mb, (size_t)d->nB, m.Mb)); chk(dup(h, d->theta, (size_t)(d->maxM + 1) * d->maxP * d->maxM, m.theta));
     chk(dup(h, d->Sh_b, ns, m.Sh_b)); chk(dup(h, d->Sh_uo, ns * 3, m.Sh_uo)); chk(dup(h, d->Sh_m, ns, m.Sh_m));
     chk(dup(h, d->Sh_inv, (size_t)d->nB * d->P, m.Sh_inv));

@@ -113,6 +113,15 @@ class NCEModel:
                 bb_[b, q] = x; bo[b, q] = o
         U, d = g["U"], g["d"]
         a("ball_b", bb_, np.int32); a("ball_uo", np.mod(bo @ U.T, d), np.int32); a("ball_end", np.array(ends), np.int32)
+        # each masked reverse-row member as an index into its site's ball-0 list
+        rloc = np.zeros((nB, J, mo), np.uint16)
+        for b in range(nB):
+            pos0 = {it: q for q, it in enumerate(lists[b][:ends[b][0]])}
+            for jj in range(J):
+                for mm in range(mo):
+                    if g["Rv_m"][b, jj, mm] and g["Rv_v"][b, jj]:
+                        rloc[b, jj, mm] = pos0[(int(g["Rv_b"][b, jj, mm]), tuple(int(x) for x in g["Rv_off"][b, jj, mm]))]
+        a("Rv_loc", rloc, np.uint16)
         self.wL = wL
         p = self.params
         a("lin", p["lin"], np.float32)
@@ -136,7 +145,7 @@ class NCEModel:
             s.d[c] = int(d[c])
         s.n_cells = int(g["n_cells"])
         for f in ("Rv_b", "Rv_uo", "Rv_p", "Rv_col", "Rv_m", "Rv_w", "Mb", "theta", "Sh_b", "Sh_uo", "Sh_m", "Sh_inv",
-                  "ball_b", "ball_uo", "ball_end", "lin", "head_w", "mu", "sd", "act_b", "act_nb", "grp_cum"):
+                  "ball_b", "ball_uo", "ball_end", "lin", "head_w", "mu", "sd", "act_b", "act_nb", "grp_cum", "Rv_loc"):
             setattr(s, f, keep[f].ctypes.data)
         s.head_b = float(p["head"]["b"])
         for l in range(self.depth):
