@@ -109,7 +109,7 @@ __device__ __forceinline__ float patched(const NceJob &jb, int lvl, const float 
 
 // Tile geometry of the layer GEMM: D/4 column groups of 4 outputs, 256/(D/4) site groups, TM sites per tile,
 // MS sites per thread (register micro-tile MS x 4).  D in {16, 32, 64, 128}.
-__host__ __device__ __forceinline__ int tile_tm(int D) { return D == 16 ? 64 : 32; }
+__host__ __device__ __forceinline__ int tile_tm(int D) { return 4 * (256 / (D / 4)); }   // 4 sites per thread
 __host__ __device__ __forceinline__ int tile_kin(int P, int C0, int D) { return (1 + P) * (C0 > D ? C0 : D); }
 
 struct LayerW {            // weights of one layer as seen by the kernel (shared or global memory)
@@ -190,26 +190,25 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
             o[i][0] = b4.x; o[i][1] = b4.y; o[i][2] = b4.z; o[i][3] = b4.w;
             g[i][0] = gb4.x; g[i][1] = gb4.y; g[i][2] = gb4.z; g[i][3] = gb4.w;
         }
+        const float *x0 = X + (size_t)sg * XS, *x1 = x0 + (size_t)SG * XS, *x2 = x1 + (size_t)SG * XS, *x3 = x2 + (size_t)SG * XS;
+#pragma unroll 4
         for (int kk = 0; kk < Kin; ++kk) {
             const float4 w4 = *reinterpret_cast<const float4 *>(LW.W + (size_t)kk * D + cg * 4);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                if (i < MS) {
-                    const float xv = X[(size_t)(sg + i * SG) * XS + kk];
-                    o[i][0] = fmaf(xv, w4.x, o[i][0]); o[i][1] = fmaf(xv, w4.y, o[i][1]);
-                    o[i][2] = fmaf(xv, w4.z, o[i][2]); o[i][3] = fmaf(xv, w4.w, o[i][3]);
-                }
-            }
-            if (LW.G && kk >= Cin) {
+            const float v0 = x0[kk], v1 = x1[kk], v2 = x2[kk], v3 = x3[kk];
+            o[0][0] = fmaf(v0, w4.x, o[0][0]); o[0][1] = fmaf(v0, w4.y, o[0][1]); o[0][2] = fmaf(v0, w4.z, o[0][2]); o[0][3] = fmaf(v0, w4.w, o[0][3]);
+            o[1][0] = fmaf(v1, w4.x, o[1][0]); o[1][1] = fmaf(v1, w4.y, o[1][1]); o[1][2] = fmaf(v1, w4.z, o[1][2]); o[1][3] = fmaf(v1, w4.w, o[1][3]);
+            o[2][0] = fmaf(v2, w4.x, o[2][0]); o[2][1] = fmaf(v2, w4.y, o[2][1]); o[2][2] = fmaf(v2, w4.z, o[2][2]); o[2][3] = fmaf(v2, w4.w, o[2][3]);
+            o[3][0] = fmaf(v3, w4.x, o[3][0]); o[3][1] = fmaf(v3, w4.y, o[3][1]); o[3][2] = fmaf(v3, w4.z, o[3][2]); o[3][3] = fmaf(v3, w4.w, o[3][3]);
+        }
+        if (LW.G) {
+#pragma unroll 4
+            for (int kk = Cin; kk < Kin; ++kk) {
                 const float4 g4 = *reinterpret_cast<const float4 *>(LW.G + (size_t)(kk - Cin) * D + cg * 4);
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    if (i < MS) {
-                        const float xv = X[(size_t)(sg + i * SG) * XS + kk];
-                        g[i][0] = fmaf(xv, g4.x, g[i][0]); g[i][1] = fmaf(xv, g4.y, g[i][1]);
-                        g[i][2] = fmaf(xv, g4.z, g[i][2]); g[i][3] = fmaf(xv, g4.w, g[i][3]);
-                    }
-                }
+                const float v0 = x0[kk], v1 = x1[kk], v2 = x2[kk], v3 = x3[kk];
+                g[0][0] = fmaf(v0, g4.x, g[0][0]); g[0][1] = fmaf(v0, g4.y, g[0][1]); g[0][2] = fmaf(v0, g4.z, g[0][2]); g[0][3] = fmaf(v0, g4.w, g[0][3]);
+                g[1][0] = fmaf(v1, g4.x, g[1][0]); g[1][1] = fmaf(v1, g4.y, g[1][1]); g[1][2] = fmaf(v1, g4.z, g[1][2]); g[1][3] = fmaf(v1, g4.w, g[1][3]);
+                g[2][0] = fmaf(v2, g4.x, g[2][0]); g[2][1] = fmaf(v2, g4.y, g[2][1]); g[2][2] = fmaf(v2, g4.z, g[2][2]); g[2][3] = fmaf(v2, g4.w, g[2][3]);
+                g[3][0] = fmaf(v3, g4.x, g[3][0]); g[3][1] = fmaf(v3, g4.y, g[3][1]); g[3][2] = fmaf(v3, g4.z, g[3][2]); g[3][3] = fmaf(v3, g4.w, g[3][3]);
             }
         }
 #pragma unroll
@@ -502,7 +501,7 @@ struct SmemPlan {
     }
 };
 
-__global__ void __launch_bounds__(256) nce_chunk_kernel(const __grid_constant__ NceJob jb, int32_t w_smem) {
+__global__ void __launch_bounds__(256, 1) nce_chunk_kernel(const __grid_constant__ NceJob jb, int32_t w_smem) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ NceCtl ctl;
     const int r = blockIdx.x;
@@ -564,7 +563,7 @@ __global__ void nce_h0_kernel(NceDev m, const int8_t *sigma, int32_t R, float *h
 }
 
 // one layer on all sites: out = layer(in); e accumulation on the last layer (weights read from global memory)
-__global__ void __launch_bounds__(256) nce_layer_all_kernel(NceJob jb, int lvl, int32_t r, const float *in, float *out,
+__global__ void __launch_bounds__(256, 1) nce_layer_all_kernel(NceJob jb, int lvl, int32_t r, const float *in, float *out,
                                                              float *e_out, int64_t chunk0, int64_t chunk_n) {
     extern __shared__ __align__(16) unsigned char smem[];
     const NceDev &m = jb.m;
