@@ -158,24 +158,43 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                 float *xr = X + (size_t)mm * XS;
                 const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
                 const int32_t b = (int32_t)((uint32_t)s % (uint32_t)m.nB);
-                for (int c = lane; c < Cin; c += 32) {
-                    auto val = [&](int32_t code) {
-                        return code >= 0 ? newl[(size_t)code * Cin + c] : cache[(size_t)(-(int64_t)code - 1) * Cin + c];
-                    };
-                    xr[c] = val(sr[0]);
-                    for (int p = 0; p < P; ++p) {
-                        const int32_t *pc = sr + 1 + p * W;
-                        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-                        int w = 0;
-                        for (; w + 4 <= W; w += 4) {
-                            const int32_t q0 = pc[w], q1 = pc[w + 1], q2 = pc[w + 2], q3 = pc[w + 3];
-                            if (q0 != INT_MIN) a0 += val(q0);
-                            if (q1 != INT_MIN) a1 += val(q1);
-                            if (q2 != INT_MIN) a2 += val(q2);
-                            if (q3 != INT_MIN) a3 += val(q3);
+                // two channels per lane (c, c + 32), all partner loads of a group of 8 issued before summing
+                const int c0 = lane, c1 = lane + 32;
+                const bool h0ok = c0 < Cin, h1ok = c1 < Cin;
+                auto row = [&](int32_t code) -> const float * {
+                    return code >= 0 ? newl + (size_t)code * Cin : cache + (size_t)(-(int64_t)code - 1) * Cin;
+                };
+                {
+                    const float *rr = row(sr[0]);
+                    if (h0ok) xr[c0] = rr[c0];
+                    if (h1ok) xr[c1] = rr[c1];
+                }
+                for (int p = 0; p < P; ++p) {
+                    const int32_t *pc = sr + 1 + p * W;
+                    float s0 = 0.f, s1 = 0.f;
+                    for (int w0 = 0; w0 < W; w0 += 8) {
+                        float va[8], vb[8];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const int32_t q = (w0 + u < W) ? pc[w0 + u] : INT_MIN;
+                            const bool ok = q != INT_MIN;
+                            const float *rr = ok ? row(q) : cache;
+                            va[u] = (ok && h0ok) ? rr[c0] : 0.f;
+                            vb[u] = (ok && h1ok) ? rr[c1] : 0.f;
                         }
-                        for (; w < W; ++w) { const int32_t q = pc[w]; if (q != INT_MIN) a0 += val(q); }
-                        xr[Cin + p * Cin + c] = ((a0 + a1) + (a2 + a3)) * m.Sh_inv[b * P + p];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) { s0 += va[u]; s1 += vb[u]; }
+                    }
+                    const float inv = m.Sh_inv[b * P + p];
+                    if (h0ok) xr[Cin + p * Cin + c0] = s0 * inv;
+                    if (h1ok) xr[Cin + p * Cin + c1] = s1 * inv;
+                }
+                for (int c = lane + 64; c < Cin; c += 32) {        // widths above 64 channels
+                    xr[c] = row(sr[0])[c];
+                    for (int p = 0; p < P; ++p) {
+                        float a0 = 0.f;
+                        for (int w = 0; w < W; ++w) { const int32_t q = sr[1 + p * W + w]; if (q != INT_MIN) a0 += row(q)[c]; }
+                        xr[Cin + p * Cin + c] = a0 * m.Sh_inv[b * P + p];
                     }
                 }
             }
