@@ -161,7 +161,7 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, steps=3, warmup=1, seed=0):
+def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, steps=3, warmup=1, seed=0, cluster=0):
     exchange_every = min(exchange_every, chunk)
     """NeuralCE configuration 1: local receptive-field update, float32, R replicas 300-1400 K; a step is one
     chunk of ``chunk`` MC steps + chunk//exchange_every exchange rounds; full re-anchor every ceil(N/chunk)
@@ -172,11 +172,22 @@ def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, step
     m, sig = nce_config(L, depth, width, seed)
     _, beta = ladder(R)
     st = NCEState(m, replica_configs(sig, R, 1 + seed), beta).full_cache()
+    tune = None
+    if cluster == 0:                                   # CTAs per replica: time a short chunk for each candidate
+        from neuralce_gb300.nce import NCEState as _S
+        tune = {}
+        for cl in (1, 2, 4):
+            sc = _S(m, replica_configs(sig, R, 1 + seed), beta).full_cache()
+            sc.run_chunk(4, 0, seed=1, cluster=cl)
+            a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a_.record(); sc.run_chunk(20, 4, seed=1, cluster=cl); b_.record(); torch.cuda.synchronize()
+            tune[cl] = a_.elapsed_time(b_)
+        cluster = min(tune, key=tune.get)
     anchor = max(1, -(-m.N // chunk))
     step = 0
     def one(k):
         nonlocal step
-        st.run_chunk(chunk, step, seed=99, exchange_rounds=max(chunk // exchange_every, 1)); step += chunk
+        st.run_chunk(chunk, step, seed=99, exchange_rounds=max(chunk // exchange_every, 1), cluster=cluster); step += chunk
         if (k + 1) % anchor == 0:
             st.full_cache()
     for k in range(warmup):
@@ -192,7 +203,8 @@ def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, step
     return {"value": R * chunk * steps / tot, "unit": "swap attempts/s", "ms_per_step": float(np.mean(ms)),
             "config": f"NeuralCE fp32: {m.N} sites, R={R}, depth {depth}, width {width}, SiLU, sum readout, 12-NN shell, "
                       f"chunk {chunk} steps + {max(chunk // exchange_every, 1)} exchange rounds, re-anchor every {anchor} chunks",
-            "receptive_field": [int(x) for x in m.keep['ball_end'][0]], "accept_rate": float(st.n_acc.sum().item()) / (R * step)}
+            "receptive_field": [int(x) for x in m.keep['ball_end'][0]], "accept_rate": float(st.n_acc.sum().item()) / (R * step),
+            "ctas_per_replica": cluster, "autotune_ms": tune}
 
 
 def workload_config(args, gce):

@@ -225,6 +225,7 @@ typedef struct {
     int32_t exchange_rounds; /* neighbour-slot exchange rounds at the chunk end (0 = none) */
     int32_t ex_parity; const double *ex_u; /* host-supplied exchange randoms: (rounds) parities packed in bits,
                                               ex_u (rounds, ceil((R-1)/2)); NULL -> Philox */
+    int32_t cluster;       /* CTAs (SMs) per replica: 1, 2, 4 or 8 (thread-block cluster) */
 } nce_nce_chunk;
 
 int nce_nce_create(const nce_nce_desc *desc, nce_nce_handle *out);

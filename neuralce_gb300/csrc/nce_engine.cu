@@ -22,7 +22,11 @@
 #include <mutex>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace nce {
 
@@ -97,6 +101,7 @@ struct NceCtl {
     int64_t si, sj; double u; int32_t same, bi, bj, ki[3], kj[3], ssi, ssj;
     int32_t cnt; int32_t nl[kMaxLayers + 1];
     unsigned long long dacc;
+    int32_t err, acc;
 };
 
 // value of level lvl at site q (patched by the step's new values), channel c
@@ -122,7 +127,7 @@ struct LayerW {            // weights of one layer as seen by the kernel (shared
 template <typename Sink>
 __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const float *cache, const float *newl, const int32_t *slot,
                             int32_t nlev, const int32_t *list, int64_t pos0, int64_t cnt, const int64_t *direct0, float *X,
-                            int32_t *src, Sink sink) {
+                            int32_t *src, Sink sink, int tile_begin = 0, int tile_stride = 1) {
     const NceDev &m = jb.m;
     const int Cin = lvl == 0 ? m.C0 : m.D, D = m.D, P = m.P, W = m.W;
     const int Kin = (1 + P) * Cin, XS = Kin + 1;
@@ -130,7 +135,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
     const int ncg = D / 4, SG = 256 / ncg, TM = tile_tm(D), MS = TM / SG;
     const int cg = tid % ncg, sg = tid / ncg;
     const int PW = 1 + P * W;
-    for (int64_t t0 = 0; t0 < cnt; t0 += TM) {
+    for (int64_t t0 = (int64_t)tile_begin * TM; t0 < cnt; t0 += (int64_t)tile_stride * TM) {
         const int tm = (int)min((int64_t)TM, cnt - t0);
         // 1) source row of each site and shell partner: patched rows >= 0, cache rows -(q+1), masked partner INT_MIN
         for (int idx = tid; idx < tm * PW; idx += nt) {
@@ -254,10 +259,26 @@ __device__ __forceinline__ float group_sum(float v, int ncg) {
     return v;
 }
 
-// One MC step of one replica (all threads of the block).  Returns through ctl (thread 0 reads dE).
+// One MC step of one replica, run by a cluster of CL CTAs (CL = 1: a single CTA).  The leader (rank 0) draws the
+// proposal, builds the receptive field and the layer-0 change; every level's tiles are spread over the cluster;
+// dE partials reach the leader through distributed shared memory; the leader decides and every CTA commits its
+// share.  Every branch that changes the number of cluster barriers is taken from the leader's flags.
+struct NceCtx {
+    int rank, CL;
+    NceCtl *lctl;                       // the leader's control block (own block on the leader)
+};
+
+template <bool CLUSTER>
+__device__ __forceinline__ void csync() {
+    if (CLUSTER) { __threadfence(); cg::this_cluster().sync(); } else { __syncthreads(); }
+}
+
+template <bool CLUSTER>
 __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &ctl, unsigned long long *dh, float *X,
                          int32_t *src, const LayerW *LWs, const float *lin, const float *hw, int32_t *ent_site, int32_t *ent_pos,
-                         int8_t *ent_sig, double &E, int64_t &nacc) {
+                         int8_t *ent_sig, double &E, int64_t &nacc, const NceCtx &cx) {
+    const bool leader = cx.rank == 0;
+    const int CL = cx.CL, rank = cx.rank;
     const NceDev &m = jb.m;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int64_t N = m.N;
@@ -269,6 +290,7 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
     float *nb = jb.newbuf + (size_t)r * jb.scratch_stride;
     float *en = jb.e_new + (size_t)r * m.nmax;
     const int L = m.depth;
+    if (leader) {
     if (tid == 0) {
         int64_t i, j; double u;
         if (jb.prop_a) { i = jb.prop_a[s_idx * jb.R + t]; j = jb.prop_b[s_idx * jb.R + t]; u = jb.prop_u[s_idx * jb.R + t]; }
@@ -292,14 +314,11 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         int same = 1;
         if (i < 0 || j < 0 || i >= N || j >= N) { atomicOr(jb.err, 1); }
         else { ctl.ssi = sig[i]; ctl.ssj = sig[j]; same = ctl.ssi == ctl.ssj; }
-        ctl.si = i; ctl.sj = j; ctl.u = u; ctl.same = same; ctl.cnt = 0; ctl.dacc = 0ull;
+        ctl.si = i; ctl.sj = j; ctl.u = u; ctl.same = same; ctl.cnt = 0; ctl.dacc = 0ull; ctl.err = 0; ctl.acc = 0;
         if (!same) { coords(m, i, ctl.bi, ctl.ki); coords(m, j, ctl.bj, ctl.kj); }
     }
     __syncthreads();
-    if (ctl.same) {
-        if (tid == 0) { ++nacc; if (jb.dE_out) jb.dE_out[s_idx * jb.R + t] = 0.0; }
-        return;
-    }
+    if (!ctl.same) {
     // 2. nested unique receptive field
     for (int lvl = 0; lvl <= L; ++lvl) {
         for (int f = 0; f < 2; ++f) {
@@ -320,13 +339,12 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         if (tid == 0) ctl.nl[lvl] = ctl.cnt;
         __syncthreads();
     }
-    const int n0 = ctl.nl[0];
-    if (n0 > m.n0max || ctl.nl[L] > m.nmax) {         // cannot happen for consistent tables; refuse instead of overflow
-        if (tid == 0) atomicOr(jb.err, 4);
-        for (int p = tid; p < min(ctl.nl[L], m.nmax); p += nt) slot[list[p]] = -1;
+    if (ctl.nl[0] > m.n0max || ctl.nl[L] > m.nmax) {   // cannot happen for consistent tables; refuse instead of overflow
+        if (tid == 0) { atomicOr(jb.err, 4); ctl.err = 1; }
         __syncthreads();
-        return;
     }
+    if (!ctl.err) {
+    const int n0 = ctl.nl[0];
     // ball-0 entries of both flips: list position and occupancy (read once, reused by every row member)
     for (int f = 0; f < 2; ++f) {
         const int b = f ? ctl.bj : ctl.bi;
@@ -379,12 +397,29 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         }
     }
     __syncthreads();
-    float *nb0 = level_buf(jb, nb, 0);
+    float *nb0w = level_buf(jb, nb, 0);
     for (int idx = tid; idx < n0 * m.C0; idx += nt) {
         const int p = idx / m.C0, c = idx % m.C0;
         const int64_t s = list[p];
-        nb0[idx] = h0[(size_t)s * m.C0 + c] + (float)((double)(long long)dh[idx] * kInvFix);
+        nb0w[idx] = h0[(size_t)s * m.C0 + c] + (float)((double)(long long)dh[idx] * kInvFix);
     }
+    }   // !err
+    }   // !same
+    }   // leader
+    csync<CLUSTER>();
+    if (CLUSTER && !leader) {                          // broadcast of the leader's control block
+        if (tid == 0) ctl = *cx.lctl;
+        __syncthreads();
+    }
+    if (ctl.same || ctl.err) {
+        if (leader && tid == 0 && ctl.same) { ++nacc; if (jb.dE_out) jb.dE_out[s_idx * jb.R + t] = 0.0; }
+        if (ctl.err) for (int p = tid + rank * nt; p < min(ctl.nl[L], m.nmax); p += nt * CL) slot[list[p]] = -1;
+        csync<CLUSTER>();
+        return;
+    }
+    const int n0 = ctl.nl[0];
+    float *nb0 = level_buf(jb, nb, 0);
+    if (!leader && tid == 0) ctl.dacc = 0ull;
     __syncthreads();
     // 4. layers
     const int ncg = m.D / 4;
@@ -398,7 +433,8 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
             layer_tiles(jb, lvl, LWs[lvl], cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
                         [&](int64_t pos, int c0, const float *v) {
                             if (pos >= 0) *reinterpret_cast<float4 *>(outb + (size_t)pos * D + c0) = make_float4(v[0], v[1], v[2], v[3]);
-                        });
+                        }, rank, CL);
+            csync<CLUSTER>();
         } else {
             layer_tiles(jb, lvl, LWs[lvl], cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
                         [&](int64_t pos, int c0, const float *v) {
@@ -416,11 +452,11 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
                                 en[pos] = ev;
                                 atomicAdd(&ctl.dacc, (unsigned long long)llrint(((double)ev - (double)e[st]) * kFix));
                             }
-                        });
+                        }, rank, CL);
         }
     }
     if (L == 0) {
-        for (int p = tid; p < n0; p += nt) {
+        for (int p = tid + rank * nt; p < n0; p += nt * CL) {
             const int64_t s = list[p];
             float l0 = 0.f;
             for (int c = 0; c < m.C0; ++c) l0 = fmaf(nb0[(size_t)p * m.C0 + c], lin[c], l0);
@@ -430,9 +466,10 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         }
     }
     __syncthreads();
-    // 5. accept
-    __shared__ int acc_flag;
-    if (tid == 0) {
+    if (CLUSTER && !leader && tid == 0 && ctl.dacc) atomicAdd(&cx.lctl->dacc, ctl.dacc);   // partial dE to the leader
+    csync<CLUSTER>();
+    // 5. accept (leader), broadcast, commit split over the cluster
+    if (leader && tid == 0) {
         const double dE = (double)(long long)ctl.dacc * kInvFix / m.norm;
         const double dEeV = dE * m.scale_eV;
         const double beta = (double)jb.beta_slot[t];
@@ -440,14 +477,18 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         if (jb.force > 0) a = 1;
         else if (jb.force < 0) a = 0;
         else a = (dEeV <= 0.0) || (ctl.u < exp(-beta * dEeV));
-        acc_flag = a;
+        ctl.acc = a;
         if (jb.dE_out) jb.dE_out[s_idx * jb.R + t] = dE;
         if (a) { sig[ctl.si] = (int8_t)ctl.ssj; sig[ctl.sj] = (int8_t)ctl.ssi; E += dE; ++nacc; }
     }
+    csync<CLUSTER>();
+    __shared__ int acc_flag;
+    if (tid == 0) acc_flag = CLUSTER ? cx.lctl->acc : ctl.acc;
     __syncthreads();
     const int nL = ctl.nl[L];
+    const int ts = tid + rank * nt, tstr = nt * CL;
     if (acc_flag) {
-        for (int idx = tid; idx < n0 * m.C0; idx += nt) {
+        for (int idx = ts; idx < n0 * m.C0; idx += tstr) {
             const int p = idx / m.C0, c = idx % m.C0;
             h0[(size_t)list[p] * m.C0 + c] = nb0[idx];
         }
@@ -455,15 +496,15 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
             float *hm = jb.hmid + ((size_t)(lvl - 1) * jb.R + r) * N * m.D;
             const float *src = level_buf(jb, nb, lvl);
             const int nl = ctl.nl[lvl];
-            for (int idx = tid; idx < nl * m.D; idx += nt) {
+            for (int idx = ts; idx < nl * m.D; idx += tstr) {
                 const int p = idx / m.D, c = idx % m.D;
                 hm[(size_t)list[p] * m.D + c] = src[idx];
             }
         }
-        for (int p = tid; p < nL; p += nt) e[list[p]] = en[p];
+        for (int p = ts; p < nL; p += tstr) e[list[p]] = en[p];
     }
-    for (int p = tid; p < nL; p += nt) slot[list[p]] = -1;
-    __syncthreads();
+    for (int p = ts; p < nL; p += tstr) slot[list[p]] = -1;
+    csync<CLUSTER>();
 }
 
 // weights of all layers staged in shared memory when they fit (w_smem), else read from global memory
@@ -539,13 +580,47 @@ __global__ void __launch_bounds__(256, 1) nce_chunk_kernel(const __grid_constant
     const int t = jb.slot_of_rep[r];
     double E = jb.E[r];
     int64_t nacc = 0;
+    NceCtx cx; cx.rank = 0; cx.CL = 1; cx.lctl = &ctl;
     for (int64_t s = 0; s < jb.n_steps; ++s) {
-        nce_step(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, ent_site, ent_pos, ent_sig, E, nacc);
+        nce_step<false>(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, ent_site, ent_pos, ent_sig, E, nacc, cx);
         if (threadIdx.x == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
             jb.E_samples[((s + 1) / jb.sample_interval - 1) * jb.R + t] = E;
         __syncthreads();
     }
     if (threadIdx.x == 0) { jb.E[r] = E; jb.n_acc[r] += nacc; }
+}
+
+// the same chunk with each replica spread over a thread-block cluster of gridDim.x / R CTAs
+__global__ void __launch_bounds__(256, 1) nce_chunk_cluster_kernel(const __grid_constant__ NceJob jb, int32_t w_smem) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ NceCtl ctl;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int CL = (int)cluster.num_blocks(), rank = (int)cluster.block_rank();
+    const int r = blockIdx.x / CL;
+    if (r >= jb.R) return;                           // whole clusters only: gridDim.x == R * CL
+    const NceDev &m = jb.m;
+    const SmemPlan sp = SmemPlan::make(m);
+    unsigned long long *dh = reinterpret_cast<unsigned long long *>(smem + sp.dh);
+    float *X = reinterpret_cast<float *>(smem + sp.X);
+    int32_t *src = reinterpret_cast<int32_t *>(smem + sp.src);
+    float *wbuf = reinterpret_cast<float *>(smem + sp.w);
+    int32_t *ent_site = reinterpret_cast<int32_t *>(smem + sp.ent);
+    int32_t *ent_pos = ent_site + 2 * m.w0max;
+    int8_t *ent_sig = reinterpret_cast<int8_t *>(ent_pos + 2 * m.w0max);
+    LayerW lw[kMaxLayers]; const float *lin, *hw;
+    stage_weights(m, w_smem != 0, wbuf, lw, lin, hw);
+    NceCtx cx; cx.rank = rank; cx.CL = CL; cx.lctl = cluster.map_shared_rank(&ctl, 0);
+    cluster.sync();
+    const int t = jb.slot_of_rep[r];
+    double E = jb.E[r];
+    int64_t nacc = 0;
+    for (int64_t s = 0; s < jb.n_steps; ++s) {
+        nce_step<true>(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, ent_site, ent_pos, ent_sig, E, nacc, cx);
+        if (rank == 0 && threadIdx.x == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
+            jb.E_samples[((s + 1) / jb.sample_interval - 1) * jb.R + t] = E;
+    }
+    if (rank == 0 && threadIdx.x == 0) { jb.E[r] = E; jb.n_acc[r] += nacc; }
+    cluster.sync();                                   // no CTA leaves while others may still read its shared memory
 }
 
 // ── full cache ─────────────────────────────────────────────────────────────────────────────────────
@@ -877,8 +952,22 @@ int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_c
     if (ck->n_steps == 0) return NCE_OK;
     const bool w_smem = step_smem(h->dev, true) <= 220 * 1024;
     const size_t sm = step_smem(h->dev, w_smem);
-    NCE_CUDA(cudaFuncSetAttribute(nce_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    nce_chunk_kernel<<<st->R, 256, sm, (cudaStream_t)stream>>>(jb, w_smem ? 1 : 0);
+    const int CL = ck->cluster > 1 ? ck->cluster : 1;
+    NCE_CHECK(CL == 1 || CL == 2 || CL == 4 || CL == 8, "nce_nce_run_chunk: cluster must be 1, 2, 4 or 8");
+    if (CL == 1 || h->dev.depth == 0) {
+        NCE_CUDA(cudaFuncSetAttribute(nce_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        nce_chunk_kernel<<<st->R, 256, sm, (cudaStream_t)stream>>>(jb, w_smem ? 1 : 0);
+    } else {
+        NCE_CUDA(cudaFuncSetAttribute(nce_chunk_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        cudaLaunchConfig_t cfg; std::memset(&cfg, 0, sizeof(cfg));
+        cfg.gridDim = dim3((unsigned)(st->R * CL)); cfg.blockDim = dim3(256); cfg.dynamicSmemBytes = sm;
+        cfg.stream = (cudaStream_t)stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)CL; attr[0].val.clusterDim.y = 1; attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr; cfg.numAttrs = 1;
+        NCE_CUDA(cudaLaunchKernelEx(&cfg, nce_chunk_cluster_kernel, jb, (int32_t)(w_smem ? 1 : 0)));
+    }
     NCE_CUDA(cudaGetLastError());
     if (ck->exchange_rounds > 0 && st->R > 1) {
         NCE_CHECK(st->rep_of_slot && st->ladder_id && st->n_ex, "nce_nce_run_chunk: exchange needs rep_of_slot/ladder_id/n_ex");

@@ -61,8 +61,8 @@ def test_full_cache_matches_oracle(cuda, nipt_model, which):
         assert np.abs(st.e[r].cpu().numpy() - c["e"]).max() < 1e-4
 
 
-@pytest.mark.parametrize("which", ["pkl", "bench"])
-def test_local_chain_matches_oracle(cuda, nipt_model, which):
+@pytest.mark.parametrize("which,cluster", [("pkl", 1), ("bench", 1), ("pkl", 4), ("bench", 2)])
+def test_local_chain_matches_oracle(cuda, nipt_model, which, cluster):
     """Every proposal accepted (force=1): per-step dE vs the oracle's local_delta chain, then the carried energy
     and the caches vs a full rebuild."""
     torch = cuda
@@ -79,7 +79,7 @@ def test_local_chain_matches_oracle(cuda, nipt_model, which):
     st = NCEState(m, m.sig0[None].astype(np.int8), np.ones(1)).full_cache()
     dE = torch.zeros((T, 1), dtype=torch.float64, device="cuda")
     props = tuple(torch.as_tensor(x.reshape(T, 1)).cuda() for x in (pi, pj, pu))
-    st.run_chunk(T, 0, proposals=props, dE_out=dE, force=1)
+    st.run_chunk(T, 0, proposals=props, dE_out=dE, force=1, cluster=cluster)
     torch.cuda.synchronize()
     cache = orc.full_cache(m.sig0.astype(np.int64))
     E0 = orc.energy_of(cache)
@@ -97,7 +97,8 @@ def test_local_chain_matches_oracle(cuda, nipt_model, which):
     assert int(st.n_acc[0].item()) == T
 
 
-def test_metropolis_trajectory_matches_oracle(cuda, nipt_model):
+@pytest.mark.parametrize("cluster", [1, 4])
+def test_metropolis_trajectory_matches_oracle(cuda, nipt_model, cluster):
     """Seeded host stream, Metropolis at 600 K on 4 replicas: bit-exact occupancy vs the oracle."""
     torch = cuda
     from neuralce_gb300.nce import NCEState
@@ -111,7 +112,7 @@ def test_metropolis_trajectory_matches_oracle(cuda, nipt_model):
     pi = rng.integers(0, m.N, (T, R)).astype(np.int32); pj = rng.integers(0, m.N, (T, R)).astype(np.int32)
     pu = 1.0 - rng.random((T, R))
     st = NCEState(m, sig, beta).full_cache()
-    st.run_chunk(T, 0, proposals=tuple(torch.as_tensor(x).cuda() for x in (pi, pj, pu)))
+    st.run_chunk(T, 0, proposals=tuple(torch.as_tensor(x).cuda() for x in (pi, pj, pu)), cluster=cluster)
     torch.cuda.synchronize()
     for r in range(R):
         cache = orc.full_cache(sig[r].astype(np.int64))
@@ -119,3 +120,20 @@ def test_metropolis_trajectory_matches_oracle(cuda, nipt_model):
         if margin > 1e-4:
             assert np.array_equal(st.sigma[r].cpu().numpy(), s_ref.astype(np.int8))
             assert int(st.n_acc[r].item()) == nacc
+
+
+def test_cluster_equals_single_cta(cuda):
+    """Philox stream with exchanges: a replica spread over a 4-CTA cluster gives the same trajectory as one CTA."""
+    torch = cuda
+    from neuralce_gb300.nce import NCEState
+    from neuralce_gb300.workloads import ladder, replica_configs
+    m, orc = _model_bench(3, 6)
+    R = 4
+    _, beta = ladder(R)
+    sig = replica_configs(m.sig0, R, 3)
+    a = NCEState(m, sig, beta).full_cache(); b = NCEState(m, sig, beta).full_cache()
+    a.run_chunk(40, 0, seed=5, exchange_rounds=2, cluster=1)
+    b.run_chunk(40, 0, seed=5, exchange_rounds=2, cluster=4)
+    torch.cuda.synchronize()
+    assert torch.equal(a.sigma, b.sigma) and torch.equal(a.rep_of_slot, b.rep_of_slot)
+    assert torch.equal(a.n_acc, b.n_acc) and torch.allclose(a.E, b.E, rtol=0, atol=0)
