@@ -46,7 +46,8 @@ def parse():
     ap.add_argument("--L", type=int, default=8)
     ap.add_argument("--R", type=int, default=32)
     ap.add_argument("--chunk", type=int, default=5000)
-    ap.add_argument("--workload", choices=["ce", "nce"], default="ce")
+    ap.add_argument("--workload", choices=["ce", "nce", "ce-batch"], default="ce")
+    ap.add_argument("--batch-steps", type=int, default=3, help="chunks of the batched-form side measurement (0 = skip)")
     ap.add_argument("--nce-steps", type=int, default=3, help="chunks of the NeuralCE side measurement (0 = skip)")
     ap.add_argument("--nce-chunk", type=int, default=1000, help="MC steps per NeuralCE chunk")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -207,6 +208,52 @@ def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, step
             "ctas_per_replica": cluster, "autotune_ms": tune}
 
 
+def bench_batch(steps=3, warmup=1, chunk=5000, reanchor=10000, n_jobs=64, alone_jobs=8, alone_steps=2000):
+    """Configuration 2: 64 independent CE cells (L ~ U{4..32}, x_Pt ~ U[0.1, 0.9], R ~ U{16,32,64}) in one launch
+    per chunk, float32 dE with a float64 re-anchor every ``reanchor`` steps; compared with running jobs alone in
+    the float64 kernel (throughput of the first ``alone_jobs`` jobs, each alone)."""
+    import torch
+    from neuralce_gb300.batch import CEBatch, tune_warps
+    from neuralce_gb300.pt import PTState, run_chunk
+    from neuralce_gb300.workloads import ce_batch_config
+    from neuralce_gb300.autotune import best_warps
+    t0 = time.time()
+    jobs = ce_batch_config(n_jobs)
+    setup = time.time() - t0
+    w, tune = tune_warps(jobs, 32)
+    b = CEBatch(jobs, precision=32, warps=w)
+    for _ in range(warmup):
+        b.run_chunk(chunk)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    drift = 0.0
+    for k in range(steps):
+        ev[k][0].record(); b.run_chunk(chunk)
+        if b.step % reanchor == 0:
+            drift = max(drift, b.reanchor())
+        ev[k][1].record()
+    torch.cuda.synchronize()
+    tot = sum(a.elapsed_time(c) for a, c in ev) / 1e3
+    value = b.attempts_per_step * chunk * steps / tot
+    # each job alone in the float64 kernel
+    att = 0; secs = 0.0
+    for j in jobs[:alone_jobs]:
+        st = PTState(j["sigma"], j["gce"].batched_energy(torch.as_tensor(j["sigma"]).cuda()).cpu().numpy(), j["beta"],
+                     np.zeros(j["R"], np.int32))
+        wj, _ = best_warps(j["gce"], st, 64)
+        run_chunk(j["gce"], st, 50, 0, 5, 64, wj, do_exchange=True)
+        a_, c_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a_.record(); run_chunk(j["gce"], st, alone_steps, 50, 5, 64, wj, do_exchange=True); c_.record(); torch.cuda.synchronize()
+        secs += a_.elapsed_time(c_) / 1e3; att += j["R"] * alone_steps
+    alone = att / secs
+    return {"value": value, "unit": "swap attempts/s", "ms_per_step": 1e3 * tot / steps,
+            "config": f"{n_jobs} CE jobs in one launch per chunk: L~U{{4..32}} ({min(j['N'] for j in jobs)}-{max(j['N'] for j in jobs)} sites), "
+                      f"x_Pt~U[0.1,0.9], R~U{{16,32,64}} ({b.attempts_per_step} replicas), fp32 dE, fp64 re-anchor every {reanchor} steps, "
+                      f"chunk {chunk} steps + exchange",
+            "fp64_single_job_alone": alone, "ratio_vs_fp64_single_job": value / alone, "max_reanchor_drift_eV": drift,
+            "warps_per_replica": w, "autotune_ms": tune, "setup_s": setup}
+
+
 def workload_config(args, gce):
     return {"workload": f"CE parallel tempering fp{args.precision}: fcc Ni/Pt {args.L}x{args.L}x{args.L} conventional "
                         f"({gce.n_atoms} sites), R={args.R} replicas 300-1400 K, exchange every {args.chunk} steps, "
@@ -224,6 +271,16 @@ def main():
         return
     import torch
     torch.cuda.set_device(local)
+    if args.workload == "ce-batch":
+        from neuralce_gb300 import _lib
+        _lib.lib()
+        r = bench_batch(steps=args.steps, warmup=args.warmup)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": r["value"], "unit": "swap attempts/s", "n_gpus": world, "steps": args.steps,
+                              "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                              "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": {"workload": r["config"]},
+                              "batch": r}), flush=True)
+        return
     if args.workload == "nce":
         from neuralce_gb300 import _lib
         _lib.lib()
@@ -313,6 +370,9 @@ def main():
     nce_line = None
     if rank == 0 and args.nce_steps > 0:
         nce_line = bench_nce(steps=args.nce_steps)
+    batch_line = None
+    if rank == 0 and args.batch_steps > 0:
+        batch_line = bench_batch(steps=args.batch_steps)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, cores, sample = cpu_oracle_rate(args.L, R)
@@ -323,7 +383,7 @@ def main():
                 "vs_baseline": value / H100_PUBLISHED if (args.L == 8 and args.R == 32) else None,
                 "dtype": "f64" if args.precision == 64 else "f32", "data": "synthetic (seeded lattice, random-normal ECIs)",
                 "config": workload_config(args, gce), "clocks": clocks, "e2e": e2e, "gpu_launches": 2 * args.steps,
-                "roofline": roof, "cpu_baseline": cpu, "nce": nce_line,
+                "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "batch": batch_line,
                 "launch": {"warps_per_replica": args.warps, "path": ["auto", "general", "sign-parity"][args.path],
                            "autotune_ms": tuned},
                 "accept_rate": float(st.n_acc.sum().item()) / max(1, R * step)}

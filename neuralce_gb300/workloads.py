@@ -68,3 +68,24 @@ def nce_config(L=8, depth=3, width=64, seed=0, x_pt=0.5, model_seed=0):
     P = synthetic_model(len(cs.orbits) + 1, depth, width, 1, model_seed)
     m = NCEModel(cs, s, P, shell_edges=(0.0, 3.3), act="silu", pool="sum")
     return m, m.sig0
+
+
+def ce_batch_config(n_jobs=64, seed=2, L_range=(4, 32), R_choices=(16, 32, 64), T_min=300.0, T_max=1400.0):
+    """Batched CE workload: ``n_jobs`` independent cells with edge L ~ U{4..32} conventional cells (256 to 131,072
+    sites), Pt fraction ~ U[0.1, 0.9], replicas ~ U{16, 32, 64} on a geometric 300-1400 K ladder each; the CE
+    workload's cluster set and ECIs.  Returns a list of dicts (gce, sigma (R, N) int8, beta (R,), L, x_pt)."""
+    from .ce import GPUClusterExpansion
+    rng = np.random.default_rng(seed)
+    cs = cluster_space()
+    eci = synthetic_eci(cs, 0)
+    jobs = []
+    for k in range(n_jobs):
+        L = int(rng.integers(L_range[0], L_range[1] + 1))
+        x = float(rng.uniform(0.1, 0.9))
+        R = int(rng.choice(R_choices))
+        s = ce_structure(L, seed=1000 + k, x_pt=x)
+        gce = GPUClusterExpansion((cs, eci), s, energy_scale=len(s))
+        sig0 = gce.encode(s)
+        _, beta = ladder(R, T_min, T_max)
+        jobs.append(dict(gce=gce, sigma=replica_configs(sig0, R, 2000 + k), beta=beta, L=L, x_pt=x, R=R, N=len(s)))
+    return jobs
