@@ -60,6 +60,7 @@ struct CEJob {
     const uint32_t *chunks;// (nB, max_chunks) column-aligned row chunks: col | start << 8 | len << 24
     const int32_t *n_chunks; // (nB)
     int32_t max_chunks;
+    int32_t sig_smem;      // this job's occupancy is copied into shared memory for the chunk
 };
 
 struct CEBatch {
@@ -355,7 +356,7 @@ __device__ __forceinline__ void bin_propose(const CEJob &jb, int64_t s, int32_t 
 }
 
 template <typename Acc, int MO>
-__global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constant__ CEBatch bt, int32_t sig_smem) {
+__global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constant__ CEBatch bt, int32_t sig_budget) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ BinProp prop[64];                      // ring of two batches of 32 proposals
     __shared__ int32_t near_flag;
@@ -367,7 +368,9 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     const int ncons = nw > 1 ? nw - 1 : 1;            // consumer warps; the last warp (when there are two or more) draws proposals
     const bool producer = nw > 1 ? (warp == nw - 1) : (tid == 0);
     const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc, n_cols = jb.n_cols;
-    const BinLayout L = BinLayout::make(jb.nB, jb.J, MO, n_nbr, n_pfc, n_cols, jb.max_chunks, sizeof(Acc), jb.N, bt.tables_in_smem, sig_smem);
+    const int32_t sig_smem = jb.sig_smem;
+    const BinLayout L = BinLayout::make(jb.nB, jb.J, MO, n_nbr, n_pfc, n_cols, jb.max_chunks, sizeof(Acc), sig_budget, bt.tables_in_smem,
+                                        sig_budget > 0);
     const uint16_t *tbix; const uint8_t *trcol;
     const size_t nl = (size_t)jb.nB * jb.J * MO, ne = (size_t)jb.nB * jb.J;
     if (bt.tables_in_smem) {
@@ -817,11 +820,15 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
             t_off = std::max(t_off, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, m->n_cols, m->max_chunks, accb, 0, false, false).total);
             maxN = std::max(maxN, m->N);
         }
-        const size_t limit = 200 * 1024, sigb = (size_t)((maxN + 15) / 16 * 16);
+        const size_t limit = 200 * 1024;
         all_fit = t_on <= limit;
         const size_t base = all_fit ? t_on : t_off;
-        sig_smem = base + sigb <= limit ? 1 : 0;
-        smem = base + (sig_smem ? sigb : 0);
+        // occupancy in shared memory: the whole cell for one job when it fits, else a per-CTA budget that the
+        // jobs with small cells use (larger cells stay in global memory)
+        size_t budget = n_jobs == 1 ? (size_t)((maxN + 15) / 16 * 16) : (size_t)48 * 1024;
+        if (base + budget > limit) budget = n_jobs == 1 ? 0 : (limit > base ? (limit - base) / 16 * 16 : 0);
+        sig_smem = (int)budget;
+        smem = base + budget;
     } else {
         for (int j = 0; j < n_jobs; ++j) {
             size_t b; bool fit = precision == 64 ? tables_fit<double>(hs[j], warps, &b) : tables_fit<float>(hs[j], warps, &b);
@@ -841,6 +848,7 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
     int base = 0;
     for (int j = 0; j < n_jobs; ++j) {
         bt.job[j] = make_job(hs[j], &sts[j], &cks[j], base, use_bin);
+        bt.job[j].sig_smem = (use_bin && sig_smem > 0 && hs[j]->N <= sig_smem) ? 1 : 0;
         base += sts[j].R;
     }
     int64_t max_steps = 0;
