@@ -74,6 +74,7 @@ typedef struct {
     const uint64_t *grp_cum; /* (n_groups) cumulative choice thresholds in units of 2^-32 (last = 2^32) */
     const int32_t *Rv_col; /* (nB, J) cluster-vector column of each reverse row (non-decreasing within a site), or NULL */
     int32_t n_cols;        /* columns (<= 255 for the sign-parity kernel) */
+    const int8_t *Rv_slot; /* (nB, J) slot of the site in the template row (0 = the row's anchor), or NULL */
 } nce_ce_tables;
 
 typedef struct nce_ce_model *nce_ce_handle;

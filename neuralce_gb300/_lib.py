@@ -23,7 +23,7 @@ class NceCeTables(C.Structure):
                 ("Rv_len", vp), ("Rv_loc", vp), ("Rv_pfc", vp), ("Rv_eci", vp), ("nb_b", vp), ("nb_uo", vp),
                 ("Rt", i32), ("T_b", vp), ("T_uo", vp), ("T_pfc", vp), ("T_eci", vp), ("pf", vp),
                 ("n_groups", i32), ("max_gb", i32), ("act_b", vp), ("act_nb", vp), ("grp_cum", vp),
-                ("Rv_col", vp), ("n_cols", i32)]
+                ("Rv_col", vp), ("n_cols", i32), ("Rv_slot", vp)]
 
 
 class NcePtState(C.Structure):

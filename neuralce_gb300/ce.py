@@ -45,6 +45,7 @@ class CETables:
         g = np.floor(cum * 2.0 ** 32).astype(np.uint64); g[-1] = np.uint64(2 ** 32)
         self.grp_cum = _arr(g, np.uint64)
         self.Rv_col = _arr(tb["Rv_col"], np.int32)
+        self.Rv_slot = _arr(tb["Rv_slot"], np.int8)
         s = _lib.NceCeTables()
         s.nB, s.J, s.mo, s.n_nbr = nB, J, mo, tb["n_nbr"]
         s.n_pfc, s.max_sp = self.pf.shape[0], tb["max_sp"]
@@ -59,6 +60,7 @@ class CETables:
         s.n_groups, s.max_gb = self.act_b.shape
         s.act_b, s.act_nb, s.grp_cum = _lib.ptr(self.act_b), _lib.ptr(self.act_nb), _lib.ptr(self.grp_cum)
         s.Rv_col, s.n_cols = _lib.ptr(self.Rv_col), int(tb["n_cols"])
+        s.Rv_slot = _lib.ptr(self.Rv_slot)
         self.struct = s
 
 

@@ -148,12 +148,13 @@ def build_tables(cs: ClusterSpace, structure: Structure, parameters, energy_scal
     Rv_b = np.zeros((nB, J, mo), np.int32); Rv_off = np.zeros((nB, J, mo, 3), np.int64)
     Rv_bf = np.zeros((nB, J, mo), np.int32); Rv_eci = np.zeros((nB, J), np.float64)
     Rv_col = np.full((nB, J), len(cs.orbits), np.int32)      # padded rows: an extra column whose eci is 0
+    Rv_slot = np.full((nB, J), -1, np.int8)                    # slot of the site in the template row (0: the anchor)
     Rv_len = np.array([len(e) for e in ent], np.int32)
     for b in range(nB):
         Rv_b[b] = b
         for j, (r, m) in enumerate(ent[b]):
             Rv_b[b, j] = T_b[r]; Rv_off[b, j] = T_off[r] - T_off[r, m]; Rv_bf[b, j] = T_bf[r]; Rv_eci[b, j] = T_eci[r]
-            Rv_col[b, j] = tcol[r]
+            Rv_col[b, j] = tcol[r]; Rv_slot[b, j] = m
     Rv_uo = np.mod(Rv_off @ U.T, d).astype(np.int32)
     Rv_st = b_sl[Rv_b].astype(np.int32)
     # neighbourhood-compressed GPU layout (cell independent offsets; uo depends on the supercell)
@@ -190,7 +191,7 @@ def build_tables(cs: ClusterSpace, structure: Structure, parameters, energy_scal
                 max_sp=pf.shape[2], b_sl=b_sl, sl_species=sl_species, site_to_sl=site_to_sl,
                 T_b=T_b, T_uo=T_uo, T_bf=T_bf, T_st=T_st, T_eci=T_eci, T_msk=T_msk, T_off=T_off, Rt=Rt, mo=mo,
                 Rv_b=Rv_b, Rv_uo=Rv_uo, Rv_bf=Rv_bf, Rv_st=Rv_st, Rv_eci=Rv_eci, Rv_len=Rv_len, J=J, Rv_off=Rv_off,
-                Rv_col=Rv_col, n_cols=len(cs.orbits) + 1,
+                Rv_col=Rv_col, n_cols=len(cs.orbits) + 1, Rv_slot=Rv_slot,
                 Rv_loc=loc, Rv_pfc=Rv_pfc, nb_b=nb_b, nb_uo=nb_uo, nb_off=nb_off, n_nbr=n_nbr,
                 act_sl=act, act_b=act_b, act_nb=act_nb)
 

@@ -505,6 +505,65 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     if (tid == 0) { jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc; }
 }
 
+// Full energy on the sign-parity tables: E = zerolet + sum_c eci_c * (sum over sites of the parities of the rows anchored
+// at the site).  One warp per site: the site's neighbourhood bits are gathered once, then the anchored rows (each
+// cluster instance of the cell exactly once) are folded in column-aligned chunks of 32 into exact integer counts.
+__global__ void __launch_bounds__(256) ce_energy_bin_kernel(const __grid_constant__ CEJob jb, const int8_t *__restrict__ sigma,
+                                                             const uint16_t *__restrict__ erows, const uint32_t *__restrict__ echunks,
+                                                             const int32_t *__restrict__ n_echunks, int32_t max_echunks,
+                                                             const double *__restrict__ ecol, int32_t mo, double *partial) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc, n_cols = jb.n_cols;
+    long long *cnt = reinterpret_cast<long long *>(smem);                       // [warp][n_cols]
+    uint8_t *bits = reinterpret_cast<uint8_t *>(cnt + (size_t)nw * n_cols);      // [warp][n_pfc][n_nbr]
+    uint8_t *wb = bits + (size_t)warp * n_pfc * n_nbr;
+    long long *wc = cnt + (size_t)warp * n_cols;
+    for (int c = lane; c < n_cols; c += 32) wc[c] = 0;
+    const int r = blockIdx.y;
+    const int8_t *sig = sigma + (int64_t)r * jb.N;
+    for (int64_t s = (int64_t)blockIdx.x * nw + warp; s < jb.N; s += (int64_t)gridDim.x * nw) {
+        int32_t b, k[3];
+        site_coords32(jb, s, b, k);
+        for (int n = lane; n < n_nbr; n += 32) {
+            const int e = b * n_nbr + n;
+            const int32_t *uo = jb.nb_uo + 3 * e;
+            const uint32_t st = ((((uint32_t)wrap_add(k[0], __ldg(uo), jb.d0) * (uint32_t)jb.d1 + (uint32_t)wrap_add(k[1], __ldg(uo + 1), jb.d1)) *
+                                  (uint32_t)jb.d2 + (uint32_t)wrap_add(k[2], __ldg(uo + 2), jb.d2)) * (uint32_t)jb.nB + (uint32_t)__ldg(jb.nb_b + e));
+            const int so = sig[st];
+            for (int c = 0; c < n_pfc; ++c) wb[c * n_nbr + n] = jb.sbits[c * 4 + so];
+        }
+        __syncwarp();
+        const int nch = __ldg(n_echunks + b);
+        for (int q = 0; q < nch; ++q) {
+            const uint32_t d = __ldg(echunks + (size_t)b * max_echunks + q);
+            const int col = (int)(d & 0xffu), start = (int)((d >> 8) & 0xffffu), len = (int)(d >> 24);
+            int sgn = 0;
+            if (lane < len) {
+                const int j = __ldg(erows + (size_t)b * jb.J + start + lane);
+                const uint16_t *bx = jb.bix + ((size_t)b * jb.J + j) * mo;   // padded members: column 0, bits always 0
+                unsigned x = 0;
+                for (int m = 0; m < mo; ++m) x ^= wb[__ldg(bx + m)];
+                sgn = (x & 1u) ? -1 : 1;
+            }
+            const int n = (int)__reduce_add_sync(0xffffffffu, (unsigned)sgn);
+            if (lane == 0) wc[col] += n;
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    if (warp == 0) {
+        double part = 0.0;
+        for (int c = lane; c < n_cols; c += 32) {
+            long long tot = 0;
+            for (int w = 0; w < nw; ++w) tot += cnt[(size_t)w * n_cols + c];
+            part += ecol[c] * (double)tot;
+        }
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+        if (lane == 0) partial[(int64_t)r * gridDim.x + blockIdx.x] = part;
+    }
+}
+
 // chunk-end exchange of temperature slots, one CTA (thread 0) per job
 struct CEExJob {
     int32_t R; double *E; const float *beta_slot; int32_t *rep_of_slot, *slot_of_rep; const int32_t *ladder_id;
@@ -654,6 +713,8 @@ struct nce_ce_model {
     uint8_t *sbits = nullptr; uint16_t *bix = nullptr; uint8_t *rcol = nullptr; double *ecol2_64 = nullptr; float *ecol2_32 = nullptr;
     int32_t n_cols = 0;
     uint32_t *chunks = nullptr; int32_t *n_chunks = nullptr; int32_t max_chunks = 0;
+    uint16_t *erows = nullptr; uint32_t *echunks = nullptr; int32_t *n_echunks = nullptr; int32_t max_echunks = 0;
+    double *ecol1 = nullptr;                 // eci of each column (full-energy kernel)
     double *energy_partial = nullptr; size_t energy_partial_n = 0;
     int device = 0;
     std::mutex mu;
@@ -673,7 +734,7 @@ static int upload(T *&dst, const T *src, size_t n) {
 
 static int free_model(nce_ce_model *m) {
     void *ptrs[] = {m->loc, m->pfc, m->eci64, m->eci32, m->rv_len, m->nb_b, m->nb_uo, m->pf64, m->pf32, m->act_b,
-                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->bix, m->rcol, m->ecol2_64, m->ecol2_32, m->chunks, m->n_chunks,
+                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->bix, m->rcol, m->ecol2_64, m->ecol2_32, m->chunks, m->n_chunks, m->erows, m->echunks, m->n_echunks, m->ecol1,
                     m->energy_partial, m->staging_base};
     for (void *p : ptrs) if (p) cudaFree(p);
     delete m;
@@ -1012,19 +1073,19 @@ int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
         }
     // column eci: every reverse row of one cluster-vector column must carry the same eci
     if (bin && t->Rv_col && t->n_cols >= 1 && t->n_cols <= 255 && (int64_t)t->n_pfc * t->n_nbr <= 65535 && t->J <= 65535) {
-        std::vector<double> ec((size_t)t->n_cols, 0.0); std::vector<char> seen((size_t)t->n_cols, 0);
+        std::vector<double> colv((size_t)t->n_cols, 0.0); std::vector<char> seen((size_t)t->n_cols, 0);
         for (int b = 0; b < t->nB && bin; ++b)
             for (int q = 0; q < t->Rv_len[b]; ++q) {
                 const int c = t->Rv_col[(size_t)b * t->J + q];
                 const double v = t->Rv_eci[(size_t)b * t->J + q];
                 if (c < 0 || c >= t->n_cols) { bin = false; break; }
-                if (!seen[c]) { seen[c] = 1; ec[c] = v; }
-                else if (ec[c] != v) { bin = false; break; }
+                if (!seen[c]) { seen[c] = 1; colv[c] = v; }
+                else if (colv[c] != v) { bin = false; break; }
                 if (q > 0 && c < t->Rv_col[(size_t)b * t->J + q - 1]) { bin = false; break; }   // rows sorted by column
             }
         if (bin && !rc) {
-            std::vector<double> e2(ec.size()); std::vector<float> f2(ec.size());
-            for (size_t i = 0; i < ec.size(); ++i) { e2[i] = 2.0 * ec[i]; f2[i] = 2.0f * (float)ec[i]; }
+            std::vector<double> e2(colv.size()); std::vector<float> f2(colv.size());
+            for (size_t i = 0; i < colv.size(); ++i) { e2[i] = 2.0 * colv[i]; f2[i] = 2.0f * (float)colv[i]; }
             std::vector<uint16_t> bx(nl); std::vector<uint8_t> rc8((size_t)t->nB * t->J);
             for (size_t i = 0; i < nl; ++i) bx[i] = (uint16_t)(t->Rv_pfc[i] * t->n_nbr + t->Rv_loc[i]);
             for (size_t i = 0; i < rc8.size(); ++i) rc8[i] = (uint8_t)std::max(0, std::min(254, t->Rv_col[i]));
@@ -1054,6 +1115,33 @@ int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
             if (!rc) rc = upload(m->n_chunks, nch.data(), nch.size());
             m->max_chunks = (int32_t)mx;
             m->n_cols = t->n_cols;
+            // rows anchored at the site (slot 0): every cluster instance of the cell exactly once, for the full energy
+            if (t->Rv_slot && !rc) {
+                std::vector<uint16_t> er((size_t)t->nB * t->J, 0);
+                std::vector<std::vector<uint32_t>> ec(t->nB);
+                for (int b = 0; b < t->nB; ++b) {
+                    int ne = 0;
+                    for (int q = 0; q < t->Rv_len[b]; ++q)
+                        if (t->Rv_slot[(size_t)b * t->J + q] == 0) er[(size_t)b * t->J + ne++] = (uint16_t)q;
+                    int q = 0;
+                    while (q < ne) {
+                        const int c = t->Rv_col[(size_t)b * t->J + er[(size_t)b * t->J + q]];
+                        int e = q;
+                        while (e < ne && e - q < 32 && t->Rv_col[(size_t)b * t->J + er[(size_t)b * t->J + e]] == c) ++e;
+                        ec[b].push_back((uint32_t)c | ((uint32_t)q << 8) | ((uint32_t)(e - q) << 24));
+                        q = e;
+                    }
+                }
+                size_t me = 1;
+                for (auto &v : ec) me = std::max(me, v.size());
+                std::vector<uint32_t> ef((size_t)t->nB * me, 0u); std::vector<int32_t> ne((size_t)t->nB);
+                for (int b = 0; b < t->nB; ++b) { ne[b] = (int32_t)ec[b].size(); std::copy(ec[b].begin(), ec[b].end(), ef.begin() + (size_t)b * me); }
+                if (!rc) rc = upload(m->erows, er.data(), er.size());
+                if (!rc) rc = upload(m->echunks, ef.data(), ef.size());
+                if (!rc) rc = upload(m->n_echunks, ne.data(), ne.size());
+                if (!rc) rc = upload(m->ecol1, colv.data(), colv.size());
+                m->max_echunks = (int32_t)me;
+            }
             m->binary = !rc;
         }
     }
@@ -1082,6 +1170,28 @@ int nce_ce_energy(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t preci
         h->energy_partial = nullptr; h->energy_partial_n = 0;
         NCE_CUDA(cudaMalloc((void **)&h->energy_partial, sizeof(double) * need));
         h->energy_partial_n = need;
+    }
+    if (h->binary && h->erows) {
+        // sign-parity full energy: one warp per site, 8 warps per block
+        const int wpb = 8;
+        const int64_t nb2 = std::max<int64_t>(1, std::min<int64_t>((h->N + wpb - 1) / wpb, 2048));
+        const size_t need2 = (size_t)nb2 * R;
+        if (need2 > h->energy_partial_n) {
+            if (h->energy_partial) { cudaStreamSynchronize(s); cudaFree(h->energy_partial); }
+            h->energy_partial = nullptr; h->energy_partial_n = 0;
+            NCE_CUDA(cudaMalloc((void **)&h->energy_partial, sizeof(double) * need2));
+            h->energy_partial_n = need2;
+        }
+        nce_pt_chunk ck0; std::memset(&ck0, 0, sizeof(ck0)); ck0.precision = 64;
+        CEJob jb = make_job(h, nullptr, &ck0, 0, true);
+        const size_t sm = sizeof(long long) * wpb * h->n_cols + (size_t)wpb * h->n_pfc * h->n_nbr;
+        NCE_CUDA(cudaFuncSetAttribute(ce_energy_bin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        ce_energy_bin_kernel<<<dim3((unsigned)nb2, R), wpb * 32, sm, s>>>(jb, sigma, h->erows, h->echunks, h->n_echunks, h->max_echunks,
+                                                                          h->ecol1, h->mo, h->energy_partial);
+        NCE_CUDA(cudaGetLastError());
+        ce_energy_finish<<<(R + 127) / 128, 128, 0, s>>>(h->energy_partial, (int32_t)nb2, R, h->zerolet, E);
+        NCE_CUDA(cudaGetLastError());
+        return NCE_OK;
     }
     dim3 grid(nblk, R);
     if (precision == 64)
