@@ -506,48 +506,68 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
 }
 
 // Full energy on the sign-parity tables: E = zerolet + sum_c eci_c * (sum over sites of the parities of the rows anchored
-// at the site).  One warp per site: the site's neighbourhood bits are gathered once, then the anchored rows (each
-// cluster instance of the cell exactly once) are folded in column-aligned chunks of 32 into exact integer counts.
+// at the site).  Persistent blocks per replica stage the anchored-row tables in shared memory; one warp per site
+// gathers the site's neighbourhood bits, then folds the anchored rows (each cluster instance of the cell exactly
+// once) in column-aligned chunks of 32 into exact integer counts per column.
+template <int MO>
 __global__ void __launch_bounds__(256) ce_energy_bin_kernel(const __grid_constant__ CEJob jb, const int8_t *__restrict__ sigma,
                                                              const uint16_t *__restrict__ erows, const uint32_t *__restrict__ echunks,
                                                              const int32_t *__restrict__ n_echunks, int32_t max_echunks,
-                                                             const double *__restrict__ ecol, int32_t mo, double *partial) {
+                                                             const double *__restrict__ ecol, uint32_t sbit_mask, double *partial) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc, n_cols = jb.n_cols;
-    long long *cnt = reinterpret_cast<long long *>(smem);                       // [warp][n_cols]
-    uint8_t *bits = reinterpret_cast<uint8_t *>(cnt + (size_t)nw * n_cols);      // [warp][n_pfc][n_nbr]
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc, n_cols = jb.n_cols, nB = jb.nB, J = jb.J;
+    // shared: bix (nB, J, MO) | erows (nB, J) | echunks (nB, max_echunks) | nb (nB, n_nbr) int4 | counts | bits
+    size_t o = 0;
+    auto al = [](size_t x) { return (x + 15) / 16 * 16; };
+    uint16_t *sbix = reinterpret_cast<uint16_t *>(smem + o); o = al(o + sizeof(uint16_t) * (size_t)nB * J * MO);
+    uint16_t *serows = reinterpret_cast<uint16_t *>(smem + o); o = al(o + sizeof(uint16_t) * (size_t)nB * J);
+    uint32_t *sech = reinterpret_cast<uint32_t *>(smem + o); o = al(o + sizeof(uint32_t) * (size_t)nB * max_echunks);
+    int4 *snb = reinterpret_cast<int4 *>(smem + o); o = al(o + sizeof(int4) * (size_t)nB * n_nbr);
+    long long *cnt = reinterpret_cast<long long *>(smem + o); o = al(o + sizeof(long long) * (size_t)nw * n_cols);
+    uint8_t *bits = smem + o;
+    for (size_t i = tid; i < (size_t)nB * J * MO; i += nt) sbix[i] = __ldg(jb.bix + i);
+    for (size_t i = tid; i < (size_t)nB * J; i += nt) serows[i] = __ldg(erows + i);
+    for (size_t i = tid; i < (size_t)nB * max_echunks; i += nt) sech[i] = __ldg(echunks + i);
+    for (int i = tid; i < nB * n_nbr; i += nt)
+        snb[i] = make_int4(__ldg(jb.nb_uo + 3 * i), __ldg(jb.nb_uo + 3 * i + 1), __ldg(jb.nb_uo + 3 * i + 2), __ldg(jb.nb_b + i));
+    for (int i = tid; i < nw * n_cols; i += nt) cnt[i] = 0;
+    __syncthreads();
     uint8_t *wb = bits + (size_t)warp * n_pfc * n_nbr;
     long long *wc = cnt + (size_t)warp * n_cols;
-    for (int c = lane; c < n_cols; c += 32) wc[c] = 0;
     const int r = blockIdx.y;
     const int8_t *sig = sigma + (int64_t)r * jb.N;
     for (int64_t s = (int64_t)blockIdx.x * nw + warp; s < jb.N; s += (int64_t)gridDim.x * nw) {
         int32_t b, k[3];
         site_coords32(jb, s, b, k);
         for (int n = lane; n < n_nbr; n += 32) {
-            const int e = b * n_nbr + n;
-            const int32_t *uo = jb.nb_uo + 3 * e;
-            const uint32_t st = ((((uint32_t)wrap_add(k[0], __ldg(uo), jb.d0) * (uint32_t)jb.d1 + (uint32_t)wrap_add(k[1], __ldg(uo + 1), jb.d1)) *
-                                  (uint32_t)jb.d2 + (uint32_t)wrap_add(k[2], __ldg(uo + 2), jb.d2)) * (uint32_t)jb.nB + (uint32_t)__ldg(jb.nb_b + e));
+            const int4 e = snb[b * n_nbr + n];
+            const uint32_t st = ((((uint32_t)wrap_add(k[0], e.x, jb.d0) * (uint32_t)jb.d1 + (uint32_t)wrap_add(k[1], e.y, jb.d1)) *
+                                  (uint32_t)jb.d2 + (uint32_t)wrap_add(k[2], e.z, jb.d2)) * (uint32_t)jb.nB + (uint32_t)e.w);
             const int so = sig[st];
-            for (int c = 0; c < n_pfc; ++c) wb[c * n_nbr + n] = jb.sbits[c * 4 + so];
+            for (int c = 0; c < n_pfc; ++c) wb[c * n_nbr + n] = (uint8_t)((sbit_mask >> (c * 4 + so)) & 1u);
         }
         __syncwarp();
         const int nch = __ldg(n_echunks + b);
-        for (int q = 0; q < nch; ++q) {
-            const uint32_t d = __ldg(echunks + (size_t)b * max_echunks + q);
-            const int col = (int)(d & 0xffu), start = (int)((d >> 8) & 0xffffu), len = (int)(d >> 24);
-            int sgn = 0;
-            if (lane < len) {
-                const int j = __ldg(erows + (size_t)b * jb.J + start + lane);
-                const uint16_t *bx = jb.bix + ((size_t)b * jb.J + j) * mo;   // padded members: column 0, bits always 0
-                unsigned x = 0;
-                for (int m = 0; m < mo; ++m) x ^= wb[__ldg(bx + m)];
-                sgn = (x & 1u) ? -1 : 1;
-            }
-            const int n = (int)__reduce_add_sync(0xffffffffu, (unsigned)sgn);
-            if (lane == 0) wc[col] += n;
+        auto chunk_sign = [&](int q, int &col) -> int {
+            const uint32_t d = sech[(size_t)b * max_echunks + q];
+            col = (int)(d & 0xffu);
+            const int start = (int)((d >> 8) & 0xffffu), len = (int)(d >> 24);
+            if (lane >= len) return 0;
+            const int j = serows[(size_t)b * J + start + lane];
+            const uint16_t *bx = sbix + ((size_t)b * J + j) * MO;
+            unsigned x = 0;
+#pragma unroll
+            for (int m = 0; m < MO; ++m) x ^= wb[bx[m]];
+            return (x & 1u) ? -1 : 1;
+        };
+        for (int q = 0; q < nch; q += 2) {
+            int c1 = 0, c2 = 0;
+            const int s1 = chunk_sign(q, c1);
+            const int s2 = (q + 1 < nch) ? chunk_sign(q + 1, c2) : 0;
+            const int n1 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s1);
+            const int n2 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s2);
+            if (lane == 0) { wc[c1] += n1; if (q + 1 < nch) wc[c2] += n2; }
         }
         __syncwarp();
     }
@@ -559,7 +579,7 @@ __global__ void __launch_bounds__(256) ce_energy_bin_kernel(const __grid_constan
             for (int w = 0; w < nw; ++w) tot += cnt[(size_t)w * n_cols + c];
             part += ecol[c] * (double)tot;
         }
-        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+        for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
         if (lane == 0) partial[(int64_t)r * gridDim.x + blockIdx.x] = part;
     }
 }
@@ -715,6 +735,7 @@ struct nce_ce_model {
     uint32_t *chunks = nullptr; int32_t *n_chunks = nullptr; int32_t max_chunks = 0;
     uint16_t *erows = nullptr; uint32_t *echunks = nullptr; int32_t *n_echunks = nullptr; int32_t max_echunks = 0;
     double *ecol1 = nullptr;                 // eci of each column (full-energy kernel)
+    uint32_t sbit_mask = 0;                  // sign bit of point function (column c, species q) at bit c*4+q
     double *energy_partial = nullptr; size_t energy_partial_n = 0;
     int device = 0;
     std::mutex mu;
@@ -1090,6 +1111,8 @@ int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
             for (size_t i = 0; i < nl; ++i) bx[i] = (uint16_t)(t->Rv_pfc[i] * t->n_nbr + t->Rv_loc[i]);
             for (size_t i = 0; i < rc8.size(); ++i) rc8[i] = (uint8_t)std::max(0, std::min(254, t->Rv_col[i]));
             rc = upload(m->sbits, sb.data(), sb.size());
+            for (int c = 0; c < t->n_pfc && c < 8; ++c)
+                for (int q = 0; q < 4; ++q) m->sbit_mask |= (uint32_t)(sb[(size_t)c * 4 + q] & 1u) << (c * 4 + q);
             if (!rc) rc = upload(m->bix, bx.data(), bx.size());
             if (!rc) rc = upload(m->rcol, rc8.data(), rc8.size());
             if (!rc) rc = upload(m->ecol2_64, e2.data(), e2.size());
@@ -1171,10 +1194,13 @@ int nce_ce_energy(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t preci
         NCE_CUDA(cudaMalloc((void **)&h->energy_partial, sizeof(double) * need));
         h->energy_partial_n = need;
     }
-    if (h->binary && h->erows) {
-        // sign-parity full energy: one warp per site, 8 warps per block
+    if (h->binary && h->erows && h->mo <= 8) {
+        // sign-parity full energy: persistent blocks (about four per SM over all configurations), 8 warps each
         const int wpb = 8;
-        const int64_t nb2 = std::max<int64_t>(1, std::min<int64_t>((h->N + wpb - 1) / wpb, 2048));
+        int nsm = 152;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
+        const int64_t want = std::max<int64_t>(1, (int64_t)4 * nsm / R);
+        const int64_t nb2 = std::max<int64_t>(1, std::min<int64_t>(want, (h->N + wpb - 1) / wpb));
         const size_t need2 = (size_t)nb2 * R;
         if (need2 > h->energy_partial_n) {
             if (h->energy_partial) { cudaStreamSynchronize(s); cudaFree(h->energy_partial); }
@@ -1184,10 +1210,22 @@ int nce_ce_energy(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t preci
         }
         nce_pt_chunk ck0; std::memset(&ck0, 0, sizeof(ck0)); ck0.precision = 64;
         CEJob jb = make_job(h, nullptr, &ck0, 0, true);
-        const size_t sm = sizeof(long long) * wpb * h->n_cols + (size_t)wpb * h->n_pfc * h->n_nbr;
-        NCE_CUDA(cudaFuncSetAttribute(ce_energy_bin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        ce_energy_bin_kernel<<<dim3((unsigned)nb2, R), wpb * 32, sm, s>>>(jb, sigma, h->erows, h->echunks, h->n_echunks, h->max_echunks,
-                                                                          h->ecol1, h->mo, h->energy_partial);
+        auto al = [](size_t x) { return (x + 15) / 16 * 16; };
+        const size_t sm = al(sizeof(uint16_t) * (size_t)h->nB * h->J * h->mo) + al(sizeof(uint16_t) * (size_t)h->nB * h->J) +
+                          al(sizeof(uint32_t) * (size_t)h->nB * h->max_echunks) + al(sizeof(int4) * (size_t)h->nB * h->n_nbr) +
+                          al(sizeof(long long) * wpb * h->n_cols) + (size_t)wpb * h->n_pfc * h->n_nbr;
+        NCE_CHECK(sm <= 200 * 1024, "nce_ce_energy: tables too large for the shared-memory energy kernel");
+        const uint32_t mask = h->sbit_mask;
+        NCE_CHECK(h->n_pfc <= 8, "nce_ce_energy: more than 8 point-function columns on the sign-parity path");
+        switch (h->mo) {
+#define NCE_EB(M) case M: \
+            NCE_CUDA(cudaFuncSetAttribute(ce_energy_bin_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)); \
+            ce_energy_bin_kernel<M><<<dim3((unsigned)nb2, R), wpb * 32, sm, s>>>(jb, sigma, h->erows, h->echunks, h->n_echunks, \
+                                                                                 h->max_echunks, h->ecol1, mask, h->energy_partial); break;
+            NCE_EB(1) NCE_EB(2) NCE_EB(3) NCE_EB(4) NCE_EB(5) NCE_EB(6) NCE_EB(7) NCE_EB(8)
+#undef NCE_EB
+            default: break;
+        }
         NCE_CUDA(cudaGetLastError());
         ce_energy_finish<<<(R + 127) / 128, 128, 0, s>>>(h->energy_partial, (int32_t)nb2, R, h->zerolet, E);
         NCE_CUDA(cudaGetLastError());
