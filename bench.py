@@ -42,6 +42,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
     ap.add_argument("--warps", type=int, default=0, help="warps per replica (0 = autotune)")
+    ap.add_argument("--cluster", type=int, default=0, help="CTAs per replica, thread-block cluster (0 = autotune)")
     ap.add_argument("--path", type=int, default=0, help="0 auto, 1 general products, 2 sign parity")
     ap.add_argument("--L", type=int, default=8)
     ap.add_argument("--R", type=int, default=32)
@@ -305,14 +306,18 @@ def main():
     E0 = gce.batched_energy(torch.as_tensor(sig_r).cuda()).cpu().numpy()
     st = PTState(sig_r, E0, beta, np.zeros(R, np.int32))
     tuned = None
-    if args.warps == 0:
-        from neuralce_gb300.autotune import best_warps
-        args.warps, tuned = best_warps(gce, st, args.precision, args.path)
+    if args.warps == 0 or args.cluster == 0:
+        from neuralce_gb300.autotune import best_launch
+        ws = (args.warps,) if args.warps else (4, 8, 16, 32)
+        cls = (args.cluster,) if args.cluster else ((1, 2, 4, 8) if args.path != 1 else (1,))
+        (args.warps, args.cluster), t = best_launch(gce, st, args.precision, args.path, ws, cls)
+        tuned = {f"{w}x{c}": round(v, 3) for (w, c), v in t.items()}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
     step = 0
     for _ in range(args.warmup):
-        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, 1, None, True, path=args.path); step += T
+        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, 1, None, True, path=args.path,
+                  cluster=args.cluster); step += T
     torch.cuda.synchronize()
     clk = Clocks(local); clk.start()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -322,7 +327,8 @@ def main():
     for k in range(args.steps):
         flush.zero_()
         ev[k][0].record(stream)
-        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, 1, None, True, path=args.path)
+        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, 1, None, True, path=args.path,
+                  cluster=args.cluster)
         ev[k][1].record(stream)
         step += T
     torch.cuda.synchronize()
@@ -346,7 +352,7 @@ def main():
         h_emr = pin(st.E_min_rep.cpu().numpy()); h_nacc = pin(st.n_acc.cpu().numpy()); h_nex = pin(st.n_ex.cpu().numpy())
         h_samp = pin(np.zeros((1, R)))
         torch.cuda.synchronize()
-        ck = make_chunk(T, step, 42 + rank, args.precision, args.warps, None, T, None, True, path=args.path)
+        ck = make_chunk(T, step, 42 + rank, args.precision, args.warps, None, T, None, True, path=args.path, cluster=args.cluster)
         def host_call():
             _lib.check(_lib.lib().nce_ce_run_chunk_host(gce.handle, R, h_sig.data_ptr(), h_E.data_ptr(), h_b.data_ptr(),
                                                         h_ros.data_ptr(), h_sor.data_ptr(), h_lid.data_ptr(), h_emr.data_ptr(),
@@ -365,7 +371,7 @@ def main():
     ms_chunk = float(np.mean(per_ms))
     achieved = R * T * B_GATHER / (ms_chunk / 1e3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
-            "kernel": "ce_pt_chunk_kernel", "peak_source": src,
+            "kernel": "ce_pt_chunk_kernel" if args.path == 1 else "ce_bin_chunk_kernel", "peak_source": src,
             "algorithmic_bytes_per_launch": R * T * B_GATHER}
     nce_line = None
     if rank == 0 and args.nce_steps > 0:
@@ -384,7 +390,8 @@ def main():
                 "dtype": "f64" if args.precision == 64 else "f32", "data": "synthetic (seeded lattice, random-normal ECIs)",
                 "config": workload_config(args, gce), "clocks": clocks, "e2e": e2e, "gpu_launches": 2 * args.steps,
                 "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "batch": batch_line,
-                "launch": {"warps_per_replica": args.warps, "path": ["auto", "general", "sign-parity"][args.path],
+                "launch": {"warps_per_cta": args.warps, "ctas_per_replica": args.cluster,
+                           "path": ["auto", "general", "sign-parity"][args.path],
                            "autotune_ms": tuned},
                 "accept_rate": float(st.n_acc.sum().item()) / max(1, R * step)}
         print(json.dumps(line), flush=True)

@@ -133,6 +133,8 @@ typedef struct {
     int32_t precision;         /* 64 or 32 */
     int32_t warps;             /* warps per replica (0 = default) */
     int32_t path;              /* 0 auto, 1 general point-function products, 2 sign parity (point functions in {-1,+1}) */
+    int32_t cluster;           /* sign parity: CTAs per replica (1, 2, 4, 8; thread-block cluster); the cell must fit in
+                                  shared memory, otherwise one CTA is used */
 } nce_pt_chunk;
 
 int nce_ce_run_chunk(nce_ce_handle h, const nce_pt_state *st, const nce_pt_chunk *ck, void *stream);

@@ -34,7 +34,7 @@ class NcePtState(C.Structure):
 class NcePtChunk(C.Structure):
     _fields_ = [("n_steps", i64), ("step0", i64), ("prop_a", vp), ("prop_b", vp), ("prop_u", vp), ("seed", u64),
                 ("sample_interval", i64), ("E_samples", vp), ("do_exchange", i32), ("ex_parity", i32),
-                ("ex_u", vp), ("precision", i32), ("warps", i32), ("path", i32)]
+                ("ex_u", vp), ("precision", i32), ("warps", i32), ("path", i32), ("cluster", i32)]
 
 
 class NceNceDesc(C.Structure):

@@ -1,28 +1,42 @@
-"""Launch-shape autotuner of the CE chunk kernel: warps per replica (CTA size).
+"""Launch-shape autotuner of the CE chunk kernel: warps per CTA and CTAs per replica (thread-block cluster).
 
-Per-step latency, not throughput, bounds a Markov chain, and the best CTA size depends on the number of rows
-per site, the replica count relative to the 152 SMs and the precision.  The tuner times a short chunk of the
-real kernel for each candidate on a scratch copy of the state (the job's own state is untouched) and keeps the
-fastest; results are cached per (tables, R, precision, path)."""
+Per-step latency, not throughput, bounds a Markov chain, and the best shape depends on the number of rows per
+site, the replica count relative to the 152 SMs and the precision: with few replicas, spreading each replica
+over a cluster of 2-8 CTAs puts idle SMs to work on the row phase at the price of one cluster barrier per
+evaluated swap.  The tuner times a short chunk of the real kernel for each candidate on a scratch copy of the
+state (the job's own state is untouched) and keeps the fastest; results are cached per (tables, R, precision,
+path)."""
 from __future__ import annotations
 
 _cache = {}
 
 
-def best_warps(gce, st, precision=64, path=0, candidates=(2, 4, 8, 16, 32), steps=300, seed=12345):
+def best_launch(gce, st, precision=64, path=0, warps=(2, 4, 8, 16, 32), clusters=(1,), steps=300, seed=12345):
+    """((warps, cluster), {(warps, cluster): ms}) of the fastest candidate."""
     import torch
+    from . import _lib
     from .pt import PTState, run_chunk
-    key = (id(gce), st.R, precision, path)
+    key = (id(gce), st.R, precision, path, tuple(warps), tuple(clusters))
     if key in _cache:
         return _cache[key]
     scratch = PTState(st.sigma.cpu().numpy(), st.E.cpu().numpy(), st.beta_slot.cpu().numpy(), st.ladder_id.cpu().numpy())
     timings = {}
-    for w in candidates:
-        run_chunk(gce, scratch, 20, 0, seed, precision, w, path=path)          # warm-up / attribute set-up
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(); run_chunk(gce, scratch, steps, 20, seed, precision, w, path=path); b.record()
-        torch.cuda.synchronize()
-        timings[w] = a.elapsed_time(b)
+    for cl in clusters:
+        for w in warps:
+            try:
+                run_chunk(gce, scratch, 20, 0, seed, precision, w, path=path, cluster=cl)  # warm-up / attribute set-up
+            except _lib.NceError:
+                continue                                  # shape not launchable (cluster does not fit a GPC)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(); run_chunk(gce, scratch, steps, 20, seed, precision, w, path=path, cluster=cl); b.record()
+            torch.cuda.synchronize()
+            timings[(w, cl)] = a.elapsed_time(b)
     best = min(timings, key=timings.get)
     _cache[key] = (best, timings)
     return best, timings
+
+
+def best_warps(gce, st, precision=64, path=0, candidates=(2, 4, 8, 16, 32), steps=300, seed=12345):
+    """Warps per replica with one CTA per replica: (warps, {warps: ms})."""
+    (w, _), t = best_launch(gce, st, precision, path, candidates, (1,), steps, seed)
+    return w, {k[0]: v for k, v in t.items()}

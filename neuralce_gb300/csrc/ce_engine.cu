@@ -20,7 +20,11 @@
 #include <string>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace nce {
 
@@ -324,7 +328,7 @@ struct BinLayout {
         L.ecol = o; o = al(o + acc_bytes * (size_t)n_cols, 16);
         if (sig_smem) { L.sig = o; o = al(o + (size_t)N, 16); } else { L.sig = 0; }
         L.bits = o; o = al(o + 2 * (size_t)n_pfc * n_nbr, 16);
-        L.cnt = o; o = al(o + sizeof(int32_t) * (size_t)n_cols, 16);
+        L.cnt = o; o = al(o + sizeof(int32_t) * 2 * (size_t)n_cols, 16);   // two buffers (step parity)
         L.total = o;
         return L;
     }
@@ -355,14 +359,20 @@ __device__ __forceinline__ void bin_propose(const CEJob &jb, int64_t s, int32_t 
     site_coords32(jb, ia, P.ba, P.ka); site_coords32(jb, ib, P.bb, P.kb);
 }
 
-template <typename Acc, int MO>
+template <typename Acc, int MO, bool CLUSTER>
 __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constant__ CEBatch bt, int32_t sig_budget) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ BinProp prop[64];                      // ring of two batches of 32 proposals
     __shared__ int32_t near_flag;
-    const int j = find_job(bt, blockIdx.x);
+    // CLUSTER: one replica per thread-block cluster; every CTA keeps its own copy of the replica's occupancy and draws
+    // the same proposals, the row chunks are split over the CTAs and the per-column counts are added into every
+    // CTA's counters through distributed shared memory, so all CTAs reach the same decision.
+    int CL = 1, rank = 0;
+    if (CLUSTER) { cg::cluster_group cl = cg::this_cluster(); CL = (int)cl.num_blocks(); rank = (int)cl.block_rank(); }
+    const int rep_idx = blockIdx.x / CL;
+    const int j = find_job(bt, rep_idx);
     const CEJob &jb = bt.job[j];
-    const int r = blockIdx.x - jb.cta_base;
+    const int r = rep_idx - jb.cta_base;
     if (r >= jb.R) return;
     const int tid = threadIdx.x, nt = blockDim.x, nw = nt >> 5, lane = tid & 31, warp = tid >> 5;
     const int ncons = nw > 1 ? nw - 1 : 1;            // consumer warps; the last warp (when there are two or more) draws proposals
@@ -388,8 +398,14 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                                                                       __ldg(jb.nb_uo + 3 * i + 2), __ldg(jb.nb_b + i));
     Acc *ecol = reinterpret_cast<Acc *>(smem + L.ecol);
     const Acc *gecol = reinterpret_cast<const Acc *>(jb.ecol2);
-    int32_t *cnt = reinterpret_cast<int32_t *>(smem + L.cnt);
-    for (int c = tid; c < n_cols; c += nt) { ecol[c] = gecol[c]; cnt[c] = 0; }
+    int32_t *cnt = reinterpret_cast<int32_t *>(smem + L.cnt);      // [parity][n_cols]
+    for (int c = tid; c < n_cols; c += nt) { ecol[c] = gecol[c]; cnt[c] = 0; cnt[n_cols + c] = 0; }
+    int32_t *rcnt[8];
+    for (int q = 0; q < 8; ++q) rcnt[q] = cnt;
+    if (CLUSTER) {
+        cg::cluster_group cl = cg::this_cluster();
+        for (int q = 0; q < CL && q < 8; ++q) rcnt[q] = cl.map_shared_rank(cnt, q);
+    }
     int8_t *gsig = jb.sigma + (int64_t)r * jb.N;
     int8_t *sig = sig_smem ? reinterpret_cast<int8_t *>(smem + L.sig) : gsig;
     if (sig_smem)
@@ -405,8 +421,13 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     if (tid == 0) near_flag = 0;
     if (warp == 0 && lane < jb.n_steps) bin_propose(jb, lane, t, prop[lane]);
     __syncthreads();
+    if (CLUSTER) cg::this_cluster().sync();              // every CTA's counters are zero before any remote add
+    // counter buffer of the current evaluated swap: alternates between swaps that reach the row phase, so that a
+    // cluster barrier always separates a CTA's clearing of a buffer from the next remote add into it
+    int par = 0;
     for (int64_t s = 0; s < jb.n_steps; ++s) {
         const BinProp &P = prop[s & 63];
+        int32_t *cntp = cnt + par * n_cols;
         const int64_t ia = P.ia, ib = P.ib;
         if ((s & 31) == 0 && (nw == 1 ? true : warp == nw - 1)) {     // draw the next batch (steps s+32 .. s+63)
             const int64_t q = s + 32 + lane;
@@ -464,24 +485,32 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                     }
                     return sgn;
                 };
-                for (int k = cw; k < total; k += 2 * ncons) {
-                    const int k2 = k + ncons;
+                const int gw = rank * ncons + cw, gstr = ncons * CL;     // consumer warps of the whole cluster
+                for (int k = gw; k < total; k += 2 * gstr) {
+                    const int k2 = k + gstr;
                     int c1 = 0, c2 = 0;
                     const int s1 = chunk_count(k, c1);
                     const int s2 = k2 < total ? chunk_count(k2, c2) : 0;
                     const int n1 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s1);
                     const int n2 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s2);
                     if (lane == 0) {
-                        if (n1) atomicAdd(&cnt[c1], n1);
-                        if (n2) atomicAdd(&cnt[c2], n2);
+                        if (CLUSTER) {
+                            for (int q = 0; q < CL; ++q) {
+                                if (n1) atomicAdd(rcnt[q] + par * n_cols + c1, n1);
+                                if (n2) atomicAdd(rcnt[q] + par * n_cols + c2, n2);
+                            }
+                        } else {
+                            if (n1) atomicAdd(&cntp[c1], n1);
+                            if (n2) atomicAdd(&cntp[c2], n2);
+                        }
                     }
                 }
             }
-            __syncthreads();
+            if (CLUSTER) cg::this_cluster().sync(); else __syncthreads();
             // 3. dE = sum_c 2 eci_c n_c (warp 0, fixed order), accept, write
             if (warp == 0) {
                 Acc part = Acc(0);
-                for (int c = lane; c < n_cols; c += 32) { const int n = cnt[c]; if (n) { part += ecol[c] * (Acc)n; cnt[c] = 0; } }
+                for (int c = lane; c < n_cols; c += 32) { const int n = cntp[c]; if (n) { part += ecol[c] * (Acc)n; cntp[c] = 0; } }
                 part = warp_sum(part);
                 if (lane == 0) {
                     const double dEd = (double)part;
@@ -491,18 +520,22 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                     }
                 }
             }
+            par ^= 1;
         }
         if (tid == 0) {
             near_flag = 0;
             Emin = fmin(Emin, E);
-            if (jb.E_samples && (s + 1) % jb.sample_interval == 0)
+            if (rank == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
                 jb.E_samples[((s + 1) / jb.sample_interval - 1) * R + t] = E;
         }
         __syncthreads();
     }
-    if (sig_smem)
-        for (int64_t i = tid; i < jb.N; i += nt) gsig[i] = sig[i];
-    if (tid == 0) { jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc; }
+    if (rank == 0) {
+        if (sig_smem)
+            for (int64_t i = tid; i < jb.N; i += nt) gsig[i] = sig[i];
+        if (tid == 0) { jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc; }
+    }
+    if (CLUSTER) cg::this_cluster().sync();              // no CTA leaves while others may still add into its counters
 }
 
 // Full energy on the sign-parity tables: E = zerolet + sum_c eci_c * (sum over sites of the parities of the rows anchored
@@ -810,18 +843,30 @@ static int launch_chunk_mo(const CEBatch &bt, int total, int warps, size_t smem,
 }
 
 template <typename Acc, int MO>
-static int launch_bin_mo(const CEBatch &bt, int total, int warps, size_t smem, int sig_smem, cudaStream_t s) {
-    auto kern = ce_bin_chunk_kernel<Acc, MO>;
-    NCE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<total, warps * 32, smem, s>>>(bt, sig_smem);
+static int launch_bin_mo(const CEBatch &bt, int total, int warps, size_t smem, int sig_smem, cudaStream_t s, int CL) {
+    if (CL <= 1) {
+        auto kern = ce_bin_chunk_kernel<Acc, MO, false>;
+        NCE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<total, warps * 32, smem, s>>>(bt, sig_smem);
+    } else {
+        auto kern = ce_bin_chunk_kernel<Acc, MO, true>;
+        NCE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        cudaLaunchConfig_t cfg; std::memset(&cfg, 0, sizeof(cfg));
+        cfg.gridDim = dim3((unsigned)(total * CL)); cfg.blockDim = dim3(warps * 32); cfg.dynamicSmemBytes = smem; cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)CL; attr[0].val.clusterDim.y = 1; attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr; cfg.numAttrs = 1;
+        NCE_CUDA(cudaLaunchKernelEx(&cfg, kern, bt, sig_smem));
+    }
     NCE_CUDA(cudaGetLastError());
     return NCE_OK;
 }
 
 template <typename Acc>
-static int launch_bin(const CEBatch &bt, int mo, int total, int warps, size_t smem, int sig_smem, cudaStream_t s) {
+static int launch_bin(const CEBatch &bt, int mo, int total, int warps, size_t smem, int sig_smem, cudaStream_t s, int CL) {
     switch (mo) {
-#define NCE_BIN_CASE(M) case M: return launch_bin_mo<Acc, M>(bt, total, warps, smem, sig_smem, s);
+#define NCE_BIN_CASE(M) case M: return launch_bin_mo<Acc, M>(bt, total, warps, smem, sig_smem, s, CL);
         NCE_BIN_CASE(1) NCE_BIN_CASE(2) NCE_BIN_CASE(3) NCE_BIN_CASE(4) NCE_BIN_CASE(5) NCE_BIN_CASE(6) NCE_BIN_CASE(7) NCE_BIN_CASE(8)
 #undef NCE_BIN_CASE
         default: return fail(NCE_ERR_UNSUPPORTED, "cluster order %d > 8", mo);
@@ -859,6 +904,8 @@ static int check_chunk(const nce_pt_state *st, const nce_pt_chunk *ck) {
               "chunk: prop_a/prop_b/prop_u must be all set or all NULL");
     NCE_CHECK(!ck->E_samples || ck->sample_interval > 0, "chunk: sample_interval must be > 0 with E_samples");
     NCE_CHECK(ck->warps >= 0 && ck->warps <= 32, "chunk: warps must be 0..32");
+    NCE_CHECK(ck->cluster == 0 || ck->cluster == 1 || ck->cluster == 2 || ck->cluster == 4 || ck->cluster == 8,
+              "chunk: cluster must be 0, 1, 2, 4 or 8");
     NCE_CHECK(!ck->do_exchange || !ck->ex_u || (ck->ex_parity == 0 || ck->ex_parity == 1), "chunk: ex_parity must be 0/1");
     (void)st;
     return NCE_OK;
@@ -937,9 +984,17 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
     for (int j = 0; j < n_jobs; ++j) max_steps = std::max(max_steps, cks[j].n_steps);
     if (max_steps > 0) {
         int rc;
+        int CL = cks[0].cluster > 1 ? cks[0].cluster : 1;
+        for (int j = 0; j < n_jobs; ++j)
+            NCE_CHECK((cks[j].cluster > 1 ? cks[j].cluster : 1) == CL, "batch: all chunks must use the same cluster");
+        if (!use_bin) CL = 1;
+        if (CL > 1) {
+            // every CTA of a cluster keeps its own copy of the occupancy: all jobs must fit the shared-memory budget
+            for (int j = 0; j < n_jobs; ++j) if (!bt.job[j].sig_smem) CL = 1;
+        }
         if (use_bin)
-            rc = precision == 64 ? launch_bin<double>(bt, mo, total, warps, smem, sig_smem, s)
-                                 : launch_bin<float>(bt, mo, total, warps, smem, sig_smem, s);
+            rc = precision == 64 ? launch_bin<double>(bt, mo, total, warps, smem, sig_smem, s, CL)
+                                 : launch_bin<float>(bt, mo, total, warps, smem, sig_smem, s, CL);
         else
             rc = precision == 64 ? launch_chunk<double>(bt, mo, total, warps, smem, s)
                                  : launch_chunk<float>(bt, mo, total, warps, smem, s);

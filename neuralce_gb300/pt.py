@@ -128,7 +128,7 @@ class PTState:
 
 
 def make_chunk(n_steps, step0, seed, precision=64, warps=0, proposals=None, sample_interval=1, E_samples=None,
-               do_exchange=False, ex_parity=0, ex_u=None, path=0):
+               do_exchange=False, ex_parity=0, ex_u=None, path=0, cluster=1):
     c = _lib.NcePtChunk()
     c.n_steps, c.step0, c.seed = int(n_steps), int(step0), int(seed) & 0xFFFFFFFFFFFFFFFF
     if proposals is not None:
@@ -136,16 +136,16 @@ def make_chunk(n_steps, step0, seed, precision=64, warps=0, proposals=None, samp
     c.sample_interval = int(sample_interval)
     c.E_samples = _lib.ptr(E_samples)
     c.do_exchange = int(bool(do_exchange)); c.ex_parity = int(ex_parity); c.ex_u = _lib.ptr(ex_u)
-    c.precision = int(precision); c.warps = int(warps); c.path = int(path)
+    c.precision = int(precision); c.warps = int(warps); c.path = int(path); c.cluster = int(cluster)
     return c
 
 
 def run_chunk(gce, st: PTState, n_steps, step0, seed, precision=64, warps=0, proposals=None, sample_interval=1,
-              E_samples=None, do_exchange=False, ex_parity=0, ex_u=None, stream=None, path=0):
+              E_samples=None, do_exchange=False, ex_parity=0, ex_u=None, stream=None, path=0, cluster=1):
     """One chunk of the persistent kernel (+ chunk-end exchange) for one job.  path: 0 auto (sign parity when the
     point functions are +-1), 1 general products, 2 sign parity."""
     ck = make_chunk(n_steps, step0, seed, precision, warps, proposals, sample_interval, E_samples, do_exchange,
-                    ex_parity, ex_u, path)
+                    ex_parity, ex_u, path, cluster)
     s = st.struct()
     _lib.check(_lib.lib().nce_ce_run_chunk(gce.handle, C.byref(s), C.byref(ck), _lib.stream_ptr(stream)),
                "nce_ce_run_chunk")

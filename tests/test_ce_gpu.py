@@ -71,10 +71,12 @@ def _compare(st, ref, E_tol):
     assert int(st.n_ex.item()) == int(ref["n_ex"][0])
 
 
-@pytest.mark.parametrize("precision,path,warps", [(64, 1, 8), (32, 1, 8), (64, 2, 8), (32, 2, 4), (64, 2, 1)])
-def test_trajectory_host_stream(cuda, precision, path, warps):
+@pytest.mark.parametrize("precision,path,warps,cluster", [(64, 1, 8, 1), (32, 1, 8, 1), (64, 2, 8, 1), (32, 2, 4, 1),
+                                                          (64, 2, 1, 1), (64, 2, 8, 2), (32, 2, 4, 4), (64, 2, 16, 8)])
+def test_trajectory_host_stream(cuda, precision, path, warps, cluster):
     """Seeded host proposal stream + exchange uniforms: bit-exact occupancy trajectory, energies, acceptance,
-    slot permutation and slot-ordered samples vs the oracle."""
+    slot permutation and slot-ordered samples vs the oracle (cluster > 1: each replica spread over that many
+    CTAs of a thread-block cluster)."""
     torch = cuda
     from neuralce_gb300.ce import proposal_stream
     from neuralce_gb300.pt import run_chunk
@@ -92,7 +94,8 @@ def test_trajectory_host_stream(cuda, precision, path, warps):
         par = chunk % 2
         Es = torch.zeros((T // si, R), dtype=torch.float64, device="cuda")
         dev = tuple(torch.as_tensor(x).cuda() for x in (pa, pb, pu))
-        run_chunk(gce, st, T, step, 0, precision, warps, dev, si, Es, True, par, torch.as_tensor(exu).cuda(), path=path)
+        run_chunk(gce, st, T, step, 0, precision, warps, dev, si, Es, True, par, torch.as_tensor(exu).cuda(), path=path,
+                  cluster=cluster)
         Es_ref = np.zeros((T // si, R))
         orc.run(ref, T, step, 0, (pa, pb, pu), si, Es_ref, True, par, exu, n_threads=4)
         torch.cuda.synchronize()
@@ -151,6 +154,47 @@ def test_batch_equals_alone(cuda):
     torch.cuda.synchronize()
     for a, b in zip(alone, sts):
         assert torch.equal(a.sigma, b.sigma) and torch.equal(a.E, b.E) and torch.equal(a.rep_of_slot, b.rep_of_slot)
+
+
+@pytest.mark.parametrize("cluster", [2, 4])
+def test_cluster_equals_single_cta(cuda, cluster):
+    """Philox stream with exchanges, 3 chunks: a replica spread over a thread-block cluster gives the same
+    trajectory as one CTA, alone and in a batch of jobs."""
+    torch = cuda
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.pt import make_chunk, run_chunk
+    R, T = 8, 2000
+    gce, orc, sig_r, beta = _setup(8, seed=12, R=R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    a = _engine_state(sig_r, E0, beta); b = _engine_state(sig_r, E0, beta)
+    for c in range(3):
+        Ea = torch.zeros((T // 10, R), dtype=torch.float64, device="cuda"); Eb = torch.zeros_like(Ea)
+        run_chunk(gce, a, T, c * T, 99, 64, 8, None, 10, Ea, True, path=2, cluster=1)
+        run_chunk(gce, b, T, c * T, 99, 64, 8, None, 10, Eb, True, path=2, cluster=cluster)
+        torch.cuda.synchronize()
+        assert torch.equal(a.sigma, b.sigma) and torch.equal(a.E, b.E) and torch.equal(Ea, Eb)
+        assert torch.equal(a.n_acc, b.n_acc) and torch.equal(a.rep_of_slot, b.rep_of_slot)
+        assert torch.equal(a.E_min_rep, b.E_min_rep)
+    assert int(a.n_acc.sum()) > 0
+    # two jobs in one clustered launch equal the same jobs alone
+    jobs = []
+    for k, (L, RR) in enumerate([(3, 3), (4, 2)]):
+        g2, o2, s2, b2 = _setup(L, seed=40 + k, R=RR)
+        jobs.append((g2, s2, np.array([o2.energy(x) for x in s2]), b2))
+    alone = []
+    for k, (g2, s2, e2, b2) in enumerate(jobs):
+        st = _engine_state(s2, e2, b2)
+        run_chunk(g2, st, 500, 0, 7 + k, 64, 8, None, 1, None, True, path=2, cluster=1)
+        alone.append(st)
+    sts = [_engine_state(s2, e2, b2) for (_, s2, e2, b2) in jobs]
+    hs = (C.c_void_p * 2)(*[j[0].handle.value for j in jobs])
+    ss = (_lib.NcePtState * 2)(*[s.struct() for s in sts])
+    cks = (_lib.NcePtChunk * 2)(*[make_chunk(500, 0, 7 + k, 64, 8, None, 1, None, True, path=2, cluster=cluster)
+                                  for k in range(2)])
+    _lib.check(_lib.lib().nce_ce_run_batch(2, hs, ss, cks, _lib.stream_ptr()), "batch")
+    torch.cuda.synchronize()
+    for x, y in zip(alone, sts):
+        assert torch.equal(x.sigma, y.sigma) and torch.equal(x.E, y.E) and torch.equal(x.rep_of_slot, y.rep_of_slot)
 
 
 def test_host_buffer_entry_point(cuda):
