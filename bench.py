@@ -210,9 +210,10 @@ def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, step
 
 
 def bench_batch(steps=3, warmup=1, chunk=5000, reanchor=10000, n_jobs=64, alone_jobs=8, alone_steps=2000):
-    """Configuration 2: 64 independent CE cells (L ~ U{4..32}, x_Pt ~ U[0.1, 0.9], R ~ U{16,32,64}) in one launch
-    per chunk, float32 dE with a float64 re-anchor every ``reanchor`` steps; compared with running jobs alone in
-    the float64 kernel (throughput of the first ``alone_jobs`` jobs, each alone)."""
+    """Configuration 2: 64 independent CE cells (L ~ U{4..32}, x_Pt ~ U[0.1, 0.9], R ~ U{16,32,64}) advanced by one
+    CUDA-graph replay per ``reanchor`` steps: reanchor/chunk persistent batch launches (float32 dE, every job's
+    exchange at each chunk end) and the exact float64 re-anchor of every carried energy from the tracked
+    cluster-vector sums.  Compared with the plain float64 kernels running the first ``alone_jobs`` jobs alone."""
     import torch
     from neuralce_gb300.batch import CEBatch, tune_warps
     from neuralce_gb300.pt import PTState, run_chunk
@@ -222,36 +223,46 @@ def bench_batch(steps=3, warmup=1, chunk=5000, reanchor=10000, n_jobs=64, alone_
     jobs = ce_batch_config(n_jobs)
     setup = time.time() - t0
     w, tune = tune_warps(jobs, 32)
-    b = CEBatch(jobs, precision=32, warps=w)
+    # float32 drift between re-anchors and exactness of the float64 re-anchor, measured eagerly on a copy
+    chk = CEBatch(jobs, precision=32, warps=w)
+    for _ in range(reanchor // chunk):
+        chk.run_chunk(chunk)
+    drift = chk.reanchor()
+    full_err = max(float((j["gce"].batched_energy(st.sigma) - st.E).abs().max().item()) for j, st in zip(jobs, chk.states))
+    del chk
+    b = CEBatch(jobs, precision=32, warps=w).capture(chunk, chunks=max(1, reanchor // chunk), reanchor=True)
     for _ in range(warmup):
-        b.run_chunk(chunk)
+        b.replay()
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    drift = 0.0
+    stream = torch.cuda.current_stream()
     for k in range(steps):
-        ev[k][0].record(); b.run_chunk(chunk)
-        if b.step % reanchor == 0:
-            drift = max(drift, b.reanchor())
-        ev[k][1].record()
+        ev[k][0].record(stream); b.replay(); ev[k][1].record(stream)
     torch.cuda.synchronize()
     tot = sum(a.elapsed_time(c) for a, c in ev) / 1e3
-    value = b.attempts_per_step * chunk * steps / tot
-    # each job alone in the float64 kernel
-    att = 0; secs = 0.0
-    for j in jobs[:alone_jobs]:
-        st = PTState(j["sigma"], j["gce"].batched_energy(torch.as_tensor(j["sigma"]).cuda()).cpu().numpy(), j["beta"],
-                     np.zeros(j["R"], np.int32))
-        wj, _ = best_warps(j["gce"], st, 64)
-        run_chunk(j["gce"], st, 50, 0, 5, 64, wj, do_exchange=True)
-        a_, c_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a_.record(); run_chunk(j["gce"], st, alone_steps, 50, 5, 64, wj, do_exchange=True); c_.record(); torch.cuda.synchronize()
-        secs += a_.elapsed_time(c_) / 1e3; att += j["R"] * alone_steps
-    alone = att / secs
+    value = b.attempts_per_step * b._graph_steps * steps / tot
+    # the first jobs alone in the plain float64 kernels: general point-function products, and sign parity
+    alone = {}
+    for path in (1, 2):
+        att = 0; secs = 0.0
+        for j in jobs[:alone_jobs]:
+            st = PTState(j["sigma"], j["gce"].batched_energy(torch.as_tensor(j["sigma"]).cuda()).cpu().numpy(), j["beta"],
+                         np.zeros(j["R"], np.int32))
+            wj, _ = best_warps(j["gce"], st, 64, path)
+            run_chunk(j["gce"], st, 50, 0, 5, 64, wj, do_exchange=True, path=path)
+            a_, c_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a_.record(); run_chunk(j["gce"], st, alone_steps, 50, 5, 64, wj, do_exchange=True, path=path); c_.record()
+            torch.cuda.synchronize()
+            secs += a_.elapsed_time(c_) / 1e3; att += j["R"] * alone_steps
+        alone[path] = att / secs
     return {"value": value, "unit": "swap attempts/s", "ms_per_step": 1e3 * tot / steps,
-            "config": f"{n_jobs} CE jobs in one launch per chunk: L~U{{4..32}} ({min(j['N'] for j in jobs)}-{max(j['N'] for j in jobs)} sites), "
-                      f"x_Pt~U[0.1,0.9], R~U{{16,32,64}} ({b.attempts_per_step} replicas), fp32 dE, fp64 re-anchor every {reanchor} steps, "
-                      f"chunk {chunk} steps + exchange",
-            "fp64_single_job_alone": alone, "ratio_vs_fp64_single_job": value / alone, "max_reanchor_drift_eV": drift,
+            "config": f"{n_jobs} CE jobs, one CUDA graph per {b._graph_steps} steps: L~U{{4..32}} "
+                      f"({min(j['N'] for j in jobs)}-{max(j['N'] for j in jobs)} sites), x_Pt~U[0.1,0.9], R~U{{16,32,64}} "
+                      f"({b.attempts_per_step} replicas), fp32 dE, {max(1, reanchor // chunk)} batch launches of {chunk} steps "
+                      f"+ exchange, then the fp64 re-anchor from exact cluster-vector sums",
+            "fp64_single_job_alone": alone[1], "ratio_vs_fp64_single_job": value / alone[1],
+            "fp64_sign_parity_single_job_alone": alone[2], "ratio_vs_fp64_sign_parity_single_job": value / alone[2],
+            "max_fp32_drift_before_reanchor_eV": drift, "max_reanchored_vs_full_recompute_eV": full_err,
             "warps_per_replica": w, "autotune_ms": tune, "setup_s": setup}
 
 

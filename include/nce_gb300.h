@@ -101,6 +101,16 @@ int nce_ce_delta(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t n, con
                  const int64_t *ia, const int64_t *ib, const int8_t *sa_new, const int8_t *sb_new,
                  int32_t precision, int32_t warps, double *out, void *stream);
 
+/* Cluster-vector sums of R configurations (sign-parity tables only): cv[r, c] = sum over the cluster instances
+ * of column c of the product of the point functions (+-1), exact integers.  cv is (R, n_cols) int64 on the device.
+ * E = zerolet + sum_c eci_c * cv[r, c] (the orbit's eci per instance).  No counterpart in the reference, whose
+ * float64 re-anchor recomputes the energy from scratch (ce_gpu_implicit.py energy_a). */
+int nce_ce_cluster_counts(nce_ce_handle h, const int8_t *sigma, int32_t R, int64_t *cv, void *stream);
+
+/* E[r] = zerolet + sum_c eci_c * cv[r, c] in float64, columns in order (the exact re-anchor of the carried
+ * energies from tracked cluster-vector sums). */
+int nce_ce_energy_from_counts(nce_ce_handle h, const int64_t *cv, int32_t R, double *E, void *stream);
+
 /* Parallel-tempering state of one job, all device pointers. */
 typedef struct {
     int32_t R;             /* replicas = temperature slots */
@@ -114,6 +124,10 @@ typedef struct {
     double *E_min_rep;     /* (R) running minimum of E per replica */
     int64_t *n_acc;        /* (R) accepted swaps per replica (accumulated) */
     int64_t *n_ex;         /* (1) accepted exchanges (accumulated) */
+    int64_t *cv;           /* (R, n_cols) or NULL: per replica, the sums over all cluster instances of each
+                              cluster-vector column of the product of point functions (exact integers on the
+                              sign-parity path), kept current by the chunk kernel; the float64 energy follows
+                              from them exactly (nce_ce_energy_from_counts) */
 } nce_pt_state;
 
 /* One chunk of steps.  Proposals: host-supplied stream (prop_a/prop_b/prop_u device arrays indexed
@@ -135,6 +149,9 @@ typedef struct {
     int32_t path;              /* 0 auto, 1 general point-function products, 2 sign parity (point functions in {-1,+1}) */
     int32_t cluster;           /* sign parity: CTAs per replica (1, 2, 4, 8; thread-block cluster); the cell must fit in
                                   shared memory, otherwise one CTA is used */
+    int64_t *step_dev;         /* device counter or NULL: when set, the chunk's first global step is read from it
+                                  (step0 is ignored) and it advances by n_steps when the chunk ends, so that a
+                                  captured CUDA graph of chunks continues the Philox stream on every replay */
 } nce_pt_chunk;
 
 int nce_ce_run_chunk(nce_ce_handle h, const nce_pt_state *st, const nce_pt_chunk *ck, void *stream);

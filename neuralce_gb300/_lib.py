@@ -28,13 +28,13 @@ class NceCeTables(C.Structure):
 
 class NcePtState(C.Structure):
     _fields_ = [("R", i32), ("N", i64), ("sigma", vp), ("E", vp), ("beta_slot", vp), ("rep_of_slot", vp),
-                ("slot_of_rep", vp), ("ladder_id", vp), ("E_min_rep", vp), ("n_acc", vp), ("n_ex", vp)]
+                ("slot_of_rep", vp), ("ladder_id", vp), ("E_min_rep", vp), ("n_acc", vp), ("n_ex", vp), ("cv", vp)]
 
 
 class NcePtChunk(C.Structure):
     _fields_ = [("n_steps", i64), ("step0", i64), ("prop_a", vp), ("prop_b", vp), ("prop_u", vp), ("seed", u64),
                 ("sample_interval", i64), ("E_samples", vp), ("do_exchange", i32), ("ex_parity", i32),
-                ("ex_u", vp), ("precision", i32), ("warps", i32), ("path", i32), ("cluster", i32)]
+                ("ex_u", vp), ("precision", i32), ("warps", i32), ("path", i32), ("cluster", i32), ("step_dev", vp)]
 
 
 class NceNceDesc(C.Structure):
@@ -70,6 +70,8 @@ SIGNATURES = {
     "nce_ce_energy": (i32, [vp, vp, i32, i32, vp, vp]),
     "nce_ce_delta": (i32, [vp, vp, i32, i32, vp, vp, vp, vp, vp, i32, i32, vp, vp]),
     "nce_ce_run_chunk": (i32, [vp, P(NcePtState), P(NcePtChunk), vp]),
+    "nce_ce_cluster_counts": (i32, [vp, vp, i32, vp, vp]),
+    "nce_ce_energy_from_counts": (i32, [vp, vp, i32, vp, vp]),
     "nce_ce_run_batch": (i32, [i32, P(vp), P(NcePtState), P(NcePtChunk), vp]),
     "nce_ce_run_chunk_host": (i32, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, P(NcePtChunk), vp]),
     "nce_ce_errors": (i32, [vp, P(i32)]),

@@ -172,6 +172,23 @@ class GPUClusterExpansion:
                    "nce_ce_energy")
         return E
 
+    def cluster_counts(self, sigma_batch):
+        """(R, n_cols) int64 cluster-vector sums of device configurations (point functions in {-1, +1})."""
+        import torch
+        sd = sigma_batch.reshape(-1, self.n_atoms).contiguous()
+        cv = torch.empty((sd.shape[0], self.info["n_cols"]), dtype=torch.int64, device=sd.device)
+        _lib.check(_lib.lib().nce_ce_cluster_counts(self.handle, sd.data_ptr(), sd.shape[0], cv.data_ptr(), _lib.stream_ptr()),
+                   "nce_ce_cluster_counts")
+        return cv
+
+    def energy_from_counts(self, cv):
+        """float64 energies E = zerolet + sum_c eci_c cv[:, c]."""
+        import torch
+        E = torch.empty(cv.shape[0], dtype=torch.float64, device=cv.device)
+        _lib.check(_lib.lib().nce_ce_energy_from_counts(self.handle, cv.data_ptr(), cv.shape[0], E.data_ptr(), _lib.stream_ptr()),
+                   "nce_ce_energy_from_counts")
+        return E
+
     def energy(self, sigma, precision=64):
         return float(self.batched_energy(sigma, precision)[0].item())
 

@@ -51,6 +51,7 @@ struct CEJob {
     int32_t R;
     // chunk
     int64_t n_steps, step0;
+    const int64_t *step_dev;   // device step counter (overrides step0) or null
     const int32_t *prop_a, *prop_b; const double *prop_u;
     uint64_t seed;
     int64_t sample_interval; double *E_samples;
@@ -65,6 +66,7 @@ struct CEJob {
     const int32_t *n_chunks; // (nB)
     int32_t max_chunks;
     int32_t sig_smem;      // this job's occupancy is copied into shared memory for the chunk
+    int64_t *cv;           // (R, n_cols) tracked cluster-vector sums or null
 };
 
 struct CEBatch {
@@ -258,13 +260,14 @@ __global__ void __launch_bounds__(1024) ce_pt_chunk_kernel(const __grid_constant
     double E = jb.E[r], Emin = jb.E_min_rep[r];
     int64_t nacc = 0;
     const int R = jb.R;
+    const int64_t g0 = jb.step_dev ? *jb.step_dev : jb.step0;
     for (int64_t s = 0; s < jb.n_steps; ++s) {
         if (threadIdx.x == 0) {
             int64_t ia, ib; double u;
             if (jb.prop_a) {
                 ia = jb.prop_a[s * R + t]; ib = jb.prop_b[s * R + t]; u = jb.prop_u[s * R + t];
             } else {
-                propose(jb, jb.step0 + s, t, ia, ib, u);
+                propose(jb, g0 + s, t, ia, ib, u);
             }
             int valid = 0;
             if (ia < 0 || ib < 0 || ia >= jb.N || ib >= jb.N) {
@@ -312,7 +315,7 @@ struct BinProp {
 };
 
 struct BinLayout {
-    size_t bix, rcol, chunk, nb, ecol, sig, bits, cnt, total;
+    size_t bix, rcol, chunk, nb, ecol, sig, bits, cnt, dcv, total;
     __host__ __device__ static BinLayout make(int nB, int J, int mo, int n_nbr, int n_pfc, int n_cols, int max_chunks, size_t acc_bytes,
                                                 int64_t N, bool tables, bool sig_smem) {
         BinLayout L; size_t o = 0;
@@ -329,6 +332,7 @@ struct BinLayout {
         if (sig_smem) { L.sig = o; o = al(o + (size_t)N, 16); } else { L.sig = 0; }
         L.bits = o; o = al(o + 2 * (size_t)n_pfc * n_nbr, 16);
         L.cnt = o; o = al(o + sizeof(int32_t) * 2 * (size_t)n_cols, 16);   // two buffers (step parity)
+        L.dcv = o; o = al(o + sizeof(int32_t) * (size_t)n_cols, 16);       // chunk change of the cluster-vector sums
         L.total = o;
         return L;
     }
@@ -344,12 +348,12 @@ __device__ __forceinline__ void site_coords32(const CEJob &jb, int64_t i, int32_
     k[1] = (int32_t)(c12 - (uint32_t)k[0] * d1);
 }
 
-__device__ __forceinline__ void bin_propose(const CEJob &jb, int64_t s, int32_t t, BinProp &P) {
+__device__ __forceinline__ void bin_propose(const CEJob &jb, int64_t g0, int64_t s, int32_t t, BinProp &P) {
     int64_t ia, ib; double u;
     if (jb.prop_a) {
         ia = jb.prop_a[s * jb.R + t]; ib = jb.prop_b[s * jb.R + t]; u = jb.prop_u[s * jb.R + t];
     } else {
-        propose(jb, jb.step0 + s, t, ia, ib, u);
+        propose(jb, g0 + s, t, ia, ib, u);
     }
     if (ia < 0 || ib < 0 || ia >= jb.N || ib >= jb.N) {
         atomicOr(jb.err, 1);
@@ -399,7 +403,9 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     Acc *ecol = reinterpret_cast<Acc *>(smem + L.ecol);
     const Acc *gecol = reinterpret_cast<const Acc *>(jb.ecol2);
     int32_t *cnt = reinterpret_cast<int32_t *>(smem + L.cnt);      // [parity][n_cols]
-    for (int c = tid; c < n_cols; c += nt) { ecol[c] = gecol[c]; cnt[c] = 0; cnt[n_cols + c] = 0; }
+    int32_t *dcv = reinterpret_cast<int32_t *>(smem + L.dcv);
+    const bool track = jb.cv != nullptr;
+    for (int c = tid; c < n_cols; c += nt) { ecol[c] = gecol[c]; cnt[c] = 0; cnt[n_cols + c] = 0; dcv[c] = 0; }
     int32_t *rcnt[8];
     for (int q = 0; q < 8; ++q) rcnt[q] = cnt;
     if (CLUSTER) {
@@ -418,8 +424,9 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     int64_t nacc = 0;
     const int R = jb.R;
     // proposals are drawn 32 at a time (one per lane of the producer warp), one batch ahead of their use
+    const int64_t g0 = jb.step_dev ? *jb.step_dev : jb.step0;
     if (tid == 0) near_flag = 0;
-    if (warp == 0 && lane < jb.n_steps) bin_propose(jb, lane, t, prop[lane]);
+    if (warp == 0 && lane < jb.n_steps) bin_propose(jb, g0, lane, t, prop[lane]);
     __syncthreads();
     if (CLUSTER) cg::this_cluster().sync();              // every CTA's counters are zero before any remote add
     // counter buffer of the current evaluated swap: alternates between swaps that reach the row phase, so that a
@@ -431,7 +438,7 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
         const int64_t ia = P.ia, ib = P.ib;
         if ((s & 31) == 0 && (nw == 1 ? true : warp == nw - 1)) {     // draw the next batch (steps s+32 .. s+63)
             const int64_t q = s + 32 + lane;
-            if (q < jb.n_steps) bin_propose(jb, q, t, prop[q & 63]);
+            if (q < jb.n_steps) bin_propose(jb, g0, q, t, prop[q & 63]);
         }
         const int sa = sig[ia], sb = sig[ib];
         if (sa != sb) {
@@ -510,15 +517,22 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
             // 3. dE = sum_c 2 eci_c n_c (warp 0, fixed order), accept, write
             if (warp == 0) {
                 Acc part = Acc(0);
-                for (int c = lane; c < n_cols; c += 32) { const int n = cntp[c]; if (n) { part += ecol[c] * (Acc)n; cntp[c] = 0; } }
-                part = warp_sum(part);
-                if (lane == 0) {
-                    const double dEd = (double)part;
-                    if (P.logu < -beta * dEd) {
-                        sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new;
-                        E += dEd; ++nacc;
-                    }
+                for (int c = lane; c < n_cols; c += 32) {
+                    const int n = cntp[c];
+                    if (n) { part += ecol[c] * (Acc)n; if (!track) cntp[c] = 0; }
                 }
+                part = warp_sum(part);                  // butterfly: every lane holds the same sum
+                const double dEd = (double)part;
+                const bool accept = P.logu < -beta * dEd;
+                if (lane == 0 && accept) {
+                    sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new;
+                    E += dEd; ++nacc;
+                }
+                if (track)                              // each changed row moves its column's sum by +-2
+                    for (int c = lane; c < n_cols; c += 32) {
+                        const int n = cntp[c];
+                        if (n) { if (accept) dcv[c] += 2 * n; cntp[c] = 0; }
+                    }
             }
             par ^= 1;
         }
@@ -534,6 +548,8 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
         if (sig_smem)
             for (int64_t i = tid; i < jb.N; i += nt) gsig[i] = sig[i];
         if (tid == 0) { jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc; }
+        if (track)
+            for (int c = tid; c < n_cols; c += nt) jb.cv[(int64_t)r * n_cols + c] += dcv[c];
     }
     if (CLUSTER) cg::this_cluster().sync();              // no CTA leaves while others may still add into its counters
 }
@@ -546,7 +562,8 @@ template <int MO>
 __global__ void __launch_bounds__(256) ce_energy_bin_kernel(const __grid_constant__ CEJob jb, const int8_t *__restrict__ sigma,
                                                              const uint16_t *__restrict__ erows, const uint32_t *__restrict__ echunks,
                                                              const int32_t *__restrict__ n_echunks, int32_t max_echunks,
-                                                             const double *__restrict__ ecol, uint32_t sbit_mask, double *partial) {
+                                                             const double *__restrict__ ecol, uint32_t sbit_mask, double *partial,
+                                                             unsigned long long *cv_out) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
     const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc, n_cols = jb.n_cols, nB = jb.nB, J = jb.J;
@@ -611,10 +628,21 @@ __global__ void __launch_bounds__(256) ce_energy_bin_kernel(const __grid_constan
             long long tot = 0;
             for (int w = 0; w < nw; ++w) tot += cnt[(size_t)w * n_cols + c];
             part += ecol[c] * (double)tot;
+            if (cv_out) atomicAdd(cv_out + (int64_t)r * n_cols + c, (unsigned long long)tot);   // two's complement sum
         }
         for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
         if (lane == 0) partial[(int64_t)r * gridDim.x + blockIdx.x] = part;
     }
+}
+
+// E[r] = zerolet + sum_c eci_c * cv[r, c], columns in order (one thread per configuration)
+__global__ void ce_energy_counts_kernel(const int64_t *__restrict__ cv, int32_t R, int32_t n_cols, const double *__restrict__ ecol,
+                                        double zerolet, double *E) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    double e = 0.0;
+    for (int c = 0; c < n_cols; ++c) e += ecol[c] * (double)cv[(int64_t)r * n_cols + c];
+    E[r] = zerolet + e;
 }
 
 // chunk-end exchange of temperature slots, one CTA (thread 0) per job
@@ -623,6 +651,7 @@ struct CEExJob {
     int64_t *n_ex; uint64_t seed; int64_t g_end; int32_t parity; const double *ex_u;
     double *E_samples; int64_t last_row; int32_t do_exchange;
     double E_scale; int32_t rounds;          // energies in eV = E * E_scale; exchange rounds back to back
+    int64_t *step_dev; int64_t n_steps;      // device step counter advanced by the chunk (or null)
 };
 struct CEExBatch { int32_t n_jobs; CEExJob job[kMaxJobs]; };
 
@@ -631,12 +660,14 @@ __global__ void ce_exchange_kernel(const __grid_constant__ CEExBatch bt) {
     const int j = blockIdx.x;
     if (j >= bt.n_jobs || threadIdx.x != 0) return;
     const CEExJob &x = bt.job[j];
+    const int64_t g_end = x.step_dev ? *x.step_dev + x.n_steps : x.g_end;
+    if (x.step_dev) *x.step_dev = g_end;      // the chunk kernel has finished reading it (stream order)
     if (!x.do_exchange || x.R < 2) return;
     int32_t *perm = xsm;
     int32_t *ros = perm + x.R;
     const int R = x.R;
     const uint32_t k0 = (uint32_t)x.seed, k1 = (uint32_t)(x.seed >> 32);
-    const uint32_t c0 = (uint32_t)x.g_end, c1 = (uint32_t)((uint64_t)x.g_end >> 32);
+    const uint32_t c0 = (uint32_t)g_end, c1 = (uint32_t)((uint64_t)g_end >> 32);
     const int npair = R / 2;                 // ceil((R-1)/2)
     int64_t nswap = 0;
     for (int q = 0; q < max(x.rounds, 1); ++q) {
@@ -822,10 +853,10 @@ static CEJob make_job(const nce_ce_model *m, const nce_pt_state *st, const nce_p
     j.n_cells = m->n_cells; j.N = m->N; j.err = m->err;
     if (st) {
         j.sigma = st->sigma; j.E = st->E; j.beta_slot = st->beta_slot; j.slot_of_rep = st->slot_of_rep;
-        j.E_min_rep = st->E_min_rep; j.n_acc = st->n_acc; j.R = st->R;
+        j.E_min_rep = st->E_min_rep; j.n_acc = st->n_acc; j.R = st->R; j.cv = st->cv;
     }
     if (ck) {
-        j.n_steps = ck->n_steps; j.step0 = ck->step0; j.prop_a = ck->prop_a; j.prop_b = ck->prop_b; j.prop_u = ck->prop_u;
+        j.n_steps = ck->n_steps; j.step0 = ck->step0; j.step_dev = ck->step_dev; j.prop_a = ck->prop_a; j.prop_b = ck->prop_b; j.prop_u = ck->prop_u;
         j.seed = ck->seed; j.sample_interval = ck->sample_interval > 0 ? ck->sample_interval : 1;
         j.E_samples = ck->E_samples;
     }
@@ -936,6 +967,8 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
     NCE_CHECK(path >= 0 && path <= 2, "chunk: path must be 0 (auto), 1 (general) or 2 (sign parity)");
     NCE_CHECK(path != 2 || all_bin, "chunk: the sign-parity path needs point functions in {-1, +1}");
     const bool use_bin = (path == 2) || (path == 0 && all_bin);
+    for (int j = 0; j < n_jobs; ++j)
+        NCE_CHECK(!sts[j].cv || use_bin, "chunk: tracked cluster-vector sums need the sign-parity path");
     CEBatch bt; std::memset(&bt, 0, sizeof(bt));
     bt.n_jobs = n_jobs;
     size_t smem = 0; bool all_fit = true;
@@ -1013,7 +1046,8 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
         x.last_row = (ck.E_samples && ck.n_steps > 0 && ck.n_steps % ck.sample_interval == 0) ? ck.n_steps / ck.sample_interval - 1 : -1;
         x.do_exchange = ck.do_exchange && st.R > 1;
         x.E_scale = 1.0; x.rounds = 1;
-        any = any || x.do_exchange;
+        x.step_dev = ck.step_dev; x.n_steps = ck.n_steps;
+        any = any || x.do_exchange || x.step_dev;
     }
     if (any) {
         const size_t xs = sizeof(int32_t) * 2 * (size_t)max_R;
@@ -1069,6 +1103,9 @@ static int launch_delta(const CEJob &jb, int mo, int n, const int32_t *rep, cons
 }  // namespace nce
 
 using namespace nce;
+
+static int energy_impl(nce_ce_model *h, const int8_t *sigma, int32_t R, int32_t precision, double *E, int64_t *cv_out,
+                       cudaStream_t s);
 
 extern "C" {
 
@@ -1238,7 +1275,32 @@ int nce_ce_energy(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t preci
     NCE_CHECK(h && sigma && E && R >= 1, "nce_ce_energy: bad argument");
     NCE_CHECK(precision == 64 || precision == 32, "nce_ce_energy: precision must be 64 or 32");
     std::lock_guard<std::mutex> lk(h->mu);
+    return energy_impl(h, sigma, R, precision, E, nullptr, (cudaStream_t)stream);
+}
+
+int nce_ce_cluster_counts(nce_ce_handle h, const int8_t *sigma, int32_t R, int64_t *cv, void *stream) {
+    NCE_CHECK(h && sigma && cv && R >= 1, "nce_ce_cluster_counts: bad argument");
+    NCE_CHECK(h->binary && h->erows && h->mo <= 8, "nce_ce_cluster_counts: needs point functions in {-1, +1}");
+    std::lock_guard<std::mutex> lk(h->mu);
     cudaStream_t s = (cudaStream_t)stream;
+    NCE_CUDA(cudaMemsetAsync(cv, 0, sizeof(int64_t) * (size_t)R * h->n_cols, s));
+    return energy_impl(h, sigma, R, 64, nullptr, cv, s);
+}
+
+int nce_ce_energy_from_counts(nce_ce_handle h, const int64_t *cv, int32_t R, double *E, void *stream) {
+    NCE_CHECK(h && cv && E && R >= 1, "nce_ce_energy_from_counts: bad argument");
+    NCE_CHECK(h->binary && h->ecol1, "nce_ce_energy_from_counts: needs point functions in {-1, +1}");
+    ce_energy_counts_kernel<<<(R + 127) / 128, 128, 0, (cudaStream_t)stream>>>(cv, R, h->n_cols, h->ecol1, h->zerolet, E);
+    NCE_CUDA(cudaGetLastError());
+    return NCE_OK;
+}
+
+}  // extern "C"
+
+// full energy of R configurations; cv_out (R, n_cols) additionally receives the cluster-vector sums (sign-parity
+// kernel only, zeroed by the caller); E may be null when only the sums are wanted
+static int energy_impl(nce_ce_model *h, const int8_t *sigma, int32_t R, int32_t precision, double *E, int64_t *cv_out,
+                       cudaStream_t s) {
     const int threads = 256;
     int nblk = (int)std::min<int64_t>((h->n_cells + threads - 1) / threads, 1184);
     nblk = std::max(nblk, 1);
@@ -1276,16 +1338,20 @@ int nce_ce_energy(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t preci
 #define NCE_EB(M) case M: \
             NCE_CUDA(cudaFuncSetAttribute(ce_energy_bin_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)); \
             ce_energy_bin_kernel<M><<<dim3((unsigned)nb2, R), wpb * 32, sm, s>>>(jb, sigma, h->erows, h->echunks, h->n_echunks, \
-                                                                                 h->max_echunks, h->ecol1, mask, h->energy_partial); break;
+                                                                                 h->max_echunks, h->ecol1, mask, h->energy_partial, \
+                                                                                 (unsigned long long *)cv_out); break;
             NCE_EB(1) NCE_EB(2) NCE_EB(3) NCE_EB(4) NCE_EB(5) NCE_EB(6) NCE_EB(7) NCE_EB(8)
 #undef NCE_EB
             default: break;
         }
         NCE_CUDA(cudaGetLastError());
-        ce_energy_finish<<<(R + 127) / 128, 128, 0, s>>>(h->energy_partial, (int32_t)nb2, R, h->zerolet, E);
-        NCE_CUDA(cudaGetLastError());
+        if (E) {
+            ce_energy_finish<<<(R + 127) / 128, 128, 0, s>>>(h->energy_partial, (int32_t)nb2, R, h->zerolet, E);
+            NCE_CUDA(cudaGetLastError());
+        }
         return NCE_OK;
     }
+    NCE_CHECK(E && !cv_out, "energy: cluster-vector sums need the sign-parity tables");
     dim3 grid(nblk, R);
     if (precision == 64)
         ce_energy_kernel<double><<<grid, threads, 0, s>>>(sigma, h->N, h->n_cells, h->nB, (int)h->d[0], (int)h->d[1], (int)h->d[2],
@@ -1300,6 +1366,8 @@ int nce_ce_energy(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t preci
     NCE_CUDA(cudaGetLastError());
     return NCE_OK;
 }
+
+extern "C" {
 
 int nce_ce_delta(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t n, const int32_t *rep, const int64_t *ia,
                  const int64_t *ib, const int8_t *sa_new, const int8_t *sb_new, int32_t precision, int32_t warps,
@@ -1363,7 +1431,7 @@ int nce_ce_run_chunk_host(nce_ce_handle h, int32_t R, int8_t *sigma_host, double
         h->staging_bytes = o;
     }
     char *b = (char *)h->staging_base;
-    nce_pt_state st;
+    nce_pt_state st; std::memset(&st, 0, sizeof(st));
     st.R = R; st.N = N; st.sigma = (int8_t *)(b + off[0]); st.E = (double *)(b + off[1]); st.beta_slot = (float *)(b + off[2]);
     st.rep_of_slot = (int32_t *)(b + off[3]); st.slot_of_rep = (int32_t *)(b + off[4]); st.ladder_id = (int32_t *)(b + off[5]);
     st.E_min_rep = (double *)(b + off[6]); st.n_acc = (int64_t *)(b + off[7]); st.n_ex = (int64_t *)(b + off[8]);

@@ -105,12 +105,27 @@ class PTState:
         self.n_ex = torch.zeros(1, dtype=torch.int64, device=device)
         self._min = torch.zeros(1, dtype=torch.float64, device=device)
         self._arg = torch.zeros(1, dtype=torch.int32, device=device)
+        self.cv = None
+
+    def track_counts(self, gce):
+        """Keep the replicas' cluster-vector sums (exact integers, sign-parity tables) current from now on; the
+        carried energies can then be re-anchored exactly with ``reanchor_from_counts``."""
+        self.cv = gce.cluster_counts(self.sigma)
+        return self
+
+    def reanchor_from_counts(self, gce):
+        """float64 energies from the tracked sums; returns the largest change of a carried energy."""
+        E = gce.energy_from_counts(self.cv)
+        drift = float((E - self.E).abs().max().item())
+        self.E.copy_(E)
+        return drift
 
     def struct(self):
         s = _lib.NcePtState()
         s.R, s.N = self.R, self.N
         for f in ("sigma", "E", "beta_slot", "rep_of_slot", "slot_of_rep", "ladder_id", "E_min_rep", "n_acc", "n_ex"):
             setattr(s, f, getattr(self, f).data_ptr())
+        s.cv = self.cv.data_ptr() if self.cv is not None else None
         return s
 
     def minimum(self, stream=None):

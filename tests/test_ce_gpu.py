@@ -252,3 +252,50 @@ def test_out_of_range_proposal_is_flagged(cuda):
     flags = _lib.i32()
     _lib.check(_lib.lib().nce_ce_errors(gce.handle, C.byref(flags)), "errors")
     assert flags.value & 1
+
+
+def test_tracked_cluster_vector_sums(cuda):
+    """Sign-parity chunks keep the replicas' cluster-vector sums exact: after Philox chunks with exchanges the
+    tracked integers equal a recount of the final occupancies, and the energies that follow from them equal a
+    float64 full recompute; fp32 carried energies re-anchor onto them."""
+    torch = cuda
+    from neuralce_gb300.pt import run_chunk
+    R, T = 8, 3000
+    gce, orc, sig_r, beta = _setup(5, seed=13, R=R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    for precision, cluster in ((64, 1), (32, 2)):
+        st = _engine_state(sig_r, E0, beta).track_counts(gce)
+        assert np.abs(gce.energy_from_counts(st.cv).cpu().numpy() - E0).max() < 1e-9
+        for c in range(3):
+            run_chunk(gce, st, T, c * T, 4321, precision, 8, None, 1, None, True, path=2, cluster=cluster)
+        torch.cuda.synchronize()
+        assert torch.equal(st.cv, gce.cluster_counts(st.sigma))
+        Ef = gce.batched_energy(st.sigma).cpu().numpy()
+        assert np.abs(gce.energy_from_counts(st.cv).cpu().numpy() - Ef).max() < 1e-9
+        drift = st.reanchor_from_counts(gce)
+        assert drift < (1e-9 if precision == 64 else 1e-3)
+        assert np.abs(st.E.cpu().numpy() - Ef).max() < 1e-9
+        assert int(st.n_acc.sum()) > 0
+
+
+def test_graph_replay_equals_eager_batch(cuda):
+    """A CUDA graph of batch chunks (device step counters, exact re-anchor) replays to the same trajectories as
+    eager launches of the same chunks."""
+    torch = cuda
+    from neuralce_gb300.batch import CEBatch
+    from neuralce_gb300.workloads import ladder, replica_configs, ce_config
+    jobs = []
+    for k, (L, R) in enumerate([(3, 4), (4, 6), (5, 2)]):
+        gce, sig = ce_config(L, seed=60 + k)
+        _, beta = ladder(R)
+        jobs.append({"gce": gce, "sigma": replica_configs(sig, R, 61 + k), "beta": beta, "R": R, "N": gce.n_atoms})
+    a = CEBatch(jobs, precision=32, warps=8)
+    b = CEBatch(jobs, precision=32, warps=8).capture(400, chunks=2, reanchor=True)
+    for _ in range(3):
+        a.run_chunk(400); a.run_chunk(400); a.reanchor()
+        b.replay()
+    torch.cuda.synchronize()
+    assert a.step == b.step == 2400
+    for x, y in zip(a.states, b.states):
+        assert torch.equal(x.sigma, y.sigma) and torch.equal(x.cv, y.cv) and torch.equal(x.rep_of_slot, y.rep_of_slot)
+        assert torch.equal(x.E, y.E) and torch.equal(x.n_acc, y.n_acc)
