@@ -254,6 +254,81 @@ int nce_nce_full_cache(nce_nce_handle h, const nce_nce_state *st, void *stream);
 int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_chunk *ck, void *stream);
 int nce_nce_errors(nce_nce_handle h, int32_t *flags);
 
+/* ── Job server (serving form) ──────────────────────────────────────────────────────────────────────────────
+ * A resident server that runs many parallel-tempering jobs at once.  Jobs are admitted in submission order as
+ * device memory within the server's budget frees up (a later job that fits may start before an earlier one
+ * that does not, unless the earlier one has waited longer than starve_s); their state stays on the device until
+ * they finish.  Two host worker threads drive the GPU: one advances every running CE job with one persistent
+ * batch launch per round (continuous batching: jobs join and leave between rounds), the other the NeuralCE jobs
+ * on a few streams, so the two kinds overlap on the device.  A job's chunks depend only on its own parameters,
+ * so its result is the same alone and in any mix.  No call below waits for the device.
+ * The reference has no serving mode; these entry points are new (they replace running neuralce-mc per job). */
+typedef struct nce_server *nce_server_handle;
+
+typedef struct {
+    int64_t hbm_budget;    /* bytes of device memory for job state; 0 = 90% of the free memory at creation */
+    int32_t max_batch;     /* CE jobs per persistent launch (1..64; 0 = 64) */
+    int32_t precision;     /* CE dE precision, 32 (carried energies re-anchored exactly every chunk) or 64 */
+    int32_t warps;         /* CE warps per replica (0 = 8) */
+    int32_t nce_cluster;   /* NeuralCE CTAs per replica (0 = 1) */
+    int32_t nce_streams;   /* NeuralCE streams (0 = 4) */
+    double starve_s;       /* no job overtakes one that has waited this long (0 = 5 s) */
+} nce_server_config;
+
+#define NCE_JOB_CE   0
+#define NCE_JOB_NCE  1
+
+typedef struct {
+    int32_t kind;          /* NCE_JOB_CE (model = nce_ce_handle) or NCE_JOB_NCE (model = nce_nce_handle) */
+    void *model;           /* must stay valid until the job has finished or been cancelled */
+    int32_t R;
+    const int8_t *sigma;   /* host (R, N) initial occupancies (copied at submission) */
+    const float *beta_slot;/* host (R) */
+    const int32_t *ladder_id; /* host (R) or NULL (one ladder) */
+    int64_t n_steps;       /* MC steps per replica */
+    int64_t exchange_every;/* steps between slot exchanges = chunk length (> 0) */
+    uint64_t seed;         /* Philox key of the job's proposals and exchanges */
+    int32_t reanchor_chunks; /* NeuralCE: full cache rebuild every this many chunks (0 = ceil(N / exchange_every)) */
+    /* host outputs, written before the job is reported done (any may be NULL) */
+    int8_t *sigma_out;     /* (R, N) */
+    double *E_out;         /* (R) */
+    int64_t *n_acc_out;    /* (R) */
+    int32_t *rep_of_slot_out; /* (R) */
+    int64_t *n_ex_out;     /* (1) */
+} nce_job_desc;
+
+#define NCE_JOB_QUEUED     0
+#define NCE_JOB_RUNNING    1
+#define NCE_JOB_DONE       2
+#define NCE_JOB_CANCELLED  3
+#define NCE_JOB_FAILED     4
+
+typedef struct {
+    int32_t status;        /* NCE_JOB_* */
+    int32_t error;         /* NCE_ERR_* of a failed job */
+    int64_t steps_done, n_steps;
+    int64_t device_bytes;  /* device memory the job holds while it runs */
+    double t_submit, t_start, t_end;   /* seconds on the server's clock (steady, from creation); -1 if not yet */
+} nce_job_info;
+
+typedef struct {
+    int64_t queued, running, done, cancelled, failed;
+    int64_t bytes_used, hbm_budget;
+    int64_t rounds_ce, rounds_nce;
+    int64_t attempts;      /* swap attempts completed (replicas x steps) */
+    double now;            /* server clock */
+} nce_server_stats;
+
+int nce_server_create(const nce_server_config *cfg, nce_server_handle *out);
+int nce_server_destroy(nce_server_handle s);         /* cancels what is left and joins the workers */
+/* NCE_ERR_NOMEM when the job can never fit the budget; NCE_ERR_INVALID for bad descriptors. */
+int nce_job_submit(nce_server_handle s, const nce_job_desc *job, int64_t *job_id);
+int nce_job_poll(nce_server_handle s, int64_t job_id, nce_job_info *info);
+int nce_job_cancel(nce_server_handle s, int64_t job_id);
+int nce_server_query(nce_server_handle s, nce_server_stats *stats);
+/* text of the error that failed a job */
+int nce_job_error(nce_server_handle s, int64_t job_id, char *buf, size_t n);
+
 /* Philox4x32-10 on the host (same function the kernels use), for tests and host drivers. */
 void nce_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

@@ -59,6 +59,28 @@ class NceNceChunk(C.Structure):
                 ("ex_parity", i32), ("ex_u", vp), ("cluster", i32)]
 
 
+class NceServerConfig(C.Structure):
+    _fields_ = [("hbm_budget", i64), ("max_batch", i32), ("precision", i32), ("warps", i32), ("nce_cluster", i32),
+                ("nce_streams", i32), ("starve_s", f64)]
+
+
+class NceJobDesc(C.Structure):
+    _fields_ = [("kind", i32), ("model", vp), ("R", i32), ("sigma", vp), ("beta_slot", vp), ("ladder_id", vp),
+                ("n_steps", i64), ("exchange_every", i64), ("seed", u64), ("reanchor_chunks", i32),
+                ("sigma_out", vp), ("E_out", vp), ("n_acc_out", vp), ("rep_of_slot_out", vp), ("n_ex_out", vp)]
+
+
+class NceJobInfo(C.Structure):
+    _fields_ = [("status", i32), ("error", i32), ("steps_done", i64), ("n_steps", i64), ("device_bytes", i64),
+                ("t_submit", f64), ("t_start", f64), ("t_end", f64)]
+
+
+class NceServerStats(C.Structure):
+    _fields_ = [("queued", i64), ("running", i64), ("done", i64), ("cancelled", i64), ("failed", i64),
+                ("bytes_used", i64), ("hbm_budget", i64), ("rounds_ce", i64), ("rounds_nce", i64), ("attempts", i64),
+                ("now", f64)]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -77,6 +99,13 @@ SIGNATURES = {
     "nce_ce_errors": (i32, [vp, P(i32)]),
     "nce_pt_minimum": (i32, [P(NcePtState), vp, vp, vp]),
     "nce_philox4x32": (None, [P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)]),
+    "nce_server_create": (i32, [P(NceServerConfig), P(vp)]),
+    "nce_server_destroy": (i32, [vp]),
+    "nce_job_submit": (i32, [vp, P(NceJobDesc), P(i64)]),
+    "nce_job_poll": (i32, [vp, i64, P(NceJobInfo)]),
+    "nce_job_cancel": (i32, [vp, i64]),
+    "nce_server_query": (i32, [vp, P(NceServerStats)]),
+    "nce_job_error": (i32, [vp, i64, C.c_char_p, C.c_size_t]),
     "nce_nce_create": (i32, [P(NceNceDesc), P(vp)]),
     "nce_nce_destroy": (i32, [vp]),
     "nce_nce_full_cache": (i32, [vp, P(NceNceState), vp]),

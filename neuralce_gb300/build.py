@@ -17,7 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libnce_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["abi.cu", "ce_engine.cu", "nce_engine.cu"]
+SOURCES = ["abi.cu", "ce_engine.cu", "nce_engine.cu", "server.cu"]
 
 
 def nvcc():

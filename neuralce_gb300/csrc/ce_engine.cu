@@ -1102,6 +1102,14 @@ static int launch_delta(const CEJob &jb, int mo, int n, const int32_t *rep, cons
 
 }  // namespace nce
 
+namespace nce {
+int ce_model_dims(nce_ce_handle h, int64_t *N, int32_t *n_cols, int32_t *mo, int32_t *binary) {
+    NCE_CHECK(h, "null CE handle");
+    *N = h->N; *n_cols = h->n_cols; *mo = h->mo; *binary = (h->binary && h->erows) ? 1 : 0;
+    return NCE_OK;
+}
+}  // namespace nce
+
 using namespace nce;
 
 static int energy_impl(nce_ce_model *h, const int8_t *sigma, int32_t R, int32_t precision, double *E, int64_t *cv_out,

@@ -14,6 +14,10 @@ namespace nce {
 std::string &last_error();
 int fail(int code, const char *fmt, ...);
 
+// shapes of a model handle, for the job server's memory accounting
+int ce_model_dims(nce_ce_handle h, int64_t *N, int32_t *n_cols, int32_t *mo, int32_t *binary);
+int nce_model_dims(nce_nce_handle h, int64_t *N, int32_t *C0, int32_t *D, int32_t *depth);
+
 #define NCE_CUDA(call)                                                                        \
     do {                                                                                      \
         cudaError_t e_ = (call);                                                              \

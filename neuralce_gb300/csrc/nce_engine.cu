@@ -780,6 +780,14 @@ static NceJob make_nce_job(nce_nce_model *h, const nce_nce_state *st) {
 
 using namespace nce;
 
+namespace nce {
+int nce_model_dims(nce_nce_handle h, int64_t *N, int32_t *C0, int32_t *D, int32_t *depth) {
+    NCE_CHECK(h, "null NCE handle");
+    *N = h->dev.N; *C0 = h->dev.C0; *D = h->dev.D; *depth = h->dev.depth;
+    return NCE_OK;
+}
+}  // namespace nce
+
 extern "C" {
 
 int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {

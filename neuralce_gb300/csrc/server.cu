@@ -1,0 +1,557 @@
+// Job server of libnce_gb300 (serving form): admission by a device-memory budget, continuous batching of CE
+// jobs into one persistent launch per round, NeuralCE jobs on side streams, all state resident on the device
+// while a job runs.  Host code only; the device work is the engines' own entry points.
+//
+// Threads: the caller's threads only touch host structures under `mu` (submit, poll, cancel, query never wait
+// for the device).  Worker 0 drives the CE jobs on one stream, worker 1 the NeuralCE jobs on `nce_streams`
+// streams; each worker admits jobs of its kind, launches one round, waits for its own streams, then retires
+// finished jobs (outputs copied to the caller's host buffers, device memory returned with cudaFreeAsync).
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <limits>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "common.cuh"
+
+namespace nce {
+namespace {
+
+struct SJob {
+    int64_t id = 0;
+    nce_job_desc d{};                 // output pointers as given; input pointers replaced by the host copies
+    int64_t N = 0;
+    int32_t n_cols = 0, mo = 0, binary = 0, C0 = 0, D = 0, depth = 0;
+    std::vector<int8_t> sig; std::vector<float> beta; std::vector<int32_t> lid;
+    int64_t bytes = 0;
+    int status = NCE_JOB_QUEUED, error = 0;
+    std::string msg;
+    int64_t done = 0;
+    bool cancel = false;
+    double t_submit = -1.0, t_start = -1.0, t_end = -1.0;
+    char *dev = nullptr;              // one device block holding the job's state
+    nce_pt_state st{};
+    nce_nce_state nst{};
+    int32_t chunks = 0, anchor = 1;
+    cudaStream_t stream = nullptr;
+};
+
+inline int64_t al256(int64_t x) { return (x + 255) / 256 * 256; }
+
+// device bytes of a job's state, and the offsets of its arrays
+struct Plan {
+    std::vector<int64_t> off;
+    int64_t total = 0;
+    int64_t add(int64_t n) { off.push_back(total); total += al256(std::max<int64_t>(n, 1)); return off.back(); }
+};
+
+Plan ce_plan(int32_t R, int64_t N, int32_t n_cols, bool track) {
+    Plan p;
+    p.add((int64_t)R * N);                       // 0 sigma
+    p.add(8ll * R);                              // 1 E
+    p.add(4ll * R);                              // 2 beta
+    p.add(4ll * R); p.add(4ll * R); p.add(4ll * R);   // 3 ros, 4 sor, 5 lid
+    p.add(8ll * R);                              // 6 E_min
+    p.add(8ll * R);                              // 7 n_acc
+    p.add(8);                                    // 8 n_ex
+    p.add(track ? 8ll * R * n_cols : 0);         // 9 cv
+    return p;
+}
+
+Plan nce_plan(int32_t R, int64_t N, int32_t C0, int32_t D, int32_t depth) {
+    Plan p;
+    p.add((int64_t)R * N);                       // 0 sigma
+    p.add(4ll * R * N * C0);                     // 1 h0
+    p.add(depth >= 2 ? 4ll * (depth - 1) * R * N * D : 0);   // 2 hmid
+    p.add(4ll * R * N);                          // 3 e
+    p.add(8ll * R);                              // 4 E
+    p.add(4ll * R);                              // 5 beta
+    p.add(4ll * R); p.add(4ll * R); p.add(4ll * R);   // 6 ros, 7 sor, 8 lid
+    p.add(8ll * R);                              // 9 n_acc
+    p.add(8);                                    // 10 n_ex
+    return p;
+}
+
+}  // namespace
+}  // namespace nce
+
+using namespace nce;
+
+struct nce_server {
+    nce_server_config cfg{};
+    int device = 0;
+    std::mutex mu;
+    std::condition_variable wake;
+    std::map<int64_t, std::shared_ptr<SJob>> jobs;
+    std::deque<std::shared_ptr<SJob>> pending[2];
+    std::vector<std::shared_ptr<SJob>> active[2];
+    int64_t next_id = 1, bytes_used = 0;
+    int64_t n_done = 0, n_cancelled = 0, n_failed = 0, rounds[2] = {0, 0};
+    std::atomic<int64_t> attempts{0};
+    std::atomic<bool> stop{false};
+    std::thread worker[2];
+    std::chrono::steady_clock::time_point t0;
+    cudaStream_t ce_stream = nullptr;
+    std::vector<cudaStream_t> nce_streams;
+    int rr = 0;
+
+    double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+};
+
+namespace {
+
+// retire a job whose device memory is released (called with mu held)
+void release_locked(nce_server *S, SJob &j, int status) {
+    if (j.dev) S->bytes_used -= j.bytes;
+    j.dev = nullptr;
+    j.status = status;
+    j.t_end = S->now();
+    if (status == NCE_JOB_DONE) ++S->n_done;
+    else if (status == NCE_JOB_CANCELLED) ++S->n_cancelled;
+    else if (status == NCE_JOB_FAILED) ++S->n_failed;
+}
+
+// pick the pending jobs of `kind` that fit the budget now (mu held); reserves their bytes
+std::vector<std::shared_ptr<SJob>> admit_locked(nce_server *S, int kind) {
+    std::vector<std::shared_ptr<SJob>> out;
+    const double t = S->now();
+    // the oldest pending job of either kind; nothing overtakes it once it has waited starve_s
+    std::shared_ptr<SJob> oldest;
+    for (int k = 0; k < 2; ++k)
+        for (auto &p : S->pending[k])
+            if (!p->cancel && (!oldest || p->id < oldest->id)) oldest = p;
+    auto &q = S->pending[kind];
+    for (auto it = q.begin(); it != q.end();) {
+        auto &p = *it;
+        if (p->cancel) {
+            release_locked(S, *p, NCE_JOB_CANCELLED);
+            it = q.erase(it);
+            continue;
+        }
+        if (oldest && oldest != p && t - oldest->t_submit > S->cfg.starve_s && oldest->id < p->id) break;
+        if (S->bytes_used + p->bytes <= S->cfg.hbm_budget) {
+            S->bytes_used += p->bytes;
+            p->dev = reinterpret_cast<char *>(1);      // reserved; allocated by the worker
+            p->status = NCE_JOB_RUNNING;
+            p->t_start = t;
+            out.push_back(p);
+            it = q.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    return out;
+}
+
+void fail_job(nce_server *S, SJob &j, int rc) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    j.error = rc;
+    j.msg = last_error();
+    if (j.dev) S->bytes_used -= j.bytes;
+    j.dev = nullptr;
+    j.status = NCE_JOB_FAILED;
+    j.t_end = S->now();
+    ++S->n_failed;
+}
+
+int start_ce(nce_server *S, SJob &j, cudaStream_t s) {
+    const int32_t R = j.d.R;
+    const bool track = j.binary != 0;
+    Plan p = ce_plan(R, j.N, j.n_cols, track);
+    void *base = nullptr;
+    NCE_CUDA(cudaMallocAsync(&base, (size_t)p.total, s));
+    j.dev = (char *)base;
+    char *b = j.dev;
+    nce_pt_state &st = j.st;
+    std::memset(&st, 0, sizeof(st));
+    st.R = R; st.N = j.N; st.sigma = (int8_t *)(b + p.off[0]); st.E = (double *)(b + p.off[1]); st.beta_slot = (float *)(b + p.off[2]);
+    st.rep_of_slot = (int32_t *)(b + p.off[3]); st.slot_of_rep = (int32_t *)(b + p.off[4]); st.ladder_id = (int32_t *)(b + p.off[5]);
+    st.E_min_rep = (double *)(b + p.off[6]); st.n_acc = (int64_t *)(b + p.off[7]); st.n_ex = (int64_t *)(b + p.off[8]);
+    st.cv = track ? (int64_t *)(b + p.off[9]) : nullptr;
+    std::vector<int32_t> iota(R);
+    for (int i = 0; i < R; ++i) iota[i] = i;
+    std::vector<double> inf(R, std::numeric_limits<double>::infinity());
+    NCE_CUDA(cudaMemcpyAsync(st.sigma, j.sig.data(), (size_t)R * j.N, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync((void *)st.beta_slot, j.beta.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync((void *)st.ladder_id, j.lid.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync(st.rep_of_slot, iota.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync(st.slot_of_rep, iota.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync(st.E_min_rep, inf.data(), 8 * (size_t)R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemsetAsync(st.n_acc, 0, 8 * (size_t)R, s));
+    NCE_CUDA(cudaMemsetAsync(st.n_ex, 0, 8, s));
+    nce_ce_handle h = (nce_ce_handle)j.d.model;
+    int rc = nce_ce_energy(h, st.sigma, R, 64, st.E, s);
+    if (rc) return rc;
+    if (track) { rc = nce_ce_cluster_counts(h, st.sigma, R, st.cv, s); if (rc) return rc; }
+    NCE_CUDA(cudaMemcpyAsync(st.E_min_rep, st.E, 8, cudaMemcpyDeviceToDevice, s));   // replica 0, as PT set-up does
+    NCE_CUDA(cudaStreamSynchronize(s));                                            // host copies may be freed now
+    return NCE_OK;
+}
+
+int start_nce(nce_server *S, SJob &j, cudaStream_t s) {
+    const int32_t R = j.d.R;
+    Plan p = nce_plan(R, j.N, j.C0, j.D, j.depth);
+    void *base = nullptr;
+    NCE_CUDA(cudaMallocAsync(&base, (size_t)p.total, s));
+    j.dev = (char *)base;
+    char *b = j.dev;
+    nce_nce_state &st = j.nst;
+    std::memset(&st, 0, sizeof(st));
+    st.R = R; st.N = j.N; st.sigma = (int8_t *)(b + p.off[0]); st.h0 = (float *)(b + p.off[1]);
+    st.hmid = j.depth >= 2 ? (float *)(b + p.off[2]) : nullptr; st.e = (float *)(b + p.off[3]); st.E = (double *)(b + p.off[4]);
+    st.beta_slot = (float *)(b + p.off[5]); st.rep_of_slot = (int32_t *)(b + p.off[6]); st.slot_of_rep = (int32_t *)(b + p.off[7]);
+    st.ladder_id = (int32_t *)(b + p.off[8]); st.n_acc = (int64_t *)(b + p.off[9]); st.n_ex = (int64_t *)(b + p.off[10]);
+    std::vector<int32_t> iota(R);
+    for (int i = 0; i < R; ++i) iota[i] = i;
+    NCE_CUDA(cudaMemcpyAsync(st.sigma, j.sig.data(), (size_t)R * j.N, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync((void *)st.beta_slot, j.beta.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync((void *)st.ladder_id, j.lid.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync(st.rep_of_slot, iota.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync(st.slot_of_rep, iota.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemsetAsync(st.n_acc, 0, 8 * (size_t)R, s));
+    NCE_CUDA(cudaMemsetAsync(st.n_ex, 0, 8, s));
+    int rc = nce_nce_full_cache((nce_nce_handle)j.d.model, &st, s);
+    if (rc) return rc;
+    NCE_CUDA(cudaStreamSynchronize(s));
+    return NCE_OK;
+}
+
+// copy the outputs to the caller's buffers and return the device memory (worker thread, job's stream)
+int finish(SJob &j, cudaStream_t s) {
+    const int32_t R = j.d.R;
+    const bool ce = j.d.kind == NCE_JOB_CE;
+    const int8_t *sig = ce ? j.st.sigma : j.nst.sigma;
+    const double *E = ce ? j.st.E : j.nst.E;
+    const int64_t *na = ce ? j.st.n_acc : j.nst.n_acc;
+    const int32_t *ros = ce ? j.st.rep_of_slot : j.nst.rep_of_slot;
+    const int64_t *nx = ce ? j.st.n_ex : j.nst.n_ex;
+    if (j.d.sigma_out) NCE_CUDA(cudaMemcpyAsync(j.d.sigma_out, sig, (size_t)R * j.N, cudaMemcpyDeviceToHost, s));
+    if (j.d.E_out) NCE_CUDA(cudaMemcpyAsync(j.d.E_out, E, 8 * (size_t)R, cudaMemcpyDeviceToHost, s));
+    if (j.d.n_acc_out) NCE_CUDA(cudaMemcpyAsync(j.d.n_acc_out, na, 8 * (size_t)R, cudaMemcpyDeviceToHost, s));
+    if (j.d.rep_of_slot_out) NCE_CUDA(cudaMemcpyAsync(j.d.rep_of_slot_out, ros, 4 * (size_t)R, cudaMemcpyDeviceToHost, s));
+    if (j.d.n_ex_out) NCE_CUDA(cudaMemcpyAsync(j.d.n_ex_out, nx, 8, cudaMemcpyDeviceToHost, s));
+    NCE_CUDA(cudaFreeAsync(j.dev, s));
+    NCE_CUDA(cudaStreamSynchronize(s));
+    return NCE_OK;
+}
+
+void drop(SJob &j, cudaStream_t s) {
+    if (j.dev && j.dev != reinterpret_cast<char *>(1)) { cudaFreeAsync(j.dev, s); cudaStreamSynchronize(s); }
+}
+
+// admit, start, and take the list of running jobs of `kind`; returns false when the server stops
+bool gather(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &run) {
+    std::vector<std::shared_ptr<SJob>> fresh;
+    {
+        std::unique_lock<std::mutex> lk(S->mu);
+        for (;;) {
+            if (S->stop) return false;
+            fresh = admit_locked(S, kind);
+            // running jobs cancelled since the last round leave now
+            auto &a = S->active[kind];
+            for (auto it = a.begin(); it != a.end();) {
+                if ((*it)->cancel) {
+                    SJob &j = **it;
+                    cudaStream_t s = kind == 0 ? S->ce_stream : j.stream;
+                    lk.unlock(); drop(j, s); lk.lock();
+                    j.dev = reinterpret_cast<char *>(1);
+                    release_locked(S, j, NCE_JOB_CANCELLED);
+                    it = a.erase(it);
+                } else {
+                    ++it;
+                }
+            }
+            if (!fresh.empty() || !a.empty()) break;
+            S->wake.wait_for(lk, std::chrono::milliseconds(2));
+        }
+    }
+    for (auto &p : fresh) {
+        SJob &j = *p;
+        int rc;
+        if (kind == 0) {
+            rc = start_ce(S, j, S->ce_stream);
+        } else {
+            // jobs on one model share its scratch buffers, so they share a stream; other jobs spread over the streams
+            std::shared_ptr<SJob> twin;
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
+                for (auto &q : S->active[1]) if (q->d.model == j.d.model) twin = q;
+            }
+            j.stream = twin ? twin->stream : S->nce_streams[S->rr++ % S->nce_streams.size()];
+            rc = start_nce(S, j, j.stream);
+        }
+        if (rc) {
+            drop(j, kind == 0 ? S->ce_stream : j.stream);
+            j.dev = reinterpret_cast<char *>(1);
+            fail_job(S, j, rc);
+            continue;
+        }
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->active[kind].push_back(p);
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    run = S->active[kind];
+    return true;
+}
+
+void retire(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &run) {
+    for (auto &p : run) {
+        SJob &j = *p;
+        if (j.status != NCE_JOB_RUNNING || j.done < j.d.n_steps) continue;
+        const int rc = finish(j, kind == 0 ? S->ce_stream : j.stream);
+        std::lock_guard<std::mutex> lk(S->mu);
+        auto &a = S->active[kind];
+        a.erase(std::remove(a.begin(), a.end(), p), a.end());
+        if (rc) {
+            j.error = rc; j.msg = last_error();
+            release_locked(S, j, NCE_JOB_FAILED);
+        } else {
+            release_locked(S, j, NCE_JOB_DONE);
+        }
+    }
+}
+
+void fail_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &jobs, int rc) {
+    std::string m = last_error();
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto &a = S->active[kind];
+    for (auto &p : jobs) {
+        if (p->status != NCE_JOB_RUNNING) continue;
+        p->error = rc; p->msg = m;
+        a.erase(std::remove(a.begin(), a.end(), p), a.end());
+        release_locked(S, *p, NCE_JOB_FAILED);        // device memory stays with the failed context
+    }
+}
+
+int64_t chunk_len(const SJob &j) { return std::min(j.d.exchange_every - j.done % j.d.exchange_every, j.d.n_steps - j.done); }
+
+// CE worker: one persistent batch launch per round over every running CE job (grouped by cluster order)
+void ce_worker(nce_server *S) {
+    cudaSetDevice(S->device);
+    std::vector<std::shared_ptr<SJob>> run;
+    while (gather(S, 0, run)) {
+        if (run.empty()) continue;
+        std::map<int32_t, std::vector<std::shared_ptr<SJob>>> by_mo;
+        for (auto &p : run) by_mo[p->mo].push_back(p);
+        int rc = NCE_OK;
+        for (auto &g : by_mo) {
+            auto &v = g.second;
+            for (size_t a = 0; a < v.size() && rc == NCE_OK; a += (size_t)S->cfg.max_batch) {
+                const int n = (int)std::min<size_t>((size_t)S->cfg.max_batch, v.size() - a);
+                std::vector<nce_ce_handle> hs(n); std::vector<nce_pt_state> ss(n); std::vector<nce_pt_chunk> cs(n);
+                for (int i = 0; i < n; ++i) {
+                    SJob &j = *v[a + i];
+                    hs[i] = (nce_ce_handle)j.d.model; ss[i] = j.st;
+                    nce_pt_chunk &c = cs[i];
+                    std::memset(&c, 0, sizeof(c));
+                    c.n_steps = chunk_len(j); c.step0 = j.done; c.seed = j.d.seed; c.sample_interval = 1;
+                    c.do_exchange = ((j.done + c.n_steps) % j.d.exchange_every) == 0;
+                    c.precision = S->cfg.precision; c.warps = S->cfg.warps; c.path = 0; c.cluster = 1;
+                }
+                rc = nce_ce_run_batch(n, hs.data(), ss.data(), cs.data(), S->ce_stream);
+                for (int i = 0; i < n && rc == NCE_OK; ++i) {
+                    SJob &j = *v[a + i];
+                    if (j.st.cv) rc = nce_ce_energy_from_counts(hs[i], j.st.cv, j.d.R, j.st.E, S->ce_stream);
+                }
+                if (rc == NCE_OK)
+                    for (int i = 0; i < n; ++i) {
+                        SJob &j = *v[a + i];
+                        const int64_t len = cs[i].n_steps;
+                        j.done += len;
+                        S->attempts += len * j.d.R;
+                    }
+            }
+        }
+        if (rc == NCE_OK) {
+            const cudaError_t e = cudaStreamSynchronize(S->ce_stream);
+            if (e != cudaSuccess) rc = fail(NCE_ERR_CUDA, "CE round: %s", cudaGetErrorString(e));
+        }
+        if (rc) { fail_round(S, 0, run, rc); continue; }
+        { std::lock_guard<std::mutex> lk(S->mu); ++S->rounds[0]; }
+        retire(S, 0, run);
+    }
+}
+
+// NeuralCE worker: every running job advances one chunk per round, jobs spread over the worker's streams
+void nce_worker(nce_server *S) {
+    cudaSetDevice(S->device);
+    std::vector<std::shared_ptr<SJob>> run;
+    while (gather(S, 1, run)) {
+        if (run.empty()) continue;
+        int rc = NCE_OK;
+        for (auto &p : run) {
+            SJob &j = *p;
+            nce_nce_chunk c; std::memset(&c, 0, sizeof(c));
+            c.n_steps = chunk_len(j); c.step0 = j.done; c.seed = j.d.seed; c.sample_interval = 1;
+            c.exchange_rounds = ((j.done + c.n_steps) % j.d.exchange_every) == 0 ? 1 : 0;
+            c.cluster = S->cfg.nce_cluster;
+            rc = nce_nce_run_chunk((nce_nce_handle)j.d.model, &j.nst, &c, j.stream);
+            if (rc) break;
+            ++j.chunks;
+            if (j.chunks % j.anchor == 0) { rc = nce_nce_full_cache((nce_nce_handle)j.d.model, &j.nst, j.stream); if (rc) break; }
+            j.done += c.n_steps;
+            S->attempts += c.n_steps * j.d.R;
+        }
+        if (rc == NCE_OK)
+            for (cudaStream_t s : S->nce_streams) {
+                const cudaError_t e = cudaStreamSynchronize(s);
+                if (e != cudaSuccess) { rc = fail(NCE_ERR_CUDA, "NeuralCE round: %s", cudaGetErrorString(e)); break; }
+            }
+        if (rc) { fail_round(S, 1, run, rc); continue; }
+        { std::lock_guard<std::mutex> lk(S->mu); ++S->rounds[1]; }
+        retire(S, 1, run);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int nce_server_create(const nce_server_config *cfg, nce_server_handle *out) {
+    NCE_CHECK(out, "nce_server_create: null argument");
+    auto S = std::make_unique<nce_server>();
+    if (cfg) S->cfg = *cfg;
+    nce_server_config &c = S->cfg;
+    if (c.max_batch <= 0) c.max_batch = 64;
+    NCE_CHECK(c.max_batch <= 64, "nce_server_create: max_batch must be <= 64");
+    if (c.precision == 0) c.precision = 32;
+    NCE_CHECK(c.precision == 32 || c.precision == 64, "nce_server_create: precision must be 32 or 64");
+    if (c.warps <= 0) c.warps = 8;
+    NCE_CHECK(c.warps <= 32, "nce_server_create: warps must be <= 32");
+    if (c.nce_cluster <= 0) c.nce_cluster = 1;
+    if (c.nce_streams <= 0) c.nce_streams = 4;
+    NCE_CHECK(c.nce_streams <= 32, "nce_server_create: nce_streams must be <= 32");
+    if (c.starve_s <= 0.0) c.starve_s = 5.0;
+    NCE_CUDA(cudaGetDevice(&S->device));
+    if (c.hbm_budget <= 0) {
+        size_t fr = 0, tot = 0;
+        NCE_CUDA(cudaMemGetInfo(&fr, &tot));
+        c.hbm_budget = (int64_t)(0.9 * (double)fr);
+    }
+    NCE_CUDA(cudaStreamCreateWithFlags(&S->ce_stream, cudaStreamNonBlocking));
+    for (int i = 0; i < c.nce_streams; ++i) {
+        cudaStream_t s;
+        NCE_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        S->nce_streams.push_back(s);
+    }
+    // keep freed job memory in the pool for the next admissions instead of returning it to the driver
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, S->device) == cudaSuccess) {
+        uint64_t keep = (uint64_t)c.hbm_budget;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    S->t0 = std::chrono::steady_clock::now();
+    nce_server *raw = S.release();
+    raw->worker[0] = std::thread(ce_worker, raw);
+    raw->worker[1] = std::thread(nce_worker, raw);
+    *out = raw;
+    return NCE_OK;
+}
+
+int nce_server_destroy(nce_server_handle S) {
+    if (!S) return NCE_OK;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stop = true;
+    }
+    S->wake.notify_all();
+    for (auto &w : S->worker) if (w.joinable()) w.join();
+    for (int k = 0; k < 2; ++k)
+        for (auto &p : S->active[k]) drop(*p, k == 0 ? S->ce_stream : p->stream);
+    cudaStreamDestroy(S->ce_stream);
+    for (cudaStream_t s : S->nce_streams) cudaStreamDestroy(s);
+    delete S;
+    return NCE_OK;
+}
+
+int nce_job_submit(nce_server_handle S, const nce_job_desc *d, int64_t *job_id) {
+    NCE_CHECK(S && d && job_id, "nce_job_submit: null argument");
+    NCE_CHECK(d->kind == NCE_JOB_CE || d->kind == NCE_JOB_NCE, "nce_job_submit: kind must be NCE_JOB_CE or NCE_JOB_NCE");
+    NCE_CHECK(d->model && d->R >= 1 && d->sigma && d->beta_slot, "nce_job_submit: model, R, sigma and beta_slot are required");
+    NCE_CHECK(d->n_steps >= 1 && d->exchange_every >= 1, "nce_job_submit: n_steps and exchange_every must be >= 1");
+    auto j = std::make_shared<SJob>();
+    j->d = *d;
+    if (d->kind == NCE_JOB_CE) {
+        int rc = ce_model_dims((nce_ce_handle)d->model, &j->N, &j->n_cols, &j->mo, &j->binary);
+        if (rc) return rc;
+        j->bytes = ce_plan(d->R, j->N, j->n_cols, j->binary != 0).total;
+        NCE_CHECK(d->R <= 25600, "nce_job_submit: too many replicas for the exchange kernel");
+    } else {
+        int rc = nce_model_dims((nce_nce_handle)d->model, &j->N, &j->C0, &j->D, &j->depth);
+        if (rc) return rc;
+        j->bytes = nce_plan(d->R, j->N, j->C0, j->D, j->depth).total;
+        j->anchor = d->reanchor_chunks > 0 ? d->reanchor_chunks
+                                          : (int32_t)std::max<int64_t>(1, (j->N + d->exchange_every - 1) / d->exchange_every);
+    }
+    j->sig.assign(d->sigma, d->sigma + (size_t)d->R * j->N);
+    j->beta.assign(d->beta_slot, d->beta_slot + d->R);
+    if (d->ladder_id) j->lid.assign(d->ladder_id, d->ladder_id + d->R);
+    else j->lid.assign(d->R, 0);
+    j->d.sigma = nullptr; j->d.beta_slot = nullptr; j->d.ladder_id = nullptr;
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (j->bytes > S->cfg.hbm_budget)
+        return fail(NCE_ERR_NOMEM, "nce_job_submit: the job needs %lld bytes of device memory, the budget is %lld",
+                    (long long)j->bytes, (long long)S->cfg.hbm_budget);
+    j->id = S->next_id++;
+    j->t_submit = S->now();
+    S->jobs[j->id] = j;
+    S->pending[d->kind].push_back(j);
+    *job_id = j->id;
+    S->wake.notify_all();
+    return NCE_OK;
+}
+
+int nce_job_poll(nce_server_handle S, int64_t id, nce_job_info *info) {
+    NCE_CHECK(S && info, "nce_job_poll: null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->jobs.find(id);
+    NCE_CHECK(it != S->jobs.end(), "nce_job_poll: unknown job %lld", (long long)id);
+    const SJob &j = *it->second;
+    info->status = j.status; info->error = j.error; info->steps_done = j.done; info->n_steps = j.d.n_steps;
+    info->device_bytes = j.bytes; info->t_submit = j.t_submit; info->t_start = j.t_start; info->t_end = j.t_end;
+    return NCE_OK;
+}
+
+int nce_job_cancel(nce_server_handle S, int64_t id) {
+    NCE_CHECK(S, "nce_job_cancel: null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->jobs.find(id);
+    NCE_CHECK(it != S->jobs.end(), "nce_job_cancel: unknown job %lld", (long long)id);
+    SJob &j = *it->second;
+    if (j.status == NCE_JOB_QUEUED || j.status == NCE_JOB_RUNNING) j.cancel = true;
+    S->wake.notify_all();
+    return NCE_OK;
+}
+
+int nce_server_query(nce_server_handle S, nce_server_stats *o) {
+    NCE_CHECK(S && o, "nce_server_query: null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    o->queued = (int64_t)(S->pending[0].size() + S->pending[1].size());
+    o->running = (int64_t)(S->active[0].size() + S->active[1].size());
+    o->done = S->n_done; o->cancelled = S->n_cancelled; o->failed = S->n_failed;
+    o->bytes_used = S->bytes_used; o->hbm_budget = S->cfg.hbm_budget;
+    o->rounds_ce = S->rounds[0]; o->rounds_nce = S->rounds[1];
+    o->attempts = S->attempts.load();
+    o->now = S->now();
+    return NCE_OK;
+}
+
+int nce_job_error(nce_server_handle S, int64_t id, char *buf, size_t n) {
+    NCE_CHECK(S && buf && n > 0, "nce_job_error: bad argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->jobs.find(id);
+    NCE_CHECK(it != S->jobs.end(), "nce_job_error: unknown job %lld", (long long)id);
+    std::snprintf(buf, n, "%s", it->second->msg.c_str());
+    return NCE_OK;
+}
+
+}  // extern "C"

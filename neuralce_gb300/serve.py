@@ -1,0 +1,142 @@
+"""Serving form: a resident job server for parallel-tempering jobs (``nce_server_*`` / ``nce_job_*`` in
+libnce_gb300).
+
+Jobs of different cells, replica counts, compositions and models (CE or NeuralCE) are submitted while others run;
+the server admits them in submission order as device memory within its budget frees up, keeps their state on
+the device, advances every running CE job with one persistent batch launch per round (continuous batching) and
+the NeuralCE jobs on side streams, and copies each job's final state into host arrays when it finishes.  A job's
+chunks (exchange interval, Philox key and global step of every chunk) depend only on its own parameters, so its
+result is the same alone and in any mix.  The reference has no serving mode: a job here is one
+``run_pt_mcmc`` call (``neuralce/ce/pt_mcmc_ce.py:587-601``) or NeuralCE ``_run_replicas``
+(``neuralce/nce/mcmc.py:288-422``) without the file outputs.
+
+Every call here is host-only and returns at once; ``wait`` polls with sleeps.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import _lib
+
+STATUS = {0: "queued", 1: "running", 2: "done", 3: "cancelled", 4: "failed"}
+
+
+class Job:
+    """Handle of a submitted job; ``result()`` holds the final state once ``done``."""
+
+    def __init__(self, server, kind, model, R, N):
+        self.server, self.kind, self.model, self.R, self.N = server, kind, model, R, N
+        self.sigma = np.zeros((R, N), np.int8)
+        self.E = np.zeros(R, np.float64)
+        self.n_acc = np.zeros(R, np.int64)
+        self.rep_of_slot = np.zeros(R, np.int32)
+        self.n_ex = np.zeros(1, np.int64)
+        self.id = None
+
+    def info(self):
+        return self.server.poll(self)
+
+    @property
+    def status(self):
+        return self.info()["status"]
+
+    def result(self):
+        inf = self.info()
+        if inf["status"] != "done":
+            raise RuntimeError(f"job {self.id} is {inf['status']}")
+        return dict(sigma=self.sigma, E=self.E, n_acc=self.n_acc, rep_of_slot=self.rep_of_slot, n_ex=int(self.n_ex[0]),
+                    latency_s=inf["t_end"] - inf["t_submit"])
+
+
+class Server:
+    def __init__(self, hbm_budget=0, max_batch=64, precision=32, warps=8, nce_cluster=1, nce_streams=4, starve_s=5.0):
+        cfg = _lib.NceServerConfig()
+        cfg.hbm_budget, cfg.max_batch, cfg.precision, cfg.warps = int(hbm_budget), int(max_batch), int(precision), int(warps)
+        cfg.nce_cluster, cfg.nce_streams, cfg.starve_s = int(nce_cluster), int(nce_streams), float(starve_s)
+        h = C.c_void_p()
+        _lib.check(_lib.lib().nce_server_create(C.byref(cfg), C.byref(h)), "nce_server_create")
+        self._h = h
+        self._jobs = {}
+
+    def _submit(self, kind, model_handle, model, sigma, beta_slot, n_steps, exchange_every, seed, ladder_id,
+                reanchor_chunks=0):
+        sigma = np.ascontiguousarray(np.asarray(sigma, np.int8))
+        R, N = sigma.shape
+        beta = np.ascontiguousarray(np.asarray(beta_slot, np.float32))
+        if beta.shape != (R,):
+            raise ValueError(f"beta_slot must have {R} entries")
+        lid = None if ladder_id is None else np.ascontiguousarray(np.asarray(ladder_id, np.int32))
+        job = Job(self, kind, model, R, N)
+        d = _lib.NceJobDesc()
+        d.kind, d.model, d.R = kind, model_handle, R
+        d.sigma, d.beta_slot, d.ladder_id = sigma.ctypes.data, beta.ctypes.data, (lid.ctypes.data if lid is not None else None)
+        d.n_steps, d.exchange_every, d.seed = int(n_steps), int(exchange_every), int(seed) & 0xFFFFFFFFFFFFFFFF
+        d.reanchor_chunks = int(reanchor_chunks)
+        d.sigma_out, d.E_out, d.n_acc_out = job.sigma.ctypes.data, job.E.ctypes.data, job.n_acc.ctypes.data
+        d.rep_of_slot_out, d.n_ex_out = job.rep_of_slot.ctypes.data, job.n_ex.ctypes.data
+        jid = C.c_int64()
+        _lib.check(_lib.lib().nce_job_submit(self._h, C.byref(d), C.byref(jid)), "nce_job_submit")
+        job.id = int(jid.value)
+        self._jobs[job.id] = job
+        return job
+
+    def submit_ce(self, gce, sigma, beta_slot, n_steps, exchange_every=5000, seed=0, ladder_id=None):
+        """A CE parallel-tempering job: ``sigma`` (R, N) species indices in canonical site order."""
+        return self._submit(0, gce.handle.value, gce, sigma, beta_slot, n_steps, exchange_every, seed, ladder_id)
+
+    def submit_nce(self, model, sigma, beta_slot, n_steps, exchange_every=1000, seed=0, ladder_id=None, reanchor_chunks=0):
+        """A NeuralCE parallel-tempering job on an ``nce.NCEModel``; the full caches are rebuilt every
+        ``reanchor_chunks`` chunks (0: ceil(N / exchange_every), the reference driver's default)."""
+        return self._submit(1, model.handle.value, model, sigma, beta_slot, n_steps, exchange_every, seed, ladder_id,
+                            reanchor_chunks)
+
+    def poll(self, job):
+        inf = _lib.NceJobInfo()
+        _lib.check(_lib.lib().nce_job_poll(self._h, int(job.id), C.byref(inf)), "nce_job_poll")
+        out = {k: getattr(inf, k) for k, _ in inf._fields_}
+        out["status"] = STATUS[inf.status]
+        if inf.status == 4:
+            buf = C.create_string_buffer(2048)
+            _lib.lib().nce_job_error(self._h, int(job.id), buf, len(buf))
+            out["message"] = buf.value.decode(errors="replace")
+        return out
+
+    def cancel(self, job):
+        _lib.check(_lib.lib().nce_job_cancel(self._h, int(job.id)), "nce_job_cancel")
+
+    def wait(self, jobs, timeout=None, poll_s=0.0005):
+        """Poll until every job has left the queued/running states; returns their infos."""
+        t0 = time.time()
+        jobs = list(jobs)
+        while True:
+            infos = [self.poll(j) for j in jobs]
+            if all(i["status"] not in ("queued", "running") for i in infos):
+                return infos
+            if timeout is not None and time.time() - t0 > timeout:
+                raise TimeoutError(f"{sum(i['status'] in ('queued', 'running') for i in infos)} jobs still open")
+            time.sleep(poll_s)
+
+    def stats(self):
+        s = _lib.NceServerStats()
+        _lib.check(_lib.lib().nce_server_query(self._h, C.byref(s)), "nce_server_query")
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def close(self):
+        if self._h is not None:
+            _lib.lib().nce_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
