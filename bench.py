@@ -47,7 +47,8 @@ def parse():
     ap.add_argument("--L", type=int, default=8)
     ap.add_argument("--R", type=int, default=32)
     ap.add_argument("--chunk", type=int, default=5000)
-    ap.add_argument("--workload", choices=["ce", "nce", "ce-batch"], default="ce")
+    ap.add_argument("--workload", choices=["ce", "nce", "ce-batch", "serve"], default="ce")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the serving side measurement (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=3, help="chunks of the batched-form side measurement (0 = skip)")
     ap.add_argument("--nce-steps", type=int, default=3, help="chunks of the NeuralCE side measurement (0 = skip)")
     ap.add_argument("--nce-chunk", type=int, default=1000, help="MC steps per NeuralCE chunk")
@@ -266,6 +267,89 @@ def bench_batch(steps=3, warmup=1, chunk=5000, reanchor=10000, n_jobs=64, alone_
             "warps_per_replica": w, "autotune_ms": tune, "setup_s": setup}
 
 
+def bench_serve(seconds=10.0, rate=50.0, ce_scale=0.01, nce_scale=0.0002, nce_max_sites=32768, seed=4, alone_jobs=0,
+                ce_exchange=500, nce_exchange=20):
+    """Configuration 4 (serving), scaled: Poisson arrivals at ``rate`` jobs/s for ``seconds``, CE or NeuralCE 50/50,
+    sites log-uniform 256..1,048,576 (NeuralCE capped at ``nce_max_sites``), x_Pt ~ U[0.1, 0.9], R ~ U{8..128},
+    steps log-uniform 10k..1M times ``ce_scale`` / ``nce_scale``.  Jobs are submitted to the job server at their
+    arrival times (models and occupancies prepared beforehand); reports p50/p99 job latency (submission to
+    results on the host) and the aggregate swap attempts/s over the makespan.  Capacity: the stream's CE jobs
+    submitted at once, against the same jobs run one after another in the plain float64 kernel (``alone_jobs``
+    limits that to the first jobs; 0 = all)."""
+    import torch
+    from neuralce_gb300.pt import PTState, run_chunk
+    from neuralce_gb300.serve import Server
+    from neuralce_gb300.workloads import ServeModels, ladder, random_occupancy, serve_stream
+    t0 = time.time()
+    jobs = serve_stream(rate, seconds, seed, ce_scale, nce_scale, nce_max_sites)
+    models = ServeModels()
+    for j in jobs:
+        j["model"] = models.ce(j["L"]) if j["kind"] == "ce" else models.nce(j["L"])
+        j["sigma"] = random_occupancy(j["N"], j["x_pt"], j["R"], j["seed"] & 0xFFFFFFFF)
+        j["beta"] = ladder(j["R"])[1]
+    setup = time.time() - t0
+    srv = Server(precision=32, warps=8)
+    hs = []
+    start = time.perf_counter()
+    for j in jobs:
+        while time.perf_counter() - start < j["t"]:
+            time.sleep(0.0002)
+        if j["kind"] == "ce":
+            hs.append(srv.submit_ce(j["model"], j["sigma"], j["beta"], j["steps"], ce_exchange, j["seed"]))
+        else:
+            hs.append(srv.submit_nce(j["model"], j["sigma"], j["beta"], j["steps"], nce_exchange, j["seed"]))
+    infos = srv.wait(hs, timeout=1800)
+    st = srv.stats()
+    srv.close()
+    ok = [i for i in infos if i["status"] == "done"]
+    lat = np.array([i["t_end"] - i["t_submit"] for i in ok])
+    makespan = max(i["t_end"] for i in ok) - min(i["t_submit"] for i in ok)
+    kinds = {k: np.array([i["t_end"] - i["t_submit"] for i, j in zip(infos, jobs) if j["kind"] == k and i["status"] == "done"])
+             for k in ("ce", "nce")}
+    att = {k: sum(j["R"] * j["steps"] for j in jobs if j["kind"] == k) for k in ("ce", "nce")}
+    # capacity: every CE job of the stream submitted at once; then each alone, one after another, in the plain
+    # float64 kernel (general point-function products), chunks of the same exchange interval
+    ce_jobs = [j for j in jobs if j["kind"] == "ce"]
+    srv = Server(precision=32, warps=8)
+    b0 = time.perf_counter()
+    bh = [srv.submit_ce(j["model"], j["sigma"], j["beta"], j["steps"], ce_exchange, j["seed"]) for j in ce_jobs]
+    binf = srv.wait(bh, timeout=1800)
+    burst_s = max(i["t_end"] for i in binf) - min(i["t_submit"] for i in binf)
+    srv.close()
+    a_att, a_s = 0, 0.0
+    for j in ce_jobs[:alone_jobs] if alone_jobs else ce_jobs:
+        gce = j["model"]
+        E0 = gce.batched_energy(torch.as_tensor(j["sigma"]).cuda()).cpu().numpy()
+        stt = PTState(j["sigma"], E0, j["beta"], np.zeros(j["R"], np.int32))
+        run_chunk(gce, stt, 20, 0, 1, 64, 8, None, 1, None, False, path=1)
+        torch.cuda.synchronize()
+        e0 = time.perf_counter()
+        done = 0
+        while done < j["steps"]:
+            n = min(ce_exchange, j["steps"] - done)
+            run_chunk(gce, stt, n, done, j["seed"], 64, 8, None, 1, None, (done + n) % ce_exchange == 0, path=1)
+            done += n
+        torch.cuda.synchronize()
+        a_s += time.perf_counter() - e0; a_att += j["R"] * j["steps"]
+    pct = lambda a, q: float(np.percentile(a, q)) if len(a) else None
+    ce_rate = att["ce"] / makespan
+    return {"value": st["attempts"] / makespan, "unit": "swap attempts/s", "ms_per_step": 1e3 * makespan,
+            "config": f"serving: Poisson {rate:g} jobs/s for {seconds:g} s ({len(jobs)} jobs), CE/NeuralCE 50/50, "
+                      f"sites log-U 256..1M (NeuralCE <= {nce_max_sites}), x_Pt U[0.1,0.9], R U{{8..128}}, steps log-U "
+                      f"10k..1M x {ce_scale:g} (CE) / x {nce_scale:g} (NeuralCE), exchange every {ce_exchange} / {nce_exchange}; "
+                      f"CE fp32 with exact fp64 re-anchor per chunk, NeuralCE fp32",
+            "jobs": len(jobs), "done": len(ok), "failed": st["failed"],
+            "latency_s": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max()) if len(lat) else None,
+                          "ce_p50": pct(kinds["ce"], 50), "ce_p99": pct(kinds["ce"], 99),
+                          "nce_p50": pct(kinds["nce"], 50), "nce_p99": pct(kinds["nce"], 99)},
+            "makespan_s": makespan, "attempts": st["attempts"], "attempts_ce": att["ce"], "attempts_nce": att["nce"],
+            "ce_attempts_per_s_poisson": ce_rate,
+            "ce_capacity_attempts_per_s": att["ce"] / burst_s, "ce_capacity_makespan_s": burst_s,
+            "fp64_single_job_alone": (a_att / a_s) if a_s else None,
+            "ratio_ce_capacity_vs_fp64_alone": (att["ce"] / burst_s) / (a_att / a_s) if a_s else None,
+            "rounds": {"ce": st["rounds_ce"], "nce": st["rounds_nce"]}, "setup_s": setup}
+
+
 def workload_config(args, gce):
     return {"workload": f"CE parallel tempering fp{args.precision}: fcc Ni/Pt {args.L}x{args.L}x{args.L} conventional "
                         f"({gce.n_atoms} sites), R={args.R} replicas 300-1400 K, exchange every {args.chunk} steps, "
@@ -292,6 +376,16 @@ def main():
                               "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
                               "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": {"workload": r["config"]},
                               "batch": r}), flush=True)
+        return
+    if args.workload == "serve":
+        from neuralce_gb300 import _lib
+        _lib.lib()
+        r = bench_serve(seconds=args.serve_seconds or 10.0)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": r["value"], "unit": "swap attempts/s", "n_gpus": world, "steps": 1,
+                              "warmup": 0, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                              "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": {"workload": r["config"]},
+                              "serve": r}), flush=True)
         return
     if args.workload == "nce":
         from neuralce_gb300 import _lib
@@ -390,6 +484,9 @@ def main():
     batch_line = None
     if rank == 0 and args.batch_steps > 0:
         batch_line = bench_batch(steps=args.batch_steps)
+    serve_line = None
+    if rank == 0 and args.serve_seconds > 0:
+        serve_line = bench_serve(seconds=args.serve_seconds)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, cores, sample = cpu_oracle_rate(args.L, R)
@@ -400,7 +497,7 @@ def main():
                 "vs_baseline": value / H100_PUBLISHED if (args.L == 8 and args.R == 32) else None,
                 "dtype": "f64" if args.precision == 64 else "f32", "data": "synthetic (seeded lattice, random-normal ECIs)",
                 "config": workload_config(args, gce), "clocks": clocks, "e2e": e2e, "gpu_launches": 2 * args.steps,
-                "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "batch": batch_line,
+                "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "batch": batch_line, "serve": serve_line,
                 "launch": {"warps_per_cta": args.warps, "ctas_per_replica": args.cluster,
                            "path": ["auto", "general", "sign-parity"][args.path],
                            "autotune_ms": tuned},

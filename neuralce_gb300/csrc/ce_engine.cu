@@ -554,85 +554,99 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     if (CLUSTER) cg::this_cluster().sync();              // no CTA leaves while others may still add into its counters
 }
 
-// Full energy on the sign-parity tables: E = zerolet + sum_c eci_c * (sum over sites of the parities of the rows anchored
-// at the site).  Persistent blocks per replica stage the anchored-row tables in shared memory; one warp per site
-// gathers the site's neighbourhood bits, then folds the anchored rows (each cluster instance of the cell exactly
-// once) in column-aligned chunks of 32 into exact integer counts per column.
-template <int MO>
-__global__ void __launch_bounds__(256) ce_energy_bin_kernel(const __grid_constant__ CEJob jb, const int8_t *__restrict__ sigma,
-                                                             const uint16_t *__restrict__ erows, const uint32_t *__restrict__ echunks,
-                                                             const int32_t *__restrict__ n_echunks, int32_t max_echunks,
-                                                             const double *__restrict__ ecol, uint32_t sbit_mask, double *partial,
-                                                             unsigned long long *cv_out) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
-    const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc, n_cols = jb.n_cols, nB = jb.nB, J = jb.J;
-    // shared: bix (nB, J, MO) | erows (nB, J) | echunks (nB, max_echunks) | nb (nB, n_nbr) int4 | counts | bits
-    size_t o = 0;
-    auto al = [](size_t x) { return (x + 15) / 16 * 16; };
-    uint16_t *sbix = reinterpret_cast<uint16_t *>(smem + o); o = al(o + sizeof(uint16_t) * (size_t)nB * J * MO);
-    uint16_t *serows = reinterpret_cast<uint16_t *>(smem + o); o = al(o + sizeof(uint16_t) * (size_t)nB * J);
-    uint32_t *sech = reinterpret_cast<uint32_t *>(smem + o); o = al(o + sizeof(uint32_t) * (size_t)nB * max_echunks);
-    int4 *snb = reinterpret_cast<int4 *>(smem + o); o = al(o + sizeof(int4) * (size_t)nB * n_nbr);
-    long long *cnt = reinterpret_cast<long long *>(smem + o); o = al(o + sizeof(long long) * (size_t)nw * n_cols);
-    uint8_t *bits = smem + o;
-    for (size_t i = tid; i < (size_t)nB * J * MO; i += nt) sbix[i] = __ldg(jb.bix + i);
-    for (size_t i = tid; i < (size_t)nB * J; i += nt) serows[i] = __ldg(erows + i);
-    for (size_t i = tid; i < (size_t)nB * max_echunks; i += nt) sech[i] = __ldg(echunks + i);
-    for (int i = tid; i < nB * n_nbr; i += nt)
-        snb[i] = make_int4(__ldg(jb.nb_uo + 3 * i), __ldg(jb.nb_uo + 3 * i + 1), __ldg(jb.nb_uo + 3 * i + 2), __ldg(jb.nb_b + i));
-    for (int i = tid; i < nw * n_cols; i += nt) cnt[i] = 0;
+// Full energy on the sign-parity tables, bit-sliced.  The occupancies become bit planes: per replica, point-
+// function column with sign changes and basis site, one row of 2 * d2 bits per (k0, k1) holding the sign bit of
+// every k2 twice over, so that any offset in [0, d2) reads 32 consecutive bits with one funnel shift.  A thread
+// then takes 32 consecutive anchors along k2 and, for every cluster instance anchored at a site (the reverse rows
+// of slot 0: each instance of the cell exactly once), XORs the members' shifted plane words: bit j is the parity
+// of anchor j's product and the column's sum gains (valid anchors) - 2 popcount(parity).  Counts are exact
+// integers; E = zerolet + sum_c eci_c * count_c follows in float64.
+__global__ void ce_bitplane_kernel(const int8_t *__restrict__ sigma, int32_t R, int64_t N, int32_t nB, int64_t d0d1, int32_t d2,
+                                   int32_t W2, const int32_t *__restrict__ plane_pfc, int32_t n_pl,
+                                   const uint8_t *__restrict__ sbits, uint32_t *__restrict__ planes) {
+    // one warp per plane row (replica, plane, basis, k0 * d1 + k1)
+    const int64_t rows = (int64_t)R * n_pl * nB * d0d1;
+    const int lane = threadIdx.x & 31;
+    const int64_t wstride = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < rows; w += wstride) {
+        const int64_t kk = w % d0d1;
+        int64_t t = w / d0d1;
+        const int b = (int)(t % nB); t /= nB;
+        const int pl = (int)(t % n_pl);
+        const int64_t r = t / n_pl;
+        const uint8_t *sb = sbits + 4 * plane_pfc[pl];
+        const int8_t *sg = sigma + r * N + kk * d2 * nB + b;
+        uint32_t *out = planes + w * W2;
+        for (int q = 0; q < W2; ++q) {
+            const int pos = q * 32 + lane;
+            uint32_t bit = 0;
+            if (pos < 2 * d2) {
+                const int k2 = pos < d2 ? pos : pos - d2;
+                bit = sb[sg[(int64_t)k2 * nB] & 3];
+            }
+            const uint32_t word = __ballot_sync(0xffffffffu, bit != 0u);
+            if (lane == 0) out[q] = word;
+        }
+    }
+}
+
+// grid (item blocks x row slices, nB, R): threads over the (k0, k1, 32-anchor word) items of anchor basis
+// blockIdx.y, replica blockIdx.z; a small cell's rows are split into slices over more blocks.  Every lane of a
+// warp walks the same rows (lanes past the last item count nothing).
+__global__ void __launch_bounds__(256) ce_energy_bits_kernel(const uint32_t *__restrict__ planes, int32_t P, int32_t d0, int32_t d1,
+                                                              int32_t d2, int32_t W2, const uint32_t *__restrict__ brows,
+                                                              const int4 *__restrict__ bmem, const int32_t *__restrict__ brow_off,
+                                                              const int32_t *__restrict__ brow_n, int32_t n_cols, int32_t slices,
+                                                              unsigned long long *__restrict__ cv) {
+    extern __shared__ unsigned long long ccnt[];
+    const int b = blockIdx.y, r = blockIdx.z, lane = threadIdx.x & 31;
+    const int slice = (int)(blockIdx.x % (unsigned)slices), iblk = (int)(blockIdx.x / (unsigned)slices);
+    const int iblocks = (int)(gridDim.x / (unsigned)slices);
+    for (int c = threadIdx.x; c < n_cols; c += blockDim.x) ccnt[c] = 0ull;
     __syncthreads();
-    uint8_t *wb = bits + (size_t)warp * n_pfc * n_nbr;
-    long long *wc = cnt + (size_t)warp * n_cols;
-    const int r = blockIdx.y;
-    const int8_t *sig = sigma + (int64_t)r * jb.N;
-    for (int64_t s = (int64_t)blockIdx.x * nw + warp; s < jb.N; s += (int64_t)gridDim.x * nw) {
-        int32_t b, k[3];
-        site_coords32(jb, s, b, k);
-        for (int n = lane; n < n_nbr; n += 32) {
-            const int4 e = snb[b * n_nbr + n];
-            const uint32_t st = ((((uint32_t)wrap_add(k[0], e.x, jb.d0) * (uint32_t)jb.d1 + (uint32_t)wrap_add(k[1], e.y, jb.d1)) *
-                                  (uint32_t)jb.d2 + (uint32_t)wrap_add(k[2], e.z, jb.d2)) * (uint32_t)jb.nB + (uint32_t)e.w);
-            const int so = sig[st];
-            for (int c = 0; c < n_pfc; ++c) wb[c * n_nbr + n] = (uint8_t)((sbit_mask >> (c * 4 + so)) & 1u);
+    const int Wn = (d2 + 31) >> 5;
+    const int64_t items = (int64_t)d0 * d1 * Wn;
+    const uint32_t *pr = planes + (int64_t)r * P * d0 * d1 * W2;
+    const int nall = brow_n[b];
+    const int q0 = (int)((int64_t)nall * slice / slices), q1 = (int)((int64_t)nall * (slice + 1) / slices);
+    const uint32_t *rows = brows + brow_off[b];
+    auto flush = [&](int col, int acc) {
+        const int sum = (int)__reduce_add_sync(0xffffffffu, (unsigned)acc);
+        if (lane == 0 && sum) atomicAdd(&ccnt[col], (unsigned long long)(long long)sum);
+    };
+    for (int64_t base = (int64_t)iblk * blockDim.x; base < items; base += (int64_t)iblocks * blockDim.x) {
+        const int64_t it = base + threadIdx.x;
+        const bool live = it < items;
+        const int64_t itc = live ? it : 0;
+        const int w = (int)(itc % Wn);
+        const int64_t kk = itc / Wn;
+        const int k1 = (int)(kk % d1), k0 = (int)(kk / d1);
+        const int nv = live ? min(32, d2 - 32 * w) : 0;
+        const uint32_t mask = nv >= 32 ? 0xffffffffu : ((1u << nv) - 1u);
+        int col = -1, acc = 0;
+        for (int q = q0; q < q1; ++q) {
+            const uint32_t rd = __ldg(rows + q);
+            const int c = (int)(rd & 0xffu), nm = (int)((rd >> 8) & 0xfu), st = (int)(rd >> 12);
+            if (c != col) {
+                if (col >= 0) flush(col, acc);
+                col = c; acc = 0;
+            }
+            uint32_t par = 0;
+            for (int m = 0; m < nm; ++m) {
+                const int4 e = __ldg(bmem + st + m);           // (plane, uo0, uo1, uo2)
+                int a0 = k0 + e.y; a0 -= a0 >= d0 ? d0 : 0;
+                int a1 = k1 + e.z; a1 -= a1 >= d1 ? d1 : 0;
+                const int pos = 32 * w + e.w;
+                const uint32_t *row = pr + (((int64_t)e.x * d0 + a0) * d1 + a1) * W2 + (pos >> 5);
+                par ^= __funnelshift_r(__ldg(row), __ldg(row + 1), (unsigned)(pos & 31));
+            }
+            acc += nv - 2 * __popc(par & mask);
         }
-        __syncwarp();
-        const int nch = __ldg(n_echunks + b);
-        auto chunk_sign = [&](int q, int &col) -> int {
-            const uint32_t d = sech[(size_t)b * max_echunks + q];
-            col = (int)(d & 0xffu);
-            const int start = (int)((d >> 8) & 0xffffu), len = (int)(d >> 24);
-            if (lane >= len) return 0;
-            const int j = serows[(size_t)b * J + start + lane];
-            const uint16_t *bx = sbix + ((size_t)b * J + j) * MO;
-            unsigned x = 0;
-#pragma unroll
-            for (int m = 0; m < MO; ++m) x ^= wb[bx[m]];
-            return (x & 1u) ? -1 : 1;
-        };
-        for (int q = 0; q < nch; q += 2) {
-            int c1 = 0, c2 = 0;
-            const int s1 = chunk_sign(q, c1);
-            const int s2 = (q + 1 < nch) ? chunk_sign(q + 1, c2) : 0;
-            const int n1 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s1);
-            const int n2 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s2);
-            if (lane == 0) { wc[c1] += n1; if (q + 1 < nch) wc[c2] += n2; }
-        }
-        __syncwarp();
+        if (col >= 0) flush(col, acc);
     }
     __syncthreads();
-    if (warp == 0) {
-        double part = 0.0;
-        for (int c = lane; c < n_cols; c += 32) {
-            long long tot = 0;
-            for (int w = 0; w < nw; ++w) tot += cnt[(size_t)w * n_cols + c];
-            part += ecol[c] * (double)tot;
-            if (cv_out) atomicAdd(cv_out + (int64_t)r * n_cols + c, (unsigned long long)tot);   // two's complement sum
-        }
-        for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
-        if (lane == 0) partial[(int64_t)r * gridDim.x + blockIdx.x] = part;
-    }
+    for (int c = threadIdx.x; c < n_cols; c += blockDim.x)
+        if (ccnt[c]) atomicAdd(cv + (int64_t)r * n_cols + c, ccnt[c]);
 }
 
 // E[r] = zerolet + sum_c eci_c * cv[r, c], columns in order (one thread per configuration)
@@ -797,9 +811,13 @@ struct nce_ce_model {
     uint8_t *sbits = nullptr; uint16_t *bix = nullptr; uint8_t *rcol = nullptr; double *ecol2_64 = nullptr; float *ecol2_32 = nullptr;
     int32_t n_cols = 0;
     uint32_t *chunks = nullptr; int32_t *n_chunks = nullptr; int32_t max_chunks = 0;
-    uint16_t *erows = nullptr; uint32_t *echunks = nullptr; int32_t *n_echunks = nullptr; int32_t max_echunks = 0;
+    // bit-sliced full energy: rows anchored at a site (col | members << 8 | first member << 12) per anchor basis,
+    // members (plane, uo0, uo1, uo2), the point-function column of each plane
+    uint32_t *brows = nullptr; int4 *bmem = nullptr; int32_t *brow_off = nullptr, *brow_n = nullptr;
+    int32_t *plane_pfc = nullptr; int32_t n_planes = 0;
     double *ecol1 = nullptr;                 // eci of each column (full-energy kernel)
-    uint32_t sbit_mask = 0;                  // sign bit of point function (column c, species q) at bit c*4+q
+    uint32_t *planes = nullptr; size_t planes_n = 0;        // scratch: bit planes of the configurations
+    int64_t *cv_scratch = nullptr; size_t cv_scratch_n = 0;  // scratch: cluster-vector sums for the energy
     double *energy_partial = nullptr; size_t energy_partial_n = 0;
     int device = 0;
     std::mutex mu;
@@ -819,7 +837,7 @@ static int upload(T *&dst, const T *src, size_t n) {
 
 static int free_model(nce_ce_model *m) {
     void *ptrs[] = {m->loc, m->pfc, m->eci64, m->eci32, m->rv_len, m->nb_b, m->nb_uo, m->pf64, m->pf32, m->act_b,
-                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->bix, m->rcol, m->ecol2_64, m->ecol2_32, m->chunks, m->n_chunks, m->erows, m->echunks, m->n_echunks, m->ecol1,
+                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->bix, m->rcol, m->ecol2_64, m->ecol2_32, m->chunks, m->n_chunks, m->brows, m->bmem, m->brow_off, m->brow_n, m->plane_pfc, m->ecol1, m->planes, m->cv_scratch,
                     m->energy_partial, m->staging_base};
     for (void *p : ptrs) if (p) cudaFree(p);
     delete m;
@@ -1105,7 +1123,7 @@ static int launch_delta(const CEJob &jb, int mo, int n, const int32_t *rep, cons
 namespace nce {
 int ce_model_dims(nce_ce_handle h, int64_t *N, int32_t *n_cols, int32_t *mo, int32_t *binary) {
     NCE_CHECK(h, "null CE handle");
-    *N = h->N; *n_cols = h->n_cols; *mo = h->mo; *binary = (h->binary && h->erows) ? 1 : 0;
+    *N = h->N; *n_cols = h->n_cols; *mo = h->mo; *binary = (h->binary && h->brows) ? 1 : 0;
     return NCE_OK;
 }
 }  // namespace nce
@@ -1211,8 +1229,6 @@ int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
             for (size_t i = 0; i < nl; ++i) bx[i] = (uint16_t)(t->Rv_pfc[i] * t->n_nbr + t->Rv_loc[i]);
             for (size_t i = 0; i < rc8.size(); ++i) rc8[i] = (uint8_t)std::max(0, std::min(254, t->Rv_col[i]));
             rc = upload(m->sbits, sb.data(), sb.size());
-            for (int c = 0; c < t->n_pfc && c < 8; ++c)
-                for (int q = 0; q < 4; ++q) m->sbit_mask |= (uint32_t)(sb[(size_t)c * 4 + q] & 1u) << (c * 4 + q);
             if (!rc) rc = upload(m->bix, bx.data(), bx.size());
             if (!rc) rc = upload(m->rcol, rc8.data(), rc8.size());
             if (!rc) rc = upload(m->ecol2_64, e2.data(), e2.size());
@@ -1240,30 +1256,42 @@ int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
             m->n_cols = t->n_cols;
             // rows anchored at the site (slot 0): every cluster instance of the cell exactly once, for the full energy
             if (t->Rv_slot && !rc) {
-                std::vector<uint16_t> er((size_t)t->nB * t->J, 0);
-                std::vector<std::vector<uint32_t>> ec(t->nB);
-                for (int b = 0; b < t->nB; ++b) {
-                    int ne = 0;
-                    for (int q = 0; q < t->Rv_len[b]; ++q)
-                        if (t->Rv_slot[(size_t)b * t->J + q] == 0) er[(size_t)b * t->J + ne++] = (uint16_t)q;
-                    int q = 0;
-                    while (q < ne) {
-                        const int c = t->Rv_col[(size_t)b * t->J + er[(size_t)b * t->J + q]];
-                        int e = q;
-                        while (e < ne && e - q < 32 && t->Rv_col[(size_t)b * t->J + er[(size_t)b * t->J + e]] == c) ++e;
-                        ec[b].push_back((uint32_t)c | ((uint32_t)q << 8) | ((uint32_t)(e - q) << 24));
-                        q = e;
-                    }
+                std::vector<int32_t> pmap((size_t)t->n_pfc, -1), ppfc;
+                for (int c = 0; c < t->n_pfc; ++c) {
+                    bool any = false;
+                    for (int q = 0; q < 4; ++q) any = any || (sb[(size_t)c * 4 + q] != 0);
+                    if (any) { pmap[c] = (int32_t)ppfc.size(); ppfc.push_back(c); }
                 }
-                size_t me = 1;
-                for (auto &v : ec) me = std::max(me, v.size());
-                std::vector<uint32_t> ef((size_t)t->nB * me, 0u); std::vector<int32_t> ne((size_t)t->nB);
-                for (int b = 0; b < t->nB; ++b) { ne[b] = (int32_t)ec[b].size(); std::copy(ec[b].begin(), ec[b].end(), ef.begin() + (size_t)b * me); }
-                if (!rc) rc = upload(m->erows, er.data(), er.size());
-                if (!rc) rc = upload(m->echunks, ef.data(), ef.size());
-                if (!rc) rc = upload(m->n_echunks, ne.data(), ne.size());
-                if (!rc) rc = upload(m->ecol1, colv.data(), colv.size());
-                m->max_echunks = (int32_t)me;
+                std::vector<uint32_t> rows; std::vector<int4> mem; std::vector<int32_t> roff(t->nB), rn(t->nB);
+                for (int b = 0; b < t->nB; ++b) {
+                    roff[b] = (int32_t)rows.size();
+                    for (int q = 0; q < t->Rv_len[b]; ++q) {
+                        if (t->Rv_slot[(size_t)b * t->J + q] != 0) continue;
+                        const uint32_t start = (uint32_t)mem.size();
+                        int nm = 0;
+                        for (int k = 0; k < t->mo; ++k) {
+                            const size_t e = ((size_t)b * t->J + q) * t->mo + k;
+                            const int pl = pmap[t->Rv_pfc[e]];
+                            if (pl < 0) continue;                          // constant point function (padded member)
+                            const int loc = t->Rv_loc[e];
+                            const size_t nb = (size_t)b * t->n_nbr + loc;
+                            mem.push_back(make_int4(pl * t->nB + t->nb_b[nb], t->nb_uo[3 * nb], t->nb_uo[3 * nb + 1], t->nb_uo[3 * nb + 2]));
+                            ++nm;
+                        }
+                        if (nm > 15 || start >= (1u << 20)) { bin = false; break; }
+                        rows.push_back((uint32_t)t->Rv_col[(size_t)b * t->J + q] | ((uint32_t)nm << 8) | (start << 12));
+                    }
+                    rn[b] = (int32_t)rows.size() - roff[b];
+                }
+                if (bin && !ppfc.empty()) {
+                    if (!rc) rc = upload(m->brows, rows.data(), rows.size());
+                    if (!rc) rc = upload(m->bmem, mem.data(), mem.size());
+                    if (!rc) rc = upload(m->brow_off, roff.data(), roff.size());
+                    if (!rc) rc = upload(m->brow_n, rn.data(), rn.size());
+                    if (!rc) rc = upload(m->plane_pfc, ppfc.data(), ppfc.size());
+                    if (!rc) rc = upload(m->ecol1, colv.data(), colv.size());
+                    m->n_planes = (int32_t)ppfc.size();
+                }
             }
             m->binary = !rc;
         }
@@ -1288,7 +1316,7 @@ int nce_ce_energy(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t preci
 
 int nce_ce_cluster_counts(nce_ce_handle h, const int8_t *sigma, int32_t R, int64_t *cv, void *stream) {
     NCE_CHECK(h && sigma && cv && R >= 1, "nce_ce_cluster_counts: bad argument");
-    NCE_CHECK(h->binary && h->erows && h->mo <= 8, "nce_ce_cluster_counts: needs point functions in {-1, +1}");
+    NCE_CHECK(h->binary && h->brows, "nce_ce_cluster_counts: needs point functions in {-1, +1}");
     std::lock_guard<std::mutex> lk(h->mu);
     cudaStream_t s = (cudaStream_t)stream;
     NCE_CUDA(cudaMemsetAsync(cv, 0, sizeof(int64_t) * (size_t)R * h->n_cols, s));
@@ -1309,6 +1337,55 @@ int nce_ce_energy_from_counts(nce_ce_handle h, const int64_t *cv, int32_t R, dou
 // kernel only, zeroed by the caller); E may be null when only the sums are wanted
 static int energy_impl(nce_ce_model *h, const int8_t *sigma, int32_t R, int32_t precision, double *E, int64_t *cv_out,
                        cudaStream_t s) {
+    if (h->binary && h->brows) {
+        // sign-parity full energy, bit-sliced: planes of the configurations, exact column sums, float64 energy
+        NCE_CHECK(R <= 65535, "energy: at most 65535 configurations per call");
+        const int64_t d0 = h->d[0], d1 = h->d[1], d2 = h->d[2];
+        NCE_CHECK(d2 < (1 << 28) && d0 * d1 < (1ll << 40), "energy: lattice too large");
+        const int32_t W2 = (int32_t)((2 * d2 + 31) / 32 + 1);
+        const int32_t P = h->n_planes * h->nB;
+        const size_t need_p = (size_t)R * P * d0 * d1 * W2;
+        if (need_p > h->planes_n) {
+            if (h->planes) { cudaStreamSynchronize(s); cudaFree(h->planes); }
+            h->planes = nullptr; h->planes_n = 0;
+            NCE_CUDA(cudaMalloc((void **)&h->planes, sizeof(uint32_t) * need_p));
+            h->planes_n = need_p;
+        }
+        int64_t *cv = cv_out;
+        if (!cv) {
+            const size_t need_c = (size_t)R * h->n_cols;
+            if (need_c > h->cv_scratch_n) {
+                if (h->cv_scratch) { cudaStreamSynchronize(s); cudaFree(h->cv_scratch); }
+                h->cv_scratch = nullptr; h->cv_scratch_n = 0;
+                NCE_CUDA(cudaMalloc((void **)&h->cv_scratch, sizeof(int64_t) * need_c));
+                h->cv_scratch_n = need_c;
+            }
+            cv = h->cv_scratch;
+            NCE_CUDA(cudaMemsetAsync(cv, 0, sizeof(int64_t) * need_c, s));
+        }
+        const int64_t prow = (int64_t)R * P * d0 * d1;
+        const int pb = (int)std::min<int64_t>((prow + 7) / 8, 1 << 20);
+        ce_bitplane_kernel<<<pb, 256, 0, s>>>(sigma, R, h->N, h->nB, d0 * d1, (int32_t)d2, W2, h->plane_pfc, h->n_planes, h->sbits,
+                                              h->planes);
+        NCE_CUDA(cudaGetLastError());
+        const int64_t items = d0 * d1 * ((d2 + 31) / 32);
+        const int64_t ib = std::min<int64_t>((items + 255) / 256, 8192);
+        // small cells: split the rows so that the launch still covers the SMs (about 4 blocks per SM)
+        int nsm = 152;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
+        const int64_t have = ib * h->nB * R;
+        const int slices = (int)std::max<int64_t>(1, std::min<int64_t>(32, (4ll * nsm + have - 1) / have));
+        ce_energy_bits_kernel<<<dim3((unsigned)(ib * slices), h->nB, R), 256, sizeof(unsigned long long) * h->n_cols, s>>>(
+            h->planes, P, (int32_t)d0, (int32_t)d1, (int32_t)d2, W2, h->brows, h->bmem, h->brow_off, h->brow_n, h->n_cols, slices,
+            (unsigned long long *)cv);
+        NCE_CUDA(cudaGetLastError());
+        if (E) {
+            ce_energy_counts_kernel<<<(R + 127) / 128, 128, 0, s>>>(cv, R, h->n_cols, h->ecol1, h->zerolet, E);
+            NCE_CUDA(cudaGetLastError());
+        }
+        return NCE_OK;
+    }
+    NCE_CHECK(E && !cv_out, "energy: cluster-vector sums need the sign-parity tables");
     const int threads = 256;
     int nblk = (int)std::min<int64_t>((h->n_cells + threads - 1) / threads, 1184);
     nblk = std::max(nblk, 1);
@@ -1319,47 +1396,6 @@ static int energy_impl(nce_ce_model *h, const int8_t *sigma, int32_t R, int32_t 
         NCE_CUDA(cudaMalloc((void **)&h->energy_partial, sizeof(double) * need));
         h->energy_partial_n = need;
     }
-    if (h->binary && h->erows && h->mo <= 8) {
-        // sign-parity full energy: persistent blocks (about four per SM over all configurations), 8 warps each
-        const int wpb = 8;
-        int nsm = 152;
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
-        const int64_t want = std::max<int64_t>(1, (int64_t)4 * nsm / R);
-        const int64_t nb2 = std::max<int64_t>(1, std::min<int64_t>(want, (h->N + wpb - 1) / wpb));
-        const size_t need2 = (size_t)nb2 * R;
-        if (need2 > h->energy_partial_n) {
-            if (h->energy_partial) { cudaStreamSynchronize(s); cudaFree(h->energy_partial); }
-            h->energy_partial = nullptr; h->energy_partial_n = 0;
-            NCE_CUDA(cudaMalloc((void **)&h->energy_partial, sizeof(double) * need2));
-            h->energy_partial_n = need2;
-        }
-        nce_pt_chunk ck0; std::memset(&ck0, 0, sizeof(ck0)); ck0.precision = 64;
-        CEJob jb = make_job(h, nullptr, &ck0, 0, true);
-        auto al = [](size_t x) { return (x + 15) / 16 * 16; };
-        const size_t sm = al(sizeof(uint16_t) * (size_t)h->nB * h->J * h->mo) + al(sizeof(uint16_t) * (size_t)h->nB * h->J) +
-                          al(sizeof(uint32_t) * (size_t)h->nB * h->max_echunks) + al(sizeof(int4) * (size_t)h->nB * h->n_nbr) +
-                          al(sizeof(long long) * wpb * h->n_cols) + (size_t)wpb * h->n_pfc * h->n_nbr;
-        NCE_CHECK(sm <= 200 * 1024, "nce_ce_energy: tables too large for the shared-memory energy kernel");
-        const uint32_t mask = h->sbit_mask;
-        NCE_CHECK(h->n_pfc <= 8, "nce_ce_energy: more than 8 point-function columns on the sign-parity path");
-        switch (h->mo) {
-#define NCE_EB(M) case M: \
-            NCE_CUDA(cudaFuncSetAttribute(ce_energy_bin_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)); \
-            ce_energy_bin_kernel<M><<<dim3((unsigned)nb2, R), wpb * 32, sm, s>>>(jb, sigma, h->erows, h->echunks, h->n_echunks, \
-                                                                                 h->max_echunks, h->ecol1, mask, h->energy_partial, \
-                                                                                 (unsigned long long *)cv_out); break;
-            NCE_EB(1) NCE_EB(2) NCE_EB(3) NCE_EB(4) NCE_EB(5) NCE_EB(6) NCE_EB(7) NCE_EB(8)
-#undef NCE_EB
-            default: break;
-        }
-        NCE_CUDA(cudaGetLastError());
-        if (E) {
-            ce_energy_finish<<<(R + 127) / 128, 128, 0, s>>>(h->energy_partial, (int32_t)nb2, R, h->zerolet, E);
-            NCE_CUDA(cudaGetLastError());
-        }
-        return NCE_OK;
-    }
-    NCE_CHECK(E && !cv_out, "energy: cluster-vector sums need the sign-parity tables");
     dim3 grid(nblk, R);
     if (precision == 64)
         ce_energy_kernel<double><<<grid, threads, 0, s>>>(sigma, h->N, h->n_cells, h->nB, (int)h->d[0], (int)h->d[1], (int)h->d[2],

@@ -89,3 +89,64 @@ def ce_batch_config(n_jobs=64, seed=2, L_range=(4, 32), R_choices=(16, 32, 64), 
         _, beta = ladder(R, T_min, T_max)
         jobs.append(dict(gce=gce, sigma=replica_configs(sig0, R, 2000 + k), beta=beta, L=L, x_pt=x, R=R, N=len(s)))
     return jobs
+
+
+def serve_stream(rate=50.0, seconds=600.0, seed=4, ce_scale=1.0, nce_scale=1.0, nce_max_sites=1 << 20,
+                 N_range=(256, 1 << 20), R_range=(8, 128), steps_range=(10_000, 1_000_000)):
+    """Serving workload: Poisson arrivals at ``rate`` jobs/s for ``seconds``; model CE or NeuralCE 50/50; sites
+    log-uniform in N_range rounded to 4 L^3 (NeuralCE cells capped at ``nce_max_sites``); Pt fraction ~ U[0.1, 0.9];
+    replicas ~ U{8..128}; steps per replica log-uniform in steps_range, multiplied by ``ce_scale`` / ``nce_scale``.
+    Returns a list of job descriptions (arrival time, kind, L, N, x_pt, R, steps, seed)."""
+    rng = np.random.default_rng(seed)
+    jobs, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            break
+        kind = "ce" if rng.random() < 0.5 else "nce"
+        N = float(np.exp(rng.uniform(np.log(N_range[0]), np.log(N_range[1]))))
+        if kind == "nce":
+            N = min(N, nce_max_sites)
+        L = max(4, int(round((N / 4.0) ** (1.0 / 3.0))))
+        x = float(rng.uniform(0.1, 0.9))
+        R = int(rng.integers(R_range[0], R_range[1] + 1))
+        steps = float(np.exp(rng.uniform(np.log(steps_range[0]), np.log(steps_range[1]))))
+        steps = max(1, int(round(steps * (ce_scale if kind == "ce" else nce_scale))))
+        jobs.append(dict(t=t, kind=kind, L=L, N=4 * L ** 3, x_pt=x, R=R, steps=steps, seed=int(rng.integers(1 << 62))))
+    return jobs
+
+
+def random_occupancy(N, x_pt, R, seed):
+    """(R, N) int8 canonical occupancies of a binary fcc cell, each replica an independent random arrangement
+    with round(x_pt N) Pt (species index 1)."""
+    rng = np.random.default_rng(seed)
+    n_pt = int(round(x_pt * N))
+    base = np.zeros(N, np.int8); base[:n_pt] = 1
+    return np.stack([rng.permutation(base) for _ in range(R)])
+
+
+class ServeModels:
+    """Per-cell models of the serving workload, built once and shared by every job on that cell (a job's model
+    must stay valid while it runs; jobs on one CE model share the CE worker's stream)."""
+
+    def __init__(self, depth=3, width=64, eci_seed=0, model_seed=0):
+        self.depth, self.width, self.eci_seed, self.model_seed = depth, width, eci_seed, model_seed
+        self._ce, self._nce = {}, {}
+
+    def ce(self, L):
+        if L not in self._ce:
+            from .ce import GPUClusterExpansion
+            cs = cluster_space()
+            s = fcc_conventional(A_FCC, (L, L, L))
+            self._ce[L] = GPUClusterExpansion((cs, synthetic_eci(cs, self.eci_seed)), s, energy_scale=len(s))
+        return self._ce[L]
+
+    def nce(self, L):
+        if L not in self._nce:
+            from .nce import NCEModel, synthetic_model
+            cs = cluster_space()
+            s = fcc_conventional(A_FCC, (L, L, L))
+            s.numbers = np.full(len(s), Z_OF["Ni"], np.int64)
+            P = synthetic_model(len(cs.orbits) + 1, self.depth, self.width, 1, self.model_seed)
+            self._nce[L] = NCEModel(cs, s, P, shell_edges=(0.0, 3.3), act="silu", pool="sum")
+        return self._nce[L]
