@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--L", type=int, default=8)
     ap.add_argument("--R", type=int, default=32)
     ap.add_argument("--chunk", type=int, default=5000)
-    ap.add_argument("--workload", choices=["ce", "nce", "ce-batch", "serve"], default="ce")
+    ap.add_argument("--workload", choices=["ce", "nce", "ce-batch", "serve", "ce-large"], default="ce")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the serving side measurement (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=3, help="chunks of the batched-form side measurement (0 = skip)")
     ap.add_argument("--nce-steps", type=int, default=3, help="chunks of the NeuralCE side measurement (0 = skip)")
@@ -300,6 +300,7 @@ def bench_serve(seconds=10.0, rate=50.0, ce_scale=0.01, nce_scale=0.0002, nce_ma
             hs.append(srv.submit_nce(j["model"], j["sigma"], j["beta"], j["steps"], nce_exchange, j["seed"]))
     infos = srv.wait(hs, timeout=1800)
     st = srv.stats()
+    failures = [i.get("message", "") for i in infos if i["status"] == "failed"][:3]
     srv.close()
     ok = [i for i in infos if i["status"] == "done"]
     lat = np.array([i["t_end"] - i["t_submit"] for i in ok])
@@ -338,7 +339,7 @@ def bench_serve(seconds=10.0, rate=50.0, ce_scale=0.01, nce_scale=0.0002, nce_ma
                       f"sites log-U 256..1M (NeuralCE <= {nce_max_sites}), x_Pt U[0.1,0.9], R U{{8..128}}, steps log-U "
                       f"10k..1M x {ce_scale:g} (CE) / x {nce_scale:g} (NeuralCE), exchange every {ce_exchange} / {nce_exchange}; "
                       f"CE fp32 with exact fp64 re-anchor per chunk, NeuralCE fp32",
-            "jobs": len(jobs), "done": len(ok), "failed": st["failed"],
+            "jobs": len(jobs), "done": len(ok), "failed": st["failed"], "failures": failures,
             "latency_s": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max()) if len(lat) else None,
                           "ce_p50": pct(kinds["ce"], 50), "ce_p99": pct(kinds["ce"], 99),
                           "nce_p50": pct(kinds["nce"], 50), "nce_p99": pct(kinds["nce"], 99)},
@@ -348,6 +349,68 @@ def bench_serve(seconds=10.0, rate=50.0, ce_scale=0.01, nce_scale=0.0002, nce_ma
             "fp64_single_job_alone": (a_att / a_s) if a_s else None,
             "ratio_ce_capacity_vs_fp64_alone": (att["ce"] / burst_s) / (a_att / a_s) if a_s else None,
             "rounds": {"ce": st["rounds_ce"], "nce": st["rounds_nce"]}, "setup_s": setup}
+
+
+def bench_large(L=136, R=256, chunk=5000, steps=3, warmup=1, precision=32, seed=0):
+    """Configuration 3 (CE part): fcc L^3 conventional cell (L = 136: 10,061,824 sites), 50/50, R temperatures
+    300-1400 K; float32 dE, float64 exchange and carried energies re-anchored exactly from the tracked
+    cluster-vector sums after every chunk.  Occupancies are drawn on the device (one seeded permutation per
+    replica).  A step is one chunk of ``chunk`` MC steps per replica + exchange + re-anchor."""
+    import torch
+    from neuralce_gb300.autotune import best_launch
+    from neuralce_gb300.pt import PTState, run_chunk
+    from neuralce_gb300.workloads import ServeModels, ladder
+    t0 = time.time()
+    gce = ServeModels().ce(L)
+    N = gce.n_atoms
+    setup_tables = time.time() - t0
+    g = torch.Generator(device="cuda"); g.manual_seed(seed)
+    n_pt = N // 2
+    sig = torch.empty((R, N), dtype=torch.int8, device="cuda")
+    for r in range(R):
+        sig[r] = (torch.randperm(N, device="cuda", generator=g) < n_pt).to(torch.int8)
+    _, beta = ladder(R)
+    st = PTState(np.zeros((R, 1), np.int8), np.zeros(R), beta, np.zeros(R, np.int32))
+    st.sigma, st.N = sig, N
+    st.E = gce.batched_energy(sig)
+    st.E_min_rep = torch.full((R,), float("inf"), dtype=torch.float64, device="cuda"); st.E_min_rep[0] = st.E[0]
+    st.track_counts(gce)
+    torch.cuda.synchronize()
+    setup = time.time() - t0
+    (w, cl), tune = best_launch(gce, st, precision, 0, (8, 16, 32), (1,), steps=200)
+    step = 0
+    from neuralce_gb300 import _lib
+
+    def one():
+        nonlocal step
+        run_chunk(gce, st, chunk, step, 77, precision, w, None, 1, None, True, path=0)
+        _lib.check(_lib.lib().nce_ce_energy_from_counts(gce.handle, st.cv.data_ptr(), R, st.E.data_ptr(), _lib.stream_ptr()),
+                   "nce_ce_energy_from_counts")             # exact float64 re-anchor, in place
+        step += chunk
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    stream = torch.cuda.current_stream()
+    for k in range(steps):
+        ev[k][0].record(stream); one(); ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    tot = sum(ms) / 1e3
+    # exactness: tracked sums vs a recount, re-anchored energies vs a float64 full recompute
+    cv_ok = bool(torch.equal(st.cv, gce.cluster_counts(st.sigma)))
+    Ef = gce.batched_energy(st.sigma)
+    torch.cuda.synchronize()
+    a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a_.record(); gce.batched_energy(st.sigma); b_.record(); torch.cuda.synchronize()
+    return {"value": R * chunk * steps / tot, "unit": "swap attempts/s", "ms_per_step": float(np.mean(ms)),
+            "config": f"CE large cell: fcc {L}^3 conventional ({N} sites), R={R} 300-1400 K, fp{precision} dE, chunk {chunk} "
+                      f"steps + fp64 exchange + exact fp64 re-anchor from cluster-vector sums",
+            "sites": N, "replicas": R, "state_bytes": R * N, "warps_per_replica": w, "autotune_ms": {str(k): v for k, v in tune.items()},
+            "tracked_sums_equal_recount": cv_ok, "max_E_vs_full_recompute_eV": float((Ef - st.E).abs().max().item()),
+            "full_energy_ms": a_.elapsed_time(b_), "full_energy_site_replicas_per_s": R * N / (a_.elapsed_time(b_) / 1e3),
+            "accept_rate": float(st.n_acc.sum().item()) / (R * step), "setup_s": setup, "tables_s": setup_tables,
+            "vs_h100_published_4344547": R * chunk * steps / tot / 4_344_547}
 
 
 def workload_config(args, gce):
@@ -376,6 +439,17 @@ def main():
                               "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
                               "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": {"workload": r["config"]},
                               "batch": r}), flush=True)
+        return
+    if args.workload == "ce-large":
+        from neuralce_gb300 import _lib
+        _lib.lib()
+        r = bench_large(steps=args.steps if args.steps != 40 else 3, warmup=max(1, min(args.warmup, 2)))
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": r["value"], "unit": "swap attempts/s", "n_gpus": world,
+                              "steps": args.steps if args.steps != 40 else 3, "warmup": max(1, min(args.warmup, 2)),
+                              "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                              "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": {"workload": r["config"]},
+                              "large": r}), flush=True)
         return
     if args.workload == "serve":
         from neuralce_gb300 import _lib

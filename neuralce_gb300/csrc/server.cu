@@ -3,9 +3,11 @@
 // while a job runs.  Host code only; the device work is the engines' own entry points.
 //
 // Threads: the caller's threads only touch host structures under `mu` (submit, poll, cancel, query never wait
-// for the device).  Worker 0 drives the CE jobs on one stream, worker 1 the NeuralCE jobs on `nce_streams`
-// streams; each worker admits jobs of its kind, launches one round, waits for its own streams, then retires
-// finished jobs (outputs copied to the caller's host buffers, device memory returned with cudaFreeAsync).
+// for the device).  The io thread admits jobs (upload, initial energies or caches) and retires them (outputs
+// copied to the caller's host buffers, device memory returned with cudaFreeAsync) on its own stream, so neither
+// stalls the device work; the CE thread runs rounds of persistent batch launches over every running CE job (up
+// to max_batch jobs per launch, launches spread over a few streams), the NeuralCE thread one chunk per running
+// NeuralCE job per round on `nce_streams` streams.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -94,14 +96,15 @@ struct nce_server {
     std::map<int64_t, std::shared_ptr<SJob>> jobs;
     std::deque<std::shared_ptr<SJob>> pending[2];
     std::vector<std::shared_ptr<SJob>> active[2];
+    std::deque<std::shared_ptr<SJob>> retiring[2];   // finished or cancelled running jobs, for the io threads
     int64_t next_id = 1, bytes_used = 0;
     int64_t n_done = 0, n_cancelled = 0, n_failed = 0, rounds[2] = {0, 0};
     std::atomic<int64_t> attempts{0};
     std::atomic<bool> stop{false};
-    std::thread worker[2];
+    std::thread worker[4];                           // CE rounds, NeuralCE rounds, CE io, NeuralCE io
     std::chrono::steady_clock::time_point t0;
-    cudaStream_t ce_stream = nullptr;
-    std::vector<cudaStream_t> nce_streams;
+    cudaStream_t io_streams[2] = {nullptr, nullptr};
+    std::vector<cudaStream_t> ce_streams, nce_streams;
     int rr = 0;
 
     double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
@@ -189,9 +192,10 @@ int start_ce(nce_server *S, SJob &j, cudaStream_t s) {
     NCE_CUDA(cudaMemsetAsync(st.n_acc, 0, 8 * (size_t)R, s));
     NCE_CUDA(cudaMemsetAsync(st.n_ex, 0, 8, s));
     nce_ce_handle h = (nce_ce_handle)j.d.model;
-    int rc = nce_ce_energy(h, st.sigma, R, 64, st.E, s);
+    // one pass over the configurations: the exact sums, and the float64 energies from them
+    int rc = track ? nce_ce_cluster_counts(h, st.sigma, R, st.cv, s) : nce_ce_energy(h, st.sigma, R, 64, st.E, s);
     if (rc) return rc;
-    if (track) { rc = nce_ce_cluster_counts(h, st.sigma, R, st.cv, s); if (rc) return rc; }
+    if (track) { rc = nce_ce_energy_from_counts(h, st.cv, R, st.E, s); if (rc) return rc; }
     NCE_CUDA(cudaMemcpyAsync(st.E_min_rep, st.E, 8, cudaMemcpyDeviceToDevice, s));   // replica 0, as PT set-up does
     NCE_CUDA(cudaStreamSynchronize(s));                                            // host copies may be freed now
     return NCE_OK;
@@ -248,76 +252,94 @@ void drop(SJob &j, cudaStream_t s) {
     if (j.dev && j.dev != reinterpret_cast<char *>(1)) { cudaFreeAsync(j.dev, s); cudaStreamSynchronize(s); }
 }
 
-// admit, start, and take the list of running jobs of `kind`; returns false when the server stops
-bool gather(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &run) {
-    std::vector<std::shared_ptr<SJob>> fresh;
-    {
-        std::unique_lock<std::mutex> lk(S->mu);
-        for (;;) {
-            if (S->stop) return false;
-            fresh = admit_locked(S, kind);
-            // running jobs cancelled since the last round leave now
-            auto &a = S->active[kind];
-            for (auto it = a.begin(); it != a.end();) {
-                if ((*it)->cancel) {
-                    SJob &j = **it;
-                    cudaStream_t s = kind == 0 ? S->ce_stream : j.stream;
-                    lk.unlock(); drop(j, s); lk.lock();
-                    j.dev = reinterpret_cast<char *>(1);
-                    release_locked(S, j, NCE_JOB_CANCELLED);
-                    it = a.erase(it);
-                } else {
-                    ++it;
-                }
+// io thread of one kind: admit (start) queued jobs that fit and retire finished or cancelled ones
+void io_worker(nce_server *S, int kind) {
+    cudaSetDevice(S->device);
+    cudaStream_t ios = S->io_streams[kind];
+    for (;;) {
+        std::vector<std::shared_ptr<SJob>> fresh, out;
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            for (;;) {
+                if (S->stop) return;
+                out.assign(S->retiring[kind].begin(), S->retiring[kind].end());
+                S->retiring[kind].clear();
+                fresh = admit_locked(S, kind);
+                if (!out.empty() || !fresh.empty()) break;
+                S->wake.wait_for(lk, std::chrono::milliseconds(2));
             }
-            if (!fresh.empty() || !a.empty()) break;
-            S->wake.wait_for(lk, std::chrono::milliseconds(2));
         }
-    }
-    for (auto &p : fresh) {
-        SJob &j = *p;
-        int rc;
-        if (kind == 0) {
-            rc = start_ce(S, j, S->ce_stream);
-        } else {
-            // jobs on one model share its scratch buffers, so they share a stream; other jobs spread over the streams
-            std::shared_ptr<SJob> twin;
-            {
-                std::lock_guard<std::mutex> lk(S->mu);
-                for (auto &q : S->active[1]) if (q->d.model == j.d.model) twin = q;
-            }
-            j.stream = twin ? twin->stream : S->nce_streams[S->rr++ % S->nce_streams.size()];
-            rc = start_nce(S, j, j.stream);
-        }
-        if (rc) {
-            drop(j, kind == 0 ? S->ce_stream : j.stream);
+        for (auto &p : out) {
+            SJob &j = *p;
+            int rc = NCE_OK;
+            if (j.cancel) drop(j, ios);
+            else rc = finish(j, ios);
+            std::lock_guard<std::mutex> lk(S->mu);
             j.dev = reinterpret_cast<char *>(1);
-            fail_job(S, j, rc);
-            continue;
+            if (j.cancel) {
+                release_locked(S, j, NCE_JOB_CANCELLED);
+            } else if (rc) {
+                j.error = rc; j.msg = last_error();
+                release_locked(S, j, NCE_JOB_FAILED);
+            } else {
+                release_locked(S, j, NCE_JOB_DONE);
+            }
         }
-        std::lock_guard<std::mutex> lk(S->mu);
-        S->active[kind].push_back(p);
+        for (auto &p : fresh) {
+            SJob &j = *p;
+            int rc;
+            cudaStream_t s = ios;
+            if (kind == 0) {
+                rc = start_ce(S, j, s);
+            } else {
+                // jobs on one model share its scratch buffers, so they share a stream (set-up included)
+                {
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    std::shared_ptr<SJob> twin;
+                    for (auto &q : S->active[1]) if (q->d.model == j.d.model) twin = q;
+                    j.stream = twin ? twin->stream : S->nce_streams[S->rr++ % S->nce_streams.size()];
+                }
+                s = j.stream;
+                rc = start_nce(S, j, s);
+            }
+            if (rc) {
+                drop(j, s);
+                j.dev = reinterpret_cast<char *>(1);
+                fail_job(S, j, rc);
+                continue;
+            }
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->active[kind].push_back(p);
+            S->wake.notify_all();
+        }
     }
-    std::lock_guard<std::mutex> lk(S->mu);
-    run = S->active[kind];
-    return true;
 }
 
-void retire(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &run) {
-    for (auto &p : run) {
-        SJob &j = *p;
-        if (j.status != NCE_JOB_RUNNING || j.done < j.d.n_steps) continue;
-        const int rc = finish(j, kind == 0 ? S->ce_stream : j.stream);
-        std::lock_guard<std::mutex> lk(S->mu);
+// running jobs of `kind` for the next round (cancelled ones go to the io thread); false when the server stops
+bool take_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &run) {
+    std::unique_lock<std::mutex> lk(S->mu);
+    for (;;) {
+        if (S->stop) return false;
         auto &a = S->active[kind];
-        a.erase(std::remove(a.begin(), a.end(), p), a.end());
-        if (rc) {
-            j.error = rc; j.msg = last_error();
-            release_locked(S, j, NCE_JOB_FAILED);
-        } else {
-            release_locked(S, j, NCE_JOB_DONE);
+        for (auto it = a.begin(); it != a.end();) {
+            if ((*it)->cancel) { S->retiring[kind].push_back(*it); it = a.erase(it); }
+            else ++it;
         }
+        if (!a.empty()) { run = a; return true; }
+        S->wake.wait_for(lk, std::chrono::milliseconds(2));
     }
+}
+
+void end_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &run) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    ++S->rounds[kind];
+    auto &a = S->active[kind];
+    for (auto &p : run)
+        if (p->done >= p->d.n_steps) {
+            a.erase(std::remove(a.begin(), a.end(), p), a.end());
+            S->retiring[kind].push_back(p);
+        }
+    S->wake.notify_all();
 }
 
 void fail_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &jobs, int rc) {
@@ -334,18 +356,19 @@ void fail_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &job
 
 int64_t chunk_len(const SJob &j) { return std::min(j.d.exchange_every - j.done % j.d.exchange_every, j.d.n_steps - j.done); }
 
-// CE worker: one persistent batch launch per round over every running CE job (grouped by cluster order)
+// CE thread: one round = persistent batch launches over every running CE job (grouped by cluster order, at most
+// max_batch jobs per launch, launches spread over the CE streams), each job's exact re-anchor after its chunk
 void ce_worker(nce_server *S) {
     cudaSetDevice(S->device);
     std::vector<std::shared_ptr<SJob>> run;
-    while (gather(S, 0, run)) {
-        if (run.empty()) continue;
+    while (take_round(S, 0, run)) {
         std::map<int32_t, std::vector<std::shared_ptr<SJob>>> by_mo;
         for (auto &p : run) by_mo[p->mo].push_back(p);
-        int rc = NCE_OK;
-        for (auto &g : by_mo) {
-            auto &v = g.second;
-            for (size_t a = 0; a < v.size() && rc == NCE_OK; a += (size_t)S->cfg.max_batch) {
+        int rc = NCE_OK, g = 0;
+        for (auto &grp : by_mo) {
+            auto &v = grp.second;
+            for (size_t a = 0; a < v.size() && rc == NCE_OK; a += (size_t)S->cfg.max_batch, ++g) {
+                cudaStream_t s = S->ce_streams[g % S->ce_streams.size()];
                 const int n = (int)std::min<size_t>((size_t)S->cfg.max_batch, v.size() - a);
                 std::vector<nce_ce_handle> hs(n); std::vector<nce_pt_state> ss(n); std::vector<nce_pt_chunk> cs(n);
                 for (int i = 0; i < n; ++i) {
@@ -357,36 +380,34 @@ void ce_worker(nce_server *S) {
                     c.do_exchange = ((j.done + c.n_steps) % j.d.exchange_every) == 0;
                     c.precision = S->cfg.precision; c.warps = S->cfg.warps; c.path = 0; c.cluster = 1;
                 }
-                rc = nce_ce_run_batch(n, hs.data(), ss.data(), cs.data(), S->ce_stream);
+                rc = nce_ce_run_batch(n, hs.data(), ss.data(), cs.data(), s);
                 for (int i = 0; i < n && rc == NCE_OK; ++i) {
                     SJob &j = *v[a + i];
-                    if (j.st.cv) rc = nce_ce_energy_from_counts(hs[i], j.st.cv, j.d.R, j.st.E, S->ce_stream);
+                    if (j.st.cv) rc = nce_ce_energy_from_counts(hs[i], j.st.cv, j.d.R, j.st.E, s);
                 }
                 if (rc == NCE_OK)
                     for (int i = 0; i < n; ++i) {
                         SJob &j = *v[a + i];
-                        const int64_t len = cs[i].n_steps;
-                        j.done += len;
-                        S->attempts += len * j.d.R;
+                        j.done += cs[i].n_steps;
+                        S->attempts += cs[i].n_steps * j.d.R;
                     }
             }
         }
-        if (rc == NCE_OK) {
-            const cudaError_t e = cudaStreamSynchronize(S->ce_stream);
-            if (e != cudaSuccess) rc = fail(NCE_ERR_CUDA, "CE round: %s", cudaGetErrorString(e));
-        }
+        if (rc == NCE_OK)
+            for (cudaStream_t s : S->ce_streams) {
+                const cudaError_t e = cudaStreamSynchronize(s);
+                if (e != cudaSuccess) { rc = fail(NCE_ERR_CUDA, "CE round: %s", cudaGetErrorString(e)); break; }
+            }
         if (rc) { fail_round(S, 0, run, rc); continue; }
-        { std::lock_guard<std::mutex> lk(S->mu); ++S->rounds[0]; }
-        retire(S, 0, run);
+        end_round(S, 0, run);
     }
 }
 
-// NeuralCE worker: every running job advances one chunk per round, jobs spread over the worker's streams
+// NeuralCE thread: every running job advances one chunk per round on its stream
 void nce_worker(nce_server *S) {
     cudaSetDevice(S->device);
     std::vector<std::shared_ptr<SJob>> run;
-    while (gather(S, 1, run)) {
-        if (run.empty()) continue;
+    while (take_round(S, 1, run)) {
         int rc = NCE_OK;
         for (auto &p : run) {
             SJob &j = *p;
@@ -407,8 +428,7 @@ void nce_worker(nce_server *S) {
                 if (e != cudaSuccess) { rc = fail(NCE_ERR_CUDA, "NeuralCE round: %s", cudaGetErrorString(e)); break; }
             }
         if (rc) { fail_round(S, 1, run, rc); continue; }
-        { std::lock_guard<std::mutex> lk(S->mu); ++S->rounds[1]; }
-        retire(S, 1, run);
+        end_round(S, 1, run);
     }
 }
 
@@ -437,22 +457,30 @@ int nce_server_create(const nce_server_config *cfg, nce_server_handle *out) {
         NCE_CUDA(cudaMemGetInfo(&fr, &tot));
         c.hbm_budget = (int64_t)(0.9 * (double)fr);
     }
-    NCE_CUDA(cudaStreamCreateWithFlags(&S->ce_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) NCE_CUDA(cudaStreamCreateWithFlags(&S->io_streams[k], cudaStreamNonBlocking));
+    for (int i = 0; i < 4; ++i) {
+        cudaStream_t s;
+        NCE_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        S->ce_streams.push_back(s);
+    }
     for (int i = 0; i < c.nce_streams; ++i) {
         cudaStream_t s;
         NCE_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
         S->nce_streams.push_back(s);
     }
-    // keep freed job memory in the pool for the next admissions instead of returning it to the driver
+    // keep up to a quarter of the budget of freed job memory in the pool for the next admissions; the rest goes
+    // back to the driver, where the models' own allocations can use it
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, S->device) == cudaSuccess) {
-        uint64_t keep = (uint64_t)c.hbm_budget;
+        uint64_t keep = (uint64_t)(c.hbm_budget / 4);
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
     S->t0 = std::chrono::steady_clock::now();
     nce_server *raw = S.release();
     raw->worker[0] = std::thread(ce_worker, raw);
     raw->worker[1] = std::thread(nce_worker, raw);
+    raw->worker[2] = std::thread(io_worker, raw, 0);
+    raw->worker[3] = std::thread(io_worker, raw, 1);
     *out = raw;
     return NCE_OK;
 }
@@ -465,9 +493,12 @@ int nce_server_destroy(nce_server_handle S) {
     }
     S->wake.notify_all();
     for (auto &w : S->worker) if (w.joinable()) w.join();
-    for (int k = 0; k < 2; ++k)
-        for (auto &p : S->active[k]) drop(*p, k == 0 ? S->ce_stream : p->stream);
-    cudaStreamDestroy(S->ce_stream);
+    for (int k = 0; k < 2; ++k) {
+        for (auto &p : S->active[k]) drop(*p, S->io_streams[k]);
+        for (auto &p : S->retiring[k]) drop(*p, S->io_streams[k]);
+        cudaStreamDestroy(S->io_streams[k]);
+    }
+    for (cudaStream_t s : S->ce_streams) cudaStreamDestroy(s);
     for (cudaStream_t s : S->nce_streams) cudaStreamDestroy(s);
     delete S;
     return NCE_OK;
@@ -536,7 +567,7 @@ int nce_server_query(nce_server_handle S, nce_server_stats *o) {
     NCE_CHECK(S && o, "nce_server_query: null argument");
     std::lock_guard<std::mutex> lk(S->mu);
     o->queued = (int64_t)(S->pending[0].size() + S->pending[1].size());
-    o->running = (int64_t)(S->active[0].size() + S->active[1].size());
+    o->running = (int64_t)(S->active[0].size() + S->active[1].size() + S->retiring[0].size() + S->retiring[1].size());
     o->done = S->n_done; o->cancelled = S->n_cancelled; o->failed = S->n_failed;
     o->bytes_used = S->bytes_used; o->hbm_budget = S->cfg.hbm_budget;
     o->rounds_ce = S->rounds[0]; o->rounds_nce = S->rounds[1];
