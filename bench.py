@@ -549,7 +549,10 @@ def main():
     hbm, src = peaks()
     ms_chunk = float(np.mean(per_ms))
     achieved = R * T * B_GATHER / (ms_chunk / 1e3) / 1e9
-    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+    # DRAM bytes per launch from one ncu capture of this workload (dram__bytes_read.sum + dram__bytes_write.sum of
+    # ce_bin_chunk_kernel, 2,048 sites, R = 32, 5,000 steps): the tables and occupancies live in shared memory
+    traffic = 139_776 if (args.L == 8 and args.R == 32 and T == 5000 and args.path != 1) else None
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
             "kernel": "ce_pt_chunk_kernel" if args.path == 1 else "ce_bin_chunk_kernel", "peak_source": src,
             "algorithmic_bytes_per_launch": R * T * B_GATHER}
     nce_line = None
