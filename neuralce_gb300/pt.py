@@ -52,6 +52,7 @@ class MCMCConfig:
     # engine options (not in the reference)
     precision: int = 64
     warps: int = 0
+    cluster: int = 1                 # CTAs per replica (thread-block cluster, sign-parity path)
     reanchor_every: int = 0          # chunks between float64 full-energy re-anchors (0 = never, as the reference)
 
 
@@ -213,7 +214,9 @@ def run_pt_mcmc(gce, cfg: MCMCConfig, verbose=True):
     else:
         temps, betas, lid, lpos = build_interleaved_ladders(cfg.T_min, cfg.T_max, n_per, n_ladders)
     chunk = int(cfg.chunk_size); si = int(cfg.sample_interval); ex_int = int(cfg.exchange_interval)
-    if n_total > 1 and ex_int % chunk != 0:
+    if ex_int <= 0:                   # independent chains (single-T / multi-T runs): no exchange
+        ex_int = 0
+    elif n_total > 1 and ex_int % chunk != 0:
         import math
         if ex_int < chunk:
             chunk = ex_int
@@ -280,10 +283,10 @@ def run_pt_mcmc(gce, cfg: MCMCConfig, verbose=True):
 
     def one_chunk(record):
         nonlocal step, sigma_min, E_min
-        do_ex = n_total > 1 and (step + chunk) % ex_int == 0
+        do_ex = n_total > 1 and ex_int > 0 and (step + chunk) % ex_int == 0
         E_before = E_min
         run_chunk(gce, st, chunk, step, cfg.seed, cfg.precision, cfg.warps, None, si, Es_dev if record else None,
-                  do_ex)
+                  do_ex, cluster=cfg.cluster)
         step += chunk
         mn, arg = st.minimum()
         m = float(mn.item())
@@ -316,7 +319,7 @@ def run_pt_mcmc(gce, cfg: MCMCConfig, verbose=True):
     wall = time.time() - t0
     n_sw = cfg.n_steps * n_total
     pairs = (n_per // 2) * n_ladders
-    n_ex_att = (cfg.n_steps // ex_int) * pairs
+    n_ex_att = (cfg.n_steps // ex_int) * pairs if ex_int else 0
     swap_rate = float(st.n_acc.sum().item()) / max(1, n_sw)
     ex_rate = float(st.n_ex.item()) / max(1, n_ex_att)
     log(f"\nDone in {wall:.1f}s  ({n_sw / max(wall, 1e-9):,.0f} swap attempts/s)\n  swap acceptance     : {swap_rate:.4f}\n"
