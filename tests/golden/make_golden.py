@@ -9,6 +9,9 @@ the reference mounted; the fixtures are committed, so the tests never read the r
                         standardisation, channel selection, cutoffs, shells, primitive) and its L1_0 energy on the
                         2x2x3 conventional cell from results/ptni_exact/exact_N48.json ("E_L10", eV/atom)
 
+  exact_N48.json        the exact (enumerated) thermodynamics of that model on that cell at 24 Pt / 24 Ni, from
+                        results/ptni_exact/exact_N48.json: temperature grid (K), <E> (eV/atom), C_V (k_B/atom)
+
 Usage: python tests/golden/make_golden.py /path/to/reference
 """
 import json
@@ -43,6 +46,9 @@ def main(ref):
                primitive_frac=mdl["primitive"].frac.tolist(), primitive_numbers=mdl["primitive"].numbers.tolist(),
                cell=[2, 2, 3], E_L10=float(ex["E_L10"]), E_min=float(ex["E_min"]), E_max=float(ex["E_max"]), N=int(ex["N"]))
     json.dump(nce, open(os.path.join(HERE, "nipt_v3_nomax_sel.json"), "w"))
+    th = dict(source="results/ptni_exact/exact_N48.json", N=int(ex["N"]), nPt=int(ex["nPt"]), cell=[2, 2, 3],
+              T=tl(ex["T"]), E=tl(ex["E"]), Cv=tl(ex["Cv"]), E_L10=float(ex["E_L10"]))
+    json.dump(th, open(os.path.join(HERE, "exact_N48.json"), "w"))
 
 
 if __name__ == "__main__":
