@@ -119,7 +119,9 @@ typedef struct {
     double *E;             /* (R) carried energy per replica */
     const float *beta_slot;/* (R) 1/(kB T) of each temperature slot (float32, as the reference) */
     int32_t *rep_of_slot;  /* (R) replica holding slot t */
-    int32_t *slot_of_rep;  /* (R) inverse */
+    int32_t *slot_of_rep;  /* (R) inverse; a shard of a larger ladder may hold that ladder's slots here (beta_slot then
+                              has the ladder's length; proposals are keyed by these slots; no in-kernel exchange or
+                              E_samples in that use) */
     const int32_t *ladder_id; /* (R) ladder of each slot (exchange only within a ladder) */
     double *E_min_rep;     /* (R) running minimum of E per replica */
     int64_t *n_acc;        /* (R) accepted swaps per replica (accumulated) */

@@ -299,3 +299,23 @@ def test_graph_replay_equals_eager_batch(cuda):
     for x, y in zip(a.states, b.states):
         assert torch.equal(x.sigma, y.sigma) and torch.equal(x.cv, y.cv) and torch.equal(x.rep_of_slot, y.rep_of_slot)
         assert torch.equal(x.E, y.E) and torch.equal(x.n_acc, y.n_acc)
+
+
+def test_sharded_runner_equals_device_exchange(cuda):
+    """One rank of the multi-GPU ladder layout (global slots in slot_of_rep, host exchange from gathered energies)
+    runs the same trajectory as the single-GPU kernel with its device exchange."""
+    torch = cuda
+    from neuralce_gb300.dist import ShardedLadder, run_sharded_chunks
+    from neuralce_gb300.pt import run_chunk
+    R, T = 8, 800
+    gce, orc, sig_r, beta = _setup(4, seed=31, R=R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    a = _engine_state(sig_r, E0, beta)
+    for c in range(3):
+        run_chunk(gce, a, T, c * T, 55, 64, 8, None, 1, None, True, path=2)
+    shard = ShardedLadder(beta)
+    b, _ = run_sharded_chunks(gce, shard, sig_r, 3, T, 55, 64, 8, path=2)
+    torch.cuda.synchronize()
+    assert torch.equal(a.sigma, b.sigma) and torch.allclose(a.E, b.E, rtol=0, atol=1e-9)
+    assert np.array_equal(a.rep_of_slot.cpu().numpy(), shard.rep_of_slot)
+    assert int(a.n_ex.item()) == shard.n_ex > 0
