@@ -47,7 +47,8 @@ def parse():
     ap.add_argument("--L", type=int, default=8)
     ap.add_argument("--R", type=int, default=32)
     ap.add_argument("--chunk", type=int, default=5000)
-    ap.add_argument("--workload", choices=["ce", "nce", "ce-batch", "serve", "ce-large"], default="ce")
+    ap.add_argument("--workload", choices=["ce", "nce", "ce-batch", "serve", "ce-large", "nce-large"], default="ce")
+    ap.add_argument("--nce-mma", type=int, default=-1, help="NeuralCE contractions: 0 fp32, 1 bf16, 3 split bf16 (-1: workload default)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the serving side measurement (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=3, help="chunks of the batched-form side measurement (0 = skip)")
     ap.add_argument("--nce-steps", type=int, default=3, help="chunks of the NeuralCE side measurement (0 = skip)")
@@ -413,6 +414,66 @@ def bench_large(L=136, R=256, chunk=5000, steps=3, warmup=1, precision=32, seed=
             "vs_h100_published_4344547": R * chunk * steps / tot / 4_344_547}
 
 
+def bench_nce_large(L=64, R=64, width=128, depth=3, chunk=100, steps=3, warmup=1, mma=1, seed=0, cluster=0):
+    """Configuration 3 (NeuralCE part): fcc L^3 conventional cell (L = 64: 1,048,576 sites), R replicas 300-1400 K,
+    the configuration-1 architecture widened to ``width``; layer contractions in bf16 on tensor cores with float32
+    accumulation (``mma`` 1; 3 = split bf16, 0 = float32 CUDA cores).  Occupancies drawn on the device.  A step is
+    one chunk of ``chunk`` MC steps per replica + one exchange round; the full caches are built once (timed
+    separately)."""
+    import torch
+    from neuralce_gb300.nce import NCEModel, NCEState, synthetic_model
+    from neuralce_gb300.workloads import A_FCC, cluster_space, ladder
+    from neuralce_gb300.io import Z_OF, fcc_conventional
+    t0 = time.time()
+    cs = cluster_space()
+    s = fcc_conventional(A_FCC, (L, L, L)); s.numbers = np.full(len(s), Z_OF["Ni"], np.int64)
+    P = synthetic_model(len(cs.orbits) + 1, depth, width, 1, seed)
+    m = NCEModel(cs, s, P, shell_edges=(0.0, 3.3), act="silu", pool="sum", mma=mma)
+    N = m.N
+    setup_model = time.time() - t0
+    g = torch.Generator(device="cuda"); g.manual_seed(seed)
+    sig = torch.empty((R, N), dtype=torch.int8, device="cuda")
+    for r in range(R):
+        sig[r] = (torch.randperm(N, device="cuda", generator=g) < N // 2).to(torch.int8)
+    _, beta = ladder(R)
+    st = NCEState(m, np.zeros((R, 1), np.int8), beta)
+    st.N = N; st.sigma = sig
+    st.h0 = torch.zeros((R, N, m.C0), dtype=torch.float32, device="cuda")
+    st.hmid = torch.zeros((max(depth - 1, 0), R, N, m.D), dtype=torch.float32, device="cuda") if depth >= 2 else None
+    st.e = torch.zeros((R, N), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a_.record(); st.full_cache(); b_.record(); torch.cuda.synchronize()
+    full_ms = a_.elapsed_time(b_)
+    tune = None
+    if cluster == 0:
+        tune = {}
+        for cl in (1, 2, 4):
+            st.run_chunk(2, 0, seed=1, cluster=cl)
+            a_.record(); st.run_chunk(10, 2, seed=1, cluster=cl); b_.record(); torch.cuda.synchronize()
+            tune[cl] = a_.elapsed_time(b_)
+        cluster = min(tune, key=tune.get)
+    step = 100
+    for _ in range(warmup):
+        st.run_chunk(chunk, step, seed=99, exchange_rounds=1, cluster=cluster); step += chunk
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        ev[k][0].record(); st.run_chunk(chunk, step, seed=99, exchange_rounds=1, cluster=cluster); ev[k][1].record(); step += chunk
+    torch.cuda.synchronize()
+    ms = [x.elapsed_time(y) for x, y in ev]
+    tot = sum(ms) / 1e3
+    E_car = st.E.clone(); st.full_cache(); torch.cuda.synchronize()
+    drift = float((st.E - E_car).abs().max().item())
+    return {"value": R * chunk * steps / tot, "unit": "swap attempts/s", "ms_per_step": float(np.mean(ms)),
+            "config": f"NeuralCE large cell: fcc {L}^3 conventional ({N} sites), R={R}, depth {depth}, width {width}, SiLU, sum, "
+                      f"{['fp32 CUDA cores', 'bf16 tensor cores (fp32 accumulation)', '', 'split-bf16 tensor cores'][mma]}, "
+                      f"chunk {chunk} steps + 1 exchange round",
+            "sites": N, "replicas": R, "full_cache_ms": full_ms, "ctas_per_replica": cluster, "autotune_ms": tune,
+            "carried_vs_rebuilt_energy_eV": drift, "device_state_GB": (R * N * (1 + 4 * m.C0 + 4 + 4 * m.D * max(depth - 1, 0))) / 1e9,
+            "setup_model_s": setup_model}
+
+
 def workload_config(args, gce):
     return {"workload": f"CE parallel tempering fp{args.precision}: fcc Ni/Pt {args.L}x{args.L}x{args.L} conventional "
                         f"({gce.n_atoms} sites), R={args.R} replicas 300-1400 K, exchange every {args.chunk} steps, "
@@ -450,6 +511,17 @@ def main():
                               "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
                               "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": {"workload": r["config"]},
                               "large": r}), flush=True)
+        return
+    if args.workload == "nce-large":
+        from neuralce_gb300 import _lib
+        _lib.lib()
+        st_, wu_ = (args.steps if args.steps != 40 else 3), max(1, min(args.warmup, 2))
+        r = bench_nce_large(steps=st_, warmup=wu_, mma=(1 if args.nce_mma < 0 else args.nce_mma))
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": r["value"], "unit": "swap attempts/s", "n_gpus": world, "steps": st_,
+                              "warmup": wu_, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                              "vs_baseline": None, "dtype": "bf16" if args.nce_mma in (-1, 1) else "f32", "data": "synthetic",
+                              "config": {"workload": r["config"]}, "large": r}), flush=True)
         return
     if args.workload == "serve":
         from neuralce_gb300 import _lib
@@ -489,8 +561,9 @@ def main():
         from neuralce_gb300.autotune import best_launch
         ws = (args.warps,) if args.warps else (4, 8, 16, 32)
         cls = (args.cluster,) if args.cluster else ((1, 2, 4, 8) if args.path != 1 else (1,))
-        (args.warps, args.cluster), t = best_launch(gce, st, args.precision, args.path, ws, cls)
-        tuned = {f"{w}x{c}": round(v, 3) for (w, c), v in t.items()}
+        paths = (2, 3) if args.path == 0 else (args.path,)
+        (args.warps, args.cluster, args.path), t = best_launch(gce, st, args.precision, args.path, ws, cls, paths=paths)
+        tuned = {f"{w}x{c}/p{p}": round(v, 3) for (w, c, p), v in t.items()}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
     step = 0
@@ -551,9 +624,10 @@ def main():
     achieved = R * T * B_GATHER / (ms_chunk / 1e3) / 1e9
     # DRAM bytes per launch from one ncu capture of this workload (dram__bytes_read.sum + dram__bytes_write.sum of
     # ce_bin_chunk_kernel, 2,048 sites, R = 32, 5,000 steps): the tables and occupancies live in shared memory
-    traffic = 139_776 if (args.L == 8 and args.R == 32 and T == 5000 and args.path != 1) else None
+    traffic = 139_776 if (args.L == 8 and args.R == 32 and T == 5000 and args.path == 2) else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-            "kernel": "ce_pt_chunk_kernel" if args.path == 1 else "ce_bin_chunk_kernel", "peak_source": src,
+            "kernel": {1: "ce_pt_chunk_kernel", 3: "ce_bin2_chunk_kernel"}.get(args.path, "ce_bin_chunk_kernel"),
+            "peak_source": src,
             "algorithmic_bytes_per_launch": R * T * B_GATHER}
     nce_line = None
     if rank == 0 and args.nce_steps > 0:
@@ -576,7 +650,7 @@ def main():
                 "config": workload_config(args, gce), "clocks": clocks, "e2e": e2e, "gpu_launches": 2 * args.steps,
                 "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "batch": batch_line, "serve": serve_line,
                 "launch": {"warps_per_cta": args.warps, "ctas_per_replica": args.cluster,
-                           "path": ["auto", "general", "sign-parity"][args.path],
+                           "path": ["auto", "general", "sign-parity", "sign-parity, two steps in flight"][args.path],
                            "autotune_ms": tuned},
                 "accept_rate": float(st.n_acc.sum().item()) / max(1, R * step)}
         print(json.dumps(line), flush=True)

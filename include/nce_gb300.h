@@ -148,7 +148,8 @@ typedef struct {
     const double *ex_u;        /* (ceil((R-1)/2)) device uniforms, or NULL -> Philox */
     int32_t precision;         /* 64 or 32 */
     int32_t warps;             /* warps per replica (0 = default) */
-    int32_t path;              /* 0 auto, 1 general point-function products, 2 sign parity (point functions in {-1,+1}) */
+    int32_t path;              /* 0 auto, 1 general point-function products, 2 sign parity (point functions in {-1,+1}),
+                                  3 sign parity with two steps evaluated together (cluster order <= 4) */
     int32_t cluster;           /* sign parity: CTAs per replica (1, 2, 4, 8; thread-block cluster); the cell must fit in
                                   shared memory, otherwise one CTA is used */
     int64_t *step_dev;         /* device counter or NULL: when set, the chunk's first global step is read from it
@@ -222,6 +223,10 @@ typedef struct {
     int32_t n_groups, max_gb;
     const int32_t *act_b, *act_nb; const uint64_t *grp_cum;   /* swap groups, as in nce_ce_tables */
     const uint16_t *Rv_loc;/* (nB, J, mo) index of each masked row member in its site's ball-0 list (ball_b/ball_uo order) */
+    int32_t mma;           /* layer contractions: 0 float32 on CUDA cores; 1 bf16 operands on tensor cores (mma.sync,
+                              float32 accumulation); 3 the same with each operand split into two bf16 terms
+                              (hi*hi + hi*lo + lo*hi, near-float32 accuracy).  Tensor-core forms need an ungated model.
+                              Full caches and steps use the same form, so a run samples one consistent energy. */
 } nce_nce_desc;
 
 typedef struct nce_nce_model *nce_nce_handle;

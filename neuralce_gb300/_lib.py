@@ -45,7 +45,8 @@ class NceNceDesc(C.Structure):
                 ("ball_b", vp), ("ball_uo", vp), ("ball_end", vp), ("lin", vp), ("head_w", vp), ("head_b", f64),
                 ("W_cat", vp * 4), ("bias", vp * 4), ("G_cat", vp * 4), ("gate_b", vp * 4), ("mu", vp), ("sd", vp),
                 ("act", i32), ("gate", i32), ("norm", f64), ("scale_eV", f64),
-                ("n_groups", i32), ("max_gb", i32), ("act_b", vp), ("act_nb", vp), ("grp_cum", vp), ("Rv_loc", vp)]
+                ("n_groups", i32), ("max_gb", i32), ("act_b", vp), ("act_nb", vp), ("grp_cum", vp), ("Rv_loc", vp),
+                ("mma", i32)]
 
 
 class NceNceState(C.Structure):

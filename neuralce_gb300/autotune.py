@@ -11,14 +11,23 @@ from __future__ import annotations
 _cache = {}
 
 
-def best_launch(gce, st, precision=64, path=0, warps=(2, 4, 8, 16, 32), clusters=(1,), steps=300, seed=12345):
-    """((warps, cluster), {(warps, cluster): ms}) of the fastest candidate."""
+def best_launch(gce, st, precision=64, path=0, warps=(2, 4, 8, 16, 32), clusters=(1,), steps=300, seed=12345, paths=None):
+    """((warps, cluster), {(warps, cluster): ms}) of the fastest candidate; with ``paths`` (e.g. (2, 3)) the path is
+    tuned too: ((warps, cluster, path), {(warps, cluster, path): ms})."""
     import torch
     from . import _lib
     from .pt import PTState, run_chunk
-    key = (id(gce), st.R, precision, path, tuple(warps), tuple(clusters))
+    key = (id(gce), st.R, precision, path, tuple(warps), tuple(clusters), tuple(paths or ()))
     if key in _cache:
         return _cache[key]
+    if paths:
+        timings = {}
+        for p in paths:
+            _, t = best_launch(gce, st, precision, p, warps, clusters, steps, seed)
+            timings.update({k + (p,): v for k, v in t.items()})
+        best = min(timings, key=timings.get)
+        _cache[key] = (best, timings)
+        return best, timings
     scratch = PTState(st.sigma.cpu().numpy(), st.E.cpu().numpy(), st.beta_slot.cpu().numpy(), st.ladder_id.cpu().numpy())
     timings = {}
     for cl in clusters:

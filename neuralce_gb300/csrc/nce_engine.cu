@@ -23,6 +23,7 @@
 #include <vector>
 
 #include <cooperative_groups.h>
+#include <cuda_bf16.h>
 
 #include "common.cuh"
 
@@ -55,6 +56,7 @@ struct NceDev {
     int32_t n_groups, max_gb; const int32_t *act_b, *act_nb; const uint64_t *grp_cum;
     const uint16_t *Rv_loc;                   // (nB, J, mo) index of each row member in its site's ball-0 list
     int32_t w0max;                            // ball-0 entries per basis, maximum
+    int32_t mma;                              // 0 float32 CUDA cores, 1 bf16 tensor cores, 3 split bf16 (3 products)
 };
 
 struct NceJob {
@@ -116,6 +118,24 @@ __device__ __forceinline__ float patched(const NceJob &jb, int lvl, const float 
 // MS sites per thread (register micro-tile MS x 4).  D in {16, 32, 64, 128}.
 __host__ __device__ __forceinline__ int tile_tm(int D) { return 4 * (256 / (D / 4)); }   // 4 sites per thread
 __host__ __device__ __forceinline__ int tile_kin(int P, int C0, int D) { return (1 + P) * (C0 > D ? C0 : D); }
+
+// bf16 tensor-core helpers: mma.sync m16n8k16 (row-major A, column-major B, float32 accumulation).  Fragment
+// layout (g = lane / 4, t = lane % 4): A regs {r g, k 2t..2t+1}, {r g+8, k 2t..}, {r g, k 2t+8..}, {r g+8, k 2t+8..};
+// B regs {k 2t..2t+1, n g}, {k 2t+8..2t+9, n g}; C {r g, n 2t..2t+1}, {r g+8, n 2t..2t+1}.
+__device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t *>(&v); }
+
+__device__ __forceinline__ void bf16_split(float x0, float x1, uint32_t &hi, uint32_t &lo) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+    const float2 hf = __bfloat1622float2(h);
+    hi = bf16x2_bits(h);
+    lo = bf16x2_bits(__floats2bfloat162_rn(x0 - hf.x, x1 - hf.y));
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float d[4], const uint32_t a[4], const uint32_t b[2]) {
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
 
 struct LayerW {            // weights of one layer as seen by the kernel (shared or global memory)
     const float *W, *b, *G, *gb;
@@ -205,6 +225,84 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
             }
         }
         __syncthreads();
+        if (m.mma) {
+            // 3') tensor cores: the tile's [TM x Kin] x [Kin x D] on mma.sync bf16 (split operands when m.mma == 3);
+            // warps tile the output in 16 x 8 blocks (mt x nt = 4 per warp), then bias + activation go through a
+            // [TM x (D + 4)] staging tile (over X) to the sink in the CUDA-core mapping
+            const int lane = tid & 31, warp = tid >> 5, g8 = lane >> 2, t4 = lane & 3;
+            const int wn = D >= 32 ? D / 32 : 1, wm = 8 / wn, NB = D / wn, nt = NB / 8, MB = TM / wm, mt = MB / 16;
+            const int row0 = (warp / wn) * MB, col0 = (warp % wn) * NB;
+            const bool split = m.mma == 3;
+            float acc[4][4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int nj = q % nt;
+                const int c = col0 + nj * 8 + 2 * t4;
+                const float b0 = LW.b[c], b1 = LW.b[c + 1];
+                acc[q][0] = b0; acc[q][1] = b1; acc[q][2] = b0; acc[q][3] = b1;
+            }
+            auto xv = [&](int r, int k) -> float { return k < Kin ? X[(size_t)r * XS + k] : 0.f; };
+            auto wv = [&](int k, int n) -> float { return k < Kin ? LW.W[(size_t)k * D + n] : 0.f; };
+            for (int k0 = 0; k0 < Kin; k0 += 16) {
+                const int ka = k0 + 2 * t4;
+                uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
+#pragma unroll
+                for (int mi = 0; mi < 2; ++mi) {
+                    if (mi < mt) {
+                        const int r = row0 + mi * 16 + g8;
+                        const float x00 = xv(r, ka), x01 = xv(r, ka + 1), x10 = xv(r + 8, ka), x11 = xv(r + 8, ka + 1);
+                        const float x02 = xv(r, ka + 8), x03 = xv(r, ka + 9), x12 = xv(r + 8, ka + 8), x13 = xv(r + 8, ka + 9);
+                        if (split) {
+                            bf16_split(x00, x01, ah[mi][0], al[mi][0]); bf16_split(x10, x11, ah[mi][1], al[mi][1]);
+                            bf16_split(x02, x03, ah[mi][2], al[mi][2]); bf16_split(x12, x13, ah[mi][3], al[mi][3]);
+                        } else {
+                            ah[mi][0] = bf16x2_bits(__floats2bfloat162_rn(x00, x01)); ah[mi][1] = bf16x2_bits(__floats2bfloat162_rn(x10, x11));
+                            ah[mi][2] = bf16x2_bits(__floats2bfloat162_rn(x02, x03)); ah[mi][3] = bf16x2_bits(__floats2bfloat162_rn(x12, x13));
+                        }
+                    }
+                }
+#pragma unroll
+                for (int nj = 0; nj < 4; ++nj) {
+                    if (nj < nt) {
+                        const int n = col0 + nj * 8 + g8;
+                        const float w0 = wv(ka, n), w1 = wv(ka + 1, n), w2 = wv(ka + 8, n), w3 = wv(ka + 9, n);
+                        if (split) {
+                            bf16_split(w0, w1, bh[nj][0], bl[nj][0]); bf16_split(w2, w3, bh[nj][1], bl[nj][1]);
+                        } else {
+                            bh[nj][0] = bf16x2_bits(__floats2bfloat162_rn(w0, w1)); bh[nj][1] = bf16x2_bits(__floats2bfloat162_rn(w2, w3));
+                        }
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int mi = q / nt, nj = q % nt;
+                    mma_bf16_16816(acc[q], ah[mi], bh[nj]);
+                    if (split) { mma_bf16_16816(acc[q], ah[mi], bl[nj]); mma_bf16_16816(acc[q], al[mi], bh[nj]); }
+                }
+            }
+            __syncthreads();                                   // every warp is done reading X
+            const int YS = D + 4;
+            float *Y = X;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int mi = q / nt, nj = q % nt;
+                const int r = row0 + mi * 16 + g8, c = col0 + nj * 8 + 2 * t4;
+                Y[(size_t)r * YS + c] = act_fn(m.act, acc[q][0]); Y[(size_t)r * YS + c + 1] = act_fn(m.act, acc[q][1]);
+                Y[(size_t)(r + 8) * YS + c] = act_fn(m.act, acc[q][2]); Y[(size_t)(r + 8) * YS + c + 1] = act_fn(m.act, acc[q][3]);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                if (i < MS) {
+                    const int mm = sg + i * SG;
+                    const float4 y = *reinterpret_cast<const float4 *>(Y + (size_t)mm * YS + cg * 4);
+                    float v[4] = {y.x, y.y, y.z, y.w};
+                    sink(mm < tm ? t0 + mm : -1, cg * 4, v);
+                }
+            }
+            __syncthreads();
+            continue;
+        }
         // 3) register micro-tile GEMM: MS sites x 4 columns per thread
         float o[4][4], g[4][4];
         const float4 b4 = *reinterpret_cast<const float4 *>(LW.b + cg * 4);
@@ -800,6 +898,8 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
               "nce_nce_create: bad lattice");
     NCE_CHECK(d->act == 0 || d->act == 1, "nce_nce_create: act must be 0 (tanh) or 1 (silu)");
     NCE_CHECK(d->norm > 0.0, "nce_nce_create: norm must be > 0");
+    NCE_CHECK(d->mma == 0 || d->mma == 1 || d->mma == 3, "nce_nce_create: mma must be 0, 1 or 3");
+    NCE_CHECK(d->mma == 0 || !d->gate, "nce_nce_create: the tensor-core forms need an ungated model");
     const int64_t N = d->n_cells * d->nB;
     NCE_CHECK(N < (1ll << 31) - 1, "nce_nce_create: more than 2^31 sites");
     NCE_CHECK(d->n_groups >= 1 && d->max_gb >= 1 && d->act_b && d->act_nb && d->grp_cum, "nce_nce_create: no swap group");
@@ -844,6 +944,7 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
     m.nB = d->nB; m.J = d->J; m.mo = d->mo; m.P = d->P; m.W = d->W; m.depth = d->depth; m.C0 = d->C0; m.D = d->D;
     m.maxM = d->maxM; m.maxP = d->maxP; m.d0 = (int32_t)d->d[0]; m.d1 = (int32_t)d->d[1]; m.d2 = (int32_t)d->d[2];
     m.N = N; m.n_cells = d->n_cells; m.wL = d->wL; m.act = d->act; m.gate = d->gate; m.norm = d->norm; m.scale_eV = d->scale_eV;
+    m.mma = d->mma;
     m.head_b = (float)d->head_b;
     m.n0max = 2 * n0max; m.nmax = 2 * nLmax; m.w0max = n0max;
     NCE_CHECK(d->Rv_loc, "nce_nce_create: Rv_loc required");

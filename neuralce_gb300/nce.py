@@ -61,8 +61,9 @@ class NCEModel:
     """Geometry + parameters of one cell, uploaded to the device (``nce_nce_create``)."""
 
     def __init__(self, cs, structure, params, mu=None, sd=None, shell_edges=(0.0, 3.3), act="tanh", pool="mean",
-                 ys=1.0, ym=0.0):
+                 ys=1.0, ym=0.0, mma=0):
         depth = len(params["layers"])
+        self.mma = int(mma)          # 0 float32 CUDA cores, 1 bf16 tensor cores, 3 split-bf16 tensor cores
         self.cs, self.params, self.act, self.pool = cs, params, act, pool
         self.geo = geo = build_geometry(cs, structure, list(shell_edges), depth)
         K1 = geo["K"] + 1
@@ -155,6 +156,7 @@ class NCEModel:
         s.act = 0 if self.act == "tanh" else 1
         s.gate = int(gate)
         s.norm = self.norm; s.scale_eV = self.scale_eV
+        s.mma = self.mma
         s.n_groups, s.max_gb = keep["act_b"].shape
         self.desc = s
 

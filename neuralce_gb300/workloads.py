@@ -58,7 +58,7 @@ def replica_configs(sigma, R, seed):
     return np.stack([sigma[rng.permutation(len(sigma))] for _ in range(R)]).astype(np.int8)
 
 
-def nce_config(L=8, depth=3, width=64, seed=0, x_pt=0.5, model_seed=0):
+def nce_config(L=8, depth=3, width=64, seed=0, x_pt=0.5, model_seed=0, mma=0):
     """(NCEModel, canonical sigma) of the synthetic NeuralCE workload: the CE workload's cell and cluster set as
     layer 0 (38 channels), ``depth`` graph-convolution layers of ``width`` over the 12-neighbour shell, SiLU,
     sum readout, weights ~ N(0, 1/fan_in) from ``model_seed``."""
@@ -66,7 +66,7 @@ def nce_config(L=8, depth=3, width=64, seed=0, x_pt=0.5, model_seed=0):
     cs = cluster_space()
     s = ce_structure(L, seed, x_pt)
     P = synthetic_model(len(cs.orbits) + 1, depth, width, 1, model_seed)
-    m = NCEModel(cs, s, P, shell_edges=(0.0, 3.3), act="silu", pool="sum")
+    m = NCEModel(cs, s, P, shell_edges=(0.0, 3.3), act="silu", pool="sum", mma=mma)
     return m, m.sig0
 
 

@@ -72,7 +72,9 @@ def _compare(st, ref, E_tol):
 
 
 @pytest.mark.parametrize("precision,path,warps,cluster", [(64, 1, 8, 1), (32, 1, 8, 1), (64, 2, 8, 1), (32, 2, 4, 1),
-                                                          (64, 2, 1, 1), (64, 2, 8, 2), (32, 2, 4, 4), (64, 2, 16, 8)])
+                                                          (64, 2, 1, 1), (64, 2, 8, 2), (32, 2, 4, 4), (64, 2, 16, 8),
+                                                          (64, 3, 8, 1), (32, 3, 4, 1), (64, 3, 1, 1), (64, 3, 16, 2),
+                                                          (32, 3, 8, 4)])
 def test_trajectory_host_stream(cuda, precision, path, warps, cluster):
     """Seeded host proposal stream + exchange uniforms: bit-exact occupancy trajectory, energies, acceptance,
     slot permutation and slot-ordered samples vs the oracle (cluster > 1: each replica spread over that many
@@ -106,7 +108,7 @@ def test_trajectory_host_stream(cuda, precision, path, warps, cluster):
     assert int(st.n_acc.sum()) > 0
 
 
-@pytest.mark.parametrize("path", [1, 2])
+@pytest.mark.parametrize("path", [1, 2, 3])
 def test_trajectory_philox_multichunk(cuda, path):
     """Device Philox stream, 3 chunks with exchanges: equals the oracle's Philox restatement."""
     torch = cuda
@@ -156,8 +158,8 @@ def test_batch_equals_alone(cuda):
         assert torch.equal(a.sigma, b.sigma) and torch.equal(a.E, b.E) and torch.equal(a.rep_of_slot, b.rep_of_slot)
 
 
-@pytest.mark.parametrize("cluster", [2, 4])
-def test_cluster_equals_single_cta(cuda, cluster):
+@pytest.mark.parametrize("cluster,path", [(2, 2), (4, 2), (2, 3), (4, 3)])
+def test_cluster_equals_single_cta(cuda, cluster, path):
     """Philox stream with exchanges, 3 chunks: a replica spread over a thread-block cluster gives the same
     trajectory as one CTA, alone and in a batch of jobs."""
     torch = cuda
@@ -170,7 +172,7 @@ def test_cluster_equals_single_cta(cuda, cluster):
     for c in range(3):
         Ea = torch.zeros((T // 10, R), dtype=torch.float64, device="cuda"); Eb = torch.zeros_like(Ea)
         run_chunk(gce, a, T, c * T, 99, 64, 8, None, 10, Ea, True, path=2, cluster=1)
-        run_chunk(gce, b, T, c * T, 99, 64, 8, None, 10, Eb, True, path=2, cluster=cluster)
+        run_chunk(gce, b, T, c * T, 99, 64, 8, None, 10, Eb, True, path=path, cluster=cluster)
         torch.cuda.synchronize()
         assert torch.equal(a.sigma, b.sigma) and torch.equal(a.E, b.E) and torch.equal(Ea, Eb)
         assert torch.equal(a.n_acc, b.n_acc) and torch.equal(a.rep_of_slot, b.rep_of_slot)
@@ -189,7 +191,7 @@ def test_cluster_equals_single_cta(cuda, cluster):
     sts = [_engine_state(s2, e2, b2) for (_, s2, e2, b2) in jobs]
     hs = (C.c_void_p * 2)(*[j[0].handle.value for j in jobs])
     ss = (_lib.NcePtState * 2)(*[s.struct() for s in sts])
-    cks = (_lib.NcePtChunk * 2)(*[make_chunk(500, 0, 7 + k, 64, 8, None, 1, None, True, path=2, cluster=cluster)
+    cks = (_lib.NcePtChunk * 2)(*[make_chunk(500, 0, 7 + k, 64, 8, None, 1, None, True, path=path, cluster=cluster)
                                   for k in range(2)])
     _lib.check(_lib.lib().nce_ce_run_batch(2, hs, ss, cks, _lib.stream_ptr()), "batch")
     torch.cuda.synchronize()
@@ -229,11 +231,13 @@ def test_sign_parity_small_cells(cuda, L):
     gce, orc, sig_r, beta = _setup(L, seed=9, R=R)
     E0 = np.array([orc.energy(x) for x in sig_r])
     a = _engine_state(sig_r, E0, beta); b = _engine_state(sig_r, E0, beta); ref = new_state(sig_r, E0, beta)
+    c = _engine_state(sig_r, E0, beta)
     run_chunk(gce, a, T, 0, 31, 64, 2, None, 1, None, True, path=1)
     run_chunk(gce, b, T, 0, 31, 64, 2, None, 1, None, True, path=2)
+    run_chunk(gce, c, T, 0, 31, 64, 2, None, 1, None, True, path=3)
     orc.run(ref, T, 0, 31, None, 1, None, True)
     torch.cuda.synchronize()
-    _compare(a, ref, 1e-9); _compare(b, ref, 1e-9)
+    _compare(a, ref, 1e-9); _compare(b, ref, 1e-9); _compare(c, ref, 1e-9)
 
 
 def test_out_of_range_proposal_is_flagged(cuda):
@@ -263,11 +267,11 @@ def test_tracked_cluster_vector_sums(cuda):
     R, T = 8, 3000
     gce, orc, sig_r, beta = _setup(5, seed=13, R=R)
     E0 = np.array([orc.energy(x) for x in sig_r])
-    for precision, cluster in ((64, 1), (32, 2)):
+    for precision, cluster, path in ((64, 1, 2), (32, 2, 2), (64, 1, 3), (32, 4, 3)):
         st = _engine_state(sig_r, E0, beta).track_counts(gce)
         assert np.abs(gce.energy_from_counts(st.cv).cpu().numpy() - E0).max() < 1e-9
         for c in range(3):
-            run_chunk(gce, st, T, c * T, 4321, precision, 8, None, 1, None, True, path=2, cluster=cluster)
+            run_chunk(gce, st, T, c * T, 4321, precision, 8, None, 1, None, True, path=path, cluster=cluster)
         torch.cuda.synchronize()
         assert torch.equal(st.cv, gce.cluster_counts(st.sigma))
         Ef = gce.batched_energy(st.sigma).cpu().numpy()

@@ -137,3 +137,65 @@ def test_cluster_equals_single_cta(cuda):
     torch.cuda.synchronize()
     assert torch.equal(a.sigma, b.sigma) and torch.equal(a.rep_of_slot, b.rep_of_slot)
     assert torch.equal(a.n_acc, b.n_acc) and torch.allclose(a.E, b.E, rtol=0, atol=0)
+
+
+def _model_bench_mma(L, seed, mma, width=64):
+    from neuralce_gb300.nce import NCEModel, synthetic_model
+    from neuralce_gb300.workloads import cluster_space
+    from oracle.nce_oracle import NCEOracle
+    cs = cluster_space()
+    s = random_cell((L, L, L), seed)
+    P = synthetic_model(len(cs.orbits) + 1, 3, width, 1, 0)
+    m = NCEModel(cs, s, P, shell_edges=(0.0, 3.3), act="silu", pool="sum", mma=mma)
+    return m, NCEOracle(m.geo, P, act="silu", pool="sum")
+
+
+@pytest.mark.parametrize("mma,width", [(3, 64), (3, 128), (1, 64), (3, 32)])
+def test_tensor_core_forms_vs_oracle(cuda, mma, width):
+    """Layer contractions on tensor cores: split bf16 (mma 3) stays within the float32 bounds of the oracle
+    (energies 1e-4 eV, per-step dE 1e-4 eV); plain bf16 operands (mma 1) within its stated bound (per-step dE
+    5e-2 eV on this model, whose total energy is ~1e2 eV); a chain of forced moves keeps the carried energy equal
+    to a rebuild of the caches in the same form."""
+    torch = cuda
+    from neuralce_gb300.nce import NCEState
+    from oracle.nce_oracle import run_chain
+    m, orc = _model_bench_mma(3, 4, mma, width)
+    tol_E, tol_dE = (1e-4 * max(1.0, m.N / 64), 1e-4) if mma == 3 else (5e-1, 5e-2)
+    rng = np.random.default_rng(3)
+    sig = np.stack([m.sig0[rng.permutation(m.N)] for _ in range(2)]).astype(np.int8)
+    st = NCEState(m, sig, np.ones(2)).full_cache()
+    torch.cuda.synchronize()
+    for r in range(2):
+        c = orc.full_cache(sig[r].astype(np.int64))
+        assert abs(float(st.E[r]) - orc.energy_of(c)) * m.scale_eV < tol_E, (float(st.E[r]), orc.energy_of(c))
+    T = 8
+    pi = rng.integers(0, m.N, T).astype(np.int32); pj = rng.integers(0, m.N, T).astype(np.int32)
+    st = NCEState(m, m.sig0[None].astype(np.int8), np.ones(1)).full_cache()
+    dE = torch.zeros((T, 1), dtype=torch.float64, device="cuda")
+    props = tuple(torch.as_tensor(x.reshape(T, 1)).cuda() for x in (pi, pj, np.full(T, 0.5)))
+    st.run_chunk(T, 0, proposals=props, dE_out=dE, force=1)
+    torch.cuda.synchronize()
+    cache = orc.full_cache(m.sig0.astype(np.int64))
+    _, sig_ref, _, _, dEs, _ = run_chain(orc, cache, m.sig0, pi, pj, np.full(T, 0.5), 0.0, m.scale_eV)
+    err = np.abs((dE.cpu().numpy()[:, 0] - dEs) * m.scale_eV).max()
+    print(f"mma {mma} width {width}: max |dE - oracle| = {err:.3e} eV")
+    assert err < tol_dE, err
+    assert np.array_equal(st.sigma[0].cpu().numpy(), sig_ref.astype(np.int8))
+    Ecar = float(st.E[0].item())
+    st2 = NCEState(m, st.sigma.cpu().numpy(), np.ones(1)).full_cache()
+    torch.cuda.synchronize()
+    assert abs(Ecar - float(st2.E[0].item())) * m.scale_eV < 1e-4 * max(1.0, m.N / 64)
+
+
+def test_tensor_core_cluster_equals_single_cta(cuda):
+    torch = cuda
+    from neuralce_gb300.nce import NCEState
+    from neuralce_gb300.workloads import ladder, replica_configs
+    m, _ = _model_bench_mma(3, 6, 3)
+    _, beta = ladder(4)
+    sig = replica_configs(m.sig0, 4, 3)
+    a = NCEState(m, sig, beta).full_cache(); b = NCEState(m, sig, beta).full_cache()
+    a.run_chunk(30, 0, seed=5, exchange_rounds=2, cluster=1)
+    b.run_chunk(30, 0, seed=5, exchange_rounds=2, cluster=4)
+    torch.cuda.synchronize()
+    assert torch.equal(a.sigma, b.sigma) and torch.equal(a.rep_of_slot, b.rep_of_slot) and torch.equal(a.E, b.E)
