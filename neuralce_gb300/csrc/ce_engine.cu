@@ -21,6 +21,7 @@
 #include <vector>
 
 #include <cooperative_groups.h>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -67,6 +68,8 @@ struct CEJob {
     int32_t max_chunks;
     int32_t sig_smem;      // this job's occupancy is copied into shared memory for the chunk
     int64_t *cv;           // (R, n_cols) tracked cluster-vector sums or null
+    const int64_t *ecol_fix; // (n_cols) 2 eci of each column in fixed point (x 2^fix_shift), float64 kernels
+    int32_t fix_shift;
 };
 
 struct CEBatch {
@@ -311,6 +314,7 @@ __global__ void __launch_bounds__(1024) ce_pt_chunk_kernel(const __grid_constant
 // kernel's precision (float64 or float32); the counts are exact.
 struct BinProp {
     int64_t ia, ib; double logu;
+    int64_t thr;                  // fixed-point acceptance threshold: accept iff dE * 2^S < thr (float64 kernels)
     int32_t ka[3], kb[3], ba, bb;
 };
 
@@ -360,6 +364,18 @@ __device__ __forceinline__ void bin_propose(const CEJob &jb, int64_t g0, int64_t
         ia = ib = 0;                                   // same site -> same species -> rejected step
     }
     P.ia = ia; P.ib = ib; P.logu = log(u);
+    if (jb.fix_shift > 0) {
+        // logu < -beta dE  <=>  dE < -logu / beta (beta > 0)  <=>  dE 2^S < ceil(-logu / beta 2^S)
+        const double beta = (double)jb.beta_slot[t];
+        if (beta > 0.0) {
+            const double xs = -P.logu / beta * ldexp(1.0, jb.fix_shift);
+            P.thr = xs >= 4.611686018427388e18 ? (int64_t)4611686018427387904ll : (int64_t)ceil(xs);
+        } else {
+            P.thr = P.logu < 0.0 ? (int64_t)4611686018427387904ll : -(int64_t)4611686018427387904ll;
+        }
+    } else {
+        P.thr = 0;
+    }
     site_coords32(jb, ia, P.ba, P.ka); site_coords32(jb, ib, P.bb, P.kb);
 }
 
@@ -417,10 +433,24 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     if (sig_smem)
         for (int64_t i = tid; i < jb.N; i += nt) sig[i] = gsig[i];
     uint8_t *bits = smem + L.bits;                         // [side][pfc][n_nbr]
-    const uint8_t *sbits = jb.sbits;                       // [pfc][species < 4] -> sign bit
+    uint32_t smask = 0;                                    // sign bit of (point-function column c, species q) at c*4+q
+    for (int c = 0; c < n_pfc; ++c)
+        for (int q = 0; q < 4; ++q) smask |= (uint32_t)(__ldg(jb.sbits + c * 4 + q) & 1u) << (c * 4 + q);
     const int32_t t = jb.slot_of_rep[r];
     const double beta = (double)jb.beta_slot[t];
     double E = jb.E[r], Emin = jb.E_min_rep[r];
+    // float64: the step's dE is an exact fixed-point integer sum (x 2^S); the chunk's energy change and its running
+    // minimum are kept in it and turned into float64 at the samples and at the end
+    constexpr bool FIX = std::is_same<Acc, double>::value;
+    const bool fix = FIX && jb.fix_shift > 0;
+    const double fscale = fix ? ldexp(1.0, -jb.fix_shift) : 0.0;
+    const double E0c = E;
+    long long dsum = 0, dmin = 0;
+    long long *efix = reinterpret_cast<long long *>(ecol);
+    if (fix) {
+        __syncthreads();                                   // ecol (float64) was just written; the same bytes take the fixed-point values
+        for (int c = tid; c < n_cols; c += nt) efix[c] = (long long)__ldg(jb.ecol_fix + c);
+    }
     int64_t nacc = 0;
     const int R = jb.R;
     // proposals are drawn 32 at a time (one per lane of the producer warp), one batch ahead of their use
@@ -458,7 +488,7 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                 if (isa) near_flag = 1;
                 uint8_t *bs = bits + (size_t)side * n_pfc * n_nbr;
                 for (int c = 0; c < n_pfc; ++c)
-                    bs[c * n_nbr + n] = (uint8_t)(sbits[c * 4 + so] | (sbits[c * 4 + sn] << 1) | (isa << 2));
+                    bs[c * n_nbr + n] = (uint8_t)(((smask >> (c * 4 + so)) & 1u) | (((smask >> (c * 4 + sn)) & 1u) << 1) | (isa << 2));
             }
             __syncthreads();
             if (!producer || nw == 1) {
@@ -516,17 +546,33 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
             if (CLUSTER) cg::this_cluster().sync(); else __syncthreads();
             // 3. dE = sum_c 2 eci_c n_c (warp 0, fixed order), accept, write
             if (warp == 0) {
-                Acc part = Acc(0);
-                for (int c = lane; c < n_cols; c += 32) {
-                    const int n = cntp[c];
-                    if (n) { part += ecol[c] * (Acc)n; if (!track) cntp[c] = 0; }
-                }
-                part = warp_sum(part);                  // butterfly: every lane holds the same sum
-                const double dEd = (double)part;
-                const bool accept = P.logu < -beta * dEd;
-                if (lane == 0 && accept) {
-                    sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new;
-                    E += dEd; ++nacc;
+                bool accept;
+                if (fix) {
+                    long long part = 0;
+                    for (int c = lane; c < n_cols; c += 32) {
+                        const int n = cntp[c];
+                        if (n) { part += (long long)n * efix[c]; if (!track) cntp[c] = 0; }
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+                    accept = part < P.thr;
+                    if (lane == 0 && accept) {
+                        sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new;
+                        dsum += part; ++nacc;
+                    }
+                } else {
+                    Acc part = Acc(0);
+                    for (int c = lane; c < n_cols; c += 32) {
+                        const int n = cntp[c];
+                        if (n) { part += ecol[c] * (Acc)n; if (!track) cntp[c] = 0; }
+                    }
+                    part = warp_sum(part);              // butterfly: every lane holds the same sum
+                    const double dEd = (double)part;
+                    accept = P.logu < -beta * dEd;
+                    if (lane == 0 && accept) {
+                        sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new;
+                        E += dEd; ++nacc;
+                    }
                 }
                 if (track)                              // each changed row moves its column's sum by +-2
                     for (int c = lane; c < n_cols; c += 32) {
@@ -538,11 +584,21 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
         }
         if (tid == 0) {
             near_flag = 0;
-            Emin = fmin(Emin, E);
-            if (rank == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
-                jb.E_samples[((s + 1) / jb.sample_interval - 1) * R + t] = E;
+            if (fix) {
+                dmin = dsum < dmin ? dsum : dmin;
+                if (rank == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
+                    jb.E_samples[((s + 1) / jb.sample_interval - 1) * R + t] = E0c + (double)dsum * fscale;
+            } else {
+                Emin = fmin(Emin, E);
+                if (rank == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
+                    jb.E_samples[((s + 1) / jb.sample_interval - 1) * R + t] = E;
+            }
         }
         __syncthreads();
+    }
+    if (fix && tid == 0 && jb.n_steps > 0) {
+        E = E0c + (double)dsum * fscale;
+        Emin = fmin(Emin, E0c + (double)dmin * fscale);
     }
     if (rank == 0) {
         if (sig_smem)
@@ -1055,6 +1111,7 @@ struct nce_ce_model {
     int32_t *err = nullptr;                  // device error word
     bool binary = false;                     // every point-function value is -1 or +1 (sign-parity kernel applies)
     uint8_t *sbits = nullptr; uint16_t *bix = nullptr; uint8_t *rcol = nullptr; double *ecol2_64 = nullptr; float *ecol2_32 = nullptr;
+    int64_t *ecol_fix = nullptr; int32_t fix_shift = 0;   // 2 eci per column x 2^fix_shift (exact dE sums, float64 path)
     int32_t n_cols = 0;
     uint32_t *chunks = nullptr; int32_t *n_chunks = nullptr; int32_t max_chunks = 0;
     // bit-sliced full energy: rows anchored at a site (col | members << 8 | first member << 12) per anchor basis,
@@ -1083,7 +1140,7 @@ static int upload(T *&dst, const T *src, size_t n) {
 
 static int free_model(nce_ce_model *m) {
     void *ptrs[] = {m->loc, m->pfc, m->eci64, m->eci32, m->rv_len, m->nb_b, m->nb_uo, m->pf64, m->pf32, m->act_b,
-                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->bix, m->rcol, m->ecol2_64, m->ecol2_32, m->chunks, m->n_chunks, m->brows, m->bmem, m->brow_off, m->brow_n, m->plane_pfc, m->ecol1, m->planes, m->cv_scratch,
+                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->bix, m->rcol, m->ecol2_64, m->ecol2_32, m->ecol_fix, m->chunks, m->n_chunks, m->brows, m->bmem, m->brow_off, m->brow_n, m->plane_pfc, m->ecol1, m->planes, m->cv_scratch,
                     m->energy_partial, m->staging_base};
     for (void *p : ptrs) if (p) cudaFree(p);
     delete m;
@@ -1107,6 +1164,7 @@ static CEJob make_job(const nce_ce_model *m, const nce_pt_state *st, const nce_p
     j.loc = m->loc; j.pfc = m->pfc; j.eci = p64 ? (const void *)m->eci64 : (const void *)m->eci32;
     j.sbits = m->sbits; j.bix = m->bix; j.rcol = m->rcol; j.n_cols = m->n_cols;
     j.ecol2 = p64 ? (const void *)m->ecol2_64 : (const void *)m->ecol2_32;
+    j.ecol_fix = m->ecol_fix; j.fix_shift = p64 ? m->fix_shift : 0;
     j.chunks = m->chunks; j.n_chunks = m->n_chunks; j.max_chunks = m->max_chunks;
     (void)bin;
     j.rv_len = m->rv_len; j.nb_b = m->nb_b; j.nb_uo = m->nb_uo; j.pf = p64 ? (const void *)m->pf64 : (const void *)m->pf32;
@@ -1477,7 +1535,7 @@ int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
         if (e != cudaSuccess) rc = fail(NCE_ERR_CUDA, "nce_ce_create: %s", cudaGetErrorString(e));
     }
     // sign-parity eligibility: every point-function value is exactly -1 or +1, at most 4 species
-    bool bin = t->max_sp <= 4;
+    bool bin = t->max_sp <= 4 && t->n_pfc <= 8;          // sign bits of (column, species) fit one 32-bit mask
     std::vector<uint8_t> sb((size_t)t->n_pfc * 4, 0);
     for (int c = 0; c < t->n_pfc && bin; ++c)
         for (int q = 0; q < t->max_sp; ++q) {
@@ -1508,6 +1566,19 @@ int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
             if (!rc) rc = upload(m->bix, bx.data(), bx.size());
             if (!rc) rc = upload(m->rcol, rc8.data(), rc8.size());
             if (!rc) rc = upload(m->ecol2_64, e2.data(), e2.size());
+            {
+                // fixed point for exact dE sums: |sum_c n_c e_c| <= 2 J max|e| 2^S < 2^61
+                double emax = 0.0;
+                for (double v : e2) emax = std::max(emax, std::fabs(v));
+                int S = 60;
+                if (emax > 0.0) S = std::min(60, (int)std::floor(61.0 - std::log2(2.0 * t->J * emax)));
+                if (S >= 20) {
+                    std::vector<int64_t> ef(e2.size());
+                    for (size_t i = 0; i < e2.size(); ++i) ef[i] = (int64_t)std::llround(std::ldexp(e2[i], S));
+                    if (!rc) rc = upload(m->ecol_fix, ef.data(), ef.size());
+                    m->fix_shift = S;
+                }
+            }
             if (!rc) rc = upload(m->ecol2_32, f2.data(), f2.size());
             // column-aligned chunks of at most 32 consecutive rows
             std::vector<std::vector<uint32_t>> ch(t->nB);

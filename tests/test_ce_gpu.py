@@ -171,7 +171,7 @@ def test_cluster_equals_single_cta(cuda, cluster, path):
     a = _engine_state(sig_r, E0, beta); b = _engine_state(sig_r, E0, beta)
     for c in range(3):
         Ea = torch.zeros((T // 10, R), dtype=torch.float64, device="cuda"); Eb = torch.zeros_like(Ea)
-        run_chunk(gce, a, T, c * T, 99, 64, 8, None, 10, Ea, True, path=2, cluster=1)
+        run_chunk(gce, a, T, c * T, 99, 64, 8, None, 10, Ea, True, path=path, cluster=1)
         run_chunk(gce, b, T, c * T, 99, 64, 8, None, 10, Eb, True, path=path, cluster=cluster)
         torch.cuda.synchronize()
         assert torch.equal(a.sigma, b.sigma) and torch.equal(a.E, b.E) and torch.equal(Ea, Eb)
@@ -186,7 +186,7 @@ def test_cluster_equals_single_cta(cuda, cluster, path):
     alone = []
     for k, (g2, s2, e2, b2) in enumerate(jobs):
         st = _engine_state(s2, e2, b2)
-        run_chunk(g2, st, 500, 0, 7 + k, 64, 8, None, 1, None, True, path=2, cluster=1)
+        run_chunk(g2, st, 500, 0, 7 + k, 64, 8, None, 1, None, True, path=path, cluster=1)
         alone.append(st)
     sts = [_engine_state(s2, e2, b2) for (_, s2, e2, b2) in jobs]
     hs = (C.c_void_p * 2)(*[j[0].handle.value for j in jobs])
