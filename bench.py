@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--L", type=int, default=8)
     ap.add_argument("--R", type=int, default=32)
     ap.add_argument("--chunk", type=int, default=5000)
-    ap.add_argument("--workload", choices=["ce", "nce", "ce-batch", "serve", "ce-large", "nce-large"], default="ce")
+    ap.add_argument("--workload", choices=["ce", "nce", "ce-batch", "serve", "ce-large", "nce-large", "ce-energy"], default="ce")
     ap.add_argument("--nce-mma", type=int, default=-1, help="NeuralCE contractions: 0 fp32, 1 bf16, 3 split bf16 (-1: workload default)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the serving side measurement (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=3, help="chunks of the batched-form side measurement (0 = skip)")
@@ -165,7 +165,7 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, steps=3, warmup=1, seed=0, cluster=0):
+def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, steps=3, warmup=1, seed=0, cluster=0, mma=0):
     exchange_every = min(exchange_every, chunk)
     """NeuralCE configuration 1: local receptive-field update, float32, R replicas 300-1400 K; a step is one
     chunk of ``chunk`` MC steps + chunk//exchange_every exchange rounds; full re-anchor every ceil(N/chunk)
@@ -173,7 +173,7 @@ def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, step
     import torch
     from neuralce_gb300.nce import NCEState
     from neuralce_gb300.workloads import ladder, nce_config, replica_configs
-    m, sig = nce_config(L, depth, width, seed)
+    m, sig = nce_config(L, depth, width, seed, mma=mma)
     _, beta = ladder(R)
     st = NCEState(m, replica_configs(sig, R, 1 + seed), beta).full_cache()
     tune = None
@@ -208,7 +208,28 @@ def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, step
             "config": f"NeuralCE fp32: {m.N} sites, R={R}, depth {depth}, width {width}, SiLU, sum readout, 12-NN shell, "
                       f"chunk {chunk} steps + {max(chunk // exchange_every, 1)} exchange rounds, re-anchor every {anchor} chunks",
             "receptive_field": [int(x) for x in m.keep['ball_end'][0]], "accept_rate": float(st.n_acc.sum().item()) / (R * step),
-            "ctas_per_replica": cluster, "autotune_ms": tune}
+            "ctas_per_replica": cluster, "autotune_ms": tune,
+            "contractions": ["fp32 CUDA cores", "bf16 tensor cores", "", "split-bf16 tensor cores"][mma]}
+
+
+def bench_energy(L=64, R=128, reps=5, seed=0):
+    """Full energy (the re-anchor / set-up kernel) of R configurations of an L^3 conventional fcc cell on the
+    sign-parity tables: bit planes + exact column sums + float64 energies."""
+    import torch
+    from neuralce_gb300.workloads import ServeModels, random_occupancy
+    gce = ServeModels().ce(L)
+    sig = torch.as_tensor(random_occupancy(gce.n_atoms, 0.5, R, seed)).cuda()
+    gce.batched_energy(sig)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        gce.batched_energy(sig)
+    b.record(); torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    return {"value": gce.n_atoms * R / (ms / 1e3), "unit": "site-replicas/s", "ms_per_step": ms,
+            "config": f"full energy, bit-sliced: fcc {L}^3 conventional ({gce.n_atoms} sites) x {R} configurations",
+            "rows_per_site": int(gce.info["Rt"]) // int(gce.info["nB"])}
 
 
 def bench_batch(steps=3, warmup=1, chunk=5000, reanchor=10000, n_jobs=64, alone_jobs=8, alone_steps=2000):
@@ -512,6 +533,16 @@ def main():
                               "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": {"workload": r["config"]},
                               "large": r}), flush=True)
         return
+    if args.workload == "ce-energy":
+        from neuralce_gb300 import _lib
+        _lib.lib()
+        r = bench_energy(L=64 if args.L == 8 else args.L, R=128 if args.R == 32 else args.R)
+        if rank == 0:
+            print(json.dumps({"metric": "full-energy site-replicas/s", "value": r["value"], "unit": r["unit"], "n_gpus": world,
+                              "steps": 5, "warmup": 1, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+                              "scaling": "weak", "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic",
+                              "config": {"workload": r["config"]}, "energy": r}), flush=True)
+        return
     if args.workload == "nce-large":
         from neuralce_gb300 import _lib
         _lib.lib()
@@ -536,7 +567,8 @@ def main():
     if args.workload == "nce":
         from neuralce_gb300 import _lib
         _lib.lib()
-        r = bench_nce(L=args.L, R=args.R, chunk=args.nce_chunk, steps=args.steps, warmup=args.warmup, seed=rank)
+        r = bench_nce(L=args.L, R=args.R, chunk=args.nce_chunk, steps=args.steps, warmup=args.warmup, seed=rank,
+                      mma=max(args.nce_mma, 0))
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": r["value"], "unit": "swap attempts/s", "n_gpus": world, "steps": args.steps,
                               "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
