@@ -1536,11 +1536,20 @@ int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
     }
     // sign-parity eligibility: every point-function value is exactly -1 or +1, at most 4 species
     bool bin = t->max_sp <= 4 && t->n_pfc <= 8;          // sign bits of (column, species) fit one 32-bit mask
+    // point-function columns the rows use (an inert sublattice's unused columns, and species a sublattice does not
+    // allow, carry 0 in the table and do not matter)
+    std::vector<char> used((size_t)t->n_pfc, 0);
+    for (int b = 0; b < t->nB; ++b)
+        for (int q = 0; q < t->Rv_len[b]; ++q)
+            for (int k = 0; k < t->mo; ++k) {
+                const int c = t->Rv_pfc[((size_t)b * t->J + q) * t->mo + k];
+                if (c >= 0 && c < t->n_pfc) used[c] = 1;
+            }
     std::vector<uint8_t> sb((size_t)t->n_pfc * 4, 0);
     for (int c = 0; c < t->n_pfc && bin; ++c)
-        for (int q = 0; q < t->max_sp; ++q) {
+        for (int q = 0; q < t->max_sp && used[c]; ++q) {
             const double v = t->pf[(size_t)c * t->max_sp + q];
-            if (v == 1.0) sb[(size_t)c * 4 + q] = 0;
+            if (v == 1.0 || v == 0.0) sb[(size_t)c * 4 + q] = 0;
             else if (v == -1.0) sb[(size_t)c * 4 + q] = 1;
             else bin = false;
         }
