@@ -57,6 +57,11 @@ struct NceDev {
     const uint16_t *Rv_loc;                   // (nB, J, mo) index of each row member in its site's ball-0 list
     int32_t w0max;                            // ball-0 entries per basis, maximum
     int32_t mma;                              // 0 float32 CUDA cores, 1 bf16 tensor cores, 3 split bf16 (3 products)
+    // point functions +-1 (l0bin): the layer-0 change of a row is 0 or +-2 w exactly; Rv_wfix = llrint(2 w 2^40),
+    // thsign[(M * maxP + p) * maxM + s] = 1 where theta < 0
+    int32_t l0bin; const long long *Rv_wfix; const uint8_t *thsign;
+    const int32_t *Rv_desc;                   // (nB, J, mo) l0bin member: loc | valid << 16 | sign bits of species 0..3 << 20
+    const long long *col_wfix;                // (K + 1) l0bin: the (shared) 2 w 2^40 of each channel's rows
 };
 
 struct NceJob {
@@ -357,6 +362,18 @@ __device__ __forceinline__ float group_sum(float v, int ncg) {
     return v;
 }
 
+// energy of a site from its last-layer outputs (this lane's 4 columns at c0) and its layer-0 row hr: every lane of
+// the site's group adds its head terms and its share of the linear layer-0 term (channels c0/4, c0/4 + ncg, ...),
+// then one group sum.  The full caches and the local update both use it, so unchanged inputs give identical bits.
+__device__ __forceinline__ float site_energy(const float *v, int c0, const float *hw, const float *hr, const float *lin, int C0,
+                                             int ncg) {
+    float part = 0.f;
+    for (int q = 0; q < 4; ++q) part = fmaf(v[q], hw[c0 + q], part);
+    if (hr)
+        for (int c = c0 >> 2; c < C0; c += ncg) part = fmaf(hr[c], lin[c], part);
+    return group_sum(part, ncg);
+}
+
 // One MC step of one replica, run by a cluster of CL CTAs (CL = 1: a single CTA).  The leader (rank 0) draws the
 // proposal, builds the receptive field and the layer-0 change; every level's tiles are spread over the cluster;
 // dE partials reach the leader through distributed shared memory; the leader decides and every CTA commits its
@@ -457,7 +474,72 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
     for (int idx = tid; idx < n0 * m.C0; idx += nt) dh[idx] = 0ull;
     __syncthreads();
     const int Jt = 2 * m.J;
-    for (int rr = tid; rr < Jt; rr += nt) {
+    if (m.l0bin) {
+        // +-1 point functions: parities of the old and new products; each changed row moves its members' channel by
+        // exactly +-2 w, and all rows of one channel share w, so the change is an integer count per (site, channel)
+        // (32-bit atomics) times that channel's fixed-point 2 w.  Every row of a flip contains that flip's site, and
+        // the rows of a channel are consecutive, so the site's own count is summed per warp and channel run.
+        int32_t *dcount = reinterpret_cast<int32_t *>(dh);
+        const int lane = tid & 31;
+        for (int base = tid - lane; base < Jt; base += nt) {
+            const int rr = base + lane;
+            int f = 0, ch = 0, csign = 0, pc = 0;
+            long long wf = 0;
+            if (rr < Jt) {
+                f = rr >= m.J;
+                const int jr = f ? rr - m.J : rr;
+                const int b = f ? ctl.bj : ctl.bi;
+                const int e = b * m.J + jr;
+                wf = m.Rv_wfix[e];
+                if (wf != 0) {
+                    unsigned po = 0, pn = 0;
+                    int32_t pos[8], own[8];
+                    const int32_t *es = ent_site + f * m.w0max;
+                    const int32_t centre = f ? (int32_t)ctl.sj : (int32_t)ctl.si;
+                    int n_own = 0;
+                    int32_t dsc[8];
+                    for (int mm = 0; mm < m.mo; ++mm) dsc[mm] = __ldg(m.Rv_desc + (size_t)e * m.mo + mm);   // loads in flight together
+                    for (int mm = 0; mm < m.mo; ++mm) {
+                        own[mm] = 0;
+                        const int32_t d = dsc[mm];
+                        if (!((d >> 16) & 1)) continue;
+                        const int q = d & 0xffff;
+                        const int32_t st = es[q];
+                        pos[mm] = ent_pos[f * m.w0max + q];
+                        own[mm] = st == centre;
+                        n_own += own[mm];
+                        int so = ent_sig[f * m.w0max + q], sn = so;
+                        if (f == 0) { if (st == (int32_t)ctl.si) sn = ctl.ssj; }
+                        else {
+                            if (st == (int32_t)ctl.si) { so = ctl.ssj; sn = ctl.ssj; }
+                            if (st == (int32_t)ctl.sj) sn = ctl.ssi;
+                        }
+                        po ^= (unsigned)(d >> (20 + so)) & 1u; pn ^= (unsigned)(d >> (20 + sn)) & 1u;
+                    }
+                    if (po != pn) {
+                        const long long fx = pn ? -wf : wf;         // new product -1: (pn - po) w = -2 w
+                        ch = m.Rv_col[e] + 1;
+                        (void)fx;
+                        for (int mm = 0; mm < m.mo; ++mm) {
+                            if (!((dsc[mm] >> 16) & 1)) continue;
+                            const int p = pos[mm];
+                            if (p < 0 || p >= n0) { atomicOr(jb.err, 8); continue; }
+                            if (own[mm] && n_own == 1) { csign = pn ? -1 : 1; pc = p; continue; }
+                            atomicAdd(&dcount[(size_t)p * m.C0 + ch], pn ? -1 : 1);
+                        }
+                    }
+                }
+            }
+            const unsigned key = csign ? (((unsigned)f << 16) | (unsigned)ch) : 0xffffffffu;
+            const unsigned peers = __match_any_sync(0xffffffffu, key);
+            const unsigned plus = __ballot_sync(0xffffffffu, csign > 0), minus = __ballot_sync(0xffffffffu, csign < 0);
+            if (csign && lane == __ffs(peers) - 1) {
+                const int k = __popc(peers & plus) - __popc(peers & minus);
+                if (k) atomicAdd(&dcount[(size_t)pc * m.C0 + ch], k);
+            }
+        }
+    }
+    for (int rr = tid; rr < Jt && !m.l0bin; rr += nt) {
         const int f = rr >= m.J, jr = f ? rr - m.J : rr;
         const int b = f ? ctl.bj : ctl.bi;
         const int e = b * m.J + jr;
@@ -496,10 +578,20 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
     }
     __syncthreads();
     float *nb0w = level_buf(jb, nb, 0);
+    if (m.l0bin) {
+        const int32_t *dcount = reinterpret_cast<const int32_t *>(dh);
+        for (int idx = tid; idx < n0 * m.C0; idx += nt) {
+            const int p = idx / m.C0, c = idx % m.C0;
+            const int64_t s = list[p];
+            const long long fx = (long long)dcount[idx] * m.col_wfix[c];
+            nb0w[idx] = h0[(size_t)s * m.C0 + c] + (float)((double)fx * kInvFix);
+        }
+    } else {
     for (int idx = tid; idx < n0 * m.C0; idx += nt) {
         const int p = idx / m.C0, c = idx % m.C0;
         const int64_t s = list[p];
         nb0w[idx] = h0[(size_t)s * m.C0 + c] + (float)((double)(long long)dh[idx] * kInvFix);
+    }
     }
     }   // !err
     }   // !same
@@ -536,17 +628,17 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         } else {
             layer_tiles(jb, lvl, LWs[lvl], cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
                         [&](int64_t pos, int c0, const float *v) {
-                            float part = 0.f;
-                            for (int q = 0; q < 4; ++q) part = fmaf(v[q], hw[c0 + q], part);
-                            part = group_sum(part, ncg);
-                            if (pos >= 0 && c0 == 0) {
-                                const int64_t st = list[pos];
-                                float l0 = 0.f;
+                            const float *hr = nullptr;
+                            int64_t st = 0;
+                            if (pos >= 0) {
+                                st = list[pos];
                                 const int p0 = slot[st];
-                                const float *hr = (p0 >= 0 && p0 < n0) ? nb0 + (size_t)p0 * m.C0 : h0 + (size_t)st * m.C0;
-                                for (int c = 0; c < m.C0; ++c) l0 = fmaf(hr[c], lin[c], l0);
+                                hr = (p0 >= 0 && p0 < n0) ? nb0 + (size_t)p0 * m.C0 : h0 + (size_t)st * m.C0;
+                            }
+                            const float tot = site_energy(v, c0, hw, hr, lin, m.C0, ncg);
+                            if (pos >= 0 && c0 == 0) {
                                 const bool active = m.Mb[st % m.nB] > 1;
-                                const float ev = active ? l0 + part : 0.f;
+                                const float ev = active ? tot : 0.f;
                                 en[pos] = ev;
                                 atomicAdd(&ctl.dacc, (unsigned long long)llrint(((double)ev - (double)e[st]) * kFix));
                             }
@@ -775,15 +867,9 @@ __global__ void __launch_bounds__(256, 1) nce_layer_all_kernel(NceJob jb, int lv
         });
     } else {
         layer_tiles(jb, lvl, LW, in, nullptr, nullptr, 0, nullptr, 0, cnt, &a, X, src, [&](int64_t pos, int c0, const float *v) {
-            float part = 0.f;
-            for (int q = 0; q < 4; ++q) part = fmaf(v[q], __ldg(m.head_w + c0 + q), part);
-            part = group_sum(part, ncg);
-            if (pos >= 0 && c0 == 0) {
-                const int64_t st = a + pos;
-                float l0 = 0.f;
-                for (int c = 0; c < m.C0; ++c) l0 = fmaf(h0[(size_t)st * m.C0 + c], __ldg(m.lin + c), l0);
-                e_out[st] = (m.Mb[st % m.nB] > 1) ? l0 + part : 0.f;
-            }
+            const int64_t st = a + pos;
+            const float tot = site_energy(v, c0, m.head_w, pos >= 0 ? h0 + (size_t)st * m.C0 : nullptr, m.lin, m.C0, ncg);
+            if (pos >= 0 && c0 == 0) e_out[st] = (m.Mb[st % m.nB] > 1) ? tot : 0.f;
         });
     }
 }
@@ -958,6 +1044,51 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
     chk(dup(h, d->Rv_b, nr, m.Rv_b)); chk(dup(h, d->Rv_uo, nr * 3, m.Rv_uo)); chk(dup(h, d->Rv_p, nr, m.Rv_p));
     chk(dup(h, d->Rv_m, nr, m.Rv_m)); chk(dup(h, d->Rv_loc, nr, m.Rv_loc)); chk(dup(h, d->Rv_col, (size_t)d->nB * d->J, m.Rv_col)); chk(dup(h, d->Rv_w, (size_t)d->nB * d->J, m.Rv_w));
     chk(dup(h, d->Mb, (size_t)d->nB, m.Mb)); chk(dup(h, d->theta, (size_t)(d->maxM + 1) * d->maxP * d->maxM, m.theta));
+    {
+        // +-1 point functions on every (M, p, species) a row can use -> exact integer layer-0 changes
+        const size_t nth = (size_t)(d->maxM + 1) * d->maxP * d->maxM;
+        std::vector<uint8_t> ts(nth, 0);
+        bool bin = true;
+        for (size_t i = 0; i < nr && bin; ++i) {
+            if (!d->Rv_m[i]) continue;
+            const int M = d->Mb[d->Rv_b[i]], pi = d->Rv_p[i];
+            for (int sp = 0; sp < M; ++sp) {
+                const double v = d->theta[((size_t)M * d->maxP + pi) * d->maxM + sp];
+                if (v == 1.0) ts[((size_t)M * d->maxP + pi) * d->maxM + sp] = 0;
+                else if (v == -1.0) ts[((size_t)M * d->maxP + pi) * d->maxM + sp] = 1;
+                else { bin = false; break; }
+            }
+        }
+        bin = bin && d->maxM <= 4;
+        for (int b = 0; b < d->nB; ++b)
+            for (int q = 0; q < d->ball_end[b * (d->depth + 1)]; ++q) bin = bin && q < 0x10000;
+        m.l0bin = bin ? 1 : 0;
+        if (bin) {
+            std::vector<long long> wf((size_t)d->nB * d->J);
+            for (size_t i = 0; i < wf.size(); ++i) wf[i] = llrint(2.0 * d->Rv_w[i] * kFix);
+            std::vector<long long> cw((size_t)d->C0, 0);
+            std::vector<char> cseen((size_t)d->C0, 0);
+            for (size_t i = 0; i < wf.size() && bin; ++i) {
+                if (wf[i] == 0) continue;
+                const int ch = d->Rv_col[i] + 1;
+                if (ch < 0 || ch >= d->C0) { bin = false; break; }
+                if (!cseen[ch]) { cseen[ch] = 1; cw[ch] = wf[i]; }
+                else if (cw[ch] != wf[i]) bin = false;
+            }
+            m.l0bin = bin ? 1 : 0;
+            std::vector<int32_t> dsc(nr, 0);
+            for (size_t i = 0; i < nr; ++i) {
+                if (!d->Rv_m[i]) continue;
+                const int M = d->Mb[d->Rv_b[i]], pi = d->Rv_p[i];
+                int32_t v = (int32_t)d->Rv_loc[i] | (1 << 16);
+                for (int sp = 0; sp < M; ++sp) v |= (int32_t)ts[((size_t)M * d->maxP + pi) * d->maxM + sp] << (20 + sp);
+                dsc[i] = v;
+            }
+            chk(dup(h, wf.data(), wf.size(), m.Rv_wfix)); chk(dup(h, ts.data(), ts.size(), m.thsign));
+            chk(dup(h, dsc.data(), dsc.size(), m.Rv_desc));
+            chk(dup(h, cw.data(), cw.size(), m.col_wfix));
+        }
+    }
     chk(dup(h, d->Sh_b, ns, m.Sh_b)); chk(dup(h, d->Sh_uo, ns * 3, m.Sh_uo)); chk(dup(h, d->Sh_m, ns, m.Sh_m));
     chk(dup(h, d->Sh_inv, (size_t)d->nB * d->P, m.Sh_inv));
     chk(dup(h, d->ball_b, nbl, m.ball_b)); chk(dup(h, d->ball_uo, nbl * 3, m.ball_uo));
