@@ -181,7 +181,47 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
         }
         __syncthreads();
         // 2) X = [h | masked shell means] of the tile's sites: one warp per site, lanes over channels (coalesced rows)
-        {
+        if (P == 1 && W <= 12 && Cin <= 64) {
+            // one shell of at most 12 partners: two sites per warp with all 2 x 13 rows' loads in flight at once
+            const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+            const int c0 = lane, c1 = lane + 32;
+            const bool h0ok = c0 < Cin, h1ok = c1 < Cin;
+            auto row = [&](int32_t code) -> const float * {
+                return code >= 0 ? newl + (size_t)code * Cin : cache + (size_t)(-(int64_t)code - 1) * Cin;
+            };
+            for (int mm = warp; mm < tm; mm += 2 * nwarp) {
+                const int mb = mm + nwarp;
+                const bool two = mb < tm;
+                float va[2][13], vb[2][13];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int32_t *sr = src + (h ? mb : mm) * PW;
+                    const bool on = h == 0 || two;
+#pragma unroll
+                    for (int u = 0; u < 13; ++u) {
+                        const int32_t q = (on && u <= W) ? sr[u] : INT_MIN;
+                        const bool ok = q != INT_MIN;
+                        const float *rr = ok ? row(q) : cache;
+                        va[h][u] = (ok && h0ok) ? rr[c0] : 0.f;
+                        vb[h][u] = (ok && h1ok) ? rr[c1] : 0.f;
+                    }
+                }
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (h == 1 && !two) break;
+                    const int ms = h ? mb : mm;
+                    float *xr = X + (size_t)ms * XS;
+                    const int64_t s = direct0 ? (*direct0 + pos0 + t0 + ms) : list[pos0 + t0 + ms];
+                    const int32_t b = (int32_t)((uint32_t)s % (uint32_t)m.nB);
+                    float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+                    for (int u = 1; u < 13; ++u) { s0 += va[h][u]; s1 += vb[h][u]; }
+                    const float inv = m.Sh_inv[b * P];
+                    if (h0ok) { xr[c0] = va[h][0]; xr[Cin + c0] = s0 * inv; }
+                    if (h1ok) { xr[c1] = vb[h][0]; xr[Cin + c1] = s1 * inv; }
+                }
+            }
+        } else {
             const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
             for (int mm = warp; mm < tm; mm += nwarp) {
                 const int32_t *sr = src + mm * PW;
