@@ -385,8 +385,10 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     __shared__ BinProp prop[64];                      // ring of two batches of 32 proposals
     __shared__ int32_t near_flag;
     // CLUSTER: one replica per thread-block cluster; every CTA keeps its own copy of the replica's occupancy and draws
-    // the same proposals, the row chunks are split over the CTAs and the per-column counts are added into every
-    // CTA's counters through distributed shared memory, so all CTAs reach the same decision.
+    // the same proposals, the row chunks are split over the CTAs, each CTA counts its chunks locally, and after the
+    // cluster barrier every CTA reads all CTAs' counts through distributed shared memory, so all reach the same
+    // decision.  A count buffer is cleared by its owner only after the next cluster barrier (when every CTA has
+    // read it); the two buffers alternate between evaluated swaps.
     int CL = 1, rank = 0;
     if (CLUSTER) { cg::cluster_group cl = cg::this_cluster(); CL = (int)cl.num_blocks(); rank = (int)cl.block_rank(); }
     const int rep_idx = blockIdx.x / CL;
@@ -531,27 +533,29 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                     const int n1 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s1);
                     const int n2 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s2);
                     if (lane == 0) {
-                        if (CLUSTER) {
-                            for (int q = 0; q < CL; ++q) {
-                                if (n1) atomicAdd(rcnt[q] + par * n_cols + c1, n1);
-                                if (n2) atomicAdd(rcnt[q] + par * n_cols + c2, n2);
-                            }
-                        } else {
-                            if (n1) atomicAdd(&cntp[c1], n1);
-                            if (n2) atomicAdd(&cntp[c2], n2);
-                        }
+                        if (n1) atomicAdd(&cntp[c1], n1);
+                        if (n2) atomicAdd(&cntp[c2], n2);
                     }
                 }
             }
             if (CLUSTER) cg::this_cluster().sync(); else __syncthreads();
             // 3. dE = sum_c 2 eci_c n_c (warp 0, fixed order), accept, write
             if (warp == 0) {
+                // this swap's count of column c, summed over the cluster's CTAs
+                auto count = [&](int c) -> int {
+                    if (!CLUSTER) return cntp[c];
+                    int n = 0;
+                    for (int q = 0; q < CL; ++q) n += rcnt[q][par * n_cols + c];
+                    return n;
+                };
+                if (CLUSTER)                            // every CTA has read the other buffer (previous swap) by now
+                    for (int c = lane; c < n_cols; c += 32) cnt[(par ^ 1) * n_cols + c] = 0;
                 bool accept;
                 if (fix) {
                     long long part = 0;
                     for (int c = lane; c < n_cols; c += 32) {
-                        const int n = cntp[c];
-                        if (n) { part += (long long)n * efix[c]; if (!track) cntp[c] = 0; }
+                        const int n = count(c);
+                        if (n) { part += (long long)n * efix[c]; if (!track && !CLUSTER) cntp[c] = 0; }
                     }
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
@@ -563,8 +567,8 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                 } else {
                     Acc part = Acc(0);
                     for (int c = lane; c < n_cols; c += 32) {
-                        const int n = cntp[c];
-                        if (n) { part += ecol[c] * (Acc)n; if (!track) cntp[c] = 0; }
+                        const int n = count(c);
+                        if (n) { part += ecol[c] * (Acc)n; if (!track && !CLUSTER) cntp[c] = 0; }
                     }
                     part = warp_sum(part);              // butterfly: every lane holds the same sum
                     const double dEd = (double)part;
@@ -576,8 +580,8 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                 }
                 if (track)                              // each changed row moves its column's sum by +-2
                     for (int c = lane; c < n_cols; c += 32) {
-                        const int n = cntp[c];
-                        if (n) { if (accept) dcv[c] += 2 * n; cntp[c] = 0; }
+                        const int n = count(c);
+                        if (n) { if (accept) dcv[c] += 2 * n; if (!CLUSTER) cntp[c] = 0; }
                     }
             }
             par ^= 1;
