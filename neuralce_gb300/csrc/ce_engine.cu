@@ -557,8 +557,14 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                         const int n = count(c);
                         if (n) { part += (long long)n * efix[c]; if (!track && !CLUSTER) cntp[c] = 0; }
                     }
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+                    // exact warp sum of |part| < 2^61 in three 21-bit slices (hardware 32-bit reductions, no carries lost)
+                    {
+                        const unsigned l0 = (unsigned)(part & 0x1fffff), l1 = (unsigned)((part >> 21) & 0x1fffff);
+                        const int l2 = (int)(part >> 42);
+                        const unsigned s0 = __reduce_add_sync(0xffffffffu, l0), s1 = __reduce_add_sync(0xffffffffu, l1);
+                        const int s2 = __reduce_add_sync(0xffffffffu, l2);
+                        part = (long long)s0 + ((long long)s1 << 21) + ((long long)s2 << 42);
+                    }
                     accept = part < P.thr;
                     if (lane == 0 && accept) {
                         sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new;
