@@ -62,6 +62,9 @@ struct NceDev {
     int32_t l0bin; const long long *Rv_wfix; const uint8_t *thsign;
     const int32_t *Rv_desc;                   // (nB, J, mo) l0bin member: loc | valid << 16 | sign bits of species 0..3 << 20
     const long long *col_wfix;                // (K + 1) l0bin: the (shared) 2 w 2^40 of each channel's rows
+    // bit-sliced layer 0 (full caches; l0bin with every member on point function 0): per basis, the reverse rows'
+    // members as (basis, uo0, uo1, uo2) or basis -1, each row's channel, and the channel weight (w, float64)
+    int32_t h0bits; const int4 *h0mem; const double *col_w;
 };
 
 struct NceJob {
@@ -855,6 +858,111 @@ __global__ void __launch_bounds__(256, 1) nce_chunk_cluster_kernel(const __grid_
 
 // ── full cache ─────────────────────────────────────────────────────────────────────────────────────
 // h0 by pulling every reverse row of each site (deterministic), standardised, float32
+// Layer 0 of every site, bit-sliced (+-1 point functions): one plane per basis holds the sign bit of each site,
+// each (k0, k1) row twice over (2 d2 bits) so that any offset in [0, d2) reads 32 consecutive bits.  A thread takes
+// 32 consecutive sites along k2 and, for every reverse row of their basis (all slots: every cluster instance that
+// contains the site), XORs the members' shifted plane words: bit j is the parity of site j's product.  Odd parities
+// are counted per site in a vertical (bit-sliced) counter while the rows of one channel go by; the channel value is
+// then (rows - 2 odd) w - mu / sd, as the float64 row sum gives.
+__global__ void nce_plane_kernel(NceDev m, const int8_t *__restrict__ sigma, int32_t R, int32_t W2, uint32_t *__restrict__ planes) {
+    const int64_t d0d1 = (int64_t)m.d0 * m.d1;
+    const int64_t rows = (int64_t)R * m.nB * d0d1;
+    const int lane = threadIdx.x & 31;
+    const int64_t wstride = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < rows; w += wstride) {
+        const int64_t kk = w % d0d1;
+        const int64_t t = w / d0d1;
+        const int b = (int)(t % m.nB);
+        const int64_t r = t / m.nB;
+        const int M = m.Mb[b];
+        const uint8_t *ts = m.thsign + (size_t)M * m.maxP * m.maxM;          // point function 0 of M species
+        const int8_t *sg = sigma + r * m.N + kk * m.d2 * m.nB + b;
+        uint32_t *out = planes + w * W2;
+        for (int q = 0; q < W2; ++q) {
+            const int pos = q * 32 + lane;
+            uint32_t bit = 0;
+            if (pos < 2 * m.d2) {
+                const int k2 = pos < m.d2 ? pos : pos - m.d2;
+                bit = ts[sg[(int64_t)k2 * m.nB] & 3];
+            }
+            const uint32_t word = __ballot_sync(0xffffffffu, bit != 0u);
+            if (lane == 0) out[q] = word;
+        }
+    }
+}
+
+// grid (blocks, nB, R): threads over the (k0, k1, 32-site word) items of basis blockIdx.y, replica blockIdx.z
+__global__ void __launch_bounds__(128) nce_h0_bits_kernel(NceDev m, const uint32_t *__restrict__ planes, int32_t W2, float *h0) {
+    const int b = blockIdx.y, r = blockIdx.z;
+    const int d0 = m.d0, d1 = m.d1, d2 = m.d2;
+    const int Wn = (d2 + 31) >> 5;
+    const int64_t items = (int64_t)d0 * d1 * Wn;
+    const int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= items) return;
+    const int w = (int)(it % Wn);
+    const int64_t kk = it / Wn;
+    const int k1 = (int)(kk % d1), k0 = (int)(kk / d1);
+    const int nv = min(32, d2 - 32 * w);
+    const uint32_t mask = nv >= 32 ? 0xffffffffu : ((1u << nv) - 1u);
+    const uint32_t *pr = planes + (int64_t)r * m.nB * d0 * d1 * W2;
+    const int C0 = m.C0;
+    // site j of the word: canonical index ((k0 d1 + k1) d2 + 32 w + j) nB + b
+    float *out0 = h0 + (((int64_t)r * m.N) + ((int64_t)(k0 * d1 + k1) * d2 + 32 * w) * m.nB + b) * C0;
+    const int64_t sstride = (int64_t)m.nB * C0;
+    if (m.Mb[b] < 2) {                                       // inactive sites: zeros
+        for (int j = 0; j < nv; ++j) for (int c = 0; c < C0; ++c) out0[j * sstride + c] = 0.f;
+        return;
+    }
+    const float ch0 = (float)((1.0 - (double)m.mu[0]) / (double)m.sd[0]);
+    for (int j = 0; j < nv; ++j) out0[j * sstride] = ch0;
+    constexpr int NQ = 13;                                    // vertical counter planes: up to 8191 rows per channel
+    uint32_t cnt[NQ];
+    auto flush = [&](int ch, int nrows) {
+        const double wc = m.col_w[ch], base = (double)m.mu[ch] / (double)m.sd[ch];
+        for (int j = 0; j < nv; ++j) {
+            int odd = 0;
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) odd |= (int)((cnt[q] >> j) & 1u) << q;
+            out0[j * sstride + ch] = (float)((double)(nrows - 2 * odd) * wc - base);
+        }
+    };
+    int ch_cur = 1, nrows = 0;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) cnt[q] = 0u;
+    const int4 *mem = m.h0mem + (size_t)b * m.J * m.mo;
+    for (int jr = 0; jr < m.J; ++jr) {
+        const int e = b * m.J + jr;
+        if (m.Rv_wfix[e] == 0) continue;
+        const int ch = m.Rv_col[e] + 1;
+        if (ch != ch_cur) {
+            flush(ch_cur, nrows);
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) cnt[q] = 0u;
+            for (int c = ch_cur + 1; c < ch; ++c) flush(c, 0);
+            ch_cur = ch; nrows = 0;
+        }
+        uint32_t par = 0;
+        for (int mm = 0; mm < m.mo; ++mm) {
+            const int4 d = mem[jr * m.mo + mm];                // (member basis or -1, uo0, uo1, uo2)
+            if (d.x < 0) continue;
+            int a0 = k0 + d.y; a0 -= a0 >= d0 ? d0 : 0;
+            int a1 = k1 + d.z; a1 -= a1 >= d1 ? d1 : 0;
+            const int pos = 32 * w + d.w;
+            const uint32_t *row = pr + (((int64_t)d.x * d0 + a0) * d1 + a1) * W2 + (pos >> 5);
+            par ^= __funnelshift_r(__ldg(row), __ldg(row + 1), (unsigned)(pos & 31));
+        }
+        // add the odd-parity bits into the vertical counter (ripple carry)
+        uint32_t carry = par & mask;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) { const uint32_t t = cnt[q] & carry; cnt[q] ^= carry; carry = t; }
+        ++nrows;
+    }
+    flush(ch_cur, nrows);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) cnt[q] = 0u;
+    for (int c = ch_cur + 1; c < C0; ++c) flush(c, 0);
+}
+
 __global__ void nce_h0_kernel(NceDev m, const int8_t *sigma, int32_t R, float *h0) {
     const int64_t total = (int64_t)R * m.N;
     for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (int64_t)gridDim.x * blockDim.x) {
@@ -950,6 +1058,7 @@ struct nce_nce_model {
     // scratch for R replicas
     int32_t *slot = nullptr, *list = nullptr; float *newbuf = nullptr, *e_new = nullptr; int64_t stride = 0; int32_t R_alloc = 0;
     unsigned long long *eacc = nullptr; int32_t eacc_n = 0;
+    uint32_t *planes = nullptr; size_t planes_n = 0;      // bit planes of the configurations (bit-sliced layer 0)
 };
 
 namespace nce {
@@ -1127,6 +1236,33 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
             chk(dup(h, wf.data(), wf.size(), m.Rv_wfix)); chk(dup(h, ts.data(), ts.size(), m.thsign));
             chk(dup(h, dsc.data(), dsc.size(), m.Rv_desc));
             chk(dup(h, cw.data(), cw.size(), m.col_wfix));
+            // bit-sliced layer 0: every member on point function 0, rows of a basis sorted by channel, at most 8191
+            // rows per channel (13-bit counters), channel weights w
+            bool hb = m.l0bin != 0 && d->C0 >= 2;
+            std::vector<int4> hm(nr, make_int4(-1, 0, 0, 0));
+            std::vector<double> cwd((size_t)d->C0, 0.0);
+            for (int b = 0; b < d->nB && hb; ++b) {
+                int last = 0, run = 0;
+                for (int j = 0; j < d->J && hb; ++j) {
+                    const size_t e = (size_t)b * d->J + j;
+                    if (wf[e] == 0) continue;
+                    const int ch = d->Rv_col[e] + 1;
+                    if (ch < last) hb = false;
+                    run = ch == last ? run + 1 : 1; last = ch;
+                    if (run > 8191) hb = false;
+                    cwd[ch] = d->Rv_w[e];
+                    for (int k = 0; k < d->mo; ++k) {
+                        const size_t i = e * d->mo + k;
+                        if (!d->Rv_m[i]) continue;
+                        if (d->Rv_p[i] != 0) hb = false;
+                        hm[i] = make_int4(d->Rv_b[i], d->Rv_uo[3 * i], d->Rv_uo[3 * i + 1], d->Rv_uo[3 * i + 2]);
+                    }
+                }
+            }
+            if (hb) {
+                chk(dup(h, hm.data(), hm.size(), m.h0mem)); chk(dup(h, cwd.data(), cwd.size(), m.col_w));
+                m.h0bits = 1;
+            }
         }
     }
     chk(dup(h, d->Sh_b, ns, m.Sh_b)); chk(dup(h, d->Sh_uo, ns * 3, m.Sh_uo)); chk(dup(h, d->Sh_m, ns, m.Sh_m));
@@ -1163,7 +1299,8 @@ int nce_nce_destroy(nce_nce_handle h) {
     if (!h) return NCE_OK;
     cudaDeviceSynchronize();
     for (void *p : h->allocs) cudaFree(p);
-    for (void *p : {(void *)h->slot, (void *)h->list, (void *)h->newbuf, (void *)h->e_new, (void *)h->err, (void *)h->eacc}) if (p) cudaFree(p);
+    for (void *p : {(void *)h->slot, (void *)h->list, (void *)h->newbuf, (void *)h->e_new, (void *)h->err, (void *)h->eacc,
+                    (void *)h->planes}) if (p) cudaFree(p);
     delete h;
     return NCE_OK;
 }
@@ -1176,7 +1313,23 @@ int nce_nce_full_cache(nce_nce_handle h, const nce_nce_state *st, void *stream) 
     cudaStream_t s = (cudaStream_t)stream;
     const NceDev &m = h->dev;
     const int64_t tot = (int64_t)st->R * m.N;
-    nce_h0_kernel<<<(int)std::min<int64_t>((tot + 127) / 128, 65535), 128, 0, s>>>(m, st->sigma, st->R, st->h0);
+    if (m.h0bits && st->R <= 65535) {
+        const int32_t W2 = (2 * m.d2 + 31) / 32 + 1;
+        const size_t need = (size_t)st->R * m.nB * m.d0 * m.d1 * W2;
+        if (need > h->planes_n) {
+            if (h->planes) { cudaStreamSynchronize(s); cudaFree(h->planes); }
+            h->planes = nullptr; h->planes_n = 0;
+            NCE_CUDA(cudaMalloc((void **)&h->planes, sizeof(uint32_t) * need));
+            h->planes_n = need;
+        }
+        const int64_t prow = (int64_t)st->R * m.nB * m.d0 * m.d1;
+        nce_plane_kernel<<<(int)std::min<int64_t>((prow + 7) / 8, 1 << 20), 256, 0, s>>>(m, st->sigma, st->R, W2, h->planes);
+        NCE_CUDA(cudaGetLastError());
+        const int64_t items = (int64_t)m.d0 * m.d1 * ((m.d2 + 31) / 32);
+        nce_h0_bits_kernel<<<dim3((unsigned)((items + 127) / 128), m.nB, st->R), 128, 0, s>>>(m, h->planes, W2, st->h0);
+    } else {
+        nce_h0_kernel<<<(int)std::min<int64_t>((tot + 127) / 128, 65535), 128, 0, s>>>(m, st->sigma, st->R, st->h0);
+    }
     NCE_CUDA(cudaGetLastError());
     NceJob jb = make_nce_job(h, st);
     const size_t xs = tile_smem(m);

@@ -22,12 +22,12 @@ def _model_pkl(mdl, s):
     return m, NCEOracle(m.geo, P, mu, sd, act="tanh", pool="mean")
 
 
-def _model_bench(L=3, seed=0):
+def _model_bench(L=3, seed=0, reps=None):
     from neuralce_gb300.nce import NCEModel, synthetic_model
     from neuralce_gb300.workloads import cluster_space
     from oracle.nce_oracle import NCEOracle
     cs = cluster_space()
-    s = random_cell((L, L, L), seed)
+    s = random_cell(reps or (L, L, L), seed)
     P = synthetic_model(len(cs.orbits) + 1, 3, 64, 1, 0)
     m = NCEModel(cs, s, P, shell_edges=(0.0, 3.3), act="silu", pool="sum")
     return m, NCEOracle(m.geo, P, act="silu", pool="sum")
@@ -42,12 +42,17 @@ def test_full_cache_golden_L10(cuda, nipt_model):
     assert abs(E - g["E_L10"]) < 2e-5, (E, g["E_L10"])
 
 
-@pytest.mark.parametrize("which", ["pkl", "bench"])
+@pytest.mark.parametrize("which", ["pkl", "bench", "long"])
 def test_full_cache_matches_oracle(cuda, nipt_model, which):
+    """Full caches (layer 0 bit-sliced over 32-site words along the last cell axis) vs the oracle; "long" is a
+    1 x 6 x 78 cell: three words per row, the last one ragged (14 sites)."""
     torch = cuda
     from neuralce_gb300.nce import NCEState
     if which == "pkl":
         m, orc = _model_pkl(nipt_model[0], random_cell((4, 4, 4), 1))
+    elif which == "long":
+        m, orc = _model_bench(seed=4, reps=(3, 3, 13))
+        assert tuple(m.geo["d"]) == (1, 6, 78)
     else:
         m, orc = _model_bench(3, 2)
     rng = np.random.default_rng(0)
