@@ -261,6 +261,12 @@ int nce_nce_full_cache(nce_nce_handle h, const nce_nce_state *st, void *stream);
 int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_chunk *ck, void *stream);
 int nce_nce_errors(nce_nce_handle h, int32_t *flags);
 
+/* Tensor-core tile GEMM of the NeuralCE layers (tcgen05, tensor-memory accumulator), exposed for testing:
+ * C[M x N] = A[M x K] B[K x N], float32 row-major device arrays, operands rounded to bf16 (split != 0: bf16 hi/lo
+ * pairs, hi*hi + hi*lo + lo*hi).  M a multiple of 128, N a multiple of 16 in [16, 256], K in [1, 256].
+ * No counterpart in the reference (its layers are XLA matmuls, local_update_implicit.py:43-80). */
+int nce_tc_gemm(const float *A, const float *B, float *C, int32_t M, int32_t N, int32_t K, int32_t split, void *stream);
+
 /* ── Job server (serving form) ──────────────────────────────────────────────────────────────────────────────
  * A resident server that runs many parallel-tempering jobs at once.  Jobs are admitted in submission order as
  * device memory within the server's budget frees up (a later job that fits may start before an earlier one

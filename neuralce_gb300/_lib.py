@@ -112,6 +112,7 @@ SIGNATURES = {
     "nce_nce_full_cache": (i32, [vp, P(NceNceState), vp]),
     "nce_nce_run_chunk": (i32, [vp, P(NceNceState), P(NceNceChunk), vp]),
     "nce_nce_errors": (i32, [vp, P(i32)]),
+    "nce_tc_gemm": (i32, [vp, vp, vp, i32, i32, i32, i32, vp]),
 }
 
 

@@ -26,6 +26,7 @@
 #include <cuda_bf16.h>
 
 #include "common.cuh"
+#include "umma.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -1119,9 +1120,80 @@ int nce_model_dims(nce_nce_handle h, int64_t *N, int32_t *C0, int32_t *D, int32_
     *N = h->dev.N; *C0 = h->dev.C0; *D = h->dev.D; *depth = h->dev.depth;
     return NCE_OK;
 }
+// ── tensor-core tile GEMM (tcgen05) ────────────────────────────────────────────────────────────
+// C[M x N] = A[M x K] B[K x N] (float32, row-major) on the tile path of the NeuralCE layers: one CTA of 4 warps
+// per 128 rows stages A and B^T as bf16 (hi, and lo = bf16(x - hi) when split) in the core-matrix layout, one
+// thread issues the MMAs into tensor memory, every warp reads its 32-lane quarter back.
+__global__ void __launch_bounds__(128) nce_tc_gemm_kernel(const float *A, const float *B, float *C, int32_t N, int32_t K,
+                                                          int32_t Kp, int32_t split, int32_t *err) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tslot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t row0 = (int64_t)blockIdx.x * 128;
+    const size_t abytes = (size_t)128 * Kp * 2, bbytes = (size_t)N * Kp * 2;
+    uint8_t *A0 = smem, *A1 = smem + abytes, *B0 = smem + (split ? 2 : 1) * abytes, *B1 = B0 + bbytes;
+    auto put = [&](uint8_t *hi, uint8_t *lo, uint32_t off, float v) {
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        *reinterpret_cast<__nv_bfloat16 *>(hi + off) = h;
+        if (split) *reinterpret_cast<__nv_bfloat16 *>(lo + off) = __float2bfloat16_rn(v - __bfloat162float(h));
+    };
+    for (int idx = tid; idx < 128 * Kp; idx += blockDim.x) {
+        const int r = idx / Kp, k = idx % Kp;
+        put(A0, A1, umma::core_off(r, k, Kp), k < K ? A[(row0 + r) * K + k] : 0.f);
+    }
+    for (int idx = tid; idx < N * Kp; idx += blockDim.x) {
+        const int n = idx / Kp, k = idx % Kp;
+        put(B0, B1, umma::core_off(n, k, Kp), k < K ? B[(size_t)k * N + n] : 0.f);
+    }
+    umma::fence_async_smem();
+    if (warp == 0) umma::tmem_alloc(&tslot, umma::tmem_cols(N));
+    if (tid == 0) umma::mbar_init(&mbar, 1);
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    const uint32_t tmem = tslot;
+    if (tid == 0) umma::issue_tile(tmem, A0, A1, B0, B1, N, Kp, split ? 3 : 1, &mbar);
+    if (!umma::mbar_wait(&mbar, 0) && lane == 0) atomicOr(err, 1);
+    umma::fence_after();
+    const int64_t row = row0 + warp * 32 + lane;
+    for (int c0 = 0; c0 < N; c0 += 16) {
+        float v[16];
+        umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) C[row * N + c0 + i] = v[i];
+    }
+    umma::fence_before();
+    __syncthreads();
+    if (warp == 0) umma::tmem_free(tmem, umma::tmem_cols(N));
+}
+
 }  // namespace nce
 
 extern "C" {
+
+int nce_tc_gemm(const float *A, const float *B, float *C, int32_t M, int32_t N, int32_t K, int32_t split, void *stream) {
+    NCE_CHECK(A && B && C, "nce_tc_gemm: null argument");
+    NCE_CHECK(M > 0 && M % 128 == 0, "nce_tc_gemm: M must be a positive multiple of 128");
+    NCE_CHECK(N >= 16 && N <= 256 && N % 16 == 0, "nce_tc_gemm: N must be a multiple of 16 in [16, 256]");
+    const int32_t Kp = (K + 15) / 16 * 16;
+    NCE_CHECK(K >= 1 && Kp <= 256, "nce_tc_gemm: K must be in [1, 256]");
+    const size_t sm = (size_t)(split ? 2 : 1) * ((size_t)128 * Kp * 2 + (size_t)N * Kp * 2);
+    NCE_CHECK(sm <= 200 * 1024, "nce_tc_gemm: tiles of %zu bytes exceed shared memory", sm);
+    cudaStream_t s = (cudaStream_t)stream;
+    int32_t *err = nullptr;
+    NCE_CUDA(cudaMallocAsync((void **)&err, sizeof(int32_t), s));
+    NCE_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), s));
+    NCE_CUDA(cudaFuncSetAttribute(nce_tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    nce_tc_gemm_kernel<<<M / 128, 128, sm, s>>>(A, B, C, N, K, Kp, split ? 1 : 0, err);
+    NCE_CUDA(cudaGetLastError());
+    int32_t h = 0;
+    NCE_CUDA(cudaMemcpyAsync(&h, err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    NCE_CUDA(cudaStreamSynchronize(s));
+    cudaFreeAsync(err, s);
+    NCE_CHECK(h == 0, "nce_tc_gemm: tensor-core completion wait timed out");
+    return NCE_OK;
+}
 
 int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
     NCE_CHECK(d && out, "nce_nce_create: null argument");

@@ -57,6 +57,18 @@ def synthetic_model(C0, depth=3, width=64, P=1, seed=0):
     return dict(lin=g((C0,), C0), layers=layers, head=dict(w=g((width,), width), b=0.0))
 
 
+def tc_gemm(A, B, split=False):
+    """A @ B on the tensor-core tile path of the layers (tcgen05): float32 CUDA tensors A (M, K), B (K, N) with
+    M % 128 == 0, N % 16 == 0 (16..256), K <= 256; operands rounded to bf16 (``split``: hi + lo pairs)."""
+    import torch
+    A = A.contiguous().float(); B = B.contiguous().float()
+    M, K = A.shape; N = B.shape[1]
+    out = torch.empty(M, N, dtype=torch.float32, device=A.device)
+    _lib.check(_lib.lib().nce_tc_gemm(A.data_ptr(), B.data_ptr(), out.data_ptr(), M, N, K, int(bool(split)),
+                                      _lib.stream_ptr()), "nce_tc_gemm")
+    return out
+
+
 class NCEModel:
     """Geometry + parameters of one cell, uploaded to the device (``nce_nce_create``)."""
 

@@ -204,3 +204,26 @@ def test_tensor_core_cluster_equals_single_cta(cuda):
     b.run_chunk(30, 0, seed=5, exchange_rounds=2, cluster=4)
     torch.cuda.synchronize()
     assert torch.equal(a.sigma, b.sigma) and torch.equal(a.rep_of_slot, b.rep_of_slot) and torch.equal(a.E, b.E)
+
+
+@pytest.mark.parametrize("K,N", [(16, 64), (76, 64), (128, 64), (256, 64), (128, 128), (80, 128), (40, 16)])
+def test_tc_gemm_matches_fp32(cuda, K, N):
+    """The tcgen05 tile GEMM (bf16 operands in the core-matrix layout, float32 accumulation in tensor memory)
+    against float64 products of the same bf16-rounded operands; the split form against the float64 product of
+    the float32 operands (hi*hi + hi*lo + lo*hi drops lo*lo: ~2^-16 relative)."""
+    torch = cuda
+    from neuralce_gb300.nce import tc_gemm
+    g = torch.Generator(device="cpu").manual_seed(K * 1000 + N)
+    A = torch.randn(256, K, generator=g).cuda()
+    B = (torch.randn(K, N, generator=g) / K ** 0.5).cuda()
+    C = tc_gemm(A, B)
+    ref = (A.bfloat16().double() @ B.bfloat16().double())
+    scale = (A.abs().double() @ B.abs().double())
+    assert ((C.double() - ref).abs() <= 1e-5 * scale + 1e-6).all(), float((C.double() - ref).abs().max())
+    Cs = tc_gemm(A, B, split=True)
+    ref64 = A.double() @ B.double()
+    err = ((Cs.double() - ref64).abs() / (scale + 1e-30)).max().item()
+    assert err < 2e-5, err
+    # the plain bf16 form is much further from the float32 product than the split form
+    err1 = ((C.double() - ref64).abs() / (scale + 1e-30)).max().item()
+    assert err1 > 4 * err
