@@ -30,6 +30,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "MC swap attempts/s (CE, NCE) vs plain FP64 form; p50/p99 PT-job latency"
+CONTRACTIONS = ["fp32 CUDA cores", "bf16 mma.sync tensor cores (fp32 accumulation)",
+                "bf16 tcgen05 tensor cores (fp32 accumulation in tensor memory)", "split-bf16 mma.sync tensor cores",
+                "split-bf16 tcgen05 tensor cores"]
 H100_PUBLISHED = 1_231_993.0          # reference CE PT, 2,048 sites, R=32, H100 (results/bench_stage/gpu_icet_*H100*.json)
 B_GATHER = 14_996                     # bytes of member occupancy per attempt, config-0 cluster set
 
@@ -48,7 +51,8 @@ def parse():
     ap.add_argument("--R", type=int, default=32)
     ap.add_argument("--chunk", type=int, default=5000)
     ap.add_argument("--workload", choices=["ce", "nce", "ce-batch", "serve", "ce-large", "nce-large", "ce-energy"], default="ce")
-    ap.add_argument("--nce-mma", type=int, default=-1, help="NeuralCE contractions: 0 fp32, 1 bf16, 3 split bf16 (-1: workload default)")
+    ap.add_argument("--nce-mma", type=int, default=-1, help="NeuralCE contractions: 0 fp32 CUDA cores; bf16 / split bf16 "
+                    "on tensor cores: 1 / 3 mma.sync, 2 / 4 tcgen05 (-1: workload default)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the serving side measurement (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=3, help="chunks of the batched-form side measurement (0 = skip)")
     ap.add_argument("--nce-steps", type=int, default=3, help="chunks of the NeuralCE side measurement (0 = skip)")
@@ -209,7 +213,7 @@ def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, step
                       f"chunk {chunk} steps + {max(chunk // exchange_every, 1)} exchange rounds, re-anchor every {anchor} chunks",
             "receptive_field": [int(x) for x in m.keep['ball_end'][0]], "accept_rate": float(st.n_acc.sum().item()) / (R * step),
             "ctas_per_replica": cluster, "autotune_ms": tune,
-            "contractions": ["fp32 CUDA cores", "bf16 tensor cores", "", "split-bf16 tensor cores"][mma]}
+            "contractions": CONTRACTIONS[mma]}
 
 
 def bench_energy(L=64, R=128, reps=5, seed=0):
@@ -290,21 +294,22 @@ def bench_batch(steps=3, warmup=1, chunk=5000, reanchor=10000, n_jobs=64, alone_
 
 
 def bench_serve(seconds=10.0, rate=50.0, ce_scale=0.01, nce_scale=0.0002, nce_max_sites=32768, seed=4, alone_jobs=0,
-                ce_exchange=500, nce_exchange=20):
+                ce_exchange=500, nce_exchange=20, nce_mma=2):
     """Configuration 4 (serving), scaled: Poisson arrivals at ``rate`` jobs/s for ``seconds``, CE or NeuralCE 50/50,
     sites log-uniform 256..1,048,576 (NeuralCE capped at ``nce_max_sites``), x_Pt ~ U[0.1, 0.9], R ~ U{8..128},
     steps log-uniform 10k..1M times ``ce_scale`` / ``nce_scale``.  Jobs are submitted to the job server at their
     arrival times (models and occupancies prepared beforehand); reports p50/p99 job latency (submission to
     results on the host) and the aggregate swap attempts/s over the makespan.  Capacity: the stream's CE jobs
     submitted at once, against the same jobs run one after another in the plain float64 kernel (``alone_jobs``
-    limits that to the first jobs; 0 = all)."""
+    limits that to the first jobs; 0 = all).  NeuralCE jobs run the precision form ``nce_mma`` (2: bf16 operands on
+    the tcgen05 tensor cores, float32 accumulation)."""
     import torch
     from neuralce_gb300.pt import PTState, run_chunk
     from neuralce_gb300.serve import Server
     from neuralce_gb300.workloads import ServeModels, ladder, random_occupancy, serve_stream
     t0 = time.time()
     jobs = serve_stream(rate, seconds, seed, ce_scale, nce_scale, nce_max_sites)
-    models = ServeModels()
+    models = ServeModels(mma=nce_mma)
     for j in jobs:
         j["model"] = models.ce(j["L"]) if j["kind"] == "ce" else models.nce(j["L"])
         j["sigma"] = random_occupancy(j["N"], j["x_pt"], j["R"], j["seed"] & 0xFFFFFFFF)
@@ -360,7 +365,7 @@ def bench_serve(seconds=10.0, rate=50.0, ce_scale=0.01, nce_scale=0.0002, nce_ma
             "config": f"serving: Poisson {rate:g} jobs/s for {seconds:g} s ({len(jobs)} jobs), CE/NeuralCE 50/50, "
                       f"sites log-U 256..1M (NeuralCE <= {nce_max_sites}), x_Pt U[0.1,0.9], R U{{8..128}}, steps log-U "
                       f"10k..1M x {ce_scale:g} (CE) / x {nce_scale:g} (NeuralCE), exchange every {ce_exchange} / {nce_exchange}; "
-                      f"CE fp32 with exact fp64 re-anchor per chunk, NeuralCE fp32",
+                      f"CE fp32 with exact fp64 re-anchor per chunk, NeuralCE {CONTRACTIONS[nce_mma]}",
             "jobs": len(jobs), "done": len(ok), "failed": st["failed"], "failures": failures,
             "latency_s": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max()) if len(lat) else None,
                           "ce_p50": pct(kinds["ce"], 50), "ce_p99": pct(kinds["ce"], 99),
@@ -435,10 +440,11 @@ def bench_large(L=136, R=256, chunk=5000, steps=3, warmup=1, precision=32, seed=
             "vs_h100_published_4344547": R * chunk * steps / tot / 4_344_547}
 
 
-def bench_nce_large(L=64, R=64, width=128, depth=3, chunk=100, steps=3, warmup=1, mma=1, seed=0, cluster=0):
+def bench_nce_large(L=64, R=64, width=128, depth=3, chunk=100, steps=3, warmup=1, mma=2, seed=0, cluster=0):
     """Configuration 3 (NeuralCE part): fcc L^3 conventional cell (L = 64: 1,048,576 sites), R replicas 300-1400 K,
-    the configuration-1 architecture widened to ``width``; layer contractions in bf16 on tensor cores with float32
-    accumulation (``mma`` 1; 3 = split bf16, 0 = float32 CUDA cores).  Occupancies drawn on the device.  A step is
+    the configuration-1 architecture widened to ``width``; layer contractions in bf16 on the tcgen05 tensor cores
+    with float32 accumulation in tensor memory (``mma`` 2; 1 = the same on mma.sync, 3 / 4 = split bf16 on mma.sync /
+    tcgen05, 0 = float32 CUDA cores).  Occupancies drawn on the device.  A step is
     one chunk of ``chunk`` MC steps per replica + one exchange round; the full caches are built once (timed
     separately)."""
     import torch
@@ -488,7 +494,7 @@ def bench_nce_large(L=64, R=64, width=128, depth=3, chunk=100, steps=3, warmup=1
     drift = float((st.E - E_car).abs().max().item())
     return {"value": R * chunk * steps / tot, "unit": "swap attempts/s", "ms_per_step": float(np.mean(ms)),
             "config": f"NeuralCE large cell: fcc {L}^3 conventional ({N} sites), R={R}, depth {depth}, width {width}, SiLU, sum, "
-                      f"{['fp32 CUDA cores', 'bf16 tensor cores (fp32 accumulation)', '', 'split-bf16 tensor cores'][mma]}, "
+                      f"{CONTRACTIONS[mma]}, "
                       f"chunk {chunk} steps + 1 exchange round",
             "sites": N, "replicas": R, "full_cache_ms": full_ms, "ctas_per_replica": cluster, "autotune_ms": tune,
             "carried_vs_rebuilt_energy_eV": drift, "device_state_GB": (R * N * (1 + 4 * m.C0 + 4 + 4 * m.D * max(depth - 1, 0))) / 1e9,
@@ -547,11 +553,11 @@ def main():
         from neuralce_gb300 import _lib
         _lib.lib()
         st_, wu_ = (args.steps if args.steps != 40 else 3), max(1, min(args.warmup, 2))
-        r = bench_nce_large(steps=st_, warmup=wu_, mma=(1 if args.nce_mma < 0 else args.nce_mma))
+        r = bench_nce_large(steps=st_, warmup=wu_, mma=(2 if args.nce_mma < 0 else args.nce_mma))
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": r["value"], "unit": "swap attempts/s", "n_gpus": world, "steps": st_,
                               "warmup": wu_, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-                              "vs_baseline": None, "dtype": "bf16" if args.nce_mma in (-1, 1) else "f32", "data": "synthetic",
+                              "vs_baseline": None, "dtype": "bf16" if args.nce_mma in (-1, 1, 2) else "f32", "data": "synthetic",
                               "config": {"workload": r["config"]}, "large": r}), flush=True)
         return
     if args.workload == "serve":
@@ -661,9 +667,10 @@ def main():
             "kernel": {1: "ce_pt_chunk_kernel", 3: "ce_bin2_chunk_kernel"}.get(args.path, "ce_bin_chunk_kernel"),
             "peak_source": src,
             "algorithmic_bytes_per_launch": R * T * B_GATHER}
-    nce_line = None
+    nce_line = nce_tc_line = None
     if rank == 0 and args.nce_steps > 0:
         nce_line = bench_nce(steps=args.nce_steps)
+        nce_tc_line = bench_nce(steps=args.nce_steps, mma=4)
     batch_line = None
     if rank == 0 and args.batch_steps > 0:
         batch_line = bench_batch(steps=args.batch_steps)
@@ -680,7 +687,7 @@ def main():
                 "vs_baseline": value / H100_PUBLISHED if (args.L == 8 and args.R == 32) else None,
                 "dtype": "f64" if args.precision == 64 else "f32", "data": "synthetic (seeded lattice, random-normal ECIs)",
                 "config": workload_config(args, gce), "clocks": clocks, "e2e": e2e, "gpu_launches": 2 * args.steps,
-                "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "batch": batch_line, "serve": serve_line,
+                "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "nce_tcgen05_split": nce_tc_line, "batch": batch_line, "serve": serve_line,
                 "launch": {"warps_per_cta": args.warps, "ctas_per_replica": args.cluster,
                            "path": ["auto", "general", "sign-parity", "sign-parity, two steps in flight"][args.path],
                            "autotune_ms": tuned},

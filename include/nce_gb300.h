@@ -225,8 +225,10 @@ typedef struct {
     const uint16_t *Rv_loc;/* (nB, J, mo) index of each masked row member in its site's ball-0 list (ball_b/ball_uo order) */
     int32_t mma;           /* layer contractions: 0 float32 on CUDA cores; 1 bf16 operands on tensor cores (mma.sync,
                               float32 accumulation); 3 the same with each operand split into two bf16 terms
-                              (hi*hi + hi*lo + lo*hi, near-float32 accuracy).  Tensor-core forms need an ungated model.
-                              Full caches and steps use the same form, so a run samples one consistent energy. */
+                              (hi*hi + hi*lo + lo*hi, near-float32 accuracy); 2 and 4 the bf16 and split forms on
+                              the fifth-generation tensor cores (tcgen05: 128-site tiles, accumulator in tensor
+                              memory).  Tensor-core forms need an ungated model.  Full caches and steps use the same
+                              form, so a run samples one consistent energy. */
 } nce_nce_desc;
 
 typedef struct nce_nce_model *nce_nce_handle;

@@ -66,6 +66,9 @@ struct NceDev {
     // bit-sliced layer 0 (full caches; l0bin with every member on point function 0): per basis, the reverse rows'
     // members as (basis, uo0, uo1, uo2) or basis -1, each row's channel, and the channel weight (w, float64)
     int32_t h0bits; const int4 *h0mem; const double *col_w;
+    // tcgen05 layer contractions (mma 2: bf16, mma 4: split bf16): per layer the weights as the B operand in bf16
+    // core-matrix layout ([D][Kp], Kp = Kin rounded up to 16; hi, then lo when split)
+    int32_t tc, tc_split; const uint8_t *Wt[kMaxLayers];
 };
 
 struct NceJob {
@@ -125,7 +128,30 @@ __device__ __forceinline__ float patched(const NceJob &jb, int lvl, const float 
 
 // Tile geometry of the layer GEMM: D/4 column groups of 4 outputs, 256/(D/4) site groups, TM sites per tile,
 // MS sites per thread (register micro-tile MS x 4).  D in {16, 32, 64, 128}.
-__host__ __device__ __forceinline__ int tile_tm(int D) { return 4 * (256 / (D / 4)); }   // 4 sites per thread
+__host__ __device__ __forceinline__ int tile_tm(int D, int tc = 0) { return tc ? 128 : 4 * (256 / (D / 4)); }   // 4 sites per thread
+__host__ __device__ __forceinline__ int kpad16(int k) { return (k + 15) & ~15; }
+
+// tensor-memory accumulator, completion mbarrier and the staged B operand of the tcgen05 tile path; `phase` is the
+// parity of the next completion (every thread of the CTA keeps the same count)
+struct TcCtx {
+    uint32_t tmem; uint64_t *mbar; uint32_t phase; uint8_t *W;
+};
+
+// allocation by warp 0 (D columns rounded up to a power of two >= 32) and the mbarrier, for the whole kernel
+__device__ __forceinline__ void tc_begin(int D, TcCtx &tc, uint8_t *wsm, uint64_t *mbar, uint32_t *tslot) {
+    if ((threadIdx.x >> 5) == 0) umma::tmem_alloc(tslot, umma::tmem_cols(D));
+    if (threadIdx.x == 0) umma::mbar_init(mbar, 1);
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    tc.tmem = *tslot; tc.mbar = mbar; tc.phase = 0; tc.W = wsm;
+}
+
+__device__ __forceinline__ void tc_end(int D, const TcCtx &tc) {
+    umma::fence_before();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) umma::tmem_free(tc.tmem, umma::tmem_cols(D));
+}
 __host__ __device__ __forceinline__ int tile_kin(int P, int C0, int D) { return (1 + P) * (C0 > D ? C0 : D); }
 
 // bf16 tensor-core helpers: mma.sync m16n8k16 (row-major A, column-major B, float32 accumulation).  Fragment
@@ -156,14 +182,35 @@ struct LayerW {            // weights of one layer as seen by the kernel (shared
 template <typename Sink>
 __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const float *cache, const float *newl, const int32_t *slot,
                             int32_t nlev, const int32_t *list, int64_t pos0, int64_t cnt, const int64_t *direct0, float *X,
-                            int32_t *src, Sink sink, int tile_begin = 0, int tile_stride = 1) {
+                            int32_t *src, Sink sink, int tile_begin = 0, int tile_stride = 1, TcCtx *tc = nullptr) {
     const NceDev &m = jb.m;
     const int Cin = lvl == 0 ? m.C0 : m.D, D = m.D, P = m.P, W = m.W;
     const int Kin = (1 + P) * Cin, XS = Kin + 1;
     const int tid = threadIdx.x, nt = blockDim.x;
-    const int ncg = D / 4, SG = 256 / ncg, TM = tile_tm(D), MS = TM / SG;
+    const int ncg = D / 4, SG = 256 / ncg, TM = tile_tm(D, tc != nullptr), MS = TM / SG;
     const int cg = tid % ncg, sg = tid / ncg;
     const int PW = 1 + P * W;
+    // tcgen05 path: the tile is the bf16 A operand [128][Kp] (hi, then lo when split) in core-matrix layout
+    const int Kp = kpad16(Kin);
+    uint8_t *A0 = reinterpret_cast<uint8_t *>(X), *A1 = A0 + (size_t)128 * Kp * 2;
+    if (tc) {
+        // this layer's B operand into shared memory (read by the tensor cores after the first tile barrier)
+        const size_t n16 = (size_t)Kp * D * 2 * (m.tc_split ? 2 : 1) / 16;
+        const uint4 *g = reinterpret_cast<const uint4 *>(m.Wt[lvl]);
+        uint4 *d = reinterpret_cast<uint4 *>(tc->W);
+        for (size_t i = tid; i < n16; i += nt) d[i] = __ldg(g + i);
+        umma::fence_async_smem();
+    }
+    auto xput = [&](int ms, int k, float v) {
+        if (tc) {
+            const uint32_t off = umma::core_off(ms, k, Kp);
+            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+            *reinterpret_cast<__nv_bfloat16 *>(A0 + off) = h;
+            if (m.tc_split) *reinterpret_cast<__nv_bfloat16 *>(A1 + off) = __float2bfloat16_rn(v - __bfloat162float(h));
+        } else {
+            X[(size_t)ms * XS + k] = v;
+        }
+    };
     for (int64_t t0 = (int64_t)tile_begin * TM; t0 < cnt; t0 += (int64_t)tile_stride * TM) {
         const int tm = (int)min((int64_t)TM, cnt - t0);
         // 1) source row of each site and shell partner: patched rows >= 0, cache rows -(q+1), masked partner INT_MIN
@@ -214,22 +261,49 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                 for (int h = 0; h < 2; ++h) {
                     if (h == 1 && !two) break;
                     const int ms = h ? mb : mm;
-                    float *xr = X + (size_t)ms * XS;
                     const int64_t s = direct0 ? (*direct0 + pos0 + t0 + ms) : list[pos0 + t0 + ms];
                     const int32_t b = (int32_t)((uint32_t)s % (uint32_t)m.nB);
                     float s0 = 0.f, s1 = 0.f;
 #pragma unroll
                     for (int u = 1; u < 13; ++u) { s0 += va[h][u]; s1 += vb[h][u]; }
                     const float inv = m.Sh_inv[b * P];
-                    if (h0ok) { xr[c0] = va[h][0]; xr[Cin + c0] = s0 * inv; }
-                    if (h1ok) { xr[c1] = vb[h][0]; xr[Cin + c1] = s1 * inv; }
+                    if (h0ok) { xput(ms, c0, va[h][0]); xput(ms, Cin + c0, s0 * inv); }
+                    if (h1ok) { xput(ms, c1, vb[h][0]); xput(ms, Cin + c1, s1 * inv); }
+                }
+            }
+        } else if (P == 1 && W <= 12 && Cin <= 128) {
+            // one shell, up to 128 channels: one site per warp, four channels per lane, all 13 rows' loads in flight
+            const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+            auto row = [&](int32_t code) -> const float * {
+                return code >= 0 ? newl + (size_t)code * Cin : cache + (size_t)(-(int64_t)code - 1) * Cin;
+            };
+            for (int mm = warp; mm < tm; mm += nwarp) {
+                const int32_t *sr = src + mm * PW;
+                float v[4][13];
+#pragma unroll
+                for (int u = 0; u < 13; ++u) {
+                    const int32_t q = u <= W ? sr[u] : INT_MIN;
+                    const bool ok = q != INT_MIN;
+                    const float *rr = ok ? row(q) : cache;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) v[j][u] = (ok && lane + 32 * j < Cin) ? rr[lane + 32 * j] : 0.f;
+                }
+                const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
+                const float inv = m.Sh_inv[(int32_t)((uint32_t)s % (uint32_t)m.nB) * P];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int c = lane + 32 * j;
+                    if (c >= Cin) continue;
+                    float a = 0.f;
+#pragma unroll
+                    for (int u = 1; u < 13; ++u) a += v[j][u];
+                    xput(mm, c, v[j][0]); xput(mm, Cin + c, a * inv);
                 }
             }
         } else {
             const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
             for (int mm = warp; mm < tm; mm += nwarp) {
                 const int32_t *sr = src + mm * PW;
-                float *xr = X + (size_t)mm * XS;
                 const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
                 const int32_t b = (int32_t)((uint32_t)s % (uint32_t)m.nB);
                 // two channels per lane (c, c + 32), all partner loads of a group of 8 issued before summing
@@ -240,8 +314,8 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                 };
                 {
                     const float *rr = row(sr[0]);
-                    if (h0ok) xr[c0] = rr[c0];
-                    if (h1ok) xr[c1] = rr[c1];
+                    if (h0ok) xput(mm, c0, rr[c0]);
+                    if (h1ok) xput(mm, c1, rr[c1]);
                 }
                 for (int p = 0; p < P; ++p) {
                     const int32_t *pc = sr + 1 + p * W;
@@ -260,21 +334,62 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                         for (int u = 0; u < 8; ++u) { s0 += va[u]; s1 += vb[u]; }
                     }
                     const float inv = m.Sh_inv[b * P + p];
-                    if (h0ok) xr[Cin + p * Cin + c0] = s0 * inv;
-                    if (h1ok) xr[Cin + p * Cin + c1] = s1 * inv;
+                    if (h0ok) xput(mm, Cin + p * Cin + c0, s0 * inv);
+                    if (h1ok) xput(mm, Cin + p * Cin + c1, s1 * inv);
                 }
                 for (int c = lane + 64; c < Cin; c += 32) {        // widths above 64 channels
-                    xr[c] = row(sr[0])[c];
+                    xput(mm, c, row(sr[0])[c]);
                     for (int p = 0; p < P; ++p) {
                         float a0 = 0.f;
                         for (int w = 0; w < W; ++w) { const int32_t q = sr[1 + p * W + w]; if (q != INT_MIN) a0 += row(q)[c]; }
-                        xr[Cin + p * Cin + c] = a0 * m.Sh_inv[b * P + p];
+                        xput(mm, Cin + p * Cin + c, a0 * m.Sh_inv[b * P + p]);
                     }
                 }
             }
         }
+        if (tc) {
+            // zero K padding of the tile's rows (rows past tm only feed outputs that are dropped)
+            const int kz = Kp - Kin;
+            for (int idx = tid; idx < tm * kz; idx += nt) xput(idx / kz, Kin + idx % kz, 0.f);
+            umma::fence_async_smem();
+        }
         __syncthreads();
-        if (m.mma) {
+        if (tc) {
+            // 3'') tcgen05: one thread issues the tile's MMAs into tensor memory; every warp then reads its lane
+            // quarter (rows 32 (warp % 4) ..) and half of the columns, adds the bias, activates and stages the rows
+            // in Y (over the A operand) for the sink's CUDA-core mapping
+            if (tid == 0) umma::issue_tile(tc->tmem, A0, A1, tc->W, tc->W + (size_t)Kp * D * 2, D, Kp, m.tc_split ? 3 : 1, tc->mbar);
+            if (!umma::mbar_wait(tc->mbar, tc->phase) && (tid & 31) == 0) atomicOr(jb.err, 32);
+            tc->phase ^= 1u;
+            umma::fence_after();
+            const int warp = tid >> 5, q = warp & 3, hh = warp >> 2;
+            const int cw = D / 2 >= 16 ? D / 2 : 16;
+            const int YS = D + 4;
+            float *Y = X;
+            const int rrow = q * 32 + (tid & 31);
+            for (int c0 = hh * cw; c0 < min(D, (hh + 1) * cw); c0 += 16) {
+                float v[16];
+                umma::tmem_ld16(tc->tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+                for (int i = 0; i < 16; i += 4) {
+                    float4 o;
+                    o.x = act_fn(m.act, v[i] + LW.b[c0 + i]); o.y = act_fn(m.act, v[i + 1] + LW.b[c0 + i + 1]);
+                    o.z = act_fn(m.act, v[i + 2] + LW.b[c0 + i + 2]); o.w = act_fn(m.act, v[i + 3] + LW.b[c0 + i + 3]);
+                    *reinterpret_cast<float4 *>(Y + (size_t)rrow * YS + c0 + i) = o;
+                }
+            }
+            umma::fence_before();
+            __syncthreads();
+            for (int i = 0; i < MS; ++i) {
+                const int mm = sg + i * SG;
+                const float4 y = *reinterpret_cast<const float4 *>(Y + (size_t)mm * YS + cg * 4);
+                float v[4] = {y.x, y.y, y.z, y.w};
+                sink(mm < tm ? t0 + mm : -1, cg * 4, v);
+            }
+            __syncthreads();
+            continue;
+        }
+        if (m.mma == 1 || m.mma == 3) {
             // 3') tensor cores: the tile's [TM x Kin] x [Kin x D] on mma.sync bf16 (split operands when m.mma == 3);
             // warps tile the output in 16 x 8 blocks (mt x nt = 4 per warp), then bias + activation go through a
             // [TM x (D + 4)] staging tile (over X) to the sink in the CUDA-core mapping
@@ -435,7 +550,7 @@ __device__ __forceinline__ void csync() {
 template <bool CLUSTER>
 __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &ctl, unsigned long long *dh, float *X,
                          int32_t *src, const LayerW *LWs, const float *lin, const float *hw, int32_t *ent_site, int32_t *ent_pos,
-                         int8_t *ent_sig, double &E, int64_t &nacc, const NceCtx &cx) {
+                         int8_t *ent_sig, double &E, int64_t &nacc, const NceCtx &cx, TcCtx *tc) {
     const bool leader = cx.rank == 0;
     const int CL = cx.CL, rank = cx.rank;
     const NceDev &m = jb.m;
@@ -515,7 +630,8 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         }
     }
     // 3. layer-0 change (fixed point)
-    for (int idx = tid; idx < n0 * m.C0; idx += nt) dh[idx] = 0ull;
+    if (m.l0bin) { for (int idx = tid; idx < n0 * m.C0; idx += nt) reinterpret_cast<int32_t *>(dh)[idx] = 0; }
+    else { for (int idx = tid; idx < n0 * m.C0; idx += nt) dh[idx] = 0ull; }
     __syncthreads();
     const int Jt = 2 * m.J;
     if (m.l0bin) {
@@ -667,7 +783,7 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
             layer_tiles(jb, lvl, LWs[lvl], cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
                         [&](int64_t pos, int c0, const float *v) {
                             if (pos >= 0) *reinterpret_cast<float4 *>(outb + (size_t)pos * D + c0) = make_float4(v[0], v[1], v[2], v[3]);
-                        }, rank, CL);
+                        }, rank, CL, tc);
             csync<CLUSTER>();
         } else {
             layer_tiles(jb, lvl, LWs[lvl], cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
@@ -686,7 +802,7 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
                                 en[pos] = ev;
                                 atomicAdd(&ctl.dacc, (unsigned long long)llrint(((double)ev - (double)e[st]) * kFix));
                             }
-                        }, rank, CL);
+                        }, rank, CL, tc);
         }
     }
     if (L == 0) {
@@ -777,17 +893,27 @@ __host__ __device__ inline size_t weight_floats(int depth, int P, int C0, int D,
     return o;
 }
 
-// shared-memory plan of the step kernel (byte offsets, 16-byte aligned): dh | X tile | partner codes | weights
+// shared-memory plan of the step kernel (byte offsets, 16-byte aligned): dh | X tile | partner codes | tcgen05 B
+// operand | ball-0 entries | weights.  with_dh = false: the tile part alone (full-cache kernel).  On the tcgen05
+// path the X tile holds the bf16 A operand(s) [128][Kp] or the float32 output rows [128][D + 4], whichever is larger.
 struct SmemPlan {
-    size_t dh, X, src, ent, w, dh_bytes, tile_end, total_w;
-    __host__ __device__ static SmemPlan make(const NceDev &m) {
+    size_t dh, X, src, wt, ent, w, dh_bytes, tile_end, total_w;
+    __host__ __device__ static SmemPlan make(const NceDev &m, bool with_dh = true) {
         auto al = [](size_t x) { return (x + 15) / 16 * 16; };
+        auto al128 = [](size_t x) { return (x + 127) / 128 * 128; };
         SmemPlan p;
-        const int TM = tile_tm(m.D), Kmax = tile_kin(m.P, m.C0, m.D);
-        p.dh = 0; p.dh_bytes = al(sizeof(unsigned long long) * (size_t)m.n0max * m.C0);
-        p.X = p.dh_bytes;
-        p.src = al(p.X + sizeof(float) * (size_t)TM * (Kmax + 1));
-        p.tile_end = al(p.src + sizeof(int32_t) * (size_t)TM * (1 + m.P * m.W));
+        const int TM = tile_tm(m.D, m.tc), Kmax = tile_kin(m.P, m.C0, m.D);
+        // layer-0 change per (site, channel): int32 counts for +-1 point functions, int64 fixed point otherwise
+        p.dh = 0; p.dh_bytes = with_dh ? al((m.l0bin ? sizeof(int32_t) : sizeof(unsigned long long)) * (size_t)m.n0max * m.C0) : 0;
+        p.X = al128(p.dh_bytes);
+        size_t xb = sizeof(float) * (size_t)TM * (Kmax + 1);
+        if (m.tc) {
+            const size_t ab = (size_t)128 * kpad16(Kmax) * 2 * (m.tc_split ? 2 : 1), yb = sizeof(float) * 128 * (size_t)(m.D + 4);
+            xb = ab > yb ? ab : yb;
+        }
+        p.src = al(p.X + xb);
+        p.wt = al128(p.src + sizeof(int32_t) * (size_t)TM * (1 + m.P * m.W));
+        p.tile_end = p.wt + (m.tc ? (size_t)kpad16(Kmax) * m.D * 2 * (m.tc_split ? 2 : 1) : 0);
         p.ent = p.tile_end;
         p.w = al(p.ent + (sizeof(int32_t) * 2 + 1) * 2 * (size_t)m.w0max);
         p.total_w = al(p.w + sizeof(float) * weight_floats(m.depth, m.P, m.C0, m.D, m.gate));
@@ -811,17 +937,22 @@ __global__ void __launch_bounds__(256, 1) nce_chunk_kernel(const __grid_constant
     int8_t *ent_sig = reinterpret_cast<int8_t *>(ent_pos + 2 * m.w0max);
     LayerW lw[kMaxLayers]; const float *lin, *hw;
     stage_weights(m, w_smem != 0, wbuf, lw, lin, hw);
+    __shared__ __align__(8) uint64_t tc_mbar;
+    __shared__ uint32_t tc_slot;
+    TcCtx tcx;
+    if (m.tc) tc_begin(m.D, tcx, smem + sp.wt, &tc_mbar, &tc_slot);
     const int t = jb.slot_of_rep[r];
     double E = jb.E[r];
     int64_t nacc = 0;
     NceCtx cx; cx.rank = 0; cx.CL = 1; cx.lctl = &ctl;
     for (int64_t s = 0; s < jb.n_steps; ++s) {
-        nce_step<false>(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, ent_site, ent_pos, ent_sig, E, nacc, cx);
+        nce_step<false>(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, ent_site, ent_pos, ent_sig, E, nacc, cx, m.tc ? &tcx : nullptr);
         if (threadIdx.x == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
             jb.E_samples[((s + 1) / jb.sample_interval - 1) * jb.R + t] = E;
         __syncthreads();
     }
     if (threadIdx.x == 0) { jb.E[r] = E; jb.n_acc[r] += nacc; }
+    if (m.tc) tc_end(m.D, tcx);
 }
 
 // the same chunk with each replica spread over a thread-block cluster of gridDim.x / R CTAs
@@ -843,18 +974,23 @@ __global__ void __launch_bounds__(256, 1) nce_chunk_cluster_kernel(const __grid_
     int8_t *ent_sig = reinterpret_cast<int8_t *>(ent_pos + 2 * m.w0max);
     LayerW lw[kMaxLayers]; const float *lin, *hw;
     stage_weights(m, w_smem != 0, wbuf, lw, lin, hw);
+    __shared__ __align__(8) uint64_t tc_mbar;
+    __shared__ uint32_t tc_slot;
+    TcCtx tcx;
+    if (m.tc) tc_begin(m.D, tcx, smem + sp.wt, &tc_mbar, &tc_slot);
     NceCtx cx; cx.rank = rank; cx.CL = CL; cx.lctl = cluster.map_shared_rank(&ctl, 0);
     cluster.sync();
     const int t = jb.slot_of_rep[r];
     double E = jb.E[r];
     int64_t nacc = 0;
     for (int64_t s = 0; s < jb.n_steps; ++s) {
-        nce_step<true>(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, ent_site, ent_pos, ent_sig, E, nacc, cx);
+        nce_step<true>(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, ent_site, ent_pos, ent_sig, E, nacc, cx, m.tc ? &tcx : nullptr);
         if (rank == 0 && threadIdx.x == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
             jb.E_samples[((s + 1) / jb.sample_interval - 1) * jb.R + t] = E;
     }
     if (rank == 0 && threadIdx.x == 0) { jb.E[r] = E; jb.n_acc[r] += nacc; }
     cluster.sync();                                   // no CTA leaves while others may still read its shared memory
+    if (m.tc) tc_end(m.D, tcx);
 }
 
 // ── full cache ─────────────────────────────────────────────────────────────────────────────────────
@@ -1000,27 +1136,33 @@ __global__ void __launch_bounds__(256, 1) nce_layer_all_kernel(NceJob jb, int lv
                                                              float *e_out, int64_t chunk0, int64_t chunk_n) {
     extern __shared__ __align__(16) unsigned char smem[];
     const NceDev &m = jb.m;
-    const int TM = tile_tm(m.D);
-    const SmemPlan sp = SmemPlan::make(m);
-    float *X = reinterpret_cast<float *>(smem + sp.X - sp.dh_bytes);
-    int32_t *src = reinterpret_cast<int32_t *>(smem + sp.src - sp.dh_bytes);
+    const int TM = tile_tm(m.D, m.tc);
+    const SmemPlan sp = SmemPlan::make(m, false);
+    float *X = reinterpret_cast<float *>(smem + sp.X);
+    int32_t *src = reinterpret_cast<int32_t *>(smem + sp.src);
     const int64_t per = ((chunk_n + gridDim.x - 1) / gridDim.x + TM - 1) / TM * TM;
     const int64_t a = chunk0 + (int64_t)blockIdx.x * per, cnt = max((int64_t)0, min(per, chunk0 + chunk_n - a));
     if (cnt <= 0) return;
+    __shared__ __align__(8) uint64_t tc_mbar;
+    __shared__ uint32_t tc_slot;
+    TcCtx tcx;
+    if (m.tc) tc_begin(m.D, tcx, smem + sp.wt, &tc_mbar, &tc_slot);
+    TcCtx *tcp = m.tc ? &tcx : nullptr;
     const float *h0 = jb.h0 + (size_t)r * m.N * m.C0;
     const int D = m.D, ncg = D / 4;
     LayerW LW; LW.W = m.Wc[lvl]; LW.b = m.bias[lvl]; LW.G = m.gate ? m.G[lvl] : nullptr; LW.gb = m.gate ? m.gb[lvl] : nullptr;
     if (out) {
         layer_tiles(jb, lvl, LW, in, nullptr, nullptr, 0, nullptr, 0, cnt, &a, X, src, [&](int64_t pos, int c0, const float *v) {
             if (pos >= 0) *reinterpret_cast<float4 *>(out + (size_t)(a + pos) * D + c0) = make_float4(v[0], v[1], v[2], v[3]);
-        });
+        }, 0, 1, tcp);
     } else {
         layer_tiles(jb, lvl, LW, in, nullptr, nullptr, 0, nullptr, 0, cnt, &a, X, src, [&](int64_t pos, int c0, const float *v) {
             const int64_t st = a + pos;
             const float tot = site_energy(v, c0, m.head_w, pos >= 0 ? h0 + (size_t)st * m.C0 : nullptr, m.lin, m.C0, ncg);
             if (pos >= 0 && c0 == 0) e_out[st] = (m.Mb[st % m.nB] > 1) ? tot : 0.f;
-        });
+        }, 0, 1, tcp);
     }
+    if (m.tc) tc_end(m.D, tcx);
 }
 
 __global__ void nce_e0_kernel(NceDev m, const float *h0, int64_t n, float *e) {
@@ -1076,9 +1218,11 @@ static int dup(nce_nce_model *h, const T *src, size_t n, const T *&dst) {
     return NCE_OK;
 }
 
+// dynamic shared memory of the step kernels: 227 KB per CTA less the kernels' static shared memory
+constexpr size_t kStepSmemMax = 232448 - 1024;
+
 static size_t tile_smem(const NceDev &m) {
-    const SmemPlan p = SmemPlan::make(m);
-    return p.tile_end - p.dh_bytes;
+    return SmemPlan::make(m, false).tile_end;
 }
 
 static size_t step_smem(const NceDev &m, bool w_smem) {
@@ -1126,7 +1270,7 @@ int nce_model_dims(nce_nce_handle h, int64_t *N, int32_t *C0, int32_t *D, int32_
 // thread issues the MMAs into tensor memory, every warp reads its 32-lane quarter back.
 __global__ void __launch_bounds__(128) nce_tc_gemm_kernel(const float *A, const float *B, float *C, int32_t N, int32_t K,
                                                           int32_t Kp, int32_t split, int32_t *err) {
-    extern __shared__ __align__(128) unsigned char smem[];
+    extern __shared__ __align__(16) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -1205,7 +1349,7 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
               "nce_nce_create: bad lattice");
     NCE_CHECK(d->act == 0 || d->act == 1, "nce_nce_create: act must be 0 (tanh) or 1 (silu)");
     NCE_CHECK(d->norm > 0.0, "nce_nce_create: norm must be > 0");
-    NCE_CHECK(d->mma == 0 || d->mma == 1 || d->mma == 3, "nce_nce_create: mma must be 0, 1 or 3");
+    NCE_CHECK(d->mma >= 0 && d->mma <= 4, "nce_nce_create: mma must be 0, 1, 2, 3 or 4");
     NCE_CHECK(d->mma == 0 || !d->gate, "nce_nce_create: the tensor-core forms need an ungated model");
     const int64_t N = d->n_cells * d->nB;
     NCE_CHECK(N < (1ll << 31) - 1, "nce_nce_create: more than 2^31 sites");
@@ -1252,6 +1396,8 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
     m.maxM = d->maxM; m.maxP = d->maxP; m.d0 = (int32_t)d->d[0]; m.d1 = (int32_t)d->d[1]; m.d2 = (int32_t)d->d[2];
     m.N = N; m.n_cells = d->n_cells; m.wL = d->wL; m.act = d->act; m.gate = d->gate; m.norm = d->norm; m.scale_eV = d->scale_eV;
     m.mma = d->mma;
+    m.tc = (d->mma == 2 || d->mma == 4) && d->depth > 0 ? 1 : 0;
+    m.tc_split = d->mma == 4 ? 1 : 0;
     m.head_b = (float)d->head_b;
     m.n0max = 2 * n0max; m.nmax = 2 * nLmax; m.w0max = n0max;
     NCE_CHECK(d->Rv_loc, "nce_nce_create: Rv_loc required");
@@ -1351,13 +1497,33 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
         chk(dup(h, d->W_cat[l], (size_t)(1 + d->P) * Cin * d->D, m.Wc[l]));
         chk(dup(h, d->bias[l], (size_t)d->D, m.bias[l]));
         if (d->gate) { chk(dup(h, d->G_cat[l], (size_t)d->P * Cin * d->D, m.G[l])); chk(dup(h, d->gate_b[l], (size_t)d->D, m.gb[l])); }
+        if (m.tc) {
+            // B operand of the tcgen05 tiles: B[n][k] = W[k][n] in bf16 core-matrix layout, hi then lo (split)
+            const int Kin = (1 + d->P) * Cin, Kp = kpad16(Kin);
+            const size_t half = (size_t)Kp * d->D * 2;
+            std::vector<uint8_t> wt(half * (m.tc_split ? 2 : 1), 0);
+            for (int n = 0; n < d->D; ++n)
+                for (int k = 0; k < Kin; ++k) {
+                    const float v = d->W_cat[l][(size_t)k * d->D + n];
+                    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+                    const uint32_t off = umma::core_off(n, k, Kp);
+                    std::memcpy(&wt[off], &hi, 2);
+                    if (m.tc_split) {
+                        const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+                        std::memcpy(&wt[half + off], &lo, 2);
+                    }
+                }
+            chk(dup(h, wt.data(), wt.size(), m.Wt[l]));
+        }
     }
     if (!rc) {
         cudaError_t e = cudaMalloc((void **)&h->err, sizeof(int32_t));
         if (e == cudaSuccess) e = cudaMemset(h->err, 0, sizeof(int32_t));
         if (e != cudaSuccess) rc = fail(NCE_ERR_CUDA, "nce_nce_create: %s", cudaGetErrorString(e));
     }
-    if (!rc && step_smem(m, false) > 220 * 1024) rc = fail(NCE_ERR_UNSUPPORTED, "nce_nce_create: receptive field too large for shared memory");
+    if (!rc && step_smem(m, false) > kStepSmemMax)
+        rc = fail(NCE_ERR_UNSUPPORTED, "nce_nce_create: receptive field%s too large for shared memory (%zu bytes)",
+                  m.tc ? " and tensor-core tiles" : "", step_smem(m, false));
     if (rc) {
         for (void *p : h->allocs) cudaFree(p);
         delete h;
@@ -1406,7 +1572,7 @@ int nce_nce_full_cache(nce_nce_handle h, const nce_nce_state *st, void *stream) 
     NceJob jb = make_nce_job(h, st);
     const size_t xs = tile_smem(m);
     NCE_CUDA(cudaFuncSetAttribute(nce_layer_all_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
-    const int blocks = (int)std::min<int64_t>((m.N + tile_tm(m.D) - 1) / tile_tm(m.D), 1216);
+    const int blocks = (int)std::min<int64_t>((m.N + tile_tm(m.D, m.tc) - 1) / tile_tm(m.D, m.tc), 1216);
     if (m.depth == 0) {
         nce_e0_kernel<<<(int)std::min<int64_t>((tot + 255) / 256, 65535), 256, 0, s>>>(m, st->h0, tot, st->e);
         NCE_CUDA(cudaGetLastError());
@@ -1455,7 +1621,7 @@ int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_c
     jb.seed = ck->seed; jb.sample_interval = ck->sample_interval > 0 ? ck->sample_interval : 1; jb.E_samples = ck->E_samples;
     jb.dE_out = ck->dE_out; jb.force = ck->force;
     if (ck->n_steps == 0) return NCE_OK;
-    const bool w_smem = step_smem(h->dev, true) <= 220 * 1024;
+    const bool w_smem = step_smem(h->dev, true) <= kStepSmemMax;
     const size_t sm = step_smem(h->dev, w_smem);
     const int CL = ck->cluster > 1 ? ck->cluster : 1;
     NCE_CHECK(CL == 1 || CL == 2 || CL == 4 || CL == 8, "nce_nce_run_chunk: cluster must be 1, 2, 4 or 8");

@@ -75,7 +75,8 @@ class NCEModel:
     def __init__(self, cs, structure, params, mu=None, sd=None, shell_edges=(0.0, 3.3), act="tanh", pool="mean",
                  ys=1.0, ym=0.0, mma=0):
         depth = len(params["layers"])
-        self.mma = int(mma)          # 0 float32 CUDA cores, 1 bf16 tensor cores, 3 split-bf16 tensor cores
+        # 0 float32 CUDA cores; bf16 / split-bf16 tensor cores: 1 / 3 mma.sync, 2 / 4 tcgen05 (tensor memory)
+        self.mma = int(mma)
         self.cs, self.params, self.act, self.pool = cs, params, act, pool
         self.geo = geo = build_geometry(cs, structure, list(shell_edges), depth)
         K1 = geo["K"] + 1

@@ -129,8 +129,8 @@ class ServeModels:
     """Per-cell models of the serving workload, built once and shared by every job on that cell (a job's model
     must stay valid while it runs; jobs on one CE model share the CE worker's stream)."""
 
-    def __init__(self, depth=3, width=64, eci_seed=0, model_seed=0):
-        self.depth, self.width, self.eci_seed, self.model_seed = depth, width, eci_seed, model_seed
+    def __init__(self, depth=3, width=64, eci_seed=0, model_seed=0, mma=0):
+        self.depth, self.width, self.eci_seed, self.model_seed, self.mma = depth, width, eci_seed, model_seed, mma
         self._ce, self._nce = {}, {}
 
     def ce(self, L):
@@ -148,5 +148,5 @@ class ServeModels:
             s = fcc_conventional(A_FCC, (L, L, L))
             s.numbers = np.full(len(s), Z_OF["Ni"], np.int64)
             P = synthetic_model(len(cs.orbits) + 1, self.depth, self.width, 1, self.model_seed)
-            self._nce[L] = NCEModel(cs, s, P, shell_edges=(0.0, 3.3), act="silu", pool="sum")
+            self._nce[L] = NCEModel(cs, s, P, shell_edges=(0.0, 3.3), act="silu", pool="sum", mma=self.mma)
         return self._nce[L]

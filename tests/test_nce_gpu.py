@@ -155,17 +155,18 @@ def _model_bench_mma(L, seed, mma, width=64):
     return m, NCEOracle(m.geo, P, act="silu", pool="sum")
 
 
-@pytest.mark.parametrize("mma,width", [(3, 64), (3, 128), (1, 64), (3, 32)])
+@pytest.mark.parametrize("mma,width", [(3, 64), (3, 128), (1, 64), (3, 32), (4, 64), (4, 32), (2, 64), (2, 128),
+                                       (2, 16)])
 def test_tensor_core_forms_vs_oracle(cuda, mma, width):
-    """Layer contractions on tensor cores: split bf16 (mma 3) stays within the float32 bounds of the oracle
-    (energies 1e-4 eV, per-step dE 1e-4 eV); plain bf16 operands (mma 1) within its stated bound (per-step dE
-    5e-2 eV on this model, whose total energy is ~1e2 eV); a chain of forced moves keeps the carried energy equal
-    to a rebuild of the caches in the same form."""
+    """Layer contractions on tensor cores (mma.sync: 1, 3; tcgen05 with tensor-memory accumulators: 2, 4): split
+    bf16 (3, 4) stays within the float32 bounds of the oracle (energies 1e-4 eV, per-step dE 1e-4 eV); plain bf16
+    operands (1, 2) within its stated bound (per-step dE 5e-2 eV on this model, whose total energy is ~1e2 eV); a
+    chain of forced moves keeps the carried energy equal to a rebuild of the caches in the same form."""
     torch = cuda
     from neuralce_gb300.nce import NCEState
     from oracle.nce_oracle import run_chain
     m, orc = _model_bench_mma(3, 4, mma, width)
-    tol_E, tol_dE = (1e-4 * max(1.0, m.N / 64), 1e-4) if mma == 3 else (5e-1, 5e-2)
+    tol_E, tol_dE = (1e-4 * max(1.0, m.N / 64), 1e-4) if mma in (3, 4) else (5e-1, 5e-2)
     rng = np.random.default_rng(3)
     sig = np.stack([m.sig0[rng.permutation(m.N)] for _ in range(2)]).astype(np.int8)
     st = NCEState(m, sig, np.ones(2)).full_cache()
@@ -192,11 +193,12 @@ def test_tensor_core_forms_vs_oracle(cuda, mma, width):
     assert abs(Ecar - float(st2.E[0].item())) * m.scale_eV < 1e-4 * max(1.0, m.N / 64)
 
 
-def test_tensor_core_cluster_equals_single_cta(cuda):
+@pytest.mark.parametrize("mma", [3, 4, 2])
+def test_tensor_core_cluster_equals_single_cta(cuda, mma):
     torch = cuda
     from neuralce_gb300.nce import NCEState
     from neuralce_gb300.workloads import ladder, replica_configs
-    m, _ = _model_bench_mma(3, 6, 3)
+    m, _ = _model_bench_mma(3, 6, mma)
     _, beta = ladder(4)
     sig = replica_configs(m.sig0, 4, 3)
     a = NCEState(m, sig, beta).full_cache(); b = NCEState(m, sig, beta).full_cache()
@@ -227,3 +229,11 @@ def test_tc_gemm_matches_fp32(cuda, K, N):
     # the plain bf16 form is much further from the float32 product than the split form
     err1 = ((C.double() - ref64).abs() / (scale + 1e-30)).max().item()
     assert err1 > 4 * err
+
+
+def test_tcgen05_split_too_wide_is_refused(cuda):
+    """Split operands at width 128 need more shared memory than a CTA has: creation fails with a message."""
+    from neuralce_gb300 import _lib
+    m, _ = _model_bench_mma(3, 4, 4, 128)
+    with pytest.raises(_lib.NceError, match="shared memory"):
+        m.handle
