@@ -1129,9 +1129,7 @@ struct nce_ce_model {
     uint32_t *brows = nullptr; int4 *bmem = nullptr; int32_t *brow_off = nullptr, *brow_n = nullptr;
     int32_t *plane_pfc = nullptr; int32_t n_planes = 0;
     double *ecol1 = nullptr;                 // eci of each column (full-energy kernel)
-    uint32_t *planes = nullptr; size_t planes_n = 0;        // scratch: bit planes of the configurations
-    int64_t *cv_scratch = nullptr; size_t cv_scratch_n = 0;  // scratch: cluster-vector sums for the energy
-    double *energy_partial = nullptr; size_t energy_partial_n = 0;
+
     int device = 0;
     std::mutex mu;
     // staging for the host-buffer entry point
@@ -1150,8 +1148,8 @@ static int upload(T *&dst, const T *src, size_t n) {
 
 static int free_model(nce_ce_model *m) {
     void *ptrs[] = {m->loc, m->pfc, m->eci64, m->eci32, m->rv_len, m->nb_b, m->nb_uo, m->pf64, m->pf32, m->act_b,
-                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->bix, m->rcol, m->ecol2_64, m->ecol2_32, m->ecol_fix, m->chunks, m->n_chunks, m->brows, m->bmem, m->brow_off, m->brow_n, m->plane_pfc, m->ecol1, m->planes, m->cv_scratch,
-                    m->energy_partial, m->staging_base};
+                    m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->bix, m->rcol, m->ecol2_64, m->ecol2_32, m->ecol_fix, m->chunks, m->n_chunks, m->brows, m->bmem, m->brow_off, m->brow_n, m->plane_pfc, m->ecol1,
+                    m->staging_base};
     for (void *p : ptrs) if (p) cudaFree(p);
     delete m;
     return NCE_OK;
@@ -1199,7 +1197,7 @@ static CEJob make_job(const nce_ce_model *m, const nce_pt_state *st, const nce_p
 template <typename Real, int MO>
 static int launch_chunk_mo(const CEBatch &bt, int total, int warps, size_t smem, cudaStream_t s) {
     auto kern = ce_pt_chunk_kernel<Real, MO>;
-    NCE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NCE_CUDA(::nce::raise_smem_limit((const void *)kern, smem));
     kern<<<total, warps * 32, smem, s>>>(bt);
     NCE_CUDA(cudaGetLastError());
     return NCE_OK;
@@ -1207,7 +1205,7 @@ static int launch_chunk_mo(const CEBatch &bt, int total, int warps, size_t smem,
 
 static int launch_bin_kernel(void (*kern)(CEBatch, int32_t), const CEBatch &bt, int total, int warps, size_t smem, int sig_smem,
                              cudaStream_t s, int CL) {
-    NCE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NCE_CUDA(::nce::raise_smem_limit((const void *)kern, smem));
     if (CL <= 1) {
         kern<<<total, warps * 32, smem, s>>>(bt, sig_smem);
     } else {
@@ -1236,11 +1234,11 @@ static int launch_bin_mo(const CEBatch &bt, int total, int warps, size_t smem, i
     }
     if (CL <= 1) {
         auto kern = ce_bin_chunk_kernel<Acc, MO, false>;
-        NCE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        NCE_CUDA(::nce::raise_smem_limit((const void *)kern, smem));
         kern<<<total, warps * 32, smem, s>>>(bt, sig_smem);
     } else {
         auto kern = ce_bin_chunk_kernel<Acc, MO, true>;
-        NCE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        NCE_CUDA(::nce::raise_smem_limit((const void *)kern, smem));
         cudaLaunchConfig_t cfg; std::memset(&cfg, 0, sizeof(cfg));
         cfg.gridDim = dim3((unsigned)(total * CL)); cfg.blockDim = dim3(warps * 32); cfg.dynamicSmemBytes = smem; cfg.stream = s;
         cudaLaunchAttribute attr[1];
@@ -1414,7 +1412,7 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
     if (any) {
         const size_t xs = sizeof(int32_t) * 2 * (size_t)max_R;
         NCE_CHECK(xs <= 200 * 1024, "batch: %d replicas per job exceed the exchange kernel's shared memory", max_R);
-        NCE_CUDA(cudaFuncSetAttribute(ce_exchange_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
+        NCE_CUDA(::nce::raise_smem_limit((const void *)ce_exchange_kernel, xs));
         ce_exchange_kernel<<<n_jobs, 32, xs, s>>>(ex);
         NCE_CUDA(cudaGetLastError());
     }
@@ -1434,7 +1432,7 @@ int launch_exchange(int32_t R, double *E, double E_scale, const float *beta_slot
     x.do_exchange = 1; x.E_scale = E_scale; x.rounds = rounds;
     const size_t xs = sizeof(int32_t) * 2 * (size_t)R;
     NCE_CHECK(xs <= 200 * 1024, "exchange: %d replicas exceed the exchange kernel's shared memory", R);
-    NCE_CUDA(cudaFuncSetAttribute(ce_exchange_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
+    NCE_CUDA(::nce::raise_smem_limit((const void *)ce_exchange_kernel, xs));
     ce_exchange_kernel<<<1, 32, xs, s>>>(ex);
     NCE_CUDA(cudaGetLastError());
     return NCE_OK;
@@ -1445,7 +1443,7 @@ static int launch_delta_mo(const CEJob &jb, int n, const int32_t *rep, const int
                            const int8_t *sa, const int8_t *sb, double *out, int warps, cudaStream_t s) {
     const size_t smem = Layout<Real>::make(jb.nB, jb.J, MO, jb.n_nbr, jb.n_pfc, warps, false).total;
     auto kern = ce_delta_kernel<Real, MO>;
-    NCE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NCE_CUDA(::nce::raise_smem_limit((const void *)kern, smem));
     kern<<<n, warps * 32, smem, s>>>(jb, n, rep, ia, ib, sa, sb, out);
     NCE_CUDA(cudaGetLastError());
     return NCE_OK;
@@ -1710,29 +1708,19 @@ static int energy_impl(nce_ce_model *h, const int8_t *sigma, int32_t R, int32_t 
         NCE_CHECK(d2 < (1 << 28) && d0 * d1 < (1ll << 40), "energy: lattice too large");
         const int32_t W2 = (int32_t)((2 * d2 + 31) / 32 + 1);
         const int32_t P = h->n_planes * h->nB;
-        const size_t need_p = (size_t)R * P * d0 * d1 * W2;
-        if (need_p > h->planes_n) {
-            if (h->planes) { cudaStreamSynchronize(s); cudaFree(h->planes); }
-            h->planes = nullptr; h->planes_n = 0;
-            NCE_CUDA(cudaMalloc((void **)&h->planes, sizeof(uint32_t) * need_p));
-            h->planes_n = need_p;
-        }
+        StreamScratch planes, cvs;
+        NCE_CUDA(planes.alloc(sizeof(uint32_t) * (size_t)R * P * d0 * d1 * W2, s));
         int64_t *cv = cv_out;
         if (!cv) {
             const size_t need_c = (size_t)R * h->n_cols;
-            if (need_c > h->cv_scratch_n) {
-                if (h->cv_scratch) { cudaStreamSynchronize(s); cudaFree(h->cv_scratch); }
-                h->cv_scratch = nullptr; h->cv_scratch_n = 0;
-                NCE_CUDA(cudaMalloc((void **)&h->cv_scratch, sizeof(int64_t) * need_c));
-                h->cv_scratch_n = need_c;
-            }
-            cv = h->cv_scratch;
+            NCE_CUDA(cvs.alloc(sizeof(int64_t) * need_c, s));
+            cv = (int64_t *)cvs.p;
             NCE_CUDA(cudaMemsetAsync(cv, 0, sizeof(int64_t) * need_c, s));
         }
         const int64_t prow = (int64_t)R * P * d0 * d1;
         const int pb = (int)std::min<int64_t>((prow + 7) / 8, 1 << 20);
         ce_bitplane_kernel<<<pb, 256, 0, s>>>(sigma, R, h->N, h->nB, d0 * d1, (int32_t)d2, W2, h->plane_pfc, h->n_planes, h->sbits,
-                                              h->planes);
+                                              (uint32_t *)planes.p);
         NCE_CUDA(cudaGetLastError());
         const int64_t items = d0 * d1 * ((d2 + 31) / 32);
         const int64_t ib = std::min<int64_t>((items + 255) / 256, 8192);
@@ -1742,7 +1730,7 @@ static int energy_impl(nce_ce_model *h, const int8_t *sigma, int32_t R, int32_t 
         const int64_t have = ib * h->nB * R;
         const int slices = (int)std::max<int64_t>(1, std::min<int64_t>(32, (4ll * nsm + have - 1) / have));
         ce_energy_bits_kernel<<<dim3((unsigned)(ib * slices), h->nB, R), 256, sizeof(unsigned long long) * h->n_cols, s>>>(
-            h->planes, P, (int32_t)d0, (int32_t)d1, (int32_t)d2, W2, h->brows, h->bmem, h->brow_off, h->brow_n, h->n_cols, slices,
+            (const uint32_t *)planes.p, P, (int32_t)d0, (int32_t)d1, (int32_t)d2, W2, h->brows, h->bmem, h->brow_off, h->brow_n, h->n_cols, slices,
             (unsigned long long *)cv);
         NCE_CUDA(cudaGetLastError());
         if (E) {
@@ -1755,24 +1743,20 @@ static int energy_impl(nce_ce_model *h, const int8_t *sigma, int32_t R, int32_t 
     const int threads = 256;
     int nblk = (int)std::min<int64_t>((h->n_cells + threads - 1) / threads, 1184);
     nblk = std::max(nblk, 1);
-    const size_t need = (size_t)nblk * R;
-    if (need > h->energy_partial_n) {
-        if (h->energy_partial) { cudaStreamSynchronize(s); cudaFree(h->energy_partial); }
-        h->energy_partial = nullptr; h->energy_partial_n = 0;
-        NCE_CUDA(cudaMalloc((void **)&h->energy_partial, sizeof(double) * need));
-        h->energy_partial_n = need;
-    }
+    StreamScratch partial;
+    NCE_CUDA(partial.alloc(sizeof(double) * (size_t)nblk * R, s));
+    double *energy_partial = (double *)partial.p;
     dim3 grid(nblk, R);
     if (precision == 64)
         ce_energy_kernel<double><<<grid, threads, 0, s>>>(sigma, h->N, h->n_cells, h->nB, (int)h->d[0], (int)h->d[1], (int)h->d[2],
                                                           h->Rt, h->mo, h->T_b, h->T_uo, h->T_pfc, h->T_eci64, h->pf64, h->max_sp,
-                                                          h->energy_partial);
+                                                          energy_partial);
     else
         ce_energy_kernel<float><<<grid, threads, 0, s>>>(sigma, h->N, h->n_cells, h->nB, (int)h->d[0], (int)h->d[1], (int)h->d[2],
                                                          h->Rt, h->mo, h->T_b, h->T_uo, h->T_pfc, h->T_eci32, h->pf32, h->max_sp,
-                                                         h->energy_partial);
+                                                         energy_partial);
     NCE_CUDA(cudaGetLastError());
-    ce_energy_finish<<<(R + 127) / 128, 128, 0, s>>>(h->energy_partial, nblk, R, h->zerolet, E);
+    ce_energy_finish<<<(R + 127) / 128, 128, 0, s>>>(energy_partial, nblk, R, h->zerolet, E);
     NCE_CUDA(cudaGetLastError());
     return NCE_OK;
 }

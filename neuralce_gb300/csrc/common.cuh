@@ -14,6 +14,19 @@ namespace nce {
 std::string &last_error();
 int fail(int code, const char *fmt, ...);
 
+// Raise (never lower) a kernel's dynamic shared-memory limit on the current device, under a process-wide lock.
+// The attribute belongs to the function, not to the launch, so host threads that launch one kernel with different
+// sizes (the job server's CE and NeuralCE threads share the exchange kernel) must not undo each other's setting.
+cudaError_t raise_smem_limit(const void *func, size_t bytes);
+
+// Scratch of one call, allocated and released in the order of its stream: calls on one model handle may run on
+// several streams at once (a job's admission and another job's re-anchor), so no per-handle scratch is shared.
+struct StreamScratch {
+    void *p = nullptr; cudaStream_t s = nullptr;
+    cudaError_t alloc(size_t bytes, cudaStream_t st) { s = st; return cudaMallocAsync(&p, bytes, st); }
+    ~StreamScratch() { if (p) cudaFreeAsync(p, s); }
+};
+
 // shapes of a model handle, for the job server's memory accounting
 int ce_model_dims(nce_ce_handle h, int64_t *N, int32_t *n_cols, int32_t *mo, int32_t *binary);
 int nce_model_dims(nce_nce_handle h, int64_t *N, int32_t *C0, int32_t *D, int32_t *depth);

@@ -1200,9 +1200,8 @@ struct nce_nce_model {
     int32_t *err = nullptr;
     // scratch for R replicas
     int32_t *slot = nullptr, *list = nullptr; float *newbuf = nullptr, *e_new = nullptr; int64_t stride = 0; int32_t R_alloc = 0;
-    unsigned long long *eacc = nullptr; int32_t eacc_n = 0;
-    uint32_t *planes = nullptr; size_t planes_n = 0;      // bit planes of the configurations (bit-sliced layer 0)
 };
+
 
 namespace nce {
 
@@ -1328,7 +1327,7 @@ int nce_tc_gemm(const float *A, const float *B, float *C, int32_t M, int32_t N, 
     int32_t *err = nullptr;
     NCE_CUDA(cudaMallocAsync((void **)&err, sizeof(int32_t), s));
     NCE_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), s));
-    NCE_CUDA(cudaFuncSetAttribute(nce_tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    NCE_CUDA(::nce::raise_smem_limit((const void *)nce_tc_gemm_kernel, sm));
     nce_tc_gemm_kernel<<<M / 128, 128, sm, s>>>(A, B, C, N, K, Kp, split ? 1 : 0, err);
     NCE_CUDA(cudaGetLastError());
     int32_t h = 0;
@@ -1537,8 +1536,7 @@ int nce_nce_destroy(nce_nce_handle h) {
     if (!h) return NCE_OK;
     cudaDeviceSynchronize();
     for (void *p : h->allocs) cudaFree(p);
-    for (void *p : {(void *)h->slot, (void *)h->list, (void *)h->newbuf, (void *)h->e_new, (void *)h->err, (void *)h->eacc,
-                    (void *)h->planes}) if (p) cudaFree(p);
+    for (void *p : {(void *)h->slot, (void *)h->list, (void *)h->newbuf, (void *)h->e_new, (void *)h->err}) if (p) cudaFree(p);
     delete h;
     return NCE_OK;
 }
@@ -1553,25 +1551,20 @@ int nce_nce_full_cache(nce_nce_handle h, const nce_nce_state *st, void *stream) 
     const int64_t tot = (int64_t)st->R * m.N;
     if (m.h0bits && st->R <= 65535) {
         const int32_t W2 = (2 * m.d2 + 31) / 32 + 1;
-        const size_t need = (size_t)st->R * m.nB * m.d0 * m.d1 * W2;
-        if (need > h->planes_n) {
-            if (h->planes) { cudaStreamSynchronize(s); cudaFree(h->planes); }
-            h->planes = nullptr; h->planes_n = 0;
-            NCE_CUDA(cudaMalloc((void **)&h->planes, sizeof(uint32_t) * need));
-            h->planes_n = need;
-        }
+        StreamScratch planes;
+        NCE_CUDA(planes.alloc(sizeof(uint32_t) * (size_t)st->R * m.nB * m.d0 * m.d1 * W2, s));
         const int64_t prow = (int64_t)st->R * m.nB * m.d0 * m.d1;
-        nce_plane_kernel<<<(int)std::min<int64_t>((prow + 7) / 8, 1 << 20), 256, 0, s>>>(m, st->sigma, st->R, W2, h->planes);
+        nce_plane_kernel<<<(int)std::min<int64_t>((prow + 7) / 8, 1 << 20), 256, 0, s>>>(m, st->sigma, st->R, W2, (uint32_t *)planes.p);
         NCE_CUDA(cudaGetLastError());
         const int64_t items = (int64_t)m.d0 * m.d1 * ((m.d2 + 31) / 32);
-        nce_h0_bits_kernel<<<dim3((unsigned)((items + 127) / 128), m.nB, st->R), 128, 0, s>>>(m, h->planes, W2, st->h0);
+        nce_h0_bits_kernel<<<dim3((unsigned)((items + 127) / 128), m.nB, st->R), 128, 0, s>>>(m, (const uint32_t *)planes.p, W2, st->h0);
     } else {
         nce_h0_kernel<<<(int)std::min<int64_t>((tot + 127) / 128, 65535), 128, 0, s>>>(m, st->sigma, st->R, st->h0);
     }
     NCE_CUDA(cudaGetLastError());
     NceJob jb = make_nce_job(h, st);
     const size_t xs = tile_smem(m);
-    NCE_CUDA(cudaFuncSetAttribute(nce_layer_all_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs));
+    NCE_CUDA(::nce::raise_smem_limit((const void *)nce_layer_all_kernel, xs));
     const int blocks = (int)std::min<int64_t>((m.N + tile_tm(m.D, m.tc) - 1) / tile_tm(m.D, m.tc), 1216);
     if (m.depth == 0) {
         nce_e0_kernel<<<(int)std::min<int64_t>((tot + 255) / 256, 65535), 256, 0, s>>>(m, st->h0, tot, st->e);
@@ -1590,17 +1583,13 @@ int nce_nce_full_cache(nce_nce_handle h, const nce_nce_state *st, void *stream) 
             NCE_CUDA(cudaGetLastError());
         }
     }
-    if (h->eacc_n < st->R) {
-        if (h->eacc) { cudaStreamSynchronize(s); cudaFree(h->eacc); }
-        h->eacc = nullptr; h->eacc_n = 0;
-        NCE_CUDA(cudaMalloc((void **)&h->eacc, sizeof(unsigned long long) * st->R));
-        h->eacc_n = st->R;
-    }
-    NCE_CUDA(cudaMemsetAsync(h->eacc, 0, sizeof(unsigned long long) * st->R, s));
+    StreamScratch eacc;
+    NCE_CUDA(eacc.alloc(sizeof(unsigned long long) * st->R, s));
+    NCE_CUDA(cudaMemsetAsync(eacc.p, 0, sizeof(unsigned long long) * st->R, s));
     dim3 g((unsigned)std::min<int64_t>((m.N + 255) / 256, 1024), st->R);
-    nce_energy_kernel<<<g, 256, 0, s>>>(m, st->e, st->R, st->E, h->eacc);
+    nce_energy_kernel<<<g, 256, 0, s>>>(m, st->e, st->R, st->E, (unsigned long long *)eacc.p);
     NCE_CUDA(cudaGetLastError());
-    nce_energy_finish<<<(st->R + 127) / 128, 128, 0, s>>>(m, h->eacc, st->R, st->E);
+    nce_energy_finish<<<(st->R + 127) / 128, 128, 0, s>>>(m, (const unsigned long long *)eacc.p, st->R, st->E);
     NCE_CUDA(cudaGetLastError());
     return NCE_OK;
 }
@@ -1626,10 +1615,10 @@ int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_c
     const int CL = ck->cluster > 1 ? ck->cluster : 1;
     NCE_CHECK(CL == 1 || CL == 2 || CL == 4 || CL == 8, "nce_nce_run_chunk: cluster must be 1, 2, 4 or 8");
     if (CL == 1 || h->dev.depth == 0) {
-        NCE_CUDA(cudaFuncSetAttribute(nce_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        NCE_CUDA(::nce::raise_smem_limit((const void *)nce_chunk_kernel, sm));
         nce_chunk_kernel<<<st->R, 256, sm, (cudaStream_t)stream>>>(jb, w_smem ? 1 : 0);
     } else {
-        NCE_CUDA(cudaFuncSetAttribute(nce_chunk_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        NCE_CUDA(::nce::raise_smem_limit((const void *)nce_chunk_cluster_kernel, sm));
         cudaLaunchConfig_t cfg; std::memset(&cfg, 0, sizeof(cfg));
         cfg.gridDim = dim3((unsigned)(st->R * CL)); cfg.blockDim = dim3(256); cfg.dynamicSmemBytes = sm;
         cfg.stream = (cudaStream_t)stream;

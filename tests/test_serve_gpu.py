@@ -129,3 +129,35 @@ def test_admission_by_budget_and_cancel(cuda):
         infos = srv.wait([hl, h2], timeout=120)
         assert infos[0]["status"] == "cancelled" and infos[1]["status"] == "done"
         assert srv.stats()["bytes_used"] == 0
+
+
+def test_nce_jobs_sharing_a_model(cuda):
+    """Several NeuralCE jobs on one model, re-anchored after every chunk, submitted together: admissions (full
+    caches on the io stream) overlap other jobs' re-anchors on their streams; every result equals the job alone.
+    Run in the bf16 tcgen05 form."""
+    from neuralce_gb300.nce import NCEModel, synthetic_model
+    from neuralce_gb300.serve import Server
+    from neuralce_gb300.workloads import cluster_space, ladder, replica_configs
+    from tests.conftest import random_cell
+    cs = cluster_space()
+    m = NCEModel(cs, random_cell((3, 3, 3), 90), synthetic_model(len(cs.orbits) + 1, 3, 32, 1, 4), shell_edges=(0.0, 3.3),
+                 act="silu", pool="sum", mma=2)
+    jobs = []
+    for k in range(6):
+        R = 3 + k % 3
+        jobs.append(dict(sigma=replica_configs(m.sig0, R, 300 + k), beta=ladder(R)[1], steps=40 + 10 * k, seed=700 + k))
+    def run(srv, j):
+        return srv.submit_nce(m, j["sigma"], j["beta"], j["steps"], 10, j["seed"], reanchor_chunks=1)
+    alone = []
+    with Server(precision=32) as srv:
+        for j in jobs:
+            h = run(srv, j)
+            info, = srv.wait([h], timeout=300)
+            assert info["status"] == "done", info
+            alone.append(h.result())
+    with Server(precision=32) as srv:
+        hs = [run(srv, j) for j in jobs]
+        infos = srv.wait(hs, timeout=300)
+        assert all(i["status"] == "done" for i in infos), infos
+        for h, a in zip(hs, alone):
+            _same(h.result(), a)
