@@ -1869,8 +1869,8 @@ int nce_ce_run_chunk_host(nce_ce_handle h, int32_t R, int8_t *sigma_host, double
 
 // ── full energy without any allocation ─────────────────────────────────────────────────────────────
 // Some callers cannot allocate device memory once they are running: a process whose device memory is all
-// reserved up front by its own pool (so a library cudaMalloc would fail or fragment it), or a latency-bound
-// loop where cudaMalloc/cudaFree would add an implicit device synchronisation.  nce_ce_energy_noalloc serves
+// reserved up front by its own pool (nce_ce_energy takes its scratch from the device's default stream-ordered
+// pool, which would fail or fragment it), or a loop that must not touch any allocator.  nce_ce_energy_noalloc serves
 // them: the per-block float64 partials of ce_energy_kernel live in the fixed array below, which the CUDA driver
 // places in device memory with the rest of this library's image on each device the library is used on, and
 // which stays there until the process exits.  Every call on a device shares this one array; calls that overlap
