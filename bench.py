@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--L", type=int, default=8)
     ap.add_argument("--R", type=int, default=32)
     ap.add_argument("--chunk", type=int, default=5000)
-    ap.add_argument("--workload", choices=["ce", "nce", "ce-batch", "serve", "ce-large", "nce-large", "ce-energy"], default="ce")
+    ap.add_argument("--workload", choices=["ce", "nce", "ce-batch", "serve", "ce-large", "nce-large", "ce-energy", "nce-shipped"], default="ce")
     ap.add_argument("--nce-mma", type=int, default=-1, help="NeuralCE contractions: 0 fp32 CUDA cores; bf16 / split bf16 "
                     "on tensor cores: 1 / 3 mma.sync, 2 / 4 tcgen05 (-1: workload default)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the serving side measurement (0 = skip)")
@@ -169,15 +169,20 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, steps=3, warmup=1, seed=0, cluster=0, mma=0):
-    exchange_every = min(exchange_every, chunk)
+def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, steps=3, warmup=1, seed=0, cluster=0, mma=0,
+              shipped=False):
     """NeuralCE configuration 1: local receptive-field update, float32, R replicas 300-1400 K; a step is one
     chunk of ``chunk`` MC steps + chunk//exchange_every exchange rounds; full re-anchor every ceil(N/chunk)
-    chunks (the reference driver's default)."""
+    chunks (the reference driver's default).  ``shipped``: the reference's shipped PtNi model instead of the
+    configuration-1 network (the model of its published 144,636 steps/s at 2,048 sites, R = 32, H100)."""
+    exchange_every = min(exchange_every, chunk)
     import torch
     from neuralce_gb300.nce import NCEState
-    from neuralce_gb300.workloads import ladder, nce_config, replica_configs
-    m, sig = nce_config(L, depth, width, seed, mma=mma)
+    from neuralce_gb300.workloads import ladder, nce_config, replica_configs, shipped_nce_config
+    if shipped:
+        m, sig = shipped_nce_config(os.path.join(ROOT, "tests", "golden", "nipt_v3_nomax_sel.json"), L, seed, mma=mma)
+    else:
+        m, sig = nce_config(L, depth, width, seed, mma=mma)
     _, beta = ladder(R)
     st = NCEState(m, replica_configs(sig, R, 1 + seed), beta).full_cache()
     tune = None
@@ -208,9 +213,13 @@ def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, step
     torch.cuda.synchronize()
     ms = [a.elapsed_time(b) for a, b in ev]
     tot = sum(ms) / 1e3
-    return {"value": R * chunk * steps / tot, "unit": "swap attempts/s", "ms_per_step": float(np.mean(ms)),
-            "config": f"NeuralCE fp32: {m.N} sites, R={R}, depth {depth}, width {width}, SiLU, sum readout, 12-NN shell, "
+    net = ("the reference's shipped PtNi model (depth 1, width 16, 3 shells, sigmoid gate, tanh, mean readout)" if shipped
+           else f"depth {depth}, width {width}, SiLU, sum readout, 12-NN shell")
+    value = R * chunk * steps / tot
+    return {"value": value, "unit": "swap attempts/s", "ms_per_step": float(np.mean(ms)),
+            "config": f"NeuralCE: {m.N} sites, R={R}, {net}, "
                       f"chunk {chunk} steps + {max(chunk // exchange_every, 1)} exchange rounds, re-anchor every {anchor} chunks",
+            "vs_h100_published_144636": (value / 144_636) if (shipped and m.N == 2048 and R == 32) else None,
             "receptive_field": [int(x) for x in m.keep['ball_end'][0]], "accept_rate": float(st.n_acc.sum().item()) / (R * step),
             "ctas_per_replica": cluster, "autotune_ms": tune,
             "contractions": CONTRACTIONS[mma]}
@@ -570,11 +579,11 @@ def main():
                               "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": {"workload": r["config"]},
                               "serve": r}), flush=True)
         return
-    if args.workload == "nce":
+    if args.workload in ("nce", "nce-shipped"):
         from neuralce_gb300 import _lib
         _lib.lib()
         r = bench_nce(L=args.L, R=args.R, chunk=args.nce_chunk, steps=args.steps, warmup=args.warmup, seed=rank,
-                      mma=max(args.nce_mma, 0))
+                      mma=max(args.nce_mma, 0), shipped=args.workload == "nce-shipped")
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": r["value"], "unit": "swap attempts/s", "n_gpus": world, "steps": args.steps,
                               "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -667,10 +676,11 @@ def main():
             "kernel": {1: "ce_pt_chunk_kernel", 3: "ce_bin2_chunk_kernel"}.get(args.path, "ce_bin_chunk_kernel"),
             "peak_source": src,
             "algorithmic_bytes_per_launch": R * T * B_GATHER}
-    nce_line = nce_tc_line = None
+    nce_line = nce_tc_line = nce_shipped_line = None
     if rank == 0 and args.nce_steps > 0:
         nce_line = bench_nce(steps=args.nce_steps)
         nce_tc_line = bench_nce(steps=args.nce_steps, mma=4)
+        nce_shipped_line = bench_nce(steps=args.nce_steps, shipped=True)
     batch_line = None
     if rank == 0 and args.batch_steps > 0:
         batch_line = bench_batch(steps=args.batch_steps)
@@ -687,7 +697,7 @@ def main():
                 "vs_baseline": value / H100_PUBLISHED if (args.L == 8 and args.R == 32) else None,
                 "dtype": "f64" if args.precision == 64 else "f32", "data": "synthetic (seeded lattice, random-normal ECIs)",
                 "config": workload_config(args, gce), "clocks": clocks, "e2e": e2e, "gpu_launches": 2 * args.steps,
-                "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "nce_tcgen05_split": nce_tc_line, "batch": batch_line, "serve": serve_line,
+                "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "nce_tcgen05_split": nce_tc_line, "nce_shipped_model": nce_shipped_line, "batch": batch_line, "serve": serve_line,
                 "launch": {"warps_per_cta": args.warps, "ctas_per_replica": args.cluster,
                            "path": ["auto", "general", "sign-parity", "sign-parity, two steps in flight"][args.path],
                            "autotune_ms": tuned},

@@ -190,6 +190,8 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
     const int ncg = D / 4, SG = 256 / ncg, TM = tile_tm(D, tc != nullptr), MS = TM / SG;
     const int cg = tid % ncg, sg = tid / ncg;
     const int PW = 1 + P * W;
+    int32_t *tsite = src + TM * PW;                          // the tile's sites
+    float *tinv = reinterpret_cast<float *>(tsite + TM);     // 1 / |first-shell partners| of each
     // tcgen05 path: the tile is the bf16 A operand [128][Kp] (hi, then lo when split) in core-matrix layout
     const int Kp = kpad16(Kin);
     uint8_t *A0 = reinterpret_cast<uint8_t *>(X), *A1 = A0 + (size_t)128 * Kp * 2;
@@ -213,22 +215,43 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
     };
     for (int64_t t0 = (int64_t)tile_begin * TM; t0 < cnt; t0 += (int64_t)tile_stride * TM) {
         const int tm = (int)min((int64_t)TM, cnt - t0);
-        // 1) source row of each site and shell partner: patched rows >= 0, cache rows -(q+1), masked partner INT_MIN
-        for (int idx = tid; idx < tm * PW; idx += nt) {
-            const int mm = idx / PW, q = idx % PW;
+        // 1) the tile's sites and their first shell's 1/|partners| into shared memory, then the source row of each
+        //    site and shell partner: patched rows >= 0, cache rows -(q+1), masked partner INT_MIN.  Four items per
+        //    thread with their slot-map loads in flight together.
+        for (int mm = tid; mm < tm; mm += nt) {
             const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
-            int64_t site = s;
-            if (q > 0) {
-                int32_t b, k[3]; coords(m, s, b, k);
-                const int e0 = b * P * W + (q - 1);
-                site = m.Sh_m[e0] ? site_at(m, k, m.Sh_uo + 3 * e0, m.Sh_b[e0]) : -1;
+            tsite[mm] = (int32_t)s;
+            tinv[mm] = m.Sh_inv[(int32_t)((uint32_t)s % (uint32_t)m.nB) * P];
+        }
+        __syncthreads();
+        for (int base = tid; base < tm * PW; base += 4 * nt) {
+            int64_t site[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int idx = base + u * nt;
+                site[u] = -1;
+                if (idx < tm * PW) {
+                    const int mm = idx / PW, q = idx % PW;
+                    const int64_t s = tsite[mm];
+                    site[u] = s;
+                    if (q > 0) {
+                        int32_t b, k[3]; coords(m, s, b, k);
+                        const int e0 = b * P * W + (q - 1);
+                        site[u] = m.Sh_m[e0] ? site_at(m, k, m.Sh_uo + 3 * e0, m.Sh_b[e0]) : -1;
+                    }
+                }
             }
-            int32_t code = INT_MIN;
-            if (site >= 0) {
-                const int32_t p = slot ? slot[site] : -1;
-                code = (p >= 0 && p < nlev) ? p : -(int32_t)(site + 1);
+            int32_t pv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) pv[u] = (slot && site[u] >= 0) ? slot[site[u]] : -1;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int idx = base + u * nt;
+                if (idx >= tm * PW) continue;
+                int32_t code = INT_MIN;
+                if (site[u] >= 0) code = (pv[u] >= 0 && pv[u] < nlev) ? pv[u] : -(int32_t)(site[u] + 1);
+                src[idx] = code;
             }
-            src[idx] = code;
         }
         __syncthreads();
         // 2) X = [h | masked shell means] of the tile's sites: one warp per site, lanes over channels (coalesced rows)
@@ -261,12 +284,10 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                 for (int h = 0; h < 2; ++h) {
                     if (h == 1 && !two) break;
                     const int ms = h ? mb : mm;
-                    const int64_t s = direct0 ? (*direct0 + pos0 + t0 + ms) : list[pos0 + t0 + ms];
-                    const int32_t b = (int32_t)((uint32_t)s % (uint32_t)m.nB);
                     float s0 = 0.f, s1 = 0.f;
 #pragma unroll
                     for (int u = 1; u < 13; ++u) { s0 += va[h][u]; s1 += vb[h][u]; }
-                    const float inv = m.Sh_inv[b * P];
+                    const float inv = tinv[ms];
                     if (h0ok) { xput(ms, c0, va[h][0]); xput(ms, Cin + c0, s0 * inv); }
                     if (h1ok) { xput(ms, c1, vb[h][0]); xput(ms, Cin + c1, s1 * inv); }
                 }
@@ -288,8 +309,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
 #pragma unroll
                     for (int j = 0; j < 4; ++j) v[j][u] = (ok && lane + 32 * j < Cin) ? rr[lane + 32 * j] : 0.f;
                 }
-                const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
-                const float inv = m.Sh_inv[(int32_t)((uint32_t)s % (uint32_t)m.nB) * P];
+                const float inv = tinv[mm];
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const int c = lane + 32 * j;
@@ -912,7 +932,7 @@ struct SmemPlan {
             xb = ab > yb ? ab : yb;
         }
         p.src = al(p.X + xb);
-        p.wt = al128(p.src + sizeof(int32_t) * (size_t)TM * (1 + m.P * m.W));
+        p.wt = al128(p.src + sizeof(int32_t) * (size_t)TM * (1 + m.P * m.W + 2));
         p.tile_end = p.wt + (m.tc ? (size_t)kpad16(Kmax) * m.D * 2 * (m.tc_split ? 2 : 1) : 0);
         p.ent = p.tile_end;
         p.w = al(p.ent + (sizeof(int32_t) * 2 + 1) * 2 * (size_t)m.w0max);

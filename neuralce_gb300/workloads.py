@@ -70,6 +70,29 @@ def nce_config(L=8, depth=3, width=64, seed=0, x_pt=0.5, model_seed=0, mma=0):
     return m, m.sig0
 
 
+def shipped_nce_config(path, L=8, seed=0, x_pt=0.5, mma=0):
+    """(NCEModel, canonical sigma): the reference's shipped PtNi NeuralCE model (its model.pkl content stored as
+    JSON: depth 1, width 16, three shells, sigmoid gate, tanh, mean readout; the model its published GPU
+    throughput is quoted on) on an L^3 conventional fcc cell at x_pt, a = 3.924 A."""
+    import json
+    from .lattice import Primitive
+    from .nce import NCEModel, expand_params
+    with open(path) as f:
+        g = json.load(f)
+    arr = lambda x: np.asarray(x, float)
+    P = g["params0"]
+    params = dict(lin=arr(P["lin"]), layers=[{k: arr(v) for k, v in lay.items()} for lay in P["layers"]],
+                  head={k: (float(v) if np.ndim(v) == 0 else arr(v)) for k, v in P["head"].items()})
+    prim = Primitive(cell=arr(g["primitive_cell"]), frac=arr(g["primitive_frac"]),
+                     species=g["chemical_symbols"] * len(g["primitive_numbers"]), numbers=np.array(g["primitive_numbers"]))
+    mdl = dict(params=[params], mu=arr(g["mu"]), sd=arr(g["sd"]), keep=np.array(g["keep"]), K_chem=g["K_chem"])
+    cs = ClusterSpace.build(prim, g["cutoffs"])
+    Pm, mu, sd = expand_params(mdl, 0)
+    m = NCEModel(cs, ce_structure(L, seed, x_pt), Pm, mu, sd, shell_edges=g["shell_edges"], act="tanh", pool="mean",
+                 ys=g["ys"], ym=g["ym"], mma=mma)
+    return m, m.sig0
+
+
 def ce_batch_config(n_jobs=64, seed=2, L_range=(4, 32), R_choices=(16, 32, 64), T_min=300.0, T_max=1400.0):
     """Batched CE workload: ``n_jobs`` independent cells with edge L ~ U{4..32} conventional cells (256 to 131,072
     sites), Pt fraction ~ U[0.1, 0.9], replicas ~ U{16, 32, 64} on a geometric 300-1400 K ladder each; the CE
