@@ -192,6 +192,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
     const int PW = 1 + P * W;
     int32_t *tsite = src + TM * PW;                          // the tile's sites
     float *tinv = reinterpret_cast<float *>(tsite + TM);     // 1 / |first-shell partners| of each
+    int4 *tk = reinterpret_cast<int4 *>(tinv + TM);          // (basis, k0, k1, k2) of each
     // tcgen05 path: the tile is the bf16 A operand [128][Kp] (hi, then lo when split) in core-matrix layout
     const int Kp = kpad16(Kin);
     uint8_t *A0 = reinterpret_cast<uint8_t *>(X), *A1 = A0 + (size_t)128 * Kp * 2;
@@ -220,8 +221,10 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
         //    thread with their slot-map loads in flight together.
         for (int mm = tid; mm < tm; mm += nt) {
             const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
+            int32_t b, k[3]; coords(m, s, b, k);
             tsite[mm] = (int32_t)s;
-            tinv[mm] = m.Sh_inv[(int32_t)((uint32_t)s % (uint32_t)m.nB) * P];
+            tinv[mm] = m.Sh_inv[b * P];
+            tk[mm] = make_int4(b, k[0], k[1], k[2]);
         }
         __syncthreads();
         for (int base = tid; base < tm * PW; base += 4 * nt) {
@@ -232,11 +235,11 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                 site[u] = -1;
                 if (idx < tm * PW) {
                     const int mm = idx / PW, q = idx % PW;
-                    const int64_t s = tsite[mm];
-                    site[u] = s;
+                    site[u] = tsite[mm];
                     if (q > 0) {
-                        int32_t b, k[3]; coords(m, s, b, k);
-                        const int e0 = b * P * W + (q - 1);
+                        const int4 c = tk[mm];
+                        const int32_t k[3] = {c.y, c.z, c.w};
+                        const int e0 = c.x * P * W + (q - 1);
                         site[u] = m.Sh_m[e0] ? site_at(m, k, m.Sh_uo + 3 * e0, m.Sh_b[e0]) : -1;
                     }
                 }
@@ -318,6 +321,39 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
 #pragma unroll
                     for (int u = 1; u < 13; ++u) a += v[j][u];
                     xput(mm, c, v[j][0]); xput(mm, Cin + c, a * inv);
+                }
+            }
+        } else if (Cin <= 32 && W <= 32) {
+            // narrow inputs and wide shells (the reference's shipped model: 18 channels, shells of 12 / 6 / 24):
+            // one lane per channel, two sites per warp, all partner loads of one shell of both sites in flight
+            const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+            const bool cok = lane < Cin;
+            auto row = [&](int32_t code) -> const float * {
+                return code >= 0 ? newl + (size_t)code * Cin : cache + (size_t)(-(int64_t)code - 1) * Cin;
+            };
+            for (int mm = warp; mm < tm; mm += 2 * nwarp) {
+                const int mb = mm + nwarp;
+                const bool two = mb < tm;
+                const int32_t *sa = src + mm * PW, *sb = src + (two ? mb : mm) * PW;
+                const float xa = cok ? row(sa[0])[lane] : 0.f, xb = (cok && two) ? row(sb[0])[lane] : 0.f;
+                if (cok) { xput(mm, lane, xa); if (two) xput(mb, lane, xb); }
+                const int ba = tk[mm].x, bb = tk[two ? mb : mm].x;
+                for (int p = 0; p < P; ++p) {
+                    float va[32], vb[32];
+#pragma unroll
+                    for (int u = 0; u < 32; ++u) {
+                        const int32_t qa = u < W ? sa[1 + p * W + u] : INT_MIN;
+                        const int32_t qb = (two && u < W) ? sb[1 + p * W + u] : INT_MIN;
+                        va[u] = (cok && qa != INT_MIN) ? row(qa)[lane] : 0.f;
+                        vb[u] = (cok && qb != INT_MIN) ? row(qb)[lane] : 0.f;
+                    }
+                    float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+                    for (int u = 0; u < 32; ++u) { s0 += va[u]; s1 += vb[u]; }
+                    if (cok) {
+                        xput(mm, Cin + p * Cin + lane, s0 * m.Sh_inv[ba * P + p]);
+                        if (two) xput(mb, Cin + p * Cin + lane, s1 * m.Sh_inv[bb * P + p]);
+                    }
                 }
             }
         } else {
@@ -932,7 +968,7 @@ struct SmemPlan {
             xb = ab > yb ? ab : yb;
         }
         p.src = al(p.X + xb);
-        p.wt = al128(p.src + sizeof(int32_t) * (size_t)TM * (1 + m.P * m.W + 2));
+        p.wt = al128(p.src + sizeof(int32_t) * (size_t)TM * (1 + m.P * m.W + 6));
         p.tile_end = p.wt + (m.tc ? (size_t)kpad16(Kmax) * m.D * 2 * (m.tc_split ? 2 : 1) : 0);
         p.ent = p.tile_end;
         p.w = al(p.ent + (sizeof(int32_t) * 2 + 1) * 2 * (size_t)m.w0max);
