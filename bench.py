@@ -186,21 +186,27 @@ def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, step
     _, beta = ladder(R)
     st = NCEState(m, replica_configs(sig, R, 1 + seed), beta).full_cache()
     tune = None
-    if cluster == 0:                                   # CTAs per replica: time a short chunk for each candidate
+    per_sm = 1
+    if cluster == 0:            # CTAs per replica and per SM: time a short chunk for each candidate that fits
+        from neuralce_gb300 import _lib
         from neuralce_gb300.nce import NCEState as _S
         tune = {}
-        for cl in (1, 2, 4):
+        for cl, ps in ((1, 1), (2, 1), (4, 1), (2, 2), (4, 2), (8, 2)):
             sc = _S(m, replica_configs(sig, R, 1 + seed), beta).full_cache()
-            sc.run_chunk(4, 0, seed=1, cluster=cl)
+            try:
+                sc.run_chunk(4, 0, seed=1, cluster=cl, ctas_per_sm=ps)
+            except _lib.NceError:
+                continue
             a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a_.record(); sc.run_chunk(20, 4, seed=1, cluster=cl); b_.record(); torch.cuda.synchronize()
-            tune[cl] = a_.elapsed_time(b_)
-        cluster = min(tune, key=tune.get)
+            a_.record(); sc.run_chunk(20, 4, seed=1, cluster=cl, ctas_per_sm=ps); b_.record(); torch.cuda.synchronize()
+            tune[f"{cl}x{ps}"] = a_.elapsed_time(b_)
+        cluster, per_sm = (int(x) for x in min(tune, key=tune.get).split("x"))
     anchor = max(1, -(-m.N // chunk))
     step = 0
     def one(k):
         nonlocal step
-        st.run_chunk(chunk, step, seed=99, exchange_rounds=max(chunk // exchange_every, 1), cluster=cluster); step += chunk
+        st.run_chunk(chunk, step, seed=99, exchange_rounds=max(chunk // exchange_every, 1), cluster=cluster,
+                     ctas_per_sm=per_sm); step += chunk
         if (k + 1) % anchor == 0:
             st.full_cache()
     for k in range(warmup):
@@ -221,7 +227,7 @@ def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, step
                       f"chunk {chunk} steps + {max(chunk // exchange_every, 1)} exchange rounds, re-anchor every {anchor} chunks",
             "vs_h100_published_144636": (value / 144_636) if (shipped and m.N == 2048 and R == 32) else None,
             "receptive_field": [int(x) for x in m.keep['ball_end'][0]], "accept_rate": float(st.n_acc.sum().item()) / (R * step),
-            "ctas_per_replica": cluster, "autotune_ms": tune,
+            "ctas_per_replica": cluster, "ctas_per_sm": per_sm, "autotune_ms": tune,
             "contractions": CONTRACTIONS[mma]}
 
 
@@ -676,10 +682,11 @@ def main():
             "kernel": {1: "ce_pt_chunk_kernel", 3: "ce_bin2_chunk_kernel"}.get(args.path, "ce_bin_chunk_kernel"),
             "peak_source": src,
             "algorithmic_bytes_per_launch": R * T * B_GATHER}
-    nce_line = nce_tc_line = nce_shipped_line = None
+    nce_line = nce_tc_line = nce_bf16_line = nce_shipped_line = None
     if rank == 0 and args.nce_steps > 0:
         nce_line = bench_nce(steps=args.nce_steps)
         nce_tc_line = bench_nce(steps=args.nce_steps, mma=4)
+        nce_bf16_line = bench_nce(steps=args.nce_steps, mma=2)
         nce_shipped_line = bench_nce(steps=args.nce_steps, shipped=True)
     batch_line = None
     if rank == 0 and args.batch_steps > 0:
@@ -697,7 +704,7 @@ def main():
                 "vs_baseline": value / H100_PUBLISHED if (args.L == 8 and args.R == 32) else None,
                 "dtype": "f64" if args.precision == 64 else "f32", "data": "synthetic (seeded lattice, random-normal ECIs)",
                 "config": workload_config(args, gce), "clocks": clocks, "e2e": e2e, "gpu_launches": 2 * args.steps,
-                "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "nce_tcgen05_split": nce_tc_line, "nce_shipped_model": nce_shipped_line, "batch": batch_line, "serve": serve_line,
+                "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "nce_tcgen05_split": nce_tc_line, "nce_tcgen05_bf16": nce_bf16_line, "nce_shipped_model": nce_shipped_line, "batch": batch_line, "serve": serve_line,
                 "launch": {"warps_per_cta": args.warps, "ctas_per_replica": args.cluster,
                            "path": ["auto", "general", "sign-parity", "sign-parity, two steps in flight"][args.path],
                            "autotune_ms": tuned},

@@ -255,6 +255,8 @@ typedef struct {
     int32_t ex_parity; const double *ex_u; /* host-supplied exchange randoms: (rounds) parities packed in bits,
                                               ex_u (rounds, ceil((R-1)/2)); NULL -> Philox */
     int32_t cluster;       /* CTAs (SMs) per replica: 1, 2, 4 or 8 (thread-block cluster) */
+    int32_t ctas_per_sm;   /* 0 or 1: one CTA per SM; 2: two CTAs per SM (at most 128 registers a thread, layer
+                              weights read through L1; the CTA's shared memory must fit half an SM) */
 } nce_nce_chunk;
 
 int nce_nce_create(const nce_nce_desc *desc, nce_nce_handle *out);

@@ -57,7 +57,7 @@ class NceNceState(C.Structure):
 class NceNceChunk(C.Structure):
     _fields_ = [("n_steps", i64), ("step0", i64), ("prop_a", vp), ("prop_b", vp), ("prop_u", vp), ("seed", u64),
                 ("sample_interval", i64), ("E_samples", vp), ("dE_out", vp), ("force", i32), ("exchange_rounds", i32),
-                ("ex_parity", i32), ("ex_u", vp), ("cluster", i32)]
+                ("ex_parity", i32), ("ex_u", vp), ("cluster", i32), ("ctas_per_sm", i32)]
 
 
 class NceServerConfig(C.Structure):

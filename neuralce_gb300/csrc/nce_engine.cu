@@ -128,7 +128,12 @@ __device__ __forceinline__ float patched(const NceJob &jb, int lvl, const float 
 
 // Tile geometry of the layer GEMM: D/4 column groups of 4 outputs, 256/(D/4) site groups, TM sites per tile,
 // MS sites per thread (register micro-tile MS x 4).  D in {16, 32, 64, 128}.
-__host__ __device__ __forceinline__ int tile_tm(int D, int tc = 0) { return tc ? 128 : 4 * (256 / (D / 4)); }   // 4 sites per thread
+// Tile rows: 128 on the tcgen05 path; otherwise MS sites per thread x SG = 256 / (D / 4) site groups, MS = 4
+// (the mma.sync warp tiling needs it), on the float32 path at most 128 rows (D = 16: MS = 2)
+__host__ __device__ __forceinline__ int tile_tm(int D, int tc = 0, int mma = 0) {
+    const int SG = 256 / (D / 4);
+    return tc ? 128 : (mma ? 4 : (SG >= 64 ? 2 : 4)) * SG;
+}
 __host__ __device__ __forceinline__ int kpad16(int k) { return (k + 15) & ~15; }
 
 // tensor-memory accumulator, completion mbarrier and the staged B operand of the tcgen05 tile path; `phase` is the
@@ -187,7 +192,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
     const int Cin = lvl == 0 ? m.C0 : m.D, D = m.D, P = m.P, W = m.W;
     const int Kin = (1 + P) * Cin, XS = Kin + 1;
     const int tid = threadIdx.x, nt = blockDim.x;
-    const int ncg = D / 4, SG = 256 / ncg, TM = tile_tm(D, tc != nullptr), MS = TM / SG;
+    const int ncg = D / 4, SG = 256 / ncg, TM = tile_tm(D, tc != nullptr, m.mma), MS = TM / SG;
     const int cg = tid % ncg, sg = tid / ncg;
     const int PW = 1 + P * W;
     int32_t *tsite = src + TM * PW;                          // the tile's sites
@@ -532,7 +537,9 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
             o[i][0] = b4.x; o[i][1] = b4.y; o[i][2] = b4.z; o[i][3] = b4.w;
             g[i][0] = gb4.x; g[i][1] = gb4.y; g[i][2] = gb4.z; g[i][3] = gb4.w;
         }
-        const float *x0 = X + (size_t)sg * XS, *x1 = x0 + (size_t)SG * XS, *x2 = x1 + (size_t)SG * XS, *x3 = x2 + (size_t)SG * XS;
+        // rows sg + i SG, i < MS (MS = 2: the last two micro-tile rows repeat the first two and are not used)
+        const float *x0 = X + (size_t)sg * XS, *x1 = x0 + (size_t)SG * XS;
+        const float *x2 = MS > 2 ? x1 + (size_t)SG * XS : x0, *x3 = MS > 2 ? x2 + (size_t)SG * XS : x1;
 #pragma unroll 4
         for (int kk = 0; kk < Kin; ++kk) {
             const float4 w4 = *reinterpret_cast<const float4 *>(LW.W + (size_t)kk * D + cg * 4);
@@ -958,7 +965,7 @@ struct SmemPlan {
         auto al = [](size_t x) { return (x + 15) / 16 * 16; };
         auto al128 = [](size_t x) { return (x + 127) / 128 * 128; };
         SmemPlan p;
-        const int TM = tile_tm(m.D, m.tc), Kmax = tile_kin(m.P, m.C0, m.D);
+        const int TM = tile_tm(m.D, m.tc, m.mma), Kmax = tile_kin(m.P, m.C0, m.D);
         // layer-0 change per (site, channel): int32 counts for +-1 point functions, int64 fixed point otherwise
         p.dh = 0; p.dh_bytes = with_dh ? al((m.l0bin ? sizeof(int32_t) : sizeof(unsigned long long)) * (size_t)m.n0max * m.C0) : 0;
         p.X = al128(p.dh_bytes);
@@ -977,7 +984,10 @@ struct SmemPlan {
     }
 };
 
-__global__ void __launch_bounds__(256, 1) nce_chunk_kernel(const __grid_constant__ NceJob jb, int32_t w_smem) {
+// MINB = CTAs resident per SM: 1 (all registers) or 2 (at most 128 registers a thread, twice the warps to hide
+// the latency of the gathers and barriers when two CTAs' shared memory fits an SM)
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) nce_chunk_kernel(const __grid_constant__ NceJob jb, int32_t w_smem) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ NceCtl ctl;
     const int r = blockIdx.x;
@@ -1012,7 +1022,8 @@ __global__ void __launch_bounds__(256, 1) nce_chunk_kernel(const __grid_constant
 }
 
 // the same chunk with each replica spread over a thread-block cluster of gridDim.x / R CTAs
-__global__ void __launch_bounds__(256, 1) nce_chunk_cluster_kernel(const __grid_constant__ NceJob jb, int32_t w_smem) {
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) nce_chunk_cluster_kernel(const __grid_constant__ NceJob jb, int32_t w_smem) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ NceCtl ctl;
     cg::cluster_group cluster = cg::this_cluster();
@@ -1192,7 +1203,7 @@ __global__ void __launch_bounds__(256, 1) nce_layer_all_kernel(NceJob jb, int lv
                                                              float *e_out, int64_t chunk0, int64_t chunk_n) {
     extern __shared__ __align__(16) unsigned char smem[];
     const NceDev &m = jb.m;
-    const int TM = tile_tm(m.D, m.tc);
+    const int TM = tile_tm(m.D, m.tc, m.mma);
     const SmemPlan sp = SmemPlan::make(m, false);
     float *X = reinterpret_cast<float *>(smem + sp.X);
     int32_t *src = reinterpret_cast<int32_t *>(smem + sp.src);
@@ -1275,6 +1286,8 @@ static int dup(nce_nce_model *h, const T *src, size_t n, const T *&dst) {
 
 // dynamic shared memory of the step kernels: 227 KB per CTA less the kernels' static shared memory
 constexpr size_t kStepSmemMax = 232448 - 1024;
+// two CTAs per SM: 228 KB of shared memory per SM, less 1 KB reserved per CTA and the static shared memory
+constexpr size_t kStepSmemMax2 = 233472 / 2 - 2048;
 
 static size_t tile_smem(const NceDev &m) {
     return SmemPlan::make(m, false).tile_end;
@@ -1621,7 +1634,7 @@ int nce_nce_full_cache(nce_nce_handle h, const nce_nce_state *st, void *stream) 
     NceJob jb = make_nce_job(h, st);
     const size_t xs = tile_smem(m);
     NCE_CUDA(::nce::raise_smem_limit((const void *)nce_layer_all_kernel, xs));
-    const int blocks = (int)std::min<int64_t>((m.N + tile_tm(m.D, m.tc) - 1) / tile_tm(m.D, m.tc), 1216);
+    const int blocks = (int)std::min<int64_t>((m.N + tile_tm(m.D, m.tc, m.mma) - 1) / tile_tm(m.D, m.tc, m.mma), 1216);
     if (m.depth == 0) {
         nce_e0_kernel<<<(int)std::min<int64_t>((tot + 255) / 256, 65535), 256, 0, s>>>(m, st->h0, tot, st->e);
         NCE_CUDA(cudaGetLastError());
@@ -1666,15 +1679,21 @@ int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_c
     jb.seed = ck->seed; jb.sample_interval = ck->sample_interval > 0 ? ck->sample_interval : 1; jb.E_samples = ck->E_samples;
     jb.dE_out = ck->dE_out; jb.force = ck->force;
     if (ck->n_steps == 0) return NCE_OK;
-    const bool w_smem = step_smem(h->dev, true) <= kStepSmemMax;
+    const int per_sm = ck->ctas_per_sm > 1 ? ck->ctas_per_sm : 1;
+    NCE_CHECK(per_sm <= 2, "nce_nce_run_chunk: ctas_per_sm must be 1 or 2");
+    const size_t lim = per_sm == 2 ? kStepSmemMax2 : kStepSmemMax;
+    const bool w_smem = step_smem(h->dev, true) <= lim;
     const size_t sm = step_smem(h->dev, w_smem);
+    NCE_CHECK(sm <= lim, "nce_nce_run_chunk: %zu bytes of shared memory per CTA do not fit %d CTAs per SM", sm, per_sm);
     const int CL = ck->cluster > 1 ? ck->cluster : 1;
     NCE_CHECK(CL == 1 || CL == 2 || CL == 4 || CL == 8, "nce_nce_run_chunk: cluster must be 1, 2, 4 or 8");
     if (CL == 1 || h->dev.depth == 0) {
-        NCE_CUDA(::nce::raise_smem_limit((const void *)nce_chunk_kernel, sm));
-        nce_chunk_kernel<<<st->R, 256, sm, (cudaStream_t)stream>>>(jb, w_smem ? 1 : 0);
+        auto kern = per_sm == 2 ? nce_chunk_kernel<2> : nce_chunk_kernel<1>;
+        NCE_CUDA(::nce::raise_smem_limit((const void *)kern, sm));
+        kern<<<st->R, 256, sm, (cudaStream_t)stream>>>(jb, w_smem ? 1 : 0);
     } else {
-        NCE_CUDA(::nce::raise_smem_limit((const void *)nce_chunk_cluster_kernel, sm));
+        auto kern = per_sm == 2 ? nce_chunk_cluster_kernel<2> : nce_chunk_cluster_kernel<1>;
+        NCE_CUDA(::nce::raise_smem_limit((const void *)kern, sm));
         cudaLaunchConfig_t cfg; std::memset(&cfg, 0, sizeof(cfg));
         cfg.gridDim = dim3((unsigned)(st->R * CL)); cfg.blockDim = dim3(256); cfg.dynamicSmemBytes = sm;
         cfg.stream = (cudaStream_t)stream;
@@ -1682,7 +1701,7 @@ int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_c
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = (unsigned)CL; attr[0].val.clusterDim.y = 1; attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr; cfg.numAttrs = 1;
-        NCE_CUDA(cudaLaunchKernelEx(&cfg, nce_chunk_cluster_kernel, jb, (int32_t)(w_smem ? 1 : 0)));
+        NCE_CUDA(cudaLaunchKernelEx(&cfg, kern, jb, (int32_t)(w_smem ? 1 : 0)));
     }
     NCE_CUDA(cudaGetLastError());
     if (ck->exchange_rounds > 0 && st->R > 1) {

@@ -127,18 +127,22 @@ def test_metropolis_trajectory_matches_oracle(cuda, nipt_model, cluster):
             assert int(st.n_acc[r].item()) == nacc
 
 
-def test_cluster_equals_single_cta(cuda):
-    """Philox stream with exchanges: a replica spread over a 4-CTA cluster gives the same trajectory as one CTA."""
+@pytest.mark.parametrize("cluster,per_sm,shipped", [(4, 1, False), (1, 2, False), (4, 2, False), (8, 2, False),
+                                                   (4, 1, True), (2, 2, True), (8, 2, True)])
+def test_cluster_equals_single_cta(cuda, nipt_model, cluster, per_sm, shipped):
+    """Philox stream with exchanges: a replica spread over a cluster of CTAs, and CTAs sharing an SM two by two
+    (128 registers a thread), give the same trajectory as one CTA per replica; the configuration-1 network and
+    the reference's shipped model (three shells of up to 24 partners)."""
     torch = cuda
     from neuralce_gb300.nce import NCEState
     from neuralce_gb300.workloads import ladder, replica_configs
-    m, orc = _model_bench(3, 6)
+    m, orc = _model_pkl(nipt_model[0], random_cell((4, 4, 4), 6)) if shipped else _model_bench(3, 6)
     R = 4
     _, beta = ladder(R)
     sig = replica_configs(m.sig0, R, 3)
     a = NCEState(m, sig, beta).full_cache(); b = NCEState(m, sig, beta).full_cache()
     a.run_chunk(40, 0, seed=5, exchange_rounds=2, cluster=1)
-    b.run_chunk(40, 0, seed=5, exchange_rounds=2, cluster=4)
+    b.run_chunk(40, 0, seed=5, exchange_rounds=2, cluster=cluster, ctas_per_sm=per_sm)
     torch.cuda.synchronize()
     assert torch.equal(a.sigma, b.sigma) and torch.equal(a.rep_of_slot, b.rep_of_slot)
     assert torch.equal(a.n_acc, b.n_acc) and torch.allclose(a.E, b.E, rtol=0, atol=0)
