@@ -37,6 +37,7 @@ int launch_exchange(int32_t R, double *E, double E_scale, const float *beta_slot
                     cudaStream_t s);
 
 constexpr int kMaxLayers = 4;
+constexpr int kZeroRow = 256;                 // >= every layer's input width
 constexpr double kFix = 1099511627776.0;      // 2^40
 constexpr double kInvFix = 1.0 / 1099511627776.0;
 
@@ -69,6 +70,7 @@ struct NceDev {
     // tcgen05 layer contractions (mma 2: bf16, mma 4: split bf16): per layer the weights as the B operand in bf16
     // core-matrix layout ([D][Kp], Kp = Kin rounded up to 16; hi, then lo when split)
     int32_t tc, tc_split; const uint8_t *Wt[kMaxLayers];
+    const float *zrow;                        // kZeroRow zeros: the row a masked shell partner reads
 };
 
 struct NceJob {
@@ -195,7 +197,9 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
     const int ncg = D / 4, SG = 256 / ncg, TM = tile_tm(D, tc != nullptr, m.mma), MS = TM / SG;
     const int cg = tid % ncg, sg = tid / ncg;
     const int PW = 1 + P * W;
-    int32_t *tsite = src + TM * PW;                          // the tile's sites
+    // row of each site and shell partner: the step's new value, the cache, or a row of zeros (masked partner)
+    const float **srcp = reinterpret_cast<const float **>(src);
+    int32_t *tsite = reinterpret_cast<int32_t *>(srcp + TM * PW);   // the tile's sites
     float *tinv = reinterpret_cast<float *>(tsite + TM);     // 1 / |first-shell partners| of each
     int4 *tk = reinterpret_cast<int4 *>(tinv + TM);          // (basis, k0, k1, k2) of each
     // tcgen05 path: the tile is the bf16 A operand [128][Kp] (hi, then lo when split) in core-matrix layout
@@ -256,36 +260,31 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
             for (int u = 0; u < 4; ++u) {
                 const int idx = base + u * nt;
                 if (idx >= tm * PW) continue;
-                int32_t code = INT_MIN;
-                if (site[u] >= 0) code = (pv[u] >= 0 && pv[u] < nlev) ? pv[u] : -(int32_t)(site[u] + 1);
-                src[idx] = code;
+                srcp[idx] = site[u] < 0 ? m.zrow
+                          : (pv[u] >= 0 && pv[u] < nlev) ? newl + (size_t)pv[u] * Cin : cache + (size_t)site[u] * Cin;
             }
         }
         __syncthreads();
-        // 2) X = [h | masked shell means] of the tile's sites: one warp per site, lanes over channels (coalesced rows)
+        // 2) X = [h | masked shell means] of the tile's sites: lanes over channels (coalesced rows); masked
+        //    partners read the zero row, so every sum runs over all W slots in order
+        const float *zr = m.zrow;
         if (P == 1 && W <= 12 && Cin <= 64) {
             // one shell of at most 12 partners: two sites per warp with all 2 x 13 rows' loads in flight at once
             const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
             const int c0 = lane, c1 = lane + 32;
             const bool h0ok = c0 < Cin, h1ok = c1 < Cin;
-            auto row = [&](int32_t code) -> const float * {
-                return code >= 0 ? newl + (size_t)code * Cin : cache + (size_t)(-(int64_t)code - 1) * Cin;
-            };
             for (int mm = warp; mm < tm; mm += 2 * nwarp) {
                 const int mb = mm + nwarp;
                 const bool two = mb < tm;
                 float va[2][13], vb[2][13];
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    const int32_t *sr = src + (h ? mb : mm) * PW;
-                    const bool on = h == 0 || two;
+                    const float *const *sr = srcp + (two ? (h ? mb : mm) : mm) * PW;
 #pragma unroll
                     for (int u = 0; u < 13; ++u) {
-                        const int32_t q = (on && u <= W) ? sr[u] : INT_MIN;
-                        const bool ok = q != INT_MIN;
-                        const float *rr = ok ? row(q) : cache;
-                        va[h][u] = (ok && h0ok) ? rr[c0] : 0.f;
-                        vb[h][u] = (ok && h1ok) ? rr[c1] : 0.f;
+                        const float *rr = u <= W ? sr[u] : zr;
+                        va[h][u] = h0ok ? rr[c0] : 0.f;
+                        vb[h][u] = h1ok ? rr[c1] : 0.f;
                     }
                 }
 #pragma unroll
@@ -303,19 +302,14 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
         } else if (P == 1 && W <= 12 && Cin <= 128) {
             // one shell, up to 128 channels: one site per warp, four channels per lane, all 13 rows' loads in flight
             const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
-            auto row = [&](int32_t code) -> const float * {
-                return code >= 0 ? newl + (size_t)code * Cin : cache + (size_t)(-(int64_t)code - 1) * Cin;
-            };
             for (int mm = warp; mm < tm; mm += nwarp) {
-                const int32_t *sr = src + mm * PW;
+                const float *const *sr = srcp + mm * PW;
                 float v[4][13];
 #pragma unroll
                 for (int u = 0; u < 13; ++u) {
-                    const int32_t q = u <= W ? sr[u] : INT_MIN;
-                    const bool ok = q != INT_MIN;
-                    const float *rr = ok ? row(q) : cache;
+                    const float *rr = u <= W ? sr[u] : zr;
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) v[j][u] = (ok && lane + 32 * j < Cin) ? rr[lane + 32 * j] : 0.f;
+                    for (int j = 0; j < 4; ++j) v[j][u] = lane + 32 * j < Cin ? rr[lane + 32 * j] : 0.f;
                 }
                 const float inv = tinv[mm];
 #pragma unroll
@@ -333,24 +327,20 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
             // one lane per channel, two sites per warp, all partner loads of one shell of both sites in flight
             const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
             const bool cok = lane < Cin;
-            auto row = [&](int32_t code) -> const float * {
-                return code >= 0 ? newl + (size_t)code * Cin : cache + (size_t)(-(int64_t)code - 1) * Cin;
-            };
+            const int cl = cok ? lane : 0;
             for (int mm = warp; mm < tm; mm += 2 * nwarp) {
                 const int mb = mm + nwarp;
                 const bool two = mb < tm;
-                const int32_t *sa = src + mm * PW, *sb = src + (two ? mb : mm) * PW;
-                const float xa = cok ? row(sa[0])[lane] : 0.f, xb = (cok && two) ? row(sb[0])[lane] : 0.f;
+                const float *const *sa = srcp + mm * PW, *const *sb = srcp + (two ? mb : mm) * PW;
+                const float xa = sa[0][cl], xb = sb[0][cl];
                 if (cok) { xput(mm, lane, xa); if (two) xput(mb, lane, xb); }
                 const int ba = tk[mm].x, bb = tk[two ? mb : mm].x;
                 for (int p = 0; p < P; ++p) {
                     float va[32], vb[32];
 #pragma unroll
                     for (int u = 0; u < 32; ++u) {
-                        const int32_t qa = u < W ? sa[1 + p * W + u] : INT_MIN;
-                        const int32_t qb = (two && u < W) ? sb[1 + p * W + u] : INT_MIN;
-                        va[u] = (cok && qa != INT_MIN) ? row(qa)[lane] : 0.f;
-                        vb[u] = (cok && qb != INT_MIN) ? row(qb)[lane] : 0.f;
+                        va[u] = u < W ? sa[1 + p * W + u][cl] : 0.f;
+                        vb[u] = u < W ? sb[1 + p * W + u][cl] : 0.f;
                     }
                     float s0 = 0.f, s1 = 0.f;
 #pragma unroll
@@ -364,32 +354,23 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
         } else {
             const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
             for (int mm = warp; mm < tm; mm += nwarp) {
-                const int32_t *sr = src + mm * PW;
-                const int64_t s = direct0 ? (*direct0 + pos0 + t0 + mm) : list[pos0 + t0 + mm];
-                const int32_t b = (int32_t)((uint32_t)s % (uint32_t)m.nB);
+                const float *const *sr = srcp + mm * PW;
+                const int32_t b = tk[mm].x;
                 // two channels per lane (c, c + 32), all partner loads of a group of 8 issued before summing
                 const int c0 = lane, c1 = lane + 32;
                 const bool h0ok = c0 < Cin, h1ok = c1 < Cin;
-                auto row = [&](int32_t code) -> const float * {
-                    return code >= 0 ? newl + (size_t)code * Cin : cache + (size_t)(-(int64_t)code - 1) * Cin;
-                };
-                {
-                    const float *rr = row(sr[0]);
-                    if (h0ok) xput(mm, c0, rr[c0]);
-                    if (h1ok) xput(mm, c1, rr[c1]);
-                }
+                if (h0ok) xput(mm, c0, sr[0][c0]);
+                if (h1ok) xput(mm, c1, sr[0][c1]);
                 for (int p = 0; p < P; ++p) {
-                    const int32_t *pc = sr + 1 + p * W;
+                    const float *const *pc = sr + 1 + p * W;
                     float s0 = 0.f, s1 = 0.f;
                     for (int w0 = 0; w0 < W; w0 += 8) {
                         float va[8], vb[8];
 #pragma unroll
                         for (int u = 0; u < 8; ++u) {
-                            const int32_t q = (w0 + u < W) ? pc[w0 + u] : INT_MIN;
-                            const bool ok = q != INT_MIN;
-                            const float *rr = ok ? row(q) : cache;
-                            va[u] = (ok && h0ok) ? rr[c0] : 0.f;
-                            vb[u] = (ok && h1ok) ? rr[c1] : 0.f;
+                            const float *rr = w0 + u < W ? pc[w0 + u] : zr;
+                            va[u] = h0ok ? rr[c0] : 0.f;
+                            vb[u] = h1ok ? rr[c1] : 0.f;
                         }
 #pragma unroll
                         for (int u = 0; u < 8; ++u) { s0 += va[u]; s1 += vb[u]; }
@@ -399,10 +380,10 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                     if (h1ok) xput(mm, Cin + p * Cin + c1, s1 * inv);
                 }
                 for (int c = lane + 64; c < Cin; c += 32) {        // widths above 64 channels
-                    xput(mm, c, row(sr[0])[c]);
+                    xput(mm, c, sr[0][c]);
                     for (int p = 0; p < P; ++p) {
                         float a0 = 0.f;
-                        for (int w = 0; w < W; ++w) { const int32_t q = sr[1 + p * W + w]; if (q != INT_MIN) a0 += row(q)[c]; }
+                        for (int w = 0; w < W; ++w) a0 += sr[1 + p * W + w][c];
                         xput(mm, Cin + p * Cin + c, a0 * m.Sh_inv[b * P + p]);
                     }
                 }
@@ -680,14 +661,36 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         if (tid == 0) { atomicOr(jb.err, 4); ctl.err = 1; }
         __syncthreads();
     }
-    if (!ctl.err) {
+    }   // !same
+    }   // leader
+    csync<CLUSTER>();
+    if (CLUSTER && !leader) {                          // broadcast of the leader's control block
+        if (tid == 0) ctl = *cx.lctl;
+        __syncthreads();
+    }
+    if (ctl.same || ctl.err) {
+        if (leader && tid == 0 && ctl.same) { ++nacc; if (jb.dE_out) jb.dE_out[s_idx * jb.R + t] = 0.0; }
+        if (ctl.err) for (int p = tid + rank * nt; p < min(ctl.nl[L], m.nmax); p += nt * CL) slot[list[p]] = -1;
+        csync<CLUSTER>();
+        return;
+    }
+    // 3. layer-0 change.  With +-1 point functions on a cluster, the rows are split over its CTAs (32-row chunks),
+    //    each CTA counting into its own shared memory, and the new layer-0 rows sum the CTAs' counts through
+    //    distributed shared memory; otherwise the leader does all of it.
+    {
     const int n0 = ctl.nl[0];
-    // ball-0 entries of both flips: list position and occupancy (read once, reused by every row member)
+    const bool spread = CLUSTER && m.l0bin;
+    if (spread || leader) {
+    // ball-0 entries of both flips: list position and occupancy (read once, reused by every row member); the
+    // leader listed the sites while claiming them, the other CTAs of a cluster enumerate them again
     for (int f = 0; f < 2; ++f) {
         const int b = f ? ctl.bj : ctl.bi;
+        const int32_t *k = f ? ctl.kj : ctl.ki;
         const int q1 = m.ball_end[b * (L + 1)];
         for (int q = tid; q < q1; q += nt) {
-            const int32_t st = ent_site[f * m.w0max + q];
+            int32_t st;
+            if (leader) st = ent_site[f * m.w0max + q];
+            else { st = (int32_t)site_at(m, k, m.ball_uo + 3 * (b * m.wL + q), m.ball_b[b * m.wL + q]); ent_site[f * m.w0max + q] = st; }
             ent_pos[f * m.w0max + q] = slot[st];
             ent_sig[f * m.w0max + q] = sig[st];
         }
@@ -704,7 +707,7 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         // the rows of a channel are consecutive, so the site's own count is summed per warp and channel run.
         int32_t *dcount = reinterpret_cast<int32_t *>(dh);
         const int lane = tid & 31;
-        for (int base = tid - lane; base < Jt; base += nt) {
+        for (int base = tid - lane + (spread ? rank * nt : 0); base < Jt; base += nt * (spread ? CL : 1)) {
             const int rr = base + lane;
             int f = 0, ch = 0, csign = 0, pc = 0;
             long long wf = 0;
@@ -800,6 +803,23 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         }
     }
     __syncthreads();
+    }
+    if constexpr (CLUSTER) {
+        if (spread) {
+            csync<CLUSTER>();                              // every CTA's counts are complete
+            cg::cluster_group cluster = cg::this_cluster();
+            const int32_t *dcount = reinterpret_cast<const int32_t *>(dh);
+            float *nb0w = level_buf(jb, nb, 0);
+            for (int idx = tid + rank * nt; idx < n0 * m.C0; idx += nt * CL) {
+                const int p = idx / m.C0, c = idx % m.C0;
+                long long cnt = 0;
+                for (int q = 0; q < CL; ++q) cnt += cluster.map_shared_rank(dcount, q)[idx];
+                const int64_t s = list[p];
+                nb0w[idx] = h0[(size_t)s * m.C0 + c] + (float)((double)(cnt * m.col_wfix[c]) * kInvFix);
+            }
+        }
+    }
+    if (!spread && leader) {
     float *nb0w = level_buf(jb, nb, 0);
     if (m.l0bin) {
         const int32_t *dcount = reinterpret_cast<const int32_t *>(dh);
@@ -816,26 +836,16 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         nb0w[idx] = h0[(size_t)s * m.C0 + c] + (float)((double)(long long)dh[idx] * kInvFix);
     }
     }
-    }   // !err
-    }   // !same
-    }   // leader
-    csync<CLUSTER>();
-    if (CLUSTER && !leader) {                          // broadcast of the leader's control block
-        if (tid == 0) ctl = *cx.lctl;
-        __syncthreads();
     }
-    if (ctl.same || ctl.err) {
-        if (leader && tid == 0 && ctl.same) { ++nacc; if (jb.dE_out) jb.dE_out[s_idx * jb.R + t] = 0.0; }
-        if (ctl.err) for (int p = tid + rank * nt; p < min(ctl.nl[L], m.nmax); p += nt * CL) slot[list[p]] = -1;
-        csync<CLUSTER>();
-        return;
     }
+    csync<CLUSTER>();                                  // the new layer-0 rows are complete
     const int n0 = ctl.nl[0];
     float *nb0 = level_buf(jb, nb, 0);
     if (!leader && tid == 0) ctl.dacc = 0ull;
     __syncthreads();
     // 4. layers
     const int ncg = m.D / 4;
+    unsigned long long dloc = 0ull;                  // this thread's share of dE (fixed point)
     for (int lvl = 0; lvl < L; ++lvl) {
         const float *cache = lvl == 0 ? h0 : jb.hmid + ((size_t)(lvl - 1) * jb.R + r) * N * m.D;
         const float *newl = level_buf(jb, nb, lvl);
@@ -863,7 +873,7 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
                                 const bool active = m.Mb[st % m.nB] > 1;
                                 const float ev = active ? tot : 0.f;
                                 en[pos] = ev;
-                                atomicAdd(&ctl.dacc, (unsigned long long)llrint(((double)ev - (double)e[st]) * kFix));
+                                dloc += (unsigned long long)llrint(((double)ev - (double)e[st]) * kFix);
                             }
                         }, rank, CL, tc);
         }
@@ -875,9 +885,12 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
             for (int c = 0; c < m.C0; ++c) l0 = fmaf(nb0[(size_t)p * m.C0 + c], lin[c], l0);
             const float ev = m.Mb[s % m.nB] > 1 ? l0 : 0.f;
             en[p] = ev;
-            atomicAdd(&ctl.dacc, (unsigned long long)llrint(((double)ev - (double)e[s]) * kFix));
+            dloc += (unsigned long long)llrint(((double)ev - (double)e[s]) * kFix);
         }
     }
+    // the fixed-point partials of this thread, then of its warp, into the CTA's sum (integer: order-free)
+    for (int o = 16; o > 0; o >>= 1) dloc += __shfl_xor_sync(0xffffffffu, dloc, o);
+    if ((tid & 31) == 0 && dloc) atomicAdd(&ctl.dacc, dloc);
     __syncthreads();
     if (CLUSTER && !leader && tid == 0 && ctl.dacc) atomicAdd(&cx.lctl->dacc, ctl.dacc);   // partial dE to the leader
     csync<CLUSTER>();
@@ -975,7 +988,7 @@ struct SmemPlan {
             xb = ab > yb ? ab : yb;
         }
         p.src = al(p.X + xb);
-        p.wt = al128(p.src + sizeof(int32_t) * (size_t)TM * (1 + m.P * m.W + 6));
+        p.wt = al128(p.src + sizeof(const float *) * (size_t)TM * (1 + m.P * m.W) + sizeof(int32_t) * (size_t)TM * 6);
         p.tile_end = p.wt + (m.tc ? (size_t)kpad16(Kmax) * m.D * 2 * (m.tc_split ? 2 : 1) : 0);
         p.ent = p.tile_end;
         p.w = al(p.ent + (sizeof(int32_t) * 2 + 1) * 2 * (size_t)m.w0max);
@@ -1479,6 +1492,10 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
     chk(dup(h, d->Rv_b, nr, m.Rv_b)); chk(dup(h, d->Rv_uo, nr * 3, m.Rv_uo)); chk(dup(h, d->Rv_p, nr, m.Rv_p));
     chk(dup(h, d->Rv_m, nr, m.Rv_m)); chk(dup(h, d->Rv_loc, nr, m.Rv_loc)); chk(dup(h, d->Rv_col, (size_t)d->nB * d->J, m.Rv_col)); chk(dup(h, d->Rv_w, (size_t)d->nB * d->J, m.Rv_w));
     chk(dup(h, d->Mb, (size_t)d->nB, m.Mb)); chk(dup(h, d->theta, (size_t)(d->maxM + 1) * d->maxP * d->maxM, m.theta));
+    {
+        const std::vector<float> z((size_t)kZeroRow, 0.f);
+        chk(dup(h, z.data(), z.size(), m.zrow));
+    }
     {
         // +-1 point functions on every (M, p, species) a row can use -> exact integer layer-0 changes
         const size_t nth = (size_t)(d->maxM + 1) * d->maxP * d->maxM;

@@ -128,7 +128,7 @@ def test_metropolis_trajectory_matches_oracle(cuda, nipt_model, cluster):
 
 
 @pytest.mark.parametrize("cluster,per_sm,shipped", [(4, 1, False), (1, 2, False), (4, 2, False), (8, 2, False),
-                                                   (4, 1, True), (2, 2, True), (8, 2, True)])
+                                                   (4, 1, True), (8, 1, True)])
 def test_cluster_equals_single_cta(cuda, nipt_model, cluster, per_sm, shipped):
     """Philox stream with exchanges: a replica spread over a cluster of CTAs, and CTAs sharing an SM two by two
     (128 registers a thread), give the same trajectory as one CTA per replica; the configuration-1 network and
@@ -241,3 +241,18 @@ def test_tcgen05_split_too_wide_is_refused(cuda):
     m, _ = _model_bench_mma(3, 4, 4, 128)
     with pytest.raises(_lib.NceError, match="shared memory"):
         m.handle
+
+
+def test_two_ctas_per_sm_refused_when_too_large(cuda, nipt_model):
+    """The shipped model's tiles (73 partner rows per site) need more than half an SM's shared memory: a chunk
+    asking for two CTAs per SM fails with a message and changes nothing."""
+    torch = cuda
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.nce import NCEState
+    m, _ = _model_pkl(nipt_model[0], random_cell((4, 4, 4), 6))
+    st = NCEState(m, m.sig0[None].astype(np.int8), np.ones(1)).full_cache()
+    sig0 = st.sigma.clone()
+    with pytest.raises(_lib.NceError, match="shared memory"):
+        st.run_chunk(10, 0, seed=1, cluster=2, ctas_per_sm=2)
+    torch.cuda.synchronize()
+    assert torch.equal(st.sigma, sig0)
