@@ -107,6 +107,12 @@ __device__ __forceinline__ float act_fn(int act, float x) {
     return act == 0 ? tanhf(x) : x / (1.0f + expf(-x));
 }
 
+// the activation of the tensor-core epilogue: SiLU through the hardware exponential and division (a few ulp, far
+// below the bf16 operands' rounding; full caches and steps share it)
+__device__ __forceinline__ float act_fn_tc(int act, float x) {
+    return act == 0 ? tanhf(x) : __fdividef(x, 1.0f + __expf(-x));
+}
+
 // newbuf layout per replica: level 0 block (n0max x C0), then level l (1..depth-1) blocks (nmax x D)
 __device__ __forceinline__ float *level_buf(const NceJob &jb, float *base, int lvl) {
     if (lvl == 0) return base;
@@ -202,6 +208,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
     int32_t *tsite = reinterpret_cast<int32_t *>(srcp + TM * PW);   // the tile's sites
     float *tinv = reinterpret_cast<float *>(tsite + TM);     // 1 / |first-shell partners| of each
     int4 *tk = reinterpret_cast<int4 *>(tinv + TM);          // (basis, k0, k1, k2) of each
+    int32_t *tslot = reinterpret_cast<int32_t *>(tk + TM);   // slot-map value of each (-1: not in the field)
     // tcgen05 path: the tile is the bf16 A operand [128][Kp] (hi, then lo when split) in core-matrix layout
     const int Kp = kpad16(Kin);
     uint8_t *A0 = reinterpret_cast<uint8_t *>(X), *A1 = A0 + (size_t)128 * Kp * 2;
@@ -260,6 +267,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
             for (int u = 0; u < 4; ++u) {
                 const int idx = base + u * nt;
                 if (idx >= tm * PW) continue;
+                if (idx % PW == 0) tslot[idx / PW] = pv[u];
                 srcp[idx] = site[u] < 0 ? m.zrow
                           : (pv[u] >= 0 && pv[u] < nlev) ? newl + (size_t)pv[u] * Cin : cache + (size_t)site[u] * Cin;
             }
@@ -415,8 +423,8 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
 #pragma unroll
                 for (int i = 0; i < 16; i += 4) {
                     float4 o;
-                    o.x = act_fn(m.act, v[i] + LW.b[c0 + i]); o.y = act_fn(m.act, v[i + 1] + LW.b[c0 + i + 1]);
-                    o.z = act_fn(m.act, v[i + 2] + LW.b[c0 + i + 2]); o.w = act_fn(m.act, v[i + 3] + LW.b[c0 + i + 3]);
+                    o.x = act_fn_tc(m.act, v[i] + LW.b[c0 + i]); o.y = act_fn_tc(m.act, v[i + 1] + LW.b[c0 + i + 1]);
+                    o.z = act_fn_tc(m.act, v[i + 2] + LW.b[c0 + i + 2]); o.w = act_fn_tc(m.act, v[i + 3] + LW.b[c0 + i + 3]);
                     *reinterpret_cast<float4 *>(Y + (size_t)rrow * YS + c0 + i) = o;
                 }
             }
@@ -426,7 +434,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                 const int mm = sg + i * SG;
                 const float4 y = *reinterpret_cast<const float4 *>(Y + (size_t)mm * YS + cg * 4);
                 float v[4] = {y.x, y.y, y.z, y.w};
-                sink(mm < tm ? t0 + mm : -1, cg * 4, v);
+                sink(mm < tm ? t0 + mm : -1, cg * 4, v, tsite[mm < tm ? mm : 0], tslot[mm < tm ? mm : 0]);
             }
             __syncthreads();
             continue;
@@ -503,7 +511,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                     const int mm = sg + i * SG;
                     const float4 y = *reinterpret_cast<const float4 *>(Y + (size_t)mm * YS + cg * 4);
                     float v[4] = {y.x, y.y, y.z, y.w};
-                    sink(mm < tm ? t0 + mm : -1, cg * 4, v);
+                    sink(mm < tm ? t0 + mm : -1, cg * 4, v, tsite[mm < tm ? mm : 0], tslot[mm < tm ? mm : 0]);
                 }
             }
             __syncthreads();
@@ -552,7 +560,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                     if (LW.G) a *= 1.0f / (1.0f + expf(-g[i][q]));
                     v[q] = a;
                 }
-                sink(mm < tm ? t0 + mm : -1, cg * 4, v);
+                sink(mm < tm ? t0 + mm : -1, cg * 4, v, tsite[mm < tm ? mm : 0], tslot[mm < tm ? mm : 0]);
             }
         }
         __syncthreads();
@@ -854,20 +862,17 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
             float *outb = level_buf(jb, nb, lvl + 1);
             const int D = m.D;
             layer_tiles(jb, lvl, LWs[lvl], cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
-                        [&](int64_t pos, int c0, const float *v) {
+                        [&](int64_t pos, int c0, const float *v, int32_t, int32_t) {
                             if (pos >= 0) *reinterpret_cast<float4 *>(outb + (size_t)pos * D + c0) = make_float4(v[0], v[1], v[2], v[3]);
                         }, rank, CL, tc);
             csync<CLUSTER>();
         } else {
             layer_tiles(jb, lvl, LWs[lvl], cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
-                        [&](int64_t pos, int c0, const float *v) {
+                        [&](int64_t pos, int c0, const float *v, int32_t site, int32_t p0) {
+                            // the tile passes the site and its slot value (read while building the tile)
                             const float *hr = nullptr;
-                            int64_t st = 0;
-                            if (pos >= 0) {
-                                st = list[pos];
-                                const int p0 = slot[st];
-                                hr = (p0 >= 0 && p0 < n0) ? nb0 + (size_t)p0 * m.C0 : h0 + (size_t)st * m.C0;
-                            }
+                            const int64_t st = site;
+                            if (pos >= 0) hr = (p0 >= 0 && p0 < n0) ? nb0 + (size_t)p0 * m.C0 : h0 + (size_t)st * m.C0;
                             const float tot = site_energy(v, c0, hw, hr, lin, m.C0, ncg);
                             if (pos >= 0 && c0 == 0) {
                                 const bool active = m.Mb[st % m.nB] > 1;
@@ -988,7 +993,7 @@ struct SmemPlan {
             xb = ab > yb ? ab : yb;
         }
         p.src = al(p.X + xb);
-        p.wt = al128(p.src + sizeof(const float *) * (size_t)TM * (1 + m.P * m.W) + sizeof(int32_t) * (size_t)TM * 6);
+        p.wt = al128(p.src + sizeof(const float *) * (size_t)TM * (1 + m.P * m.W) + sizeof(int32_t) * (size_t)TM * 7);
         p.tile_end = p.wt + (m.tc ? (size_t)kpad16(Kmax) * m.D * 2 * (m.tc_split ? 2 : 1) : 0);
         p.ent = p.tile_end;
         p.w = al(p.ent + (sizeof(int32_t) * 2 + 1) * 2 * (size_t)m.w0max);
@@ -1232,11 +1237,11 @@ __global__ void __launch_bounds__(256, 1) nce_layer_all_kernel(NceJob jb, int lv
     const int D = m.D, ncg = D / 4;
     LayerW LW; LW.W = m.Wc[lvl]; LW.b = m.bias[lvl]; LW.G = m.gate ? m.G[lvl] : nullptr; LW.gb = m.gate ? m.gb[lvl] : nullptr;
     if (out) {
-        layer_tiles(jb, lvl, LW, in, nullptr, nullptr, 0, nullptr, 0, cnt, &a, X, src, [&](int64_t pos, int c0, const float *v) {
+        layer_tiles(jb, lvl, LW, in, nullptr, nullptr, 0, nullptr, 0, cnt, &a, X, src, [&](int64_t pos, int c0, const float *v, int32_t, int32_t) {
             if (pos >= 0) *reinterpret_cast<float4 *>(out + (size_t)(a + pos) * D + c0) = make_float4(v[0], v[1], v[2], v[3]);
         }, 0, 1, tcp);
     } else {
-        layer_tiles(jb, lvl, LW, in, nullptr, nullptr, 0, nullptr, 0, cnt, &a, X, src, [&](int64_t pos, int c0, const float *v) {
+        layer_tiles(jb, lvl, LW, in, nullptr, nullptr, 0, nullptr, 0, cnt, &a, X, src, [&](int64_t pos, int c0, const float *v, int32_t, int32_t) {
             const int64_t st = a + pos;
             const float tot = site_energy(v, c0, m.head_w, pos >= 0 ? h0 + (size_t)st * m.C0 : nullptr, m.lin, m.C0, ncg);
             if (pos >= 0 && c0 == 0) e_out[st] = (m.Mb[st % m.nB] > 1) ? tot : 0.f;
