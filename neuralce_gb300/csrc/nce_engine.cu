@@ -243,22 +243,27 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
             tk[mm] = make_int4(b, k[0], k[1], k[2]);
         }
         __syncthreads();
+        // item idx = mm PW + q, stepped by nt without divisions: (mm, q) advance by (nt / PW, nt % PW) with a carry
+        const int dq = nt % PW, dm = nt / PW;
+        int im = tid / PW, iq = tid % PW;
         for (int base = tid; base < tm * PW; base += 4 * nt) {
             int64_t site[4];
+            int mmu[4], qu[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                const int idx = base + u * nt;
+                mmu[u] = im; qu[u] = iq;
                 site[u] = -1;
-                if (idx < tm * PW) {
-                    const int mm = idx / PW, q = idx % PW;
-                    site[u] = tsite[mm];
-                    if (q > 0) {
-                        const int4 c = tk[mm];
+                if (base + u * nt < tm * PW) {
+                    site[u] = tsite[im];
+                    if (iq > 0) {
+                        const int4 c = tk[im];
                         const int32_t k[3] = {c.y, c.z, c.w};
-                        const int e0 = c.x * P * W + (q - 1);
+                        const int e0 = c.x * P * W + (iq - 1);
                         site[u] = m.Sh_m[e0] ? site_at(m, k, m.Sh_uo + 3 * e0, m.Sh_b[e0]) : -1;
                     }
                 }
+                iq += dq; im += dm;
+                if (iq >= PW) { iq -= PW; ++im; }
             }
             int32_t pv[4];
 #pragma unroll
@@ -267,7 +272,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
             for (int u = 0; u < 4; ++u) {
                 const int idx = base + u * nt;
                 if (idx >= tm * PW) continue;
-                if (idx % PW == 0) tslot[idx / PW] = pv[u];
+                if (qu[u] == 0) tslot[mmu[u]] = pv[u];
                 srcp[idx] = site[u] < 0 ? m.zrow
                           : (pv[u] >= 0 && pv[u] < nlev) ? newl + (size_t)pv[u] * Cin : cache + (size_t)site[u] * Cin;
             }
