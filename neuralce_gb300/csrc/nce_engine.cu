@@ -113,10 +113,12 @@ __device__ __forceinline__ float act_fn_tc(int act, float x) {
     return act == 0 ? tanhf(x) : __fdividef(x, 1.0f + __expf(-x));
 }
 
-// newbuf layout per replica: level 0 block (n0max x C0), then level l (1..depth-1) blocks (nmax x D)
+// newbuf layout per replica: level 0 block (n0max x C0, rounded up to 4 floats so that every later block and
+// replica starts on 16 bytes for float4 rows), then level l (1..depth-1) blocks (nmax x D)
+__host__ __device__ __forceinline__ size_t l0_floats(const NceDev &m) { return ((size_t)m.n0max * m.C0 + 3) & ~(size_t)3; }
 __device__ __forceinline__ float *level_buf(const NceJob &jb, float *base, int lvl) {
     if (lvl == 0) return base;
-    return base + (size_t)jb.m.n0max * jb.m.C0 + (size_t)(lvl - 1) * jb.m.nmax * jb.m.D;
+    return base + l0_floats(jb.m) + (size_t)(lvl - 1) * jb.m.nmax * jb.m.D;
 }
 
 struct NceCtl {
@@ -823,12 +825,15 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
             cg::cluster_group cluster = cg::this_cluster();
             const int32_t *dcount = reinterpret_cast<const int32_t *>(dh);
             float *nb0w = level_buf(jb, nb, 0);
-            for (int idx = tid + rank * nt; idx < n0 * m.C0; idx += nt * CL) {
-                const int p = idx / m.C0, c = idx % m.C0;
-                long long cnt = 0;
-                for (int q = 0; q < CL; ++q) cnt += cluster.map_shared_rank(dcount, q)[idx];
-                const int64_t s = list[p];
-                nb0w[idx] = h0[(size_t)s * m.C0 + c] + (float)((double)(cnt * m.col_wfix[c]) * kInvFix);
+            const int lane = tid & 31, gw = (tid >> 5) + rank * (nt >> 5), nw = (nt >> 5) * CL;
+            for (int p = gw; p < n0; p += nw) {
+                const float *hrow = h0 + (size_t)list[p] * m.C0;
+                for (int c = lane; c < m.C0; c += 32) {
+                    const int idx = p * m.C0 + c;
+                    long long cnt = 0;
+                    for (int q = 0; q < CL; ++q) cnt += cluster.map_shared_rank(dcount, q)[idx];
+                    nb0w[idx] = hrow[c] + (float)((double)(cnt * m.col_wfix[c]) * kInvFix);
+                }
             }
         }
     }
@@ -924,17 +929,22 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
     const int nL = ctl.nl[L];
     const int ts = tid + rank * nt, tstr = nt * CL;
     if (acc_flag) {
-        for (int idx = ts; idx < n0 * m.C0; idx += tstr) {
-            const int p = idx / m.C0, c = idx % m.C0;
-            h0[(size_t)list[p] * m.C0 + c] = nb0[idx];
+        // a warp per row over the cluster's warps: the row's site read once, columns by lanes (float4 for D)
+        const int lane = tid & 31, gw = (tid >> 5) + rank * (nt >> 5), nw = (nt >> 5) * CL;
+        for (int p = gw; p < n0; p += nw) {
+            float *dst = h0 + (size_t)list[p] * m.C0;
+            const float *srow = nb0 + (size_t)p * m.C0;
+            for (int c = lane; c < m.C0; c += 32) dst[c] = srow[c];
         }
+        const int D4 = m.D / 4;
         for (int lvl = 1; lvl < L; ++lvl) {
             float *hm = jb.hmid + ((size_t)(lvl - 1) * jb.R + r) * N * m.D;
             const float *src = level_buf(jb, nb, lvl);
             const int nl = ctl.nl[lvl];
-            for (int idx = ts; idx < nl * m.D; idx += tstr) {
-                const int p = idx / m.D, c = idx % m.D;
-                hm[(size_t)list[p] * m.D + c] = src[idx];
+            for (int p = gw; p < nl; p += nw) {
+                float4 *dst = reinterpret_cast<float4 *>(hm + (size_t)list[p] * m.D);
+                const float4 *srow = reinterpret_cast<const float4 *>(src + (size_t)p * m.D);
+                for (int c = lane; c < D4; c += 32) dst[c] = srow[c];
             }
         }
         for (int p = ts; p < nL; p += tstr) e[list[p]] = en[p];
@@ -1325,7 +1335,7 @@ static int ensure_scratch(nce_nce_model *h, int32_t R) {
     if (h->R_alloc >= R) return NCE_OK;
     for (void *p : {(void *)h->slot, (void *)h->list, (void *)h->newbuf, (void *)h->e_new}) if (p) cudaFree(p);
     const NceDev &m = h->dev;
-    h->stride = (int64_t)m.n0max * m.C0 + (int64_t)std::max(0, m.depth - 1) * m.nmax * m.D;
+    h->stride = (int64_t)l0_floats(m) + (int64_t)std::max(0, m.depth - 1) * m.nmax * m.D;
     NCE_CUDA(cudaMalloc((void **)&h->slot, sizeof(int32_t) * (size_t)R * m.N));
     NCE_CUDA(cudaMemset(h->slot, 0xFF, sizeof(int32_t) * (size_t)R * m.N));
     NCE_CUDA(cudaMalloc((void **)&h->list, sizeof(int32_t) * (size_t)R * m.nmax));
