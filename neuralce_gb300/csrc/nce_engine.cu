@@ -232,6 +232,20 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
             X[(size_t)ms * XS + k] = v;
         }
     };
+    // channels k, k + 1 (k even): one 4-byte bf16 pair on the tcgen05 path
+    auto xput2 = [&](int ms, int k, float v0, float v1) {
+        if (tc) {
+            const uint32_t off = umma::core_off(ms, k, Kp);
+            const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+            *reinterpret_cast<__nv_bfloat162 *>(A0 + off) = h;
+            if (m.tc_split) {
+                const float2 hf = __bfloat1622float2(h);
+                *reinterpret_cast<__nv_bfloat162 *>(A1 + off) = __floats2bfloat162_rn(v0 - hf.x, v1 - hf.y);
+            }
+        } else {
+            X[(size_t)ms * XS + k] = v0; X[(size_t)ms * XS + k + 1] = v1;
+        }
+    };
     for (int64_t t0 = (int64_t)tile_begin * TM; t0 < cnt; t0 += (int64_t)tile_stride * TM) {
         const int tm = (int)min((int64_t)TM, cnt - t0);
         // 1) the tile's sites and their first shell's 1/|partners| into shared memory, then the source row of each
@@ -283,23 +297,23 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
         // 2) X = [h | masked shell means] of the tile's sites: lanes over channels (coalesced rows); masked
         //    partners read the zero row, so every sum runs over all W slots in order
         const float *zr = m.zrow;
-        if (P == 1 && W <= 12 && Cin <= 64) {
-            // one shell of at most 12 partners: two sites per warp with all 2 x 13 rows' loads in flight at once
+        if (P == 1 && W <= 12 && Cin <= 64 && (Cin & 1) == 0) {
+            // one shell of at most 12 partners: two sites per warp with all 2 x 13 rows' loads in flight at once;
+            // a lane takes the channel pair (2 lane, 2 lane + 1) as one 8-byte load
             const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
-            const int c0 = lane, c1 = lane + 32;
-            const bool h0ok = c0 < Cin, h1ok = c1 < Cin;
+            const int c0 = 2 * lane;
+            const bool ok = c0 < Cin;
             for (int mm = warp; mm < tm; mm += 2 * nwarp) {
                 const int mb = mm + nwarp;
                 const bool two = mb < tm;
-                float va[2][13], vb[2][13];
+                float2 v[2][13];
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const float *const *sr = srcp + (two ? (h ? mb : mm) : mm) * PW;
 #pragma unroll
                     for (int u = 0; u < 13; ++u) {
                         const float *rr = u <= W ? sr[u] : zr;
-                        va[h][u] = h0ok ? rr[c0] : 0.f;
-                        vb[h][u] = h1ok ? rr[c1] : 0.f;
+                        v[h][u] = ok ? *reinterpret_cast<const float2 *>(rr + c0) : make_float2(0.f, 0.f);
                     }
                 }
 #pragma unroll
@@ -308,10 +322,9 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                     const int ms = h ? mb : mm;
                     float s0 = 0.f, s1 = 0.f;
 #pragma unroll
-                    for (int u = 1; u < 13; ++u) { s0 += va[h][u]; s1 += vb[h][u]; }
+                    for (int u = 1; u < 13; ++u) { s0 += v[h][u].x; s1 += v[h][u].y; }
                     const float inv = tinv[ms];
-                    if (h0ok) { xput(ms, c0, va[h][0]); xput(ms, Cin + c0, s0 * inv); }
-                    if (h1ok) { xput(ms, c1, vb[h][0]); xput(ms, Cin + c1, s1 * inv); }
+                    if (ok) xput2(ms, c0, v[h][0].x, v[h][0].y), xput2(ms, Cin + c0, s0 * inv, s1 * inv);
                 }
             }
         } else if (P == 1 && W <= 12 && Cin <= 128) {
