@@ -9,9 +9,13 @@ the whole job is 40 such steps.  Proposals come from the device Philox stream.
   value     swap attempts/s with the state resident in HBM, CUDA events around each chunk on its stream,
             L2 flushed (256 MB write) between timed chunks outside the events
   e2e       the same chunks through nce_ce_run_chunk_host: pinned host buffers in and out every chunk
-  roofline  dominant kernel ce_pt_chunk_kernel; algorithmic bytes per attempt = 14,996 B of int8
-            member-occupancy reads (2 x 7,498 member slots of the rows of both sites)
+  roofline  dominant kernel ce_bin_chunk_kernel (sign-parity form); algorithmic bytes per attempt = 14,996 B
+            of int8 member-occupancy reads (2 x 7,498 member slots of the rows of both sites)
   cpu_baseline  the oracle's C restatement on the host cores (bounded sample, all threads)
+  side lines  nce (configuration 1, float32), nce_tcgen05_split / nce_tcgen05_bf16 (the same on tcgen05
+            tensor cores), nce_shipped_model (the reference's shipped PtNi model on the same cell), batch
+            (configuration 2), serve (configuration 4, scaled)
+--workload nce | nce-shipped | ce-batch | ce-large | nce-large | serve | ce-energy prints one of them alone.
 --impl reference times the oracle port on the host cores (the reference's own CPU paths, JAX and icet,
 are not installed on this image) with the same metric.
 """
