@@ -123,6 +123,26 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def bf16_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return json.load(open(p))["bf16_tflops"], "measured"
+    return 1900.0, "fallback"
+
+
+def nce_flops_per_attempt(m):
+    """Layer-contraction FLOPs of one attempt, upper bound before the two flips' receptive fields are merged:
+    2 flops x sum over layers l = 1..depth of 2 ball_l sites x ((1 + P) Cin_l) x D (exact ball sizes of the
+    cell's tables; basis 0)."""
+    ends = [int(x) for x in m.keep["ball_end"][0]]
+    P = int(m.geo["P"])
+    f = 0
+    for lvl in range(1, m.depth + 1):
+        cin = m.C0 if lvl == 1 else m.D
+        f += 2 * ends[lvl] * (1 + P) * cin * m.D
+    return 2 * f
+
+
 def cpu_oracle_rate(L, R, target_s=10.0, threads=None):
     """attempts/s of the C oracle on the host cores for the same workload (bounded sample)."""
     from neuralce_gb300.workloads import ce_config, ladder, replica_configs
@@ -226,12 +246,18 @@ def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, step
     net = ("the reference's shipped PtNi model (depth 1, width 16, 3 shells, sigmoid gate, tanh, mean readout)" if shipped
            else f"depth {depth}, width {width}, SiLU, sum readout, 12-NN shell")
     value = R * chunk * steps / tot
+    flops = nce_flops_per_attempt(m)
+    pk, src = bf16_peak()
+    roof = {"bound": "tensor", "achieved": value * flops / 1e12, "peak": pk, "unit": "TFLOP/s",
+            "frac": value * flops / 1e12 / pk, "traffic": None, "peak_source": src, "flops_per_attempt": flops,
+            "note": "layer contractions only, against the measured dense bf16 peak; the step is bound by the "
+                    "receptive-field gathers and per-level barriers of the Markov chain"}
     return {"value": value, "unit": "swap attempts/s", "ms_per_step": float(np.mean(ms)),
             "config": f"NeuralCE: {m.N} sites, R={R}, {net}, "
                       f"chunk {chunk} steps + {max(chunk // exchange_every, 1)} exchange rounds, re-anchor every {anchor} chunks",
             "vs_h100_published_144636": (value / 144_636) if (shipped and m.N == 2048 and R == 32) else None,
             "receptive_field": [int(x) for x in m.keep['ball_end'][0]], "accept_rate": float(st.n_acc.sum().item()) / (R * step),
-            "ctas_per_replica": cluster, "ctas_per_sm": per_sm, "autotune_ms": tune,
+            "ctas_per_replica": cluster, "ctas_per_sm": per_sm, "autotune_ms": tune, "roofline": roof,
             "contractions": CONTRACTIONS[mma]}
 
 
