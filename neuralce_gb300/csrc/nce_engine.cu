@@ -145,6 +145,8 @@ __host__ __device__ __forceinline__ int tile_tm(int D, int tc = 0, int mma = 0) 
     return tc ? 128 : (mma ? 4 : (SG >= 64 ? 2 : 4)) * SG;
 }
 __host__ __device__ __forceinline__ int kpad16(int k) { return (k + 15) & ~15; }
+// float32 tile row stride: a multiple of 4 floats (16-byte rows for float4 reads along K) above Kin
+__host__ __device__ __forceinline__ int x_stride(int kin) { return (kin + 4) & ~3; }
 
 // tensor-memory accumulator, completion mbarrier and the staged B operand of the tcgen05 tile path; `phase` is the
 // parity of the next completion (every thread of the CTA keeps the same count)
@@ -200,7 +202,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                             int32_t *src, Sink sink, int tile_begin = 0, int tile_stride = 1, TcCtx *tc = nullptr) {
     const NceDev &m = jb.m;
     const int Cin = lvl == 0 ? m.C0 : m.D, D = m.D, P = m.P, W = m.W;
-    const int Kin = (1 + P) * Cin, XS = Kin + 1;
+    const int Kin = (1 + P) * Cin, XS = x_stride(Kin);
     const int tid = threadIdx.x, nt = blockDim.x;
     const int ncg = D / 4, SG = 256 / ncg, TM = tile_tm(D, tc != nullptr, m.mma), MS = TM / SG;
     const int cg = tid % ncg, sg = tid / ncg;
@@ -549,15 +551,25 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
         // rows sg + i SG, i < MS (MS = 2: the last two micro-tile rows repeat the first two and are not used)
         const float *x0 = X + (size_t)sg * XS, *x1 = x0 + (size_t)SG * XS;
         const float *x2 = MS > 2 ? x1 + (size_t)SG * XS : x0, *x3 = MS > 2 ? x2 + (size_t)SG * XS : x1;
-#pragma unroll 4
-        for (int kk = 0; kk < Kin; ++kk) {
-            const float4 w4 = *reinterpret_cast<const float4 *>(LW.W + (size_t)kk * D + cg * 4);
-            const float v0 = x0[kk], v1 = x1[kk], v2 = x2[kk], v3 = x3[kk];
+        auto fma16 = [&](float v0, float v1, float v2, float v3, const float4 w4) {
             o[0][0] = fmaf(v0, w4.x, o[0][0]); o[0][1] = fmaf(v0, w4.y, o[0][1]); o[0][2] = fmaf(v0, w4.z, o[0][2]); o[0][3] = fmaf(v0, w4.w, o[0][3]);
             o[1][0] = fmaf(v1, w4.x, o[1][0]); o[1][1] = fmaf(v1, w4.y, o[1][1]); o[1][2] = fmaf(v1, w4.z, o[1][2]); o[1][3] = fmaf(v1, w4.w, o[1][3]);
             o[2][0] = fmaf(v2, w4.x, o[2][0]); o[2][1] = fmaf(v2, w4.y, o[2][1]); o[2][2] = fmaf(v2, w4.z, o[2][2]); o[2][3] = fmaf(v2, w4.w, o[2][3]);
             o[3][0] = fmaf(v3, w4.x, o[3][0]); o[3][1] = fmaf(v3, w4.y, o[3][1]); o[3][2] = fmaf(v3, w4.z, o[3][2]); o[3][3] = fmaf(v3, w4.w, o[3][3]);
+        };
+        // four K at a time: one 16-byte read of each site row, the same fma order as one K at a time
+        int kk = 0;
+        for (; kk + 4 <= Kin; kk += 4) {
+            const float4 a0 = *reinterpret_cast<const float4 *>(x0 + kk), a1 = *reinterpret_cast<const float4 *>(x1 + kk);
+            const float4 a2 = *reinterpret_cast<const float4 *>(x2 + kk), a3 = *reinterpret_cast<const float4 *>(x3 + kk);
+            const float *wk = LW.W + (size_t)kk * D + cg * 4;
+            fma16(a0.x, a1.x, a2.x, a3.x, *reinterpret_cast<const float4 *>(wk));
+            fma16(a0.y, a1.y, a2.y, a3.y, *reinterpret_cast<const float4 *>(wk + D));
+            fma16(a0.z, a1.z, a2.z, a3.z, *reinterpret_cast<const float4 *>(wk + 2 * D));
+            fma16(a0.w, a1.w, a2.w, a3.w, *reinterpret_cast<const float4 *>(wk + 3 * D));
         }
+        for (; kk < Kin; ++kk)
+            fma16(x0[kk], x1[kk], x2[kk], x3[kk], *reinterpret_cast<const float4 *>(LW.W + (size_t)kk * D + cg * 4));
         if (LW.G) {
 #pragma unroll 4
             for (int kk = Cin; kk < Kin; ++kk) {
@@ -1015,7 +1027,7 @@ struct SmemPlan {
         // layer-0 change per (site, channel): int32 counts for +-1 point functions, int64 fixed point otherwise
         p.dh = 0; p.dh_bytes = with_dh ? al((m.l0bin ? sizeof(int32_t) : sizeof(unsigned long long)) * (size_t)m.n0max * m.C0) : 0;
         p.X = al128(p.dh_bytes);
-        size_t xb = sizeof(float) * (size_t)TM * (Kmax + 1);
+        size_t xb = sizeof(float) * (size_t)TM * x_stride(Kmax);
         if (m.tc) {
             const size_t ab = (size_t)128 * kpad16(Kmax) * 2 * (m.tc_split ? 2 : 1), yb = sizeof(float) * 128 * (size_t)(m.D + 4);
             xb = ab > yb ? ab : yb;
