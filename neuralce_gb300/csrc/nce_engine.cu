@@ -782,10 +782,8 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
                         }
                         po ^= (unsigned)(d >> (20 + so)) & 1u; pn ^= (unsigned)(d >> (20 + sn)) & 1u;
                     }
-                    if (po != pn) {
-                        const long long fx = pn ? -wf : wf;         // new product -1: (pn - po) w = -2 w
+                    if (po != pn) {                                  // new product -1: (pn - po) w = -2 w
                         ch = m.Rv_col[e] + 1;
-                        (void)fx;
                         for (int mm = 0; mm < m.mo; ++mm) {
                             if (!((dsc[mm] >> 16) & 1)) continue;
                             const int p = pos[mm];
@@ -1119,7 +1117,6 @@ __global__ void __launch_bounds__(256, MINB) nce_chunk_cluster_kernel(const __gr
 }
 
 // ── full cache ─────────────────────────────────────────────────────────────────────────────────────
-// h0 by pulling every reverse row of each site (deterministic), standardised, float32
 // Layer 0 of every site, bit-sliced (+-1 point functions): one plane per basis holds the sign bit of each site,
 // each (k0, k1) row twice over (2 d2 bits) so that any offset in [0, d2) reads 32 consecutive bits.  A thread takes
 // 32 consecutive sites along k2 and, for every reverse row of their basis (all slots: every cluster instance that
@@ -1225,6 +1222,8 @@ __global__ void __launch_bounds__(128) nce_h0_bits_kernel(NceDev m, const uint32
     for (int c = ch_cur + 1; c < C0; ++c) flush(c, 0);
 }
 
+// Layer 0 of every site for general point functions: every reverse row of each site pulled in float64 (fixed
+// order, deterministic), standardised, float32
 __global__ void nce_h0_kernel(NceDev m, const int8_t *sigma, int32_t R, float *h0) {
     const int64_t total = (int64_t)R * m.N;
     for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (int64_t)gridDim.x * blockDim.x) {
