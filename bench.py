@@ -706,8 +706,9 @@ def main():
     ms_chunk = float(np.mean(per_ms))
     achieved = R * T * B_GATHER / (ms_chunk / 1e3) / 1e9
     # DRAM bytes per launch from one ncu capture of this workload (dram__bytes_read.sum + dram__bytes_write.sum of
-    # ce_bin_chunk_kernel, 2,048 sites, R = 32, 5,000 steps): the tables and occupancies live in shared memory
-    traffic = 139_776 if (args.L == 8 and args.R == 32 and T == 5000 and args.path == 2) else None
+    # ce_bin_chunk_kernel, 2,048 sites, R = 32, 5,000 steps, 16 warps x 8 CTAs): the tables and occupancies live in
+    # shared memory
+    traffic = 155_392 if (args.L == 8 and args.R == 32 and T == 5000 and args.path == 2) else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
             "kernel": {1: "ce_pt_chunk_kernel", 3: "ce_bin2_chunk_kernel"}.get(args.path, "ce_bin_chunk_kernel"),
             "peak_source": src,
