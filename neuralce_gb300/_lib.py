@@ -144,6 +144,22 @@ def check(rc, what=""):
         raise NceError(f"{what}: status {rc}: {buf.value.decode(errors='replace')}")
 
 
+CE_ERROR_FLAGS = {1: "a proposal index was out of range (the move was rejected)",
+                  2: "a delta query was out of range (NaN returned)"}
+NCE_ERROR_FLAGS = {1: "a proposal index was out of range", 4: "a receptive field exceeded its tables",
+                   8: "a row member was outside the layer-0 ball", 32: "a tensor-core completion wait timed out"}
+
+
+def raise_device_errors(fn, handle, table, what):
+    """Read and clear a model handle's device error word (``nce_ce_errors`` / ``nce_nce_errors``); raise NceError
+    naming every flag that was set."""
+    f = C.c_int32(0)
+    check(fn(handle, C.byref(f)), what)
+    if f.value:
+        names = "; ".join(t for b, t in table.items() if f.value & b) or "unknown flag"
+        raise NceError(f"{what}: device error flags 0x{f.value:x}: {names}")
+
+
 def ptr(x):
     """device/host address of a torch tensor or numpy array (None -> NULL)."""
     if x is None:

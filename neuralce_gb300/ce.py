@@ -155,6 +155,10 @@ class GPUClusterExpansion:
         basis, _, _, _ = site_decompose(prim.cell, prim.frac, structure.cell, structure.positions)
         return encode_species(self.cs, structure, basis)[self.perm]
 
+    def check_errors(self):
+        """Raise NceError if a kernel on this model flagged an error since the last check (and clear the flags)."""
+        _lib.raise_device_errors(_lib.lib().nce_ce_errors, self.handle, _lib.CE_ERROR_FLAGS, "CE kernels")
+
     # ── energies ──
     def _sigma_dev(self, sigma):
         import torch

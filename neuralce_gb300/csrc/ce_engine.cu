@@ -1898,6 +1898,19 @@ static int noalloc_partials(double **out) {
 }
 }  // namespace nce
 
+namespace nce {
+int ce_error_peek(nce_ce_handle h, int32_t *flags) {
+    NCE_CHECK(h && flags, "ce_error_peek: null argument");
+    NCE_CUDA(cudaMemcpy(flags, h->err, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return NCE_OK;
+}
+const char *ce_error_text(int32_t f) {
+    if (f & 2) return "a delta query was out of range (NaN returned)";
+    if (f & 1) return "a proposal index was out of range (the move was rejected)";
+    return "no error";
+}
+}  // namespace nce
+
 extern "C" {
 
 int nce_ce_energy_noalloc(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t precision, double *E, void *stream) {

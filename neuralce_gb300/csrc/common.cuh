@@ -27,6 +27,13 @@ struct StreamScratch {
     ~StreamScratch() { if (p) cudaFreeAsync(p, s); }
 };
 
+// device error flags of a model handle without clearing them (the job server checks them when a job ends), and
+// the text of a flag word
+int ce_error_peek(nce_ce_handle h, int32_t *flags);
+int nce_error_peek(nce_nce_handle h, int32_t *flags);
+const char *ce_error_text(int32_t flags);
+const char *nce_error_text(int32_t flags);
+
 // shapes of a model handle, for the job server's memory accounting
 int ce_model_dims(nce_ce_handle h, int64_t *N, int32_t *n_cols, int32_t *mo, int32_t *binary);
 int nce_model_dims(nce_nce_handle h, int64_t *N, int32_t *C0, int32_t *D, int32_t *depth);

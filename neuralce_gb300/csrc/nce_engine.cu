@@ -1439,6 +1439,21 @@ __global__ void __launch_bounds__(128) nce_tc_gemm_kernel(const float *A, const 
 
 }  // namespace nce
 
+namespace nce {
+int nce_error_peek(nce_nce_handle h, int32_t *flags) {
+    NCE_CHECK(h && flags, "nce_error_peek: null argument");
+    NCE_CUDA(cudaMemcpy(flags, h->err, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return NCE_OK;
+}
+const char *nce_error_text(int32_t f) {
+    if (f & 32) return "a tensor-core completion wait timed out";
+    if (f & 8) return "a row member was outside the layer-0 ball";
+    if (f & 4) return "a receptive field exceeded its tables";
+    if (f & 1) return "a proposal index was out of range";
+    return "no error";
+}
+}  // namespace nce
+
 extern "C" {
 
 int nce_tc_gemm(const float *A, const float *B, float *C, int32_t M, int32_t N, int32_t K, int32_t split, void *stream) {

@@ -245,6 +245,14 @@ int finish(SJob &j, cudaStream_t s) {
     if (j.d.n_ex_out) NCE_CUDA(cudaMemcpyAsync(j.d.n_ex_out, nx, 8, cudaMemcpyDeviceToHost, s));
     NCE_CUDA(cudaFreeAsync(j.dev, s));
     NCE_CUDA(cudaStreamSynchronize(s));
+    // a device error flag on the job's model fails the job (the flags stay set for the model's other jobs)
+    int32_t flags = 0;
+    const int rc = ce ? ce_error_peek((nce_ce_handle)j.d.model, &flags) : nce_error_peek((nce_nce_handle)j.d.model, &flags);
+    if (rc) return rc;
+    if (flags) {
+        const int code = (flags & 32) ? NCE_ERR_TIMEOUT : NCE_ERR_INVALID;
+        return fail(code, "device error flags 0x%x on the job's model: %s", flags, ce ? ce_error_text(flags) : nce_error_text(flags));
+    }
     return NCE_OK;
 }
 

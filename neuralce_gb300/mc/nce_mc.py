@@ -169,6 +169,7 @@ def _run_replicas(mc, betas, n_steps, seed, chunk, log_every, sample_interval, o
                      drift_log=np.array(drift_log, np.float64), traj=(traj[0] if traj else np.zeros((R, 0))),
                      cfg_betas=betas.astype(np.float64), **{"cfg_" + k: v for k, v in want.items()})
             os.replace(ck_path + ".tmp.npz", ck_path)
+    st.model.check_errors()                               # device error flags raise here
     wall = time.time() - t0
     os.makedirs(out_dir, exist_ok=True)
     E_chunk = np.array(E_chunk); acc_chunk = np.array(acc_chunk); traj = np.concatenate(traj, axis=1)

@@ -181,6 +181,10 @@ class NCEModel:
             self._handle = h
         return self._handle
 
+    def check_errors(self):
+        """Raise NceError if a kernel on this model flagged an error since the last check (and clear the flags)."""
+        _lib.raise_device_errors(_lib.lib().nce_nce_errors, self.handle, _lib.NCE_ERROR_FLAGS, "NeuralCE kernels")
+
     def close(self):
         if self._handle is not None:
             _lib.lib().nce_nce_destroy(self._handle)

@@ -316,6 +316,7 @@ def run_pt_mcmc(gce, cfg: MCMCConfig, verbose=True):
                      cfg_temps=temps, cfg_run_id=str(cfg.run_id or ""))
             os.replace(ck_path + ".tmp.npz", ck_path)
     torch.cuda.synchronize()
+    gce.check_errors()                                    # device error flags raise here, as the reference's errors
     wall = time.time() - t0
     n_sw = cfg.n_steps * n_total
     pairs = (n_per // 2) * n_ladders

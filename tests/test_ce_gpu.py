@@ -323,3 +323,30 @@ def test_sharded_runner_equals_device_exchange(cuda):
     assert torch.equal(a.sigma, b.sigma) and torch.allclose(a.E, b.E, rtol=0, atol=1e-9)
     assert np.array_equal(a.rep_of_slot.cpu().numpy(), shard.rep_of_slot)
     assert int(a.n_ex.item()) == shard.n_ex > 0
+
+
+@pytest.mark.parametrize("path", [1, 2])
+def test_out_of_range_proposal_is_rejected_and_reported(cuda, path):
+    """A host proposal naming a site outside the cell is rejected by the kernel's own bounds check (the chain
+    continues as if the two sites had the same species) and reported: check_errors raises NceError once, naming
+    the flag, and clears it."""
+    torch = cuda
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.ce import proposal_stream
+    from neuralce_gb300.pt import run_chunk
+    R, T = 4, 200
+    gce, orc, sig_r, beta = _setup(4, seed=5, R=R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    pa, pb, pu = proposal_stream(gce, R, T, seed=3)
+    bad_a = pa.copy(); bad_a[17, 2] = gce.n_atoms                 # one entry one past the last site
+    a = _engine_state(sig_r, E0, beta); b = _engine_state(sig_r, E0, beta)
+    same_b = pb.copy(); same_b[17, 2] = pa[17, 2]                  # the rejected move, written as a same-site draw
+    run_chunk(gce, a, T, 0, 0, 64, 8, tuple(torch.as_tensor(x).cuda() for x in (bad_a, pb, pu)), path=path)
+    torch.cuda.synchronize()
+    with pytest.raises(_lib.NceError, match="proposal index was out of range"):
+        gce.check_errors()
+    gce.check_errors()                                             # cleared
+    run_chunk(gce, b, T, 0, 0, 64, 8, tuple(torch.as_tensor(x).cuda() for x in (pa, same_b, pu)), path=path)
+    torch.cuda.synchronize()
+    gce.check_errors()
+    assert torch.equal(a.sigma, b.sigma) and torch.equal(a.E, b.E)

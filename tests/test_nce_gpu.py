@@ -256,3 +256,32 @@ def test_two_ctas_per_sm_refused_when_too_large(cuda, nipt_model):
         st.run_chunk(10, 0, seed=1, cluster=2, ctas_per_sm=2)
     torch.cuda.synchronize()
     assert torch.equal(st.sigma, sig0)
+
+
+def test_out_of_range_proposal_is_reported(cuda):
+    """A host proposal naming a site outside the cell is turned into a no-op by the kernel's bounds check and
+    reported: check_errors raises NceError once, naming the flag, and clears it; the chain equals the one where
+    that proposal picks the same site twice."""
+    torch = cuda
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.nce import NCEState
+    from neuralce_gb300.workloads import ladder, replica_configs
+    m, _ = _model_bench(3, 9)
+    R, T = 3, 30
+    _, beta = ladder(R)
+    sig = replica_configs(m.sig0, R, 4)
+    rng = np.random.default_rng(2)
+    pi = rng.integers(0, m.N, (T, R)).astype(np.int32); pj = rng.integers(0, m.N, (T, R)).astype(np.int32)
+    pu = 1.0 - rng.random((T, R))
+    bad = pi.copy(); bad[11, 1] = m.N
+    same = pj.copy(); same[11, 1] = pi[11, 1]
+    a = NCEState(m, sig, beta).full_cache(); b = NCEState(m, sig, beta).full_cache()
+    a.run_chunk(T, 0, proposals=tuple(torch.as_tensor(x).cuda() for x in (bad, pj, pu)))
+    torch.cuda.synchronize()
+    with pytest.raises(_lib.NceError, match="proposal index was out of range"):
+        m.check_errors()
+    m.check_errors()
+    b.run_chunk(T, 0, proposals=tuple(torch.as_tensor(x).cuda() for x in (pi, same, pu)))
+    torch.cuda.synchronize()
+    m.check_errors()
+    assert torch.equal(a.sigma, b.sigma) and torch.equal(a.E, b.E) and torch.equal(a.n_acc, b.n_acc)
