@@ -683,14 +683,27 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
             const int b = f ? ctl.bj : ctl.bi;
             const int32_t *k = f ? ctl.kj : ctl.ki;
             const int q0 = lvl ? m.ball_end[b * (L + 1) + lvl - 1] : 0, q1 = m.ball_end[b * (L + 1) + lvl];
-            for (int q = q0 + tid; q < q1; q += nt) {
-                const int e0 = b * m.wL + q;
-                const int64_t s = site_at(m, k, m.ball_uo + 3 * e0, m.ball_b[e0]);
-                if (lvl == 0) ent_site[f * m.w0max + q] = (int32_t)s;
-                if (atomicCAS(&slot[s], -1, -2) == -1) {
-                    const int p = atomicAdd(&ctl.cnt, 1);
-                    list[p] = (int32_t)s; slot[s] = p;
+            // four offsets per thread with their claims (global compare-and-swap) in flight together
+            for (int q = q0 + tid; q < q1; q += 4 * nt) {
+                int32_t sq[4], won[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int qq = q + u * nt;
+                    sq[u] = -1;
+                    if (qq < q1) {
+                        const int e0 = b * m.wL + qq;
+                        sq[u] = (int32_t)site_at(m, k, m.ball_uo + 3 * e0, m.ball_b[e0]);
+                        if (lvl == 0) ent_site[f * m.w0max + qq] = sq[u];
+                    }
                 }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) won[u] = sq[u] >= 0 && atomicCAS(&slot[sq[u]], -1, -2) == -1;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (won[u]) {
+                        const int p = atomicAdd(&ctl.cnt, 1);
+                        list[p] = sq[u]; slot[sq[u]] = p;
+                    }
             }
         }
         __syncthreads();
