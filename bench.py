@@ -215,7 +215,7 @@ def bench_nce(L=8, R=32, depth=3, width=64, chunk=1000, exchange_every=100, step
         from neuralce_gb300 import _lib
         from neuralce_gb300.nce import NCEState as _S
         tune = {}
-        for cl, ps in ((1, 1), (2, 1), (4, 1), (2, 2), (4, 2), (8, 2)):
+        for cl, ps in ((1, 1), (2, 1), (4, 1), (8, 1), (2, 2), (4, 2), (8, 2)):
             sc = _S(m, replica_configs(sig, R, 1 + seed), beta).full_cache()
             try:
                 sc.run_chunk(4, 0, seed=1, cluster=cl, ctas_per_sm=ps)
