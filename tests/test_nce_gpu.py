@@ -285,3 +285,44 @@ def test_out_of_range_proposal_is_reported(cuda):
     torch.cuda.synchronize()
     m.check_errors()
     assert torch.equal(a.sigma, b.sigma) and torch.equal(a.E, b.E) and torch.equal(a.n_acc, b.n_acc)
+
+
+def _ternary_model(seed=1, mma=0):
+    from neuralce_gb300.ce_tables import ClusterSpace
+    from neuralce_gb300.io import Z_OF, fcc_conventional, fcc_primitive
+    from neuralce_gb300.nce import NCEModel, synthetic_model
+    from oracle.nce_oracle import NCEOracle
+    cs = ClusterSpace.build(fcc_primitive(3.924, ("Ni", "Pt", "Cu")), [6.0, 4.5])
+    s = fcc_conventional(3.924, (3, 3, 3))
+    r = np.random.RandomState(seed)
+    s.numbers = np.array([Z_OF[x] for x in r.choice(["Ni", "Pt", "Cu"], len(s))], np.int64)
+    P = synthetic_model(len(cs.orbits) + 1, 2, 32, 1, 0)
+    m = NCEModel(cs, s, P, shell_edges=(0.0, 3.3), act="silu", pool="sum", mma=mma)
+    return m, NCEOracle(m.geo, P, act="silu", pool="sum")
+
+
+@pytest.mark.parametrize("cluster", [1, 4])
+def test_ternary_point_functions(cuda, cluster):
+    """Three species per site: point functions -cos(2 pi s / 3) are not +-1, so layer 0 runs the general float64
+    row products (full cache) and the int64 fixed-point row changes (step).  Full cache and a forced-move chain
+    against the oracle; a cluster of CTAs equals one CTA."""
+    torch = cuda
+    from neuralce_gb300.nce import NCEState
+    from oracle.nce_oracle import run_chain
+    m, orc = _ternary_model()
+    st = NCEState(m, m.sig0[None].astype(np.int8), np.ones(1)).full_cache()
+    torch.cuda.synchronize()
+    c = orc.full_cache(m.sig0.astype(np.int64))
+    assert np.abs(st.h0[0].cpu().numpy() - c["h0"]).max() < 2e-5
+    assert abs(float(st.E[0]) - orc.energy_of(c)) * m.scale_eV < 1e-4 * max(1.0, m.N / 64)
+    T = 10
+    rng = np.random.default_rng(8)
+    pi = rng.integers(0, m.N, T).astype(np.int32); pj = rng.integers(0, m.N, T).astype(np.int32)
+    dE = torch.zeros((T, 1), dtype=torch.float64, device="cuda")
+    props = tuple(torch.as_tensor(x.reshape(T, 1)).cuda() for x in (pi, pj, np.full(T, 0.5)))
+    st.run_chunk(T, 0, proposals=props, dE_out=dE, force=1, cluster=cluster)
+    torch.cuda.synchronize()
+    _, sig_ref, _, _, dEs, _ = run_chain(orc, c, m.sig0, pi, pj, np.full(T, 0.5), 0.0, m.scale_eV)
+    assert np.abs((dE.cpu().numpy()[:, 0] - dEs) * m.scale_eV).max() < 1e-4
+    assert np.array_equal(st.sigma[0].cpu().numpy(), sig_ref.astype(np.int8))
+    m.check_errors()
