@@ -36,3 +36,22 @@ def test_binding_signatures_cover_the_header():
     from neuralce_gb300 import _lib
     names = set(declared()) - {"nce_ce_energy_noalloc"}
     assert names <= set(_lib.SIGNATURES), names - set(_lib.SIGNATURES)
+
+
+def test_device_error_flags_are_named():
+    """Host decoding of a model's device error word: every set flag is named in the NceError, a clear word
+    raises nothing (the C entry point is replaced by a fake that writes the word)."""
+    import ctypes as C
+    from neuralce_gb300 import _lib
+
+    def fake(word):
+        def fn(handle, ptr):
+            C.cast(ptr, C.POINTER(C.c_int32))[0] = word
+            return 0
+        return fn
+    _lib.raise_device_errors(fake(0), None, _lib.NCE_ERROR_FLAGS, "NeuralCE kernels")
+    with pytest.raises(_lib.NceError) as e:
+        _lib.raise_device_errors(fake(1 | 32), None, _lib.NCE_ERROR_FLAGS, "NeuralCE kernels")
+    assert "0x21" in str(e.value) and "out of range" in str(e.value) and "tensor-core" in str(e.value)
+    with pytest.raises(_lib.NceError, match="delta query"):
+        _lib.raise_device_errors(fake(2), None, _lib.CE_ERROR_FLAGS, "CE kernels")
