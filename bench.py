@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=3, help="chunks of the batched-form side measurement (0 = skip)")
     ap.add_argument("--nce-steps", type=int, default=3, help="chunks of the NeuralCE side measurement (0 = skip)")
     ap.add_argument("--nce-chunk", type=int, default=1000, help="MC steps per NeuralCE chunk")
+    ap.add_argument("--nce-width", type=int, default=64, help="layer width of the --workload nce network")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -619,6 +620,7 @@ def main():
         from neuralce_gb300 import _lib
         _lib.lib()
         r = bench_nce(L=args.L, R=args.R, chunk=args.nce_chunk, steps=args.steps, warmup=args.warmup, seed=rank,
+                      width=args.nce_width,
                       mma=max(args.nce_mma, 0), shipped=args.workload == "nce-shipped")
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": r["value"], "unit": "swap attempts/s", "n_gpus": world, "steps": args.steps,
