@@ -1,7 +1,7 @@
 """One temperature ladder over several GPUs (one process per GPU): replicas are sharded into contiguous ranges,
 configurations never leave their GPU, and at every exchange the ranks all-gather the R float64 energies and
-recompute the same slot permutation (``neuralce/ce/pt_mcmc_ce.py:748-760``), as the benchmark spec's multi-GPU
-layout asks (one collective of R x 8 bytes per exchange, no data-path collective).
+recompute the same slot permutation (``neuralce/ce/pt_mcmc_ce.py:748-760``): one collective of R x 8 bytes per
+exchange and no data-path collective.
 
 On a rank, the chunk kernel runs its local replicas with ``slot_of_rep`` holding their GLOBAL temperature slots
 and ``beta_slot`` the global ladder, so every proposal is keyed by (seed, global step, global slot) exactly as in

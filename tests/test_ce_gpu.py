@@ -1,7 +1,7 @@
 """GPU parity of the CE engine against the C oracle (float64), through the C-ABI.
 
 Tolerances: float64 kernel dE within 1e-10 eV of the oracle (only the summation order differs); float32
-kernel dE within 1e-6 eV (spec bound).  Occupancy trajectories on a seeded stream are bit-exact;
+kernel dE within 1e-6 eV (the stated CE bound).  Occupancy trajectories on a seeded stream are bit-exact;
 steps whose Metropolis margin |beta*dE + ln u| is below 1e-9 (fp64) / 1e-5 (fp32) would be allowed to differ
 and are counted -- none occur for these seeds.
 """

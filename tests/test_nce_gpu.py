@@ -1,7 +1,7 @@
 """GPU parity of the NeuralCE engine against the float64 oracle, through the C ABI.
 
 Tolerances (float32 engine): energies within 2e-5 eV/atom of the oracle; per-swap dE within 1e-4 eV
-(spec NCE bound) in eV of the total energy; occupancy trajectories on a seeded stream bit-exact except at
+(the stated NeuralCE bound) in eV of the total energy; occupancy trajectories on a seeded stream bit-exact except at
 steps whose Metropolis margin |beta dE_eV + ln u| is below 1e-4 (counted: none occur for these seeds).
 """
 import numpy as np
