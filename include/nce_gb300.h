@@ -35,7 +35,7 @@ extern "C" {
 #define NCE_OK                 0
 #define NCE_ERR_INVALID       -1   /* bad argument (size, pointer, range) */
 #define NCE_ERR_CUDA          -2   /* a CUDA call failed */
-#define NCE_ERR_UNSUPPORTED   -3   /* valid but not supported by this build (e.g. cluster order > 8) */
+#define NCE_ERR_UNSUPPORTED   -3   /* valid but not supported by this library (e.g. cluster order > 8) */
 #define NCE_ERR_TIMEOUT       -4   /* a bounded device wait gave up */
 #define NCE_ERR_NOMEM         -5   /* device allocation failed / admission refused */
 

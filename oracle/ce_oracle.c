@@ -1,7 +1,7 @@
 /* CPU oracle of the cluster-expansion parallel-tempering path -- TEST INFRASTRUCTURE ONLY.
  *
- * Used by the tests, the smoke check and the CPU-baseline legs of bench.py as the checker; the product
- * never links or calls it.  float64 throughout, sequential sums in the reference's order.
+ * Used by the tests, the smoke check and the CPU-baseline legs of bench.py to check the product path;
+ * the product never links or calls it.  float64 throughout, sequential sums in the reference's order.
  *
  * Restates, on the reference's own table layout (Rv_b / Rv_uo / Rv_st / Rv_bf / Rv_eci per basis site):
  *   delta_energy_a          neuralce/ce/ce_gpu_implicit.py:181-191  (rows of i_a, plus rows of i_b not containing i_a)

@@ -1,7 +1,7 @@
 """CPU oracle for the cluster-expansion PT path -- TEST INFRASTRUCTURE ONLY.
 
 Only tests, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py``
-may import this module.  It is the checker, never the product path.
+may import this module.  It checks the product path and is never part of it.
 
 Two independent restatements of the reference, both in float64:
 

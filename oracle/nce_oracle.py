@@ -1,6 +1,6 @@
 """CPU oracle of the NeuralCE receptive-field update -- TEST INFRASTRUCTURE ONLY.
 
-Only tests, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py`` may use this module; it is the checker.
+Only tests, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py`` may use this module; it checks the product path and is never part of it.
 numpy, float64 by default.  Restates, on the geometry of ``neuralce_gb300.nce_geometry.build_geometry``:
 
   h0_full        neuralce/nce/gpu_layer0_implicit.py:151-171
