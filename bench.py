@@ -645,7 +645,7 @@ def main():
     if args.warps == 0 or args.cluster == 0:
         from neuralce_gb300.autotune import best_launch
         ws = (args.warps,) if args.warps else (4, 8, 16, 32)
-        cls = (args.cluster,) if args.cluster else ((1, 2, 4, 8) if args.path != 1 else (1,))
+        cls = (args.cluster,) if args.cluster else ((1, 2, 4, 8, 16) if args.path != 1 else (1,))
         paths = (2, 3) if args.path == 0 else (args.path,)
         (args.warps, args.cluster, args.path), t = best_launch(gce, st, args.precision, args.path, ws, cls, paths=paths)
         tuned = {f"{w}x{c}/p{p}": round(v, 3) for (w, c, p), v in t.items()}

@@ -424,11 +424,11 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     int32_t *dcv = reinterpret_cast<int32_t *>(smem + L.dcv);
     const bool track = jb.cv != nullptr;
     for (int c = tid; c < n_cols; c += nt) { ecol[c] = gecol[c]; cnt[c] = 0; cnt[n_cols + c] = 0; dcv[c] = 0; }
-    int32_t *rcnt[8];
-    for (int q = 0; q < 8; ++q) rcnt[q] = cnt;
+    int32_t *rcnt[16];
+    for (int q = 0; q < 16; ++q) rcnt[q] = cnt;
     if (CLUSTER) {
         cg::cluster_group cl = cg::this_cluster();
-        for (int q = 0; q < CL && q < 8; ++q) rcnt[q] = cl.map_shared_rank(cnt, q);
+        for (int q = 0; q < CL && q < 16; ++q) rcnt[q] = cl.map_shared_rank(cnt, q);
     }
     int8_t *gsig = jb.sigma + (int64_t)r * jb.N;
     int8_t *sig = sig_smem ? reinterpret_cast<int8_t *>(smem + L.sig) : gsig;
@@ -671,11 +671,11 @@ __global__ void __launch_bounds__(1024) ce_bin2_chunk_kernel(const __grid_consta
         ecol[c] = gecol[c]; dcv[c] = 0;
         for (int q = 0; q < 4; ++q) cnt[q * n_cols + c] = 0;
     }
-    int32_t *rcnt[8];
-    for (int q = 0; q < 8; ++q) rcnt[q] = cnt;
+    int32_t *rcnt[16];
+    for (int q = 0; q < 16; ++q) rcnt[q] = cnt;
     if (CLUSTER) {
         cg::cluster_group cl = cg::this_cluster();
-        for (int q = 0; q < CL && q < 8; ++q) rcnt[q] = cl.map_shared_rank(cnt, q);
+        for (int q = 0; q < CL && q < 16; ++q) rcnt[q] = cl.map_shared_rank(cnt, q);
     }
     int8_t *gsig = jb.sigma + (int64_t)r * jb.N;
     int8_t *sig = sig_smem ? reinterpret_cast<int8_t *>(smem + L.sig) : gsig;
@@ -1206,6 +1206,7 @@ static int launch_chunk_mo(const CEBatch &bt, int total, int warps, size_t smem,
 static int launch_bin_kernel(void (*kern)(CEBatch, int32_t), const CEBatch &bt, int total, int warps, size_t smem, int sig_smem,
                              cudaStream_t s, int CL) {
     NCE_CUDA(::nce::raise_smem_limit((const void *)kern, smem));
+    if (CL > 8) NCE_CUDA(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     if (CL <= 1) {
         kern<<<total, warps * 32, smem, s>>>(bt, sig_smem);
     } else {
@@ -1239,6 +1240,8 @@ static int launch_bin_mo(const CEBatch &bt, int total, int warps, size_t smem, i
     } else {
         auto kern = ce_bin_chunk_kernel<Acc, MO, true>;
         NCE_CUDA(::nce::raise_smem_limit((const void *)kern, smem));
+        // 16 CTAs per cluster is beyond the portable size of 8 (allowed on this GPU)
+        if (CL > 8) NCE_CUDA(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
         cudaLaunchConfig_t cfg; std::memset(&cfg, 0, sizeof(cfg));
         cfg.gridDim = dim3((unsigned)(total * CL)); cfg.blockDim = dim3(warps * 32); cfg.dynamicSmemBytes = smem; cfg.stream = s;
         cudaLaunchAttribute attr[1];
@@ -1292,8 +1295,8 @@ static int check_chunk(const nce_pt_state *st, const nce_pt_chunk *ck) {
               "chunk: prop_a/prop_b/prop_u must be all set or all NULL");
     NCE_CHECK(!ck->E_samples || ck->sample_interval > 0, "chunk: sample_interval must be > 0 with E_samples");
     NCE_CHECK(ck->warps >= 0 && ck->warps <= 32, "chunk: warps must be 0..32");
-    NCE_CHECK(ck->cluster == 0 || ck->cluster == 1 || ck->cluster == 2 || ck->cluster == 4 || ck->cluster == 8,
-              "chunk: cluster must be 0, 1, 2, 4 or 8");
+    NCE_CHECK(ck->cluster == 0 || ck->cluster == 1 || ck->cluster == 2 || ck->cluster == 4 || ck->cluster == 8 ||
+              ck->cluster == 16, "chunk: cluster must be 0, 1, 2, 4, 8 or 16");
     NCE_CHECK(!ck->do_exchange || !ck->ex_u || (ck->ex_parity == 0 || ck->ex_parity == 1), "chunk: ex_parity must be 0/1");
     (void)st;
     return NCE_OK;

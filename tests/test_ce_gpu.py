@@ -158,7 +158,7 @@ def test_batch_equals_alone(cuda):
         assert torch.equal(a.sigma, b.sigma) and torch.equal(a.E, b.E) and torch.equal(a.rep_of_slot, b.rep_of_slot)
 
 
-@pytest.mark.parametrize("cluster,path", [(2, 2), (4, 2), (2, 3), (4, 3)])
+@pytest.mark.parametrize("cluster,path", [(2, 2), (4, 2), (8, 2), (16, 2), (2, 3), (4, 3)])
 def test_cluster_equals_single_cta(cuda, cluster, path):
     """Philox stream with exchanges, 3 chunks: a replica spread over a thread-block cluster gives the same
     trajectory as one CTA, alone and in a batch of jobs."""
