@@ -67,6 +67,7 @@ struct NceDev {
     // bit-sliced layer 0 (full caches; l0bin with every member on point function 0): per basis, the reverse rows'
     // members as (basis, uo0, uo1, uo2) or basis -1, each row's channel, and the channel weight (w, float64)
     int32_t h0bits; const int4 *h0mem; const double *col_w;
+    int32_t h0_slices; const int2 *h0_slice;  // (nB, S + 1) slice starts (first row, first channel); last = (J, C0)
     // tcgen05 layer contractions (mma 2: bf16, mma 4: split bf16): per layer the weights as the B operand in bf16
     // core-matrix layout ([D][Kp], Kp = Kin rounded up to 16; hi, then lo when split)
     int32_t tc, tc_split; const uint8_t *Wt[kMaxLayers];
@@ -1163,9 +1164,12 @@ __global__ void nce_plane_kernel(NceDev m, const int8_t *__restrict__ sigma, int
     }
 }
 
-// grid (blocks, nB, R): threads over the (k0, k1, 32-site word) items of basis blockIdx.y, replica blockIdx.z
+// grid (blocks, nB x S, R): threads over the (k0, k1, 32-site word) items of basis blockIdx.y / S, replica
+// blockIdx.z; slice blockIdx.y % S takes the rows and channels [h0s_row, h0s_ch] .. of the next slice (slices cut
+// the rows of a basis at channel boundaries, so small cells still fill the GPU)
 __global__ void __launch_bounds__(128) nce_h0_bits_kernel(NceDev m, const uint32_t *__restrict__ planes, int32_t W2, float *h0) {
-    const int b = blockIdx.y, r = blockIdx.z;
+    const int S = m.h0_slices, b = blockIdx.y / S, sl = blockIdx.y % S, r = blockIdx.z;
+    const int2 lo = m.h0_slice[b * (S + 1) + sl], hi = m.h0_slice[b * (S + 1) + sl + 1];   // (first row, first channel)
     const int d0 = m.d0, d1 = m.d1, d2 = m.d2;
     const int Wn = (d2 + 31) >> 5;
     const int64_t items = (int64_t)d0 * d1 * Wn;
@@ -1182,11 +1186,13 @@ __global__ void __launch_bounds__(128) nce_h0_bits_kernel(NceDev m, const uint32
     float *out0 = h0 + (((int64_t)r * m.N) + ((int64_t)(k0 * d1 + k1) * d2 + 32 * w) * m.nB + b) * C0;
     const int64_t sstride = (int64_t)m.nB * C0;
     if (m.Mb[b] < 2) {                                       // inactive sites: zeros
-        for (int j = 0; j < nv; ++j) for (int c = 0; c < C0; ++c) out0[j * sstride + c] = 0.f;
+        for (int j = 0; j < nv; ++j) for (int c = sl ? lo.y : 0; c < hi.y; ++c) out0[j * sstride + c] = 0.f;
         return;
     }
-    const float ch0 = (float)((1.0 - (double)m.mu[0]) / (double)m.sd[0]);
-    for (int j = 0; j < nv; ++j) out0[j * sstride] = ch0;
+    if (sl == 0) {
+        const float ch0 = (float)((1.0 - (double)m.mu[0]) / (double)m.sd[0]);
+        for (int j = 0; j < nv; ++j) out0[j * sstride] = ch0;
+    }
     constexpr int NQ = 13;                                    // vertical counter planes: up to 8191 rows per channel
     uint32_t cnt[NQ];
     auto flush = [&](int ch, int nrows) {
@@ -1198,11 +1204,11 @@ __global__ void __launch_bounds__(128) nce_h0_bits_kernel(NceDev m, const uint32
             out0[j * sstride + ch] = (float)((double)(nrows - 2 * odd) * wc - base);
         }
     };
-    int ch_cur = 1, nrows = 0;
+    int ch_cur = lo.y, nrows = 0;
 #pragma unroll
     for (int q = 0; q < NQ; ++q) cnt[q] = 0u;
     const int4 *mem = m.h0mem + (size_t)b * m.J * m.mo;
-    for (int jr = 0; jr < m.J; ++jr) {
+    for (int jr = lo.x; jr < hi.x; ++jr) {
         const int e = b * m.J + jr;
         if (m.Rv_wfix[e] == 0) continue;
         const int ch = m.Rv_col[e] + 1;
@@ -1229,10 +1235,10 @@ __global__ void __launch_bounds__(128) nce_h0_bits_kernel(NceDev m, const uint32
         for (int q = 0; q < NQ; ++q) { const uint32_t t = cnt[q] & carry; cnt[q] ^= carry; carry = t; }
         ++nrows;
     }
-    flush(ch_cur, nrows);
+    if (ch_cur < hi.y) flush(ch_cur, nrows);
 #pragma unroll
     for (int q = 0; q < NQ; ++q) cnt[q] = 0u;
-    for (int c = ch_cur + 1; c < C0; ++c) flush(c, 0);
+    for (int c = ch_cur + 1; c < hi.y; ++c) flush(c, 0);
 }
 
 // Layer 0 of every site for general point functions: every reverse row of each site pulled in float64 (fixed
@@ -1636,6 +1642,36 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
             }
             if (hb) {
                 chk(dup(h, hm.data(), hm.size(), m.h0mem)); chk(dup(h, cwd.data(), cwd.size(), m.col_w));
+                // slices of each basis's rows, cut where the channel changes, about equal in rows
+                const int S = 8;
+                std::vector<int2> sl((size_t)d->nB * (S + 1));
+                for (int b = 0; b < d->nB; ++b) {
+                    std::vector<int> start_row, start_ch;            // candidate cuts: first row of each channel run
+                    int nrows = 0, last = -1;
+                    for (int j = 0; j < d->J; ++j) {
+                        const size_t e = (size_t)b * d->J + j;
+                        if (wf[e] == 0) continue;
+                        const int ch = d->Rv_col[e] + 1;
+                        if (ch != last) { start_row.push_back(j); start_ch.push_back(ch); last = ch; }
+                        ++nrows;
+                    }
+                    int2 *o = &sl[(size_t)b * (S + 1)];
+                    o[0] = make_int2(0, 1);
+                    int k = 1, seen = 0, ci = 0;
+                    for (int j = 0; j < d->J && k < S; ++j) {
+                        const size_t e = (size_t)b * d->J + j;
+                        if (wf[e] == 0) continue;
+                        while (ci < (int)start_row.size() && start_row[ci] < j) ++ci;
+                        if (ci < (int)start_row.size() && start_row[ci] == j && j > 0 && seen >= (int64_t)k * nrows / S &&
+                            start_ch[ci] > o[k - 1].y)
+                            o[k++] = make_int2(j, start_ch[ci]);
+                        ++seen;
+                    }
+                    for (; k <= S; ++k) o[k] = make_int2(d->J, d->C0);      // empty trailing slices
+                    o[S] = make_int2(d->J, d->C0);
+                }
+                chk(dup(h, sl.data(), sl.size(), m.h0_slice));
+                m.h0_slices = S;
                 m.h0bits = 1;
             }
         }
@@ -1715,7 +1751,8 @@ int nce_nce_full_cache(nce_nce_handle h, const nce_nce_state *st, void *stream) 
         nce_plane_kernel<<<(int)std::min<int64_t>((prow + 7) / 8, 1 << 20), 256, 0, s>>>(m, st->sigma, st->R, W2, (uint32_t *)planes.p);
         NCE_CUDA(cudaGetLastError());
         const int64_t items = (int64_t)m.d0 * m.d1 * ((m.d2 + 31) / 32);
-        nce_h0_bits_kernel<<<dim3((unsigned)((items + 127) / 128), m.nB, st->R), 128, 0, s>>>(m, (const uint32_t *)planes.p, W2, st->h0);
+        nce_h0_bits_kernel<<<dim3((unsigned)((items + 127) / 128), m.nB * m.h0_slices, st->R), 128, 0, s>>>(
+            m, (const uint32_t *)planes.p, W2, st->h0);
     } else {
         nce_h0_kernel<<<(int)std::min<int64_t>((tot + 127) / 128, 65535), 128, 0, s>>>(m, st->sigma, st->R, st->h0);
     }
