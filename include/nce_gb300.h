@@ -7,8 +7,10 @@
  * nce_last_error() gives the message of the calling thread's last failure.
  *
  * Threading: a handle may be used from one host thread at a time; calls are asynchronous on the given
- * stream unless stated otherwise.  Table inputs are host pointers and are copied during *_create; the
- * caller keeps ownership.
+ * stream unless stated otherwise.  A NeuralCE model handle keeps one set of step scratch (slot map, site
+ * lists, new rows) for all states that use it, so its chunks must be ordered on one stream; full caches and
+ * energies take per-call scratch and may overlap on several streams.  Table inputs are host pointers and are
+ * copied during *_create; the caller keeps ownership.
  *
  * Reference interfaces replaced (paths inside the neuralce project):
  *   nce_ce_create        GPUClusterExpansion(..., table_mode='implicit')      neuralce/ce/classical_ce_gpu.py:496-535
