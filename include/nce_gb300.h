@@ -92,9 +92,10 @@ int nce_ce_energy(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t preci
 /* Same result as nce_ce_energy, for callers that cannot allocate device memory while they run (their device
  * memory is reserved up front by their own pool, or they cannot afford the device synchronisation that
  * cudaMalloc/cudaFree imply).  It allocates nothing: its scratch is a fixed array of 65,536 float64 partials
- * built into this library, one per device, kept until the process exits; R may be at most 65,536.  The first
- * call on a device looks up that array's address; make this first call before any stream capture.  Calls that
- * overlap on the GPU share the array and race.  This entry point has no counterpart in the reference. */
+ * built into this library, one per device, kept until the process exits; R may be at most 65,535 (one grid row
+ * per configuration).  The first call on a device looks up that array's address; make this first call before any
+ * stream capture.  Calls that overlap on the GPU share the array and race.  This entry point has no counterpart
+ * in the reference. */
 int nce_ce_energy_noalloc(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t precision, double *E, void *stream);
 
 /* n independent swap energy differences on device data: for query q, configuration rep[q] of sigma (R,N),

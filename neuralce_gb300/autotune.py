@@ -5,7 +5,7 @@ site, the replica count relative to the 152 SMs and the precision: with few repl
 over a cluster of 2-8 CTAs puts idle SMs to work on the row phase at the price of one cluster barrier per
 evaluated swap.  The tuner times a short chunk of the real kernel for each candidate on a scratch copy of the
 state (the job's own state is untouched) and keeps the fastest; results are cached per (tables, R, precision,
-path)."""
+path); the key names the model by its serial number, which no later model reuses."""
 from __future__ import annotations
 
 _cache = {}
@@ -17,7 +17,7 @@ def best_launch(gce, st, precision=64, path=0, warps=(2, 4, 8, 16, 32), clusters
     import torch
     from . import _lib
     from .pt import PTState, run_chunk
-    key = (id(gce), st.R, precision, path, tuple(warps), tuple(clusters), tuple(paths or ()))
+    key = (gce.serial, st.R, precision, path, tuple(warps), tuple(clusters), tuple(paths or ()))
     if key in _cache:
         return _cache[key]
     if paths:

@@ -9,12 +9,16 @@ torch only holds device buffers.
 from __future__ import annotations
 
 import ctypes as C
+import itertools
 
 import numpy as np
 
 from . import _lib
 from .ce_tables import ClusterSpace, build_tables, encode_species
 from .io import ClusterExpansionFile, Structure
+
+
+_SERIAL = itertools.count(1)      # identity of a model for launch-shape caches (never reused, unlike id())
 
 
 def _arr(x, dtype):
@@ -101,6 +105,7 @@ class GPUClusterExpansion:
                                      "name": "".join(sp)})
         self.host_tables = CETables(tb)
         self._handle = None
+        self.serial = next(_SERIAL)
 
     # ── reference attributes ──
     @property

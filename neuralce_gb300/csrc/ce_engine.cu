@@ -1743,6 +1743,7 @@ static int energy_impl(nce_ce_model *h, const int8_t *sigma, int32_t R, int32_t 
         return NCE_OK;
     }
     NCE_CHECK(E && !cv_out, "energy: cluster-vector sums need the sign-parity tables");
+    NCE_CHECK(R <= 65535, "energy: at most 65535 configurations per call");   // one grid row per configuration
     const int threads = 256;
     int nblk = (int)std::min<int64_t>((h->n_cells + threads - 1) / threads, 1184);
     nblk = std::max(nblk, 1);
@@ -1881,6 +1882,8 @@ int nce_ce_run_chunk_host(nce_ce_handle h, int32_t R, int8_t *sigma_host, double
 // has to be cleared between calls.
 namespace nce {
 constexpr int64_t kNoAllocPartials = 65536;                                    // 512 KiB of float64 partials
+// configurations per call: one grid row (gridDim.y) per configuration, and gridDim.y is at most 65,535
+constexpr int32_t kNoAllocMaxConfigs = 65535;
 static __device__ __align__(256) double g_noalloc_partials[kNoAllocPartials];
 static std::mutex g_noalloc_mu;
 static double *g_noalloc_ptr[256];                                             // per device ordinal
@@ -1919,8 +1922,8 @@ extern "C" {
 int nce_ce_energy_noalloc(nce_ce_handle h, const int8_t *sigma, int32_t R, int32_t precision, double *E, void *stream) {
     NCE_CHECK(h && sigma && E && R >= 1, "nce_ce_energy_noalloc: bad argument");
     NCE_CHECK(precision == 64 || precision == 32, "nce_ce_energy_noalloc: precision must be 64 or 32");
-    NCE_CHECK(R <= kNoAllocPartials, "nce_ce_energy_noalloc: %d configurations exceed the limit of %lld per call", R,
-              (long long)kNoAllocPartials);
+    NCE_CHECK(R <= kNoAllocMaxConfigs, "nce_ce_energy_noalloc: %d configurations exceed the limit of %d per call", R,
+              kNoAllocMaxConfigs);
     double *partial = nullptr;
     int rc = noalloc_partials(&partial);
     if (rc) return rc;

@@ -6,8 +6,9 @@ exchange and no data-path collective.
 On a rank, the chunk kernel runs its local replicas with ``slot_of_rep`` holding their GLOBAL temperature slots
 and ``beta_slot`` the global ladder, so every proposal is keyed by (seed, global step, global slot) exactly as in
 a single-process run: a sharded run reproduces the single-GPU trajectory bit for bit.  The exchange is computed
-on the host from the gathered energies with the kernels' Philox counters (parity: counter word 2 = 0xFFFFFFFF;
-uniform of pair k: word 2 = 0xFFFFFFFE, word 3 = k; words 0-1 = global step after the chunk).
+on the host from the gathered energies with the kernels' Philox counters (round q of the exchange: parity from
+counter word 2 = 0xFFFFFFFF - 2q, uniform of pair k from word 2 = 0xFFFFFFFE - 2q and word 3 = k; words 0-1 = the
+global step after the chunk).
 """
 from __future__ import annotations
 
@@ -23,13 +24,15 @@ def _u01(hi, lo):
     return (m + 1) * 2.0 ** -53
 
 
-def exchange_slots(E, beta_slot, ladder_id, rep_of_slot, seed, g_end):
-    """One neighbour-slot exchange round on the host: E (R,) float64 per replica, beta_slot (R,) float32 per slot,
-    rep_of_slot (R,) int; returns (new rep_of_slot, accepted swaps)."""
+def exchange_slots(E, beta_slot, ladder_id, rep_of_slot, seed, g_end, q=0):
+    """Round q of the neighbour-slot exchange on the host: E (R,) float64 per replica, beta_slot (R,) float32 per
+    slot, rep_of_slot (R,) int; returns (new rep_of_slot, accepted swaps).  Each round draws its own parity and
+    uniforms, as ce_exchange_kernel does."""
     R = len(rep_of_slot)
     k0, k1 = seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF
     c0, c1 = g_end & 0xFFFFFFFF, (g_end >> 32) & 0xFFFFFFFF
-    parity = _lib.philox4x32([c0, c1, 0xFFFFFFFF, 0], [k0, k1])[0] & 1
+    cq = (0xFFFFFFFF - 2 * q) & 0xFFFFFFFF
+    parity = _lib.philox4x32([c0, c1, cq, 0], [k0, k1])[0] & 1
     perm = np.arange(R)
     n = 0
     for k in range(R // 2 + 1):
@@ -39,7 +42,7 @@ def exchange_slots(E, beta_slot, ladder_id, rep_of_slot, seed, g_end):
         if ladder_id[i] != ladder_id[j]:
             continue
         log_acc = (float(np.float32(beta_slot[j])) - float(np.float32(beta_slot[i]))) * (float(E[rep_of_slot[j]]) - float(E[rep_of_slot[i]]))
-        w = _lib.philox4x32([c0, c1, 0xFFFFFFFE, k], [k0, k1])
+        w = _lib.philox4x32([c0, c1, (cq - 1) & 0xFFFFFFFF, k], [k0, k1])
         if math.log(_u01(w[0], w[1])) < log_acc:
             perm[i], perm[j] = j, i
             n += 1
@@ -88,7 +91,7 @@ class ShardedLadder:
     def exchange(self, E_local, seed, g_end, rounds=1):
         E = self.gather(E_local)
         for q in range(rounds):
-            self.rep_of_slot, n = exchange_slots(E, self.beta_slot, self.ladder_id, self.rep_of_slot, seed, g_end)
+            self.rep_of_slot, n = exchange_slots(E, self.beta_slot, self.ladder_id, self.rep_of_slot, seed, g_end, q)
             self.n_ex += n
         return E
 

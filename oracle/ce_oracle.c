@@ -38,6 +38,7 @@ typedef struct {
     int8_t *sigma; double *E; const float *beta_slot;
     int32_t *rep_of_slot, *slot_of_rep; const int32_t *ladder_id;
     double *E_min_rep; int64_t *n_acc; int64_t *n_ex;
+    int64_t *n_near;                                          /* (R) near-threshold steps per replica, or NULL */
 } orc_state;
 
 typedef struct {
@@ -45,8 +46,10 @@ typedef struct {
     const int32_t *prop_a, *prop_b; const double *prop_u;   /* [step][slot]; NULL -> Philox */
     uint64_t seed;
     int64_t sample_interval; double *E_samples;            /* [(n_steps/si)][slot] or NULL */
-    int32_t do_exchange; int32_t ex_parity; const double *ex_u; /* ex_u NULL -> Philox */
+    int32_t do_exchange; int32_t ex_parity; const double *ex_u; /* ex_u NULL -> Philox; ex_parity: bit q = round q */
     int32_t n_threads;
+    int32_t rounds;          /* exchange rounds back to back (0 or 1: one round) */
+    double near_eV;          /* a step is near its threshold when |dE - (-ln u / beta)| < near_eV */
 } orc_chunk;
 
 /* ── Philox4x32-10 ─────────────────────────────────────────────────────────────────────────────── */
@@ -86,16 +89,17 @@ void orc_propose(const orc_tables *tb, uint64_t seed, int64_t g, int32_t t, int6
     *u = u01_open0(x[2], x[3]);
 }
 
-/* exchange randoms of the chunk ending at global step g (after the step): parity and pair uniforms */
-int32_t orc_ex_parity(uint64_t seed, int64_t g) {
+/* exchange randoms of round q of the chunk ending at global step g (after the step): parity and pair uniforms,
+ * counter word 2 = 0xFFFFFFFF - 2q (parity) and 0xFFFFFFFE - 2q (uniform of pair k, word 3 = k) */
+int32_t orc_ex_parity(uint64_t seed, int64_t g, int32_t q) {
     uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
-    uint32_t ctr[4] = {(uint32_t)g, (uint32_t)((uint64_t)g >> 32), 0xFFFFFFFFu, 0u}, x[4];
+    uint32_t ctr[4] = {(uint32_t)g, (uint32_t)((uint64_t)g >> 32), 0xFFFFFFFFu - 2u * (uint32_t)q, 0u}, x[4];
     orc_philox4x32(ctr, key, x);
     return (int32_t)(x[0] & 1u);
 }
-double orc_ex_uniform(uint64_t seed, int64_t g, int32_t k) {
+double orc_ex_uniform(uint64_t seed, int64_t g, int32_t q, int32_t k) {
     uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
-    uint32_t ctr[4] = {(uint32_t)g, (uint32_t)((uint64_t)g >> 32), 0xFFFFFFFEu, (uint32_t)k}, x[4];
+    uint32_t ctr[4] = {(uint32_t)g, (uint32_t)((uint64_t)g >> 32), 0xFFFFFFFEu - 2u * (uint32_t)q, (uint32_t)k}, x[4];
     orc_philox4x32(ctr, key, x);
     return u01_open0(x[0], x[1]);
 }
@@ -157,7 +161,7 @@ static void run_replica(const orc_tables *tb, orc_state *st, const orc_chunk *ck
     int32_t t = st->slot_of_rep[r];
     double beta = (double)st->beta_slot[t];
     double E = st->E[r], Emin = st->E_min_rep[r];
-    int64_t nacc = 0;
+    int64_t nacc = 0, nnear = 0;
     for (int64_t s = 0; s < ck->n_steps; ++s) {
         int64_t ia, ib; double u;
         if (ck->prop_a) {
@@ -168,6 +172,7 @@ static void run_replica(const orc_tables *tb, orc_state *st, const orc_chunk *ck
         int32_t sa = sig[ia], sb = sig[ib];
         if (sa != sb) {
             double dE = orc_ce_delta(tb, sig, ia, ib, sb, sa);
+            if (beta > 0.0 && fabs(dE + log(u) / beta) < ck->near_eV) ++nnear;
             if (log(u) < -beta * dE) { sig[ia] = (int8_t)sb; sig[ib] = (int8_t)sa; E += dE; ++nacc; }
         }
         if (E < Emin) Emin = E;
@@ -175,26 +180,30 @@ static void run_replica(const orc_tables *tb, orc_state *st, const orc_chunk *ck
             ck->E_samples[((s + 1) / ck->sample_interval - 1) * st->R + t] = E;
     }
     st->E[r] = E; st->E_min_rep[r] = Emin; st->n_acc[r] += nacc;
+    if (st->n_near) st->n_near[r] += nnear;
 }
 
 void orc_exchange(orc_state *st, const orc_chunk *ck) {
     int32_t R = st->R;
     int64_t g = ck->step0 + ck->n_steps;            /* global step count after the chunk */
-    int32_t parity = ck->ex_u ? ck->ex_parity : orc_ex_parity(ck->seed, g);
     int32_t *perm = (int32_t *)malloc(sizeof(int32_t) * R), *ros = (int32_t *)malloc(sizeof(int32_t) * R);
-    for (int32_t i = 0; i < R; ++i) perm[i] = i;
+    const int32_t npair = R / 2;                    /* ceil((R - 1) / 2) */
     int32_t nswap = 0;
-    for (int32_t k = 0; 2 * k < R - 1; ++k) {
-        int32_t i = 2 * k + parity, j = i + 1;
-        if (j >= R) continue;
-        if (st->ladder_id[i] != st->ladder_id[j]) continue;
-        double Ei = st->E[st->rep_of_slot[i]], Ej = st->E[st->rep_of_slot[j]];
-        double log_acc = ((double)st->beta_slot[j] - (double)st->beta_slot[i]) * (Ej - Ei);
-        double u = ck->ex_u ? ck->ex_u[k] : orc_ex_uniform(ck->seed, g, k);
-        if (log(u) < log_acc) { perm[i] = j; perm[j] = i; ++nswap; }
+    for (int32_t q = 0; q < (ck->rounds > 1 ? ck->rounds : 1); ++q) {
+        int32_t parity = ck->ex_u ? ((ck->ex_parity >> q) & 1) : orc_ex_parity(ck->seed, g, q);
+        for (int32_t i = 0; i < R; ++i) perm[i] = i;
+        for (int32_t k = 0; 2 * k < R - 1; ++k) {
+            int32_t i = 2 * k + parity, j = i + 1;
+            if (j >= R) continue;
+            if (st->ladder_id[i] != st->ladder_id[j]) continue;
+            double Ei = st->E[st->rep_of_slot[i]], Ej = st->E[st->rep_of_slot[j]];
+            double log_acc = ((double)st->beta_slot[j] - (double)st->beta_slot[i]) * (Ej - Ei);
+            double u = ck->ex_u ? ck->ex_u[(int64_t)q * npair + k] : orc_ex_uniform(ck->seed, g, q, k);
+            if (log(u) < log_acc) { perm[i] = j; perm[j] = i; ++nswap; }
+        }
+        for (int32_t t = 0; t < R; ++t) ros[t] = st->rep_of_slot[perm[t]];
+        for (int32_t t = 0; t < R; ++t) { st->rep_of_slot[t] = ros[t]; st->slot_of_rep[ros[t]] = t; }
     }
-    for (int32_t t = 0; t < R; ++t) ros[t] = st->rep_of_slot[perm[t]];
-    for (int32_t t = 0; t < R; ++t) { st->rep_of_slot[t] = ros[t]; st->slot_of_rep[ros[t]] = t; }
     *st->n_ex += nswap;
     if (ck->E_samples && ck->n_steps % ck->sample_interval == 0) {       /* last sample: post-exchange slot order */
         int64_t row = ck->n_steps / ck->sample_interval - 1;

@@ -123,13 +123,14 @@ class OrcTables(ctypes.Structure):
 
 class OrcState(ctypes.Structure):
     _fields_ = [("R", _i32), ("N", _i64), ("sigma", _vp), ("E", _vp), ("beta_slot", _vp), ("rep_of_slot", _vp),
-                ("slot_of_rep", _vp), ("ladder_id", _vp), ("E_min_rep", _vp), ("n_acc", _vp), ("n_ex", _vp)]
+                ("slot_of_rep", _vp), ("ladder_id", _vp), ("E_min_rep", _vp), ("n_acc", _vp), ("n_ex", _vp),
+                ("n_near", _vp)]
 
 
 class OrcChunk(ctypes.Structure):
     _fields_ = [("n_steps", _i64), ("step0", _i64), ("prop_a", _vp), ("prop_b", _vp), ("prop_u", _vp), ("seed", _u64),
                 ("sample_interval", _i64), ("E_samples", _vp), ("do_exchange", _i32), ("ex_parity", _i32),
-                ("ex_u", _vp), ("n_threads", _i32)]
+                ("ex_u", _vp), ("n_threads", _i32), ("rounds", _i32), ("near_eV", _f64)]
 
 
 def _p(a):
@@ -190,13 +191,16 @@ class OracleCE:
         return self.c.lib.orc_ce_delta(ctypes.byref(self.s), sig.ctypes.data, int(ia), int(ib), int(sa_new), int(sb_new))
 
     def run(self, state, n_steps, step0, seed=0, proposals=None, sample_interval=1, E_samples=None, do_exchange=False,
-            ex_parity=0, ex_u=None, n_threads=1):
+            ex_parity=0, ex_u=None, n_threads=1, rounds=1, near_eV=0.0):
         """run one chunk in place on the numpy arrays of ``state`` (dict: sigma, E, beta_slot, rep_of_slot,
-        slot_of_rep, ladder_id, E_min_rep, n_acc, n_ex)."""
+        slot_of_rep, ladder_id, E_min_rep, n_acc, n_ex, optional n_near).  ``rounds`` exchange rounds at the chunk
+        end (host uniforms: ex_u (rounds, ceil((R-1)/2)), parity bit q of ex_parity); ``state["n_near"]`` (when
+        present) counts the steps with |dE + ln(u) / beta| < near_eV."""
         st = OrcState()
         st.R, st.N = state["sigma"].shape
         for k in ("sigma", "E", "beta_slot", "rep_of_slot", "slot_of_rep", "ladder_id", "E_min_rep", "n_acc", "n_ex"):
             setattr(st, k, state[k].ctypes.data)
+        st.n_near = state["n_near"].ctypes.data if "n_near" in state else None
         ck = OrcChunk()
         ck.n_steps, ck.step0, ck.seed = int(n_steps), int(step0), int(seed) & 0xFFFFFFFFFFFFFFFF
         if proposals is not None:
@@ -205,7 +209,7 @@ class OracleCE:
             ck.prop_a, ck.prop_b, ck.prop_u = pa.ctypes.data, pb.ctypes.data, pu.ctypes.data
         ck.sample_interval = int(sample_interval); ck.E_samples = _p(E_samples)
         ck.do_exchange = int(bool(do_exchange)); ck.ex_parity = int(ex_parity); ck.ex_u = _p(ex_u)
-        ck.n_threads = int(n_threads)
+        ck.n_threads = int(n_threads); ck.rounds = int(rounds); ck.near_eV = float(near_eV)
         self.c.lib.orc_ce_run(ctypes.byref(self.s), ctypes.byref(st), ctypes.byref(ck))
 
 
@@ -217,7 +221,7 @@ def new_state(sigma, E, beta_slot, ladder_id=None):
                 beta_slot=np.ascontiguousarray(beta_slot, np.float32), rep_of_slot=np.arange(R, dtype=np.int32),
                 slot_of_rep=np.arange(R, dtype=np.int32),
                 ladder_id=np.zeros(R, np.int32) if ladder_id is None else np.ascontiguousarray(ladder_id, np.int32),
-                E_min_rep=Emr, n_acc=np.zeros(R, np.int64), n_ex=np.zeros(1, np.int64))
+                E_min_rep=Emr, n_acc=np.zeros(R, np.int64), n_ex=np.zeros(1, np.int64), n_near=np.zeros(R, np.int64))
 
 
 def c_oracle_path():

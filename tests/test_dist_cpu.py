@@ -1,6 +1,7 @@
 """Multi-rank host logic on the CPU (gloo, world size 2): a ladder sharded over two ranks, each advancing its own
 replicas (the C oracle stands in for the chunk kernel) and all-gathering the energies at every exchange, gives
-the single-process trajectory bit for bit; the host exchange equals the oracle's in-process exchange."""
+the single-process trajectory bit for bit; the host exchange equals the oracle's in-process exchange, with one
+exchange round per chunk and with two (each round drawing its own parity and uniforms)."""
 import multiprocessing as mp
 import socket
 
@@ -30,7 +31,7 @@ def _local_state(shard, sig_r, E0, beta):
                 ladder_id=np.zeros(R, np.int32), E_min_rep=Emr, n_acc=np.zeros(n, np.int64), n_ex=np.zeros(1, np.int64))
 
 
-def _sharded(rank, world, port, q):
+def _sharded(rank, world, port, q, rounds=1):
     import torch.distributed as dist
     from neuralce_gb300.dist import ShardedLadder
     dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
@@ -40,17 +41,17 @@ def _sharded(rank, world, port, q):
     for c in range(CHUNKS):
         st["slot_of_rep"] = shard.local_slots()
         orc.run(st, T, c * T, SEED, do_exchange=False)
-        shard.exchange(st["E"], SEED, (c + 1) * T)
+        shard.exchange(st["E"], SEED, (c + 1) * T, rounds=rounds)
     q.put((rank, st["sigma"], st["E"], st["n_acc"], shard.rep_of_slot, shard.n_ex))
     dist.destroy_process_group()
 
 
-def _reference():
+def _reference(rounds=1):
     from oracle.ce_oracle import new_state
     orc, sig_r, E0, beta = _setup()
     ref = new_state(sig_r, E0, beta)
     for c in range(CHUNKS):
-        orc.run(ref, T, c * T, SEED, do_exchange=True)
+        orc.run(ref, T, c * T, SEED, do_exchange=True, rounds=rounds)
     return ref
 
 
@@ -60,7 +61,8 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def test_host_exchange_equals_oracle_single_rank():
+@pytest.mark.parametrize("rounds", [1, 2])
+def test_host_exchange_equals_oracle_single_rank(rounds):
     from neuralce_gb300.dist import ShardedLadder
     orc, sig_r, E0, beta = _setup()
     shard = ShardedLadder(beta)
@@ -68,8 +70,8 @@ def test_host_exchange_equals_oracle_single_rank():
     for c in range(CHUNKS):
         st["slot_of_rep"] = shard.local_slots()
         orc.run(st, T, c * T, SEED, do_exchange=False)
-        shard.exchange(st["E"], SEED, (c + 1) * T)
-    ref = _reference()
+        shard.exchange(st["E"], SEED, (c + 1) * T, rounds=rounds)
+    ref = _reference(rounds)
     assert np.array_equal(st["sigma"], ref["sigma"]) and np.array_equal(st["E"], ref["E"])
     assert np.array_equal(shard.rep_of_slot, ref["rep_of_slot"]) and shard.n_ex == int(ref["n_ex"][0])
     assert shard.n_ex > 0
@@ -80,14 +82,14 @@ def test_two_rank_ladder_equals_single_process():
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    ps = [ctx.Process(target=_sharded, args=(r, 2, port, q)) for r in range(2)]
+    ps = [ctx.Process(target=_sharded, args=(r, 2, port, q, 2)) for r in range(2)]
     for p in ps:
         p.start()
     out = sorted([q.get(timeout=240) for _ in ps], key=lambda x: x[0])
     for p in ps:
         p.join(timeout=60)
         assert p.exitcode == 0
-    ref = _reference()
+    ref = _reference(2)
     sigma = np.concatenate([o[1] for o in out]); E = np.concatenate([o[2] for o in out])
     n_acc = np.concatenate([o[3] for o in out])
     assert np.array_equal(sigma, ref["sigma"]) and np.array_equal(E, ref["E"]) and np.array_equal(n_acc, ref["n_acc"])

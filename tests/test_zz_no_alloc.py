@@ -43,11 +43,33 @@ def test_noalloc_energy_matches_energy_two_calls(cuda, precision):
         assert np.abs(got - want).max() <= tol * max(1.0, np.abs(want).max()), (got, want)
 
 
-def test_noalloc_energy_refuses_too_many_configurations(cuda):
+def test_noalloc_energy_at_the_limit(cuda):
+    """65,535 configurations (the documented maximum) of a 16-site cell run and match nce_ce_energy."""
+    torch = cuda
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.workloads import ce_config
+    f = _fn()
+    gce, sig = ce_config(2, seed=0)
+    R = 65535
+    rng = np.random.default_rng(5)
+    sig_r = np.stack([sig[rng.permutation(len(sig))] for _ in range(64)]).astype(np.int8)
+    sig_r = np.ascontiguousarray(np.tile(sig_r, (R // 64 + 1, 1))[:R])
+    sd = torch.as_tensor(sig_r).cuda()
+    want = gce.batched_energy(sd).cpu().numpy()
+    out = torch.full((R,), float("nan"), dtype=torch.float64, device="cuda")
+    _lib.check(f(gce.handle, sd.data_ptr(), R, 64, out.data_ptr(), _lib.stream_ptr()), "nce_ce_energy_noalloc")
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert np.all(np.isfinite(got))
+    assert np.abs(got - want).max() <= 1e-10 * max(1.0, np.abs(want).max())
+
+
+@pytest.mark.parametrize("R", [65536, 65537])
+def test_noalloc_energy_refuses_too_many_configurations(cuda, R):
     torch = cuda
     from neuralce_gb300.workloads import ce_config
     f = _fn()
     gce, _ = ce_config(2, seed=0)
     dummy = torch.zeros(1, dtype=torch.float64, device="cuda")
-    rc = f(gce.handle, dummy.data_ptr(), 65537, 64, dummy.data_ptr(), None)
+    rc = f(gce.handle, dummy.data_ptr(), R, 64, dummy.data_ptr(), None)
     assert rc == -1                                          # NCE_ERR_INVALID, nothing launched
