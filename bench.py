@@ -646,7 +646,7 @@ def main():
         from neuralce_gb300.autotune import best_launch
         ws = (args.warps,) if args.warps else (4, 8, 16, 32)
         cls = (args.cluster,) if args.cluster else ((1, 2, 4, 8, 16) if args.path != 1 else (1,))
-        paths = (2, 3) if args.path == 0 else (args.path,)
+        paths = (2,) if args.path == 0 else (args.path,)
         (args.warps, args.cluster, args.path), t = best_launch(gce, st, args.precision, args.path, ws, cls, paths=paths)
         tuned = {f"{w}x{c}/p{p}": round(v, 3) for (w, c, p), v in t.items()}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -712,7 +712,7 @@ def main():
     # shared memory
     traffic = 155_392 if (args.L == 8 and args.R == 32 and T == 5000 and args.path == 2) else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-            "kernel": {1: "ce_pt_chunk_kernel", 3: "ce_bin2_chunk_kernel"}.get(args.path, "ce_bin_chunk_kernel"),
+            "kernel": {1: "ce_pt_chunk_kernel"}.get(args.path, "ce_bin_chunk_kernel"),
             "peak_source": src,
             "algorithmic_bytes_per_launch": R * T * B_GATHER}
     nce_line = nce_tc_line = nce_bf16_line = nce_shipped_line = None
@@ -739,7 +739,7 @@ def main():
                 "config": workload_config(args, gce), "clocks": clocks, "e2e": e2e, "gpu_launches": 2 * args.steps,
                 "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "nce_tcgen05_split": nce_tc_line, "nce_tcgen05_bf16": nce_bf16_line, "nce_shipped_model": nce_shipped_line, "batch": batch_line, "serve": serve_line,
                 "launch": {"warps_per_cta": args.warps, "ctas_per_replica": args.cluster,
-                           "path": ["auto", "general", "sign-parity", "sign-parity, two steps in flight"][args.path],
+                           "path": ["auto", "general", "sign-parity"][args.path],
                            "autotune_ms": tuned},
                 "accept_rate": float(st.n_acc.sum().item()) / max(1, R * step)}
         print(json.dumps(line), flush=True)

@@ -133,6 +133,10 @@ typedef struct {
                               cluster-vector column of the product of point functions (exact integers on the
                               sign-parity path), kept current by the chunk kernel; the float64 energy follows
                               from them exactly (nce_ce_energy_from_counts) */
+    int64_t *n_near;       /* (R) or NULL: near-threshold steps per replica (accumulated).  A swap with dE is accepted
+                              when log u < -beta dE (neuralce/ce/pt_mcmc_ce.py:563); a step is near its threshold when
+                              |dE + ln(u) / beta| < the chunk's near_eV, the stated per-swap dE error bound of the
+                              precision form: only there can a decision differ from a float64 reference's */
 } nce_pt_state;
 
 /* One chunk of steps.  Proposals: host-supplied stream (prop_a/prop_b/prop_u device arrays indexed
@@ -151,13 +155,14 @@ typedef struct {
     const double *ex_u;        /* (ceil((R-1)/2)) device uniforms, or NULL -> Philox */
     int32_t precision;         /* 64 or 32 */
     int32_t warps;             /* warps per replica (0 = default) */
-    int32_t path;              /* 0 auto, 1 general point-function products, 2 sign parity (point functions in {-1,+1}),
-                                  3 sign parity with two steps evaluated together (cluster order <= 4) */
+    int32_t path;              /* 0 auto, 1 general point-function products, 2 sign parity (point functions in {-1,+1}) */
     int32_t cluster;           /* sign parity: CTAs per replica (1, 2, 4, 8; thread-block cluster); the cell must fit in
                                   shared memory, otherwise one CTA is used */
     int64_t *step_dev;         /* device counter or NULL: when set, the chunk's first global step is read from it
                                   (step0 is ignored) and it advances by n_steps when the chunk ends, so that a
                                   captured CUDA graph of chunks continues the Philox stream on every replay */
+    double near_eV;            /* near-threshold band of n_near; 0 = the form's stated dE error bound: 1e-9 eV at
+                                  precision 64 (its fixed-point sums are within 2e-13 eV of float64), 1e-6 eV at 32 */
 } nce_pt_chunk;
 
 int nce_ce_run_chunk(nce_ce_handle h, const nce_pt_state *st, const nce_pt_chunk *ck, void *stream);
@@ -245,6 +250,8 @@ typedef struct {
     double *E;             /* (R) energy: sum(e)/norm + head_b */
     const float *beta_slot; int32_t *rep_of_slot, *slot_of_rep; const int32_t *ladder_id;
     int64_t *n_acc, *n_ex;
+    int64_t *n_near;       /* (R) or NULL: Metropolis steps whose margin |dE_eV + ln(u) / beta| was below the chunk's
+                              near_eV (accept rule dE_eV <= 0 or u < exp(-beta dE_eV), neuralce/nce/mcmc.py:179) */
 } nce_nce_state;
 
 typedef struct {
@@ -260,6 +267,8 @@ typedef struct {
     int32_t cluster;       /* CTAs (SMs) per replica: 1, 2, 4 or 8 (thread-block cluster) */
     int32_t ctas_per_sm;   /* 0 or 1: one CTA per SM; 2: two CTAs per SM (at most 128 registers a thread, layer
                               weights read through L1; the CTA's shared memory must fit half an SM) */
+    double near_eV;        /* near-threshold band of n_near; 0 = the form's stated dE error bound: 1e-4 eV (float32
+                              and split-bf16 contractions), 1e-2 eV (bf16 contractions) */
 } nce_nce_chunk;
 
 int nce_nce_create(const nce_nce_desc *desc, nce_nce_handle *out);

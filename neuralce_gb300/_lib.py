@@ -28,13 +28,15 @@ class NceCeTables(C.Structure):
 
 class NcePtState(C.Structure):
     _fields_ = [("R", i32), ("N", i64), ("sigma", vp), ("E", vp), ("beta_slot", vp), ("rep_of_slot", vp),
-                ("slot_of_rep", vp), ("ladder_id", vp), ("E_min_rep", vp), ("n_acc", vp), ("n_ex", vp), ("cv", vp)]
+                ("slot_of_rep", vp), ("ladder_id", vp), ("E_min_rep", vp), ("n_acc", vp), ("n_ex", vp), ("cv", vp),
+                ("n_near", vp)]
 
 
 class NcePtChunk(C.Structure):
     _fields_ = [("n_steps", i64), ("step0", i64), ("prop_a", vp), ("prop_b", vp), ("prop_u", vp), ("seed", u64),
                 ("sample_interval", i64), ("E_samples", vp), ("do_exchange", i32), ("ex_parity", i32),
-                ("ex_u", vp), ("precision", i32), ("warps", i32), ("path", i32), ("cluster", i32), ("step_dev", vp)]
+                ("ex_u", vp), ("precision", i32), ("warps", i32), ("path", i32), ("cluster", i32), ("step_dev", vp),
+                ("near_eV", f64)]
 
 
 class NceNceDesc(C.Structure):
@@ -51,13 +53,14 @@ class NceNceDesc(C.Structure):
 
 class NceNceState(C.Structure):
     _fields_ = [("R", i32), ("N", i64), ("sigma", vp), ("h0", vp), ("hmid", vp), ("e", vp), ("E", vp),
-                ("beta_slot", vp), ("rep_of_slot", vp), ("slot_of_rep", vp), ("ladder_id", vp), ("n_acc", vp), ("n_ex", vp)]
+                ("beta_slot", vp), ("rep_of_slot", vp), ("slot_of_rep", vp), ("ladder_id", vp), ("n_acc", vp), ("n_ex", vp),
+                ("n_near", vp)]
 
 
 class NceNceChunk(C.Structure):
     _fields_ = [("n_steps", i64), ("step0", i64), ("prop_a", vp), ("prop_b", vp), ("prop_u", vp), ("seed", u64),
                 ("sample_interval", i64), ("E_samples", vp), ("dE_out", vp), ("force", i32), ("exchange_rounds", i32),
-                ("ex_parity", i32), ("ex_u", vp), ("cluster", i32), ("ctas_per_sm", i32)]
+                ("ex_parity", i32), ("ex_u", vp), ("cluster", i32), ("ctas_per_sm", i32), ("near_eV", f64)]
 
 
 class NceServerConfig(C.Structure):

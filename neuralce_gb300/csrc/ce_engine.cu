@@ -70,6 +70,9 @@ struct CEJob {
     int64_t *cv;           // (R, n_cols) tracked cluster-vector sums or null
     const int64_t *ecol_fix; // (n_cols) 2 eci of each column in fixed point (x 2^fix_shift), float64 kernels
     int32_t fix_shift;
+    int64_t *n_near;       // (R) near-threshold step counts or null
+    double near_eV;        // near-threshold band (eV)
+    int64_t near_fix;      // the band in fixed point, rounded up, plus one unit (threshold rounding), fixed-point kernels
 };
 
 struct CEBatch {
@@ -261,7 +264,7 @@ __global__ void __launch_bounds__(1024) ce_pt_chunk_kernel(const __grid_constant
     const int32_t t = jb.slot_of_rep[r];
     const double beta = (double)jb.beta_slot[t];
     double E = jb.E[r], Emin = jb.E_min_rep[r];
-    int64_t nacc = 0;
+    int64_t nacc = 0, nnear = 0;
     const int R = jb.R;
     const int64_t g0 = jb.step_dev ? *jb.step_dev : jb.step0;
     for (int64_t s = 0; s < jb.n_steps; ++s) {
@@ -287,6 +290,7 @@ __global__ void __launch_bounds__(1024) ce_pt_chunk_kernel(const __grid_constant
             Real dE = block_delta<Real, MO>(jb, sig, cs, smem, L, tloc, tpfc, teci);
             if (threadIdx.x == 0) {
                 const double dEd = (double)dE;
+                if (beta > 0.0 && fabs(dEd + log(cs.u) / beta) < jb.near_eV) ++nnear;
                 if (log(cs.u) < -beta * dEd) {
                     sig[cs.ia] = (int8_t)cs.sb; sig[cs.ib] = (int8_t)cs.sa;
                     E += dEd; ++nacc;
@@ -299,7 +303,10 @@ __global__ void __launch_bounds__(1024) ce_pt_chunk_kernel(const __grid_constant
                 jb.E_samples[((s + 1) / jb.sample_interval - 1) * R + t] = E;
         }
     }
-    if (threadIdx.x == 0) { jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc; }
+    if (threadIdx.x == 0) {
+        jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc;
+        if (jb.n_near) jb.n_near[r] += nnear;
+    }
 }
 
 // ── sign-parity kernel for point functions in {-1, +1} ───────────────────────────────────────────────
@@ -321,7 +328,7 @@ struct BinProp {
 struct BinLayout {
     size_t bix, rcol, chunk, nb, ecol, sig, bits, cnt, dcv, total;
     __host__ __device__ static BinLayout make(int nB, int J, int mo, int n_nbr, int n_pfc, int n_cols, int max_chunks, size_t acc_bytes,
-                                                int64_t N, bool tables, bool sig_smem, int pipe = 1) {
+                                                int64_t N, bool tables, bool sig_smem) {
         BinLayout L; size_t o = 0;
         auto al = [](size_t x, size_t a) { return (x + a - 1) / a * a; };
         if (tables) {
@@ -334,8 +341,8 @@ struct BinLayout {
         L.nb = o; o = al(o + sizeof(int32_t) * 4 * (size_t)nB * n_nbr, 16);
         L.ecol = o; o = al(o + acc_bytes * (size_t)n_cols, 16);
         if (sig_smem) { L.sig = o; o = al(o + (size_t)N, 16); } else { L.sig = 0; }
-        L.bits = o; o = al(o + (size_t)pipe * 2 * n_pfc * n_nbr, 16);       // [step][side][pfc][n_nbr]
-        L.cnt = o; o = al(o + sizeof(int32_t) * 2 * (size_t)pipe * n_cols, 16);   // [step][buffer parity][n_cols]
+        L.bits = o; o = al(o + (size_t)2 * n_pfc * n_nbr, 16);             // [side][pfc][n_nbr]
+        L.cnt = o; o = al(o + sizeof(int32_t) * 2 * (size_t)n_cols, 16);   // [buffer parity][n_cols]
         L.dcv = o; o = al(o + sizeof(int32_t) * (size_t)n_cols, 16);       // chunk change of the cluster-vector sums
         L.total = o;
         return L;
@@ -453,7 +460,7 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
         __syncthreads();                                   // ecol (float64) was just written; the same bytes take the fixed-point values
         for (int c = tid; c < n_cols; c += nt) efix[c] = (long long)__ldg(jb.ecol_fix + c);
     }
-    int64_t nacc = 0;
+    int64_t nacc = 0, nnear = 0;
     const int R = jb.R;
     // proposals are drawn 32 at a time (one per lane of the producer warp), one batch ahead of their use
     const int64_t g0 = jb.step_dev ? *jb.step_dev : jb.step0;
@@ -566,6 +573,10 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                         part = (long long)s0 + ((long long)s1 << 21) + ((long long)s2 << 42);
                     }
                     accept = part < P.thr;
+                    if (lane == 0) {                    // near the threshold: |dE 2^S - (-ln u / beta) 2^S| below the band
+                        const long long dd = part - (long long)P.thr;
+                        nnear += (dd < 0 ? -dd : dd) < (long long)jb.near_fix;
+                    }
                     if (lane == 0 && accept) {
                         sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new;
                         dsum += part; ++nacc;
@@ -579,6 +590,7 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                     part = warp_sum(part);              // butterfly: every lane holds the same sum
                     const double dEd = (double)part;
                     accept = P.logu < -beta * dEd;
+                    if (lane == 0 && beta > 0.0) nnear += fabs(dEd + P.logu / beta) < jb.near_eV;
                     if (lane == 0 && accept) {
                         sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new;
                         E += dEd; ++nacc;
@@ -613,257 +625,14 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     if (rank == 0) {
         if (sig_smem)
             for (int64_t i = tid; i < jb.N; i += nt) gsig[i] = sig[i];
-        if (tid == 0) { jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc; }
+        if (tid == 0) {
+            jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc;
+            if (jb.n_near) jb.n_near[r] += nnear;
+        }
         if (track)
             for (int c = tid; c < n_cols; c += nt) jb.cv[(int64_t)r * n_cols + c] += dcv[c];
     }
     if (CLUSTER) cg::this_cluster().sync();              // no CTA leaves while others may still add into its counters
-}
-
-// Two steps in flight (same tables and layout, two of everything per step).  Steps s and s+1 are evaluated
-// together on the configuration before step s.  Step s+1 depends on step s only when s is accepted and one of s's
-// sites is one of s+1's sites or lies in s+1's neighbourhoods (the gather sees it); s+1 is then evaluated again in
-// the next round.  Otherwise both decisions stand, in order, with the same arithmetic as one step at a time, so the
-// trajectory is the sequential one.  The row chunks of both steps form one list over the consumer warps (and the
-// CTAs of a cluster).
-template <typename Acc, int MO, bool CLUSTER>
-__global__ void __launch_bounds__(1024) ce_bin2_chunk_kernel(const __grid_constant__ CEBatch bt, int32_t sig_budget) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ BinProp prop[128];                     // proposals; at least 39 are drawn ahead of the current step
-    __shared__ int32_t flg[4];                        // near A, near B, B touches A's sites, steps advanced
-    int CL = 1, rank = 0;
-    if (CLUSTER) { cg::cluster_group cl = cg::this_cluster(); CL = (int)cl.num_blocks(); rank = (int)cl.block_rank(); }
-    const int rep_idx = blockIdx.x / CL;
-    const int j = find_job(bt, rep_idx);
-    const CEJob &jb = bt.job[j];
-    const int r = rep_idx - jb.cta_base;
-    if (r >= jb.R) return;
-    const int tid = threadIdx.x, nt = blockDim.x, nw = nt >> 5, lane = tid & 31, warp = tid >> 5;
-    const int ncons = nw > 1 ? nw - 1 : 1;
-    const bool producer = nw > 1 ? (warp == nw - 1) : (tid == 0);
-    const bool drawer = nw > 1 ? (warp == nw - 1) : true;
-    const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc, n_cols = jb.n_cols;
-    const int32_t sig_smem = jb.sig_smem;
-    const BinLayout L = BinLayout::make(jb.nB, jb.J, MO, n_nbr, n_pfc, n_cols, jb.max_chunks, sizeof(Acc), sig_budget, bt.tables_in_smem,
-                                        sig_budget > 0, 2);
-    const uint16_t *tbix; const uint8_t *trcol;
-    const size_t nl = (size_t)jb.nB * jb.J * MO, ne = (size_t)jb.nB * jb.J;
-    if (bt.tables_in_smem) {
-        uint16_t *sb = reinterpret_cast<uint16_t *>(smem + L.bix); uint8_t *sc = smem + L.rcol;
-        for (size_t i = tid; i < nl; i += nt) sb[i] = __ldg(jb.bix + i);
-        for (size_t i = tid; i < ne; i += nt) sc[i] = __ldg(jb.rcol + i);
-        tbix = sb; trcol = sc;
-    } else {
-        tbix = jb.bix; trcol = jb.rcol;
-    }
-    (void)trcol;
-    uint32_t *chunks = reinterpret_cast<uint32_t *>(smem + L.chunk);
-    for (int i = tid; i < jb.nB * jb.max_chunks; i += nt) chunks[i] = __ldg(jb.chunks + i);
-    int4 *nbt = reinterpret_cast<int4 *>(smem + L.nb);
-    for (int i = tid; i < jb.nB * n_nbr; i += nt) nbt[i] = make_int4(__ldg(jb.nb_uo + 3 * i), __ldg(jb.nb_uo + 3 * i + 1),
-                                                                      __ldg(jb.nb_uo + 3 * i + 2), __ldg(jb.nb_b + i));
-    Acc *ecol = reinterpret_cast<Acc *>(smem + L.ecol);
-    const Acc *gecol = reinterpret_cast<const Acc *>(jb.ecol2);
-    int32_t *cnt = reinterpret_cast<int32_t *>(smem + L.cnt);      // [step][parity][n_cols]
-    int32_t *dcv = reinterpret_cast<int32_t *>(smem + L.dcv);
-    const bool track = jb.cv != nullptr;
-    for (int c = tid; c < n_cols; c += nt) {
-        ecol[c] = gecol[c]; dcv[c] = 0;
-        for (int q = 0; q < 4; ++q) cnt[q * n_cols + c] = 0;
-    }
-    int32_t *rcnt[16];
-    for (int q = 0; q < 16; ++q) rcnt[q] = cnt;
-    if (CLUSTER) {
-        cg::cluster_group cl = cg::this_cluster();
-        for (int q = 0; q < CL && q < 16; ++q) rcnt[q] = cl.map_shared_rank(cnt, q);
-    }
-    int8_t *gsig = jb.sigma + (int64_t)r * jb.N;
-    int8_t *sig = sig_smem ? reinterpret_cast<int8_t *>(smem + L.sig) : gsig;
-    if (sig_smem)
-        for (int64_t i = tid; i < jb.N; i += nt) sig[i] = gsig[i];
-    uint8_t *bits = smem + L.bits;                         // [step][side][pfc][n_nbr]
-    const uint8_t *sbits = jb.sbits;
-    const int32_t t = jb.slot_of_rep[r];
-    const double beta = (double)jb.beta_slot[t];
-    double E = jb.E[r], Emin = jb.E_min_rep[r];
-    int64_t nacc = 0;
-    const int R = jb.R;
-    const int64_t n_steps = jb.n_steps;
-    const int64_t g0 = jb.step_dev ? *jb.step_dev : jb.step0;
-    int64_t drawn = n_steps < 64 ? n_steps : 64;
-    if (warp == 0) {
-        if (lane < n_steps) bin_propose(jb, g0, lane, t, prop[lane]);
-        if (lane + 32 < n_steps) bin_propose(jb, g0, lane + 32, t, prop[lane + 32]);
-    }
-    if (tid < 4) flg[tid] = 0;
-    __syncthreads();
-    if (CLUSTER) cg::this_cluster().sync();
-    auto record = [&](int64_t si) {                        // thread 0, after step si
-        Emin = fmin(Emin, E);
-        if (rank == 0 && jb.E_samples && (si + 1) % jb.sample_interval == 0)
-            jb.E_samples[((si + 1) / jb.sample_interval - 1) * R + t] = E;
-    };
-    int par = 0;
-    int64_t s = 0;
-    while (s < n_steps) {
-        if (drawn - s <= 40 && drawn < n_steps) {          // keep the ring ahead (uniform condition)
-            if (drawer) {
-                const int64_t q = drawn + lane;
-                if (q < n_steps) bin_propose(jb, g0, q, t, prop[q & 127]);
-            }
-            drawn += 32;
-        }
-        const BinProp &PA = prop[s & 127];
-        const bool hasB = s + 1 < n_steps;
-        const BinProp &PB = prop[(s + 1) & 127];
-        const int saA = sig[PA.ia], sbA = sig[PA.ib];
-        const bool vA = saA != sbA;
-        int saB = 0, sbB = 0;
-        if (hasB) { saB = sig[PB.ia]; sbB = sig[PB.ib]; }
-        const bool vB = hasB && saB != sbB;
-        int adv;
-        if (vA || vB) {
-            // 1. neighbourhood bits of both steps (entries [0, 2n) step A, [2n, 4n) step B)
-            const int ct = ncons * 32;
-            for (int q = tid; q < 4 * n_nbr && tid < ct; q += ct) {
-                const int stp = q >= 2 * n_nbr;
-                if (stp ? !vB : !vA) continue;
-                const int qq = q - stp * 2 * n_nbr;
-                const int side = qq >= n_nbr, n = side ? qq - n_nbr : qq;
-                const BinProp &P = stp ? PB : PA;
-                const int b0 = side ? P.bb : P.ba;
-                const int32_t *k = side ? P.kb : P.ka;
-                const int4 nbe = nbt[b0 * n_nbr + n];
-                const uint32_t st = ((((uint32_t)wrap_add(k[0], nbe.x, jb.d0) * (uint32_t)jb.d1 + (uint32_t)wrap_add(k[1], nbe.y, jb.d1)) *
-                                      (uint32_t)jb.d2 + (uint32_t)wrap_add(k[2], nbe.z, jb.d2)) * (uint32_t)jb.nB + (uint32_t)nbe.w);
-                const int so = sig[st];
-                const int sa_new = stp ? sbB : sbA, sb_new = stp ? saB : saA;
-                const int sn = (st == (uint32_t)P.ia) ? sa_new : ((st == (uint32_t)P.ib) ? sb_new : so);
-                const int isa = side && (st == (uint32_t)P.ia);
-                if (isa) flg[stp] = 1;
-                if (stp && (st == (uint32_t)PA.ia || st == (uint32_t)PA.ib)) flg[2] = 1;
-                uint8_t *bs = bits + ((size_t)stp * 2 + side) * n_pfc * n_nbr;
-                for (int c = 0; c < n_pfc; ++c)
-                    bs[c * n_nbr + n] = (uint8_t)(sbits[c * 4 + so] | (sbits[c * 4 + sn] << 1) | (isa << 2));
-            }
-            __syncthreads();
-            if (!producer || nw == 1) {
-                // 2. rows of both steps: one list of column-aligned chunks
-                const int ncaA = vA ? __ldg(jb.n_chunks + PA.ba) : 0, ncaB = vB ? __ldg(jb.n_chunks + PB.ba) : 0;
-                const int ncA = vA ? ncaA + __ldg(jb.n_chunks + PA.bb) : 0;
-                const int ncB = vB ? ncaB + __ldg(jb.n_chunks + PB.bb) : 0;
-                const int total = ncA + ncB;
-                const bool nearA = flg[0] != 0, nearB = flg[1] != 0;
-                const int cw = nw > 1 ? warp : 0;
-                auto chunk_count = [&](int k, int &col, int &stp) -> int {
-                    stp = k >= ncA;
-                    const int k0 = stp ? k - ncA : k;
-                    const BinProp &P = stp ? PB : PA;
-                    const int nca = stp ? ncaB : ncaA;
-                    const int side = k0 >= nca, kk = side ? k0 - nca : k0;
-                    const int b0 = side ? P.bb : P.ba;
-                    const uint32_t d = chunks[b0 * jb.max_chunks + kk];
-                    col = (int)(d & 0xffu);
-                    const int start = (int)((d >> 8) & 0xffffu), len = (int)(d >> 24);
-                    int sgn = 0;
-                    if (lane < len) {
-                        const int rr = start + lane;
-                        const uint16_t *bx = tbix + ((size_t)b0 * jb.J + rr) * MO;
-                        const uint8_t *bs = bits + ((size_t)stp * 2 + side) * n_pfc * n_nbr;
-                        unsigned x = 0, y = 0;
-                        if (MO == 4) {
-                            const uint2 w = *reinterpret_cast<const uint2 *>(bx);
-                            const unsigned v0 = bs[w.x & 0xffffu], v1 = bs[w.x >> 16], v2 = bs[w.y & 0xffffu], v3 = bs[w.y >> 16];
-                            x = v0 ^ v1 ^ v2 ^ v3; y = v0 | v1 | v2 | v3;
-                        } else {
-#pragma unroll
-                            for (int m = 0; m < MO; ++m) { const unsigned vv = bs[bx[m]]; x ^= vv; y |= vv; }
-                        }
-                        const bool skip = side && (stp ? nearB : nearA) && (y & 4u);
-                        if (!skip && ((x ^ (x >> 1)) & 1u)) sgn = (x & 1u) ? 1 : -1;
-                    }
-                    return sgn;
-                };
-                const int gw = rank * ncons + cw, gstr = ncons * CL;
-                for (int k = gw; k < total; k += 2 * gstr) {
-                    const int k2 = k + gstr;
-                    int c1 = 0, c2 = 0, p1 = 0, p2 = 0;
-                    const int s1 = chunk_count(k, c1, p1);
-                    const int s2 = k2 < total ? chunk_count(k2, c2, p2) : 0;
-                    const int n1 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s1);
-                    const int n2 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s2);
-                    if (lane == 0) {
-                        const int o1 = (p1 * 2 + par) * n_cols + c1, o2 = (p2 * 2 + par) * n_cols + c2;
-                        if (CLUSTER) {
-                            for (int q = 0; q < CL; ++q) {
-                                if (n1) atomicAdd(rcnt[q] + o1, n1);
-                                if (n2) atomicAdd(rcnt[q] + o2, n2);
-                            }
-                        } else {
-                            if (n1) atomicAdd(&cnt[o1], n1);
-                            if (n2) atomicAdd(&cnt[o2], n2);
-                        }
-                    }
-                }
-            }
-            if (CLUSTER) cg::this_cluster().sync(); else __syncthreads();
-            // 3. decisions in order (warp 0; every lane holds the same sums)
-            if (warp == 0) {
-                int32_t *cA = cnt + (0 * 2 + par) * n_cols, *cB = cnt + (1 * 2 + par) * n_cols;
-                double dEA = 0.0, dEB = 0.0;
-                bool accA = false, accB = false;
-                if (vA) {
-                    Acc part = Acc(0);
-                    for (int c = lane; c < n_cols; c += 32) { const int n = cA[c]; if (n) part += ecol[c] * (Acc)n; }
-                    part = warp_sum(part);
-                    dEA = (double)part;
-                    accA = PA.logu < -beta * dEA;
-                }
-                const bool touch = PB.ia == PA.ia || PB.ia == PA.ib || PB.ib == PA.ia || PB.ib == PA.ib;
-                const bool redo = hasB && accA && (touch || (vB && flg[2] != 0));
-                if (vB && !redo) {
-                    Acc part = Acc(0);
-                    for (int c = lane; c < n_cols; c += 32) { const int n = cB[c]; if (n) part += ecol[c] * (Acc)n; }
-                    part = warp_sum(part);
-                    dEB = (double)part;
-                    accB = PB.logu < -beta * dEB;
-                }
-                for (int c = lane; c < n_cols; c += 32) {
-                    const int na = cA[c], nb = cB[c];
-                    if (na) { if (track && accA) dcv[c] += 2 * na; cA[c] = 0; }
-                    if (nb) { if (track && accB) dcv[c] += 2 * nb; cB[c] = 0; }
-                }
-                const int a = (!hasB || redo) ? 1 : 2;
-                __syncwarp();                              // every lane has read the flags before lane 0 clears them
-                if (lane == 0) {
-                    if (accA) { sig[PA.ia] = (int8_t)sbA; sig[PA.ib] = (int8_t)saA; E += dEA; ++nacc; }
-                    record(s);
-                    if (a == 2) {
-                        if (accB) { sig[PB.ia] = (int8_t)sbB; sig[PB.ib] = (int8_t)saB; E += dEB; ++nacc; }
-                        record(s + 1);
-                    }
-                    flg[3] = a;
-                    flg[0] = flg[1] = flg[2] = 0;
-                }
-            }
-            par ^= 1;
-            __syncthreads();
-            adv = flg[3];
-        } else {
-            adv = hasB ? 2 : 1;                            // neither step changes the configuration
-            if (tid == 0) { record(s); if (hasB) record(s + 1); }
-            __syncthreads();
-        }
-        s += adv;
-    }
-    if (rank == 0) {
-        if (sig_smem)
-            for (int64_t i = tid; i < jb.N; i += nt) gsig[i] = sig[i];
-        if (tid == 0) { jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc; }
-        if (track)
-            for (int c = tid; c < n_cols; c += nt) jb.cv[(int64_t)r * n_cols + c] += dcv[c];
-    }
-    if (CLUSTER) cg::this_cluster().sync();
 }
 
 // Full energy on the sign-parity tables, bit-sliced.  The occupancies become bit planes: per replica, point-
@@ -1183,12 +952,17 @@ static CEJob make_job(const nce_ce_model *m, const nce_pt_state *st, const nce_p
     j.n_cells = m->n_cells; j.N = m->N; j.err = m->err;
     if (st) {
         j.sigma = st->sigma; j.E = st->E; j.beta_slot = st->beta_slot; j.slot_of_rep = st->slot_of_rep;
-        j.E_min_rep = st->E_min_rep; j.n_acc = st->n_acc; j.R = st->R; j.cv = st->cv;
+        j.E_min_rep = st->E_min_rep; j.n_acc = st->n_acc; j.R = st->R; j.cv = st->cv; j.n_near = st->n_near;
     }
     if (ck) {
         j.n_steps = ck->n_steps; j.step0 = ck->step0; j.step_dev = ck->step_dev; j.prop_a = ck->prop_a; j.prop_b = ck->prop_b; j.prop_u = ck->prop_u;
         j.seed = ck->seed; j.sample_interval = ck->sample_interval > 0 ? ck->sample_interval : 1;
         j.E_samples = ck->E_samples;
+        j.near_eV = ck->near_eV > 0.0 ? ck->near_eV : (p64 ? 1e-9 : 1e-6);
+        if (j.fix_shift > 0) {
+            const double nf = std::ldexp(j.near_eV, j.fix_shift);
+            j.near_fix = nf >= 4.0e18 ? (int64_t)4000000000000000000ll : (int64_t)std::ceil(nf) + 1;
+        }
     }
     j.cta_base = cta_base;
     return j;
@@ -1203,36 +977,8 @@ static int launch_chunk_mo(const CEBatch &bt, int total, int warps, size_t smem,
     return NCE_OK;
 }
 
-static int launch_bin_kernel(void (*kern)(CEBatch, int32_t), const CEBatch &bt, int total, int warps, size_t smem, int sig_smem,
-                             cudaStream_t s, int CL) {
-    NCE_CUDA(::nce::raise_smem_limit((const void *)kern, smem));
-    if (CL > 8) NCE_CUDA(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    if (CL <= 1) {
-        kern<<<total, warps * 32, smem, s>>>(bt, sig_smem);
-    } else {
-        cudaLaunchConfig_t cfg; std::memset(&cfg, 0, sizeof(cfg));
-        cfg.gridDim = dim3((unsigned)(total * CL)); cfg.blockDim = dim3(warps * 32); cfg.dynamicSmemBytes = smem; cfg.stream = s;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = (unsigned)CL; attr[0].val.clusterDim.y = 1; attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr; cfg.numAttrs = 1;
-        NCE_CUDA(cudaLaunchKernelEx(&cfg, kern, bt, sig_smem));
-    }
-    NCE_CUDA(cudaGetLastError());
-    return NCE_OK;
-}
-
 template <typename Acc, int MO>
-static int launch_bin_mo(const CEBatch &bt, int total, int warps, size_t smem, int sig_smem, cudaStream_t s, int CL, int pipe) {
-    if (pipe == 2) {
-        if constexpr (MO <= 4) {
-            auto k1 = ce_bin2_chunk_kernel<Acc, MO, false>;
-            auto kc = ce_bin2_chunk_kernel<Acc, MO, true>;
-            return launch_bin_kernel(CL <= 1 ? k1 : kc, bt, total, warps, smem, sig_smem, s, CL);
-        } else {
-            return fail(NCE_ERR_UNSUPPORTED, "two steps in flight: cluster order %d > 4", MO);
-        }
-    }
+static int launch_bin_mo(const CEBatch &bt, int total, int warps, size_t smem, int sig_smem, cudaStream_t s, int CL) {
     if (CL <= 1) {
         auto kern = ce_bin_chunk_kernel<Acc, MO, false>;
         NCE_CUDA(::nce::raise_smem_limit((const void *)kern, smem));
@@ -1255,9 +1001,9 @@ static int launch_bin_mo(const CEBatch &bt, int total, int warps, size_t smem, i
 }
 
 template <typename Acc>
-static int launch_bin(const CEBatch &bt, int mo, int total, int warps, size_t smem, int sig_smem, cudaStream_t s, int CL, int pipe) {
+static int launch_bin(const CEBatch &bt, int mo, int total, int warps, size_t smem, int sig_smem, cudaStream_t s, int CL) {
     switch (mo) {
-#define NCE_BIN_CASE(M) case M: return launch_bin_mo<Acc, M>(bt, total, warps, smem, sig_smem, s, CL, pipe);
+#define NCE_BIN_CASE(M) case M: return launch_bin_mo<Acc, M>(bt, total, warps, smem, sig_smem, s, CL);
         NCE_BIN_CASE(1) NCE_BIN_CASE(2) NCE_BIN_CASE(3) NCE_BIN_CASE(4) NCE_BIN_CASE(5) NCE_BIN_CASE(6) NCE_BIN_CASE(7) NCE_BIN_CASE(8)
 #undef NCE_BIN_CASE
         default: return fail(NCE_ERR_UNSUPPORTED, "cluster order %d > 8", mo);
@@ -1298,6 +1044,7 @@ static int check_chunk(const nce_pt_state *st, const nce_pt_chunk *ck) {
     NCE_CHECK(ck->cluster == 0 || ck->cluster == 1 || ck->cluster == 2 || ck->cluster == 4 || ck->cluster == 8 ||
               ck->cluster == 16, "chunk: cluster must be 0, 1, 2, 4, 8 or 16");
     NCE_CHECK(!ck->do_exchange || !ck->ex_u || (ck->ex_parity == 0 || ck->ex_parity == 1), "chunk: ex_parity must be 0/1");
+    NCE_CHECK(ck->near_eV >= 0.0 && ck->near_eV <= 1e3, "chunk: near_eV must be in [0, 1e3]");
     (void)st;
     return NCE_OK;
 }
@@ -1324,12 +1071,9 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
         NCE_CHECK(cks[j].path == path, "batch: all chunks must use the same path");
         all_bin = all_bin && hs[j]->binary;
     }
-    NCE_CHECK(path >= 0 && path <= 3, "chunk: path must be 0 (auto), 1 (general), 2 (sign parity) or 3 (sign parity, two "
-                                      "steps in flight)");
-    NCE_CHECK(path < 2 || all_bin, "chunk: the sign-parity paths need point functions in {-1, +1}");
-    NCE_CHECK(path != 3 || mo <= 4, "chunk: two steps in flight support cluster orders up to 4");
-    const bool use_bin = (path >= 2) || (path == 0 && all_bin);
-    const int pipe = path == 3 ? 2 : 1;
+    NCE_CHECK(path >= 0 && path <= 2, "chunk: path must be 0 (auto), 1 (general) or 2 (sign parity)");
+    NCE_CHECK(path < 2 || all_bin, "chunk: the sign-parity path needs point functions in {-1, +1}");
+    const bool use_bin = (path == 2) || (path == 0 && all_bin);
     for (int j = 0; j < n_jobs; ++j)
         NCE_CHECK(!sts[j].cv || use_bin, "chunk: tracked cluster-vector sums need the sign-parity path");
     CEBatch bt; std::memset(&bt, 0, sizeof(bt));
@@ -1341,8 +1085,8 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
         size_t t_on = 0, t_off = 0; int64_t maxN = 0;
         for (int j = 0; j < n_jobs; ++j) {
             const nce_ce_model *m = hs[j];
-            t_on = std::max(t_on, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, m->n_cols, m->max_chunks, accb, 0, true, false, pipe).total);
-            t_off = std::max(t_off, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, m->n_cols, m->max_chunks, accb, 0, false, false, pipe).total);
+            t_on = std::max(t_on, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, m->n_cols, m->max_chunks, accb, 0, true, false).total);
+            t_off = std::max(t_off, BinLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, m->n_cols, m->max_chunks, accb, 0, false, false).total);
             maxN = std::max(maxN, m->N);
         }
         const size_t limit = 200 * 1024;
@@ -1389,8 +1133,8 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
             for (int j = 0; j < n_jobs; ++j) if (!bt.job[j].sig_smem) CL = 1;
         }
         if (use_bin)
-            rc = precision == 64 ? launch_bin<double>(bt, mo, total, warps, smem, sig_smem, s, CL, pipe)
-                                 : launch_bin<float>(bt, mo, total, warps, smem, sig_smem, s, CL, pipe);
+            rc = precision == 64 ? launch_bin<double>(bt, mo, total, warps, smem, sig_smem, s, CL)
+                                 : launch_bin<float>(bt, mo, total, warps, smem, sig_smem, s, CL);
         else
             rc = precision == 64 ? launch_chunk<double>(bt, mo, total, warps, smem, s)
                                  : launch_chunk<float>(bt, mo, total, warps, smem, s);

@@ -86,6 +86,7 @@ struct NceJob {
     int64_t n_steps, step0; const int32_t *prop_a, *prop_b; const double *prop_u; uint64_t seed;
     int64_t sample_interval; double *E_samples; double *dE_out; int32_t force;   // force: 0 Metropolis, 1 accept, -1 reject
     int32_t *err;
+    int64_t *n_near; double near_eV;          // near-threshold step counts (or null) and their band in eV
 };
 
 __device__ __forceinline__ int32_t wadd(int32_t k, int32_t u, int32_t d) { int32_t q = k + u; return q >= d ? q - d : q; }
@@ -635,7 +636,7 @@ __device__ __forceinline__ void csync() {
 template <bool CLUSTER>
 __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &ctl, unsigned long long *dh, float *X,
                          int32_t *src, const LayerW *LWs, const float *lin, const float *hw, int32_t *ent_site, int32_t *ent_pos,
-                         int8_t *ent_sig, double &E, int64_t &nacc, const NceCtx &cx, TcCtx *tc) {
+                         int8_t *ent_sig, double &E, int64_t &nacc, int64_t &nnear, const NceCtx &cx, TcCtx *tc) {
     const bool leader = cx.rank == 0;
     const int CL = cx.CL, rank = cx.rank;
     const NceDev &m = jb.m;
@@ -955,6 +956,7 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         if (jb.force > 0) a = 1;
         else if (jb.force < 0) a = 0;
         else a = (dEeV <= 0.0) || (ctl.u < exp(-beta * dEeV));
+        if (jb.force == 0 && beta > 0.0 && fabs(dEeV + log(ctl.u) / beta) < jb.near_eV) ++nnear;
         ctl.acc = a;
         if (jb.dE_out) jb.dE_out[s_idx * jb.R + t] = dE;
         if (a) { sig[ctl.si] = (int8_t)ctl.ssj; sig[ctl.sj] = (int8_t)ctl.ssi; E += dE; ++nacc; }
@@ -1079,15 +1081,15 @@ __global__ void __launch_bounds__(256, MINB) nce_chunk_kernel(const __grid_const
     if (m.tc) tc_begin(m.D, tcx, smem + sp.wt, &tc_mbar, &tc_slot);
     const int t = jb.slot_of_rep[r];
     double E = jb.E[r];
-    int64_t nacc = 0;
+    int64_t nacc = 0, nnear = 0;
     NceCtx cx; cx.rank = 0; cx.CL = 1; cx.lctl = &ctl;
     for (int64_t s = 0; s < jb.n_steps; ++s) {
-        nce_step<false>(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, ent_site, ent_pos, ent_sig, E, nacc, cx, m.tc ? &tcx : nullptr);
+        nce_step<false>(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, ent_site, ent_pos, ent_sig, E, nacc, nnear, cx, m.tc ? &tcx : nullptr);
         if (threadIdx.x == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
             jb.E_samples[((s + 1) / jb.sample_interval - 1) * jb.R + t] = E;
         __syncthreads();
     }
-    if (threadIdx.x == 0) { jb.E[r] = E; jb.n_acc[r] += nacc; }
+    if (threadIdx.x == 0) { jb.E[r] = E; jb.n_acc[r] += nacc; if (jb.n_near) jb.n_near[r] += nnear; }
     if (m.tc) tc_end(m.D, tcx);
 }
 
@@ -1119,13 +1121,13 @@ __global__ void __launch_bounds__(256, MINB) nce_chunk_cluster_kernel(const __gr
     cluster.sync();
     const int t = jb.slot_of_rep[r];
     double E = jb.E[r];
-    int64_t nacc = 0;
+    int64_t nacc = 0, nnear = 0;
     for (int64_t s = 0; s < jb.n_steps; ++s) {
-        nce_step<true>(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, ent_site, ent_pos, ent_sig, E, nacc, cx, m.tc ? &tcx : nullptr);
+        nce_step<true>(jb, r, t, s, ctl, dh, X, src, lw, lin, hw, ent_site, ent_pos, ent_sig, E, nacc, nnear, cx, m.tc ? &tcx : nullptr);
         if (rank == 0 && threadIdx.x == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
             jb.E_samples[((s + 1) / jb.sample_interval - 1) * jb.R + t] = E;
     }
-    if (rank == 0 && threadIdx.x == 0) { jb.E[r] = E; jb.n_acc[r] += nacc; }
+    if (rank == 0 && threadIdx.x == 0) { jb.E[r] = E; jb.n_acc[r] += nacc; if (jb.n_near) jb.n_near[r] += nnear; }
     cluster.sync();                                   // no CTA leaves while others may still read its shared memory
     if (m.tc) tc_end(m.D, tcx);
 }
@@ -1804,6 +1806,9 @@ int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_c
     jb.n_steps = ck->n_steps; jb.step0 = ck->step0; jb.prop_a = ck->prop_a; jb.prop_b = ck->prop_b; jb.prop_u = ck->prop_u;
     jb.seed = ck->seed; jb.sample_interval = ck->sample_interval > 0 ? ck->sample_interval : 1; jb.E_samples = ck->E_samples;
     jb.dE_out = ck->dE_out; jb.force = ck->force;
+    NCE_CHECK(ck->near_eV >= 0.0, "nce_nce_run_chunk: near_eV must be >= 0");
+    jb.n_near = st->n_near;
+    jb.near_eV = ck->near_eV > 0.0 ? ck->near_eV : ((h->dev.mma == 1 || h->dev.mma == 2) ? 1e-2 : 1e-4);
     if (ck->n_steps == 0) return NCE_OK;
     const int per_sm = ck->ctas_per_sm > 1 ? ck->ctas_per_sm : 1;
     NCE_CHECK(per_sm <= 2, "nce_nce_run_chunk: ctas_per_sm must be 1 or 2");

@@ -216,11 +216,12 @@ class NCEState:
         self.ladder_id = torch.as_tensor(np.zeros(R, np.int32) if ladder_id is None else np.asarray(ladder_id, np.int32)).to(device)
         self.n_acc = torch.zeros(R, dtype=torch.int64, device=device)
         self.n_ex = torch.zeros(1, dtype=torch.int64, device=device)
+        self.n_near = torch.zeros(R, dtype=torch.int64, device=device)   # near-threshold Metropolis steps
 
     def struct(self):
         s = _lib.NceNceState()
         s.R, s.N = self.R, self.N
-        for f in ("sigma", "h0", "e", "E", "beta_slot", "rep_of_slot", "slot_of_rep", "ladder_id", "n_acc", "n_ex"):
+        for f in ("sigma", "h0", "e", "E", "beta_slot", "rep_of_slot", "slot_of_rep", "ladder_id", "n_acc", "n_ex", "n_near"):
             setattr(s, f, getattr(self, f).data_ptr())
         s.hmid = self.hmid.data_ptr() if self.hmid is not None else None
         return s
@@ -231,14 +232,14 @@ class NCEState:
         return self
 
     def run_chunk(self, n_steps, step0, seed=0, proposals=None, sample_interval=1, E_samples=None, dE_out=None, force=0,
-                  exchange_rounds=0, ex_parity=0, ex_u=None, stream=None, cluster=1, ctas_per_sm=1):
+                  exchange_rounds=0, ex_parity=0, ex_u=None, stream=None, cluster=1, ctas_per_sm=1, near_eV=0.0):
         c = _lib.NceNceChunk()
         c.n_steps, c.step0, c.seed = int(n_steps), int(step0), int(seed) & 0xFFFFFFFFFFFFFFFF
         if proposals is not None:
             c.prop_a, c.prop_b, c.prop_u = (_lib.ptr(p) for p in proposals)
         c.sample_interval = int(sample_interval); c.E_samples = _lib.ptr(E_samples); c.dE_out = _lib.ptr(dE_out)
         c.force = int(force); c.exchange_rounds = int(exchange_rounds); c.ex_parity = int(ex_parity); c.ex_u = _lib.ptr(ex_u)
-        c.cluster = int(cluster); c.ctas_per_sm = int(ctas_per_sm)
+        c.cluster = int(cluster); c.ctas_per_sm = int(ctas_per_sm); c.near_eV = float(near_eV)
         st = self.struct()
         _lib.check(_lib.lib().nce_nce_run_chunk(self.model.handle, C.byref(st), C.byref(c), _lib.stream_ptr(stream)),
                    "nce_nce_run_chunk")

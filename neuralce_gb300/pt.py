@@ -104,6 +104,7 @@ class PTState:
         self.E_min_rep = t(Emr, torch.float64)
         self.n_acc = torch.zeros(R, dtype=torch.int64, device=device)
         self.n_ex = torch.zeros(1, dtype=torch.int64, device=device)
+        self.n_near = torch.zeros(R, dtype=torch.int64, device=device)   # near-threshold steps (stated dE bound)
         self._min = torch.zeros(1, dtype=torch.float64, device=device)
         self._arg = torch.zeros(1, dtype=torch.int32, device=device)
         self.cv = None
@@ -124,7 +125,7 @@ class PTState:
     def struct(self):
         s = _lib.NcePtState()
         s.R, s.N = self.R, self.N
-        for f in ("sigma", "E", "beta_slot", "rep_of_slot", "slot_of_rep", "ladder_id", "E_min_rep", "n_acc", "n_ex"):
+        for f in ("sigma", "E", "beta_slot", "rep_of_slot", "slot_of_rep", "ladder_id", "E_min_rep", "n_acc", "n_ex", "n_near"):
             setattr(s, f, getattr(self, f).data_ptr())
         s.cv = self.cv.data_ptr() if self.cv is not None else None
         return s
@@ -144,7 +145,7 @@ class PTState:
 
 
 def make_chunk(n_steps, step0, seed, precision=64, warps=0, proposals=None, sample_interval=1, E_samples=None,
-               do_exchange=False, ex_parity=0, ex_u=None, path=0, cluster=1):
+               do_exchange=False, ex_parity=0, ex_u=None, path=0, cluster=1, near_eV=0.0):
     c = _lib.NcePtChunk()
     c.n_steps, c.step0, c.seed = int(n_steps), int(step0), int(seed) & 0xFFFFFFFFFFFFFFFF
     if proposals is not None:
@@ -153,15 +154,17 @@ def make_chunk(n_steps, step0, seed, precision=64, warps=0, proposals=None, samp
     c.E_samples = _lib.ptr(E_samples)
     c.do_exchange = int(bool(do_exchange)); c.ex_parity = int(ex_parity); c.ex_u = _lib.ptr(ex_u)
     c.precision = int(precision); c.warps = int(warps); c.path = int(path); c.cluster = int(cluster)
+    c.near_eV = float(near_eV)
     return c
 
 
 def run_chunk(gce, st: PTState, n_steps, step0, seed, precision=64, warps=0, proposals=None, sample_interval=1,
-              E_samples=None, do_exchange=False, ex_parity=0, ex_u=None, stream=None, path=0, cluster=1):
+              E_samples=None, do_exchange=False, ex_parity=0, ex_u=None, stream=None, path=0, cluster=1, near_eV=0.0):
     """One chunk of the persistent kernel (+ chunk-end exchange) for one job.  path: 0 auto (sign parity when the
-    point functions are +-1), 1 general products, 2 sign parity."""
+    point functions are +-1), 1 general products, 2 sign parity.  ``st.n_near`` counts the steps whose Metropolis
+    margin |dE + ln(u) / beta| is below ``near_eV`` (0: the precision form's stated dE bound)."""
     ck = make_chunk(n_steps, step0, seed, precision, warps, proposals, sample_interval, E_samples, do_exchange,
-                    ex_parity, ex_u, path, cluster)
+                    ex_parity, ex_u, path, cluster, near_eV)
     s = st.struct()
     _lib.check(_lib.lib().nce_ce_run_chunk(gce.handle, C.byref(s), C.byref(ck), _lib.stream_ptr(stream)),
                "nce_ce_run_chunk")

@@ -235,3 +235,39 @@ def run_chain(orc, cache, sig, prop_i, prop_j, u, beta, scale_eV):
             sig[i], sig[j] = sig[j], sig[i]
             nacc += 1; dsum += dE
     return cache, sig, dsum, nacc, np.array(dEs), margin
+
+
+def trace_chain(orc, cache, sig, prop_i, prop_j, u, beta, scale_eV, dE_engine, near_eV):
+    """Step-by-step check of an engine's Metropolis chain of one replica against this oracle.
+
+    The engine reports its dE of every step (``dE_engine``, model units; 0 for same-species draws).  Its decision
+    at a step is the reference rule (``neuralce/nce/mcmc.py:178-179``) applied to its own dE.  At each step the
+    oracle evaluates the same swap with its float64 dE and decides by the same rule.  Where the two decisions
+    differ, the step must be near its threshold -- the oracle's margin |dE_eV + ln(u) / beta| below ``near_eV`` --
+    or it is reported as a mismatch; either way the oracle then follows the engine's decision, so that every later
+    step is still checked.  Returns a dict: sig and cache after the followed chain, per-step oracle dE, the steps
+    whose decisions differ (``excused`` near the threshold, ``mismatch`` elsewhere), the number of steps the
+    engine's dE puts near the threshold (``near_engine``: what the engine counts) and the accepted count."""
+    sig = np.asarray(sig, np.int64).copy()
+    out = dict(dE=[], excused=[], mismatch=[], near_engine=0, nacc=0)
+    for k, (i, j, uu) in enumerate(zip(prop_i, prop_j, u)):
+        i, j = int(i), int(j)
+        if sig[i] == sig[j]:
+            out["dE"].append(0.0); out["nacc"] += 1
+            continue
+        dE, patch = orc.local_delta(cache, sig, [(i, int(sig[j])), (j, int(sig[i]))])
+        out["dE"].append(dE)
+        de_o, de_e = dE * scale_eV, float(dE_engine[k]) * scale_eV
+        acc_o = de_o <= 0 or uu < np.exp(-beta * de_o)
+        acc_e = de_e <= 0 or uu < np.exp(-beta * de_e)
+        if beta > 0 and abs(de_e + np.log(uu) / beta) < near_eV:
+            out["near_engine"] += 1
+        if acc_o != acc_e:
+            near_o = beta > 0 and abs(de_o + np.log(uu) / beta) < near_eV
+            out["excused" if near_o else "mismatch"].append(k)
+        if acc_e:
+            cache = orc.commit(cache, patch, True)
+            sig[i], sig[j] = sig[j], sig[i]
+            out["nacc"] += 1
+    out["sig"], out["cache"], out["dE"] = sig, cache, np.array(out["dE"])
+    return out

@@ -1,9 +1,11 @@
 """GPU parity of the CE engine against the C oracle (float64), through the C-ABI.
 
 Tolerances: float64 kernel dE within 1e-10 eV of the oracle (only the summation order differs); float32
-kernel dE within 1e-6 eV (the stated CE bound).  Occupancy trajectories on a seeded stream are bit-exact;
-steps whose Metropolis margin |beta*dE + ln u| is below 1e-9 (fp64) / 1e-5 (fp32) would be allowed to differ
-and are counted -- none occur for these seeds.
+kernel dE within 1e-6 eV (the stated CE bound).  Occupancy trajectories on a seeded stream are bit-exact.  A step
+is near its threshold when its Metropolis margin |dE + ln(u) / beta| is below the precision form's stated dE bound
+(1e-9 eV at float64, 1e-6 eV at float32): only there could a decision differ from the oracle's.  The kernels
+count such steps (``n_near``) and the oracle counts them with the same definition; the trajectory tests require
+the counts to agree, and ``test_near_threshold_steps_are_counted`` plants steps on both sides of the band.
 """
 import ctypes as C
 
@@ -63,6 +65,7 @@ def _engine_state(sig_r, E, beta):
 
 
 def _compare(st, ref, E_tol):
+    assert np.array_equal(st.n_near.cpu().numpy(), ref["n_near"]), (st.n_near.cpu().numpy(), ref["n_near"])
     assert np.array_equal(st.sigma.cpu().numpy(), ref["sigma"])
     assert np.abs(st.E.cpu().numpy() - ref["E"]).max() < E_tol
     assert np.array_equal(st.n_acc.cpu().numpy(), ref["n_acc"])
@@ -72,9 +75,7 @@ def _compare(st, ref, E_tol):
 
 
 @pytest.mark.parametrize("precision,path,warps,cluster", [(64, 1, 8, 1), (32, 1, 8, 1), (64, 2, 8, 1), (32, 2, 4, 1),
-                                                          (64, 2, 1, 1), (64, 2, 8, 2), (32, 2, 4, 4), (64, 2, 16, 8),
-                                                          (64, 3, 8, 1), (32, 3, 4, 1), (64, 3, 1, 1), (64, 3, 16, 2),
-                                                          (32, 3, 8, 4)])
+                                                          (64, 2, 1, 1), (64, 2, 8, 2), (32, 2, 4, 4), (64, 2, 16, 8)])
 def test_trajectory_host_stream(cuda, precision, path, warps, cluster):
     """Seeded host proposal stream + exchange uniforms: bit-exact occupancy trajectory, energies, acceptance,
     slot permutation and slot-ordered samples vs the oracle (cluster > 1: each replica spread over that many
@@ -99,7 +100,8 @@ def test_trajectory_host_stream(cuda, precision, path, warps, cluster):
         run_chunk(gce, st, T, step, 0, precision, warps, dev, si, Es, True, par, torch.as_tensor(exu).cuda(), path=path,
                   cluster=cluster)
         Es_ref = np.zeros((T // si, R))
-        orc.run(ref, T, step, 0, (pa, pb, pu), si, Es_ref, True, par, exu, n_threads=4)
+        orc.run(ref, T, step, 0, (pa, pb, pu), si, Es_ref, True, par, exu, n_threads=4,
+                near_eV=1e-9 if precision == 64 else 1e-6)
         torch.cuda.synchronize()
         tol = 1e-9 if precision == 64 else 1e-4
         _compare(st, ref, tol)
@@ -108,7 +110,7 @@ def test_trajectory_host_stream(cuda, precision, path, warps, cluster):
     assert int(st.n_acc.sum()) > 0
 
 
-@pytest.mark.parametrize("path", [1, 2, 3])
+@pytest.mark.parametrize("path", [1, 2])
 def test_trajectory_philox_multichunk(cuda, path):
     """Device Philox stream, 3 chunks with exchanges: equals the oracle's Philox restatement."""
     torch = cuda
@@ -122,7 +124,7 @@ def test_trajectory_philox_multichunk(cuda, path):
         Es = torch.zeros((T // 100, R), dtype=torch.float64, device="cuda")
         Es_ref = np.zeros((T // 100, R))
         run_chunk(gce, st, T, c * T, 1234, 64, 4, None, 100, Es, True, path=path)
-        orc.run(ref, T, c * T, 1234, None, 100, Es_ref, True, n_threads=4)
+        orc.run(ref, T, c * T, 1234, None, 100, Es_ref, True, n_threads=4, near_eV=1e-9)
         torch.cuda.synchronize()
         _compare(st, ref, 1e-9)
         assert np.abs(Es.cpu().numpy() - Es_ref).max() < 1e-9
@@ -158,7 +160,7 @@ def test_batch_equals_alone(cuda):
         assert torch.equal(a.sigma, b.sigma) and torch.equal(a.E, b.E) and torch.equal(a.rep_of_slot, b.rep_of_slot)
 
 
-@pytest.mark.parametrize("cluster,path", [(2, 2), (4, 2), (8, 2), (16, 2), (2, 3), (4, 3)])
+@pytest.mark.parametrize("cluster,path", [(2, 2), (4, 2), (8, 2), (16, 2)])
 def test_cluster_equals_single_cta(cuda, cluster, path):
     """Philox stream with exchanges, 3 chunks: a replica spread over a thread-block cluster gives the same
     trajectory as one CTA, alone and in a batch of jobs."""
@@ -231,13 +233,11 @@ def test_sign_parity_small_cells(cuda, L):
     gce, orc, sig_r, beta = _setup(L, seed=9, R=R)
     E0 = np.array([orc.energy(x) for x in sig_r])
     a = _engine_state(sig_r, E0, beta); b = _engine_state(sig_r, E0, beta); ref = new_state(sig_r, E0, beta)
-    c = _engine_state(sig_r, E0, beta)
     run_chunk(gce, a, T, 0, 31, 64, 2, None, 1, None, True, path=1)
     run_chunk(gce, b, T, 0, 31, 64, 2, None, 1, None, True, path=2)
-    run_chunk(gce, c, T, 0, 31, 64, 2, None, 1, None, True, path=3)
-    orc.run(ref, T, 0, 31, None, 1, None, True)
+    orc.run(ref, T, 0, 31, None, 1, None, True, near_eV=1e-9)
     torch.cuda.synchronize()
-    _compare(a, ref, 1e-9); _compare(b, ref, 1e-9); _compare(c, ref, 1e-9)
+    _compare(a, ref, 1e-9); _compare(b, ref, 1e-9)
 
 
 def test_out_of_range_proposal_is_flagged(cuda):
@@ -267,7 +267,7 @@ def test_tracked_cluster_vector_sums(cuda):
     R, T = 8, 3000
     gce, orc, sig_r, beta = _setup(5, seed=13, R=R)
     E0 = np.array([orc.energy(x) for x in sig_r])
-    for precision, cluster, path in ((64, 1, 2), (32, 2, 2), (64, 1, 3), (32, 4, 3)):
+    for precision, cluster, path in ((64, 1, 2), (32, 2, 2), (64, 8, 2), (32, 4, 2)):
         st = _engine_state(sig_r, E0, beta).track_counts(gce)
         assert np.abs(gce.energy_from_counts(st.cv).cpu().numpy() - E0).max() < 1e-9
         for c in range(3):
@@ -350,3 +350,35 @@ def test_out_of_range_proposal_is_rejected_and_reported(cuda, path):
     torch.cuda.synchronize()
     gce.check_errors()
     assert torch.equal(a.sigma, b.sigma) and torch.equal(a.E, b.E)
+
+
+@pytest.mark.parametrize("precision,path", [(64, 1), (64, 2), (32, 1), (32, 2)])
+def test_near_threshold_steps_are_counted(cuda, precision, path):
+    """Steps planted at a known Metropolis margin (u chosen from the oracle's dE): a margin inside the stated band
+    (1e-9 eV at float64, 1e-6 eV at float32) is counted in n_near, one outside it is not; both are rejected, as the
+    oracle decides."""
+    torch = cuda
+    from neuralce_gb300.pt import run_chunk
+    gce, orc, sig_r, beta = _setup(8, seed=21, R=2)
+    rng = np.random.default_rng(4)
+    sig = sig_r[0]
+    while True:                                           # a swap that raises the energy by more than 0.01 eV
+        ia, ib = (int(x) for x in rng.integers(0, gce.n_atoms, 2))
+        if sig[ia] != sig[ib]:
+            de = orc.delta(sig, ia, ib, sig[ib], sig[ia])
+            if de > 0.01:
+                break
+    band = 1e-9 if precision == 64 else 1e-6
+    b = float(beta[0])
+    margins = [0.5 * band, 3.0 * band, 1e-3]                # near, not near, far
+    T = len(margins)
+    pa = np.zeros((T, 2), np.int32); pb = np.zeros((T, 2), np.int32); pu = np.ones((T, 2))
+    pa[:, 0], pb[:, 0] = ia, ib                              # replica 1 draws same-site moves (no-ops)
+    pu[:, 0] = [np.exp(-b * (de - x)) for x in margins]
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    st = _engine_state(sig_r, E0, beta)
+    run_chunk(gce, st, T, 0, 0, precision, 8, tuple(torch.as_tensor(x).cuda() for x in (pa, pb, pu)), path=path)
+    torch.cuda.synchronize()
+    assert st.n_near.cpu().tolist() == [1, 0]
+    assert st.n_acc.cpu().tolist() == [0, 0]
+    assert np.array_equal(st.sigma.cpu().numpy(), sig_r)

@@ -102,29 +102,74 @@ def test_local_chain_matches_oracle(cuda, nipt_model, which, cluster):
     assert int(st.n_acc[0].item()) == T
 
 
-@pytest.mark.parametrize("cluster", [1, 4])
-def test_metropolis_trajectory_matches_oracle(cuda, nipt_model, cluster):
-    """Seeded host stream, Metropolis at 600 K on 4 replicas: bit-exact occupancy vs the oracle."""
-    torch = cuda
+def _metropolis_vs_oracle(torch, m, orc, R, T, seed, cluster=1, temps=(500.0, 1400.0)):
+    """Seeded host stream, Metropolis on R replicas over a geometric ladder: every step checked against the oracle
+    (``trace_chain``): per-step dE within 1e-4 eV; decisions equal except at steps within the stated bound of
+    their threshold, which the kernel counts in n_near; final occupancies equal the followed chain bit for bit."""
     from neuralce_gb300.nce import NCEState
-    from oracle.nce_oracle import run_chain
-    mdl = nipt_model[0]
-    m, orc = _model_pkl(mdl, random_cell((4, 4, 4), 5))
-    R, T = 4, 30
-    beta = np.full(R, 1.0 / (8.617333e-5 * 600.0), np.float32)
-    rng = np.random.default_rng(11)
+    from oracle.nce_oracle import trace_chain
+    beta = (1.0 / (8.617333e-5 * np.geomspace(temps[0], temps[1], R))).astype(np.float32)
+    rng = np.random.default_rng(seed)
     sig = np.stack([m.sig0[rng.permutation(m.N)] for _ in range(R)]).astype(np.int8)
     pi = rng.integers(0, m.N, (T, R)).astype(np.int32); pj = rng.integers(0, m.N, (T, R)).astype(np.int32)
     pu = 1.0 - rng.random((T, R))
     st = NCEState(m, sig, beta).full_cache()
-    st.run_chunk(T, 0, proposals=tuple(torch.as_tensor(x).cuda() for x in (pi, pj, pu)), cluster=cluster)
+    dE = torch.zeros((T, R), dtype=torch.float64, device="cuda")
+    st.run_chunk(T, 0, proposals=tuple(torch.as_tensor(x).cuda() for x in (pi, pj, pu)), dE_out=dE, cluster=cluster)
     torch.cuda.synchronize()
+    m.check_errors()
+    near_eV = 1e-2 if m.mma in (1, 2) else 1e-4
+    dEg = dE.cpu().numpy()
+    counted, excused = 0, 0
     for r in range(R):
         cache = orc.full_cache(sig[r].astype(np.int64))
-        _, s_ref, _, nacc, _, margin = run_chain(orc, cache, sig[r], pi[:, r], pj[:, r], pu[:, r], float(beta[r]), m.scale_eV)
-        if margin > 1e-4:
-            assert np.array_equal(st.sigma[r].cpu().numpy(), s_ref.astype(np.int8))
-            assert int(st.n_acc[r].item()) == nacc
+        tr = trace_chain(orc, cache, sig[r], pi[:, r], pj[:, r], pu[:, r], float(beta[r]), m.scale_eV, dEg[:, r], near_eV)
+        assert not tr["mismatch"], f"replica {r}: decisions differ away from the threshold at steps {tr['mismatch']}"
+        assert np.abs((dEg[:, r] - tr["dE"]) * m.scale_eV).max() < (1e-2 if m.mma in (1, 2) else 1e-4)
+        assert np.array_equal(st.sigma[r].cpu().numpy(), tr["sig"].astype(np.int8))
+        assert int(st.n_acc[r].item()) == tr["nacc"]
+        assert int(st.n_near[r].item()) == tr["near_engine"]
+        counted += tr["near_engine"]; excused += len(tr["excused"])
+    print(f"{R} x {T} steps: {counted} near-threshold steps counted, {excused} decisions excused")
+    return counted
+
+
+@pytest.mark.parametrize("which,cluster", [("pkl", 1), ("pkl", 4), ("bench", 1), ("bench", 2)])
+def test_metropolis_trajectory_matches_oracle(cuda, nipt_model, which, cluster):
+    """Metropolis chains of 4 replicas, 40 steps each, checked step by step against the oracle."""
+    if which == "pkl":
+        m, orc = _model_pkl(nipt_model[0], random_cell((4, 4, 4), 5))
+    else:
+        m, orc = _model_bench(3, 5)
+    _metropolis_vs_oracle(cuda, m, orc, 4, 40, 11, cluster)
+
+
+def test_near_threshold_steps_are_counted(cuda, nipt_model):
+    """A step planted near its threshold (u chosen from the oracle's dE so that the margin is 5e-5 eV, inside the
+    1e-4 eV bound and beyond the float32 engine's dE error) is counted in n_near; a step 1e-2 eV away is not."""
+    torch = cuda
+    from neuralce_gb300.nce import NCEState
+    m, orc = _model_pkl(nipt_model[0], random_cell((4, 4, 4), 8))
+    beta = np.array([1.0 / (8.617333e-5 * 800.0)], np.float32)
+    sig = m.sig0.astype(np.int64)
+    cache = orc.full_cache(sig)
+    rng = np.random.default_rng(2)
+    found = []
+    while len(found) < 2:                                 # two swaps with dE_eV > 0.05 eV (u < 1 at the threshold)
+        i, j = (int(x) for x in rng.integers(0, m.N, 2))
+        if sig[i] == sig[j]:
+            continue
+        dE, _ = orc.local_delta(cache, sig, [(i, int(sig[j])), (j, int(sig[i]))])
+        if dE * m.scale_eV > 0.05:
+            found.append((i, j, dE * m.scale_eV))
+    # step 0: margin +5e-5 eV (rejected, near); step 1: the same swap (state unchanged), margin +1e-2 eV (not near)
+    (i, j, de), b = found[0], float(beta[0])
+    u0 = np.exp(-b * (de - 5e-5)); u1 = np.exp(-b * (de - 1e-2))
+    pi = np.array([[i], [i]], np.int32); pj = np.array([[j], [j]], np.int32); pu = np.array([[u0], [u1]])
+    st = NCEState(m, sig[None].astype(np.int8), beta).full_cache()
+    st.run_chunk(2, 0, proposals=tuple(torch.as_tensor(x).cuda() for x in (pi, pj, pu)))
+    torch.cuda.synchronize()
+    assert int(st.n_near[0].item()) == 1 and int(st.n_acc[0].item()) == 0
 
 
 @pytest.mark.parametrize("cluster,per_sm,shipped", [(4, 1, False), (1, 2, False), (4, 2, False), (8, 2, False),
