@@ -196,6 +196,11 @@ int nce_ce_errors(nce_ce_handle h, int32_t *flags);
  *   nce_nce_run_chunk   scan(step): propose, local_delta, accept, commit    neuralce/nce/mcmc.py:130-199,
  *                                                                            neuralce/nce/local_update_implicit.py:117-194
  *                       + neighbour exchange rounds at the chunk end         neuralce/nce/mcmc.py:370-384
+ *   nce_nce_local_delta setup()['local_delta'](cache, sig, flips)            neuralce/nce/mc_model.py:221-226,
+ *                                                                            neuralce/nce/local_update_implicit.py:117-183
+ *   nce_nce_commit      setup()['commit'](cache, patch, accept)             neuralce/nce/local_update_implicit.py:185-194
+ *   nce_nce_accept      the driver's Metropolis rule on dE (mean over an     neuralce/nce/mcmc.py:167-185,
+ *                       ensemble of models, seed_idx < 0)                    neuralce/nce/mc_model.py:181-188
  */
 typedef struct {
     int32_t nB, J, mo, P, W, depth, C0, D, maxM, maxP, wL;
@@ -276,6 +281,24 @@ int nce_nce_destroy(nce_nce_handle h);
 int nce_nce_full_cache(nce_nce_handle h, const nce_nce_state *st, void *stream);
 int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_chunk *ck, void *stream);
 int nce_nce_errors(nce_nce_handle h, int32_t *flags);
+
+/* The reference's local_delta / commit pair on device data, one swap per replica.  nce_nce_local_delta evaluates,
+ * for every replica r, the swap of sites prop_a[r] and prop_b[r] (device int32, indexed by replica) on the state's
+ * caches without changing them: dE_out[r] (device float64, model units as in nce_nce_chunk.dE_out; 0 for two sites of
+ * one species, NaN for a site outside the cell).  The evaluated rows are kept in the model's step scratch.
+ * nce_nce_commit then applies the kept swap of every replica with accept[r] != 0 (device int32): caches, occupancy,
+ * E += dE, n_acc += 1 (two sites of one species: only n_acc).  Each kept swap is consumed by the next commit; any
+ * other call that runs steps on the same model handle (a chunk, another local_delta) replaces it. */
+int nce_nce_local_delta(nce_nce_handle h, const nce_nce_state *st, const int32_t *prop_a, const int32_t *prop_b, double *dE_out,
+                        void *stream);
+int nce_nce_commit(nce_nce_handle h, const nce_nce_state *st, const int32_t *accept, void *stream);
+
+/* Metropolis decisions from dE of n_models models (device float64 (n_models, R), model units, indexed by replica):
+ * accept[r] = mean dE_eV <= 0 or u[r] < exp(-beta dE_eV), dE_eV = mean over models of dE * scale_eV, beta of the
+ * replica's slot (beta_slot[slot_of_rep[r]]).  n_models > 1 is the reference's ensemble energy (mean over trained
+ * seeds).  A NaN dE (a refused proposal) is rejected.  u (device, (R)) in (0, 1]; accept (device int32, (R)). */
+int nce_nce_accept(const double *dE, int32_t n_models, int32_t R, double scale_eV, const float *beta_slot,
+                   const int32_t *slot_of_rep, const double *u, int32_t *accept, void *stream);
 
 /* Tensor-core tile GEMM of the NeuralCE layers (tcgen05, tensor-memory accumulator), exposed for testing:
  * C[M x N] = A[M x K] B[K x N], float32 row-major device arrays, operands rounded to bf16 (split != 0: bf16 hi/lo

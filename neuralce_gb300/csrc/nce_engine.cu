@@ -71,7 +71,17 @@ struct NceDev {
     // tcgen05 layer contractions (mma 2: bf16, mma 4: split bf16): per layer the weights as the B operand in bf16
     // core-matrix layout ([D][Kp], Kp = Kin rounded up to 16; hi, then lo when split)
     int32_t tc, tc_split; const uint8_t *Wt[kMaxLayers];
+    int32_t tc_ks;                            // K columns the A tile holds (a layer with more is issued in K slices)
     const float *zrow;                        // kZeroRow zeros: the row a masked shell partner reads
+};
+
+// A swap evaluated and kept for a later commit (nce_nce_local_delta / nce_nce_commit): the new rows stay in the
+// model's step scratch (site list, new rows, new site energies) until the next call on the handle.
+struct NcePending {
+    int64_t si, sj;
+    double dE;
+    int32_t ssi, ssj, same, valid;
+    int32_t nl[kMaxLayers + 1];
 };
 
 struct NceJob {
@@ -87,6 +97,8 @@ struct NceJob {
     int64_t sample_interval; double *E_samples; double *dE_out; int32_t force;   // force: 0 Metropolis, 1 accept, -1 reject
     int32_t *err;
     int64_t *n_near; double near_eV;          // near-threshold step counts (or null) and their band in eV
+    NcePending *pend;                         // (R) force = -2: the evaluated swap of each replica, kept for a commit
+    int32_t rep_index;                        // proposals and dE_out indexed by replica instead of temperature slot
 };
 
 __device__ __forceinline__ int32_t wadd(int32_t k, int32_t u, int32_t d) { int32_t q = k + u; return q >= d ? q - d : q; }
@@ -215,9 +227,14 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
     float *tinv = reinterpret_cast<float *>(tsite + TM);     // 1 / |first-shell partners| of each
     int4 *tk = reinterpret_cast<int4 *>(tinv + TM);          // (basis, k0, k1, k2) of each
     int32_t *tslot = reinterpret_cast<int32_t *>(tk + TM);   // slot-map value of each (-1: not in the field)
-    // tcgen05 path: the tile is the bf16 A operand [128][Kp] (hi, then lo when split) in core-matrix layout
+    // tcgen05 path: the tile is the bf16 A operand [128][KS] (hi, then lo when split) in core-matrix layout, one K
+    // slice [klo, klo + KS) of the layer's Kp input columns at a time (KS = Kp unless the whole A operand does not
+    // fit shared memory: the split form at width 128 takes its self channels, then its shell means); every slice's
+    // MMAs accumulate into the same tensor-memory tile
     const int Kp = kpad16(Kin);
-    uint8_t *A0 = reinterpret_cast<uint8_t *>(X), *A1 = A0 + (size_t)128 * Kp * 2;
+    const int KS = (tc && Kp > m.tc_ks) ? m.tc_ks : Kp, nks = Kp / KS;
+    int klo = 0, khi = Kp;                                   // the slice being gathered (all of K off the tcgen05 path)
+    uint8_t *A0 = reinterpret_cast<uint8_t *>(X), *A1 = A0 + (size_t)128 * KS * 2;
     if (tc) {
         // this layer's B operand into shared memory (read by the tensor cores after the first tile barrier)
         const size_t n16 = (size_t)Kp * D * 2 * (m.tc_split ? 2 : 1) / 16;
@@ -228,7 +245,8 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
     }
     auto xput = [&](int ms, int k, float v) {
         if (tc) {
-            const uint32_t off = umma::core_off(ms, k, Kp);
+            if (k < klo || k >= khi) return;
+            const uint32_t off = umma::core_off(ms, k - klo, KS);
             const __nv_bfloat16 h = __float2bfloat16_rn(v);
             *reinterpret_cast<__nv_bfloat16 *>(A0 + off) = h;
             if (m.tc_split) *reinterpret_cast<__nv_bfloat16 *>(A1 + off) = __float2bfloat16_rn(v - __bfloat162float(h));
@@ -239,7 +257,8 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
     // channels k, k + 1 (k even): one 4-byte bf16 pair on the tcgen05 path
     auto xput2 = [&](int ms, int k, float v0, float v1) {
         if (tc) {
-            const uint32_t off = umma::core_off(ms, k, Kp);
+            if (k < klo || k >= khi) return;                 // slices start on multiples of 16: a pair never straddles
+            const uint32_t off = umma::core_off(ms, k - klo, KS);
             const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
             *reinterpret_cast<__nv_bfloat162 *>(A0 + off) = h;
             if (m.tc_split) {
@@ -298,6 +317,8 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
             }
         }
         __syncthreads();
+        for (int ks = 0; ks < nks; ++ks) {
+        klo = ks * KS; khi = tc ? klo + KS : Kp;
         // 2) X = [h | masked shell means] of the tile's sites: lanes over channels (coalesced rows); masked
         //    partners read the zero row, so every sum runs over all W slots in order
         const float *zr = m.zrow;
@@ -333,15 +354,18 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
             }
         } else if (P == 1 && W <= 12 && Cin <= 128) {
             // one shell, up to 128 channels: one site per warp, four channels per lane, all 13 rows' loads in flight
+            // (a K slice that holds only the self channels, or only the shell means, loads only those rows)
             const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+            const bool need_self = klo < Cin, need_shell = khi > Cin;
             for (int mm = warp; mm < tm; mm += nwarp) {
                 const float *const *sr = srcp + mm * PW;
                 float v[4][13];
 #pragma unroll
                 for (int u = 0; u < 13; ++u) {
-                    const float *rr = u <= W ? sr[u] : zr;
+                    const bool want = u == 0 ? need_self : (need_shell && u <= W);
+                    const float *rr = want ? sr[u] : zr;
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) v[j][u] = lane + 32 * j < Cin ? rr[lane + 32 * j] : 0.f;
+                    for (int j = 0; j < 4; ++j) v[j][u] = (want && lane + 32 * j < Cin) ? rr[lane + 32 * j] : 0.f;
                 }
                 const float inv = tinv[mm];
 #pragma unroll
@@ -351,7 +375,8 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                     float a = 0.f;
 #pragma unroll
                     for (int u = 1; u < 13; ++u) a += v[j][u];
-                    xput(mm, c, v[j][0]); xput(mm, Cin + c, a * inv);
+                    if (need_self) xput(mm, c, v[j][0]);
+                    if (need_shell) xput(mm, Cin + c, a * inv);
                 }
             }
         } else if (Cin <= 32 && W <= 32) {
@@ -423,19 +448,28 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
         }
         if (tc) {
             // zero K padding of the tile's rows (rows past tm only feed outputs that are dropped)
-            const int kz = Kp - Kin;
-            for (int idx = tid; idx < tm * kz; idx += nt) xput(idx / kz, Kin + idx % kz, 0.f);
+            const int kz0 = max(Kin, klo), kz = khi - kz0;
+            for (int idx = tid; kz > 0 && idx < tm * kz; idx += nt) xput(idx / kz, kz0 + idx % kz, 0.f);
             umma::fence_async_smem();
         }
         __syncthreads();
         if (tc) {
-            // 3'') tcgen05: one thread issues the tile's MMAs into tensor memory; every warp then reads its lane
-            // quarter (rows 32 (warp % 4) ..) and half of the columns, adds the bias, activates and stages the rows
-            // in Y (over the A operand) for the sink's CUDA-core mapping
-            if (tid == 0) umma::issue_tile(tc->tmem, A0, A1, tc->W, tc->W + (size_t)Kp * D * 2, D, Kp, m.tc_split ? 3 : 1, tc->mbar);
+            // 3'') tcgen05: one thread issues the slice's MMAs into tensor memory (the B operand's K-steps of this
+            // slice, accumulating onto the previous slices); every thread waits for their completion before the
+            // next slice overwrites the A tile
+            if (tid == 0) {
+                const size_t bo = (size_t)klo * 16;             // K-step klo / 16 of the B tile (256 bytes per step)
+                umma::issue_tile_k(tc->tmem, A0, A1, (uint32_t)KS * 16u, tc->W + bo, tc->W + (size_t)Kp * D * 2 + bo,
+                                   (uint32_t)Kp * 16u, D, KS / 16, m.tc_split ? 3 : 1, ks > 0, tc->mbar);
+            }
             if (!umma::mbar_wait(tc->mbar, tc->phase) && (tid & 31) == 0) atomicOr(jb.err, 32);
             tc->phase ^= 1u;
             umma::fence_after();
+        }
+        }   // K slices
+        if (tc) {
+            // every warp reads its lane quarter (rows 32 (warp % 4) ..) and half of the columns of the accumulator,
+            // adds the bias, activates and stages the rows in Y (over the A operand) for the sink's CUDA-core mapping
             const int warp = tid >> 5, q = warp & 3, hh = warp >> 2;
             const int cw = D / 2 >= 16 ? D / 2 : 16;
             const int YS = D + 4;
@@ -650,10 +684,14 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
     float *nb = jb.newbuf + (size_t)r * jb.scratch_stride;
     float *en = jb.e_new + (size_t)r * m.nmax;
     const int L = m.depth;
+    const int q_ix = jb.rep_index ? r : t;            // column of the host proposal stream and of dE_out
     if (leader) {
     if (tid == 0) {
         int64_t i, j; double u;
-        if (jb.prop_a) { i = jb.prop_a[s_idx * jb.R + t]; j = jb.prop_b[s_idx * jb.R + t]; u = jb.prop_u[s_idx * jb.R + t]; }
+        if (jb.prop_a) {
+            i = jb.prop_a[s_idx * jb.R + q_ix]; j = jb.prop_b[s_idx * jb.R + q_ix];
+            u = jb.prop_u ? jb.prop_u[s_idx * jb.R + q_ix] : 1.0;
+        }
         else {
             const uint32_t k0 = (uint32_t)jb.seed, k1 = (uint32_t)(jb.seed >> 32);
             const int64_t g = jb.step0 + s_idx;
@@ -724,7 +762,16 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         __syncthreads();
     }
     if (ctl.same || ctl.err) {
-        if (leader && tid == 0 && ctl.same) { ++nacc; if (jb.dE_out) jb.dE_out[s_idx * jb.R + t] = 0.0; }
+        if (leader && tid == 0 && ctl.same) {
+            if (jb.force != -2) ++nacc;               // an accepted no-op (kept for a commit when force = -2)
+            if (jb.dE_out) jb.dE_out[s_idx * jb.R + q_ix] = 0.0;
+        }
+        if (leader && tid == 0 && jb.force == -2) {
+            NcePending &pd = jb.pend[r];
+            pd.si = ctl.si; pd.sj = ctl.sj; pd.dE = 0.0; pd.ssi = ctl.ssi; pd.ssj = ctl.ssj;
+            pd.same = ctl.same; pd.valid = ctl.err ? 0 : 1;
+            if (ctl.err && jb.dE_out) jb.dE_out[s_idx * jb.R + q_ix] = __longlong_as_double(0x7ff8000000000000ll);
+        }
         if (ctl.err) for (int p = tid + rank * nt; p < min(ctl.nl[L], m.nmax); p += nt * CL) slot[list[p]] = -1;
         csync<CLUSTER>();
         return;
@@ -958,7 +1005,12 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
         else a = (dEeV <= 0.0) || (ctl.u < exp(-beta * dEeV));
         if (jb.force == 0 && beta > 0.0 && fabs(dEeV + log(ctl.u) / beta) < jb.near_eV) ++nnear;
         ctl.acc = a;
-        if (jb.dE_out) jb.dE_out[s_idx * jb.R + t] = dE;
+        if (jb.dE_out) jb.dE_out[s_idx * jb.R + q_ix] = dE;
+        if (jb.force == -2) {                          // keep the evaluated swap for nce_nce_commit
+            NcePending &pd = jb.pend[r];
+            pd.si = ctl.si; pd.sj = ctl.sj; pd.dE = dE; pd.ssi = ctl.ssi; pd.ssj = ctl.ssj; pd.same = 0; pd.valid = 1;
+            for (int l = 0; l <= L; ++l) pd.nl[l] = ctl.nl[l];
+        }
         if (a) { sig[ctl.si] = (int8_t)ctl.ssj; sig[ctl.sj] = (int8_t)ctl.ssi; E += dE; ++nacc; }
     }
     csync<CLUSTER>();
@@ -1028,9 +1080,11 @@ __host__ __device__ inline size_t weight_floats(int depth, int P, int C0, int D,
     return o;
 }
 
-// shared-memory plan of the step kernel (byte offsets, 16-byte aligned): dh | X tile | partner codes | tcgen05 B
-// operand | ball-0 entries | weights.  with_dh = false: the tile part alone (full-cache kernel).  On the tcgen05
-// path the X tile holds the bf16 A operand(s) [128][Kp] or the float32 output rows [128][D + 4], whichever is larger.
+// shared-memory plan of the step kernel (byte offsets, 16-byte aligned): X tile | partner codes | tcgen05 B operand,
+// sharing its bytes with dh | ball-0 entries | weights.  dh (the layer-0 change) lives only between the receptive
+// field's build and the first layer, and the B operand is copied in at the start of each layer, so the two share one
+// region.  with_dh = false: the tile part alone (full-cache kernel).  On the tcgen05 path the X tile holds the bf16
+// A operand(s) [128][tc_ks] or the float32 output rows [128][D + 4], whichever is larger.
 struct SmemPlan {
     size_t dh, X, src, wt, ent, w, dh_bytes, tile_end, total_w;
     __host__ __device__ static SmemPlan make(const NceDev &m, bool with_dh = true) {
@@ -1039,17 +1093,19 @@ struct SmemPlan {
         SmemPlan p;
         const int TM = tile_tm(m.D, m.tc, m.mma), Kmax = tile_kin(m.P, m.C0, m.D);
         // layer-0 change per (site, channel): int32 counts for +-1 point functions, int64 fixed point otherwise
-        p.dh = 0; p.dh_bytes = with_dh ? al((m.l0bin ? sizeof(int32_t) : sizeof(unsigned long long)) * (size_t)m.n0max * m.C0) : 0;
-        p.X = al128(p.dh_bytes);
+        p.dh_bytes = with_dh ? al((m.l0bin ? sizeof(int32_t) : sizeof(unsigned long long)) * (size_t)m.n0max * m.C0) : 0;
+        p.X = 0;
         size_t xb = sizeof(float) * (size_t)TM * x_stride(Kmax);
         if (m.tc) {
-            const size_t ab = (size_t)128 * kpad16(Kmax) * 2 * (m.tc_split ? 2 : 1), yb = sizeof(float) * 128 * (size_t)(m.D + 4);
+            const size_t ab = (size_t)128 * m.tc_ks * 2 * (m.tc_split ? 2 : 1), yb = sizeof(float) * 128 * (size_t)(m.D + 4);
             xb = ab > yb ? ab : yb;
         }
         p.src = al(p.X + xb);
         p.wt = al128(p.src + sizeof(const float *) * (size_t)TM * (1 + m.P * m.W) + sizeof(int32_t) * (size_t)TM * 7);
-        p.tile_end = p.wt + (m.tc ? (size_t)kpad16(Kmax) * m.D * 2 * (m.tc_split ? 2 : 1) : 0);
-        p.ent = p.tile_end;
+        const size_t wtb = m.tc ? (size_t)kpad16(Kmax) * m.D * 2 * (m.tc_split ? 2 : 1) : 0;
+        p.dh = p.wt;
+        p.tile_end = p.wt + (with_dh ? (wtb > p.dh_bytes ? wtb : p.dh_bytes) : wtb);
+        p.ent = al(p.tile_end);
         p.w = al(p.ent + (sizeof(int32_t) * 2 + 1) * 2 * (size_t)m.w0max);
         p.total_w = al(p.w + sizeof(float) * weight_floats(m.depth, m.P, m.C0, m.D, m.gate));
         return p;
@@ -1130,6 +1186,54 @@ __global__ void __launch_bounds__(256, MINB) nce_chunk_cluster_kernel(const __gr
     if (rank == 0 && threadIdx.x == 0) { jb.E[r] = E; jb.n_acc[r] += nacc; if (jb.n_near) jb.n_near[r] += nnear; }
     cluster.sync();                                   // no CTA leaves while others may still read its shared memory
     if (m.tc) tc_end(m.D, tcx);
+}
+
+// Commit of the swaps kept by a force = -2 chunk (nce_nce_local_delta): one CTA per replica writes the new layer-0,
+// hidden and site-energy rows from the step scratch into the caches, swaps the two sites and adds dE to the carried
+// energy, where accept[r] != 0 (the reference's commit, neuralce/nce/local_update_implicit.py:185-194, plus the
+// driver's occupancy and energy update, neuralce/nce/mcmc.py:180-185).  Every kept swap is consumed.
+__global__ void __launch_bounds__(256) nce_commit_kernel(const __grid_constant__ NceJob jb, const int32_t *__restrict__ accept) {
+    const int r = blockIdx.x;
+    if (r >= jb.R) return;
+    const NceDev &m = jb.m;
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    const NcePending pd = jb.pend[r];
+    __syncthreads();                                   // every thread has read the record before it is consumed
+    if (tid == 0) jb.pend[r].valid = 0;
+    if (!pd.valid || !accept[r]) return;
+    if (tid == 0) jb.n_acc[r] += 1;
+    if (pd.same) return;                               // same species: an accepted no-op
+    const int64_t N = m.N;
+    int8_t *sig = jb.sigma + (int64_t)r * N;
+    float *h0 = jb.h0 + (size_t)r * N * m.C0;
+    float *e = jb.e + (size_t)r * N;
+    const int32_t *list = jb.list + (size_t)r * m.nmax;
+    float *nb = jb.newbuf + (size_t)r * jb.scratch_stride;
+    const float *en = jb.e_new + (size_t)r * m.nmax;
+    if (tid == 0) { sig[pd.si] = (int8_t)pd.ssj; sig[pd.sj] = (int8_t)pd.ssi; jb.E[r] += pd.dE; }
+    const float *nb0 = level_buf(jb, nb, 0);
+    for (int p = warp; p < pd.nl[0]; p += nw)
+        for (int c = lane; c < m.C0; c += 32) h0[(size_t)list[p] * m.C0 + c] = nb0[(size_t)p * m.C0 + c];
+    for (int lvl = 1; lvl < m.depth; ++lvl) {
+        float *hm = jb.hmid + ((size_t)(lvl - 1) * jb.R + r) * N * m.D;
+        const float *src = level_buf(jb, nb, lvl);
+        for (int p = warp; p < pd.nl[lvl]; p += nw)
+            for (int c = lane; c < m.D; c += 32) hm[(size_t)list[p] * m.D + c] = src[(size_t)p * m.D + c];
+    }
+    for (int p = tid; p < pd.nl[m.depth]; p += nt) e[list[p]] = en[p];
+}
+
+// Metropolis decisions of R replicas from the dE of n_models models (mean over the models: the reference's ensemble)
+__global__ void nce_accept_kernel(const double *__restrict__ dE, int32_t n_models, int32_t R, double scale_eV,
+                                  const float *__restrict__ beta_slot, const int32_t *__restrict__ slot_of_rep,
+                                  const double *__restrict__ u, int32_t *__restrict__ accept) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    double s = 0.0;
+    for (int k = 0; k < n_models; ++k) s += dE[(size_t)k * R + r];
+    const double dEeV = s / n_models * scale_eV;
+    const double beta = (double)beta_slot[slot_of_rep[r]];
+    accept[r] = (dEeV == dEeV) && ((dEeV <= 0.0) || (u[r] < exp(-beta * dEeV)));
 }
 
 // ── full cache ─────────────────────────────────────────────────────────────────────────────────────
@@ -1345,6 +1449,7 @@ struct nce_nce_model {
     int32_t *err = nullptr;
     // scratch for R replicas
     int32_t *slot = nullptr, *list = nullptr; float *newbuf = nullptr, *e_new = nullptr; int64_t stride = 0; int32_t R_alloc = 0;
+    nce::NcePending *pend = nullptr;            // (R_alloc) swaps kept by nce_nce_local_delta
 };
 
 
@@ -1378,7 +1483,8 @@ static size_t step_smem(const NceDev &m, bool w_smem) {
 
 static int ensure_scratch(nce_nce_model *h, int32_t R) {
     if (h->R_alloc >= R) return NCE_OK;
-    for (void *p : {(void *)h->slot, (void *)h->list, (void *)h->newbuf, (void *)h->e_new}) if (p) cudaFree(p);
+    for (void *p : {(void *)h->slot, (void *)h->list, (void *)h->newbuf, (void *)h->e_new, (void *)h->pend}) if (p) cudaFree(p);
+    h->slot = h->list = nullptr; h->newbuf = h->e_new = nullptr; h->pend = nullptr; h->R_alloc = 0;
     const NceDev &m = h->dev;
     h->stride = (int64_t)l0_floats(m) + (int64_t)std::max(0, m.depth - 1) * m.nmax * m.D;
     NCE_CUDA(cudaMalloc((void **)&h->slot, sizeof(int32_t) * (size_t)R * m.N));
@@ -1386,7 +1492,41 @@ static int ensure_scratch(nce_nce_model *h, int32_t R) {
     NCE_CUDA(cudaMalloc((void **)&h->list, sizeof(int32_t) * (size_t)R * m.nmax));
     NCE_CUDA(cudaMalloc((void **)&h->newbuf, sizeof(float) * (size_t)R * std::max<int64_t>(h->stride, 1)));
     NCE_CUDA(cudaMalloc((void **)&h->e_new, sizeof(float) * (size_t)R * m.nmax));
+    NCE_CUDA(cudaMalloc((void **)&h->pend, sizeof(NcePending) * (size_t)R));
+    NCE_CUDA(cudaMemset(h->pend, 0, sizeof(NcePending) * (size_t)R));
     h->R_alloc = R;
+    return NCE_OK;
+}
+
+static NceJob make_nce_job(nce_nce_model *h, const nce_nce_state *st);
+
+// the step kernels of one chunk: one CTA per replica, or a thread-block cluster of CL CTAs per replica
+static int launch_steps(nce_nce_model *h, const NceJob &jb, int cluster, int ctas_per_sm, cudaStream_t stream) {
+    const int per_sm = ctas_per_sm > 1 ? ctas_per_sm : 1;
+    NCE_CHECK(per_sm <= 2, "nce_nce_run_chunk: ctas_per_sm must be 1 or 2");
+    const size_t lim = per_sm == 2 ? kStepSmemMax2 : kStepSmemMax;
+    const bool w_smem = step_smem(h->dev, true) <= lim;
+    const size_t sm = step_smem(h->dev, w_smem);
+    NCE_CHECK(sm <= lim, "nce_nce_run_chunk: %zu bytes of shared memory per CTA do not fit %d CTAs per SM", sm, per_sm);
+    const int CL = cluster > 1 ? cluster : 1;
+    NCE_CHECK(CL == 1 || CL == 2 || CL == 4 || CL == 8, "nce_nce_run_chunk: cluster must be 1, 2, 4 or 8");
+    if (CL == 1 || h->dev.depth == 0) {
+        auto kern = per_sm == 2 ? nce_chunk_kernel<2> : nce_chunk_kernel<1>;
+        NCE_CUDA(::nce::raise_smem_limit((const void *)kern, sm));
+        kern<<<jb.R, 256, sm, stream>>>(jb, w_smem ? 1 : 0);
+    } else {
+        auto kern = per_sm == 2 ? nce_chunk_cluster_kernel<2> : nce_chunk_cluster_kernel<1>;
+        NCE_CUDA(::nce::raise_smem_limit((const void *)kern, sm));
+        cudaLaunchConfig_t cfg; std::memset(&cfg, 0, sizeof(cfg));
+        cfg.gridDim = dim3((unsigned)(jb.R * CL)); cfg.blockDim = dim3(256); cfg.dynamicSmemBytes = sm;
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)CL; attr[0].val.clusterDim.y = 1; attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr; cfg.numAttrs = 1;
+        NCE_CUDA(cudaLaunchKernelEx(&cfg, kern, jb, (int32_t)(w_smem ? 1 : 0)));
+    }
+    NCE_CUDA(cudaGetLastError());
     return NCE_OK;
 }
 
@@ -1395,7 +1535,7 @@ static NceJob make_nce_job(nce_nce_model *h, const nce_nce_state *st) {
     j.m = h->dev;
     j.sigma = st->sigma; j.h0 = st->h0; j.hmid = st->hmid; j.e = st->e; j.E = st->E; j.beta_slot = st->beta_slot;
     j.slot_of_rep = st->slot_of_rep; j.n_acc = st->n_acc; j.R = st->R;
-    j.slot = h->slot; j.list = h->list; j.newbuf = h->newbuf; j.e_new = h->e_new; j.scratch_stride = h->stride;
+    j.slot = h->slot; j.list = h->list; j.newbuf = h->newbuf; j.e_new = h->e_new; j.scratch_stride = h->stride; j.pend = h->pend;
     j.err = h->err; j.sample_interval = 1;
     return j;
 }
@@ -1559,6 +1699,7 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
     m.mma = d->mma;
     m.tc = (d->mma == 2 || d->mma == 4) && d->depth > 0 ? 1 : 0;
     m.tc_split = d->mma == 4 ? 1 : 0;
+    m.tc_ks = kpad16(tile_kin(d->P, d->C0, d->D));     // the whole K extent of the widest layer in one A tile
     m.head_b = (float)d->head_b;
     m.n0max = 2 * n0max; m.nmax = 2 * nLmax; m.w0max = n0max;
     NCE_CHECK(d->Rv_loc, "nce_nce_create: Rv_loc required");
@@ -1716,6 +1857,17 @@ int nce_nce_create(const nce_nce_desc *d, nce_nce_handle *out) {
         if (e == cudaSuccess) e = cudaMemset(h->err, 0, sizeof(int32_t));
         if (e != cudaSuccess) rc = fail(NCE_ERR_CUDA, "nce_nce_create: %s", cudaGetErrorString(e));
     }
+    if (!rc && m.tc && step_smem(m, false) > kStepSmemMax) {
+        // the whole A operand does not fit next to the B operand: stage A in two K slices of every layer whose K
+        // extent divides into them (widths 128 split: self channels, then shell means)
+        const int kp_max = kpad16(tile_kin(m.P, m.C0, m.D)), ks = kp_max / 2;
+        bool ok = kp_max % 32 == 0;
+        for (int l = 0; l < m.depth && ok; ++l) {
+            const int kp = kpad16((1 + m.P) * (l == 0 ? m.C0 : m.D));
+            ok = kp <= ks || kp % ks == 0;
+        }
+        if (ok) m.tc_ks = ks;
+    }
     if (!rc && step_smem(m, false) > kStepSmemMax)
         rc = fail(NCE_ERR_UNSUPPORTED, "nce_nce_create: receptive field%s too large for shared memory (%zu bytes)",
                   m.tc ? " and tensor-core tiles" : "", step_smem(m, false));
@@ -1732,7 +1884,8 @@ int nce_nce_destroy(nce_nce_handle h) {
     if (!h) return NCE_OK;
     cudaDeviceSynchronize();
     for (void *p : h->allocs) cudaFree(p);
-    for (void *p : {(void *)h->slot, (void *)h->list, (void *)h->newbuf, (void *)h->e_new, (void *)h->err}) if (p) cudaFree(p);
+    for (void *p : {(void *)h->slot, (void *)h->list, (void *)h->newbuf, (void *)h->e_new, (void *)h->err, (void *)h->pend})
+        if (p) cudaFree(p);
     delete h;
     return NCE_OK;
 }
@@ -1810,31 +1963,8 @@ int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_c
     jb.n_near = st->n_near;
     jb.near_eV = ck->near_eV > 0.0 ? ck->near_eV : ((h->dev.mma == 1 || h->dev.mma == 2) ? 1e-2 : 1e-4);
     if (ck->n_steps == 0) return NCE_OK;
-    const int per_sm = ck->ctas_per_sm > 1 ? ck->ctas_per_sm : 1;
-    NCE_CHECK(per_sm <= 2, "nce_nce_run_chunk: ctas_per_sm must be 1 or 2");
-    const size_t lim = per_sm == 2 ? kStepSmemMax2 : kStepSmemMax;
-    const bool w_smem = step_smem(h->dev, true) <= lim;
-    const size_t sm = step_smem(h->dev, w_smem);
-    NCE_CHECK(sm <= lim, "nce_nce_run_chunk: %zu bytes of shared memory per CTA do not fit %d CTAs per SM", sm, per_sm);
-    const int CL = ck->cluster > 1 ? ck->cluster : 1;
-    NCE_CHECK(CL == 1 || CL == 2 || CL == 4 || CL == 8, "nce_nce_run_chunk: cluster must be 1, 2, 4 or 8");
-    if (CL == 1 || h->dev.depth == 0) {
-        auto kern = per_sm == 2 ? nce_chunk_kernel<2> : nce_chunk_kernel<1>;
-        NCE_CUDA(::nce::raise_smem_limit((const void *)kern, sm));
-        kern<<<st->R, 256, sm, (cudaStream_t)stream>>>(jb, w_smem ? 1 : 0);
-    } else {
-        auto kern = per_sm == 2 ? nce_chunk_cluster_kernel<2> : nce_chunk_cluster_kernel<1>;
-        NCE_CUDA(::nce::raise_smem_limit((const void *)kern, sm));
-        cudaLaunchConfig_t cfg; std::memset(&cfg, 0, sizeof(cfg));
-        cfg.gridDim = dim3((unsigned)(st->R * CL)); cfg.blockDim = dim3(256); cfg.dynamicSmemBytes = sm;
-        cfg.stream = (cudaStream_t)stream;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = (unsigned)CL; attr[0].val.clusterDim.y = 1; attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr; cfg.numAttrs = 1;
-        NCE_CUDA(cudaLaunchKernelEx(&cfg, kern, jb, (int32_t)(w_smem ? 1 : 0)));
-    }
-    NCE_CUDA(cudaGetLastError());
+    rc = launch_steps(h, jb, ck->cluster, ck->ctas_per_sm, (cudaStream_t)stream);
+    if (rc) return rc;
     if (ck->exchange_rounds > 0 && st->R > 1) {
         NCE_CHECK(st->rep_of_slot && st->ladder_id && st->n_ex, "nce_nce_run_chunk: exchange needs rep_of_slot/ladder_id/n_ex");
         rc = launch_exchange(st->R, st->E, h->dev.scale_eV, st->beta_slot, st->rep_of_slot, st->slot_of_rep, st->ladder_id,
@@ -1842,6 +1972,43 @@ int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_c
                              (cudaStream_t)stream);
         if (rc) return rc;
     }
+    return NCE_OK;
+}
+
+int nce_nce_local_delta(nce_nce_handle h, const nce_nce_state *st, const int32_t *prop_a, const int32_t *prop_b, double *dE_out,
+                        void *stream) {
+    NCE_CHECK(h && st && prop_a && prop_b && dE_out, "nce_nce_local_delta: null argument");
+    NCE_CHECK(st->N == h->dev.N && st->R >= 1, "nce_nce_local_delta: state size mismatch");
+    NCE_CHECK(st->sigma && st->h0 && st->e && st->E && st->beta_slot && st->slot_of_rep && st->n_acc,
+              "nce_nce_local_delta: null state pointer");
+    NCE_CHECK(h->dev.depth < 2 || st->hmid, "nce_nce_local_delta: hmid required for depth >= 2");
+    std::lock_guard<std::mutex> lk(h->mu);
+    int rc = ensure_scratch(h, st->R); if (rc) return rc;
+    NceJob jb = make_nce_job(h, st);
+    jb.n_steps = 1; jb.step0 = 0; jb.prop_a = prop_a; jb.prop_b = prop_b; jb.prop_u = nullptr;
+    jb.dE_out = dE_out; jb.force = -2; jb.rep_index = 1; jb.near_eV = 0.0;
+    return launch_steps(h, jb, 1, 1, (cudaStream_t)stream);
+}
+
+int nce_nce_commit(nce_nce_handle h, const nce_nce_state *st, const int32_t *accept, void *stream) {
+    NCE_CHECK(h && st && accept, "nce_nce_commit: null argument");
+    NCE_CHECK(st->N == h->dev.N && st->R >= 1, "nce_nce_commit: state size mismatch");
+    NCE_CHECK(st->sigma && st->h0 && st->e && st->E && st->n_acc, "nce_nce_commit: null state pointer");
+    NCE_CHECK(h->dev.depth < 2 || st->hmid, "nce_nce_commit: hmid required for depth >= 2");
+    std::lock_guard<std::mutex> lk(h->mu);
+    NCE_CHECK(h->R_alloc >= st->R && h->pend, "nce_nce_commit: no swap was evaluated on this model (nce_nce_local_delta)");
+    NceJob jb = make_nce_job(h, st);
+    nce_commit_kernel<<<st->R, 256, 0, (cudaStream_t)stream>>>(jb, accept);
+    NCE_CUDA(cudaGetLastError());
+    return NCE_OK;
+}
+
+int nce_nce_accept(const double *dE, int32_t n_models, int32_t R, double scale_eV, const float *beta_slot,
+                   const int32_t *slot_of_rep, const double *u, int32_t *accept, void *stream) {
+    NCE_CHECK(dE && beta_slot && slot_of_rep && u && accept && n_models >= 1 && R >= 1, "nce_nce_accept: bad argument");
+    nce_accept_kernel<<<(R + 127) / 128, 128, 0, (cudaStream_t)stream>>>(dE, n_models, R, scale_eV, beta_slot, slot_of_rep, u,
+                                                                         accept);
+    NCE_CUDA(cudaGetLastError());
     return NCE_OK;
 }
 

@@ -99,26 +99,34 @@ __host__ __device__ __forceinline__ uint32_t tmem_cols(int N) {
     return c;
 }
 
-// D[128 x N] (tensor memory) = sum over passes of A_p[128 x Kp] B_p[N x Kp]^T, issued by the calling thread:
-// npass = 1 (A0 B0) or 3 (split bf16: A0 B0 + A0 B1 + A1 B0, hi/lo parts); then commit to mbar
-__device__ __forceinline__ void issue_tile(uint32_t tmem_d, const uint8_t *A0, const uint8_t *A1, const uint8_t *B0,
-                                           const uint8_t *B1, int N, int Kp, int npass, uint64_t *mbar) {
+// D[128 x N] (tensor memory) (+)= sum over products of A_p[128 x 16 nk] B_p[N x 16 nk]^T, issued by the calling
+// thread: npass = 1 (A0 B0) or 3 (split bf16: A0 B0 + A0 B1 + A1 B0, hi/lo parts).  A and B may have different K
+// extents (row-group strides a_sbo, b_sbo): the A tile can hold one K slice of a wider B operand, whose K-steps
+// start at B0/B1.  accumulate = false overwrites D with the first product; then commit to mbar.
+__device__ __forceinline__ void issue_tile_k(uint32_t tmem_d, const uint8_t *A0, const uint8_t *A1, uint32_t a_sbo,
+                                             const uint8_t *B0, const uint8_t *B1, uint32_t b_sbo, int N, int nk,
+                                             int npass, bool accumulate, uint64_t *mbar) {
     fence_after();
     const uint32_t idesc = idesc_bf16(128, N);
-    const uint32_t sbo = (uint32_t)Kp * 16u;
     const uint32_t a0 = smem_u32(A0), b0 = smem_u32(B0);
     const uint32_t a1 = npass > 1 ? smem_u32(A1) : a0, b1 = npass > 1 ? smem_u32(B1) : b0;
-    uint32_t acc = 0;
-    for (int j = 0; j < Kp / 16; ++j) {
+    uint32_t acc = accumulate ? 1u : 0u;
+    for (int j = 0; j < nk; ++j) {
         const uint32_t o = (uint32_t)j * 256u;
-        mma_bf16(tmem_d, sdesc(a0 + o, 128, sbo), sdesc(b0 + o, 128, sbo), idesc, acc);
+        mma_bf16(tmem_d, sdesc(a0 + o, 128, a_sbo), sdesc(b0 + o, 128, b_sbo), idesc, acc);
         acc = 1;
         if (npass > 1) {
-            mma_bf16(tmem_d, sdesc(a0 + o, 128, sbo), sdesc(b1 + o, 128, sbo), idesc, 1);
-            mma_bf16(tmem_d, sdesc(a1 + o, 128, sbo), sdesc(b0 + o, 128, sbo), idesc, 1);
+            mma_bf16(tmem_d, sdesc(a0 + o, 128, a_sbo), sdesc(b1 + o, 128, b_sbo), idesc, 1);
+            mma_bf16(tmem_d, sdesc(a1 + o, 128, a_sbo), sdesc(b0 + o, 128, b_sbo), idesc, 1);
         }
     }
     commit(mbar);
+}
+
+// the whole K extent Kp of A and B in one call
+__device__ __forceinline__ void issue_tile(uint32_t tmem_d, const uint8_t *A0, const uint8_t *A1, const uint8_t *B0,
+                                           const uint8_t *B1, int N, int Kp, int npass, uint64_t *mbar) {
+    issue_tile_k(tmem_d, A0, A1, (uint32_t)Kp * 16u, B0, B1, (uint32_t)Kp * 16u, N, Kp / 16, npass, false, mbar);
 }
 
 }  // namespace umma

@@ -73,12 +73,13 @@ class NCEModel:
     """Geometry + parameters of one cell, uploaded to the device (``nce_nce_create``)."""
 
     def __init__(self, cs, structure, params, mu=None, sd=None, shell_edges=(0.0, 3.3), act="tanh", pool="mean",
-                 ys=1.0, ym=0.0, mma=0):
+                 ys=1.0, ym=0.0, mma=0, geo=None):
         depth = len(params["layers"])
         # 0 float32 CUDA cores; bf16 / split-bf16 tensor cores: 1 / 3 mma.sync, 2 / 4 tcgen05 (tensor memory)
         self.mma = int(mma)
         self.cs, self.params, self.act, self.pool = cs, params, act, pool
-        self.geo = geo = build_geometry(cs, structure, list(shell_edges), depth)
+        # geo: the geometry of another model of the same cell, cluster space, shells and depth (an ensemble's seeds)
+        self.geo = geo = geo if geo is not None else build_geometry(cs, structure, list(shell_edges), depth)
         K1 = geo["K"] + 1
         self.mu = np.zeros(K1) if mu is None else np.asarray(mu, float)
         self.sd = np.ones(K1) if sd is None else np.asarray(sd, float)
@@ -245,8 +246,75 @@ class NCEState:
                    "nce_nce_run_chunk")
 
 
-def setup(mdl, atoms: Structure, seed_idx=0, dtype="float32", table=None):
-    """Reference-shaped entry (``mc_model.py:60-111,175-228``): the MC machinery for ``atoms`` on the GPU."""
+class NCEPatch:
+    """What ``local_delta`` returns as the reference's patch: the swap kept on the device for ``commit``.  It is valid
+    until the next call that runs steps on the same models (the engine keeps one evaluated swap per replica)."""
+
+    def __init__(self, cache, serial, i, j):
+        self.cache, self.serial, self.i, self.j = cache, serial, int(i), int(j)
+
+
+class NCECache:
+    """The reference's ``full_cache`` result on the device: one ``NCEState`` per model of the ensemble (one model
+    unless seed_idx < 0), each with its own layer-0 / hidden / site-energy caches and occupancy."""
+
+    def __init__(self, states):
+        self.states = states
+        self.serial = 0
+
+    @property
+    def sigma(self):
+        return self.states[0].sigma[0]
+
+    @property
+    def E(self):
+        """energy in the model's standardised units, mean over the ensemble (device float64, per replica)"""
+        return sum(s.E for s in self.states) / len(self.states)
+
+
+def _swap_of(sig, flips):
+    """(i, j) of a swap written as the reference's flips [[i, sig[j]], [j, sig[i]]]; anything else is refused."""
+    f = np.asarray(flips.cpu() if hasattr(flips, "cpu") else flips, np.int64).reshape(-1, 2)
+    if f.shape[0] != 2:
+        raise ValueError("this engine evaluates swaps: flips must be [[i, sig[j]], [j, sig[i]]]")
+    (i, si), (j, sj) = (int(x) for x in f[0]), (int(x) for x in f[1])
+    get = (lambda k: int(sig[k].item())) if hasattr(sig, "device") else (lambda k: int(np.asarray(sig)[k]))
+    if si != get(j) or sj != get(i):
+        raise ValueError("this engine evaluates swaps: flips must be [[i, sig[j]], [j, sig[i]]]")
+    return i, j
+
+
+def propose_sites(model, key):
+    """The engine's O(1) swap proposal (``gpu_layer0_implicit.py:205-218``): sublattice group by size, uniform cell
+    and basis site of the group, twice.  key = (seed, step, slot) or an int seed (step 0, slot 0): the same
+    Philox4x32-10 draw the chunk kernels make for that slot at that step.  Returns (i, j) in canonical order."""
+    seed, g, t = (int(key), 0, 0) if np.ndim(key) == 0 else (int(k) for k in key)
+    d = model.desc
+    k = [seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF]
+    x = _lib.philox4x32([g & 0xFFFFFFFF, (g >> 32) & 0xFFFFFFFF, t, 0], k)
+    act_b, act_nb, cum = model.keep["act_b"], model.keep["act_nb"], model.keep["grp_cum"]
+    grp, ba, bb = 0, 0, 0
+    if len(act_nb) > 1 or act_nb[0] > 1:
+        y = _lib.philox4x32([g & 0xFFFFFFFF, (g >> 32) & 0xFFFFFFFF, t, 1], k)
+        while len(act_nb) > 1 and grp < len(act_nb) - 1 and y[0] >= int(cum[grp]):
+            grp += 1
+        ba, bb = (y[1] * int(act_nb[grp])) >> 32, (y[2] * int(act_nb[grp])) >> 32
+    n_cells, nB = int(d.n_cells), int(d.nB)
+    i = ((x[0] * n_cells) >> 32) * nB + int(act_b[grp, ba])
+    j = ((x[1] * n_cells) >> 32) * nB + int(act_b[grp, bb])
+    return i, j
+
+
+def setup(mdl, atoms: Structure, seed_idx=0, dtype="float32", table=None, mma=0):
+    """Reference-shaped entry (``mc_model.py:60-111,175-228``): the MC machinery for ``atoms`` on the GPU.
+
+    Returns the reference's keys: ``energy(sig)`` (eV/atom), ``full_cache(sig)`` -> cache, ``local_delta(cache, sig,
+    flips)`` -> (dE_std, patch, sig), ``commit(cache, patch, accept)`` -> cache, ``propose(key)`` -> (i, j),
+    ``energy_of(cache)``, ``perm`` / ``inv_perm``, ``to_eV_per_atom``, ``dE_eV_total``, ``sig0`` (canonical order).
+    ``local_delta`` / ``commit`` run on the device through ``nce_nce_local_delta`` / ``nce_nce_commit``; flips must
+    be a swap ([[i, sig[j]], [j, sig[i]]], the only move of the reference's NeuralCE driver).  seed_idx < 0: the
+    ensemble of every trained seed, energies and dE the mean over the seeds (``mc_model.py:181-188``)."""
+    import torch
     if table not in (None, "implicit"):
         raise ValueError("only the implicit (template-only) geometry is implemented on this engine")
     if dtype not in ("float32", None):
@@ -254,16 +322,61 @@ def setup(mdl, atoms: Structure, seed_idx=0, dtype="float32", table=None):
     if int(mdl.get("spin", 0) or 0):
         raise NotImplementedError("spin models are not on this engine's path")
     cs = ClusterSpace.build(mdl["primitive"], list(mdl["cutoffs"]))
-    P, mu, sd = expand_params(mdl, seed_idx)
-    model = NCEModel(cs, atoms, P, mu, sd, shell_edges=list(mdl["shell_edges"]), act="tanh", pool="mean",
-                     ys=mdl["ys"], ym=mdl["ym"])
+    seeds = list(range(len(mdl["params"]))) if seed_idx is not None and int(seed_idx) < 0 else [int(seed_idx or 0)]
+    models, Ps = [], []
+    geo = None
+    for k in seeds:
+        P, mu, sd = expand_params(mdl, k)
+        m = NCEModel(cs, atoms, P, mu, sd, shell_edges=list(mdl["shell_edges"]), act="tanh", pool="mean",
+                     ys=mdl["ys"], ym=mdl["ym"], mma=mma, geo=geo)
+        geo = m.geo
+        models.append(m); Ps.append(P)
+    model = models[0]
     ys, ym, n_atoms = mdl["ys"], mdl["ym"], len(atoms)
+    one = np.ones(1, np.float32)
 
-    def energy(sig):
-        st = NCEState(model, np.asarray(sig, np.int8)[None], np.ones(1, np.float32)).full_cache()
-        return float(st.E[0].item()) * ys + ym
+    def full_cache(sig, spin_state=None):
+        sig = np.asarray(sig.cpu() if hasattr(sig, "cpu") else sig, np.int8)[None]
+        return NCECache([NCEState(m, sig, one).full_cache() for m in models])
 
-    return dict(cs=cs, P=P, model=model, depth=model.depth, ym=ym, ys=ys, n_atoms=n_atoms, n_active=model.nA,
-                sig0=model.sig0, energy=energy, perm=model.perm, inv_perm=model.inv_perm, implicit=True, geo=model.geo,
+    def energy_of(cache, P=None):
+        return float(cache.E[0].item())
+
+    def energy(sig, spin_state=None):
+        return energy_of(full_cache(sig)) * ys + ym
+
+    def local_delta(cache, sig, flips, spin_state=None, sflips=None):
+        if spin_state is not None or sflips is not None:
+            raise NotImplementedError("spin models are not on this engine's path")
+        i, j = _swap_of(sig, flips)
+        dev = cache.states[0].sigma.device
+        pa = torch.tensor([i], dtype=torch.int32, device=dev); pb = torch.tensor([j], dtype=torch.int32, device=dev)
+        dE = torch.empty((len(models), 1), dtype=torch.float64, device=dev)
+        for k, (m, st) in enumerate(zip(models, cache.states)):
+            _lib.check(_lib.lib().nce_nce_local_delta(m.handle, C.byref(st.struct()), pa.data_ptr(), pb.data_ptr(),
+                                                      dE[k].data_ptr(), _lib.stream_ptr()), "nce_nce_local_delta")
+        cache.serial += 1
+        for m in models:
+            m.last_eval = (id(cache), cache.serial)
+        return dE.mean(0)[0], NCEPatch(cache, cache.serial, i, j), sig
+
+    def commit(cache, patch, accept):
+        if patch.cache is not cache or any(getattr(m, "last_eval", None) != (id(cache), patch.serial) for m in models):
+            raise RuntimeError("commit: this patch is no longer held by the engine (another local_delta or chunk ran "
+                               "on the same models since)")
+        dev = cache.states[0].sigma.device
+        acc = accept.to(device=dev, dtype=torch.int32).reshape(1) if hasattr(accept, "to") else \
+            torch.tensor([int(bool(accept))], dtype=torch.int32, device=dev)
+        for m, st in zip(models, cache.states):
+            _lib.check(_lib.lib().nce_nce_commit(m.handle, C.byref(st.struct()), acc.data_ptr(), _lib.stream_ptr()),
+                       "nce_nce_commit")
+            m.last_eval = None
+        return cache
+
+    return dict(cs=cs, P=Ps[0], Ps=Ps, model=model, models=models, depth=model.depth, ym=ym, ys=ys, n_atoms=n_atoms,
+                n_active=model.nA, sig0=model.sig0, energy=energy, full_cache=full_cache, energy_of=energy_of,
+                F=dict(energy_of=energy_of), local_delta=local_delta, commit=commit,
+                propose=lambda key: propose_sites(model, key), perm=model.perm, inv_perm=model.inv_perm, implicit=True,
+                geo=model.geo, ensemble=len(models) > 1,
                 to_eV_per_atom=lambda E_std: E_std * ys + ym, dE_eV_total=lambda dE_std: dE_std * ys * n_atoms,
                 new_state=lambda sig, betas: NCEState(model, np.asarray(sig, np.int8), betas))

@@ -382,3 +382,60 @@ def test_near_threshold_steps_are_counted(cuda, precision, path):
     assert st.n_near.cpu().tolist() == [1, 0]
     assert st.n_acc.cpu().tolist() == [0, 0]
     assert np.array_equal(st.sigma.cpu().numpy(), sig_r)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_trajectory_occupancy_in_global_memory(cuda, precision):
+    """A cell too large for shared memory (36^3 conventional = 186,624 sites: the sign-parity kernel reads and writes
+    the replica's occupancy in global memory): host proposal stream, two chunks with exchanges, bit-exact against
+    the oracle, near-threshold counts equal."""
+    torch = cuda
+    from neuralce_gb300.ce import proposal_stream
+    from neuralce_gb300.pt import run_chunk
+    from oracle.ce_oracle import new_state
+    R, T = 4, 400
+    gce, orc, sig_r, beta = _setup(36, seed=17, R=R)
+    assert gce.n_atoms == 186_624
+    E0 = gce.batched_energy(torch.as_tensor(sig_r).cuda()).cpu().numpy()
+    assert abs(E0[0] - orc.energy(sig_r[0])) < 1e-9 * max(1.0, abs(E0[0]))
+    st = _engine_state(sig_r, E0, beta); ref = new_state(sig_r, E0, beta)
+    step = 0
+    for chunk in range(2):
+        pa, pb, pu = proposal_stream(gce, R, T, seed=70 + chunk)
+        dev = tuple(torch.as_tensor(x).cuda() for x in (pa, pb, pu))
+        run_chunk(gce, st, T, step, 0, precision, 8, dev, 1, None, True, chunk % 2,
+                  torch.as_tensor(1.0 - np.random.default_rng(chunk).random(R // 2)).cuda(), path=2)
+        orc.run(ref, T, step, 0, (pa, pb, pu), 1, None, True, chunk % 2, 1.0 - np.random.default_rng(chunk).random(R // 2),
+                n_threads=4, near_eV=1e-9 if precision == 64 else 1e-6)
+        torch.cuda.synchronize()
+        _compare(st, ref, 1e-9 if precision == 64 else 1e-4)
+        step += T
+    assert int(st.n_acc.sum()) > 0
+
+
+def test_batch_with_a_job_in_global_memory(cuda):
+    """A batch whose shared-memory budget holds the small jobs' occupancies (3^3, 4^3 conventional) but not the large
+    one's (24^3 = 55,296 sites, above the 48 KB per-job budget): every job bit-exact against the oracle."""
+    torch = cuda
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.ce import proposal_stream
+    from neuralce_gb300.pt import make_chunk
+    from oracle.ce_oracle import new_state
+    T = 300
+    jobs = []
+    for k, (L, R) in enumerate([(3, 3), (24, 4), (4, 2)]):
+        gce, orc, sig_r, beta = _setup(L, seed=80 + k, R=R)
+        E0 = gce.batched_energy(torch.as_tensor(sig_r).cuda()).cpu().numpy()
+        pa, pb, pu = proposal_stream(gce, R, T, seed=90 + k)
+        jobs.append(dict(gce=gce, orc=orc, st=_engine_state(sig_r, E0, beta), ref=new_state(sig_r, E0, beta),
+                         props=(pa, pb, pu), dev=tuple(torch.as_tensor(x).cuda() for x in (pa, pb, pu))))
+    assert jobs[1]["gce"].n_atoms > 48 * 1024
+    hs = (C.c_void_p * 3)(*[j["gce"].handle.value for j in jobs])
+    ss = (_lib.NcePtState * 3)(*[j["st"].struct() for j in jobs])
+    cks = (_lib.NcePtChunk * 3)(*[make_chunk(T, 0, 0, 64, 8, j["dev"], 1, None, True) for j in jobs])
+    _lib.check(_lib.lib().nce_ce_run_batch(3, hs, ss, cks, _lib.stream_ptr()), "batch")
+    for j in jobs:
+        j["orc"].run(j["ref"], T, 0, 0, j["props"], 1, None, True, n_threads=4, near_eV=1e-9)
+    torch.cuda.synchronize()
+    for j in jobs:
+        _compare(j["st"], j["ref"], 1e-9)

@@ -204,18 +204,20 @@ def _model_bench_mma(L, seed, mma, width=64):
     return m, NCEOracle(m.geo, P, act="silu", pool="sum")
 
 
-@pytest.mark.parametrize("mma,width", [(3, 64), (3, 128), (1, 64), (3, 32), (4, 64), (4, 32), (2, 64), (2, 128),
-                                       (2, 16)])
+@pytest.mark.parametrize("mma,width", [(3, 64), (3, 128), (1, 64), (3, 32), (4, 64), (4, 32), (4, 128), (2, 64),
+                                       (2, 128), (2, 16)])
 def test_tensor_core_forms_vs_oracle(cuda, mma, width):
-    """Layer contractions on tensor cores (mma.sync: 1, 3; tcgen05 with tensor-memory accumulators: 2, 4): split
-    bf16 (3, 4) stays within the float32 bounds of the oracle (energies 1e-4 eV, per-step dE 1e-4 eV); plain bf16
-    operands (1, 2) within its stated bound (per-step dE 5e-2 eV on this model, whose total energy is ~1e2 eV); a
-    chain of forced moves keeps the carried energy equal to a rebuild of the caches in the same form."""
+    """Layer contractions on tensor cores (mma.sync: 1, 3; tcgen05 with tensor-memory accumulators: 2, 4).  The split
+    bf16 forms (3, 4) -- the precision form -- stay within the benchmark spec's bound of 1e-4 eV per swap and the float32
+    energy bound; at width 128 the tcgen05 split form stages its A operand in two K slices.  Plain bf16 operands
+    (1, 2) are a labelled comparison point with their own stated bound of 1e-2 eV per swap (measured ~5e-3 eV on
+    this model, whose total energy is ~1e2 eV).  A chain of forced moves keeps the carried energy equal to a rebuild
+    of the caches in the same form."""
     torch = cuda
     from neuralce_gb300.nce import NCEState
     from oracle.nce_oracle import run_chain
     m, orc = _model_bench_mma(3, 4, mma, width)
-    tol_E, tol_dE = (1e-4 * max(1.0, m.N / 64), 1e-4) if mma in (3, 4) else (5e-1, 5e-2)
+    tol_E, tol_dE = (1e-4 * max(1.0, m.N / 64), 1e-4) if mma in (3, 4) else (5e-1, 1e-2)
     rng = np.random.default_rng(3)
     sig = np.stack([m.sig0[rng.permutation(m.N)] for _ in range(2)]).astype(np.int8)
     st = NCEState(m, sig, np.ones(2)).full_cache()
@@ -242,12 +244,12 @@ def test_tensor_core_forms_vs_oracle(cuda, mma, width):
     assert abs(Ecar - float(st2.E[0].item())) * m.scale_eV < 1e-4 * max(1.0, m.N / 64)
 
 
-@pytest.mark.parametrize("mma", [3, 4, 2])
-def test_tensor_core_cluster_equals_single_cta(cuda, mma):
+@pytest.mark.parametrize("mma,width", [(3, 64), (4, 64), (2, 64), (4, 128)])
+def test_tensor_core_cluster_equals_single_cta(cuda, mma, width):
     torch = cuda
     from neuralce_gb300.nce import NCEState
     from neuralce_gb300.workloads import ladder, replica_configs
-    m, _ = _model_bench_mma(3, 6, mma)
+    m, _ = _model_bench_mma(3, 6, mma, width)
     _, beta = ladder(4)
     sig = replica_configs(m.sig0, 4, 3)
     a = NCEState(m, sig, beta).full_cache(); b = NCEState(m, sig, beta).full_cache()
@@ -278,14 +280,6 @@ def test_tc_gemm_matches_fp32(cuda, K, N):
     # the plain bf16 form is much further from the float32 product than the split form
     err1 = ((C.double() - ref64).abs() / (scale + 1e-30)).max().item()
     assert err1 > 4 * err
-
-
-def test_tcgen05_split_too_wide_is_refused(cuda):
-    """Split operands at width 128 need more shared memory than a CTA has: creation fails with a message."""
-    from neuralce_gb300 import _lib
-    m, _ = _model_bench_mma(3, 4, 4, 128)
-    with pytest.raises(_lib.NceError, match="shared memory"):
-        m.handle
 
 
 def test_two_ctas_per_sm_refused_when_too_large(cuda, nipt_model):
@@ -371,3 +365,46 @@ def test_ternary_point_functions(cuda, cluster):
     assert np.abs((dE.cpu().numpy()[:, 0] - dEs) * m.scale_eV).max() < 1e-4
     assert np.array_equal(st.sigma[0].cpu().numpy(), sig_ref.astype(np.int8))
     m.check_errors()
+
+
+@pytest.mark.parametrize("mma,width", [(0, 64), (4, 64), (4, 128), (3, 128)])
+def test_config_cell_chain_matches_oracle(cuda, mma, width):
+    """The configuration-1 cell itself (8 x 8 x 8 conventional fcc, 2,048 sites: receptive fields of 141 / 321 / 603
+    / 1,007 sites that no longer wrap onto themselves), depth 3, SiLU, sum readout, at width 64 (configuration 1)
+    and 128 (configuration 3's width): 16 forced moves against the oracle's local_delta chain, per step within
+    1e-4 eV, then carried energy vs a rebuild of the caches."""
+    torch = cuda
+    from neuralce_gb300.nce import NCEState
+    from oracle.nce_oracle import run_chain
+    m, orc = _model_bench_mma(8, 4, mma, width)
+    assert m.N == 2048
+    T = 16
+    rng = np.random.default_rng(9)
+    pi = rng.integers(0, m.N, T).astype(np.int32); pj = rng.integers(0, m.N, T).astype(np.int32)
+    st = NCEState(m, m.sig0[None].astype(np.int8), np.ones(1)).full_cache()
+    dE = torch.zeros((T, 1), dtype=torch.float64, device="cuda")
+    props = tuple(torch.as_tensor(x.reshape(T, 1)).cuda() for x in (pi, pj, np.full(T, 0.5)))
+    st.run_chunk(T, 0, proposals=props, dE_out=dE, force=1, cluster=2)
+    torch.cuda.synchronize()
+    m.check_errors()
+    cache = orc.full_cache(m.sig0.astype(np.int64))
+    E0 = orc.energy_of(cache)
+    cache, sig_ref, dsum, _, dEs, _ = run_chain(orc, cache, m.sig0, pi, pj, np.full(T, 0.5), 0.0, m.scale_eV)
+    err = np.abs((dE.cpu().numpy()[:, 0] - dEs) * m.scale_eV).max()
+    print(f"2048 sites, mma {mma}, width {width}: max |dE - oracle| = {err:.3e} eV")
+    assert err < 1e-4, err
+    assert np.array_equal(st.sigma[0].cpu().numpy(), sig_ref.astype(np.int8))
+    Ecar = float(st.E[0].item())
+    assert abs(Ecar - (E0 + dsum)) * m.scale_eV < 1e-3           # 2,048-site sum of float32 site energies
+    st2 = NCEState(m, st.sigma.cpu().numpy(), np.ones(1)).full_cache()
+    torch.cuda.synchronize()
+    assert abs(Ecar - float(st2.E[0].item())) * m.scale_eV < 1e-3
+    assert np.abs(st2.e[0].cpu().numpy() - cache["e"]).max() < 1e-4
+
+
+@pytest.mark.parametrize("mma,width,cluster", [(0, 64, 4), (4, 64, 8), (4, 128, 4)])
+def test_config_cell_metropolis_matches_oracle(cuda, mma, width, cluster):
+    """Metropolis chains of 4 replicas on the 2,048-site configuration-1 cell, checked step by step against the
+    oracle (decisions equal except at counted near-threshold steps; occupancies bit-exact)."""
+    m, orc = _model_bench_mma(8, 5, mma, width)
+    _metropolis_vs_oracle(cuda, m, orc, 4, 24, 13, cluster)
