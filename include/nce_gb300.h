@@ -114,6 +114,16 @@ int nce_ce_cluster_counts(nce_ce_handle h, const int8_t *sigma, int32_t R, int64
  * energies from tracked cluster-vector sums). */
 int nce_ce_energy_from_counts(nce_ce_handle h, const int64_t *cv, int32_t R, double *E, void *stream);
 
+/* Local fields of R configurations sigma (R, N) (device) -> field (R, N) int64 (device): G(i) = sum over the cluster
+ * instances containing site i of 2 eci Pi, fixed point.  A swap of a and b then changes the energy by
+ * -G(a) - G(b) + 2 C(a, b) (C: the instances containing both), so the chunk kernel decides a proposal in O(1) and
+ * pays for the rows only when a swap is accepted.  Needs +-1 point functions and a cell without aliasing
+ * (nce_ce_has_local_field).  No counterpart in the reference, whose delta_energy_a re-evaluates the rows of both
+ * sites at every step (neuralce/ce/ce_gpu_implicit.py:181-191). */
+int nce_ce_field_init(nce_ce_handle h, const int8_t *sigma, int32_t R, int64_t *field, void *stream);
+/* ok = 1 when the local-field path can run on this cell; scale (may be NULL) = eV per fixed-point unit (2^-S). */
+int nce_ce_has_local_field(nce_ce_handle h, int32_t *ok, double *scale);
+
 /* Parallel-tempering state of one job, all device pointers. */
 typedef struct {
     int32_t R;             /* replicas = temperature slots */
@@ -137,6 +147,10 @@ typedef struct {
                               when log u < -beta dE (neuralce/ce/pt_mcmc_ce.py:563); a step is near its threshold when
                               |dE + ln(u) / beta| < the chunk's near_eV, the stated per-swap dE error bound of the
                               precision form: only there can a decision differ from a float64 reference's */
+    int64_t *field;        /* (R, N) or NULL: every site's local field G(i) = sum over the reverse rows of i of
+                              2 eci Pi, in the float64 kernels' fixed point (exact integers).  When set (and the cell
+                              supports it, nce_ce_has_local_field), precision-64 chunks run the local-field kernel and
+                              keep the fields current; fill it with nce_ce_field_init after (re)setting sigma. */
 } nce_pt_state;
 
 /* One chunk of steps.  Proposals: host-supplied stream (prop_a/prop_b/prop_u device arrays indexed
@@ -155,7 +169,9 @@ typedef struct {
     const double *ex_u;        /* (ceil((R-1)/2)) device uniforms, or NULL -> Philox */
     int32_t precision;         /* 64 or 32 */
     int32_t warps;             /* warps per replica (0 = default) */
-    int32_t path;              /* 0 auto, 1 general point-function products, 2 sign parity (point functions in {-1,+1}) */
+    int32_t path;              /* 0 auto (local field when the state has a field, else sign parity when the point
+                                  functions are in {-1,+1}, else general), 1 general point-function products, 2 sign
+                                  parity, 3 local field (precision 64, state.field set) */
     int32_t cluster;           /* sign parity: CTAs per replica (1, 2, 4, 8; thread-block cluster); the cell must fit in
                                   shared memory, otherwise one CTA is used */
     int64_t *step_dev;         /* device counter or NULL: when set, the chunk's first global step is read from it

@@ -29,7 +29,7 @@ class NceCeTables(C.Structure):
 class NcePtState(C.Structure):
     _fields_ = [("R", i32), ("N", i64), ("sigma", vp), ("E", vp), ("beta_slot", vp), ("rep_of_slot", vp),
                 ("slot_of_rep", vp), ("ladder_id", vp), ("E_min_rep", vp), ("n_acc", vp), ("n_ex", vp), ("cv", vp),
-                ("n_near", vp)]
+                ("n_near", vp), ("field", vp)]
 
 
 class NcePtChunk(C.Structure):
@@ -101,6 +101,8 @@ SIGNATURES = {
     "nce_ce_run_batch": (i32, [i32, P(vp), P(NcePtState), P(NcePtChunk), vp]),
     "nce_ce_run_chunk_host": (i32, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, P(NcePtChunk), vp]),
     "nce_ce_errors": (i32, [vp, P(i32)]),
+    "nce_ce_field_init": (i32, [vp, vp, i32, vp, vp]),
+    "nce_ce_has_local_field": (i32, [vp, P(i32), P(f64)]),
     "nce_pt_minimum": (i32, [P(NcePtState), vp, vp, vp]),
     "nce_philox4x32": (None, [P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)]),
     "nce_server_create": (i32, [P(NceServerConfig), P(vp)]),

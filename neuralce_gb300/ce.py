@@ -167,6 +167,8 @@ class GPUClusterExpansion:
     # ── energies ──
     def _sigma_dev(self, sigma):
         import torch
+        if isinstance(sigma, torch.Tensor) and sigma.is_cuda and sigma.dtype == torch.int8:
+            return sigma.reshape(-1, self.n_atoms).contiguous()      # already on the device: no round trip
         s = torch.as_tensor(np.asarray(sigma.cpu() if hasattr(sigma, "cpu") else sigma), dtype=torch.int8)
         return s.reshape(-1, self.n_atoms).contiguous().cuda()
 
@@ -180,6 +182,31 @@ class GPUClusterExpansion:
         _lib.check(_lib.lib().nce_ce_energy(self.handle, sd.data_ptr(), R, precision, E.data_ptr(), _lib.stream_ptr()),
                    "nce_ce_energy")
         return E
+
+    @property
+    def has_local_field(self):
+        """True when the local-field kernel can run on this cell (+-1 point functions, no aliasing)."""
+        ok = C.c_int32(0)
+        _lib.check(_lib.lib().nce_ce_has_local_field(self.handle, C.byref(ok), None), "nce_ce_has_local_field")
+        return bool(ok.value)
+
+    @property
+    def field_scale(self):
+        """eV per unit of the local fields (2^-S of the fixed point)."""
+        ok, sc = C.c_int32(0), C.c_double(0.0)
+        _lib.check(_lib.lib().nce_ce_has_local_field(self.handle, C.byref(ok), C.byref(sc)), "nce_ce_has_local_field")
+        return sc.value
+
+    def field_init(self, sigma_batch, field=None):
+        """Local fields (R, N) int64 of R configurations (``nce_ce_field_init``): G(i) = sum over the cluster instances
+        containing site i of 2 eci Pi, fixed point x 2^S."""
+        import torch
+        sd = self._sigma_dev(sigma_batch)
+        if field is None:
+            field = torch.empty(sd.shape, dtype=torch.int64, device=sd.device)
+        _lib.check(_lib.lib().nce_ce_field_init(self.handle, sd.data_ptr(), sd.shape[0], field.data_ptr(), _lib.stream_ptr()),
+                   "nce_ce_field_init")
+        return field
 
     def cluster_counts(self, sigma_batch):
         """(R, n_cols) int64 cluster-vector sums of device configurations (point functions in {-1, +1})."""

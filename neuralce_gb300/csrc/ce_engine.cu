@@ -73,6 +73,13 @@ struct CEJob {
     int64_t *n_near;       // (R) near-threshold step counts or null
     double near_eV;        // near-threshold band (eV)
     int64_t near_fix;      // the band in fixed point, rounded up, plus one unit (threshold rounding), fixed-point kernels
+    // local-field kernel
+    int64_t *field;        // (R, N) G of every site (fixed point, x 2^fix_shift)
+    const int32_t *lf_off; // (nB, n_nbr + 1) start of each neighbour's row list
+    const uint16_t *lf_idx;// rows of the site containing that neighbour as a member
+    const int16_t *lf_box; // (nB, 2e0+1, 2e1+1, 2e2+1, nB) neighbour index of a displacement, or -1
+    int32_t lf_e0, lf_e1, lf_e2, lf_nidx;
+    int32_t gf_smem;       // this job's occupancy and field are copied into shared memory for the chunk
 };
 
 struct CEBatch {
@@ -635,6 +642,300 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     if (CLUSTER) cg::this_cluster().sync();              // no CTA leaves while others may still add into its counters
 }
 
+// ── local-field kernel ───────────────────────────────────────────────────────────────────────────────
+// Every site i of a replica carries its field G(i) = sum over the reverse rows r of i of 2 eci_r Pi_r, in the
+// float64 kernels' fixed point (x 2^S, exact integers).  Flipping one site negates every product it is a member of,
+// so a swap of a and b (different species) changes the energy by
+//     dE = -G(a) - G(b) + 2 C(a, b),   C(a, b) = sum over the rows of a that also contain b of 2 eci Pi,
+// which is exactly the sum the sign-parity kernel forms (-2 eci Pi_old over the rows containing one of the two
+// sites), as the same integers.  C is non-zero only when b lies in a's neighbourhood: an O(1) lookup of the
+// displacement (a box of k-space offsets) names b's neighbourhood entry, and the rows of a that contain that entry
+// are listed per entry (lf_off / lf_idx).  A rejected swap changes nothing, so warp 0 evaluates the next 32 steps
+// at once, one per lane, on the same state: every step before the first accepted one is rejected as evaluated, and
+// the first accepted one is exact too; steps after it are evaluated again in the next round.  Near pairs (C to
+// compute) are resolved in step order by the whole warp.  Only an accepted swap costs the block: both sites' rows
+// are evaluated once (parity change per row, as the sign-parity kernel), and each neighbour's field moves by the
+// sum of its changed rows' 2 eci dPi; the two sites' own fields become -G + 2C.
+struct LfLayout {
+    size_t bix, rcol, chunk, nb, efix, off, idx, box, v, bits, nbits, dcv, fld, sig, total;
+    __host__ __device__ static LfLayout make(int nB, int J, int mo, int n_nbr, int n_pfc, int n_cols, int max_chunks, int nidx,
+                                             int boxsz, int64_t budget_sites, bool tables) {
+        LfLayout L; size_t o = 0;
+        auto al = [](size_t x, size_t a) { return (x + a - 1) / a * a; };
+        if (tables) {
+            L.bix = o; o = al(o + sizeof(uint16_t) * (size_t)nB * J * mo, 16);
+            L.rcol = o; o = al(o + (size_t)nB * J, 16);
+        } else {
+            L.bix = L.rcol = 0;
+        }
+        L.chunk = o; o = al(o + sizeof(uint32_t) * (size_t)nB * max_chunks, 16);
+        L.nb = o; o = al(o + sizeof(int4) * (size_t)nB * n_nbr, 16);
+        L.efix = o; o = al(o + sizeof(long long) * (size_t)n_cols, 16);
+        L.off = o; o = al(o + sizeof(int32_t) * (size_t)nB * (n_nbr + 1), 16);
+        L.idx = o; o = al(o + sizeof(uint16_t) * (size_t)nidx, 16);
+        L.box = o; o = al(o + sizeof(int16_t) * (size_t)nB * boxsz * nB, 16);
+        L.v = o; o = al(o + sizeof(long long) * 2 * (size_t)J, 16);                 // [side][row] 2 eci dPi (fixed point)
+        L.bits = o; o = al(o + (size_t)2 * n_pfc * n_nbr, 16);                      // [side][pfc][n_nbr] old | new << 1
+        L.nbits = o; o = al(o + (size_t)n_pfc * n_nbr, 16);                         // decider: old bits of one neighbourhood
+        L.dcv = o; o = al(o + sizeof(int32_t) * (size_t)n_cols, 16);
+        if (budget_sites > 0) {
+            L.fld = o; o = al(o + sizeof(long long) * (size_t)budget_sites, 16);
+            L.sig = o; o = al(o + (size_t)budget_sites, 16);
+        } else {
+            L.fld = L.sig = 0;
+        }
+        L.total = o;
+        return L;
+    }
+};
+
+struct LfStep {                          // the accepted swap, published by the decider warp to the block
+    int64_t ia, ib;
+    long long C;
+    int32_t ka[3], kb[3], ba, bb, sa, sb, go;
+};
+
+// neighbourhood entry of site (bb, kb) in the neighbourhood of (ba, ka), or -1 (not a neighbour)
+__device__ __forceinline__ int lf_lookup(const CEJob &jb, const int16_t *box, int ba, const int32_t ka[3], int bb,
+                                         const int32_t kb[3]) {
+    int x0 = kb[0] - ka[0], x1 = kb[1] - ka[1], x2 = kb[2] - ka[2];
+    x0 += x0 < 0 ? jb.d0 : 0; x1 += x1 < 0 ? jb.d1 : 0; x2 += x2 < 0 ? jb.d2 : 0;
+    x0 -= x0 > jb.d0 / 2 ? jb.d0 : 0; x1 -= x1 > jb.d1 / 2 ? jb.d1 : 0; x2 -= x2 > jb.d2 / 2 ? jb.d2 : 0;
+    if (x0 < -jb.lf_e0 || x0 > jb.lf_e0 || x1 < -jb.lf_e1 || x1 > jb.lf_e1 || x2 < -jb.lf_e2 || x2 > jb.lf_e2) return -1;
+    const int w1 = 2 * jb.lf_e1 + 1, w2 = 2 * jb.lf_e2 + 1, bsz = (2 * jb.lf_e0 + 1) * w1 * w2;
+    const int cell = ((x0 + jb.lf_e0) * w1 + (x1 + jb.lf_e1)) * w2 + (x2 + jb.lf_e2);
+    return box[((size_t)ba * bsz + cell) * jb.nB + bb];
+}
+
+__device__ __forceinline__ uint32_t lf_site(const CEJob &jb, const int32_t k[3], const int4 nbe) {
+    return (((uint32_t)wrap_add(k[0], nbe.x, jb.d0) * (uint32_t)jb.d1 + (uint32_t)wrap_add(k[1], nbe.y, jb.d1)) *
+            (uint32_t)jb.d2 + (uint32_t)wrap_add(k[2], nbe.z, jb.d2)) * (uint32_t)jb.nB + (uint32_t)nbe.w;
+}
+
+// exact warp sum of int64 terms whose total stays below 2^61 in magnitude (three 21-bit slices)
+__device__ __forceinline__ long long warp_sum_i64(long long part) {
+    const unsigned l0 = (unsigned)(part & 0x1fffff), l1 = (unsigned)((part >> 21) & 0x1fffff);
+    const int l2 = (int)(part >> 42);
+    const unsigned s0 = __reduce_add_sync(0xffffffffu, l0), s1 = __reduce_add_sync(0xffffffffu, l1);
+    const int s2 = __reduce_add_sync(0xffffffffu, l2);
+    return (long long)s0 + ((long long)s1 << 21) + ((long long)s2 << 42);
+}
+
+template <int MO>
+__global__ void __launch_bounds__(1024) ce_lf_chunk_kernel(const __grid_constant__ CEBatch bt, int32_t budget) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ LfStep X;
+    const int j = find_job(bt, blockIdx.x);
+    const CEJob &jb = bt.job[j];
+    const int r = blockIdx.x - jb.cta_base;
+    if (r >= jb.R) return;
+    const int tid = threadIdx.x, nt = blockDim.x, nw = nt >> 5, lane = tid & 31, warp = tid >> 5;
+    const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc, n_cols = jb.n_cols, J = jb.J;
+    const int bsz = (2 * jb.lf_e0 + 1) * (2 * jb.lf_e1 + 1) * (2 * jb.lf_e2 + 1);
+    const LfLayout L = LfLayout::make(jb.nB, J, MO, n_nbr, n_pfc, n_cols, jb.max_chunks, jb.lf_nidx, bsz, budget,
+                                      bt.tables_in_smem);
+    const uint16_t *tbix; const uint8_t *trcol;
+    const size_t nl = (size_t)jb.nB * J * MO, ne = (size_t)jb.nB * J;
+    if (bt.tables_in_smem) {
+        uint16_t *sb = reinterpret_cast<uint16_t *>(smem + L.bix); uint8_t *sc = smem + L.rcol;
+        for (size_t i = tid; i < nl; i += nt) sb[i] = __ldg(jb.bix + i);
+        for (size_t i = tid; i < ne; i += nt) sc[i] = __ldg(jb.rcol + i);
+        tbix = sb; trcol = sc;
+    } else {
+        tbix = jb.bix; trcol = jb.rcol;
+    }
+    uint32_t *chunks = reinterpret_cast<uint32_t *>(smem + L.chunk);
+    for (int i = tid; i < jb.nB * jb.max_chunks; i += nt) chunks[i] = __ldg(jb.chunks + i);
+    int4 *nbt = reinterpret_cast<int4 *>(smem + L.nb);
+    for (int i = tid; i < jb.nB * n_nbr; i += nt) nbt[i] = make_int4(__ldg(jb.nb_uo + 3 * i), __ldg(jb.nb_uo + 3 * i + 1),
+                                                                      __ldg(jb.nb_uo + 3 * i + 2), __ldg(jb.nb_b + i));
+    long long *efix = reinterpret_cast<long long *>(smem + L.efix);
+    for (int c = tid; c < n_cols; c += nt) efix[c] = (long long)__ldg(jb.ecol_fix + c);
+    int32_t *loff = reinterpret_cast<int32_t *>(smem + L.off);
+    for (int i = tid; i < jb.nB * (n_nbr + 1); i += nt) loff[i] = __ldg(jb.lf_off + i);
+    uint16_t *lidx = reinterpret_cast<uint16_t *>(smem + L.idx);
+    for (int i = tid; i < jb.lf_nidx; i += nt) lidx[i] = __ldg(jb.lf_idx + i);
+    int16_t *box = reinterpret_cast<int16_t *>(smem + L.box);
+    for (int i = tid; i < jb.nB * bsz * jb.nB; i += nt) box[i] = __ldg(jb.lf_box + i);
+    long long *v = reinterpret_cast<long long *>(smem + L.v);
+    uint8_t *bits = smem + L.bits, *nbits = smem + L.nbits;
+    int32_t *dcv = reinterpret_cast<int32_t *>(smem + L.dcv);
+    for (int c = tid; c < n_cols; c += nt) dcv[c] = 0;
+    const bool track = jb.cv != nullptr;
+    int8_t *gsig = jb.sigma + (int64_t)r * jb.N;
+    long long *gfld = reinterpret_cast<long long *>(jb.field) + (int64_t)r * jb.N;
+    int8_t *sig = jb.gf_smem ? reinterpret_cast<int8_t *>(smem + L.sig) : gsig;
+    long long *G = jb.gf_smem ? reinterpret_cast<long long *>(smem + L.fld) : gfld;
+    if (jb.gf_smem)
+        for (int64_t i = tid; i < jb.N; i += nt) { sig[i] = gsig[i]; G[i] = gfld[i]; }
+    uint32_t smask = 0;
+    for (int c = 0; c < n_pfc; ++c)
+        for (int q = 0; q < 4; ++q) smask |= (uint32_t)(__ldg(jb.sbits + c * 4 + q) & 1u) << (c * 4 + q);
+    const int32_t t = jb.slot_of_rep[r];
+    const double E0c = jb.E[r];
+    double Emin = jb.E_min_rep[r];
+    const double fscale = ldexp(1.0, -jb.fix_shift);
+    const int64_t g0 = jb.step_dev ? *jb.step_dev : jb.step0;
+    const int64_t T = jb.n_steps;
+    long long dsum = 0, dmin = 0;                          // warp 0: the chunk's energy change and its running minimum
+    int64_t nacc = 0, nnear = 0, s_cur = 0;
+    __syncthreads();
+    for (;;) {
+        if (warp == 0) {
+            if (lane == 0) X.go = 0;
+            __syncwarp();
+            while (s_cur < T) {
+                const int64_t s = s_cur + lane;
+                const bool live = s < T;
+                BinProp P;
+                int sa = 0, sb = 0, nbi = -1, valid = 0;
+                long long part = 0;
+                if (live) {
+                    bin_propose(jb, g0, s, t, P);
+                    sa = sig[P.ia]; sb = sig[P.ib];
+                    valid = sa != sb;
+                    if (valid) {
+                        nbi = lf_lookup(jb, box, P.ba, P.ka, P.bb, P.kb);
+                        part = -(G[P.ia] + G[P.ib]);
+                    }
+                }
+                bool acc = valid && nbi < 0 && part < P.thr;
+                const unsigned farm = __ballot_sync(0xffffffffu, acc);
+                const unsigned nearm = __ballot_sync(0xffffffffu, valid && nbi >= 0);
+                int first = farm ? __ffs(farm) - 1 : 32;
+                unsigned pend = nearm & (first < 32 ? ((1u << first) - 1u) : 0xffffffffu);
+                long long Cq = 0;
+                while (pend) {                             // near pairs before the first far acceptance, in step order
+                    const int q = __ffs(pend) - 1;
+                    const int qba = __shfl_sync(0xffffffffu, P.ba, q), qnb = __shfl_sync(0xffffffffu, nbi, q);
+                    int32_t qk[3];
+                    for (int c = 0; c < 3; ++c) qk[c] = __shfl_sync(0xffffffffu, P.ka[c], q);
+                    for (int n = lane; n < n_nbr; n += 32) {  // old bits of a's neighbourhood
+                        const int so = sig[lf_site(jb, qk, nbt[qba * n_nbr + n])];
+                        for (int c = 0; c < n_pfc; ++c) nbits[c * n_nbr + n] = (uint8_t)((smask >> (c * 4 + so)) & 1u);
+                    }
+                    __syncwarp();
+                    long long cp = 0;
+                    const int o0 = loff[qba * (n_nbr + 1) + qnb], o1 = loff[qba * (n_nbr + 1) + qnb + 1];
+                    for (int k = o0 + lane; k < o1; k += 32) {
+                        const int rr = lidx[k];
+                        const uint16_t *bx = tbix + ((size_t)qba * J + rr) * MO;
+                        unsigned x = 0;
+#pragma unroll
+                        for (int m = 0; m < MO; ++m) x ^= nbits[bx[m]];
+                        const long long e = efix[trcol[(size_t)qba * J + rr]];
+                        cp += (x & 1u) ? -e : e;
+                    }
+                    const long long C = warp_sum_i64(cp);
+                    __syncwarp();
+                    if (lane == q) { Cq = C; part += 2 * C; acc = part < P.thr; }
+                    if (__shfl_sync(0xffffffffu, (int)acc, q)) { first = q; break; }
+                    pend &= pend - 1;
+                }
+                const int avail = (int)(T - s_cur < 32 ? T - s_cur : 32);
+                const bool accepted = first < avail;
+                const int n_adv = accepted ? first + 1 : avail;
+                const long long dfirst = __shfl_sync(0xffffffffu, part, first & 31);
+                if (lane < n_adv && valid) {
+                    const long long dd = part - (long long)P.thr;
+                    nnear += (dd < 0 ? -dd : dd) < (long long)jb.near_fix;
+                }
+                if (jb.E_samples && lane < n_adv && (s + 1) % jb.sample_interval == 0) {
+                    const long long da = dsum + ((accepted && lane == first) ? dfirst : 0);
+                    jb.E_samples[((s + 1) / jb.sample_interval - 1) * jb.R + t] = E0c + (double)da * fscale;
+                }
+                s_cur += n_adv;
+                if (accepted) {
+                    dsum += dfirst; dmin = dsum < dmin ? dsum : dmin; ++nacc;
+                    if (lane == first) {
+                        X.ia = P.ia; X.ib = P.ib; X.C = Cq; X.ba = P.ba; X.bb = P.bb; X.sa = sa; X.sb = sb;
+                        for (int c = 0; c < 3; ++c) { X.ka[c] = P.ka[c]; X.kb[c] = P.kb[c]; }
+                        X.go = 1;
+                    }
+                    break;
+                }
+            }
+        }
+        __syncthreads();
+        if (!X.go) break;
+        // ── accepted swap: the rows of both sites, then the neighbours' fields ──
+        const int64_t ia = X.ia, ib = X.ib;
+        for (int q = tid; q < 2 * n_nbr; q += nt) {
+            const int side = q >= n_nbr, n = side ? q - n_nbr : q;
+            const uint32_t st = lf_site(jb, side ? X.kb : X.ka, nbt[(side ? X.bb : X.ba) * n_nbr + n]);
+            const int so = sig[st];
+            const int sn = (st == (uint32_t)ia) ? X.sb : ((st == (uint32_t)ib) ? X.sa : so);
+            uint8_t *bs = bits + (size_t)side * n_pfc * n_nbr;
+            for (int c = 0; c < n_pfc; ++c)
+                bs[c * n_nbr + n] = (uint8_t)(((smask >> (c * 4 + so)) & 1u) | (((smask >> (c * 4 + sn)) & 1u) << 1));
+        }
+        __syncthreads();
+        {
+            // rows in column-aligned chunks of <= 32 (lane per row): 2 eci dPi of every row; column counts when tracked
+            const int nca = __ldg(jb.n_chunks + X.ba), ncb = __ldg(jb.n_chunks + X.bb), total = nca + ncb;
+            for (int k = warp; k < total; k += nw) {
+                const int side = k >= nca, kk = side ? k - nca : k;
+                const int b0 = side ? X.bb : X.ba;
+                const uint32_t d = chunks[b0 * jb.max_chunks + kk];
+                const int col = (int)(d & 0xffu), start = (int)((d >> 8) & 0xffffu), len = (int)(d >> 24);
+                int sgn = 0;
+                if (lane < len) {
+                    const int rr = start + lane;
+                    const uint16_t *bx = tbix + ((size_t)b0 * J + rr) * MO;
+                    const uint8_t *bs = bits + (size_t)side * n_pfc * n_nbr;
+                    unsigned x = 0;
+#pragma unroll
+                    for (int m = 0; m < MO; ++m) x ^= bs[bx[m]];
+                    if ((x ^ (x >> 1)) & 1u) sgn = (x & 1u) ? 1 : -1;       // dPi = 2 sgn
+                    v[side * J + rr] = sgn ? 2 * sgn * efix[col] : 0;
+                }
+                if (track) {
+                    const int n = (int)__reduce_add_sync(0xffffffffu, (unsigned)sgn);
+                    if (lane == 0 && n) atomicAdd(&dcv[col], 2 * n);
+                }
+            }
+        }
+        __syncthreads();
+        {
+            // each neighbour's field: the sum of its changed rows, eight lanes per neighbour entry
+            const int grp = tid >> 3, gl = tid & 7, ngrp = nt >> 3, ntask = 2 * (n_nbr - 1);
+            for (int task0 = 0; task0 < ntask; task0 += ngrp) {
+                const int task = task0 + grp;
+                long long sum = 0;
+                int side = 0, n = 1;
+                if (task < ntask) {
+                    side = task >= n_nbr - 1; n = 1 + (side ? task - (n_nbr - 1) : task);
+                    const int b0 = side ? X.bb : X.ba;
+                    const int o0 = loff[b0 * (n_nbr + 1) + n], o1 = loff[b0 * (n_nbr + 1) + n + 1];
+                    for (int k = o0 + gl; k < o1; k += 8) sum += v[side * J + lidx[k]];
+                }
+#pragma unroll
+                for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
+                if (task < ntask && gl == 0 && sum) {
+                    const uint32_t st = lf_site(jb, side ? X.kb : X.ka, nbt[(side ? X.bb : X.ba) * n_nbr + n]);
+                    atomicAdd(reinterpret_cast<unsigned long long *>(G + st), (unsigned long long)sum);
+                }
+            }
+            if (tid == 0) {                                // the two sites: every row flips except those with both
+                G[ia] = -G[ia] + 2 * X.C; G[ib] = -G[ib] + 2 * X.C;
+                sig[ia] = (int8_t)X.sb; sig[ib] = (int8_t)X.sa;
+            }
+        }
+        __syncthreads();
+    }
+    if (warp == 0) nnear = (int64_t)__reduce_add_sync(0xffffffffu, (unsigned)nnear);   // each lane counted its own steps
+    if (tid == 0) {
+        jb.E[r] = E0c + (double)dsum * fscale;
+        jb.E_min_rep[r] = fmin(Emin, E0c + (double)dmin * fscale);
+        jb.n_acc[r] += nacc;
+        if (jb.n_near) jb.n_near[r] += nnear;
+    }
+    if (jb.gf_smem)
+        for (int64_t i = tid; i < jb.N; i += nt) { gsig[i] = sig[i]; gfld[i] = G[i]; }
+    if (track)
+        for (int c = tid; c < n_cols; c += nt) jb.cv[(int64_t)r * n_cols + c] += dcv[c];
+}
+
 // Full energy on the sign-parity tables, bit-sliced.  The occupancies become bit planes: per replica, point-
 // function column with sign changes and basis site, one row of 2 * d2 bits per (k0, k1) holding the sign bit of
 // every k2 twice over, so that any offset in [0, d2) reads 32 consecutive bits with one funnel shift.  A thread
@@ -728,6 +1029,76 @@ __global__ void __launch_bounds__(256) ce_energy_bits_kernel(const uint32_t *__r
     __syncthreads();
     for (int c = threadIdx.x; c < n_cols; c += blockDim.x)
         if (ccnt[c]) atomicAdd(cv + (int64_t)r * n_cols + c, ccnt[c]);
+}
+
+// Local fields of every site of R configurations, bit-sliced like the full energy: a thread takes 32 consecutive
+// sites along k2 of one basis and, for every reverse row of that basis (every cluster instance containing the
+// site), XORs the members' shifted plane words (bit j: the parity of site j's product); odd parities are counted
+// per site in a vertical counter while the rows of one column go by, and the column adds 2 eci (rows - 2 odd) to
+// each site's field (fixed point, exact).
+__global__ void __launch_bounds__(128) ce_field_bits_kernel(const uint32_t *__restrict__ planes, int32_t P, int32_t d0, int32_t d1,
+                                                             int32_t d2, int32_t W2, int32_t nB, int64_t N,
+                                                             const uint32_t *__restrict__ frows, const int4 *__restrict__ fmem,
+                                                             const int32_t *__restrict__ frow_off, const int32_t *__restrict__ frow_n,
+                                                             const int64_t *__restrict__ efix, long long *__restrict__ field) {
+    const int b = blockIdx.y, r = blockIdx.z;
+    const int Wn = (d2 + 31) >> 5;
+    const int64_t items = (int64_t)d0 * d1 * Wn;
+    const int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= items) return;
+    const int w = (int)(it % Wn);
+    const int64_t kk = it / Wn;
+    const int k1 = (int)(kk % d1), k0 = (int)(kk / d1);
+    const int nv = min(32, d2 - 32 * w);
+    const uint32_t mask = nv >= 32 ? 0xffffffffu : ((1u << nv) - 1u);
+    const uint32_t *pr = planes + (int64_t)r * P * d0 * d1 * W2;
+    constexpr int NQ = 13;                                  // up to 8191 rows per column
+    uint32_t cnt[NQ];
+    long long acc[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) acc[j] = 0;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) cnt[q] = 0u;
+    int col = -1, nrows = 0;
+    auto flush = [&]() {
+        if (col < 0 || nrows == 0) return;
+        const long long e = (long long)__ldg(efix + col);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            int odd = 0;
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) odd |= (int)((cnt[q] >> j) & 1u) << q;
+            acc[j] += e * (long long)(nrows - 2 * odd);
+        }
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) cnt[q] = 0u;
+        nrows = 0;
+    };
+    const uint32_t *rows = frows + frow_off[b];
+    const int nr = frow_n[b];
+    for (int q = 0; q < nr; ++q) {
+        const uint32_t rd = __ldg(rows + q);
+        const int c = (int)(rd & 0xffu), nm = (int)((rd >> 8) & 0xfu), st = (int)(rd >> 12);
+        if (c != col) { flush(); col = c; }
+        uint32_t par = 0;
+        for (int m = 0; m < nm; ++m) {
+            const int4 e = __ldg(fmem + st + m);                  // (plane, uo0, uo1, uo2)
+            int a0 = k0 + e.y; a0 -= a0 >= d0 ? d0 : 0;
+            int a1 = k1 + e.z; a1 -= a1 >= d1 ? d1 : 0;
+            const int pos = 32 * w + e.w;
+            const uint32_t *row = pr + (((int64_t)e.x * d0 + a0) * d1 + a1) * W2 + (pos >> 5);
+            par ^= __funnelshift_r(__ldg(row), __ldg(row + 1), (unsigned)(pos & 31));
+        }
+        uint32_t carry = par & mask;
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) { const uint32_t tq = cnt[k] & carry; cnt[k] ^= carry; carry = tq; }
+        ++nrows;
+    }
+    flush();
+    long long *out = field + (int64_t)r * N + ((int64_t)(k0 * d1 + k1) * d2 + 32 * w) * nB + b;
+#pragma unroll
+    for (int j = 0; j < 32; ++j)
+        if (j < nv) out[(int64_t)j * nB] = acc[j];
 }
 
 // E[r] = zerolet + sum_c eci_c * cv[r, c], columns in order (one thread per configuration)
@@ -898,6 +1269,12 @@ struct nce_ce_model {
     uint32_t *brows = nullptr; int4 *bmem = nullptr; int32_t *brow_off = nullptr, *brow_n = nullptr;
     int32_t *plane_pfc = nullptr; int32_t n_planes = 0;
     double *ecol1 = nullptr;                 // eci of each column (full-energy kernel)
+    // local-field kernel: per basis the rows containing each neighbourhood entry, the displacement box, and every
+    // reverse row as (col | members << 8 | first member << 12) with its members (plane, uo0, uo1, uo2) for the fields
+    bool lf_ok = false;
+    int32_t *lf_off = nullptr; uint16_t *lf_idx = nullptr; int16_t *lf_box = nullptr;
+    int32_t lf_e[3] = {0, 0, 0}, lf_nidx = 0;
+    uint32_t *frows = nullptr; int4 *fmem = nullptr; int32_t *frow_off = nullptr, *frow_n = nullptr;
 
     int device = 0;
     std::mutex mu;
@@ -918,7 +1295,7 @@ static int upload(T *&dst, const T *src, size_t n) {
 static int free_model(nce_ce_model *m) {
     void *ptrs[] = {m->loc, m->pfc, m->eci64, m->eci32, m->rv_len, m->nb_b, m->nb_uo, m->pf64, m->pf32, m->act_b,
                     m->act_nb, m->grp_cum, m->T_b, m->T_uo, m->T_pfc, m->T_eci64, m->T_eci32, m->err, m->sbits, m->bix, m->rcol, m->ecol2_64, m->ecol2_32, m->ecol_fix, m->chunks, m->n_chunks, m->brows, m->bmem, m->brow_off, m->brow_n, m->plane_pfc, m->ecol1,
-                    m->staging_base};
+                    m->staging_base, m->lf_off, m->lf_idx, m->lf_box, m->frows, m->fmem, m->frow_off, m->frow_n};
     for (void *p : ptrs) if (p) cudaFree(p);
     delete m;
     return NCE_OK;
@@ -953,11 +1330,14 @@ static CEJob make_job(const nce_ce_model *m, const nce_pt_state *st, const nce_p
     if (st) {
         j.sigma = st->sigma; j.E = st->E; j.beta_slot = st->beta_slot; j.slot_of_rep = st->slot_of_rep;
         j.E_min_rep = st->E_min_rep; j.n_acc = st->n_acc; j.R = st->R; j.cv = st->cv; j.n_near = st->n_near;
+        j.field = st->field;
     }
     if (ck) {
         j.n_steps = ck->n_steps; j.step0 = ck->step0; j.step_dev = ck->step_dev; j.prop_a = ck->prop_a; j.prop_b = ck->prop_b; j.prop_u = ck->prop_u;
         j.seed = ck->seed; j.sample_interval = ck->sample_interval > 0 ? ck->sample_interval : 1;
         j.E_samples = ck->E_samples;
+        j.lf_off = m->lf_off; j.lf_idx = m->lf_idx; j.lf_box = m->lf_box;
+        j.lf_e0 = m->lf_e[0]; j.lf_e1 = m->lf_e[1]; j.lf_e2 = m->lf_e[2]; j.lf_nidx = m->lf_nidx;
         j.near_eV = ck->near_eV > 0.0 ? ck->near_eV : (p64 ? 1e-9 : 1e-6);
         if (j.fix_shift > 0) {
             const double nf = std::ldexp(j.near_eV, j.fix_shift);
@@ -1008,6 +1388,25 @@ static int launch_bin(const CEBatch &bt, int mo, int total, int warps, size_t sm
 #undef NCE_BIN_CASE
         default: return fail(NCE_ERR_UNSUPPORTED, "cluster order %d > 8", mo);
     }
+}
+
+static int launch_lf(const CEBatch &bt, int mo, int total, int warps, size_t smem, int32_t budget, cudaStream_t s) {
+    void (*kern)(CEBatch, int32_t) = nullptr;
+    switch (mo) {
+        case 1: kern = ce_lf_chunk_kernel<1>; break;
+        case 2: kern = ce_lf_chunk_kernel<2>; break;
+        case 3: kern = ce_lf_chunk_kernel<3>; break;
+        case 4: kern = ce_lf_chunk_kernel<4>; break;
+        case 5: kern = ce_lf_chunk_kernel<5>; break;
+        case 6: kern = ce_lf_chunk_kernel<6>; break;
+        case 7: kern = ce_lf_chunk_kernel<7>; break;
+        case 8: kern = ce_lf_chunk_kernel<8>; break;
+        default: return fail(NCE_ERR_UNSUPPORTED, "cluster order %d > 8", mo);
+    }
+    NCE_CUDA(::nce::raise_smem_limit((const void *)kern, smem));
+    kern<<<total, warps * 32, smem, s>>>(bt, budget);
+    NCE_CUDA(cudaGetLastError());
+    return NCE_OK;
 }
 
 template <typename Real>
@@ -1071,16 +1470,48 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
         NCE_CHECK(cks[j].path == path, "batch: all chunks must use the same path");
         all_bin = all_bin && hs[j]->binary;
     }
-    NCE_CHECK(path >= 0 && path <= 2, "chunk: path must be 0 (auto), 1 (general) or 2 (sign parity)");
-    NCE_CHECK(path < 2 || all_bin, "chunk: the sign-parity path needs point functions in {-1, +1}");
-    const bool use_bin = (path == 2) || (path == 0 && all_bin);
+    NCE_CHECK(path >= 0 && path <= 3, "chunk: path must be 0 (auto), 1 (general), 2 (sign parity) or 3 (local field)");
+    NCE_CHECK(path < 2 || all_bin, "chunk: the sign-parity and local-field paths need point functions in {-1, +1}");
+    // local field: every job has its tables and a field buffer, float64 (fixed-point) arithmetic
+    bool all_lf = precision == 64;
+    for (int j = 0; j < n_jobs; ++j) all_lf = all_lf && hs[j]->lf_ok && sts[j].field != nullptr;
+    if (path == 3) {
+        for (int j = 0; j < n_jobs; ++j) {
+            NCE_CHECK(hs[j]->lf_ok, "chunk: the local-field path is not available for this cell (aliasing neighbourhood "
+                                    "or tables too large)");
+            NCE_CHECK(sts[j].field, "chunk: the local-field path needs the state's field buffer (nce_ce_field_init)");
+        }
+        NCE_CHECK(precision == 64, "chunk: the local-field path computes in fixed point (precision 64)");
+    }
+    const bool use_lf = path == 3 || (path == 0 && all_lf);
+    const bool use_bin = !use_lf && ((path == 2) || (path == 0 && all_bin));
     for (int j = 0; j < n_jobs; ++j)
-        NCE_CHECK(!sts[j].cv || use_bin, "chunk: tracked cluster-vector sums need the sign-parity path");
+        NCE_CHECK(!sts[j].cv || use_bin || use_lf, "chunk: tracked cluster-vector sums need the sign-parity or local-field path");
     CEBatch bt; std::memset(&bt, 0, sizeof(bt));
     bt.n_jobs = n_jobs;
     size_t smem = 0; bool all_fit = true;
     int sig_smem = 0;
-    if (use_bin) {
+    int64_t lf_budget = 0;
+    if (use_lf) {
+        size_t t_on = 0, t_off = 0; int64_t maxN = 0;
+        for (int j = 0; j < n_jobs; ++j) {
+            const nce_ce_model *m = hs[j];
+            const int bsz = (2 * m->lf_e[0] + 1) * (2 * m->lf_e[1] + 1) * (2 * m->lf_e[2] + 1);
+            t_on = std::max(t_on, LfLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, m->n_cols, m->max_chunks, m->lf_nidx, bsz, 0, true).total);
+            t_off = std::max(t_off, LfLayout::make(m->nB, m->J, mo, m->n_nbr, m->n_pfc, m->n_cols, m->max_chunks, m->lf_nidx, bsz, 0, false).total);
+            maxN = std::max(maxN, m->N);
+        }
+        const size_t limit = 200 * 1024;
+        all_fit = t_on <= limit;
+        const size_t base = all_fit ? t_on : t_off;
+        // occupancy and field (9 bytes a site) in shared memory: the whole cell of one job when it fits, else a per-CTA
+        // budget that the jobs with small cells use
+        int64_t sites = n_jobs == 1 ? maxN : (int64_t)(48 * 1024) / 9;
+        sites = (sites + 15) / 16 * 16;
+        if (base + 9 * (size_t)sites + 64 > limit) sites = n_jobs == 1 ? 0 : (int64_t)((limit > base + 64 ? (limit - base - 64) / 9 : 0) / 16 * 16);
+        lf_budget = sites;
+        smem = sites > 0 ? LfLayout::make(0, 0, 0, 0, 0, 0, 0, 0, 0, sites, false).total + base : base;
+    } else if (use_bin) {
         const size_t accb = precision == 64 ? 8 : 4;
         size_t t_on = 0, t_off = 0; int64_t maxN = 0;
         for (int j = 0; j < n_jobs; ++j) {
@@ -1118,6 +1549,7 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
     for (int j = 0; j < n_jobs; ++j) {
         bt.job[j] = make_job(hs[j], &sts[j], &cks[j], base, use_bin);
         bt.job[j].sig_smem = (use_bin && sig_smem > 0 && hs[j]->N <= sig_smem) ? 1 : 0;
+        bt.job[j].gf_smem = (use_lf && lf_budget > 0 && hs[j]->N <= lf_budget) ? 1 : 0;
         base += sts[j].R;
     }
     int64_t max_steps = 0;
@@ -1132,7 +1564,9 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
             // every CTA of a cluster keeps its own copy of the occupancy: all jobs must fit the shared-memory budget
             for (int j = 0; j < n_jobs; ++j) if (!bt.job[j].sig_smem) CL = 1;
         }
-        if (use_bin)
+        if (use_lf)
+            rc = launch_lf(bt, mo, total, warps, smem, (int32_t)lf_budget, s);
+        else if (use_bin)
             rc = precision == 64 ? launch_bin<double>(bt, mo, total, warps, smem, sig_smem, s, CL)
                                  : launch_bin<float>(bt, mo, total, warps, smem, sig_smem, s, CL);
         else
@@ -1221,6 +1655,107 @@ using namespace nce;
 
 static int energy_impl(nce_ce_model *h, const int8_t *sigma, int32_t R, int32_t precision, double *E, int64_t *cv_out,
                        cudaStream_t s);
+
+// Tables of the local-field kernel (see ce_lf_chunk_kernel).  The path is enabled when the cell has no aliasing
+// (every neighbourhood entry of a site is a different site: their k-space displacements, taken as representatives in
+// (-d/2, d/2], differ), the lists fit 16-bit indices and the displacement box stays small; otherwise lf_ok stays
+// false and the sign-parity kernel runs.  sb: sign bit of (point-function column, species), 4 species per column.
+static int build_local_field_tables(nce_ce_model *m, const nce_ce_tables *t, const std::vector<uint8_t> &sb) {
+    const int nB = t->nB, J = t->J, mo = t->mo, n_nbr = t->n_nbr;
+    std::vector<char> real((size_t)t->n_pfc, 0);           // point-function columns that change sign
+    for (int c = 0; c < t->n_pfc; ++c)
+        for (int q = 0; q < 4; ++q) real[c] = real[c] || sb[(size_t)c * 4 + q] != 0;
+    // signed k-space offsets of the neighbourhood entries, extents of the box
+    const int64_t d[3] = {t->d[0], t->d[1], t->d[2]};
+    std::vector<int32_t> so((size_t)nB * n_nbr * 3);
+    int e[3] = {0, 0, 0};
+    for (size_t i = 0; i < (size_t)nB * n_nbr; ++i)
+        for (int c = 0; c < 3; ++c) {
+            int64_t x = t->nb_uo[3 * i + c];
+            if (x > d[c] / 2) x -= d[c];
+            so[3 * i + c] = (int32_t)x;
+            e[c] = std::max(e[c], (int)std::llabs(x));
+        }
+    // (the representatives lie in (-d/2, d/2]: a displacement names one neighbourhood entry at most, unless two
+    // entries are one site, which the table construction below refuses)
+    const int w0 = 2 * e[0] + 1, w1 = 2 * e[1] + 1, w2 = 2 * e[2] + 1;
+    const int64_t bsz = (int64_t)w0 * w1 * w2;
+    if ((int64_t)nB * bsz * nB > 65536) return NCE_OK;
+    std::vector<int16_t> box((size_t)(nB * bsz * nB), (int16_t)-1);
+    for (int a = 0; a < nB; ++a)
+        for (int n = 0; n < n_nbr; ++n) {
+            const int32_t *x = &so[((size_t)a * n_nbr + n) * 3];
+            const int64_t cell = ((int64_t)(x[0] + e[0]) * w1 + (x[1] + e[1])) * w2 + (x[2] + e[2]);
+            int16_t &slot = box[((size_t)a * bsz + cell) * nB + t->nb_b[(size_t)a * n_nbr + n]];
+            if (slot >= 0) return NCE_OK;                    // two entries at one site: aliasing
+            slot = (int16_t)n;
+        }
+    // per basis and neighbourhood entry n >= 1: the rows with n as a (sign-changing) member
+    std::vector<int32_t> off((size_t)nB * (n_nbr + 1), 0);
+    std::vector<uint16_t> idx;
+    for (int a = 0; a < nB; ++a) {
+        std::vector<std::vector<uint16_t>> lists((size_t)n_nbr);
+        for (int q = 0; q < t->Rv_len[a]; ++q) {
+            int seen = 0;
+            for (int k = 0; k < mo; ++k) {
+                const size_t i = ((size_t)a * J + q) * mo + k;
+                if (!real[t->Rv_pfc[i]]) continue;
+                const int n = t->Rv_loc[i];
+                for (int k2 = 0; k2 < k; ++k2) {                 // a member listed twice: not a plain cluster instance
+                    const size_t i2 = ((size_t)a * J + q) * mo + k2;
+                    if (real[t->Rv_pfc[i2]] && t->Rv_loc[i2] == n) return NCE_OK;
+                }
+                if (n > 0) lists[n].push_back((uint16_t)q);
+                seen += n == 0;
+            }
+            if (seen != 1) return NCE_OK;                        // the row must contain its site exactly once
+        }
+        for (int n = 0; n < n_nbr; ++n) {
+            off[(size_t)a * (n_nbr + 1) + n] = (int32_t)idx.size();
+            idx.insert(idx.end(), lists[n].begin(), lists[n].end());
+        }
+        off[(size_t)a * (n_nbr + 1) + n_nbr] = (int32_t)idx.size();
+    }
+    if (idx.size() >= 65536 || idx.empty()) return NCE_OK;
+    // every reverse row with its sign-changing members, for the field initialisation
+    std::vector<int32_t> pmap((size_t)t->n_pfc, -1); int np = 0;
+    for (int c = 0; c < t->n_pfc; ++c) if (real[c]) pmap[c] = np++;
+    std::vector<uint32_t> rows; std::vector<int4> mem; std::vector<int32_t> roff(nB), rn(nB);
+    for (int a = 0; a < nB; ++a) {
+        roff[a] = (int32_t)rows.size();
+        int last = -1, run = 0;
+        for (int q = 0; q < t->Rv_len[a]; ++q) {
+            const uint32_t start = (uint32_t)mem.size();
+            int nm = 0;
+            for (int k = 0; k < mo; ++k) {
+                const size_t i = ((size_t)a * J + q) * mo + k;
+                const int pl = pmap[t->Rv_pfc[i]];
+                if (pl < 0) continue;
+                const size_t nb = (size_t)a * n_nbr + t->Rv_loc[i];
+                mem.push_back(make_int4(pl * nB + t->nb_b[nb], t->nb_uo[3 * nb], t->nb_uo[3 * nb + 1], t->nb_uo[3 * nb + 2]));
+                ++nm;
+            }
+            const int col = t->Rv_col[(size_t)a * J + q];
+            run = col == last ? run + 1 : 1; last = col;
+            if (nm > 15 || start >= (1u << 20) || run > 8191) return NCE_OK;
+            rows.push_back((uint32_t)col | ((uint32_t)nm << 8) | (start << 12));
+        }
+        rn[a] = (int32_t)rows.size() - roff[a];
+    }
+    if (np != m->n_planes) return NCE_OK;                      // same planes as the full-energy kernel
+    int rc = upload(m->lf_off, off.data(), off.size());
+    if (!rc) rc = upload(m->lf_idx, idx.data(), idx.size());
+    if (!rc) rc = upload(m->lf_box, box.data(), box.size());
+    if (!rc) rc = upload(m->frows, rows.data(), rows.size());
+    if (!rc) rc = upload(m->fmem, mem.data(), mem.size());
+    if (!rc) rc = upload(m->frow_off, roff.data(), roff.size());
+    if (!rc) rc = upload(m->frow_n, rn.data(), rn.size());
+    if (rc) return rc;
+    for (int c = 0; c < 3; ++c) m->lf_e[c] = e[c];
+    m->lf_nidx = (int32_t)idx.size();
+    m->lf_ok = true;
+    return NCE_OK;
+}
 
 extern "C" {
 
@@ -1404,6 +1939,7 @@ int nce_ce_create(const nce_ce_tables *t, nce_ce_handle *out) {
                     m->n_planes = (int32_t)ppfc.size();
                 }
             }
+            if (!rc && bin && m->brows && m->fix_shift > 0) rc = build_local_field_tables(m, t, sb);
             m->binary = !rc;
         }
     }
@@ -1687,6 +2223,38 @@ int nce_ce_energy_noalloc(nce_ce_handle h, const int8_t *sigma, int32_t R, int32
                                                          partial);
     NCE_CUDA(cudaGetLastError());
     ce_energy_finish<<<(R + 127) / 128, 128, 0, s>>>(partial, (int32_t)nblk, R, h->zerolet, E);
+    NCE_CUDA(cudaGetLastError());
+    return NCE_OK;
+}
+
+int nce_ce_has_local_field(nce_ce_handle h, int32_t *ok, double *scale) {
+    NCE_CHECK(h && ok, "nce_ce_has_local_field: null argument");
+    *ok = h->lf_ok ? 1 : 0;
+    if (scale) *scale = h->fix_shift > 0 ? std::ldexp(1.0, -h->fix_shift) : 0.0;
+    return NCE_OK;
+}
+
+int nce_ce_field_init(nce_ce_handle h, const int8_t *sigma, int32_t R, int64_t *field, void *stream) {
+    NCE_CHECK(h && sigma && field && R >= 1, "nce_ce_field_init: bad argument");
+    NCE_CHECK(h->lf_ok, "nce_ce_field_init: the local-field path is not available for this cell");
+    NCE_CHECK(R <= 65535, "nce_ce_field_init: at most 65535 configurations per call");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t d0 = h->d[0], d1 = h->d[1], d2 = h->d[2];
+    NCE_CHECK(d2 < (1 << 28) && d0 * d1 < (1ll << 40), "nce_ce_field_init: lattice too large");
+    const int32_t W2 = (int32_t)((2 * d2 + 31) / 32 + 1);
+    const int32_t P = h->n_planes * h->nB;
+    StreamScratch planes;
+    NCE_CUDA(planes.alloc(sizeof(uint32_t) * (size_t)R * P * d0 * d1 * W2, s));
+    const int64_t prow = (int64_t)R * P * d0 * d1;
+    const int pb = (int)std::min<int64_t>((prow + 7) / 8, 1 << 20);
+    ce_bitplane_kernel<<<pb, 256, 0, s>>>(sigma, R, h->N, h->nB, d0 * d1, (int32_t)d2, W2, h->plane_pfc, h->n_planes, h->sbits,
+                                          (uint32_t *)planes.p);
+    NCE_CUDA(cudaGetLastError());
+    const int64_t items = d0 * d1 * ((d2 + 31) / 32);
+    ce_field_bits_kernel<<<dim3((unsigned)((items + 127) / 128), h->nB, R), 128, 0, s>>>(
+        (const uint32_t *)planes.p, P, (int32_t)d0, (int32_t)d1, (int32_t)d2, W2, h->nB, h->N, h->frows, h->fmem, h->frow_off,
+        h->frow_n, h->ecol_fix, (long long *)field);
     NCE_CUDA(cudaGetLastError());
     return NCE_OK;
 }

@@ -105,6 +105,7 @@ class PTState:
         self.n_acc = torch.zeros(R, dtype=torch.int64, device=device)
         self.n_ex = torch.zeros(1, dtype=torch.int64, device=device)
         self.n_near = torch.zeros(R, dtype=torch.int64, device=device)   # near-threshold steps (stated dE bound)
+        self.field = None                                                  # local fields (enable_field)
         self._min = torch.zeros(1, dtype=torch.float64, device=device)
         self._arg = torch.zeros(1, dtype=torch.int32, device=device)
         self.cv = None
@@ -113,6 +114,16 @@ class PTState:
         """Keep the replicas' cluster-vector sums (exact integers, sign-parity tables) current from now on; the
         carried energies can then be re-anchored exactly with ``reanchor_from_counts``."""
         self.cv = gce.cluster_counts(self.sigma)
+        return self
+
+    def enable_field(self, gce):
+        """Give the state its local fields (when the cell supports them): precision-64 chunks then run the local-field
+        kernel, which keeps them current.  Call again after changing ``sigma`` by hand."""
+        if gce.has_local_field:
+            import torch
+            if self.field is None or self.field.shape != self.sigma.shape:
+                self.field = torch.empty(self.sigma.shape, dtype=torch.int64, device=self.sigma.device)
+            gce.field_init(self.sigma, self.field)
         return self
 
     def reanchor_from_counts(self, gce):
@@ -128,6 +139,7 @@ class PTState:
         for f in ("sigma", "E", "beta_slot", "rep_of_slot", "slot_of_rep", "ladder_id", "E_min_rep", "n_acc", "n_ex", "n_near"):
             setattr(s, f, getattr(self, f).data_ptr())
         s.cv = self.cv.data_ptr() if self.cv is not None else None
+        s.field = self.field.data_ptr() if self.field is not None else None
         return s
 
     def minimum(self, stream=None):
@@ -160,8 +172,8 @@ def make_chunk(n_steps, step0, seed, precision=64, warps=0, proposals=None, samp
 
 def run_chunk(gce, st: PTState, n_steps, step0, seed, precision=64, warps=0, proposals=None, sample_interval=1,
               E_samples=None, do_exchange=False, ex_parity=0, ex_u=None, stream=None, path=0, cluster=1, near_eV=0.0):
-    """One chunk of the persistent kernel (+ chunk-end exchange) for one job.  path: 0 auto (sign parity when the
-    point functions are +-1), 1 general products, 2 sign parity.  ``st.n_near`` counts the steps whose Metropolis
+    """One chunk of the persistent kernel (+ chunk-end exchange) for one job.  path: 0 auto (local field when the state
+    has fields, else sign parity when the point functions are +-1), 1 general products, 2 sign parity, 3 local field.  ``st.n_near`` counts the steps whose Metropolis
     margin |dE + ln(u) / beta| is below ``near_eV`` (0: the precision form's stated dE bound)."""
     ck = make_chunk(n_steps, step0, seed, precision, warps, proposals, sample_interval, E_samples, do_exchange,
                     ex_parity, ex_u, path, cluster, near_eV)

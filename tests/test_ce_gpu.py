@@ -439,3 +439,136 @@ def test_batch_with_a_job_in_global_memory(cuda):
     torch.cuda.synchronize()
     for j in jobs:
         _compare(j["st"], j["ref"], 1e-9)
+
+
+# ── local-field kernel ───────────────────────────────────────────────────────────────────────────────
+
+def test_local_field_init_is_the_flip_energy(cuda):
+    """G(i) of nce_ce_field_init is minus the energy change of flipping site i alone (the oracle's float64 delta with
+    both sites of the swap at i), in fixed point: within 1e-12 eV for every site of two configurations."""
+    torch = cuda
+    gce, orc, sig_r, _ = _setup(5, seed=2, R=2)
+    assert gce.has_local_field
+    G = gce.field_init(torch.as_tensor(sig_r).cuda()).cpu().numpy().astype(np.float64) * gce.field_scale
+    for r in range(2):
+        for i in range(gce.n_atoms):
+            s = int(sig_r[r, i]); f = 1 - s
+            assert abs(-G[r, i] - orc.delta(sig_r[r], i, i, f, f)) < 1e-12
+
+
+@pytest.mark.parametrize("L", [2, 3])
+def test_local_field_refused_on_aliasing_cells(cuda, L):
+    """Cells so small that a site's neighbourhood wraps onto itself have no local-field path: path 3 is refused with
+    a message, path 0 falls back to the sign-parity kernel."""
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.pt import run_chunk
+    gce, orc, sig_r, beta = _setup(L, seed=1, R=2)
+    assert not gce.has_local_field
+    st = _engine_state(sig_r, np.array([orc.energy(x) for x in sig_r]), beta).enable_field(gce)
+    assert st.field is None
+    with pytest.raises(_lib.NceError, match="local-field"):
+        run_chunk(gce, st, 10, 0, 1, 64, 8, path=3)
+
+
+@pytest.mark.parametrize("warps", [4, 16, 32])
+def test_local_field_trajectory_host_stream(cuda, warps):
+    """Host proposal stream with exchanges, two chunks: the local-field kernel is bit-exact against the oracle
+    (occupancies, energies, acceptance, slot permutation, samples, near-threshold counts), and its fields equal a
+    fresh nce_ce_field_init of the final occupancies."""
+    torch = cuda
+    from neuralce_gb300.ce import proposal_stream
+    from neuralce_gb300.pt import run_chunk
+    from oracle.ce_oracle import new_state
+    R, T, si = 8, 1500, 50
+    gce, orc, sig_r, beta = _setup(8, seed=3, R=R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    st = _engine_state(sig_r, E0, beta).enable_field(gce)
+    ref = new_state(sig_r, E0, beta)
+    step = 0
+    for chunk in range(2):
+        pa, pb, pu = proposal_stream(gce, R, T, seed=10 + chunk)
+        exu = 1.0 - np.random.default_rng(50 + chunk).random(R // 2)
+        Es = torch.zeros((T // si, R), dtype=torch.float64, device="cuda")
+        dev = tuple(torch.as_tensor(x).cuda() for x in (pa, pb, pu))
+        run_chunk(gce, st, T, step, 0, 64, warps, dev, si, Es, True, chunk % 2, torch.as_tensor(exu).cuda(), path=3)
+        Es_ref = np.zeros((T // si, R))
+        orc.run(ref, T, step, 0, (pa, pb, pu), si, Es_ref, True, chunk % 2, exu, n_threads=4, near_eV=1e-9)
+        torch.cuda.synchronize()
+        _compare(st, ref, 1e-9)
+        assert np.abs(Es.cpu().numpy() - Es_ref).max() < 1e-9
+        step += T
+    assert torch.equal(st.field, gce.field_init(st.sigma))
+    assert int(st.n_acc.sum()) > 0
+
+
+def test_local_field_philox_equals_sign_parity(cuda):
+    """Device Philox stream, three chunks with exchanges, 16 replicas: the local-field kernel and the sign-parity
+    kernel give the same trajectory (and both the oracle's)."""
+    torch = cuda
+    from neuralce_gb300.pt import run_chunk
+    from oracle.ce_oracle import new_state
+    R, T = 16, 1000
+    gce, orc, sig_r, beta = _setup(5, seed=5, R=R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    a = _engine_state(sig_r, E0, beta).enable_field(gce); b = _engine_state(sig_r, E0, beta); ref = new_state(sig_r, E0, beta)
+    for c in range(3):
+        Ea = torch.zeros((T // 100, R), dtype=torch.float64, device="cuda"); Eb = torch.zeros_like(Ea)
+        run_chunk(gce, a, T, c * T, 1234, 64, 8, None, 100, Ea, True, path=3)
+        run_chunk(gce, b, T, c * T, 1234, 64, 8, None, 100, Eb, True, path=2)
+        orc.run(ref, T, c * T, 1234, None, 100, None, True, n_threads=4, near_eV=1e-9)
+        torch.cuda.synchronize()
+        assert torch.equal(a.sigma, b.sigma) and torch.equal(a.E, b.E) and torch.equal(Ea, Eb)
+        assert torch.equal(a.n_acc, b.n_acc) and torch.equal(a.rep_of_slot, b.rep_of_slot)
+        assert torch.equal(a.E_min_rep, b.E_min_rep) and torch.equal(a.n_near, b.n_near)
+        _compare(a, ref, 1e-9)
+    assert torch.equal(a.field, gce.field_init(a.sigma))
+
+
+def test_local_field_in_global_memory_and_batch(cuda):
+    """Fields and occupancies in global memory (a 24^3 cell in a batch beside small ones, whose fields fit the
+    shared-memory budget), with tracked cluster-vector sums: every job bit-exact against the oracle, fields equal a
+    fresh initialisation, tracked sums equal a recount."""
+    torch = cuda
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.ce import proposal_stream
+    from neuralce_gb300.pt import make_chunk
+    from oracle.ce_oracle import new_state
+    T = 400
+    jobs = []
+    for k, (L, R) in enumerate([(5, 3), (24, 4), (6, 2)]):
+        gce, orc, sig_r, beta = _setup(L, seed=110 + k, R=R)
+        E0 = gce.batched_energy(torch.as_tensor(sig_r).cuda()).cpu().numpy()
+        pa, pb, pu = proposal_stream(gce, R, T, seed=120 + k)
+        st = _engine_state(sig_r, E0, beta).enable_field(gce).track_counts(gce)
+        jobs.append(dict(gce=gce, orc=orc, st=st, ref=new_state(sig_r, E0, beta), props=(pa, pb, pu),
+                         dev=tuple(torch.as_tensor(x).cuda() for x in (pa, pb, pu))))
+    hs = (C.c_void_p * 3)(*[j["gce"].handle.value for j in jobs])
+    ss = (_lib.NcePtState * 3)(*[j["st"].struct() for j in jobs])
+    cks = (_lib.NcePtChunk * 3)(*[make_chunk(T, 0, 0, 64, 8, j["dev"], 1, None, True, path=3) for j in jobs])
+    _lib.check(_lib.lib().nce_ce_run_batch(3, hs, ss, cks, _lib.stream_ptr()), "batch")
+    for j in jobs:
+        j["orc"].run(j["ref"], T, 0, 0, j["props"], 1, None, True, n_threads=4, near_eV=1e-9)
+    torch.cuda.synchronize()
+    for j in jobs:
+        _compare(j["st"], j["ref"], 1e-9)
+        assert torch.equal(j["st"].field, j["gce"].field_init(j["st"].sigma))
+        assert torch.equal(j["st"].cv, j["gce"].cluster_counts(j["st"].sigma))
+
+
+def test_local_field_large_cell_single_job(cuda):
+    """One 36^3 cell (186,624 sites: occupancy and fields in global memory), host stream with an exchange: bit-exact
+    against the oracle."""
+    torch = cuda
+    from neuralce_gb300.ce import proposal_stream
+    from neuralce_gb300.pt import run_chunk
+    from oracle.ce_oracle import new_state
+    R, T = 4, 400
+    gce, orc, sig_r, beta = _setup(36, seed=19, R=R)
+    E0 = gce.batched_energy(torch.as_tensor(sig_r).cuda()).cpu().numpy()
+    st = _engine_state(sig_r, E0, beta).enable_field(gce); ref = new_state(sig_r, E0, beta)
+    pa, pb, pu = proposal_stream(gce, R, T, seed=71)
+    run_chunk(gce, st, T, 0, 0, 64, 16, tuple(torch.as_tensor(x).cuda() for x in (pa, pb, pu)), 1, None, True, path=3)
+    orc.run(ref, T, 0, 0, (pa, pb, pu), 1, None, True, n_threads=4, near_eV=1e-9)
+    torch.cuda.synchronize()
+    _compare(st, ref, 1e-9)
+    assert torch.equal(st.field, gce.field_init(st.sigma))

@@ -395,10 +395,14 @@ def test_config_cell_chain_matches_oracle(cuda, mma, width):
     assert err < 1e-4, err
     assert np.array_equal(st.sigma[0].cpu().numpy(), sig_ref.astype(np.int8))
     Ecar = float(st.E[0].item())
-    assert abs(Ecar - (E0 + dsum)) * m.scale_eV < 1e-3           # 2,048-site sum of float32 site energies
+    E0g = float(NCEState(m, m.sig0[None].astype(np.int8), np.ones(1)).full_cache().E[0].item())
+    # energies of the whole cell: float32 site energies summed over 2,048 sites (the bound scales with N, as above)
+    assert abs(E0g - E0) * m.scale_eV < 1e-4 * m.N / 64
+    assert abs(Ecar - (E0g + float(dE.sum().item()))) * m.scale_eV < 1e-9
     st2 = NCEState(m, st.sigma.cpu().numpy(), np.ones(1)).full_cache()
     torch.cuda.synchronize()
     assert abs(Ecar - float(st2.E[0].item())) * m.scale_eV < 1e-3
+    assert abs(float(st2.E[0].item()) - (E0 + dsum)) * m.scale_eV < 1e-4 * m.N / 64
     assert np.abs(st2.e[0].cpu().numpy() - cache["e"]).max() < 1e-4
 
 

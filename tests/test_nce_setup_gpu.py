@@ -32,7 +32,7 @@ def test_setup_local_delta_commit_chain(cuda, nipt_model):
     assert abs(e_i - orc.energy_of(ocache)) * to_eV < 1e-4
     rng = np.random.default_rng(0)
     worst_full = worst_orc = 0.0; n = 0
-    for _ in range(40):
+    for _ in range(200):
         i, j = (int(x) for x in rng.choice(N, 2, replace=False))
         if sig[i] == sig[j]:
             continue
