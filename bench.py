@@ -39,6 +39,9 @@ CONTRACTIONS = ["fp32 CUDA cores", "bf16 mma.sync tensor cores (fp32 accumulatio
                 "split-bf16 tcgen05 tensor cores"]
 H100_PUBLISHED = 1_231_993.0          # reference CE PT, 2,048 sites, R=32, H100 (results/bench_stage/gpu_icet_*H100*.json)
 B_GATHER = 14_996                     # bytes of member occupancy per attempt, config-0 cluster set
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of the headline chunk,
+# keyed by (path, L, R, steps per chunk): profiles/ holds the captures
+TRAFFIC = {(2, 8, 32, 5000): 155_392}
 
 
 def parse():
@@ -646,14 +649,18 @@ def main():
         from neuralce_gb300.autotune import best_launch
         ws = (args.warps,) if args.warps else (4, 8, 16, 32)
         cls = (args.cluster,) if args.cluster else ((1, 2, 4, 8, 16) if args.path != 1 else (1,))
-        paths = (2,) if args.path == 0 else (args.path,)
+        paths = (2, 3) if args.path == 0 else (args.path,)
         (args.warps, args.cluster, args.path), t = best_launch(gce, st, args.precision, args.path, ws, cls, paths=paths)
         tuned = {f"{w}x{c}/p{p}": round(v, 3) for (w, c, p), v in t.items()}
+    if args.path == 3:
+        st.enable_field(gce)                               # local fields of the replicas' occupancies
+    si = 100                                               # energy samples every 100 steps (the CLI default)
+    Es = torch.zeros((T // si, R), dtype=torch.float64, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
     step = 0
     for _ in range(args.warmup):
-        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, 1, None, True, path=args.path,
+        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, si, Es, True, path=args.path,
                   cluster=args.cluster); step += T
     torch.cuda.synchronize()
     clk = Clocks(local); clk.start()
@@ -664,7 +671,7 @@ def main():
     for k in range(args.steps):
         flush.zero_()
         ev[k][0].record(stream)
-        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, 1, None, True, path=args.path,
+        run_chunk(gce, st, T, step, 42 + rank, args.precision, args.warps, None, si, Es, True, path=args.path,
                   cluster=args.cluster)
         ev[k][1].record(stream)
         step += T
@@ -687,9 +694,9 @@ def main():
         h_sig = pin(st.sigma.cpu().numpy()); h_E = pin(st.E.cpu().numpy()); h_b = pin(beta)
         h_ros = pin(st.rep_of_slot.cpu().numpy()); h_sor = pin(st.slot_of_rep.cpu().numpy()); h_lid = pin(np.zeros(R, np.int32))
         h_emr = pin(st.E_min_rep.cpu().numpy()); h_nacc = pin(st.n_acc.cpu().numpy()); h_nex = pin(st.n_ex.cpu().numpy())
-        h_samp = pin(np.zeros((1, R)))
+        h_samp = pin(np.zeros((T // si, R)))
         torch.cuda.synchronize()
-        ck = make_chunk(T, step, 42 + rank, args.precision, args.warps, None, T, None, True, path=args.path, cluster=args.cluster)
+        ck = make_chunk(T, step, 42 + rank, args.precision, args.warps, None, si, None, True, path=args.path, cluster=args.cluster)
         def host_call():
             _lib.check(_lib.lib().nce_ce_run_chunk_host(gce.handle, R, h_sig.data_ptr(), h_E.data_ptr(), h_b.data_ptr(),
                                                         h_ros.data_ptr(), h_sor.data_ptr(), h_lid.data_ptr(), h_emr.data_ptr(),
@@ -701,7 +708,7 @@ def main():
             host_call(); ck.step0 += T
         e2e_s = time.perf_counter() - t0
         h2d = R * gce.n_atoms + R * (8 + 4 + 4 + 4 + 4 + 8 + 8) + 8
-        d2h = R * gce.n_atoms + R * (8 + 4 + 4 + 8 + 8) + 8 + 8 * R
+        d2h = R * gce.n_atoms + R * (8 + 4 + 4 + 8 + 8) + 8 + 8 * R * (T // si)
         e2e = {"value": R * T * args.steps * world / e2e_s, "unit": "swap attempts/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "api": "nce_ce_run_chunk_host"}
     hbm, src = peaks()
@@ -710,9 +717,9 @@ def main():
     # DRAM bytes per launch from one ncu capture of this workload (dram__bytes_read.sum + dram__bytes_write.sum of
     # ce_bin_chunk_kernel, 2,048 sites, R = 32, 5,000 steps, 16 warps x 8 CTAs): the tables and occupancies live in
     # shared memory
-    traffic = 155_392 if (args.L == 8 and args.R == 32 and T == 5000 and args.path == 2) else None
+    traffic = TRAFFIC.get((args.path, args.L, args.R, T))
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-            "kernel": {1: "ce_pt_chunk_kernel"}.get(args.path, "ce_bin_chunk_kernel"),
+            "kernel": {1: "ce_pt_chunk_kernel", 3: "ce_lf_chunk_kernel"}.get(args.path, "ce_bin_chunk_kernel"),
             "peak_source": src,
             "algorithmic_bytes_per_launch": R * T * B_GATHER}
     nce_line = nce_tc_line = nce_bf16_line = nce_shipped_line = None
@@ -739,9 +746,11 @@ def main():
                 "config": workload_config(args, gce), "clocks": clocks, "e2e": e2e, "gpu_launches": 2 * args.steps,
                 "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "nce_tcgen05_split": nce_tc_line, "nce_tcgen05_bf16": nce_bf16_line, "nce_shipped_model": nce_shipped_line, "batch": batch_line, "serve": serve_line,
                 "launch": {"warps_per_cta": args.warps, "ctas_per_replica": args.cluster,
-                           "path": ["auto", "general", "sign-parity"][args.path],
+                           "path": ["auto", "general", "sign-parity", "local-field"][args.path],
                            "autotune_ms": tuned},
-                "accept_rate": float(st.n_acc.sum().item()) / max(1, R * step)}
+                "accept_rate": float(st.n_acc.sum().item()) / max(1, R * step),
+                "near_threshold_steps": {"count": int(st.n_near.sum().item()), "of_attempts": R * step,
+                                         "band_eV": 1e-9 if args.precision == 64 else 1e-6}}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

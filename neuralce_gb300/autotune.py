@@ -1,4 +1,5 @@
-"""Launch-shape autotuner of the CE chunk kernel: warps per CTA and CTAs per replica (thread-block cluster).
+"""Launch-shape autotuner of the CE chunk kernels: warps per CTA, CTAs per replica (thread-block cluster) and,
+optionally, the kernel (sign parity or local field).
 
 Per-step latency, not throughput, bounds a Markov chain, and the best shape depends on the number of rows per
 site, the replica count relative to the 152 SMs and the precision: with few replicas, spreading each replica
@@ -24,11 +25,17 @@ def best_launch(gce, st, precision=64, path=0, warps=(2, 4, 8, 16, 32), clusters
         timings = {}
         for p in paths:
             _, t = best_launch(gce, st, precision, p, warps, clusters, steps, seed)
-            timings.update({k + (p,): v for k, v in t.items()})
+            timings.update({k + (p,): v for k, v in t.items()})    # (a path that cannot run adds nothing)
         best = min(timings, key=timings.get)
         _cache[key] = (best, timings)
         return best, timings
     scratch = PTState(st.sigma.cpu().numpy(), st.E.cpu().numpy(), st.beta_slot.cpu().numpy(), st.ladder_id.cpu().numpy())
+    if path == 3:
+        if not gce.has_local_field or precision != 64:
+            _cache[key] = (None, {})
+            return _cache[key]
+        scratch.enable_field(gce)
+        clusters = (1,)                                   # one CTA per replica: the decider warp is the chain
     timings = {}
     for cl in clusters:
         for w in warps:

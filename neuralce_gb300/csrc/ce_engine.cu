@@ -1655,6 +1655,7 @@ using namespace nce;
 
 static int energy_impl(nce_ce_model *h, const int8_t *sigma, int32_t R, int32_t precision, double *E, int64_t *cv_out,
                        cudaStream_t s);
+static int field_init_impl(nce_ce_model *h, const int8_t *sigma, int32_t R, int64_t *field, cudaStream_t s);
 
 // Tables of the local-field kernel (see ce_lf_chunk_kernel).  The path is enabled when the cell has no aliasing
 // (every neighbourhood entry of a site is a different site: their k-space displacements, taken as representatives in
@@ -2095,12 +2096,15 @@ int nce_ce_run_chunk_host(nce_ce_handle h, int32_t R, int8_t *sigma_host, double
     const bool props = ckh->prop_a != nullptr;
     const int64_t nsamp = (E_samples_host && ckh->sample_interval > 0) ? T / ckh->sample_interval : 0;
     const int64_t nexu = ckh->ex_u ? (R - 1 + 1) / 2 : 0;
+    // the local-field path keeps per-site fields on the device; here they are rebuilt from the uploaded occupancies
+    const bool lf = h->lf_ok && ckh->precision == 64 && (ckh->path == 3 || ckh->path == 0);
     auto al = [](size_t x) { return (x + 255) / 256 * 256; };
     size_t off[16]; size_t o = 0; int k = 0;
     const size_t sizes[] = {(size_t)R * N, sizeof(double) * R, sizeof(float) * R, sizeof(int32_t) * R, sizeof(int32_t) * R,
                             sizeof(int32_t) * R, sizeof(double) * R, sizeof(int64_t) * R, sizeof(int64_t),
                             props ? sizeof(int32_t) * T * R : 0, props ? sizeof(int32_t) * T * R : 0,
-                            props ? sizeof(double) * T * R : 0, sizeof(double) * nsamp * R, sizeof(double) * nexu};
+                            props ? sizeof(double) * T * R : 0, sizeof(double) * nsamp * R, sizeof(double) * nexu,
+                            lf ? sizeof(int64_t) * R * N : 0};
     for (size_t sz : sizes) { off[k++] = o; o = al(o + sz); }
     if (o > h->staging_bytes) {
         if (h->staging_base) cudaFree(h->staging_base);
@@ -2134,6 +2138,12 @@ int nce_ce_run_chunk_host(nce_ce_handle h, int32_t R, int8_t *sigma_host, double
     if (nexu) {
         ck.ex_u = (double *)(b + off[13]);
         NCE_CUDA(cudaMemcpyAsync((void *)ck.ex_u, ckh->ex_u, sizeof(double) * nexu, cudaMemcpyHostToDevice, s));
+    }
+    if (lf) {
+        st.field = (int64_t *)(b + off[14]);
+        if (R > 65535) return fail(NCE_ERR_INVALID, "nce_ce_run_chunk_host: at most 65535 replicas on the local-field path");
+        rc = field_init_impl(h, st.sigma, R, st.field, s);
+        if (rc) return rc;
     }
     rc = run_batch(1, &h, &st, &ck, s);
     if (rc) return rc;
@@ -2236,10 +2246,15 @@ int nce_ce_has_local_field(nce_ce_handle h, int32_t *ok, double *scale) {
 
 int nce_ce_field_init(nce_ce_handle h, const int8_t *sigma, int32_t R, int64_t *field, void *stream) {
     NCE_CHECK(h && sigma && field && R >= 1, "nce_ce_field_init: bad argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    return field_init_impl(h, sigma, R, field, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+static int field_init_impl(nce_ce_model *h, const int8_t *sigma, int32_t R, int64_t *field, cudaStream_t s) {
     NCE_CHECK(h->lf_ok, "nce_ce_field_init: the local-field path is not available for this cell");
     NCE_CHECK(R <= 65535, "nce_ce_field_init: at most 65535 configurations per call");
-    std::lock_guard<std::mutex> lk(h->mu);
-    cudaStream_t s = (cudaStream_t)stream;
     const int64_t d0 = h->d[0], d1 = h->d[1], d2 = h->d[2];
     NCE_CHECK(d2 < (1 << 28) && d0 * d1 < (1ll << 40), "nce_ce_field_init: lattice too large");
     const int32_t W2 = (int32_t)((2 * d2 + 31) / 32 + 1);
@@ -2258,6 +2273,8 @@ int nce_ce_field_init(nce_ce_handle h, const int8_t *sigma, int32_t R, int64_t *
     NCE_CUDA(cudaGetLastError());
     return NCE_OK;
 }
+
+extern "C" {
 
 int nce_ce_errors(nce_ce_handle h, int32_t *flags) {
     NCE_CHECK(h && flags, "nce_ce_errors: null argument");
