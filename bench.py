@@ -65,6 +65,7 @@ def parse():
     ap.add_argument("--nce-steps", type=int, default=3, help="chunks of the NeuralCE side measurement (0 = skip)")
     ap.add_argument("--nce-chunk", type=int, default=1000, help="MC steps per NeuralCE chunk")
     ap.add_argument("--nce-width", type=int, default=64, help="layer width of the --workload nce network")
+    ap.add_argument("--large-steps", type=int, default=2, help="chunks of each configuration-3 side measurement (0 = skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -427,11 +428,12 @@ def bench_serve(seconds=10.0, rate=50.0, ce_scale=0.01, nce_scale=0.0002, nce_ma
             "rounds": {"ce": st["rounds_ce"], "nce": st["rounds_nce"]}, "setup_s": setup}
 
 
-def bench_large(L=136, R=256, chunk=5000, steps=3, warmup=1, precision=32, seed=0):
+def bench_large(L=136, R=256, chunk=5000, steps=3, warmup=1, precision=64, seed=0, path=0):
     """Configuration 3 (CE part): fcc L^3 conventional cell (L = 136: 10,061,824 sites), 50/50, R temperatures
-    300-1400 K; float32 dE, float64 exchange and carried energies re-anchored exactly from the tracked
-    cluster-vector sums after every chunk.  Occupancies are drawn on the device (one seeded permutation per
-    replica).  A step is one chunk of ``chunk`` MC steps per replica + exchange + re-anchor."""
+    300-1400 K; dE in the float64 kernels' exact fixed point (the local-field kernel when the tuner picks it, fields
+    in global memory), float64 exchange, and carried energies re-anchored exactly from the tracked cluster-vector
+    sums after every chunk.  Occupancies are drawn on the device (one seeded permutation per replica).  A step is one
+    chunk of ``chunk`` MC steps per replica + exchange + re-anchor."""
     import torch
     from neuralce_gb300.autotune import best_launch
     from neuralce_gb300.pt import PTState, run_chunk
@@ -450,16 +452,23 @@ def bench_large(L=136, R=256, chunk=5000, steps=3, warmup=1, precision=32, seed=
     st.sigma, st.N = sig, N
     st.E = gce.batched_energy(sig)
     st.E_min_rep = torch.full((R,), float("inf"), dtype=torch.float64, device="cuda"); st.E_min_rep[0] = st.E[0]
+    st.n_near = torch.zeros(R, dtype=torch.int64, device="cuda")
     st.track_counts(gce)
     torch.cuda.synchronize()
     setup = time.time() - t0
-    (w, cl), tune = best_launch(gce, st, precision, 0, (8, 16, 32), (1,), steps=200)
+    paths = (2, 3) if path == 0 and precision == 64 else ((2,) if path == 0 else (path,))
+    (w, cl, path), tune = best_launch(gce, st, precision, 0, (8, 16, 32), (1,), steps=200, paths=paths)
+    field_ms = None
+    if path == 3:
+        a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a_.record(); st.enable_field(gce); b_.record(); torch.cuda.synchronize()
+        field_ms = a_.elapsed_time(b_)
     step = 0
     from neuralce_gb300 import _lib
 
     def one():
         nonlocal step
-        run_chunk(gce, st, chunk, step, 77, precision, w, None, 1, None, True, path=0)
+        run_chunk(gce, st, chunk, step, 77, precision, w, None, 1, None, True, path=path)
         _lib.check(_lib.lib().nce_ce_energy_from_counts(gce.handle, st.cv.data_ptr(), R, st.E.data_ptr(), _lib.stream_ptr()),
                    "nce_ce_energy_from_counts")             # exact float64 re-anchor, in place
         step += chunk
@@ -473,28 +482,39 @@ def bench_large(L=136, R=256, chunk=5000, steps=3, warmup=1, precision=32, seed=
     torch.cuda.synchronize()
     ms = [a.elapsed_time(b) for a, b in ev]
     tot = sum(ms) / 1e3
-    # exactness: tracked sums vs a recount, re-anchored energies vs a float64 full recompute
+    value = R * chunk * steps / tot
+    # exactness: tracked sums vs a recount, re-anchored energies vs a float64 full recompute, fields vs a rebuild
     cv_ok = bool(torch.equal(st.cv, gce.cluster_counts(st.sigma)))
     Ef = gce.batched_energy(st.sigma)
+    field_ok = bool(torch.equal(st.field, gce.field_init(st.sigma))) if path == 3 else None
     torch.cuda.synchronize()
     a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a_.record(); gce.batched_energy(st.sigma); b_.record(); torch.cuda.synchronize()
-    return {"value": R * chunk * steps / tot, "unit": "swap attempts/s", "ms_per_step": float(np.mean(ms)),
-            "config": f"CE large cell: fcc {L}^3 conventional ({N} sites), R={R} 300-1400 K, fp{precision} dE, chunk {chunk} "
-                      f"steps + fp64 exchange + exact fp64 re-anchor from cluster-vector sums",
-            "sites": N, "replicas": R, "state_bytes": R * N, "warps_per_replica": w, "autotune_ms": {str(k): v for k, v in tune.items()},
-            "tracked_sums_equal_recount": cv_ok, "max_E_vs_full_recompute_eV": float((Ef - st.E).abs().max().item()),
+    hbm, src = peaks()
+    achieved = value * B_GATHER / 1e9
+    return {"value": value, "unit": "swap attempts/s", "ms_per_step": float(np.mean(ms)),
+            "config": f"CE large cell: fcc {L}^3 conventional ({N} sites), R={R} 300-1400 K, "
+                      f"{'local-field' if path == 3 else 'sign-parity'} kernel, fp{precision} (exact fixed point) dE, "
+                      f"chunk {chunk} steps + fp64 exchange + exact fp64 re-anchor from cluster-vector sums",
+            "sites": N, "replicas": R, "state_bytes": R * N * (9 if path == 3 else 1), "warps_per_replica": w,
+            "path": {2: "sign-parity", 3: "local-field"}[path], "autotune_ms": {str(k): round(v, 3) for k, v in tune.items()},
+            "tracked_sums_equal_recount": cv_ok, "fields_equal_rebuild": field_ok,
+            "max_E_vs_full_recompute_eV": float((Ef - st.E).abs().max().item()), "field_init_ms": field_ms,
             "full_energy_ms": a_.elapsed_time(b_), "full_energy_site_replicas_per_s": R * N / (a_.elapsed_time(b_) / 1e3),
-            "accept_rate": float(st.n_acc.sum().item()) / (R * step), "setup_s": setup, "tables_s": setup_tables,
-            "vs_h100_published_4344547": R * chunk * steps / tot / 4_344_547}
+            "accept_rate": float(st.n_acc.sum().item()) / (R * step),
+            "near_threshold_steps": int(st.n_near.sum().item()),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "peak_source": src, "bytes_per_attempt": B_GATHER},
+            "setup_s": setup, "tables_s": setup_tables, "vs_h100_published_4344547": value / 4_344_547}
 
 
-def bench_nce_large(L=64, R=64, width=128, depth=3, chunk=100, steps=3, warmup=1, mma=2, seed=0, cluster=0):
+def bench_nce_large(L=64, R=64, width=128, depth=3, chunk=100, steps=3, warmup=1, mma=4, seed=0, cluster=0):
     """Configuration 3 (NeuralCE part): fcc L^3 conventional cell (L = 64: 1,048,576 sites), R replicas 300-1400 K,
-    the configuration-1 architecture widened to ``width``; layer contractions in bf16 on the tcgen05 tensor cores
-    with float32 accumulation in tensor memory (``mma`` 2; 1 = the same on mma.sync, 3 / 4 = split bf16 on mma.sync /
-    tcgen05, 0 = float32 CUDA cores).  Occupancies drawn on the device.  A step is
-    one chunk of ``chunk`` MC steps per replica + one exchange round; the full caches are built once (timed
+    the configuration-1 architecture widened to ``width``; layer contractions as split bf16 on the tcgen05 tensor
+    cores with float32 accumulation in tensor memory (``mma`` 4, the precision form: per-swap dE within 1e-4 eV of the
+    float64 oracle, tests/test_nce_gpu.py::test_config_cell_chain_matches_oracle); 2 = plain bf16 (stated bound
+    1e-2 eV), 1 / 3 = bf16 / split bf16 on mma.sync, 0 = float32 CUDA cores.  Occupancies drawn on the device.  A step
+    is one chunk of ``chunk`` MC steps per replica + one exchange round; the full caches are built once (timed
     separately)."""
     import torch
     from neuralce_gb300.nce import NCEModel, NCEState, synthetic_model
@@ -541,7 +561,14 @@ def bench_nce_large(L=64, R=64, width=128, depth=3, chunk=100, steps=3, warmup=1
     tot = sum(ms) / 1e3
     E_car = st.E.clone(); st.full_cache(); torch.cuda.synchronize()
     drift = float((st.E - E_car).abs().max().item())
-    return {"value": R * chunk * steps / tot, "unit": "swap attempts/s", "ms_per_step": float(np.mean(ms)),
+    value = R * chunk * steps / tot
+    flops = nce_flops_per_attempt(m)
+    pk, psrc = bf16_peak()
+    return {"value": value, "unit": "swap attempts/s", "ms_per_step": float(np.mean(ms)),
+            "roofline": {"bound": "tensor", "achieved": value * flops / 1e12, "peak": pk, "unit": "TFLOP/s",
+                         "frac": value * flops / 1e12 / pk, "peak_source": psrc, "flops_per_attempt": flops},
+            "dE_error_bound_eV": 1e-4 if mma in (0, 3, 4) else 1e-2,
+            "near_threshold_steps": int(st.n_near.sum().item()),
             "config": f"NeuralCE large cell: fcc {L}^3 conventional ({N} sites), R={R}, depth {depth}, width {width}, SiLU, sum, "
                       f"{CONTRACTIONS[mma]}, "
                       f"chunk {chunk} steps + 1 exchange round",
@@ -602,11 +629,11 @@ def main():
         from neuralce_gb300 import _lib
         _lib.lib()
         st_, wu_ = (args.steps if args.steps != 40 else 3), max(1, min(args.warmup, 2))
-        r = bench_nce_large(steps=st_, warmup=wu_, mma=(2 if args.nce_mma < 0 else args.nce_mma))
+        r = bench_nce_large(steps=st_, warmup=wu_, mma=(4 if args.nce_mma < 0 else args.nce_mma))
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": r["value"], "unit": "swap attempts/s", "n_gpus": world, "steps": st_,
                               "warmup": wu_, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-                              "vs_baseline": None, "dtype": "bf16" if args.nce_mma in (-1, 1, 2) else "f32", "data": "synthetic",
+                              "vs_baseline": None, "dtype": "bf16" if args.nce_mma in (-1, 1, 2, 3, 4) else "f32", "data": "synthetic",
                               "config": {"workload": r["config"]}, "large": r}), flush=True)
         return
     if args.workload == "serve":
@@ -728,6 +755,12 @@ def main():
         nce_tc_line = bench_nce(steps=args.nce_steps, mma=4)
         nce_bf16_line = bench_nce(steps=args.nce_steps, mma=2)
         nce_shipped_line = bench_nce(steps=args.nce_steps, shipped=True)
+    large_ce_line = large_nce_line = None
+    if rank == 0 and args.large_steps > 0:
+        large_ce_line = bench_large(steps=args.large_steps, warmup=1)
+        torch.cuda.empty_cache()
+        large_nce_line = bench_nce_large(steps=args.large_steps, warmup=1)
+        torch.cuda.empty_cache()
     batch_line = None
     if rank == 0 and args.batch_steps > 0:
         batch_line = bench_batch(steps=args.batch_steps)
@@ -745,6 +778,7 @@ def main():
                 "dtype": "f64" if args.precision == 64 else "f32", "data": "synthetic (seeded lattice, random-normal ECIs)",
                 "config": workload_config(args, gce), "clocks": clocks, "e2e": e2e, "gpu_launches": 2 * args.steps,
                 "roofline": roof, "cpu_baseline": cpu, "nce": nce_line, "nce_tcgen05_split": nce_tc_line, "nce_tcgen05_bf16": nce_bf16_line, "nce_shipped_model": nce_shipped_line, "batch": batch_line, "serve": serve_line,
+                "large_ce": large_ce_line, "large_nce": large_nce_line,
                 "launch": {"warps_per_cta": args.warps, "ctas_per_replica": args.cluster,
                            "path": ["auto", "general", "sign-parity", "local-field"][args.path],
                            "autotune_ms": tuned},

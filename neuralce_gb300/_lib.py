@@ -65,7 +65,7 @@ class NceNceChunk(C.Structure):
 
 class NceServerConfig(C.Structure):
     _fields_ = [("hbm_budget", i64), ("max_batch", i32), ("precision", i32), ("warps", i32), ("nce_cluster", i32),
-                ("nce_streams", i32), ("starve_s", f64)]
+                ("nce_streams", i32), ("starve_s", f64), ("ce_kernel", i32), ("ce_lf_warps", i32)]
 
 
 class NceJobDesc(C.Structure):

@@ -36,6 +36,7 @@ def best_launch(gce, st, precision=64, path=0, warps=(2, 4, 8, 16, 32), clusters
             return _cache[key]
         scratch.enable_field(gce)
         clusters = (1,)                                   # one CTA per replica: the decider warp is the chain
+        warps = tuple(w for w in warps if w <= 16) or (16,)   # the kernel's CTAs hold at most 16 warps
     timings = {}
     for cl in clusters:
         for w in warps:

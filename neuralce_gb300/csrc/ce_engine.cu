@@ -721,15 +721,82 @@ __device__ __forceinline__ long long warp_sum_i64(long long part) {
     return (long long)s0 + ((long long)s1 << 21) + ((long long)s2 << 42);
 }
 
+// proposal of a local-field step: the sites and their coordinates as the other kernels draw them, and the uniform
+// kept as its 53 random bits (u = (m + 1) 2^-53) with ln u in float32 for the filter of the Metropolis test
+struct LfProp {
+    int64_t ia, ib;
+    uint64_t um;                     // Philox: the uniform's 53 bits
+    double uh;                       // host stream: the uniform itself (-1 for Philox)
+    float lnu;
+    int32_t ka[3], kb[3], ba, bb;
+};
+
+__device__ __forceinline__ void lf_propose(const CEJob &jb, int64_t g0, int64_t s, int32_t t, LfProp &P) {
+    int64_t ia, ib;
+    uint64_t m = 0;
+    double uh = -1.0;
+    if (jb.prop_a) {
+        ia = jb.prop_a[s * jb.R + t]; ib = jb.prop_b[s * jb.R + t];
+        uh = jb.prop_u[s * jb.R + t];
+    } else {
+        const uint32_t k0 = (uint32_t)jb.seed, k1 = (uint32_t)(jb.seed >> 32);
+        const uint32_t c0 = (uint32_t)(g0 + s), c1 = (uint32_t)((uint64_t)(g0 + s) >> 32);
+        const u32x4 x = philox4x32(c0, c1, (uint32_t)t, 0u, k0, k1);
+        int grp = 0; uint32_t ba = 0, bb = 0;
+        if (jb.n_groups > 1 || __ldg(jb.act_nb) > 1) {
+            const u32x4 y = philox4x32(c0, c1, (uint32_t)t, 1u, k0, k1);
+            if (jb.n_groups > 1)
+                while (grp < jb.n_groups - 1 && (uint64_t)y.x >= __ldg(jb.grp_cum + grp)) ++grp;
+            const uint32_t nb = (uint32_t)__ldg(jb.act_nb + grp);
+            ba = draw_index(y.y, nb); bb = draw_index(y.z, nb);
+        }
+        const uint32_t nc = (uint32_t)jb.n_cells;
+        ia = (int64_t)draw_index(x.x, nc) * jb.nB + __ldg(jb.act_b + grp * jb.max_gb + ba);
+        ib = (int64_t)draw_index(x.y, nc) * jb.nB + __ldg(jb.act_b + grp * jb.max_gb + bb);
+        m = ((uint64_t)x.z << 21) | (uint64_t)(x.w >> 11);  // draw_u01's 53 bits
+    }
+    if (ia < 0 || ib < 0 || ia >= jb.N || ib >= jb.N) { atomicOr(jb.err, 1); ia = ib = 0; }   // rejected no-op
+    P.ia = ia; P.ib = ib; P.um = m; P.uh = uh;
+    P.lnu = __logf(uh >= 0.0 ? (float)uh : (float)(m + 1ull) * 1.1102230246251565e-16f);
+    site_coords32(jb, ia, P.ba, P.ka); site_coords32(jb, ib, P.bb, P.kb);
+}
+
+// Metropolis decision of dE = part 2^-S: accept iff ln u < -beta dE (the reference's rule) with the fixed-point
+// threshold ceil(-ln u / beta 2^S) of the other float64 kernels.  float32 settles it when |beta dE + ln u| exceeds
+// 1e-6 + 1e-6 (|beta dE| + |ln u|), far above float32's error on these terms and above beta times any near-threshold
+// band; otherwise the threshold is formed in float64 (rare).  near: |part - threshold| below the band.
+__device__ __forceinline__ bool lf_accept(const CEJob &jb, long long part, const LfProp &P, float beta_f, double beta,
+                                          float scale_f, bool &near) {
+    const float bd = beta_f * ((float)part * scale_f);
+    const float y = bd + P.lnu;
+    const float tol = 1e-6f + 1e-6f * (fabsf(bd) + fabsf(P.lnu));
+    near = false;
+    if (y < -tol) return true;
+    if (y > tol) return false;
+    const double logu = log(P.uh >= 0.0 ? P.uh : (double)(P.um + 1ull) * 1.1102230246251565404236316680908203125e-16);
+    long long thr;
+    if (beta > 0.0) {
+        const double xs = -logu / beta * ldexp(1.0, jb.fix_shift);
+        thr = xs >= 4.611686018427388e18 ? 4611686018427387904ll : (long long)ceil(xs);
+    } else {
+        thr = logu < 0.0 ? 4611686018427387904ll : -4611686018427387904ll;
+    }
+    const long long dd = part - thr;
+    near = (dd < 0 ? -dd : dd) < (long long)jb.near_fix;
+    return part < thr;
+}
+
+constexpr int kLfMaxWarps = 16;                            // the decider's registers: at most 512 threads a CTA
+
 template <int MO>
-__global__ void __launch_bounds__(1024) ce_lf_chunk_kernel(const __grid_constant__ CEBatch bt, int32_t budget) {
+__global__ void __launch_bounds__(32 * kLfMaxWarps) ce_lf_chunk_kernel(const __grid_constant__ CEBatch bt, int32_t budget) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ LfStep X;
     const int j = find_job(bt, blockIdx.x);
     const CEJob &jb = bt.job[j];
     const int r = blockIdx.x - jb.cta_base;
     if (r >= jb.R) return;
-    const int tid = threadIdx.x, nt = blockDim.x, nw = nt >> 5, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
     const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc, n_cols = jb.n_cols, J = jb.J;
     const int bsz = (2 * jb.lf_e0 + 1) * (2 * jb.lf_e1 + 1) * (2 * jb.lf_e2 + 1);
     const LfLayout L = LfLayout::make(jb.nB, J, MO, n_nbr, n_pfc, n_cols, jb.max_chunks, jb.lf_nidx, bsz, budget,
@@ -744,8 +811,6 @@ __global__ void __launch_bounds__(1024) ce_lf_chunk_kernel(const __grid_constant
     } else {
         tbix = jb.bix; trcol = jb.rcol;
     }
-    uint32_t *chunks = reinterpret_cast<uint32_t *>(smem + L.chunk);
-    for (int i = tid; i < jb.nB * jb.max_chunks; i += nt) chunks[i] = __ldg(jb.chunks + i);
     int4 *nbt = reinterpret_cast<int4 *>(smem + L.nb);
     for (int i = tid; i < jb.nB * n_nbr; i += nt) nbt[i] = make_int4(__ldg(jb.nb_uo + 3 * i), __ldg(jb.nb_uo + 3 * i + 1),
                                                                       __ldg(jb.nb_uo + 3 * i + 2), __ldg(jb.nb_b + i));
@@ -772,13 +837,19 @@ __global__ void __launch_bounds__(1024) ce_lf_chunk_kernel(const __grid_constant
     for (int c = 0; c < n_pfc; ++c)
         for (int q = 0; q < 4; ++q) smask |= (uint32_t)(__ldg(jb.sbits + c * 4 + q) & 1u) << (c * 4 + q);
     const int32_t t = jb.slot_of_rep[r];
+    const float beta_f = jb.beta_slot[t];
+    const double beta = (double)beta_f;
     const double E0c = jb.E[r];
     double Emin = jb.E_min_rep[r];
     const double fscale = ldexp(1.0, -jb.fix_shift);
+    const float scale_f = ldexpf(1.0f, -jb.fix_shift);
     const int64_t g0 = jb.step_dev ? *jb.step_dev : jb.step0;
     const int64_t T = jb.n_steps;
+    const int64_t si = jb.sample_interval;
     long long dsum = 0, dmin = 0;                          // warp 0: the chunk's energy change and its running minimum
-    int64_t nacc = 0, nnear = 0, s_cur = 0;
+    int64_t nacc = 0, s_cur = 0;
+    unsigned nnear = 0;                                    // warp 0, per lane: near-threshold steps it decided
+    const int nrow_a_max = 2 * J;
     __syncthreads();
     for (;;) {
         if (warp == 0) {
@@ -787,11 +858,11 @@ __global__ void __launch_bounds__(1024) ce_lf_chunk_kernel(const __grid_constant
             while (s_cur < T) {
                 const int64_t s = s_cur + lane;
                 const bool live = s < T;
-                BinProp P;
+                LfProp P;
                 int sa = 0, sb = 0, nbi = -1, valid = 0;
                 long long part = 0;
                 if (live) {
-                    bin_propose(jb, g0, s, t, P);
+                    lf_propose(jb, g0, s, t, P);
                     sa = sig[P.ia]; sb = sig[P.ib];
                     valid = sa != sb;
                     if (valid) {
@@ -799,7 +870,8 @@ __global__ void __launch_bounds__(1024) ce_lf_chunk_kernel(const __grid_constant
                         part = -(G[P.ia] + G[P.ib]);
                     }
                 }
-                bool acc = valid && nbi < 0 && part < P.thr;
+                bool near = false;
+                bool acc = valid && nbi < 0 && lf_accept(jb, part, P, beta_f, beta, scale_f, near);
                 const unsigned farm = __ballot_sync(0xffffffffu, acc);
                 const unsigned nearm = __ballot_sync(0xffffffffu, valid && nbi >= 0);
                 int first = farm ? __ffs(farm) - 1 : 32;
@@ -828,7 +900,7 @@ __global__ void __launch_bounds__(1024) ce_lf_chunk_kernel(const __grid_constant
                     }
                     const long long C = warp_sum_i64(cp);
                     __syncwarp();
-                    if (lane == q) { Cq = C; part += 2 * C; acc = part < P.thr; }
+                    if (lane == q) { Cq = C; part += 2 * C; acc = lf_accept(jb, part, P, beta_f, beta, scale_f, near); }
                     if (__shfl_sync(0xffffffffu, (int)acc, q)) { first = q; break; }
                     pend &= pend - 1;
                 }
@@ -836,13 +908,10 @@ __global__ void __launch_bounds__(1024) ce_lf_chunk_kernel(const __grid_constant
                 const bool accepted = first < avail;
                 const int n_adv = accepted ? first + 1 : avail;
                 const long long dfirst = __shfl_sync(0xffffffffu, part, first & 31);
-                if (lane < n_adv && valid) {
-                    const long long dd = part - (long long)P.thr;
-                    nnear += (dd < 0 ? -dd : dd) < (long long)jb.near_fix;
-                }
-                if (jb.E_samples && lane < n_adv && (s + 1) % jb.sample_interval == 0) {
+                if (lane < n_adv && valid) nnear += near;
+                if (jb.E_samples && lane < n_adv && (s + 1) % si == 0) {
                     const long long da = dsum + ((accepted && lane == first) ? dfirst : 0);
-                    jb.E_samples[((s + 1) / jb.sample_interval - 1) * jb.R + t] = E0c + (double)da * fscale;
+                    jb.E_samples[((s + 1) / si - 1) * jb.R + t] = E0c + (double)da * fscale;
                 }
                 s_cur += n_adv;
                 if (accepted) {
@@ -871,34 +940,32 @@ __global__ void __launch_bounds__(1024) ce_lf_chunk_kernel(const __grid_constant
         }
         __syncthreads();
         {
-            // rows in column-aligned chunks of <= 32 (lane per row): 2 eci dPi of every row; column counts when tracked
-            const int nca = __ldg(jb.n_chunks + X.ba), ncb = __ldg(jb.n_chunks + X.bb), total = nca + ncb;
-            for (int k = warp; k < total; k += nw) {
-                const int side = k >= nca, kk = side ? k - nca : k;
-                const int b0 = side ? X.bb : X.ba;
-                const uint32_t d = chunks[b0 * jb.max_chunks + kk];
-                const int col = (int)(d & 0xffu), start = (int)((d >> 8) & 0xffffu), len = (int)(d >> 24);
-                int sgn = 0;
-                if (lane < len) {
-                    const int rr = start + lane;
+            // every row of both sites, four per thread in flight: 2 eci dPi (dPi = 2 sgn), column sums when tracked
+            const int Ja = __ldg(jb.rv_len + X.ba), Jb = __ldg(jb.rv_len + X.bb), nrow = Ja + Jb;
+            for (int q0 = tid; q0 < nrow; q0 += 4 * nt) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int q = q0 + u * nt;
+                    if (q >= nrow) break;
+                    const int side = q >= Ja, rr = side ? q - Ja : q;
+                    const int b0 = side ? X.bb : X.ba;
                     const uint16_t *bx = tbix + ((size_t)b0 * J + rr) * MO;
                     const uint8_t *bs = bits + (size_t)side * n_pfc * n_nbr;
                     unsigned x = 0;
 #pragma unroll
                     for (int m = 0; m < MO; ++m) x ^= bs[bx[m]];
-                    if ((x ^ (x >> 1)) & 1u) sgn = (x & 1u) ? 1 : -1;       // dPi = 2 sgn
+                    int sgn = 0;
+                    if ((x ^ (x >> 1)) & 1u) sgn = (x & 1u) ? 1 : -1;
+                    const int col = trcol[(size_t)b0 * J + rr];
                     v[side * J + rr] = sgn ? 2 * sgn * efix[col] : 0;
-                }
-                if (track) {
-                    const int n = (int)__reduce_add_sync(0xffffffffu, (unsigned)sgn);
-                    if (lane == 0 && n) atomicAdd(&dcv[col], 2 * n);
+                    if (track && sgn) atomicAdd(&dcv[col], 2 * sgn);
                 }
             }
         }
         __syncthreads();
         {
-            // each neighbour's field: the sum of its changed rows, eight lanes per neighbour entry
-            const int grp = tid >> 3, gl = tid & 7, ngrp = nt >> 3, ntask = 2 * (n_nbr - 1);
+            // each neighbour's field: the sum of its changed rows, four lanes per neighbour entry
+            const int grp = tid >> 2, gl = tid & 3, ngrp = nt >> 2, ntask = 2 * (n_nbr - 1);
             for (int task0 = 0; task0 < ntask; task0 += ngrp) {
                 const int task = task0 + grp;
                 long long sum = 0;
@@ -907,10 +974,15 @@ __global__ void __launch_bounds__(1024) ce_lf_chunk_kernel(const __grid_constant
                     side = task >= n_nbr - 1; n = 1 + (side ? task - (n_nbr - 1) : task);
                     const int b0 = side ? X.bb : X.ba;
                     const int o0 = loff[b0 * (n_nbr + 1) + n], o1 = loff[b0 * (n_nbr + 1) + n + 1];
-                    for (int k = o0 + gl; k < o1; k += 8) sum += v[side * J + lidx[k]];
+                    const long long *vs = v + side * J;
+                    long long s0 = 0, s1 = 0;
+                    int k = o0 + gl;
+                    for (; k + 4 < o1; k += 8) { s0 += vs[lidx[k]]; s1 += vs[lidx[k + 4]]; }
+                    if (k < o1) s0 += vs[lidx[k]];
+                    sum = s0 + s1;
                 }
-#pragma unroll
-                for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, 8);
+                sum += __shfl_xor_sync(0xffffffffu, sum, 1, 4);
+                sum += __shfl_xor_sync(0xffffffffu, sum, 2, 4);
                 if (task < ntask && gl == 0 && sum) {
                     const uint32_t st = lf_site(jb, side ? X.kb : X.ka, nbt[(side ? X.bb : X.ba) * n_nbr + n]);
                     atomicAdd(reinterpret_cast<unsigned long long *>(G + st), (unsigned long long)sum);
@@ -923,7 +995,8 @@ __global__ void __launch_bounds__(1024) ce_lf_chunk_kernel(const __grid_constant
         }
         __syncthreads();
     }
-    if (warp == 0) nnear = (int64_t)__reduce_add_sync(0xffffffffu, (unsigned)nnear);   // each lane counted its own steps
+    (void)nrow_a_max;
+    if (warp == 0) nnear = __reduce_add_sync(0xffffffffu, nnear);   // each lane counted the steps it decided
     if (tid == 0) {
         jb.E[r] = E0c + (double)dsum * fscale;
         jb.E_min_rep[r] = fmin(Emin, E0c + (double)dmin * fscale);
@@ -1404,7 +1477,7 @@ static int launch_lf(const CEBatch &bt, int mo, int total, int warps, size_t sme
         default: return fail(NCE_ERR_UNSUPPORTED, "cluster order %d > 8", mo);
     }
     NCE_CUDA(::nce::raise_smem_limit((const void *)kern, smem));
-    kern<<<total, warps * 32, smem, s>>>(bt, budget);
+    kern<<<total, std::min(warps, kLfMaxWarps) * 32, smem, s>>>(bt, budget);
     NCE_CUDA(cudaGetLastError());
     return NCE_OK;
 }

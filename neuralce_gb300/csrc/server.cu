@@ -32,7 +32,7 @@ struct SJob {
     int64_t id = 0;
     nce_job_desc d{};                 // output pointers as given; input pointers replaced by the host copies
     int64_t N = 0;
-    int32_t n_cols = 0, mo = 0, binary = 0, C0 = 0, D = 0, depth = 0;
+    int32_t n_cols = 0, mo = 0, binary = 0, C0 = 0, D = 0, depth = 0, lf = 0;   // lf: runs the local-field kernel
     std::vector<int8_t> sig; std::vector<float> beta; std::vector<int32_t> lid;
     int64_t bytes = 0;
     int status = NCE_JOB_QUEUED, error = 0;
@@ -56,7 +56,7 @@ struct Plan {
     int64_t add(int64_t n) { off.push_back(total); total += al256(std::max<int64_t>(n, 1)); return off.back(); }
 };
 
-Plan ce_plan(int32_t R, int64_t N, int32_t n_cols, bool track) {
+Plan ce_plan(int32_t R, int64_t N, int32_t n_cols, bool track, bool lf) {
     Plan p;
     p.add((int64_t)R * N);                       // 0 sigma
     p.add(8ll * R);                              // 1 E
@@ -66,6 +66,7 @@ Plan ce_plan(int32_t R, int64_t N, int32_t n_cols, bool track) {
     p.add(8ll * R);                              // 7 n_acc
     p.add(8);                                    // 8 n_ex
     p.add(track ? 8ll * R * n_cols : 0);         // 9 cv
+    p.add(lf ? 8ll * R * N : 0);                 // 10 local fields
     return p;
 }
 
@@ -169,7 +170,7 @@ void fail_job(nce_server *S, SJob &j, int rc) {
 int start_ce(nce_server *S, SJob &j, cudaStream_t s) {
     const int32_t R = j.d.R;
     const bool track = j.binary != 0;
-    Plan p = ce_plan(R, j.N, j.n_cols, track);
+    Plan p = ce_plan(R, j.N, j.n_cols, track, j.lf != 0);
     void *base = nullptr;
     NCE_CUDA(cudaMallocAsync(&base, (size_t)p.total, s));
     j.dev = (char *)base;
@@ -196,6 +197,11 @@ int start_ce(nce_server *S, SJob &j, cudaStream_t s) {
     int rc = track ? nce_ce_cluster_counts(h, st.sigma, R, st.cv, s) : nce_ce_energy(h, st.sigma, R, 64, st.E, s);
     if (rc) return rc;
     if (track) { rc = nce_ce_energy_from_counts(h, st.cv, R, st.E, s); if (rc) return rc; }
+    if (j.lf) {
+        st.field = (int64_t *)(b + p.off[10]);
+        rc = nce_ce_field_init(h, st.sigma, R, st.field, s);
+        if (rc) return rc;
+    }
     NCE_CUDA(cudaMemcpyAsync(st.E_min_rep, st.E, 8, cudaMemcpyDeviceToDevice, s));   // replica 0, as PT set-up does
     NCE_CUDA(cudaStreamSynchronize(s));                                            // host copies may be freed now
     return NCE_OK;
@@ -370,8 +376,9 @@ void ce_worker(nce_server *S) {
     cudaSetDevice(S->device);
     std::vector<std::shared_ptr<SJob>> run;
     while (take_round(S, 0, run)) {
+        // one launch takes jobs of one cluster order and one kernel (local field or sign parity)
         std::map<int32_t, std::vector<std::shared_ptr<SJob>>> by_mo;
-        for (auto &p : run) by_mo[p->mo].push_back(p);
+        for (auto &p : run) by_mo[2 * p->mo + p->lf].push_back(p);
         int rc = NCE_OK, g = 0;
         for (auto &grp : by_mo) {
             auto &v = grp.second;
@@ -386,7 +393,8 @@ void ce_worker(nce_server *S) {
                     std::memset(&c, 0, sizeof(c));
                     c.n_steps = chunk_len(j); c.step0 = j.done; c.seed = j.d.seed; c.sample_interval = 1;
                     c.do_exchange = ((j.done + c.n_steps) % j.d.exchange_every) == 0;
-                    c.precision = S->cfg.precision; c.warps = S->cfg.warps; c.path = 0; c.cluster = 1;
+                    c.precision = j.lf ? 64 : S->cfg.precision; c.path = j.lf ? 3 : 0; c.cluster = 1;
+                    c.warps = j.lf && S->cfg.ce_lf_warps > 0 ? S->cfg.ce_lf_warps : S->cfg.warps;
                 }
                 rc = nce_ce_run_batch(n, hs.data(), ss.data(), cs.data(), s);
                 for (int i = 0; i < n && rc == NCE_OK; ++i) {
@@ -522,7 +530,13 @@ int nce_job_submit(nce_server_handle S, const nce_job_desc *d, int64_t *job_id) 
     if (d->kind == NCE_JOB_CE) {
         int rc = ce_model_dims((nce_ce_handle)d->model, &j->N, &j->n_cols, &j->mo, &j->binary);
         if (rc) return rc;
-        j->bytes = ce_plan(d->R, j->N, j->n_cols, j->binary != 0).total;
+        if (S->cfg.ce_kernel == 0 && d->R <= 65535) {
+            int32_t ok = 0;
+            rc = nce_ce_has_local_field((nce_ce_handle)d->model, &ok, nullptr);
+            if (rc) return rc;
+            j->lf = ok;
+        }
+        j->bytes = ce_plan(d->R, j->N, j->n_cols, j->binary != 0, j->lf != 0).total;
         NCE_CHECK(d->R <= 25600, "nce_job_submit: too many replicas for the exchange kernel");
     } else {
         int rc = nce_model_dims((nce_nce_handle)d->model, &j->N, &j->C0, &j->D, &j->depth);

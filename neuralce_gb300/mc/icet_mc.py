@@ -46,10 +46,10 @@ def prepare_cell(ce_file, init_cif, supercell_reps=None, seed=0, log=print):
                 m = np.isin(basis, bs)
                 Z[m] = rng.permutation(Z[m])
             atoms.numbers = Z
-            log(f"PT-MC: supercell {reps} of the init cif -> {len(atoms)} atoms, species re-shuffled per sublattice "
+            log(f"[ce] cif repeated {reps}: {len(atoms)} sites; each sublattice's species permuted at random "
                 f"(seed {seed})", flush=True)
         else:
-            log(f"PT-MC: supercell {reps} of the init cif -> {len(atoms)} atoms, periodic images kept", flush=True)
+            log(f"[ce] cif repeated {reps}: {len(atoms)} sites, the ordered copies left as they are", flush=True)
     return atoms, energy_scale
 
 
@@ -84,7 +84,7 @@ def run_pt_mc(ce_path, init_cif, n_steps, T_min=100.0, T_max=2000.0, n_replicas=
             raise ValueError("--init_npz assigns one structure per temperature of a single ladder; n_ladders must be 1")
         from .init_structures import load_init_npz
         run_T = np.asarray(T_grid, float) if T_grid is not None else np.geomspace(T_min, T_max, n_replicas)
-        nums, _ = load_init_npz(init_npz, ce.primitive, atoms, run_T)
+        nums, _ = load_init_npz(init_npz, atoms, run_T)
         rows = []
         for r in range(nums.shape[0]):
             a_r = Structure(atoms.cell, atoms.positions, nums[r].astype(np.int64))

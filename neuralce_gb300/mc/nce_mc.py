@@ -46,14 +46,14 @@ def _prepare(model_path, init_cif, supercell=(1, 1, 1), seed_idx=0, dtype="float
                 m = np.isin(basis, [b for b, k in enumerate(keys) if k == key])
                 Z[m] = rng.permutation(Z[m])
             atoms.numbers = Z
-            _log(f"[ce_cnn] supercell {sc} of the init cif -> {len(atoms)} atoms, species re-shuffled per sublattice (seed {seed})")
+            _log(f"[nce] cif repeated {sc}: {len(atoms)} sites; each sublattice's species permuted at random (seed {seed})")
         else:
-            _log(f"[ce_cnn] supercell {sc} of the init cif -> {len(atoms)} atoms (periodic images kept)")
+            _log(f"[nce] cif repeated {sc}: {len(atoms)} sites, the ordered copies left as they are")
     t0 = time.time()
     mc = setup(mdl, atoms, seed_idx=seed_idx, dtype=dtype)
     mc["mdl"], mc["atoms"] = mdl, atoms
-    _log(f"[ce_cnn] model: depth {mc['depth']}, {mc['n_atoms']} atoms ({mc['n_active']} active), setup "
-         f"{time.time() - t0:.1f}s, E0 = {mc['energy'](mc['sig0']):.6f} eV/atom")
+    _log(f"[nce] network of {mc['depth']} layer(s) on {mc['n_atoms']} sites ({mc['n_active']} swappable); set up in "
+         f"{time.time() - t0:.1f} s; starting energy {mc['energy'](mc['sig0']):.6f} eV/atom")
     return mc
 
 
@@ -72,7 +72,7 @@ def _fingerprint(mc, sig):
 def _init_sig_from_npz(mc, path, temps, R):
     from .init_structures import load_init_npz
     model, atoms = mc["model"], mc["atoms"]
-    nums, _ = load_init_npz(path, mc["mdl"]["primitive"], atoms, temps)
+    nums, _ = load_init_npz(path, atoms, temps)
     if nums.shape[0] != R:
         raise ValueError(f"init_npz has {nums.shape[0]} structures for {R} replicas")
     prim = mc["mdl"]["primitive"]
@@ -105,7 +105,7 @@ def _run_replicas(mc, betas, n_steps, seed, chunk, log_every, sample_interval, o
     N = mc["n_atoms"]
     if init_npz:
         sig = _init_sig_from_npz(mc, init_npz, temps, R)
-        _log(f"[{tag}] per-replica starting structures from {init_npz} (matched by lattice position)")
+        _log(f"[{tag}] starting structures read from {init_npz}, one per temperature (sites paired by position)")
     else:
         sig = np.stack([model.sig0] * R).astype(np.int8)
     n_chunks = max(n_steps // chunk, 1)
@@ -130,8 +130,8 @@ def _run_replicas(mc, betas, n_steps, seed, chunk, log_every, sample_interval, o
             have = {k: int(ck["cfg_" + k]) for k in ints}; have["model"] = str(ck["cfg_model"])
             same_T = np.allclose(np.asarray(ck["cfg_betas"], np.float64), betas.astype(np.float64), rtol=0, atol=1e-6)
             if have != want or not same_T:
-                raise RuntimeError(f"checkpoint {ck_path} belongs to a different run (checkpoint {have} vs this run {want}, "
-                                   f"same temperatures: {same_T}); delete it to start fresh")
+                raise RuntimeError(f"{ck_path} was written by another run (it records {have}, this run is {want}, "
+                                   f"ladder unchanged: {same_T}); remove the file or choose another output directory")
             c0 = int(ck["chunk"]); drift = float(ck["drift"])
             st.sigma.copy_(torch.as_tensor(ck["sig"]).cuda())
             st.rep_of_slot.copy_(torch.as_tensor(ck["rep_of_slot"]).cuda())

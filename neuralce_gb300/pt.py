@@ -285,8 +285,8 @@ def run_pt_mcmc(gce, cfg: MCMCConfig, verbose=True):
         if not np.allclose(ck["cfg_temps"], temps, rtol=0, atol=1e-6):
             have["temps"] = "differ"; want["temps"] = "same"
         if have != want:
-            raise RuntimeError(f"checkpoint {ck_path} belongs to a different run (checkpoint {have} vs this run {want}); "
-                               "delete it to start fresh")
+            raise RuntimeError(f"{ck_path} was written by another run (it records {have}, this run is {want}); remove the "
+                               "file or choose another output directory")
         c0 = int(ck["chunk"]); si_ = int(ck["si"]); energy_samples[:si_] = ck["energy_samples"]; step = int(ck["step"])
         st.sigma.copy_(torch.as_tensor(ck["sigma"]).cuda()); st.E.copy_(torch.as_tensor(ck["E"]).cuda())
         st.rep_of_slot.copy_(torch.as_tensor(ck["rep_of_slot"]).cuda()); st.slot_of_rep.copy_(torch.as_tensor(ck["slot_of_rep"]).cuda())

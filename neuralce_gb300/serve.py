@@ -52,10 +52,15 @@ class Job:
 
 
 class Server:
-    def __init__(self, hbm_budget=0, max_batch=64, precision=32, warps=8, nce_cluster=1, nce_streams=4, starve_s=5.0):
+    """ce_kernel: 0 = CE jobs whose cell allows it run the local-field kernel (exact fixed-point dE; 8 more bytes of
+    device memory per site and replica), the rest the sign-parity kernel at ``precision``; 2 = sign parity for all."""
+
+    def __init__(self, hbm_budget=0, max_batch=64, precision=32, warps=8, nce_cluster=1, nce_streams=4, starve_s=5.0,
+                 ce_kernel=0, ce_lf_warps=0):
         cfg = _lib.NceServerConfig()
         cfg.hbm_budget, cfg.max_batch, cfg.precision, cfg.warps = int(hbm_budget), int(max_batch), int(precision), int(warps)
         cfg.nce_cluster, cfg.nce_streams, cfg.starve_s = int(nce_cluster), int(nce_streams), float(starve_s)
+        cfg.ce_kernel, cfg.ce_lf_warps = int(ce_kernel), int(ce_lf_warps)
         h = C.c_void_p()
         _lib.check(_lib.lib().nce_server_create(C.byref(cfg), C.byref(h)), "nce_server_create")
         self._h = h

@@ -75,7 +75,7 @@ def test_icet_pt_cli_outputs_and_resume(cuda, tmp_path, ptni_ce, monkeypatch):
     with pytest.raises(RuntimeError):
         run.main(args + ["--out_dir", str(c), "--checkpoint_every", "1"])
     monkeypatch.undo()
-    with pytest.raises(RuntimeError, match="different run"):
+    with pytest.raises(RuntimeError, match="another run"):
         run.main([x if x != "3" else "4" for x in args] + ["--out_dir", str(c), "--checkpoint_every", "1"])
 
 

@@ -70,9 +70,11 @@ def test_results_same_alone_and_in_mix(cuda):
         assert int(a["n_acc"].sum()) > 0
 
 
-def test_ce_job_equals_direct_chunks(cuda):
-    """A served CE job = the chunk API driven by hand: fp32 chunks of the exchange interval, exact re-anchor of
-    the carried energies from the tracked cluster-vector sums after every chunk."""
+@pytest.mark.parametrize("ce_kernel", [2, 0])
+def test_ce_job_equals_direct_chunks(cuda, ce_kernel):
+    """A served CE job = the chunk API driven by hand: chunks of the exchange interval, exact re-anchor of the
+    carried energies from the tracked cluster-vector sums after every chunk; ce_kernel 2: sign parity in fp32,
+    ce_kernel 0: the local-field kernel (exact fixed point) on this cell."""
     torch = cuda
     from neuralce_gb300.pt import PTState, run_chunk
     from neuralce_gb300.serve import Server
@@ -80,14 +82,19 @@ def test_ce_job_equals_direct_chunks(cuda):
     gce, R = j["model"], len(j["beta"])
     E0 = gce.batched_energy(torch.as_tensor(j["sigma"]).cuda()).cpu().numpy()
     st = PTState(j["sigma"], E0, j["beta"], np.zeros(R, np.int32)).track_counts(gce)
+    lf = ce_kernel == 0
+    assert gce.has_local_field
+    if lf:
+        st.enable_field(gce)
     done = 0
     while done < j["steps"]:
         n = min(j["ex"], j["steps"] - done)
-        run_chunk(gce, st, n, done, j["seed"], 32, 8, None, 1, None, (done + n) % j["ex"] == 0)
+        run_chunk(gce, st, n, done, j["seed"], 64 if lf else 32, 8, None, 1, None, (done + n) % j["ex"] == 0,
+                  path=3 if lf else 0)
         st.reanchor_from_counts(gce)
         done += n
     torch.cuda.synchronize()
-    with Server(precision=32, warps=8) as srv:
+    with Server(precision=32, warps=8, ce_kernel=ce_kernel) as srv:
         h = _submit(srv, j)
         srv.wait([h], timeout=120)
         r = h.result()
