@@ -298,6 +298,12 @@ int nce_nce_full_cache(nce_nce_handle h, const nce_nce_state *st, void *stream);
 int nce_nce_run_chunk(nce_nce_handle h, const nce_nce_state *st, const nce_nce_chunk *ck, void *stream);
 int nce_nce_errors(nce_nce_handle h, int32_t *flags);
 
+/* Makes a tensor-core completion wait run out on purpose (one CTA: tensor memory and an mbarrier set up as in the
+ * layer tiles, no MMA issued, the wait gives up after `limit` polls) and takes the layer tiles' way out of it: flag 32
+ * in the handle's device error word (read with nce_nce_errors), abandoned work drained with a bounded wait, tensor
+ * memory freed.  Tests the timeout path without faulting or hanging the GPU.  No counterpart in the reference. */
+int nce_nce_tc_wait_selftest(nce_nce_handle h, int32_t limit, void *stream);
+
 /* The reference's local_delta / commit pair on device data, one swap per replica.  nce_nce_local_delta evaluates,
  * for every replica r, the swap of sites prop_a[r] and prop_b[r] (device int32, indexed by replica) on the state's
  * caches without changing them: dE_out[r] (device float64, model units as in nce_nce_chunk.dE_out; 0 for two sites of

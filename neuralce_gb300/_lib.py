@@ -118,6 +118,7 @@ SIGNATURES = {
     "nce_nce_run_chunk": (i32, [vp, P(NceNceState), P(NceNceChunk), vp]),
     "nce_nce_errors": (i32, [vp, P(i32)]),
     "nce_nce_local_delta": (i32, [vp, P(NceNceState), vp, vp, vp, vp]),
+    "nce_nce_tc_wait_selftest": (i32, [vp, i32, vp]),
     "nce_nce_commit": (i32, [vp, P(NceNceState), vp, vp]),
     "nce_nce_accept": (i32, [vp, i32, i32, f64, vp, vp, vp, vp, vp]),
     "nce_tc_gemm": (i32, [vp, vp, vp, i32, i32, i32, i32, vp]),

@@ -163,9 +163,11 @@ __host__ __device__ __forceinline__ int kpad16(int k) { return (k + 15) & ~15; }
 __host__ __device__ __forceinline__ int x_stride(int kin) { return (kin + 4) & ~3; }
 
 // tensor-memory accumulator, completion mbarrier and the staged B operand of the tcgen05 tile path; `phase` is the
-// parity of the next completion (every thread of the CTA keeps the same count)
+// parity of the next completion (every thread of the CTA keeps the same count).  `failed`: a completion wait gave up
+// (the whole CTA agrees on it); from then on the CTA issues no MMA, writes no operand tile and reads no accumulator
+// for the rest of the kernel, and only drains the abandoned MMAs (bounded) before freeing tensor memory.
 struct TcCtx {
-    uint32_t tmem; uint64_t *mbar; uint32_t phase; uint8_t *W;
+    uint32_t tmem; uint64_t *mbar; uint32_t phase; uint8_t *W; int failed;
 };
 
 // allocation by warp 0 (D columns rounded up to a power of two >= 32) and the mbarrier, for the whole kernel
@@ -175,13 +177,28 @@ __device__ __forceinline__ void tc_begin(int D, TcCtx &tc, uint8_t *wsm, uint64_
     umma::fence_before();
     __syncthreads();
     umma::fence_after();
-    tc.tmem = *tslot; tc.mbar = mbar; tc.phase = 0; tc.W = wsm;
+    tc.tmem = *tslot; tc.mbar = mbar; tc.phase = 0; tc.W = wsm; tc.failed = 0;
 }
 
-__device__ __forceinline__ void tc_end(int D, const TcCtx &tc) {
+__device__ __forceinline__ void tc_end(int D, const TcCtx &tc, uint32_t limit = 1u << 20) {
+    // after a wait that gave up, give the abandoned MMAs one more bounded wait before their tensor memory is freed
+    if (tc.failed) umma::mbar_wait(tc.mbar, tc.phase ^ 1u, limit);
     umma::fence_before();
     __syncthreads();
     if ((threadIdx.x >> 5) == 0) umma::tmem_free(tc.tmem, umma::tmem_cols(D));
+}
+
+// the completion wait of one tile's MMAs, agreed on by the whole CTA: false when it gave up (error flag 32 set, the
+// CTA's tensor-core work stops)
+__device__ __forceinline__ bool tc_wait(TcCtx &tc, int32_t *err, uint32_t limit = 1u << 20) {
+    const bool ok = umma::mbar_wait(tc.mbar, tc.phase, limit);
+    tc.phase ^= 1u;
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicOr(err, 32);
+        tc.failed = 1;
+        return false;
+    }
+    return true;
 }
 __host__ __device__ __forceinline__ int tile_kin(int P, int C0, int D) { return (1 + P) * (C0 > D ? C0 : D); }
 
@@ -235,6 +252,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
     const int KS = (tc && Kp > m.tc_ks) ? m.tc_ks : Kp, nks = Kp / KS;
     int klo = 0, khi = Kp;                                   // the slice being gathered (all of K off the tcgen05 path)
     uint8_t *A0 = reinterpret_cast<uint8_t *>(X), *A1 = A0 + (size_t)128 * KS * 2;
+    if (tc && tc->failed) return;                            // an earlier completion wait gave up: no more tensor work
     if (tc) {
         // this layer's B operand into shared memory (read by the tensor cores after the first tile barrier)
         const size_t n16 = (size_t)Kp * D * 2 * (m.tc_split ? 2 : 1) / 16;
@@ -462,8 +480,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                 umma::issue_tile_k(tc->tmem, A0, A1, (uint32_t)KS * 16u, tc->W + bo, tc->W + (size_t)Kp * D * 2 + bo,
                                    (uint32_t)Kp * 16u, D, KS / 16, m.tc_split ? 3 : 1, ks > 0, tc->mbar);
             }
-            if (!umma::mbar_wait(tc->mbar, tc->phase) && (tid & 31) == 0) atomicOr(jb.err, 32);
-            tc->phase ^= 1u;
+            if (!tc_wait(*tc, jb.err)) return;                  // operands and accumulator left alone from here on
             umma::fence_after();
         }
         }   // K slices
@@ -1584,7 +1601,15 @@ __global__ void __launch_bounds__(128) nce_tc_gemm_kernel(const float *A, const 
     umma::fence_after();
     const uint32_t tmem = tslot;
     if (tid == 0) umma::issue_tile(tmem, A0, A1, B0, B1, N, Kp, split ? 3 : 1, &mbar);
-    if (!umma::mbar_wait(&mbar, 0) && lane == 0) atomicOr(err, 1);
+    const bool done = umma::mbar_wait(&mbar, 0);
+    if (__syncthreads_or(!done)) {                           // gave up: drain (bounded), free, report; no loads
+        if (tid == 0) atomicOr(err, 1);
+        umma::mbar_wait(&mbar, 0);
+        umma::fence_before();
+        __syncthreads();
+        if (warp == 0) umma::tmem_free(tmem, umma::tmem_cols(N));
+        return;
+    }
     umma::fence_after();
     const int64_t row = row0 + warp * 32 + lane;
     for (int c0 = 0; c0 < N; c0 += 16) {
@@ -1601,6 +1626,18 @@ __global__ void __launch_bounds__(128) nce_tc_gemm_kernel(const float *A, const 
 }  // namespace nce
 
 namespace nce {
+// A tensor-core completion wait that runs out on purpose: tensor memory and the mbarrier are set up as in the layer
+// tiles, no MMA is issued, so nothing ever arrives; the bounded wait gives up after `limit` polls and the kernel
+// takes the same way out as a layer tile (flag 32 in the model's error word, bounded drain, tensor memory freed).
+__global__ void __launch_bounds__(128) nce_tc_wait_selftest_kernel(int32_t *err, uint32_t limit) {
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t slot;
+    TcCtx tc;
+    tc_begin(32, tc, nullptr, &mbar, &slot);
+    tc_wait(tc, err, limit);                                // nothing was issued: gives up, sets flag 32 and `failed`
+    tc_end(32, tc, limit);
+}
+
 int nce_error_peek(nce_nce_handle h, int32_t *flags) {
     NCE_CHECK(h && flags, "nce_error_peek: null argument");
     NCE_CUDA(cudaMemcpy(flags, h->err, sizeof(int32_t), cudaMemcpyDeviceToHost));
@@ -2008,6 +2045,13 @@ int nce_nce_accept(const double *dE, int32_t n_models, int32_t R, double scale_e
     NCE_CHECK(dE && beta_slot && slot_of_rep && u && accept && n_models >= 1 && R >= 1, "nce_nce_accept: bad argument");
     nce_accept_kernel<<<(R + 127) / 128, 128, 0, (cudaStream_t)stream>>>(dE, n_models, R, scale_eV, beta_slot, slot_of_rep, u,
                                                                          accept);
+    NCE_CUDA(cudaGetLastError());
+    return NCE_OK;
+}
+
+int nce_nce_tc_wait_selftest(nce_nce_handle h, int32_t limit, void *stream) {
+    NCE_CHECK(h && limit >= 1, "nce_nce_tc_wait_selftest: bad argument");
+    nce_tc_wait_selftest_kernel<<<1, 128, 0, (cudaStream_t)stream>>>(h->err, (uint32_t)limit);
     NCE_CUDA(cudaGetLastError());
     return NCE_OK;
 }

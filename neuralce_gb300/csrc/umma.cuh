@@ -58,7 +58,8 @@ __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count) {
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 }
 
-// wait for the phase of the given parity to complete; gives up after `limit` polls (returns false)
+// wait for the phase of the given parity to complete; gives up after `limit` polls (returns false).  The default of
+// 2^20 polls is milliseconds, orders of magnitude above a tile's MMAs.
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint32_t limit = 1u << 20) {
     const uint32_t a = smem_u32(mbar);
     for (uint32_t i = 0; i < limit; ++i) {

@@ -412,3 +412,24 @@ def test_config_cell_metropolis_matches_oracle(cuda, mma, width, cluster):
     oracle (decisions equal except at counted near-threshold steps; occupancies bit-exact)."""
     m, orc = _model_bench_mma(8, 5, mma, width)
     _metropolis_vs_oracle(cuda, m, orc, 4, 24, 13, cluster)
+
+
+def test_tensor_core_wait_timeout_is_reported(cuda):
+    """A tensor-core completion wait that nothing completes (no MMA issued) gives up after a bounded number of polls:
+    the kernel returns, flag 32 reaches check_errors() as an NceError, the flags clear, and the context stays usable
+    (a tcgen05 chunk afterwards still matches its float32 counterpart within the bf16 bound)."""
+    torch = cuda
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.nce import NCEState
+    m, _ = _model_bench_mma(3, 4, 2, 32)
+    _lib.check(_lib.lib().nce_nce_tc_wait_selftest(m.handle, 1000, _lib.stream_ptr()), "nce_nce_tc_wait_selftest")
+    torch.cuda.synchronize()
+    with pytest.raises(_lib.NceError, match="tensor-core completion wait timed out"):
+        m.check_errors()
+    m.check_errors()                                       # cleared
+    st = NCEState(m, m.sig0[None].astype(np.int8), np.ones(1)).full_cache()
+    st.run_chunk(4, 0, seed=3, force=1)
+    torch.cuda.synchronize()
+    m.check_errors()
+    Ecar = float(st.E[0].item())
+    assert abs(Ecar - float(NCEState(m, st.sigma.cpu().numpy(), np.ones(1)).full_cache().E[0].item())) < 1e-3
