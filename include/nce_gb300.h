@@ -347,9 +347,9 @@ typedef struct {
     int32_t nce_cluster;   /* NeuralCE CTAs per replica (0 = 1) */
     int32_t nce_streams;   /* NeuralCE streams (0 = 4) */
     double starve_s;       /* no job overtakes one that has waited this long (0 = 5 s) */
-    int32_t ce_kernel;     /* 0: CE jobs whose cell allows it run the local-field kernel (exact fixed-point dE, fields of
-                              8 bytes per site and replica counted in the job's memory), the others the sign-parity
-                              kernel at `precision`; 2: every CE job on the sign-parity kernel */
+    int32_t ce_kernel;     /* 0 or 2: every CE job on the sign-parity kernel at `precision`; 3: jobs whose cell allows it
+                              on the local-field kernel (exact fixed-point dE, fields of 8 bytes per site and replica
+                              counted in the job's memory), the others on the sign-parity kernel */
     int32_t ce_lf_warps;   /* warps per replica of the local-field launches (0 = `warps`) */
 } nce_server_config;
 

@@ -530,7 +530,7 @@ int nce_job_submit(nce_server_handle S, const nce_job_desc *d, int64_t *job_id) 
     if (d->kind == NCE_JOB_CE) {
         int rc = ce_model_dims((nce_ce_handle)d->model, &j->N, &j->n_cols, &j->mo, &j->binary);
         if (rc) return rc;
-        if (S->cfg.ce_kernel == 0 && d->R <= 65535) {
+        if (S->cfg.ce_kernel == 3 && d->R <= 65535) {
             int32_t ok = 0;
             rc = nce_ce_has_local_field((nce_ce_handle)d->model, &ok, nullptr);
             if (rc) return rc;

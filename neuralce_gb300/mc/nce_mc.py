@@ -98,7 +98,7 @@ def _write_cifs(mc, sig_in, temps, out_dir):
 def _run_replicas(mc, betas, n_steps, seed, chunk, log_every, sample_interval, out_dir, tag, exchange_every=0,
                   anchor_every=None, init_npz=None, checkpoint_every=0, cluster=1):
     import torch
-    from ..nce import NCEState
+
     model = mc["model"]
     R = len(betas); betas = np.asarray(betas, np.float32)
     temps = 1.0 / (KB * betas.astype(np.float64))
@@ -117,7 +117,7 @@ def _run_replicas(mc, betas, n_steps, seed, chunk, log_every, sample_interval, o
     E_chunk, acc_chunk, drift_log, traj = [], [], [], []
     drift = 0.0
     ck_every = int(checkpoint_every or 0); ck_path = os.path.join(out_dir, "checkpoint.npz"); c0 = 0
-    st = NCEState(model, sig, betas)
+    st = mc["new_state"](sig, betas)                    # one model, or the ensemble of every trained seed
     want = None
     if ck_every:
         ck_every = int(np.ceil(ck_every / anchor_every)) * anchor_every
@@ -139,6 +139,8 @@ def _run_replicas(mc, betas, n_steps, seed, chunk, log_every, sample_interval, o
             st.n_acc.copy_(torch.as_tensor(ck["n_acc"]).cuda()); st.n_ex.copy_(torch.as_tensor(ck["n_ex"]).cuda())
             E_chunk = list(ck["E_chunk"]); acc_chunk = list(ck["acc_chunk"]); drift_log = [float(x) for x in ck["drift_log"]]
             traj = [np.asarray(ck["traj"])] if ck["traj"].shape[1] else []
+            if hasattr(st, "broadcast"):
+                st.broadcast()
             _log(f"[{tag}] resumed from {ck_path}: chunk {c0}/{n_chunks}")
     st.full_cache()
     _log(f"[{tag}] {R} replicas, {n_chunks} chunks of {chunk} steps; full re-anchor every {anchor_every} chunk(s)"
@@ -169,7 +171,7 @@ def _run_replicas(mc, betas, n_steps, seed, chunk, log_every, sample_interval, o
                      drift_log=np.array(drift_log, np.float64), traj=(traj[0] if traj else np.zeros((R, 0))),
                      cfg_betas=betas.astype(np.float64), **{"cfg_" + k: v for k, v in want.items()})
             os.replace(ck_path + ".tmp.npz", ck_path)
-    st.model.check_errors()                               # device error flags raise here
+    (st.check_errors if hasattr(st, "check_errors") else st.model.check_errors)()   # device error flags raise here
     wall = time.time() - t0
     os.makedirs(out_dir, exist_ok=True)
     E_chunk = np.array(E_chunk); acc_chunk = np.array(acc_chunk); traj = np.concatenate(traj, axis=1)

@@ -115,8 +115,6 @@ def dispatch_nce(args):
         raise ValueError("nce supports --energy_mode local (recommended) or full")
     if args.spin_allowed_file:
         raise NotImplementedError("spin models are not on this engine's path")
-    if args.model_seed < 0:
-        raise NotImplementedError("--model_seed -1 (ensemble mean) is not on this engine's path")
     common = dict(model_path=args.ckpt, init_cif=args.init_cif, seed=args.seed, log_every=args.log_every,
                   out_dir=args.out_dir, chunk=args.chunk, sample_interval=args.sample_interval,
                   supercell=tuple(args.supercell), seed_idx=args.model_seed, dtype=args.dtype,

@@ -272,6 +272,87 @@ class NCECache:
         return sum(s.E for s in self.states) / len(self.states)
 
 
+class EnsembleState:
+    """R replicas of an ensemble of models (the reference's seed_idx < 0: energies and dE are the means over the trained
+    seeds, ``neuralce/nce/mc_model.py:181-188``), with the ``NCEState`` interface the drivers use.  Each model keeps
+    its own caches of the same occupancies; a step evaluates the swap on every model (``nce_nce_local_delta``), decides
+    on the mean dE (``nce_nce_accept``) and commits the decision on every model (``nce_nce_commit``), all on the
+    device.  Proposals and uniforms are the chunk kernels' (Philox keyed by seed, global step and temperature slot);
+    exchanges use the mean energies with the kernels' exchange counters."""
+
+    def __init__(self, models, sigma, beta_slot, ladder_id=None):
+        self.models = models
+        self.states = [NCEState(m, sigma, beta_slot, ladder_id) for m in models]
+        self.model = models[0]
+        s0 = self.states[0]
+        self.R, self.N = s0.R, s0.N
+        self.beta_slot, self.ladder_id = s0.beta_slot, s0.ladder_id
+
+    sigma = property(lambda self: self.states[0].sigma)
+    rep_of_slot = property(lambda self: self.states[0].rep_of_slot)
+    slot_of_rep = property(lambda self: self.states[0].slot_of_rep)
+    n_acc = property(lambda self: self.states[0].n_acc)
+    n_ex = property(lambda self: self.states[0].n_ex)
+    n_near = property(lambda self: self.states[0].n_near)
+
+    @property
+    def E(self):
+        return sum(s.E for s in self.states) / len(self.states)
+
+    def broadcast(self):
+        """copy the first model's occupancies, slots and counters to the others (after a restore)"""
+        for s in self.states[1:]:
+            for f in ("sigma", "rep_of_slot", "slot_of_rep", "n_acc", "n_ex"):
+                getattr(s, f).copy_(getattr(self.states[0], f))
+        return self
+
+    def full_cache(self, stream=None):
+        for s in self.states:
+            s.full_cache(stream)
+        return self
+
+    def check_errors(self):
+        for m in self.models:
+            m.check_errors()
+
+    def run_chunk(self, n_steps, step0, seed=0, sample_interval=1, E_samples=None, exchange_rounds=0, **_):
+        import torch
+        from .dist import exchange_slots
+        R, S, dev = self.R, len(self.models), self.sigma.device
+        i, j, u = proposal_block(self.model, seed, step0, n_steps, self.slot_of_rep.cpu().numpy())
+        pa, pb = torch.as_tensor(i, device=dev), torch.as_tensor(j, device=dev)
+        pu = torch.as_tensor(u, device=dev)
+        dE = torch.empty((S, R), dtype=torch.float64, device=dev)
+        acc = torch.empty(R, dtype=torch.int32, device=dev)
+        L = _lib.lib(); sp = _lib.stream_ptr()
+        structs = [C.byref(st.struct()) for st in self.states]
+        s0 = self.states[0]
+        for k in range(int(n_steps)):
+            for q, (m, st) in enumerate(zip(self.models, structs)):
+                _lib.check(L.nce_nce_local_delta(m.handle, st, pa[k].data_ptr(), pb[k].data_ptr(), dE[q].data_ptr(), sp),
+                           "nce_nce_local_delta")
+            _lib.check(L.nce_nce_accept(dE.data_ptr(), S, R, self.model.scale_eV, s0.beta_slot.data_ptr(),
+                                        s0.slot_of_rep.data_ptr(), pu[k].data_ptr(), acc.data_ptr(), sp), "nce_nce_accept")
+            for m, st in zip(self.models, structs):
+                _lib.check(L.nce_nce_commit(m.handle, st, acc.data_ptr(), sp), "nce_nce_commit")
+            if E_samples is not None and (k + 1) % sample_interval == 0:
+                E_samples[(k + 1) // sample_interval - 1] = self.E[self.rep_of_slot.long()]
+        if exchange_rounds and R > 1:
+            E_eV = self.E.cpu().numpy() * self.model.scale_eV
+            ros = self.rep_of_slot.cpu().numpy().astype(np.int64)
+            lid = self.ladder_id.cpu().numpy(); beta = self.beta_slot.cpu().numpy()
+            n_ex = 0
+            for q in range(int(exchange_rounds)):
+                ros, n = exchange_slots(E_eV, beta, lid, ros, seed, int(step0) + int(n_steps), q)
+                n_ex += n
+            sor = np.empty(R, np.int64); sor[ros] = np.arange(R)
+            for st in self.states:
+                st.rep_of_slot.copy_(torch.as_tensor(ros.astype(np.int32), device=dev))
+                st.slot_of_rep.copy_(torch.as_tensor(sor.astype(np.int32), device=dev))
+                st.n_ex += n_ex
+        return self
+
+
 def _swap_of(sig, flips):
     """(i, j) of a swap written as the reference's flips [[i, sig[j]], [j, sig[i]]]; anything else is refused."""
     f = np.asarray(flips.cpu() if hasattr(flips, "cpu") else flips, np.int64).reshape(-1, 2)
@@ -282,6 +363,44 @@ def _swap_of(sig, flips):
     if si != get(j) or sj != get(i):
         raise ValueError("this engine evaluates swaps: flips must be [[i, sig[j]], [j, sig[i]]]")
     return i, j
+
+
+def _philox_np(c0, c1, c2, c3, k0, k1):
+    """Philox4x32-10 on uint64 arrays holding 32-bit words (the counter-based generator the kernels use)."""
+    M = np.uint64(0xFFFFFFFF)
+    c0, c1, c2, c3 = (np.asarray(x, np.uint64) & M for x in (c0, c1, c2, c3))
+    k0, k1 = np.uint64(k0) & M, np.uint64(k1) & M
+    for rnd in range(10):
+        if rnd:
+            k0 = (k0 + np.uint64(0x9E3779B9)) & M; k1 = (k1 + np.uint64(0xBB67AE85)) & M
+        p0 = np.uint64(0xD2511F53) * c0; p1 = np.uint64(0xCD9E8D57) * c2
+        c0, c1, c2, c3 = ((p1 >> np.uint64(32)) ^ c1 ^ k0) & M, p1 & M, ((p0 >> np.uint64(32)) ^ c3 ^ k1) & M, p0 & M
+    return c0, c1, c2, c3
+
+
+def proposal_block(model, seed, step0, n_steps, slots):
+    """The chunk kernels' proposals and uniforms for global steps step0 .. step0 + n_steps - 1 of the given temperature
+    slots (Philox counters (step, slot), key = seed): (i, j) int32 and u float64, each (n_steps, len(slots))."""
+    slots = np.asarray(slots, np.uint64)
+    g = (np.uint64(step0) + np.arange(n_steps, dtype=np.uint64))[:, None] * np.ones(len(slots), np.uint64)[None]
+    t = np.broadcast_to(slots[None], g.shape)
+    k0, k1 = int(seed) & 0xFFFFFFFF, (int(seed) >> 32) & 0xFFFFFFFF
+    lo, hi = g & np.uint64(0xFFFFFFFF), g >> np.uint64(32)
+    x = _philox_np(lo, hi, t, 0, k0, k1)
+    act_b, act_nb, cum = model.keep["act_b"], model.keep["act_nb"].astype(np.uint64), model.keep["grp_cum"]
+    grp = np.zeros(g.shape, np.int64); ba = np.zeros(g.shape, np.uint64); bb = np.zeros(g.shape, np.uint64)
+    if len(act_nb) > 1 or act_nb[0] > 1:
+        y = _philox_np(lo, hi, t, 1, k0, k1)
+        for q in range(len(act_nb) - 1):
+            grp += (y[0] >= np.uint64(cum[q])) & (grp == q)
+        nb = act_nb[grp]
+        ba, bb = (y[1] * nb) >> np.uint64(32), (y[2] * nb) >> np.uint64(32)
+    n_cells, nB = np.uint64(int(model.desc.n_cells)), int(model.desc.nB)
+    i = ((x[0] * n_cells) >> np.uint64(32)).astype(np.int64) * nB + act_b[grp, ba.astype(np.int64)]
+    j = ((x[1] * n_cells) >> np.uint64(32)).astype(np.int64) * nB + act_b[grp, bb.astype(np.int64)]
+    m = (x[2] << np.uint64(21)) | (x[3] >> np.uint64(11))
+    u = (m + np.uint64(1)).astype(np.float64) * 2.0 ** -53
+    return i.astype(np.int32), j.astype(np.int32), u
 
 
 def propose_sites(model, key):
@@ -379,4 +498,5 @@ def setup(mdl, atoms: Structure, seed_idx=0, dtype="float32", table=None, mma=0)
                 propose=lambda key: propose_sites(model, key), perm=model.perm, inv_perm=model.inv_perm, implicit=True,
                 geo=model.geo, ensemble=len(models) > 1,
                 to_eV_per_atom=lambda E_std: E_std * ys + ym, dE_eV_total=lambda dE_std: dE_std * ys * n_atoms,
-                new_state=lambda sig, betas: NCEState(model, np.asarray(sig, np.int8), betas))
+                new_state=lambda sig, betas: (EnsembleState(models, np.asarray(sig, np.int8), betas) if len(models) > 1
+                                              else NCEState(model, np.asarray(sig, np.int8), betas)))

@@ -52,8 +52,9 @@ class Job:
 
 
 class Server:
-    """ce_kernel: 0 = CE jobs whose cell allows it run the local-field kernel (exact fixed-point dE; 8 more bytes of
-    device memory per site and replica), the rest the sign-parity kernel at ``precision``; 2 = sign parity for all."""
+    """ce_kernel: 0 = every CE job on the sign-parity kernel at ``precision``; 3 = jobs whose cell allows it on the
+    local-field kernel (exact fixed-point dE; 8 more bytes of device memory per site and replica), the rest on the
+    sign-parity kernel."""
 
     def __init__(self, hbm_budget=0, max_batch=64, precision=32, warps=8, nce_cluster=1, nce_streams=4, starve_s=5.0,
                  ce_kernel=0, ce_lf_warps=0):

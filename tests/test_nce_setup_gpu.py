@@ -128,3 +128,74 @@ def test_setup_ensemble_is_the_mean_of_the_seeds(cuda, nipt_model):
     de = float(ens["local_delta"](ce, sig, fl)[0])
     d0, d1 = float(one[0]["local_delta"](c0, sig, fl)[0]), float(one[1]["local_delta"](c1, sig, fl)[0])
     assert abs(de - 0.5 * (d0 + d1)) < 1e-9
+
+
+def _two_seed_model(mdl):
+    import copy
+    mdl2 = copy.deepcopy(mdl)
+    p1 = copy.deepcopy(mdl["params"][0]); rng = np.random.default_rng(1)
+    for L in p1["layers"]:
+        for k in L:
+            L[k] = np.asarray(L[k]) * (1.0 + 0.05 * rng.standard_normal(np.shape(L[k])))
+    mdl2["params"] = [mdl["params"][0], p1]
+    return mdl2
+
+
+def test_ensemble_chain_matches_oracle(cuda, nipt_model):
+    """seed_idx = -1 chains of 3 replicas (device local_delta on both seeds' models, accept on the mean dE, commit on
+    both) against the oracle's two models driven with the same proposals, uniforms and rule: occupancies bit-exact,
+    energies within the float32 bound; then a chunk-end exchange on the mean energies."""
+    torch = cuda
+    from neuralce_gb300.nce import expand_params, proposal_block, setup
+    from neuralce_gb300.workloads import ladder
+    from oracle.nce_oracle import NCEOracle
+    mdl, _ = nipt_model
+    mdl2 = _two_seed_model(mdl)
+    mc = setup(mdl2, random_cell((4, 4, 4), 6), seed_idx=-1)
+    R, T, seed = 3, 25, 17
+    _, beta = ladder(R, 500.0, 1200.0)
+    rng = np.random.default_rng(2)
+    sig = np.stack([mc["sig0"][rng.permutation(mc["n_atoms"])] for _ in range(R)]).astype(np.int8)
+    st = mc["new_state"](sig, beta).full_cache()
+    st.run_chunk(T, 0, seed=seed)
+    torch.cuda.synchronize()
+    st.check_errors()
+    orcs = []
+    for k in range(2):
+        P, mu, sd = expand_params(mdl2, k)
+        orcs.append(NCEOracle(mc["model"].geo, P, mu, sd, act="tanh", pool="mean"))
+    pi, pj, pu = proposal_block(mc["model"], seed, 0, T, np.arange(R))
+    scale = mc["model"].scale_eV
+    for r in range(R):
+        s = sig[r].astype(np.int64).copy()
+        caches = [o.full_cache(s) for o in orcs]
+        E = np.mean([o.energy_of(c) for o, c in zip(orcs, caches)])
+        nacc = 0
+        for k in range(T):
+            i, j = int(pi[k, r]), int(pj[k, r])
+            if s[i] == s[j]:
+                nacc += 1; continue
+            out = [o.local_delta(c, s, [(i, int(s[j])), (j, int(s[i]))]) for o, c in zip(orcs, caches)]
+            dEeV = np.mean([d for d, _ in out]) * scale
+            if dEeV <= 0 or pu[k, r] < np.exp(-float(beta[r]) * dEeV):
+                caches = [o.commit(c, p, True) for o, c, (_, p) in zip(orcs, caches, out)]
+                s[i], s[j] = s[j], s[i]; nacc += 1; E += dEeV / scale
+        assert np.array_equal(st.sigma[r].cpu().numpy(), s.astype(np.int8))
+        assert int(st.n_acc[r].item()) == nacc
+        assert abs(float(st.E[r].item()) - E) * scale < 1e-4
+    # a chunk that ends with exchange rounds keeps every model's slots in step
+    st.run_chunk(5, T, seed=seed, exchange_rounds=2)
+    torch.cuda.synchronize()
+    for s_ in st.states[1:]:
+        assert torch.equal(s_.rep_of_slot, st.rep_of_slot) and torch.equal(s_.sigma, st.sigma)
+
+
+def test_ensemble_driver_runs(cuda, nipt_model, tmp_path):
+    """The NeuralCE PT driver with seed_idx = -1 (the CLI's --model_seed -1) runs and writes its outputs."""
+    from neuralce_gb300.mc import nce_mc
+    mdl, _ = nipt_model
+    res = nce_mc.run_pt_mc(_two_seed_model(mdl), random_cell((3, 3, 3), 7), n_steps=60, T_min=500.0, T_max=1500.0,
+                           n_replicas=3, exchange_every=20, chunk=30, sample_interval=10, seed_idx=-1,
+                           out_dir=str(tmp_path))
+    assert (tmp_path / "energies.npz").exists() and (tmp_path / "final_sigma.npy").exists()
+    assert res["n_replicas"] == 3 and np.isfinite(res["E_final"]).all()

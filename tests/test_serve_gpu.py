@@ -44,17 +44,20 @@ def _same(a, b):
     assert a["n_ex"] == b["n_ex"]
 
 
-def test_results_same_alone_and_in_mix(cuda):
+@pytest.mark.parametrize("ce_kernel", [0, 3])
+def test_results_same_alone_and_in_mix(cuda, ce_kernel):
+    """ce_kernel 3: the two larger CE cells run the local-field kernel, the two smaller (aliasing) ones the sign-parity
+    kernel, in separate launches of the same rounds."""
     from neuralce_gb300.serve import Server
     jobs = _ce_jobs() + _nce_jobs()
     alone = []
-    with Server(precision=32) as srv:
+    with Server(precision=32, ce_kernel=ce_kernel) as srv:
         for j in jobs:
             h = _submit(srv, j)
             info, = srv.wait([h], timeout=300)
             assert info["status"] == "done", info
             alone.append(h.result())
-    with Server(precision=32) as srv:
+    with Server(precision=32, ce_kernel=ce_kernel) as srv:
         hs = [_submit(srv, j) for j in jobs]
         infos = srv.wait(hs, timeout=300)
         assert all(i["status"] == "done" for i in infos), infos
@@ -70,11 +73,11 @@ def test_results_same_alone_and_in_mix(cuda):
         assert int(a["n_acc"].sum()) > 0
 
 
-@pytest.mark.parametrize("ce_kernel", [2, 0])
+@pytest.mark.parametrize("ce_kernel", [0, 3])
 def test_ce_job_equals_direct_chunks(cuda, ce_kernel):
     """A served CE job = the chunk API driven by hand: chunks of the exchange interval, exact re-anchor of the
-    carried energies from the tracked cluster-vector sums after every chunk; ce_kernel 2: sign parity in fp32,
-    ce_kernel 0: the local-field kernel (exact fixed point) on this cell."""
+    carried energies from the tracked cluster-vector sums after every chunk; ce_kernel 0: sign parity in fp32,
+    ce_kernel 3: the local-field kernel (exact fixed point) on this cell."""
     torch = cuda
     from neuralce_gb300.pt import PTState, run_chunk
     from neuralce_gb300.serve import Server
@@ -82,7 +85,7 @@ def test_ce_job_equals_direct_chunks(cuda, ce_kernel):
     gce, R = j["model"], len(j["beta"])
     E0 = gce.batched_energy(torch.as_tensor(j["sigma"]).cuda()).cpu().numpy()
     st = PTState(j["sigma"], E0, j["beta"], np.zeros(R, np.int32)).track_counts(gce)
-    lf = ce_kernel == 0
+    lf = ce_kernel == 3
     assert gce.has_local_field
     if lf:
         st.enable_field(gce)
