@@ -292,22 +292,22 @@ def bench_batch(steps=3, warmup=1, chunk=5000, reanchor=10000, n_jobs=64, alone_
     exchange at each chunk end) and the exact float64 re-anchor of every carried energy from the tracked
     cluster-vector sums.  Compared with the plain float64 kernels running the first ``alone_jobs`` jobs alone."""
     import torch
-    from neuralce_gb300.batch import CEBatch, tune_warps
+    from neuralce_gb300.batch import CEBatch, tune_launch
     from neuralce_gb300.pt import PTState, run_chunk
     from neuralce_gb300.workloads import ce_batch_config
     from neuralce_gb300.autotune import best_warps
     t0 = time.time()
     jobs = ce_batch_config(n_jobs)
     setup = time.time() - t0
-    w, tune = tune_warps(jobs, 32)
+    (w, cl), tune = tune_launch(jobs, 32)
     # float32 drift between re-anchors and exactness of the float64 re-anchor, measured eagerly on a copy
-    chk = CEBatch(jobs, precision=32, warps=w)
+    chk = CEBatch(jobs, precision=32, warps=w, cluster=cl)
     for _ in range(reanchor // chunk):
         chk.run_chunk(chunk)
     drift = chk.reanchor()
     full_err = max(float((j["gce"].batched_energy(st.sigma) - st.E).abs().max().item()) for j, st in zip(jobs, chk.states))
     del chk
-    b = CEBatch(jobs, precision=32, warps=w).capture(chunk, chunks=max(1, reanchor // chunk), reanchor=True)
+    b = CEBatch(jobs, precision=32, warps=w, cluster=cl).capture(chunk, chunks=max(1, reanchor // chunk), reanchor=True)
     for _ in range(warmup):
         b.replay()
     torch.cuda.synchronize()
@@ -340,7 +340,8 @@ def bench_batch(steps=3, warmup=1, chunk=5000, reanchor=10000, n_jobs=64, alone_
             "fp64_single_job_alone": alone[1], "ratio_vs_fp64_single_job": value / alone[1],
             "fp64_sign_parity_single_job_alone": alone[2], "ratio_vs_fp64_sign_parity_single_job": value / alone[2],
             "max_fp32_drift_before_reanchor_eV": drift, "max_reanchored_vs_full_recompute_eV": full_err,
-            "warps_per_replica": w, "autotune_ms": tune, "setup_s": setup}
+            "warps_per_replica": w, "ctas_per_replica_of_split_jobs": cl,
+            "autotune_ms": {f"{a}x{b_}": round(v, 3) for (a, b_), v in tune.items()}, "setup_s": setup}
 
 
 def bench_serve(seconds=10.0, rate=50.0, ce_scale=0.01, nce_scale=0.0002, nce_max_sites=32768, seed=4, alone_jobs=0,

@@ -151,6 +151,9 @@ typedef struct {
                               2 eci Pi, in the float64 kernels' fixed point (exact integers).  When set (and the cell
                               supports it, nce_ce_has_local_field), precision-64 chunks run the local-field kernel and
                               keep the fields current; fill it with nce_ce_field_init after (re)setting sigma. */
+    int32_t *ex_sync;      /* (1) or NULL: a counter, 0 between chunks.  When every job of a launch has one, the chunk-
+                              end exchange (and the step_dev advance) runs inside the chunk kernel: the last replica
+                              of a job to finish performs it and resets the counter; otherwise a second kernel does. */
 } nce_pt_state;
 
 /* One chunk of steps.  Proposals: host-supplied stream (prop_a/prop_b/prop_u device arrays indexed

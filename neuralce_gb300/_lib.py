@@ -29,7 +29,7 @@ class NceCeTables(C.Structure):
 class NcePtState(C.Structure):
     _fields_ = [("R", i32), ("N", i64), ("sigma", vp), ("E", vp), ("beta_slot", vp), ("rep_of_slot", vp),
                 ("slot_of_rep", vp), ("ladder_id", vp), ("E_min_rep", vp), ("n_acc", vp), ("n_ex", vp), ("cv", vp),
-                ("n_near", vp), ("field", vp)]
+                ("n_near", vp), ("field", vp), ("ex_sync", vp)]
 
 
 class NcePtChunk(C.Structure):

@@ -15,6 +15,7 @@ from . import _lib
 from .pt import PTState, make_chunk
 
 MAX_JOBS = 64
+SPLIT_SITES = 48 * 1024       # a job whose occupancy fits the batch kernel's per-job shared memory can be split over CTAs
 
 
 class CEBatch:
@@ -35,16 +36,27 @@ class CEBatch:
         self.warps = warps if warps else 8
         self.step = 0
 
+    def launch_groups(self):
+        """(job indices, CTAs per replica) of each launch: with a split (cluster > 1) the jobs whose occupancy fits the
+        per-job shared memory are launched split over thread-block clusters, the larger ones one CTA per replica;
+        at most 64 jobs per launch."""
+        if self.cluster <= 1:
+            idx = [(list(range(len(self.jobs))), 1)]
+        else:
+            small = [k for k, j in enumerate(self.jobs) if j["gce"].n_atoms <= SPLIT_SITES]
+            large = [k for k, j in enumerate(self.jobs) if j["gce"].n_atoms > SPLIT_SITES]
+            idx = [(g, c) for g, c in ((small, self.cluster), (large, 1)) if g]
+        return [(g[a:a + MAX_JOBS], c) for g, c in idx for a in range(0, len(g), MAX_JOBS)]
+
     def run_chunk(self, n_steps, do_exchange=True, stream=None, step_dev=None):
-        """one chunk of every job, 64 jobs per launch.  step_dev: (n_jobs,) int64 device step counters that the
-        launch reads and advances (used inside captured graphs) instead of the host step."""
-        for a in range(0, len(self.jobs), MAX_JOBS):
-            js = list(range(a, min(a + MAX_JOBS, len(self.jobs))))
+        """one chunk of every job (launch_groups).  step_dev: (n_jobs,) int64 device step counters that the launch
+        reads and advances (used inside captured graphs) instead of the host step."""
+        for js, cl in self.launch_groups():
             n = len(js)
             hs = (C.c_void_p * n)(*[self.jobs[k]["gce"].handle.value for k in js])
             ss = (_lib.NcePtState * n)(*[self.states[k].struct() for k in js])
             cks = (_lib.NcePtChunk * n)(*[make_chunk(n_steps, self.step, self.seeds[k], self.precision, self.warps, None, 1, None,
-                                                     do_exchange, path=self.path, cluster=self.cluster) for k in js])
+                                                     do_exchange, path=self.path, cluster=cl) for k in js])
             if step_dev is not None:
                 for i, k in enumerate(js):
                     cks[i].step_dev = step_dev.data_ptr() + 8 * k
@@ -102,16 +114,25 @@ class CEBatch:
         return sum(int(j["R"]) for j in self.jobs)
 
 
-def tune_warps(jobs, precision=32, candidates=(4, 8, 16, 32), steps=200):
-    """Autotune warps per replica for a batch: time a short chunk of the real batch for each candidate on
-    scratch states."""
+def tune_launch(jobs, precision=32, warps=(4, 8, 16, 32), clusters=(1, 2, 4), steps=200):
+    """Autotune a batch's launch shape, warps per CTA and the split (CTAs per replica of the jobs that can be split):
+    time a short chunk of the real batch for each candidate on scratch states.  Returns ((warps, cluster), {...: ms})."""
     import torch
-    best, times = None, {}
-    for w in candidates:
-        b = CEBatch(jobs, precision, w)
-        b.run_chunk(10, False)
-        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s0.record(); b.run_chunk(steps, False); s1.record(); torch.cuda.synchronize()
-        times[w] = s0.elapsed_time(s1)
-    best = min(times, key=times.get)
-    return best, times
+    times = {}
+    for cl in clusters:
+        for w in warps:
+            b = CEBatch(jobs, precision, w, track=False, cluster=cl)
+            try:
+                b.run_chunk(10, False)
+            except _lib.NceError:
+                continue                                   # a split that does not launch on this GPU
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(); b.run_chunk(steps, False); s1.record(); torch.cuda.synchronize()
+            times[(w, cl)] = s0.elapsed_time(s1)
+    return min(times, key=times.get), times
+
+
+def tune_warps(jobs, precision=32, candidates=(4, 8, 16, 32), steps=200):
+    """Warps per replica for a batch with one CTA per replica: (warps, {warps: ms})."""
+    (w, _), t = tune_launch(jobs, precision, candidates, (1,), steps)
+    return w, {k[0]: v for k, v in t.items()}

@@ -47,7 +47,7 @@ struct CEJob {
     int32_t d0, d1, d2;
     int64_t n_cells, N;
     // state
-    int8_t *sigma; double *E; const float *beta_slot; const int32_t *slot_of_rep;
+    int8_t *sigma; double *E; const float *beta_slot; int32_t *slot_of_rep;
     double *E_min_rep; int64_t *n_acc;
     int32_t R;
     // chunk
@@ -80,6 +80,10 @@ struct CEJob {
     const int16_t *lf_box; // (nB, 2e0+1, 2e1+1, 2e2+1, nB) neighbour index of a displacement, or -1
     int32_t lf_e0, lf_e1, lf_e2, lf_nidx;
     int32_t gf_smem;       // this job's occupancy and field are copied into shared memory for the chunk
+    // chunk-end exchange inside the chunk kernel (fused_chunk_end), when ex_sync is set
+    int32_t *rep_of_slot; const int32_t *ladder_id; int64_t *n_ex; const double *ex_u;
+    int32_t *ex_sync;      // replicas of the job done with the chunk (0 between chunks)
+    int32_t ex_flags;      // bit 0: the chunk ends on an exchange; bit 1: host parity (with ex_u)
 };
 
 struct CEBatch {
@@ -87,6 +91,7 @@ struct CEBatch {
     int32_t tables_in_smem;
     CEJob job[kMaxJobs];
 };
+static_assert(sizeof(CEBatch) <= 32764, "the batch descriptor is passed by value: kernel parameters hold 32,764 bytes");
 
 struct CEShared {          // per-step control block (shared memory)
     int64_t ia, ib;
@@ -256,6 +261,44 @@ __device__ __forceinline__ void propose(const CEJob &jb, int64_t g, int32_t t, i
     u = draw_u01(x.z, x.w);
 }
 
+// Chunk end, called by one thread of each replica (the cluster's first CTA) once its outputs are written: the last
+// replica of the job to arrive performs the job's slot exchange -- the rule, random counters and sample rewrite of
+// ce_exchange_kernel, with the pairs swapped in place -- advances the device step counter and re-arms the counter.
+// No thread waits for another, so the chunk kernel never depends on its CTAs running at the same time.
+__device__ void fused_chunk_end(const CEJob &jb, int64_t g0) {
+    __threadfence();                                      // this replica's energy is visible before it is counted
+    if (atomicAdd(jb.ex_sync, 1) != jb.R - 1) return;
+    __threadfence();
+    const int R = jb.R;
+    const int64_t g_end = g0 + jb.n_steps;
+    if (jb.step_dev) *const_cast<int64_t *>(jb.step_dev) = g_end;   // every CTA of the job has read it by now
+    if ((jb.ex_flags & 1) && R > 1) {
+        const uint32_t k0 = (uint32_t)jb.seed, k1 = (uint32_t)(jb.seed >> 32);
+        const uint32_t c0 = (uint32_t)g_end, c1 = (uint32_t)((uint64_t)g_end >> 32);
+        const uint32_t cq = 0xFFFFFFFFu;                   // round 0 of the exchange counters
+        const int parity = jb.ex_u ? ((jb.ex_flags >> 1) & 1) : (int)(philox4x32(c0, c1, cq, 0u, k0, k1).x & 1u);
+        int32_t *ros = jb.rep_of_slot;
+        int64_t nswap = 0;
+        for (int k = 0; 2 * k < R - 1; ++k) {
+            const int a = 2 * k + parity, b = a + 1;
+            if (b >= R || jb.ladder_id[a] != jb.ladder_id[b]) continue;
+            const double Ea = __ldcg(jb.E + __ldcg(ros + a)), Eb = __ldcg(jb.E + __ldcg(ros + b));
+            const double log_acc = ((double)jb.beta_slot[b] - (double)jb.beta_slot[a]) * (Eb - Ea);
+            double u;
+            if (jb.ex_u) u = jb.ex_u[k];
+            else { const u32x4 w = philox4x32(c0, c1, cq - 1u, (uint32_t)k, k0, k1); u = draw_u01(w.x, w.y); }
+            if (log(u) < log_acc) { const int32_t x = ros[a]; ros[a] = ros[b]; ros[b] = x; ++nswap; }
+        }
+        for (int q = 0; q < R; ++q) jb.slot_of_rep[ros[q]] = q;
+        *jb.n_ex += nswap;
+        if (jb.E_samples && jb.n_steps > 0 && jb.n_steps % jb.sample_interval == 0) {
+            const int64_t row = jb.n_steps / jb.sample_interval - 1;
+            for (int q = 0; q < R; ++q) jb.E_samples[row * R + q] = __ldcg(jb.E + ros[q]);
+        }
+    }
+    *jb.ex_sync = 0;
+}
+
 template <typename Real, int MO>
 __global__ void __launch_bounds__(1024) ce_pt_chunk_kernel(const __grid_constant__ CEBatch bt) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -313,6 +356,7 @@ __global__ void __launch_bounds__(1024) ce_pt_chunk_kernel(const __grid_constant
     if (threadIdx.x == 0) {
         jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc;
         if (jb.n_near) jb.n_near[r] += nnear;
+        if (jb.ex_sync) fused_chunk_end(jb, g0);
     }
 }
 
@@ -632,12 +676,14 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     if (rank == 0) {
         if (sig_smem)
             for (int64_t i = tid; i < jb.N; i += nt) gsig[i] = sig[i];
+        if (track)
+            for (int c = tid; c < n_cols; c += nt) jb.cv[(int64_t)r * n_cols + c] += dcv[c];
+        if (sig_smem || track) __syncthreads();          // the replica's outputs are written before it is counted
         if (tid == 0) {
             jb.E[r] = E; jb.E_min_rep[r] = Emin; jb.n_acc[r] += nacc;
             if (jb.n_near) jb.n_near[r] += nnear;
+            if (jb.ex_sync) fused_chunk_end(jb, g0);
         }
-        if (track)
-            for (int c = tid; c < n_cols; c += nt) jb.cv[(int64_t)r * n_cols + c] += dcv[c];
     }
     if (CLUSTER) cg::this_cluster().sync();              // no CTA leaves while others may still add into its counters
 }
@@ -997,16 +1043,18 @@ __global__ void __launch_bounds__(32 * kLfMaxWarps) ce_lf_chunk_kernel(const __g
     }
     (void)nrow_a_max;
     if (warp == 0) nnear = __reduce_add_sync(0xffffffffu, nnear);   // each lane counted the steps it decided
+    if (jb.gf_smem)
+        for (int64_t i = tid; i < jb.N; i += nt) { gsig[i] = sig[i]; gfld[i] = G[i]; }
+    if (track)
+        for (int c = tid; c < n_cols; c += nt) jb.cv[(int64_t)r * n_cols + c] += dcv[c];
+    __syncthreads();                                       // the replica's outputs are written before it is counted
     if (tid == 0) {
         jb.E[r] = E0c + (double)dsum * fscale;
         jb.E_min_rep[r] = fmin(Emin, E0c + (double)dmin * fscale);
         jb.n_acc[r] += nacc;
         if (jb.n_near) jb.n_near[r] += nnear;
+        if (jb.ex_sync) fused_chunk_end(jb, g0);
     }
-    if (jb.gf_smem)
-        for (int64_t i = tid; i < jb.N; i += nt) { gsig[i] = sig[i]; gfld[i] = G[i]; }
-    if (track)
-        for (int c = tid; c < n_cols; c += nt) jb.cv[(int64_t)r * n_cols + c] += dcv[c];
 }
 
 // Full energy on the sign-parity tables, bit-sliced.  The occupancies become bit planes: per replica, point-
@@ -1404,11 +1452,13 @@ static CEJob make_job(const nce_ce_model *m, const nce_pt_state *st, const nce_p
         j.sigma = st->sigma; j.E = st->E; j.beta_slot = st->beta_slot; j.slot_of_rep = st->slot_of_rep;
         j.E_min_rep = st->E_min_rep; j.n_acc = st->n_acc; j.R = st->R; j.cv = st->cv; j.n_near = st->n_near;
         j.field = st->field;
+        j.rep_of_slot = st->rep_of_slot; j.ladder_id = st->ladder_id; j.n_ex = st->n_ex; j.ex_sync = st->ex_sync;
     }
     if (ck) {
         j.n_steps = ck->n_steps; j.step0 = ck->step0; j.step_dev = ck->step_dev; j.prop_a = ck->prop_a; j.prop_b = ck->prop_b; j.prop_u = ck->prop_u;
         j.seed = ck->seed; j.sample_interval = ck->sample_interval > 0 ? ck->sample_interval : 1;
         j.E_samples = ck->E_samples;
+        j.ex_u = ck->ex_u; j.ex_flags = (ck->do_exchange ? 1 : 0) | ((ck->ex_parity & 1) << 1);
         j.lf_off = m->lf_off; j.lf_idx = m->lf_idx; j.lf_box = m->lf_box;
         j.lf_e0 = m->lf_e[0]; j.lf_e1 = m->lf_e[1]; j.lf_e2 = m->lf_e[2]; j.lf_nidx = m->lf_nidx;
         j.near_eV = ck->near_eV > 0.0 ? ck->near_eV : (p64 ? 1e-9 : 1e-6);
@@ -1618,9 +1668,14 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
         }
     }
     bt.tables_in_smem = all_fit ? 1 : 0;
+    // the chunk-end exchange runs inside the chunk kernel when every job has a counter and steps to run; otherwise
+    // no job counts and the exchange kernel follows the launch
+    bool fused = true;
+    for (int j = 0; j < n_jobs; ++j) fused = fused && sts[j].ex_sync != nullptr && cks[j].n_steps > 0;
     int base = 0;
     for (int j = 0; j < n_jobs; ++j) {
         bt.job[j] = make_job(hs[j], &sts[j], &cks[j], base, use_bin);
+        if (!fused) bt.job[j].ex_sync = nullptr;
         bt.job[j].sig_smem = (use_bin && sig_smem > 0 && hs[j]->N <= sig_smem) ? 1 : 0;
         bt.job[j].gf_smem = (use_lf && lf_budget > 0 && hs[j]->N <= lf_budget) ? 1 : 0;
         base += sts[j].R;
@@ -1647,7 +1702,7 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
                                  : launch_chunk<float>(bt, mo, total, warps, smem, s);
         if (rc) return rc;
     }
-    // exchange
+    if (fused) return NCE_OK;                            // the chunk kernel exchanged
     CEExBatch ex; std::memset(&ex, 0, sizeof(ex));
     ex.n_jobs = n_jobs;
     bool any = false;

@@ -106,6 +106,8 @@ class PTState:
         self.n_ex = torch.zeros(1, dtype=torch.int64, device=device)
         self.n_near = torch.zeros(R, dtype=torch.int64, device=device)   # near-threshold steps (stated dE bound)
         self.field = None                                                  # local fields (enable_field)
+        # chunk-end exchange inside the chunk kernel (the counter of replicas done); None: a separate exchange launch
+        self.ex_sync = torch.zeros(1, dtype=torch.int32, device=device)
         self._min = torch.zeros(1, dtype=torch.float64, device=device)
         self._arg = torch.zeros(1, dtype=torch.int32, device=device)
         self.cv = None
@@ -140,6 +142,7 @@ class PTState:
             setattr(s, f, getattr(self, f).data_ptr())
         s.cv = self.cv.data_ptr() if self.cv is not None else None
         s.field = self.field.data_ptr() if self.field is not None else None
+        s.ex_sync = self.ex_sync.data_ptr() if self.ex_sync is not None else None
         return s
 
     def minimum(self, stream=None):

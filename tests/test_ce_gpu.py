@@ -572,3 +572,50 @@ def test_local_field_large_cell_single_job(cuda):
     torch.cuda.synchronize()
     _compare(st, ref, 1e-9)
     assert torch.equal(st.field, gce.field_init(st.sigma))
+
+
+def test_batch_split_equals_unsplit(cuda):
+    """A batch launched with a split (small jobs over 2-CTA clusters, the large one a CTA per replica, two launches per
+    chunk) gives every job the trajectory of the unsplit batch."""
+    torch = cuda
+    from neuralce_gb300.batch import CEBatch
+    from neuralce_gb300.workloads import ce_config, ladder, replica_configs
+    jobs = []
+    for k, (L, R) in enumerate([(3, 4), (24, 3), (5, 2)]):
+        gce, sig = ce_config(L, seed=130 + k)
+        _, beta = ladder(R)
+        jobs.append({"gce": gce, "sigma": replica_configs(sig, R, 131 + k), "beta": beta, "R": R, "N": gce.n_atoms})
+    a = CEBatch(jobs, precision=32, warps=8, cluster=1)
+    b = CEBatch(jobs, precision=32, warps=8, cluster=2)
+    assert [c for _, c in b.launch_groups()] == [2, 1]
+    for _ in range(2):
+        a.run_chunk(300); b.run_chunk(300)
+    torch.cuda.synchronize()
+    for x, y in zip(a.states, b.states):
+        assert torch.equal(x.sigma, y.sigma) and torch.equal(x.E, y.E) and torch.equal(x.rep_of_slot, y.rep_of_slot)
+        assert torch.equal(x.cv, y.cv)
+
+
+@pytest.mark.parametrize("path", [1, 2, 3])
+def test_fused_exchange_equals_exchange_kernel(cuda, path):
+    """The chunk-end exchange inside the chunk kernel (the last replica to finish performs it) equals the separate
+    exchange launch: three chunks with exchanges and energy samples, host exchange uniforms in the middle one."""
+    torch = cuda
+    from neuralce_gb300.pt import run_chunk
+    R, T = 12, 500
+    gce, orc, sig_r, beta = _setup(5, seed=41, R=R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    a = _engine_state(sig_r, E0, beta); b = _engine_state(sig_r, E0, beta)
+    b.ex_sync = None                                       # the separate exchange kernel
+    if path == 3:
+        a.enable_field(gce); b.enable_field(gce)
+    for c in range(3):
+        Ea = torch.zeros((T // 50, R), dtype=torch.float64, device="cuda"); Eb = torch.zeros_like(Ea)
+        exu = torch.as_tensor(1.0 - np.random.default_rng(c).random(R // 2)).cuda() if c == 1 else None
+        for st, Es in ((a, Ea), (b, Eb)):
+            run_chunk(gce, st, T, c * T, 2024, 64, 8, None, 50, Es, True, c % 2, exu, path=path)
+        torch.cuda.synchronize()
+        assert torch.equal(a.rep_of_slot, b.rep_of_slot) and torch.equal(a.slot_of_rep, b.slot_of_rep)
+        assert torch.equal(a.n_ex, b.n_ex) and torch.equal(Ea, Eb) and torch.equal(a.E, b.E)
+        assert int(a.ex_sync.item()) == 0
+    assert int(a.n_ex.item()) > 0
