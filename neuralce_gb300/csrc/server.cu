@@ -203,8 +203,7 @@ int start_ce(nce_server *S, SJob &j, cudaStream_t s) {
         if (rc) return rc;
     }
     NCE_CUDA(cudaMemcpyAsync(st.E_min_rep, st.E, 8, cudaMemcpyDeviceToDevice, s));   // replica 0, as PT set-up does
-    NCE_CUDA(cudaStreamSynchronize(s));                                            // host copies may be freed now
-    return NCE_OK;
+    return NCE_OK;                 // the io thread synchronises once for all the jobs it admits in one pass
 }
 
 int start_nce(nce_server *S, SJob &j, cudaStream_t s) {
@@ -235,7 +234,8 @@ int start_nce(nce_server *S, SJob &j, cudaStream_t s) {
     return NCE_OK;
 }
 
-// copy the outputs to the caller's buffers and return the device memory (worker thread, job's stream)
+// copy the outputs to the caller's buffers and return the device memory (worker thread, job's stream); the caller
+// synchronises the stream, then checks the model's error flags (finish_check)
 int finish(SJob &j, cudaStream_t s) {
     const int32_t R = j.d.R;
     const bool ce = j.d.kind == NCE_JOB_CE;
@@ -250,8 +250,12 @@ int finish(SJob &j, cudaStream_t s) {
     if (j.d.rep_of_slot_out) NCE_CUDA(cudaMemcpyAsync(j.d.rep_of_slot_out, ros, 4 * (size_t)R, cudaMemcpyDeviceToHost, s));
     if (j.d.n_ex_out) NCE_CUDA(cudaMemcpyAsync(j.d.n_ex_out, nx, 8, cudaMemcpyDeviceToHost, s));
     NCE_CUDA(cudaFreeAsync(j.dev, s));
-    NCE_CUDA(cudaStreamSynchronize(s));
-    // a device error flag on the job's model fails the job (the flags stay set for the model's other jobs)
+    return NCE_OK;
+}
+
+// a device error flag on the job's model fails the job (the flags stay set for the model's other jobs)
+int finish_check(SJob &j) {
+    const bool ce = j.d.kind == NCE_JOB_CE;
     int32_t flags = 0;
     const int rc = ce ? ce_error_peek((nce_ce_handle)j.d.model, &flags) : nce_error_peek((nce_nce_handle)j.d.model, &flags);
     if (rc) return rc;
@@ -283,11 +287,20 @@ void io_worker(nce_server *S, int kind) {
                 S->wake.wait_for(lk, std::chrono::milliseconds(2));
             }
         }
-        for (auto &p : out) {
-            SJob &j = *p;
-            int rc = NCE_OK;
+        // retire: every finished job's outputs queued on the io stream, one synchronisation, then each job's flags
+        std::vector<int> frc(out.size(), NCE_OK);
+        for (size_t k = 0; k < out.size(); ++k)
+            if (!out[k]->cancel) frc[k] = finish(*out[k], ios);
+        if (!out.empty()) {
+            const cudaError_t e = cudaStreamSynchronize(ios);
+            for (size_t k = 0; k < out.size(); ++k)
+                if (!out[k]->cancel && frc[k] == NCE_OK)
+                    frc[k] = e != cudaSuccess ? fail(NCE_ERR_CUDA, "retiring a job: %s", cudaGetErrorString(e)) : finish_check(*out[k]);
+        }
+        for (size_t k = 0; k < out.size(); ++k) {
+            SJob &j = *out[k];
+            int rc = frc[k];
             if (j.cancel) drop(j, ios);
-            else rc = finish(j, ios);
             std::lock_guard<std::mutex> lk(S->mu);
             j.dev = reinterpret_cast<char *>(1);
             if (j.cancel) {
@@ -299,12 +312,24 @@ void io_worker(nce_server *S, int kind) {
                 release_locked(S, j, NCE_JOB_DONE);
             }
         }
-        for (auto &p : fresh) {
+        // admit: CE jobs' set-up queued on the io stream for all of them, one synchronisation (host copies of the
+        // inputs live in the jobs until then); NeuralCE jobs one at a time on their model's stream
+        std::vector<int> src(fresh.size(), NCE_OK);
+        if (kind == 0) {
+            for (size_t k = 0; k < fresh.size(); ++k) src[k] = start_ce(S, *fresh[k], ios);
+            if (!fresh.empty()) {
+                const cudaError_t e = cudaStreamSynchronize(ios);
+                if (e != cudaSuccess)
+                    for (auto &r : src) if (r == NCE_OK) r = fail(NCE_ERR_CUDA, "admitting a job: %s", cudaGetErrorString(e));
+            }
+        }
+        for (size_t k = 0; k < fresh.size(); ++k) {
+            auto &p = fresh[k];
             SJob &j = *p;
             int rc;
             cudaStream_t s = ios;
             if (kind == 0) {
-                rc = start_ce(S, j, s);
+                rc = src[k];
             } else {
                 // jobs on one model share its scratch buffers, so they share a stream (set-up included)
                 {
