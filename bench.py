@@ -345,15 +345,15 @@ def bench_batch(steps=3, warmup=1, chunk=5000, reanchor=10000, n_jobs=64, alone_
 
 
 def bench_serve(seconds=10.0, rate=50.0, ce_scale=0.01, nce_scale=0.0002, nce_max_sites=32768, seed=4, alone_jobs=0,
-                ce_exchange=500, nce_exchange=20, nce_mma=2):
+                ce_exchange=500, nce_exchange=20, nce_mma=4):
     """Configuration 4 (serving), scaled: Poisson arrivals at ``rate`` jobs/s for ``seconds``, CE or NeuralCE 50/50,
     sites log-uniform 256..1,048,576 (NeuralCE capped at ``nce_max_sites``), x_Pt ~ U[0.1, 0.9], R ~ U{8..128},
     steps log-uniform 10k..1M times ``ce_scale`` / ``nce_scale``.  Jobs are submitted to the job server at their
     arrival times (models and occupancies prepared beforehand); reports p50/p99 job latency (submission to
     results on the host) and the aggregate swap attempts/s over the makespan.  Capacity: the stream's CE jobs
     submitted at once, against the same jobs run one after another in the plain float64 kernel (``alone_jobs``
-    limits that to the first jobs; 0 = all).  NeuralCE jobs run the precision form ``nce_mma`` (2: bf16 operands on
-    the tcgen05 tensor cores, float32 accumulation)."""
+    limits that to the first jobs; 0 = all).  NeuralCE jobs run the precision form ``nce_mma`` (4: split bf16 operands on
+    the tcgen05 tensor cores, float32 accumulation, within 1e-4 eV per swap; 2: plain bf16)."""
     import torch
     from neuralce_gb300.pt import PTState, run_chunk
     from neuralce_gb300.serve import Server

@@ -189,6 +189,7 @@ def _run_replicas(mc, betas, n_steps, seed, chunk, log_every, sample_interval, o
     return dict(steps_per_s=float(R * chunk * (n_chunks - c0) / max(wall, 1e-9)), n_replicas=R, n_steps=int(n_steps),
                 chunk=int(chunk), E_final=[float(x) for x in E_chunk[-1]], acc_mean=float(acc_chunk.mean()),
                 drift_max=float(np.max(drift_log)), exchange_acc=(n_ex / n_try if n_try else None),
+                near_threshold_steps=int(st.n_near.sum().item()),
                 model_depth=int(mc["depth"]), n_atoms=int(N))
 
 

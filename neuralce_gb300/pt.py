@@ -68,6 +68,9 @@ class MCMCResult:
     E_min: float
     spins_final: Optional[np.ndarray]
     wall_time: float
+    # steps whose Metropolis margin |dE + ln(u)/beta| was below the precision form's stated dE bound (a decision there
+    # may differ from a float64 reference's); not in the reference's result
+    near_threshold_steps: int = 0
 
 
 def make_temperature_ladder(T_min, T_max, n_replicas):
@@ -342,7 +345,8 @@ def run_pt_mcmc(gce, cfg: MCMCConfig, verbose=True):
     swap_rate = float(st.n_acc.sum().item()) / max(1, n_sw)
     ex_rate = float(st.n_ex.item()) / max(1, n_ex_att)
     log(f"\nDone in {wall:.1f}s  ({n_sw / max(wall, 1e-9):,.0f} swap attempts/s)\n  swap acceptance     : {swap_rate:.4f}\n"
-        f"  exchange acceptance : {ex_rate:.4f}\n  E_min (production)  : {E_min:.4f}", flush=True)
+        f"  exchange acceptance : {ex_rate:.4f}\n  E_min (production)  : {E_min:.4f}\n"
+        f"  near-threshold steps: {int(st.n_near.sum().item())}", flush=True)
     np.savez(os.path.join(cfg.output_dir, "energies.npz"), energies=energy_samples[:si_], temperatures=temps,
              ladder_id=lid, n_atoms=np.int32(gce.n_atoms), swap_accept_rate=swap_rate, exchange_accept_rate=ex_rate,
              flip_accept_rate=0.0, E_min=E_min, wall_time=wall)
@@ -351,7 +355,7 @@ def run_pt_mcmc(gce, cfg: MCMCConfig, verbose=True):
     smin = sigma_min.cpu().numpy()[gce.inv_perm]
     res = MCMCResult(energies=energy_samples[:si_], temperatures=temps.astype(np.float32), swap_accept_rate=swap_rate,
                      flip_accept_rate=0.0, exchange_accept_rate=ex_rate, sigma_final=sigma_final, sigma_min=smin,
-                     E_min=E_min, spins_final=None, wall_time=wall)
+                     E_min=E_min, spins_final=None, wall_time=wall, near_threshold_steps=int(st.n_near.sum().item()))
     np.savez(os.path.join(cfg.output_dir, "mcmc_result.npz"), energies=res.energies, temperatures=res.temperatures,
              ladder_id=lid, ladder_pos=lpos, n_ladders=np.int32(n_ladders), sigma_final=res.sigma_final,
              sigma_min=res.sigma_min, E_min=res.E_min, spins_final=np.array([]), swap_accept_rate=swap_rate,

@@ -619,3 +619,34 @@ def test_fused_exchange_equals_exchange_kernel(cuda, path):
         assert torch.equal(a.n_ex, b.n_ex) and torch.equal(Ea, Eb) and torch.equal(a.E, b.E)
         assert int(a.ex_sync.item()) == 0
     assert int(a.n_ex.item()) > 0
+
+
+@pytest.mark.parametrize("cluster", [1, 4])
+def test_sign_parity_fp32_per_swap_error(cuda, cluster):
+    """Per-swap dE of the float32 sign-parity chunk kernel (the batching and serving form) against the oracle: with an
+    energy sample after every step, the change of the carried energy at each accepted step is the kernel's dE there;
+    every one is within the stated 1e-6 eV of the oracle's float64 dE, and the trajectory is the oracle's."""
+    torch = cuda
+    from neuralce_gb300.ce import proposal_stream
+    from neuralce_gb300.pt import run_chunk
+    from oracle.ce_oracle import new_state
+    R, T = 8, 600
+    gce, orc, sig_r, beta = _setup(8, seed=51, R=R)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    st = _engine_state(sig_r, E0, beta); ref = new_state(sig_r, E0, beta)
+    pa, pb, pu = proposal_stream(gce, R, T, seed=52)
+    Es = torch.zeros((T, R), dtype=torch.float64, device="cuda")
+    run_chunk(gce, st, T, 0, 0, 32, 8, tuple(torch.as_tensor(x).cuda() for x in (pa, pb, pu)), 1, Es, False, path=2,
+              cluster=cluster)
+    Es_ref = np.zeros((T, R))
+    orc.run(ref, T, 0, 0, (pa, pb, pu), 1, Es_ref, False, n_threads=4, near_eV=1e-6)
+    torch.cuda.synchronize()
+    _compare(st, ref, 1e-4)
+    g = np.diff(np.concatenate([E0[None], Es.cpu().numpy()]), axis=0)      # per step, slot order = replica order
+    o = np.diff(np.concatenate([E0[None], Es_ref]), axis=0)
+    moved = o != 0.0
+    assert moved.sum() > 100
+    err = np.abs(g - o)[moved].max()
+    print(f"float32 sign parity: {moved.sum()} accepted swaps, max |dE - oracle| = {err:.2e} eV")
+    assert err < 1e-6
+    assert np.all(g[~moved] == 0.0)

@@ -51,6 +51,7 @@ def test_icet_pt_cli_outputs_and_resume(cuda, tmp_path, ptni_ce, monkeypatch):
               "swap_accept_rate", "exchange_accept_rate", "wall_time"):
         assert k in r.files, k
     assert 0.0 < summary["swap_accept_rate"] < 1.0 and "E_min" in summary
+    assert summary["near_threshold_steps"] >= 0                # counted by the chunk kernels, reported
     # the last slot-ordered samples are the energies of the final configurations
     atoms, scale = icet_mc.prepare_cell(read_ce(ce_path), cif, (3, 3, 3), 3, log=lambda *x, **k: None)
     gce = GPUClusterExpansion(read_ce(ce_path), atoms, energy_scale=scale)
