@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
     ap.add_argument("--warps", type=int, default=0, help="warps per replica (0 = autotune)")
     ap.add_argument("--cluster", type=int, default=0, help="CTAs per replica, thread-block cluster (0 = autotune)")
-    ap.add_argument("--path", type=int, default=0, help="0 auto, 1 general products, 2 sign parity")
+    ap.add_argument("--path", type=int, default=0, help="0 auto, 1 general products, 2 sign parity, 3 local field")
     ap.add_argument("--L", type=int, default=8)
     ap.add_argument("--R", type=int, default=32)
     ap.add_argument("--chunk", type=int, default=5000)
@@ -363,7 +363,12 @@ def bench_serve(seconds=10.0, rate=50.0, ce_scale=0.01, nce_scale=0.0002, nce_ma
     models = ServeModels(mma=nce_mma)
     for j in jobs:
         j["model"] = models.ce(j["L"]) if j["kind"] == "ce" else models.nce(j["L"])
-        j["sigma"] = random_occupancy(j["N"], j["x_pt"], j["R"], j["seed"] & 0xFFFFFFFF)
+        # the job's occupancies and its result buffer in page-locked host memory, prepared with the job; the server
+        # reads the occupancies in place at admission (borrow) and writes the final ones into the result buffer
+        sig = random_occupancy(j["N"], j["x_pt"], j["R"], j["seed"] & 0xFFFFFFFF)
+        j["sigma"] = torch.empty(sig.shape, dtype=torch.int8, pin_memory=True).numpy()
+        j["sigma"][...] = sig
+        j["out"] = torch.empty(sig.shape, dtype=torch.int8, pin_memory=True).numpy()
         j["beta"] = ladder(j["R"])[1]
     setup = time.time() - t0
     ce_jobs = [j for j in jobs if j["kind"] == "ce"]
@@ -371,7 +376,8 @@ def bench_serve(seconds=10.0, rate=50.0, ce_scale=0.01, nce_scale=0.0002, nce_ma
     def burst(w):
         """every CE job of the stream submitted at once: (attempts/s over the makespan, makespan)"""
         with Server(precision=32, warps=w) as sv:
-            bh = [sv.submit_ce(j["model"], j["sigma"], j["beta"], j["steps"], ce_exchange, j["seed"]) for j in ce_jobs]
+            bh = [sv.submit_ce(j["model"], j["sigma"], j["beta"], j["steps"], ce_exchange, j["seed"], sigma_out=j["out"],
+                               borrow=True) for j in ce_jobs]
             binf = sv.wait(bh, timeout=1800)
         span = max(i["t_end"] for i in binf) - min(i["t_submit"] for i in binf)
         return sum(j["R"] * j["steps"] for j in ce_jobs) / span, span
@@ -385,9 +391,11 @@ def bench_serve(seconds=10.0, rate=50.0, ce_scale=0.01, nce_scale=0.0002, nce_ma
         while time.perf_counter() - start < j["t"]:
             time.sleep(0.0002)
         if j["kind"] == "ce":
-            hs.append(srv.submit_ce(j["model"], j["sigma"], j["beta"], j["steps"], ce_exchange, j["seed"]))
+            hs.append(srv.submit_ce(j["model"], j["sigma"], j["beta"], j["steps"], ce_exchange, j["seed"], sigma_out=j["out"],
+                                    borrow=True))
         else:
-            hs.append(srv.submit_nce(j["model"], j["sigma"], j["beta"], j["steps"], nce_exchange, j["seed"]))
+            hs.append(srv.submit_nce(j["model"], j["sigma"], j["beta"], j["steps"], nce_exchange, j["seed"], sigma_out=j["out"],
+                                     borrow=True))
     infos = srv.wait(hs, timeout=1800)
     st = srv.stats()
     failures = [i.get("message", "") for i in infos if i["status"] == "failed"][:3]

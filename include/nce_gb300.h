@@ -335,9 +335,10 @@ int nce_tc_gemm(const float *A, const float *B, float *C, int32_t M, int32_t N, 
  * A resident server that runs many parallel-tempering jobs at once.  Jobs are admitted in submission order as
  * device memory within the server's budget frees up (a later job that fits may start before an earlier one
  * that does not, unless the earlier one has waited longer than starve_s); their state stays on the device until
- * they finish.  Two host worker threads drive the GPU: one advances every running CE job with one persistent
- * batch launch per round (continuous batching: jobs join and leave between rounds), the other the NeuralCE jobs
- * on a few streams, so the two kinds overlap on the device.  A job's chunks depend only on its own parameters,
+ * they finish.  Two host worker threads drive the GPU: one advances the running CE jobs with persistent batch
+ * launches on eight lanes (streams), a job joining the next launch on an idle lane as soon as its previous one has
+ * completed (continuous batching without a global round), the other the NeuralCE jobs on a few streams, so the
+ * two kinds overlap on the device.  A job's chunks depend only on its own parameters,
  * so its result is the same alone and in any mix.  No call below waits for the device.
  * The reference has no serving mode; these entry points are new (they replace running neuralce-mc per job). */
 typedef struct nce_server *nce_server_handle;
@@ -363,7 +364,7 @@ typedef struct {
     int32_t kind;          /* NCE_JOB_CE (model = nce_ce_handle) or NCE_JOB_NCE (model = nce_nce_handle) */
     void *model;           /* must stay valid until the job has finished or been cancelled */
     int32_t R;
-    const int8_t *sigma;   /* host (R, N) initial occupancies (copied at submission) */
+    const int8_t *sigma;   /* host (R, N) initial occupancies (copied at submission unless flags borrow them) */
     const float *beta_slot;/* host (R) */
     const int32_t *ladder_id; /* host (R) or NULL (one ladder) */
     int64_t n_steps;       /* MC steps per replica */
@@ -376,7 +377,12 @@ typedef struct {
     int64_t *n_acc_out;    /* (R) */
     int32_t *rep_of_slot_out; /* (R) */
     int64_t *n_ex_out;     /* (1) */
+    int32_t flags;         /* NCE_JOB_BORROW_SIGMA: `sigma` is read in place when the job is admitted instead of being
+                              copied at submission; the caller keeps it unchanged until the job has finished, failed or
+                              been cancelled (in page-locked memory the upload is one direct copy) */
 } nce_job_desc;
+
+#define NCE_JOB_BORROW_SIGMA 1
 
 #define NCE_JOB_QUEUED     0
 #define NCE_JOB_RUNNING    1
@@ -395,7 +401,7 @@ typedef struct {
 typedef struct {
     int64_t queued, running, done, cancelled, failed;
     int64_t bytes_used, hbm_budget;
-    int64_t rounds_ce, rounds_nce;
+    int64_t rounds_ce, rounds_nce;     /* CE batch launches completed; NeuralCE rounds (one chunk per running job) */
     int64_t attempts;      /* swap attempts completed (replicas x steps) */
     double now;            /* server clock */
 } nce_server_stats;

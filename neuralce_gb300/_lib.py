@@ -71,7 +71,8 @@ class NceServerConfig(C.Structure):
 class NceJobDesc(C.Structure):
     _fields_ = [("kind", i32), ("model", vp), ("R", i32), ("sigma", vp), ("beta_slot", vp), ("ladder_id", vp),
                 ("n_steps", i64), ("exchange_every", i64), ("seed", u64), ("reanchor_chunks", i32),
-                ("sigma_out", vp), ("E_out", vp), ("n_acc_out", vp), ("rep_of_slot_out", vp), ("n_ex_out", vp)]
+                ("sigma_out", vp), ("E_out", vp), ("n_acc_out", vp), ("rep_of_slot_out", vp), ("n_ex_out", vp),
+                ("flags", i32)]
 
 
 class NceJobInfo(C.Structure):

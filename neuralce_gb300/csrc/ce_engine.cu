@@ -484,9 +484,12 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     for (int c = tid; c < n_cols; c += nt) { ecol[c] = gecol[c]; cnt[c] = 0; cnt[n_cols + c] = 0; dcv[c] = 0; }
     int32_t *rcnt[16];
     for (int q = 0; q < 16; ++q) rcnt[q] = cnt;
+    __shared__ long long pslot[2][16];                // fixed-point partial dE of each CTA of the cluster [parity][rank]
+    long long *pdst = &pslot[0][0];                   // lane q of warp 0 stores this CTA's partial into CTA q
     if (CLUSTER) {
         cg::cluster_group cl = cg::this_cluster();
         for (int q = 0; q < CL && q < 16; ++q) rcnt[q] = cl.map_shared_rank(cnt, q);
+        if (lane < CL) pdst = cl.map_shared_rank(&pslot[0][0], lane);
     }
     int8_t *gsig = jb.sigma + (int64_t)r * jb.N;
     int8_t *sig = sig_smem ? reinterpret_cast<int8_t *>(smem + L.sig) : gsig;
@@ -503,6 +506,7 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     // minimum are kept in it and turned into float64 at the samples and at the end
     constexpr bool FIX = std::is_same<Acc, double>::value;
     const bool fix = FIX && jb.fix_shift > 0;
+    const bool push = CLUSTER && fix;                  // partial dE per CTA pushed to the cluster (no remote count reads)
     const double fscale = fix ? ldexp(1.0, -jb.fix_shift) : 0.0;
     const double E0c = E;
     long long dsum = 0, dmin = 0;
@@ -596,32 +600,50 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                     }
                 }
             }
+            // exact warp sum of |part| < 2^61 in three 21-bit slices (hardware 32-bit reductions, no carries lost)
+            auto exact_sum = [](long long part) -> long long {
+                const unsigned l0 = (unsigned)(part & 0x1fffff), l1 = (unsigned)((part >> 21) & 0x1fffff);
+                const int l2 = (int)(part >> 42);
+                const unsigned s0 = __reduce_add_sync(0xffffffffu, l0), s1 = __reduce_add_sync(0xffffffffu, l1);
+                const int s2 = __reduce_add_sync(0xffffffffu, l2);
+                return (long long)s0 + ((long long)s1 << 21) + ((long long)s2 << 42);
+            };
+            if (push) {
+                // each CTA turns its own counts into an exact partial dE and stores it into slot `rank` of every CTA
+                // of the cluster; after the barrier each CTA adds the partials from its own shared memory
+                __syncthreads();
+                if (warp == 0) {
+                    long long part = 0;
+                    for (int c = lane; c < n_cols; c += 32) { const int n = cntp[c]; if (n) part += (long long)n * efix[c]; }
+                    part = exact_sum(part);
+                    if (lane < CL) pdst[par * 16 + rank] = part;
+                }
+            }
             if (CLUSTER) cg::this_cluster().sync(); else __syncthreads();
             // 3. dE = sum_c 2 eci_c n_c (warp 0, fixed order), accept, write
             if (warp == 0) {
-                // this swap's count of column c, summed over the cluster's CTAs
+                // this swap's count of column c, summed over the cluster's CTAs (this CTA's own count when pushing)
                 auto count = [&](int c) -> int {
-                    if (!CLUSTER) return cntp[c];
+                    if (!CLUSTER || push) return cntp[c];
                     int n = 0;
                     for (int q = 0; q < CL; ++q) n += rcnt[q][par * n_cols + c];
                     return n;
                 };
-                if (CLUSTER)                            // every CTA has read the other buffer (previous swap) by now
+                if (CLUSTER && !push)                   // every CTA has read the other buffer (previous swap) by now
                     for (int c = lane; c < n_cols; c += 32) cnt[(par ^ 1) * n_cols + c] = 0;
                 bool accept;
                 if (fix) {
                     long long part = 0;
-                    for (int c = lane; c < n_cols; c += 32) {
-                        const int n = count(c);
-                        if (n) { part += (long long)n * efix[c]; if (!track && !CLUSTER) cntp[c] = 0; }
-                    }
-                    // exact warp sum of |part| < 2^61 in three 21-bit slices (hardware 32-bit reductions, no carries lost)
-                    {
-                        const unsigned l0 = (unsigned)(part & 0x1fffff), l1 = (unsigned)((part >> 21) & 0x1fffff);
-                        const int l2 = (int)(part >> 42);
-                        const unsigned s0 = __reduce_add_sync(0xffffffffu, l0), s1 = __reduce_add_sync(0xffffffffu, l1);
-                        const int s2 = __reduce_add_sync(0xffffffffu, l2);
-                        part = (long long)s0 + ((long long)s1 << 21) + ((long long)s2 << 42);
+                    if (push) {
+                        for (int q = 0; q < CL; ++q) part += pslot[par][q];
+                        if (!track)
+                            for (int c = lane; c < n_cols; c += 32) cntp[c] = 0;
+                    } else {
+                        for (int c = lane; c < n_cols; c += 32) {
+                            const int n = count(c);
+                            if (n) { part += (long long)n * efix[c]; if (!track && !CLUSTER) cntp[c] = 0; }
+                        }
+                        part = exact_sum(part);
                     }
                     accept = part < P.thr;
                     if (lane == 0) {                    // near the threshold: |dE 2^S - (-ln u / beta) 2^S| below the band
@@ -650,7 +672,7 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                 if (track)                              // each changed row moves its column's sum by +-2
                     for (int c = lane; c < n_cols; c += 32) {
                         const int n = count(c);
-                        if (n) { if (accept) dcv[c] += 2 * n; if (!CLUSTER) cntp[c] = 0; }
+                        if (n) { if (accept) dcv[c] += 2 * n; if (!CLUSTER || push) cntp[c] = 0; }
                     }
             }
             par ^= 1;
@@ -673,10 +695,14 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
         E = E0c + (double)dsum * fscale;
         Emin = fmin(Emin, E0c + (double)dmin * fscale);
     }
+    if (track && push)                                   // every CTA adds the changes its own rows counted
+        for (int c = tid; c < n_cols; c += nt)
+            if (dcv[c]) atomicAdd(reinterpret_cast<unsigned long long *>(jb.cv + (int64_t)r * n_cols + c),
+                                  (unsigned long long)(long long)dcv[c]);
     if (rank == 0) {
         if (sig_smem)
             for (int64_t i = tid; i < jb.N; i += nt) gsig[i] = sig[i];
-        if (track)
+        if (track && !push)
             for (int c = tid; c < n_cols; c += nt) jb.cv[(int64_t)r * n_cols + c] += dcv[c];
         if (sig_smem || track) __syncthreads();          // the replica's outputs are written before it is counted
         if (tid == 0) {

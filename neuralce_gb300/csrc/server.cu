@@ -1,13 +1,13 @@
 // Job server of libnce_gb300 (serving form): admission by a device-memory budget, continuous batching of CE
-// jobs into one persistent launch per round, NeuralCE jobs on side streams, all state resident on the device
-// while a job runs.  Host code only; the device work is the engines' own entry points.
+// jobs into persistent batch launches on a few lanes, NeuralCE jobs on side streams, all state resident on the
+// device while a job runs.  Host code only; the device work is the engines' own entry points.
 //
 // Threads: the caller's threads only touch host structures under `mu` (submit, poll, cancel, query never wait
 // for the device).  The io thread admits jobs (upload, initial energies or caches) and retires them (outputs
 // copied to the caller's host buffers, device memory returned with cudaFreeAsync) on its own stream, so neither
-// stalls the device work; the CE thread runs rounds of persistent batch launches over every running CE job (up
-// to max_batch jobs per launch, launches spread over a few streams), the NeuralCE thread one chunk per running
-// NeuralCE job per round on `nce_streams` streams.
+// stalls the device work; the CE thread keeps eight lanes (streams) of persistent batch launches busy with the
+// running CE jobs (up to max_batch jobs per launch; a job joins the next launch as soon as its previous one has
+// completed), the NeuralCE thread one chunk per running NeuralCE job per round on `nce_streams` streams.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -34,6 +34,7 @@ struct SJob {
     int64_t N = 0;
     int32_t n_cols = 0, mo = 0, binary = 0, C0 = 0, D = 0, depth = 0, lf = 0;   // lf: runs the local-field kernel
     std::vector<int8_t> sig; std::vector<float> beta; std::vector<int32_t> lid;
+    const int8_t *sig_src = nullptr;  // the initial occupancies: `sig`, or the caller's buffer (NCE_JOB_BORROW_SIGMA)
     int64_t bytes = 0;
     int status = NCE_JOB_QUEUED, error = 0;
     std::string msg;
@@ -44,6 +45,7 @@ struct SJob {
     nce_pt_state st{};
     nce_nce_state nst{};
     int32_t chunks = 0, anchor = 1;
+    bool inflight = false;            // CE: part of a launch that has not completed (CE thread only)
     cudaStream_t stream = nullptr;
 };
 
@@ -184,7 +186,7 @@ int start_ce(nce_server *S, SJob &j, cudaStream_t s) {
     std::vector<int32_t> iota(R);
     for (int i = 0; i < R; ++i) iota[i] = i;
     std::vector<double> inf(R, std::numeric_limits<double>::infinity());
-    NCE_CUDA(cudaMemcpyAsync(st.sigma, j.sig.data(), (size_t)R * j.N, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync(st.sigma, j.sig_src, (size_t)R * j.N, cudaMemcpyHostToDevice, s));
     NCE_CUDA(cudaMemcpyAsync((void *)st.beta_slot, j.beta.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
     NCE_CUDA(cudaMemcpyAsync((void *)st.ladder_id, j.lid.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
     NCE_CUDA(cudaMemcpyAsync(st.rep_of_slot, iota.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
@@ -221,7 +223,7 @@ int start_nce(nce_server *S, SJob &j, cudaStream_t s) {
     st.ladder_id = (int32_t *)(b + p.off[8]); st.n_acc = (int64_t *)(b + p.off[9]); st.n_ex = (int64_t *)(b + p.off[10]);
     std::vector<int32_t> iota(R);
     for (int i = 0; i < R; ++i) iota[i] = i;
-    NCE_CUDA(cudaMemcpyAsync(st.sigma, j.sig.data(), (size_t)R * j.N, cudaMemcpyHostToDevice, s));
+    NCE_CUDA(cudaMemcpyAsync(st.sigma, j.sig_src, (size_t)R * j.N, cudaMemcpyHostToDevice, s));
     NCE_CUDA(cudaMemcpyAsync((void *)st.beta_slot, j.beta.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
     NCE_CUDA(cudaMemcpyAsync((void *)st.ladder_id, j.lid.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
     NCE_CUDA(cudaMemcpyAsync(st.rep_of_slot, iota.data(), 4 * (size_t)R, cudaMemcpyHostToDevice, s));
@@ -395,20 +397,77 @@ void fail_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &job
 
 int64_t chunk_len(const SJob &j) { return std::min(j.d.exchange_every - j.done % j.d.exchange_every, j.d.n_steps - j.done); }
 
-// CE thread: one round = persistent batch launches over every running CE job (grouped by cluster order, at most
-// max_batch jobs per launch, launches spread over the CE streams), each job's exact re-anchor after its chunk
+// CE thread: persistent batch launches on a few lanes (one stream each).  Every running CE job that is not in a
+// launch joins the next launch on an idle lane (jobs of one cluster order and kernel, at most max_batch a launch),
+// and that launch is followed by each job's exact re-anchor; a lane's jobs are free again as soon as its launch
+// has completed, so short and long launches do not wait for one another.  A job's chunks (length, Philox key and
+// global step) depend only on the job, so its results do not depend on which jobs share its launches.
+struct CeLane {
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev = nullptr;
+    std::vector<std::shared_ptr<SJob>> jobs;
+    std::vector<int64_t> steps;
+    bool busy = false;
+};
+
 void ce_worker(nce_server *S) {
     cudaSetDevice(S->device);
-    std::vector<std::shared_ptr<SJob>> run;
-    while (take_round(S, 0, run)) {
-        // one launch takes jobs of one cluster order and one kernel (local field or sign parity)
-        std::map<int32_t, std::vector<std::shared_ptr<SJob>>> by_mo;
-        for (auto &p : run) by_mo[2 * p->mo + p->lf].push_back(p);
-        int rc = NCE_OK, g = 0;
-        for (auto &grp : by_mo) {
+    std::vector<CeLane> lanes(S->ce_streams.size());
+    for (size_t i = 0; i < lanes.size(); ++i) {
+        lanes[i].s = S->ce_streams[i];
+        cudaEventCreateWithFlags(&lanes[i].ev, cudaEventDisableTiming);
+    }
+    std::vector<std::shared_ptr<SJob>> idle;
+    for (;;) {
+        bool moved = false;
+        // 1. completed launches: their jobs advance; finished jobs go to the io thread
+        for (auto &ln : lanes) {
+            if (!ln.busy) continue;
+            const cudaError_t e = cudaEventQuery(ln.ev);
+            if (e == cudaErrorNotReady) continue;
+            ln.busy = false; moved = true;
+            for (auto &p : ln.jobs) p->inflight = false;
+            if (e != cudaSuccess) {
+                fail_round(S, 0, ln.jobs, fail(NCE_ERR_CUDA, "CE launch: %s", cudaGetErrorString(e)));
+            } else {
+                for (size_t i = 0; i < ln.jobs.size(); ++i) {
+                    ln.jobs[i]->done += ln.steps[i];
+                    S->attempts += ln.steps[i] * ln.jobs[i]->d.R;
+                }
+                end_round(S, 0, ln.jobs);
+            }
+            ln.jobs.clear(); ln.steps.clear();
+        }
+        // 2. running jobs outside any launch (cancelled ones that are not in a launch leave for the io thread)
+        bool any_busy = false;
+        for (auto &ln : lanes) any_busy = any_busy || ln.busy;
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            if (S->stop && !any_busy) break;
+            auto &a = S->active[0];
+            idle.clear();
+            for (auto it = a.begin(); it != a.end();) {
+                auto &p = *it;
+                if (p->inflight) { ++it; continue; }
+                if (p->cancel) { S->retiring[0].push_back(p); it = a.erase(it); S->wake.notify_all(); continue; }
+                if (!S->stop) idle.push_back(p);
+                ++it;
+            }
+            if (idle.empty() && !any_busy && !moved) {
+                S->wake.wait_for(lk, std::chrono::milliseconds(2));
+                continue;
+            }
+        }
+        // 3. launches of the idle jobs on the idle lanes
+        std::map<int32_t, std::vector<std::shared_ptr<SJob>>> by_key;   // one cluster order and kernel a launch
+        for (auto &p : idle) by_key[2 * p->mo + p->lf].push_back(p);
+        bool launched = false;
+        for (auto &grp : by_key) {
             auto &v = grp.second;
-            for (size_t a = 0; a < v.size() && rc == NCE_OK; a += (size_t)S->cfg.max_batch, ++g) {
-                cudaStream_t s = S->ce_streams[g % S->ce_streams.size()];
+            for (size_t a = 0; a < v.size(); a += (size_t)S->cfg.max_batch) {
+                CeLane *ln = nullptr;
+                for (auto &l : lanes) if (!l.busy) { ln = &l; break; }
+                if (!ln) break;
                 const int n = (int)std::min<size_t>((size_t)S->cfg.max_batch, v.size() - a);
                 std::vector<nce_ce_handle> hs(n); std::vector<nce_pt_state> ss(n); std::vector<nce_pt_chunk> cs(n);
                 for (int i = 0; i < n; ++i) {
@@ -421,26 +480,29 @@ void ce_worker(nce_server *S) {
                     c.precision = j.lf ? 64 : S->cfg.precision; c.path = j.lf ? 3 : 0; c.cluster = 1;
                     c.warps = j.lf && S->cfg.ce_lf_warps > 0 ? S->cfg.ce_lf_warps : S->cfg.warps;
                 }
-                rc = nce_ce_run_batch(n, hs.data(), ss.data(), cs.data(), s);
+                int rc = nce_ce_run_batch(n, hs.data(), ss.data(), cs.data(), ln->s);
                 for (int i = 0; i < n && rc == NCE_OK; ++i) {
                     SJob &j = *v[a + i];
-                    if (j.st.cv) rc = nce_ce_energy_from_counts(hs[i], j.st.cv, j.d.R, j.st.E, s);
+                    if (j.st.cv) rc = nce_ce_energy_from_counts(hs[i], j.st.cv, j.d.R, j.st.E, ln->s);
                 }
-                if (rc == NCE_OK)
-                    for (int i = 0; i < n; ++i) {
-                        SJob &j = *v[a + i];
-                        j.done += cs[i].n_steps;
-                        S->attempts += cs[i].n_steps * j.d.R;
-                    }
+                if (rc == NCE_OK && cudaEventRecord(ln->ev, ln->s) != cudaSuccess) rc = fail(NCE_ERR_CUDA, "CE launch: event record");
+                std::vector<std::shared_ptr<SJob>> js(v.begin() + a, v.begin() + a + n);
+                if (rc) {
+                    // what was enqueued may still run: wait for the lane before the jobs' memory is given back
+                    cudaStreamSynchronize(ln->s);
+                    fail_round(S, 0, js, rc);
+                    continue;
+                }
+                ln->busy = true; launched = true;
+                ln->jobs = std::move(js);
+                for (int i = 0; i < n; ++i) { ln->jobs[i]->inflight = true; ln->steps.push_back(cs[i].n_steps); }
             }
         }
-        if (rc == NCE_OK)
-            for (cudaStream_t s : S->ce_streams) {
-                const cudaError_t e = cudaStreamSynchronize(s);
-                if (e != cudaSuccess) { rc = fail(NCE_ERR_CUDA, "CE round: %s", cudaGetErrorString(e)); break; }
-            }
-        if (rc) { fail_round(S, 0, run, rc); continue; }
-        end_round(S, 0, run);
+        if (!launched && !moved) std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    for (auto &ln : lanes) {
+        if (ln.busy) cudaEventSynchronize(ln.ev);
+        cudaEventDestroy(ln.ev);
     }
 }
 
@@ -499,7 +561,7 @@ int nce_server_create(const nce_server_config *cfg, nce_server_handle *out) {
         c.hbm_budget = (int64_t)(0.9 * (double)fr);
     }
     for (int k = 0; k < 2; ++k) NCE_CUDA(cudaStreamCreateWithFlags(&S->io_streams[k], cudaStreamNonBlocking));
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < 8; ++i) {                    // CE lanes
         cudaStream_t s;
         NCE_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
         S->ce_streams.push_back(s);
@@ -570,7 +632,13 @@ int nce_job_submit(nce_server_handle S, const nce_job_desc *d, int64_t *job_id) 
         j->anchor = d->reanchor_chunks > 0 ? d->reanchor_chunks
                                           : (int32_t)std::max<int64_t>(1, (j->N + d->exchange_every - 1) / d->exchange_every);
     }
-    j->sig.assign(d->sigma, d->sigma + (size_t)d->R * j->N);
+    NCE_CHECK((d->flags & ~NCE_JOB_BORROW_SIGMA) == 0, "nce_job_submit: unknown flags 0x%x", d->flags);
+    if (d->flags & NCE_JOB_BORROW_SIGMA) {
+        j->sig_src = d->sigma;
+    } else {
+        j->sig.assign(d->sigma, d->sigma + (size_t)d->R * j->N);
+        j->sig_src = j->sig.data();
+    }
     j->beta.assign(d->beta_slot, d->beta_slot + d->R);
     if (d->ladder_id) j->lid.assign(d->ladder_id, d->ladder_id + d->R);
     else j->lid.assign(d->R, 0);

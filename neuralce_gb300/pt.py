@@ -179,8 +179,8 @@ def make_chunk(n_steps, step0, seed, precision=64, warps=0, proposals=None, samp
 def run_chunk(gce, st: PTState, n_steps, step0, seed, precision=64, warps=0, proposals=None, sample_interval=1,
               E_samples=None, do_exchange=False, ex_parity=0, ex_u=None, stream=None, path=0, cluster=1, near_eV=0.0):
     """One chunk of the persistent kernel (+ chunk-end exchange) for one job.  path: 0 auto (local field when the state
-    has fields, else sign parity when the point functions are +-1), 1 general products, 2 sign parity, 3 local field.  ``st.n_near`` counts the steps whose Metropolis
-    margin |dE + ln(u) / beta| is below ``near_eV`` (0: the precision form's stated dE bound)."""
+    has fields, else sign parity when the point functions are +-1), 1 general products, 2 sign parity, 3 local field.
+    ``st.n_near`` counts the steps whose Metropolis margin |dE + ln(u) / beta| is below ``near_eV`` (0: the precision form's stated dE bound)."""
     ck = make_chunk(n_steps, step0, seed, precision, warps, proposals, sample_interval, E_samples, do_exchange,
                     ex_parity, ex_u, path, cluster, near_eV)
     s = st.struct()

@@ -3,8 +3,9 @@ libnce_gb300).
 
 Jobs of different cells, replica counts, compositions and models (CE or NeuralCE) are submitted while others run;
 the server admits them in submission order as device memory within its budget frees up, keeps their state on
-the device, advances every running CE job with one persistent batch launch per round (continuous batching) and
-the NeuralCE jobs on side streams, and copies each job's final state into host arrays when it finishes.  A job's
+the device, advances the running CE jobs with persistent batch launches on eight lanes (a job joins the next
+launch on an idle lane as soon as its previous one has completed: continuous batching) and the NeuralCE jobs on
+side streams, and copies each job's final state into host arrays when it finishes.  A job's
 chunks (exchange interval, Philox key and global step of every chunk) depend only on its own parameters, so its
 result is the same alone and in any mix.  The reference has no serving mode: a job here is one
 ``run_pt_mcmc`` call (``neuralce/ce/pt_mcmc_ce.py:587-601``) or NeuralCE ``_run_replicas``
@@ -27,9 +28,10 @@ STATUS = {0: "queued", 1: "running", 2: "done", 3: "cancelled", 4: "failed"}
 class Job:
     """Handle of a submitted job; ``result()`` holds the final state once ``done``."""
 
-    def __init__(self, server, kind, model, R, N):
+    def __init__(self, server, kind, model, R, N, sigma_out=None, borrowed=None):
         self.server, self.kind, self.model, self.R, self.N = server, kind, model, R, N
-        self.sigma = np.zeros((R, N), np.int8)
+        self.sigma = np.zeros((R, N), np.int8) if sigma_out is None else sigma_out
+        self._borrowed = borrowed              # the caller's initial occupancies, read by the server at admission
         self.E = np.zeros(R, np.float64)
         self.n_acc = np.zeros(R, np.int64)
         self.rep_of_slot = np.zeros(R, np.int32)
@@ -68,15 +70,19 @@ class Server:
         self._jobs = {}
 
     def _submit(self, kind, model_handle, model, sigma, beta_slot, n_steps, exchange_every, seed, ladder_id,
-                reanchor_chunks=0):
+                reanchor_chunks=0, sigma_out=None, borrow=False):
         sigma = np.ascontiguousarray(np.asarray(sigma, np.int8))
         R, N = sigma.shape
         beta = np.ascontiguousarray(np.asarray(beta_slot, np.float32))
         if beta.shape != (R,):
             raise ValueError(f"beta_slot must have {R} entries")
         lid = None if ladder_id is None else np.ascontiguousarray(np.asarray(ladder_id, np.int32))
-        job = Job(self, kind, model, R, N)
+        if sigma_out is not None and (sigma_out.shape != (R, N) or sigma_out.dtype != np.int8
+                                      or not sigma_out.flags["C_CONTIGUOUS"] or not sigma_out.flags["WRITEABLE"]):
+            raise ValueError(f"sigma_out must be a writeable C-contiguous ({R}, {N}) int8 array")
+        job = Job(self, kind, model, R, N, sigma_out, sigma if borrow else None)
         d = _lib.NceJobDesc()
+        d.flags = 1 if borrow else 0
         d.kind, d.model, d.R = kind, model_handle, R
         d.sigma, d.beta_slot, d.ladder_id = sigma.ctypes.data, beta.ctypes.data, (lid.ctypes.data if lid is not None else None)
         d.n_steps, d.exchange_every, d.seed = int(n_steps), int(exchange_every), int(seed) & 0xFFFFFFFFFFFFFFFF
@@ -89,15 +95,24 @@ class Server:
         self._jobs[job.id] = job
         return job
 
-    def submit_ce(self, gce, sigma, beta_slot, n_steps, exchange_every=5000, seed=0, ladder_id=None):
-        """A CE parallel-tempering job: ``sigma`` (R, N) species indices in canonical site order."""
-        return self._submit(0, gce.handle.value, gce, sigma, beta_slot, n_steps, exchange_every, seed, ladder_id)
+    def submit_ce(self, gce, sigma, beta_slot, n_steps, exchange_every=5000, seed=0, ladder_id=None, sigma_out=None,
+                  borrow=False):
+        """A CE parallel-tempering job: ``sigma`` (R, N) species indices in canonical site order.  ``sigma_out``: the
+        array that receives the final occupancies (default: a new one); ``borrow``: the server reads ``sigma`` in
+        place when it admits the job instead of copying it now; the job keeps a reference, and the caller must not
+        change it until the job has left the queued and running states.  Both avoid host copies of large cells;
+        in page-locked memory (e.g. ``torch.empty(..., pin_memory=True).numpy()``) the uploads and downloads are
+        direct copies."""
+        return self._submit(0, gce.handle.value, gce, sigma, beta_slot, n_steps, exchange_every, seed, ladder_id,
+                            sigma_out=sigma_out, borrow=borrow)
 
-    def submit_nce(self, model, sigma, beta_slot, n_steps, exchange_every=1000, seed=0, ladder_id=None, reanchor_chunks=0):
+    def submit_nce(self, model, sigma, beta_slot, n_steps, exchange_every=1000, seed=0, ladder_id=None, reanchor_chunks=0,
+                   sigma_out=None, borrow=False):
         """A NeuralCE parallel-tempering job on an ``nce.NCEModel``; the full caches are rebuilt every
-        ``reanchor_chunks`` chunks (0: ceil(N / exchange_every), the reference driver's default)."""
+        ``reanchor_chunks`` chunks (0: ceil(N / exchange_every), the reference driver's default).  ``sigma_out`` and
+        ``borrow`` as in ``submit_ce``."""
         return self._submit(1, model.handle.value, model, sigma, beta_slot, n_steps, exchange_every, seed, ladder_id,
-                            reanchor_chunks)
+                            reanchor_chunks, sigma_out=sigma_out, borrow=borrow)
 
     def poll(self, job):
         inf = _lib.NceJobInfo()

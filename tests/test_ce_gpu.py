@@ -75,7 +75,8 @@ def _compare(st, ref, E_tol):
 
 
 @pytest.mark.parametrize("precision,path,warps,cluster", [(64, 1, 8, 1), (32, 1, 8, 1), (64, 2, 8, 1), (32, 2, 4, 1),
-                                                          (64, 2, 1, 1), (64, 2, 8, 2), (32, 2, 4, 4), (64, 2, 16, 8)])
+                                                          (64, 2, 1, 1), (64, 2, 8, 2), (32, 2, 4, 4), (64, 2, 16, 8),
+                                                          (32, 2, 16, 2)])
 def test_trajectory_host_stream(cuda, precision, path, warps, cluster):
     """Seeded host proposal stream + exchange uniforms: bit-exact occupancy trajectory, energies, acceptance,
     slot permutation and slot-ordered samples vs the oracle (cluster > 1: each replica spread over that many
@@ -232,12 +233,14 @@ def test_sign_parity_small_cells(cuda, L):
     R, T = 4, 400
     gce, orc, sig_r, beta = _setup(L, seed=9, R=R)
     E0 = np.array([orc.energy(x) for x in sig_r])
-    a = _engine_state(sig_r, E0, beta); b = _engine_state(sig_r, E0, beta); ref = new_state(sig_r, E0, beta)
+    a, b, c = (_engine_state(sig_r, E0, beta) for _ in range(3))
+    ref = new_state(sig_r, E0, beta)
     run_chunk(gce, a, T, 0, 31, 64, 2, None, 1, None, True, path=1)
     run_chunk(gce, b, T, 0, 31, 64, 2, None, 1, None, True, path=2)
+    run_chunk(gce, c, T, 0, 31, 64, 2, None, 1, None, True, path=2, cluster=2)   # partial dE pushed over a cluster
     orc.run(ref, T, 0, 31, None, 1, None, True, near_eV=1e-9)
     torch.cuda.synchronize()
-    _compare(a, ref, 1e-9); _compare(b, ref, 1e-9)
+    _compare(a, ref, 1e-9); _compare(b, ref, 1e-9); _compare(c, ref, 1e-9)
 
 
 def test_out_of_range_proposal_is_flagged(cuda):

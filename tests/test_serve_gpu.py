@@ -73,6 +73,39 @@ def test_results_same_alone_and_in_mix(cuda, ce_kernel):
         assert int(a["n_acc"].sum()) > 0
 
 
+def test_borrowed_page_locked_buffers(cuda):
+    """Jobs whose occupancies are read in place at admission (borrow) from page-locked memory, with the final
+    occupancies written into caller buffers, give the same results as jobs whose inputs were copied at submission."""
+    torch = cuda
+    from neuralce_gb300.serve import Server
+    jobs = _ce_jobs() + _nce_jobs()
+    with Server(precision=32) as srv:
+        hs = [_submit(srv, j) for j in jobs]
+        assert all(i["status"] == "done" for i in srv.wait(hs, timeout=300))
+        want = [h.result() for h in hs]
+    pins, outs = [], []
+    for j in jobs:
+        p = torch.empty(j["sigma"].shape, dtype=torch.int8, pin_memory=True).numpy()
+        p[...] = j["sigma"]
+        pins.append(p)
+        outs.append(torch.empty(j["sigma"].shape, dtype=torch.int8, pin_memory=True).numpy())
+    with Server(precision=32) as srv:
+        hs = []
+        for j, p, o in zip(jobs, pins, outs):
+            if j["kind"] == "ce":
+                hs.append(srv.submit_ce(j["model"], p, j["beta"], j["steps"], j["ex"], j["seed"], sigma_out=o, borrow=True))
+            else:
+                hs.append(srv.submit_nce(j["model"], p, j["beta"], j["steps"], j["ex"], j["seed"], reanchor_chunks=2,
+                                         sigma_out=o, borrow=True))
+        assert all(i["status"] == "done" for i in srv.wait(hs, timeout=300))
+        for h, o, w in zip(hs, outs, want):
+            r = h.result()
+            assert r["sigma"] is o
+            _same(r, w)
+    for p, j in zip(pins, jobs):                   # the borrowed inputs are read, never written
+        assert np.array_equal(p, j["sigma"])
+
+
 @pytest.mark.parametrize("ce_kernel", [0, 3])
 def test_ce_job_equals_direct_chunks(cuda, ce_kernel):
     """A served CE job = the chunk API driven by hand: chunks of the exchange interval, exact re-anchor of the
