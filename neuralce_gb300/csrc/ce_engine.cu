@@ -441,12 +441,17 @@ template <typename Acc, int MO, bool CLUSTER>
 __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constant__ CEBatch bt, int32_t sig_budget) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ BinProp prop[64];                      // ring of two batches of 32 proposals
-    __shared__ int32_t near_flag;
+    __shared__ int32_t near_flag[2];                  // per evaluated-swap parity
     // CLUSTER: one replica per thread-block cluster; every CTA keeps its own copy of the replica's occupancy and draws
-    // the same proposals, the row chunks are split over the CTAs, each CTA counts its chunks locally, and after the
-    // cluster barrier every CTA reads all CTAs' counts through distributed shared memory, so all reach the same
-    // decision.  A count buffer is cleared by its owner only after the next cluster barrier (when every CTA has
-    // read it); the two buffers alternate between evaluated swaps.
+    // the same proposals, and the row chunks are split over the CTAs.  Fixed point (float64): every warp adds its
+    // chunks' exact partial dE into the evaluated swap's accumulator of every CTA of the cluster (a local shared
+    // atomic without a cluster), and after the barrier every warp of every CTA reads the total and reaches the same
+    // decision; the accumulators alternate between evaluated swaps and each CTA clears its previous one after the
+    // next step's first barrier.  The accepted swap is written to the occupancy by one thread; until the next
+    // barrier every thread reads the two sites through the swap it holds in registers, so no barrier follows the
+    // decision.  float32: each CTA counts its chunks per column, after the barrier the decision warp reads all
+    // CTAs' counts (through distributed shared memory with a cluster) and sums the columns in a fixed order, and a
+    // barrier ends the step; a count buffer is cleared by its owner only after the next cluster barrier.
     int CL = 1, rank = 0;
     if (CLUSTER) { cg::cluster_group cl = cg::this_cluster(); CL = (int)cl.num_blocks(); rank = (int)cl.block_rank(); }
     const int rep_idx = blockIdx.x / CL;
@@ -482,14 +487,11 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     int32_t *dcv = reinterpret_cast<int32_t *>(smem + L.dcv);
     const bool track = jb.cv != nullptr;
     for (int c = tid; c < n_cols; c += nt) { ecol[c] = gecol[c]; cnt[c] = 0; cnt[n_cols + c] = 0; dcv[c] = 0; }
-    int32_t *rcnt[16];
-    for (int q = 0; q < 16; ++q) rcnt[q] = cnt;
-    __shared__ long long pslot[2][16];                // fixed-point partial dE of each CTA of the cluster [parity][rank]
-    long long *pdst = &pslot[0][0];                   // lane q of warp 0 stores this CTA's partial into CTA q
+    __shared__ long long pslot[2];                    // fixed-point dE accumulator of the evaluated swap [parity]
+    unsigned long long *pdst = reinterpret_cast<unsigned long long *>(pslot);   // lane q adds into CTA q's accumulator
     if (CLUSTER) {
         cg::cluster_group cl = cg::this_cluster();
-        for (int q = 0; q < CL && q < 16; ++q) rcnt[q] = cl.map_shared_rank(cnt, q);
-        if (lane < CL) pdst = cl.map_shared_rank(&pslot[0][0], lane);
+        if (lane < CL) pdst = reinterpret_cast<unsigned long long *>(cl.map_shared_rank(pslot, lane));
     }
     int8_t *gsig = jb.sigma + (int64_t)r * jb.N;
     int8_t *sig = sig_smem ? reinterpret_cast<int8_t *>(smem + L.sig) : gsig;
@@ -506,7 +508,8 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     // minimum are kept in it and turned into float64 at the samples and at the end
     constexpr bool FIX = std::is_same<Acc, double>::value;
     const bool fix = FIX && jb.fix_shift > 0;
-    const bool push = CLUSTER && fix;                  // partial dE per CTA pushed to the cluster (no remote count reads)
+    // fixed point over a cluster: per-warp partial dE into every CTA's accumulator, the decision in every thread
+    const bool wsum = CLUSTER && fix;
     const double fscale = fix ? ldexp(1.0, -jb.fix_shift) : 0.0;
     const double E0c = E;
     long long dsum = 0, dmin = 0;
@@ -516,28 +519,37 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
         for (int c = tid; c < n_cols; c += nt) efix[c] = (long long)__ldg(jb.ecol_fix + c);
     }
     int64_t nacc = 0, nnear = 0;
+    int64_t scd = jb.sample_interval, srow = 0;            // steps to the next sample, sample rows written (thread 0)
     const int R = jb.R;
     // proposals are drawn 32 at a time (one per lane of the producer warp), one batch ahead of their use
     const int64_t g0 = jb.step_dev ? *jb.step_dev : jb.step0;
-    if (tid == 0) near_flag = 0;
+    if (tid < 2) { near_flag[tid] = 0; pslot[tid] = 0; }
     if (warp == 0 && lane < jb.n_steps) bin_propose(jb, g0, lane, t, prop[lane]);
     __syncthreads();
     if (CLUSTER) cg::this_cluster().sync();              // every CTA's counters are zero before any remote add
     // counter buffer of the current evaluated swap: alternates between swaps that reach the row phase, so that a
     // cluster barrier always separates a CTA's clearing of a buffer from the next remote add into it
     int par = 0;
+    // the last accepted swap, not yet covered by a barrier (fixed-point form): sites and their new species
+    uint32_t pnd_a = 0xffffffffu, pnd_b = 0xffffffffu; int pnd_sa = 0, pnd_sb = 0;
+    auto occ = [&](uint32_t i) -> int {
+        return i == pnd_a ? pnd_sa : (i == pnd_b ? pnd_sb : (int)sig[i]);
+    };
     for (int64_t s = 0; s < jb.n_steps; ++s) {
         const BinProp &P = prop[s & 63];
         int32_t *cntp = cnt + par * n_cols;
-        const int64_t ia = P.ia, ib = P.ib;
+        // the producer overwrites this slot (with step s + 64) once it starts step s + 1: what the fixed-point
+        // decision needs is read now (sites are below 2^32)
+        const uint32_t ia = (uint32_t)P.ia, ib = (uint32_t)P.ib;
+        const int64_t thr = P.thr;
         if ((s & 31) == 0 && (nw == 1 ? true : warp == nw - 1)) {     // draw the next batch (steps s+32 .. s+63)
             const int64_t q = s + 32 + lane;
             if (q < jb.n_steps) bin_propose(jb, g0, q, t, prop[q & 63]);
         }
-        const int sa = sig[ia], sb = sig[ib];
+        const int sa = occ(ia), sb = occ(ib);
         if (sa != sb) {
             const int sa_new = sb, sb_new = sa;
-            // 1. neighbourhood bits (consumer threads); near_flag was cleared before the previous barrier
+            // 1. neighbourhood bits (consumer threads); near_flag[par] was cleared two evaluated swaps ago
             const int ct = ncons * 32;
             for (int q = tid; q < 2 * n_nbr && tid < ct; q += ct) {
                 const int side = q >= n_nbr, n = side ? q - n_nbr : q;
@@ -546,20 +558,28 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                 const int4 nbe = nbt[b0 * n_nbr + n];
                 const uint32_t st = ((((uint32_t)wrap_add(k[0], nbe.x, jb.d0) * (uint32_t)jb.d1 + (uint32_t)wrap_add(k[1], nbe.y, jb.d1)) *
                                       (uint32_t)jb.d2 + (uint32_t)wrap_add(k[2], nbe.z, jb.d2)) * (uint32_t)jb.nB + (uint32_t)nbe.w);
-                const int so = sig[st];
+                const int so = occ(st);
                 const int sn = (st == (uint32_t)ia) ? sa_new : ((st == (uint32_t)ib) ? sb_new : so);
                 const int isa = side && (st == (uint32_t)ia);
-                if (isa) near_flag = 1;
+                if (isa) near_flag[par] = 1;
                 uint8_t *bs = bits + (size_t)side * n_pfc * n_nbr;
                 for (int c = 0; c < n_pfc; ++c)
                     bs[c * n_nbr + n] = (uint8_t)(((smask >> (c * 4 + so)) & 1u) | (((smask >> (c * 4 + sn)) & 1u) << 1) | (isa << 2));
             }
-            __syncthreads();
+        }
+        if (wsum || sa != sb) {
+            __syncthreads();                               // with per-warp sums this barrier is passed on every step
+            pnd_a = pnd_b = 0xffffffffu;                   // the occupancy now holds every accepted swap
+        }
+        if (sa != sb) {
+            const int sa_new = sb, sb_new = sa;
+            if (wsum && tid == 0) pslot[par ^ 1] = 0;      // every warp of the cluster has read it (before this barrier)
+            long long pw = 0;                              // this warp's exact partial dE (fixed point)
             if (!producer || nw == 1) {
                 // 2. rows: column-aligned chunks of <= 32 rows (one lane per row); one integer reduction per chunk
                 const int nca = __ldg(jb.n_chunks + P.ba), ncb = __ldg(jb.n_chunks + P.bb);
                 const int total = nca + ncb;
-                const bool near = near_flag != 0;
+                const bool near = near_flag[par] != 0;
                 const int cw = nw > 1 ? warp : 0;
                 auto chunk_count = [&](int k, int &col) -> int {
                     const int side = k >= nca, kk = side ? k - nca : k;
@@ -594,61 +614,60 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                     const int s2 = k2 < total ? chunk_count(k2, c2) : 0;
                     const int n1 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s1);
                     const int n2 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s2);
-                    if (lane == 0) {
+                    if (wsum) pw += (long long)n1 * efix[c1] + (long long)n2 * efix[c2];
+                    if (lane == 0 && (!wsum || track)) {
                         if (n1) atomicAdd(&cntp[c1], n1);
                         if (n2) atomicAdd(&cntp[c2], n2);
                     }
                 }
-            }
-            // exact warp sum of |part| < 2^61 in three 21-bit slices (hardware 32-bit reductions, no carries lost)
-            auto exact_sum = [](long long part) -> long long {
-                const unsigned l0 = (unsigned)(part & 0x1fffff), l1 = (unsigned)((part >> 21) & 0x1fffff);
-                const int l2 = (int)(part >> 42);
-                const unsigned s0 = __reduce_add_sync(0xffffffffu, l0), s1 = __reduce_add_sync(0xffffffffu, l1);
-                const int s2 = __reduce_add_sync(0xffffffffu, l2);
-                return (long long)s0 + ((long long)s1 << 21) + ((long long)s2 << 42);
-            };
-            if (push) {
-                // each CTA turns its own counts into an exact partial dE and stores it into slot `rank` of every CTA
-                // of the cluster; after the barrier each CTA adds the partials from its own shared memory
-                __syncthreads();
-                if (warp == 0) {
-                    long long part = 0;
-                    for (int c = lane; c < n_cols; c += 32) { const int n = cntp[c]; if (n) part += (long long)n * efix[c]; }
-                    part = exact_sum(part);
-                    if (lane < CL) pdst[par * 16 + rank] = part;
-                }
+                if (wsum && pw != 0 && lane < CL) atomicAdd(pdst + par, (unsigned long long)pw);
             }
             if (CLUSTER) cg::this_cluster().sync(); else __syncthreads();
-            // 3. dE = sum_c 2 eci_c n_c (warp 0, fixed order), accept, write
-            if (warp == 0) {
-                // this swap's count of column c, summed over the cluster's CTAs (this CTA's own count when pushing)
+            // 3. dE = sum_c 2 eci_c n_c, accept, write
+            if (wsum) {
+                // every thread takes the decision; one thread writes the occupancy and the statistics
+                const long long part = pslot[par];
+                const bool accept = part < thr;
+                if (accept) { pnd_a = ia; pnd_b = ib; pnd_sa = sa_new; pnd_sb = sb_new; }
+                if (tid == 0) {
+                    const long long dd = part - thr;       // near the threshold: |dE 2^S - (-ln u / beta) 2^S| below the band
+                    nnear += (dd < 0 ? -dd : dd) < (long long)jb.near_fix;
+                    near_flag[par] = 0;
+                    if (accept) { sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new; dsum += part; ++nacc; }
+                }
+                if (track && warp == 0)                    // each changed row moves its column's sum by +-2
+                    for (int c = lane; c < n_cols; c += 32) {
+                        const int n = cntp[c];
+                        if (n) { if (accept) dcv[c] += 2 * n; cntp[c] = 0; }
+                    }
+            } else if (warp == 0) {
+                // this swap's count of column c, summed over the cluster's CTAs
                 auto count = [&](int c) -> int {
-                    if (!CLUSTER || push) return cntp[c];
+                    if (!CLUSTER) return cntp[c];
                     int n = 0;
-                    for (int q = 0; q < CL; ++q) n += rcnt[q][par * n_cols + c];
+                    for (int q = 0; q < CL; ++q) n += *cg::this_cluster().map_shared_rank(cntp + c, q);
                     return n;
                 };
-                if (CLUSTER && !push)                   // every CTA has read the other buffer (previous swap) by now
+                if (CLUSTER)                            // every CTA has read the other buffer (previous swap) by now
                     for (int c = lane; c < n_cols; c += 32) cnt[(par ^ 1) * n_cols + c] = 0;
                 bool accept;
                 if (fix) {
                     long long part = 0;
-                    if (push) {
-                        for (int q = 0; q < CL; ++q) part += pslot[par][q];
-                        if (!track)
-                            for (int c = lane; c < n_cols; c += 32) cntp[c] = 0;
-                    } else {
-                        for (int c = lane; c < n_cols; c += 32) {
-                            const int n = count(c);
-                            if (n) { part += (long long)n * efix[c]; if (!track && !CLUSTER) cntp[c] = 0; }
-                        }
-                        part = exact_sum(part);
+                    for (int c = lane; c < n_cols; c += 32) {
+                        const int n = count(c);
+                        if (n) { part += (long long)n * efix[c]; if (!track) cntp[c] = 0; }
                     }
-                    accept = part < P.thr;
+                    // exact warp sum of |part| < 2^61 in three 21-bit slices (hardware 32-bit reductions, no carries lost)
+                    const unsigned l0 = (unsigned)(part & 0x1fffff), l1 = (unsigned)((part >> 21) & 0x1fffff);
+                    const int l2 = (int)(part >> 42);
+                    const unsigned s0 = __reduce_add_sync(0xffffffffu, l0), s1 = __reduce_add_sync(0xffffffffu, l1);
+                    const int s2 = __reduce_add_sync(0xffffffffu, l2);
+                    part = (long long)s0 + ((long long)s1 << 21) + ((long long)s2 << 42);
+                    accept = part < thr;
                     if (lane == 0) {                    // near the threshold: |dE 2^S - (-ln u / beta) 2^S| below the band
-                        const long long dd = part - (long long)P.thr;
+                        const long long dd = part - thr;
                         nnear += (dd < 0 ? -dd : dd) < (long long)jb.near_fix;
+                        near_flag[par] = 0;
                     }
                     if (lane == 0 && accept) {
                         sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new;
@@ -662,8 +681,9 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                     }
                     part = warp_sum(part);              // butterfly: every lane holds the same sum
                     const double dEd = (double)part;
-                    accept = P.logu < -beta * dEd;
+                    accept = P.logu < -beta * dEd;     // the float form's barrier at the step end keeps P intact
                     if (lane == 0 && beta > 0.0) nnear += fabs(dEd + P.logu / beta) < jb.near_eV;
+                    if (lane == 0) near_flag[par] = 0;
                     if (lane == 0 && accept) {
                         sig[ia] = (int8_t)sa_new; sig[ib] = (int8_t)sb_new;
                         E += dEd; ++nacc;
@@ -672,37 +692,35 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                 if (track)                              // each changed row moves its column's sum by +-2
                     for (int c = lane; c < n_cols; c += 32) {
                         const int n = count(c);
-                        if (n) { if (accept) dcv[c] += 2 * n; if (!CLUSTER || push) cntp[c] = 0; }
+                        if (n) { if (accept) dcv[c] += 2 * n; if (!CLUSTER) cntp[c] = 0; }
                     }
             }
             par ^= 1;
         }
         if (tid == 0) {
-            near_flag = 0;
-            if (fix) {
-                dmin = dsum < dmin ? dsum : dmin;
-                if (rank == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
-                    jb.E_samples[((s + 1) / jb.sample_interval - 1) * R + t] = E0c + (double)dsum * fscale;
-            } else {
-                Emin = fmin(Emin, E);
-                if (rank == 0 && jb.E_samples && (s + 1) % jb.sample_interval == 0)
-                    jb.E_samples[((s + 1) / jb.sample_interval - 1) * R + t] = E;
+            if (fix) dmin = dsum < dmin ? dsum : dmin;
+            else Emin = fmin(Emin, E);
+            if (--scd == 0) {                              // a sample every sample_interval steps
+                scd = jb.sample_interval;
+                if (rank == 0 && jb.E_samples) jb.E_samples[srow * R + t] = fix ? E0c + (double)dsum * fscale : E;
+                ++srow;
             }
         }
-        __syncthreads();
+        if (!wsum) __syncthreads();                        // the decision warp has written the occupancy
     }
+    __syncthreads();                                       // every accepted swap is in the occupancy
     if (fix && tid == 0 && jb.n_steps > 0) {
         E = E0c + (double)dsum * fscale;
         Emin = fmin(Emin, E0c + (double)dmin * fscale);
     }
-    if (track && push)                                   // every CTA adds the changes its own rows counted
+    if (track && wsum)                                   // every CTA adds the changes its own rows counted
         for (int c = tid; c < n_cols; c += nt)
             if (dcv[c]) atomicAdd(reinterpret_cast<unsigned long long *>(jb.cv + (int64_t)r * n_cols + c),
                                   (unsigned long long)(long long)dcv[c]);
     if (rank == 0) {
         if (sig_smem)
             for (int64_t i = tid; i < jb.N; i += nt) gsig[i] = sig[i];
-        if (track && !push)
+        if (track && !wsum)
             for (int c = tid; c < n_cols; c += nt) jb.cv[(int64_t)r * n_cols + c] += dcv[c];
         if (sig_smem || track) __syncthreads();          // the replica's outputs are written before it is counted
         if (tid == 0) {
