@@ -242,6 +242,15 @@ __device__ __forceinline__ int find_job(const CEBatch &bt, int cta) {
     return j;
 }
 
+// job j's descriptor into shared memory (all threads of the CTA; synchronises)
+__device__ __forceinline__ void copy_job(const CEBatch &bt, int j, CEJob &dst) {
+    static_assert(sizeof(CEJob) % 4 == 0, "the descriptor is copied in 4-byte words");
+    const int *src = reinterpret_cast<const int *>(&bt.job[j]);
+    int *d = reinterpret_cast<int *>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(CEJob) / 4); i += blockDim.x) d[i] = src[i];
+    __syncthreads();
+}
+
 // proposal of slot t at global step g (same layout as the C oracle)
 __device__ __forceinline__ void propose(const CEJob &jb, int64_t g, int32_t t, int64_t &ia, int64_t &ib, double &u) {
     const uint32_t k0 = (uint32_t)jb.seed, k1 = (uint32_t)(jb.seed >> 32);
@@ -456,7 +465,11 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     if (CLUSTER) { cg::cluster_group cl = cg::this_cluster(); CL = (int)cl.num_blocks(); rank = (int)cl.block_rank(); }
     const int rep_idx = blockIdx.x / CL;
     const int j = find_job(bt, rep_idx);
-    const CEJob &jb = bt.job[j];
+    // the job's descriptor in shared memory: kernel-parameter reads at a computed job index go through the constant
+    // cache, which the batch descriptor (up to 31 KB) overflows, and the step loop reads the descriptor throughout
+    __shared__ CEJob sjob;
+    copy_job(bt, j, sjob);
+    const CEJob &jb = sjob;
     const int r = rep_idx - jb.cta_base;
     if (r >= jb.R) return;
     const int tid = threadIdx.x, nt = blockDim.x, nw = nt >> 5, lane = tid & 31, warp = tid >> 5;
@@ -883,7 +896,9 @@ __global__ void __launch_bounds__(32 * kLfMaxWarps) ce_lf_chunk_kernel(const __g
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ LfStep X;
     const int j = find_job(bt, blockIdx.x);
-    const CEJob &jb = bt.job[j];
+    __shared__ CEJob sjob;                            // the descriptor in shared memory (see ce_bin_chunk_kernel)
+    copy_job(bt, j, sjob);
+    const CEJob &jb = sjob;
     const int r = blockIdx.x - jb.cta_base;
     if (r >= jb.R) return;
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
