@@ -39,9 +39,10 @@ CONTRACTIONS = ["fp32 CUDA cores", "bf16 mma.sync tensor cores (fp32 accumulatio
                 "split-bf16 tcgen05 tensor cores"]
 H100_PUBLISHED = 1_231_993.0          # reference CE PT, 2,048 sites, R=32, H100 (results/bench_stage/gpu_icet_*H100*.json)
 B_GATHER = 14_996                     # bytes of member occupancy per attempt, config-0 cluster set
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of the headline chunk,
-# keyed by (path, L, R, steps per chunk): profiles/ holds the captures
-TRAFFIC = {(2, 8, 32, 5000): 155_392}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of the headline kernel,
+# keyed by (path, L, R, steps per chunk): profiles/ holds the capture (a 1000-step chunk; the tables and occupancy
+# are read once per launch, so the figure does not grow with the steps)
+TRAFFIC = {(2, 8, 32, 5000): 168_448}
 
 
 def parse():
@@ -693,7 +694,8 @@ def main():
         ws = (args.warps,) if args.warps else (4, 8, 16, 32)
         cls = (args.cluster,) if args.cluster else ((1, 2, 4, 8, 16) if args.path != 1 else (1,))
         paths = (2, 3) if args.path == 0 else (args.path,)
-        (args.warps, args.cluster, args.path), t = best_launch(gce, st, args.precision, args.path, ws, cls, paths=paths)
+        (args.warps, args.cluster, args.path), t = best_launch(gce, st, args.precision, args.path, ws, cls, steps=1000,
+                                                               paths=paths)
         tuned = {f"{w}x{c}/p{p}": round(v, 3) for (w, c, p), v in t.items()}
     if args.path == 3:
         st.enable_field(gce)                               # local fields of the replicas' occupancies
