@@ -386,16 +386,15 @@ struct BinProp {
 };
 
 struct BinLayout {
-    size_t bix, rcol, chunk, nb, ecol, sig, bits, cnt, dcv, total;
+    size_t bix, chunk, nb, ecol, sig, bits, cnt, dcv, total;
     __host__ __device__ static BinLayout make(int nB, int J, int mo, int n_nbr, int n_pfc, int n_cols, int max_chunks, size_t acc_bytes,
                                                 int64_t N, bool tables, bool sig_smem) {
         BinLayout L; size_t o = 0;
         auto al = [](size_t x, size_t a) { return (x + a - 1) / a * a; };
         if (tables) {
             L.bix = o; o = al(o + sizeof(uint16_t) * (size_t)nB * J * mo, 16);
-            L.rcol = o; o = al(o + (size_t)nB * J, 16);
         } else {
-            L.bix = L.rcol = 0;
+            L.bix = 0;
         }
         L.chunk = o; o = al(o + sizeof(uint32_t) * (size_t)nB * max_chunks, 16);
         L.nb = o; o = al(o + sizeof(int32_t) * 4 * (size_t)nB * n_nbr, 16);
@@ -446,7 +445,7 @@ __device__ __forceinline__ void bin_propose(const CEJob &jb, int64_t g0, int64_t
     site_coords32(jb, ia, P.ba, P.ka); site_coords32(jb, ib, P.bb, P.kb);
 }
 
-template <typename Acc, int MO, bool CLUSTER>
+template <typename Acc, int MO, bool CLUSTER, bool SMT>
 __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constant__ CEBatch bt, int32_t sig_budget) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ BinProp prop[64];                      // ring of two batches of 32 proposals
@@ -477,17 +476,18 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     const bool producer = nw > 1 ? (warp == nw - 1) : (tid == 0);
     const int n_nbr = jb.n_nbr, n_pfc = jb.n_pfc, n_cols = jb.n_cols;
     const int32_t sig_smem = jb.sig_smem;
-    const BinLayout L = BinLayout::make(jb.nB, jb.J, MO, n_nbr, n_pfc, n_cols, jb.max_chunks, sizeof(Acc), sig_budget, bt.tables_in_smem,
+    const BinLayout L = BinLayout::make(jb.nB, jb.J, MO, n_nbr, n_pfc, n_cols, jb.max_chunks, sizeof(Acc), sig_budget, SMT,
                                         sig_budget > 0);
-    const uint16_t *tbix; const uint8_t *trcol;
-    const size_t nl = (size_t)jb.nB * jb.J * MO, ne = (size_t)jb.nB * jb.J;
-    if (bt.tables_in_smem) {
-        uint16_t *sb = reinterpret_cast<uint16_t *>(smem + L.bix); uint8_t *sc = smem + L.rcol;
+    // SMT (the launch's tables fit in shared memory): the member table is staged there, and the compiler sees a
+    // shared-memory pointer (32-bit addresses, shared loads); otherwise it is read from global memory
+    const uint16_t *tbix;
+    const size_t nl = (size_t)jb.nB * jb.J * MO;
+    if (SMT) {
+        uint16_t *sb = reinterpret_cast<uint16_t *>(smem + L.bix);
         for (size_t i = tid; i < nl; i += nt) sb[i] = __ldg(jb.bix + i);
-        for (size_t i = tid; i < ne; i += nt) sc[i] = __ldg(jb.rcol + i);
-        tbix = sb; trcol = sc;
+        tbix = sb;
     } else {
-        tbix = jb.bix; trcol = jb.rcol;
+        tbix = jb.bix;
     }
     uint32_t *chunks = reinterpret_cast<uint32_t *>(smem + L.chunk);        // [basis][k]: col | start << 8 | len << 24
     for (int i = tid; i < jb.nB * jb.max_chunks; i += nt) chunks[i] = __ldg(jb.chunks + i);
@@ -501,11 +501,6 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     const bool track = jb.cv != nullptr;
     for (int c = tid; c < n_cols; c += nt) { ecol[c] = gecol[c]; cnt[c] = 0; cnt[n_cols + c] = 0; dcv[c] = 0; }
     __shared__ long long pslot[2];                    // fixed-point dE accumulator of the evaluated swap [parity]
-    unsigned long long *pdst = reinterpret_cast<unsigned long long *>(pslot);   // lane q adds into CTA q's accumulator
-    if (CLUSTER) {
-        cg::cluster_group cl = cg::this_cluster();
-        if (lane < CL) pdst = reinterpret_cast<unsigned long long *>(cl.map_shared_rank(pslot, lane));
-    }
     int8_t *gsig = jb.sigma + (int64_t)r * jb.N;
     int8_t *sig = sig_smem ? reinterpret_cast<int8_t *>(smem + L.sig) : gsig;
     if (sig_smem)
@@ -516,23 +511,23 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
         for (int q = 0; q < 4; ++q) smask |= (uint32_t)(__ldg(jb.sbits + c * 4 + q) & 1u) << (c * 4 + q);
     const int32_t t = jb.slot_of_rep[r];
     const double beta = (double)jb.beta_slot[t];
-    double E = jb.E[r], Emin = jb.E_min_rep[r];
     // float64: the step's dE is an exact fixed-point integer sum (x 2^S); the chunk's energy change and its running
-    // minimum are kept in it and turned into float64 at the samples and at the end
+    // minimum are kept in it and turned into float64 at the samples and at the end (from the chunk's first energy,
+    // which no one writes before the end of the chunk); float32 carries the energy
     constexpr bool FIX = std::is_same<Acc, double>::value;
-    const bool fix = FIX && jb.fix_shift > 0;
+    constexpr bool fix = FIX;                            // float64 launches need fixed point (checked on the host)
     // fixed point over a cluster: per-warp partial dE into every CTA's accumulator, the decision in every thread
-    const bool wsum = CLUSTER && fix;
-    const double fscale = fix ? ldexp(1.0, -jb.fix_shift) : 0.0;
-    const double E0c = E;
+    constexpr bool wsum = CLUSTER && fix;
+    double E = fix ? 0.0 : jb.E[r], Emin = fix ? 0.0 : jb.E_min_rep[r];
+    auto fixed_energy = [&](long long d) -> double { return jb.E[r] + (double)d * ldexp(1.0, -jb.fix_shift); };
     long long dsum = 0, dmin = 0;
     long long *efix = reinterpret_cast<long long *>(ecol);
     if (fix) {
         __syncthreads();                                   // ecol (float64) was just written; the same bytes take the fixed-point values
         for (int c = tid; c < n_cols; c += nt) efix[c] = (long long)__ldg(jb.ecol_fix + c);
     }
-    int64_t nacc = 0, nnear = 0;
-    int64_t scd = jb.sample_interval, srow = 0;            // steps to the next sample, sample rows written (thread 0)
+    int32_t nacc = 0, nnear = 0;                           // a chunk has fewer than 2^31 steps (checked on the host)
+    int32_t scd = (int32_t)min(jb.sample_interval, jb.n_steps + 1), srow = 0;   // steps to the next sample, rows written
     const int R = jb.R;
     // proposals are drawn 32 at a time (one per lane of the producer warp), one batch ahead of their use
     const int64_t g0 = jb.step_dev ? *jb.step_dev : jb.step0;
@@ -548,7 +543,8 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     auto occ = [&](uint32_t i) -> int {
         return i == pnd_a ? pnd_sa : (i == pnd_b ? pnd_sb : (int)sig[i]);
     };
-    for (int64_t s = 0; s < jb.n_steps; ++s) {
+    const int32_t n_steps = (int32_t)jb.n_steps;
+    for (int32_t s = 0; s < n_steps; ++s) {
         const BinProp &P = prop[s & 63];
         int32_t *cntp = cnt + par * n_cols;
         // the producer overwrites this slot (with step s + 64) once it starts step s + 1: what the fixed-point
@@ -556,8 +552,8 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
         const uint32_t ia = (uint32_t)P.ia, ib = (uint32_t)P.ib;
         const int64_t thr = P.thr;
         if ((s & 31) == 0 && (nw == 1 ? true : warp == nw - 1)) {     // draw the next batch (steps s+32 .. s+63)
-            const int64_t q = s + 32 + lane;
-            if (q < jb.n_steps) bin_propose(jb, g0, q, t, prop[q & 63]);
+            const int32_t q = s + 32 + lane;
+            if (q < n_steps) bin_propose(jb, g0, q, t, prop[q & 63]);
         }
         const int sa = occ(ia), sb = occ(ib);
         if (sa != sb) {
@@ -590,21 +586,26 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
             long long pw = 0;                              // this warp's exact partial dE (fixed point)
             if (!producer || nw == 1) {
                 // 2. rows: column-aligned chunks of <= 32 rows (one lane per row); one integer reduction per chunk
-                const int nca = __ldg(jb.n_chunks + P.ba), ncb = __ldg(jb.n_chunks + P.bb);
+                // per-side bases held in registers for the loop (shared-memory atomics below could alias the
+                // descriptor and proposal, which would otherwise be re-read every chunk)
+                const int ba = P.ba, bb = P.bb;
+                const int nca = __ldg(jb.n_chunks + ba), ncb = __ldg(jb.n_chunks + bb);
                 const int total = nca + ncb;
                 const bool near = near_flag[par] != 0;
                 const int cw = nw > 1 ? warp : 0;
+                const int maxc = jb.max_chunks, J = jb.J;
+                const int offa = ba * maxc, offb = bb * maxc - nca;     // chunk k of side a / side b (k >= nca)
+                const uint16_t *rwa = tbix + (size_t)ba * J * MO, *rwb = tbix + (size_t)bb * J * MO;
+                const uint8_t *bsb = bits + (size_t)n_pfc * n_nbr;
                 auto chunk_count = [&](int k, int &col) -> int {
-                    const int side = k >= nca, kk = side ? k - nca : k;
-                    const int b0 = side ? P.bb : P.ba;
-                    const uint32_t d = chunks[b0 * jb.max_chunks + kk];
+                    const bool side = k >= nca;
+                    const uint32_t d = chunks[(side ? offb : offa) + k];
                     col = (int)(d & 0xffu);
                     const int start = (int)((d >> 8) & 0xffffu), len = (int)(d >> 24);
                     int sgn = 0;
                     if (lane < len) {
-                        const int rr = start + lane;
-                        const uint16_t *bx = tbix + ((size_t)b0 * jb.J + rr) * MO;
-                        const uint8_t *bs = bits + (size_t)side * n_pfc * n_nbr;
+                        const uint16_t *bx = (side ? rwb : rwa) + (start + lane) * MO;
+                        const uint8_t *bs = side ? bsb : bits;
                         unsigned x = 0, y = 0;
                         if (MO == 4) {
                             const uint2 w = *reinterpret_cast<const uint2 *>(bx);
@@ -633,7 +634,9 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                         if (n2) atomicAdd(&cntp[c2], n2);
                     }
                 }
-                if (wsum && pw != 0 && lane < CL) atomicAdd(pdst + par, (unsigned long long)pw);
+                if (wsum && pw != 0 && lane < CL)           // lane q adds into CTA q's accumulator
+                    atomicAdd(reinterpret_cast<unsigned long long *>(cg::this_cluster().map_shared_rank(pslot + par, lane)),
+                              (unsigned long long)pw);
             }
             if (CLUSTER) cg::this_cluster().sync(); else __syncthreads();
             // 3. dE = sum_c 2 eci_c n_c, accept, write
@@ -714,17 +717,17 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
             if (fix) dmin = dsum < dmin ? dsum : dmin;
             else Emin = fmin(Emin, E);
             if (--scd == 0) {                              // a sample every sample_interval steps
-                scd = jb.sample_interval;
-                if (rank == 0 && jb.E_samples) jb.E_samples[srow * R + t] = fix ? E0c + (double)dsum * fscale : E;
+                scd = (int32_t)jb.sample_interval;
+                if (rank == 0 && jb.E_samples) jb.E_samples[(int64_t)srow * R + t] = fix ? fixed_energy(dsum) : E;
                 ++srow;
             }
         }
         if (!wsum) __syncthreads();                        // the decision warp has written the occupancy
     }
     __syncthreads();                                       // every accepted swap is in the occupancy
-    if (fix && tid == 0 && jb.n_steps > 0) {
-        E = E0c + (double)dsum * fscale;
-        Emin = fmin(Emin, E0c + (double)dmin * fscale);
+    if (fix && tid == 0) {
+        E = fixed_energy(dsum);
+        Emin = jb.n_steps > 0 ? fmin(jb.E_min_rep[r], fixed_energy(dmin)) : jb.E_min_rep[r];
     }
     if (track && wsum)                                   // every CTA adds the changes its own rows counted
         for (int c = tid; c < n_cols; c += nt)
@@ -1539,14 +1542,14 @@ static int launch_chunk_mo(const CEBatch &bt, int total, int warps, size_t smem,
     return NCE_OK;
 }
 
-template <typename Acc, int MO>
-static int launch_bin_mo(const CEBatch &bt, int total, int warps, size_t smem, int sig_smem, cudaStream_t s, int CL) {
+template <typename Acc, int MO, bool SMT>
+static int launch_bin_smt(const CEBatch &bt, int total, int warps, size_t smem, int sig_smem, cudaStream_t s, int CL) {
     if (CL <= 1) {
-        auto kern = ce_bin_chunk_kernel<Acc, MO, false>;
+        auto kern = ce_bin_chunk_kernel<Acc, MO, false, SMT>;
         NCE_CUDA(::nce::raise_smem_limit((const void *)kern, smem));
         kern<<<total, warps * 32, smem, s>>>(bt, sig_smem);
     } else {
-        auto kern = ce_bin_chunk_kernel<Acc, MO, true>;
+        auto kern = ce_bin_chunk_kernel<Acc, MO, true, SMT>;
         NCE_CUDA(::nce::raise_smem_limit((const void *)kern, smem));
         // 16 CTAs per cluster is beyond the portable size of 8 (allowed on this GPU)
         if (CL > 8) NCE_CUDA(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
@@ -1560,6 +1563,12 @@ static int launch_bin_mo(const CEBatch &bt, int total, int warps, size_t smem, i
     }
     NCE_CUDA(cudaGetLastError());
     return NCE_OK;
+}
+
+template <typename Acc, int MO>
+static int launch_bin_mo(const CEBatch &bt, int total, int warps, size_t smem, int sig_smem, cudaStream_t s, int CL) {
+    return bt.tables_in_smem ? launch_bin_smt<Acc, MO, true>(bt, total, warps, smem, sig_smem, s, CL)
+                             : launch_bin_smt<Acc, MO, false>(bt, total, warps, smem, sig_smem, s, CL);
 }
 
 template <typename Acc>
@@ -1616,7 +1625,7 @@ static int check_state(const nce_ce_model *m, const nce_pt_state *st) {
 
 static int check_chunk(const nce_pt_state *st, const nce_pt_chunk *ck) {
     NCE_CHECK(ck, "chunk: null");
-    NCE_CHECK(ck->n_steps >= 0, "chunk: n_steps < 0");
+    NCE_CHECK(ck->n_steps >= 0 && ck->n_steps < 2147483647ll, "chunk: n_steps must be in [0, 2^31 - 1)");
     NCE_CHECK(ck->precision == 64 || ck->precision == 32, "chunk: precision must be 64 or 32");
     NCE_CHECK((ck->prop_a == nullptr) == (ck->prop_b == nullptr) && (ck->prop_a == nullptr) == (ck->prop_u == nullptr),
               "chunk: prop_a/prop_b/prop_u must be all set or all NULL");
@@ -1666,7 +1675,13 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
         NCE_CHECK(precision == 64, "chunk: the local-field path computes in fixed point (precision 64)");
     }
     const bool use_lf = path == 3 || (path == 0 && all_lf);
-    const bool use_bin = !use_lf && ((path == 2) || (path == 0 && all_bin));
+    // the float64 sign-parity kernel sums in fixed point: a table whose column eci allow no exact fixed point (never
+    // for eci of physical size) runs the general kernel
+    bool all_fix = true;
+    for (int j = 0; j < n_jobs; ++j) all_fix = all_fix && hs[j]->fix_shift > 0;
+    NCE_CHECK(!(path == 2 && precision == 64 && !all_fix),
+              "chunk: the float64 sign-parity path needs fixed-point column eci (2 J max|eci| below 2^41)");
+    const bool use_bin = !use_lf && ((path == 2) || (path == 0 && all_bin && (precision == 32 || all_fix)));
     for (int j = 0; j < n_jobs; ++j)
         NCE_CHECK(!sts[j].cv || use_bin || use_lf, "chunk: tracked cluster-vector sums need the sign-parity or local-field path");
     CEBatch bt; std::memset(&bt, 0, sizeof(bt));
