@@ -545,16 +545,20 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     };
     const int32_t n_steps = (int32_t)jb.n_steps;
     for (int32_t s = 0; s < n_steps; ++s) {
+        // a step whose two sites hold the same species changes nothing and passes no barrier; every 32 steps one
+        // barrier lets the producer refill the half of the ring that the last 32 steps used
+        if ((s & 31) == 0) {
+            __syncthreads();
+            pnd_a = pnd_b = 0xffffffffu;                   // the occupancy holds every accepted swap
+            if (nw == 1 ? true : warp == nw - 1) {         // draw the next batch (steps s+32 .. s+63)
+                const int32_t q = s + 32 + lane;
+                if (q < n_steps) bin_propose(jb, g0, q, t, prop[q & 63]);
+            }
+        }
         const BinProp &P = prop[s & 63];
         int32_t *cntp = cnt + par * n_cols;
-        // the producer overwrites this slot (with step s + 64) once it starts step s + 1: what the fixed-point
-        // decision needs is read now (sites are below 2^32)
-        const uint32_t ia = (uint32_t)P.ia, ib = (uint32_t)P.ib;
+        const uint32_t ia = (uint32_t)P.ia, ib = (uint32_t)P.ib;        // sites are below 2^32
         const int64_t thr = P.thr;
-        if ((s & 31) == 0 && (nw == 1 ? true : warp == nw - 1)) {     // draw the next batch (steps s+32 .. s+63)
-            const int32_t q = s + 32 + lane;
-            if (q < n_steps) bin_propose(jb, g0, q, t, prop[q & 63]);
-        }
         const int sa = occ(ia), sb = occ(ib);
         if (sa != sb) {
             const int sa_new = sb, sb_new = sa;
@@ -576,11 +580,9 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                     bs[c * n_nbr + n] = (uint8_t)(((smask >> (c * 4 + so)) & 1u) | (((smask >> (c * 4 + sn)) & 1u) << 1) | (isa << 2));
             }
         }
-        if (wsum || sa != sb) {
-            __syncthreads();                               // with per-warp sums this barrier is passed on every step
-            pnd_a = pnd_b = 0xffffffffu;                   // the occupancy now holds every accepted swap
-        }
         if (sa != sb) {
+            __syncthreads();
+            pnd_a = pnd_b = 0xffffffffu;                   // the occupancy now holds every accepted swap
             const int sa_new = sb, sb_new = sa;
             if (wsum && tid == 0) pslot[par ^ 1] = 0;      // every warp of the cluster has read it (before this barrier)
             long long pw = 0;                              // this warp's exact partial dE (fixed point)
@@ -711,6 +713,7 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                         if (n) { if (accept) dcv[c] += 2 * n; if (!CLUSTER) cntp[c] = 0; }
                     }
             }
+            if (!wsum) __syncthreads();                    // the decision warp has written the occupancy
             par ^= 1;
         }
         if (tid == 0) {
@@ -722,7 +725,6 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                 ++srow;
             }
         }
-        if (!wsum) __syncthreads();                        // the decision warp has written the occupancy
     }
     __syncthreads();                                       // every accepted swap is in the occupancy
     if (fix && tid == 0) {
