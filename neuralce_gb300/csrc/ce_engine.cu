@@ -592,54 +592,66 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                 // descriptor and proposal, which would otherwise be re-read every chunk)
                 const int ba = P.ba, bb = P.bb;
                 const int nca = __ldg(jb.n_chunks + ba), ncb = __ldg(jb.n_chunks + bb);
-                const int total = nca + ncb;
                 const bool near = near_flag[par] != 0;
                 const int cw = nw > 1 ? warp : 0;
                 const int maxc = jb.max_chunks, J = jb.J;
-                const int offa = ba * maxc, offb = bb * maxc - nca;     // chunk k of side a / side b (k >= nca)
+                const int offa = ba * maxc, offb = bb * maxc;            // chunk k of side a / side b
                 const uint16_t *rwa = tbix + (size_t)ba * J * MO, *rwb = tbix + (size_t)bb * J * MO;
                 const uint8_t *bsb = bits + (size_t)n_pfc * n_nbr;
                 // a rows loop per kind of step: with the other site in the neighbourhood (near) the rows of b that
                 // contain a were counted with a and are skipped; otherwise no row needs that test
                 auto rows = [&](auto near_c) {
                     constexpr bool NEAR = decltype(near_c)::value;
-                    auto chunk_count = [&](int k, int &col) -> int {
-                        const bool side = k >= nca;
-                        const uint32_t d = chunks[(side ? offb : offa) + k];
+                    // chunk k of one side: the sign of each row's change, one lane per row
+                    auto chunk_count = [&](auto side_c, int k, int &col) -> int {
+                        constexpr bool SIDE = decltype(side_c)::value;
+                        const uint32_t d = chunks[(SIDE ? offb : offa) + k];
                         col = (int)(d & 0xffu);
                         const int start = (int)((d >> 8) & 0xffffu), len = (int)(d >> 24);
                         int sgn = 0;
                         if (lane < len) {
-                            const uint16_t *bx = (side ? rwb : rwa) + (start + lane) * MO;
-                            const uint8_t *bs = side ? bsb : bits;
+                            const uint16_t *bx = (SIDE ? rwb : rwa) + (start + lane) * MO;
+                            const uint8_t *bs = SIDE ? bsb : bits;
                             unsigned x = 0, y = 0;
                             if (MO == 4) {
                                 const uint2 w = *reinterpret_cast<const uint2 *>(bx);
                                 const unsigned v0 = bs[w.x & 0xffffu], v1 = bs[w.x >> 16], v2 = bs[w.y & 0xffffu], v3 = bs[w.y >> 16];
                                 x = v0 ^ v1 ^ v2 ^ v3;
-                                if (NEAR) y = v0 | v1 | v2 | v3;
+                                if (NEAR && SIDE) y = v0 | v1 | v2 | v3;
                             } else {
 #pragma unroll
-                                for (int m = 0; m < MO; ++m) { const unsigned vv = bs[bx[m]]; x ^= vv; if (NEAR) y |= vv; }
+                                for (int m = 0; m < MO; ++m) { const unsigned vv = bs[bx[m]]; x ^= vv; if (NEAR && SIDE) y |= vv; }
                             }
-                            const bool skip = NEAR && side && (y & 4u);
+                            const bool skip = NEAR && SIDE && (y & 4u);
                             if (!skip && ((x ^ (x >> 1)) & 1u)) sgn = (x & 1u) ? 1 : -1;   // odd old parity: Pi -1 -> +1
                         }
                         return sgn;
                     };
-                    const int gw = rank * ncons + cw, gstr = ncons * CL;     // consumer warps of the whole cluster
-                    for (int k = gw; k < total; k += 2 * gstr) {
-                        const int k2 = k + gstr;
-                        int c1 = 0, c2 = 0;
-                        const int s1 = chunk_count(k, c1);
-                        const int s2 = k2 < total ? chunk_count(k2, c2) : 0;
-                        const int n1 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s1);
-                        const int n2 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s2);
-                        if (wsum) pw += (long long)n1 * efix[c1] + (long long)n2 * efix[c2];
-                        if (lane == 0 && (!wsum || track)) {
-                            if (n1) atomicAdd(&cntp[c1], n1);
-                            if (n2) atomicAdd(&cntp[c2], n2);
+                    // the consumer warps of the whole cluster are split between the two sides in proportion to their
+                    // chunks; a warp takes its side's chunks round-robin, two at a time
+                    const int gw = rank * ncons + cw, gstr = ncons * CL;
+                    auto side_loop = [&](auto side_c, int n, int k0, int stride) {
+                        for (int k = k0; k < n; k += 2 * stride) {
+                            const int k2 = k + stride;
+                            int c1 = 0, c2 = 0;
+                            const int s1 = chunk_count(side_c, k, c1);
+                            const int s2 = k2 < n ? chunk_count(side_c, k2, c2) : 0;
+                            const int n1 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s1);
+                            const int n2 = (int)__reduce_add_sync(0xffffffffu, (unsigned)s2);
+                            if (wsum) pw += (long long)n1 * efix[c1] + (long long)n2 * efix[c2];
+                            if (lane == 0 && (!wsum || track)) {
+                                if (n1) atomicAdd(&cntp[c1], n1);
+                                if (n2) atomicAdd(&cntp[c2], n2);
+                            }
                         }
+                    };
+                    if (gstr >= 2) {
+                        const int wa = min(gstr - 1, max(1, (gstr * nca + (nca + ncb) / 2) / max(1, nca + ncb)));
+                        if (gw < wa) side_loop(std::false_type{}, nca, gw, wa);
+                        else side_loop(std::true_type{}, ncb, gw - wa, gstr - wa);
+                    } else {
+                        side_loop(std::false_type{}, nca, 0, 1);
+                        side_loop(std::true_type{}, ncb, 0, 1);
                     }
                 };
                 if (near) rows(std::true_type{}); else rows(std::false_type{});
