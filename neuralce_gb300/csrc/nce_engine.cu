@@ -397,6 +397,35 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
                     if (need_shell) xput(mm, Cin + c, a * inv);
                 }
             }
+        } else if (Cin <= 20 && (Cin & 1) == 0 && W <= 32) {
+            // narrow inputs and wide shells (the reference's shipped model: 18 channels, shells of 12 / 6 / 24): a lane
+            // takes one channel pair of one of three sites per warp (Cin / 2 lanes a site, 8-byte loads), all partner
+            // loads of one shell in flight; each channel's sum runs over the W slots in order, as below
+            const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+            const int hc = Cin >> 1, sl = lane / hc, c0 = 2 * (lane - sl * hc);
+            for (int m0 = warp * 3; m0 < tm; m0 += nwarp * 3) {
+                const int mm = m0 + (sl < 3 ? sl : 0);
+                const bool ok = sl < 3 && mm < tm;
+                const float *const *sr = srcp + (ok ? mm : m0) * PW;
+                if (ok) {
+                    const float2 x = *reinterpret_cast<const float2 *>(sr[0] + c0);
+                    xput2(mm, c0, x.x, x.y);
+                }
+                const int b = tk[ok ? mm : m0].x;
+                for (int p = 0; p < P; ++p) {
+                    float2 v[32];
+#pragma unroll
+                    for (int u = 0; u < 32; ++u)
+                        v[u] = (ok && u < W) ? *reinterpret_cast<const float2 *>(sr[1 + p * W + u] + c0) : make_float2(0.f, 0.f);
+                    float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+                    for (int u = 0; u < 32; ++u) { s0 += v[u].x; s1 += v[u].y; }
+                    if (ok) {
+                        const float inv = m.Sh_inv[b * P + p];
+                        xput2(mm, Cin + p * Cin + c0, s0 * inv, s1 * inv);
+                    }
+                }
+            }
         } else if (Cin <= 32 && W <= 32) {
             // narrow inputs and wide shells (the reference's shipped model: 18 channels, shells of 12 / 6 / 24):
             // one lane per channel, two sites per warp, all partner loads of one shell of both sites in flight
