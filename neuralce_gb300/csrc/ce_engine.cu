@@ -559,6 +559,20 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
         int32_t *cntp = cnt + par * n_cols;
         const uint32_t ia = (uint32_t)P.ia, ib = (uint32_t)P.ib;        // sites are below 2^32
         const int64_t thr = P.thr;
+        if (!sig_smem && s + 1 < n_steps) {
+            // occupancy in global memory (cells beyond the shared-memory budget): the next step's two
+            // neighbourhoods are fetched into L2 while this step runs, one site a consumer thread (a step's first
+            // reads would otherwise wait on DRAM); the slot of step s + 1 is not refilled before step s + 33
+            const BinProp &Q = prop[(s + 1) & 63];
+            for (int q = tid; q < 2 * n_nbr && tid < ncons * 32; q += ncons * 32) {
+                const int side = q >= n_nbr, n = side ? q - n_nbr : q;
+                const int32_t *k = side ? Q.kb : Q.ka;
+                const int4 nbe = nbt[(side ? Q.bb : Q.ba) * n_nbr + n];
+                const uint32_t st = ((((uint32_t)wrap_add(k[0], nbe.x, jb.d0) * (uint32_t)jb.d1 + (uint32_t)wrap_add(k[1], nbe.y, jb.d1)) *
+                                      (uint32_t)jb.d2 + (uint32_t)wrap_add(k[2], nbe.z, jb.d2)) * (uint32_t)jb.nB + (uint32_t)nbe.w);
+                asm volatile("prefetch.global.L2 [%0];" :: "l"(gsig + st));
+            }
+        }
         const int sa = occ(ia), sb = occ(ib);
         if (sa != sb) {
             const int sa_new = sb, sb_new = sa;
