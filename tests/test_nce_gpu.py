@@ -208,7 +208,7 @@ def _model_bench_mma(L, seed, mma, width=64):
                                        (2, 128), (2, 16)])
 def test_tensor_core_forms_vs_oracle(cuda, mma, width):
     """Layer contractions on tensor cores (mma.sync: 1, 3; tcgen05 with tensor-memory accumulators: 2, 4).  The split
-    bf16 forms (3, 4) -- the precision form -- stay within the benchmark spec's bound of 1e-4 eV per swap and the float32
+    bf16 forms (3, 4) -- the precision form -- stay within the NeuralCE per-swap bound of 1e-4 eV and the float32
     energy bound; at width 128 the tcgen05 split form stages its A operand in two K slices.  Plain bf16 operands
     (1, 2) are a labelled comparison point with their own stated bound of 1e-2 eV per swap (measured ~5e-3 eV on
     this model, whose total energy is ~1e2 eV).  A chain of forced moves keeps the carried energy equal to a rebuild
