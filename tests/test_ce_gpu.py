@@ -243,6 +243,18 @@ def test_sign_parity_small_cells(cuda, L):
     _compare(a, ref, 1e-9); _compare(b, ref, 1e-9); _compare(c, ref, 1e-9)
 
 
+def test_chunk_of_two_billion_steps_is_refused(cuda):
+    """The chunk kernels count steps in 32 bits: a chunk of 2^31 - 1 steps or more is refused before any launch."""
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.pt import run_chunk
+    gce, orc, sig_r, beta = _setup(3, R=2)
+    E0 = np.array([orc.energy(x) for x in sig_r])
+    st = _engine_state(sig_r, E0, beta)
+    with pytest.raises(_lib.NceError, match="n_steps"):
+        run_chunk(gce, st, 2 ** 31, 0, 0, 64, 4, path=2)
+    assert np.array_equal(st.sigma.cpu().numpy(), sig_r)
+
+
 def test_out_of_range_proposal_is_flagged(cuda):
     """A proposal index outside [0, N) is rejected by the kernel's bounds check and reported, not read."""
     torch = cuda

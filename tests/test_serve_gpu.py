@@ -204,3 +204,26 @@ def test_nce_jobs_sharing_a_model(cuda):
         assert all(i["status"] == "done" for i in infos), infos
         for h, a in zip(hs, alone):
             _same(h.result(), a)
+
+
+def test_submit_refuses_unknown_flags_and_bad_output_buffers(cuda):
+    """Descriptor flags other than NCE_JOB_BORROW_SIGMA are refused at submission, and so is an output buffer of the
+    wrong shape; nothing is queued."""
+    import ctypes as C
+    from neuralce_gb300 import _lib
+    from neuralce_gb300.serve import Server
+    j = _ce_jobs()[0]
+    with Server() as srv:
+        R, N = j["sigma"].shape
+        with pytest.raises(ValueError, match="sigma_out"):
+            srv.submit_ce(j["model"], j["sigma"], j["beta"], 100, 50, 1, sigma_out=np.zeros((R, N + 1), np.int8))
+        sig = np.ascontiguousarray(j["sigma"]); beta = np.ascontiguousarray(j["beta"], np.float32)
+        out = np.zeros_like(sig)
+        d = _lib.NceJobDesc()
+        d.kind, d.model, d.R = 0, j["model"].handle.value, R
+        d.sigma, d.beta_slot, d.n_steps, d.exchange_every, d.seed = sig.ctypes.data, beta.ctypes.data, 100, 50, 1
+        d.sigma_out = out.ctypes.data
+        d.flags = 2
+        jid = C.c_int64()
+        assert _lib.lib().nce_job_submit(srv._h, C.byref(d), C.byref(jid)) == -1      # NCE_ERR_INVALID
+        assert srv.stats()["queued"] == 0 and srv.stats()["running"] == 0
