@@ -1759,6 +1759,25 @@ static int run_batch(int n_jobs, const nce_ce_handle *hs, const nce_pt_state *st
         // jobs with small cells use (larger cells stay in global memory)
         size_t budget = n_jobs == 1 ? (size_t)((maxN + 15) / 16 * 16) : (size_t)48 * 1024;
         if (base + budget > limit) budget = n_jobs == 1 ? 0 : (limit > base ? (limit - base) / 16 * 16 : 0);
+        if (n_jobs == 1 && budget > 0 && cks[0].cluster <= 1) {
+            // one job: its occupancy goes on chip only while that costs no resident replicas; a cell that would
+            // push replicas into a second wave of CTAs stays in global memory (the kernel prefetches each next
+            // step's neighbourhoods into L2)
+            int dev = 0, smem_sm = 0, n_sm = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+            cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+            const int threads = warps * 32;
+            auto resident = [&](size_t dyn) -> int64_t {
+                const size_t per_cta = dyn + 5 * 1024 + 1024;          // + static shared memory and the reserve
+                int64_t b = (int64_t)(smem_sm / per_cta);
+                b = std::min<int64_t>(b, 65536 / (64 * threads));        // 64 registers a thread
+                b = std::min<int64_t>(b, 2048 / threads);
+                return b * n_sm;
+            };
+            if (smem_sm > 0 && n_sm > 0 && resident(base + budget) < total && resident(base) > resident(base + budget))
+                budget = 0;
+        }
         sig_smem = (int)budget;
         smem = base + budget;
     } else {
