@@ -337,8 +337,8 @@ int nce_tc_gemm(const float *A, const float *B, float *C, int32_t M, int32_t N, 
  * that does not, unless the earlier one has waited longer than starve_s); their state stays on the device until
  * they finish.  Two host worker threads drive the GPU: one advances the running CE jobs with persistent batch
  * launches on eight lanes (streams), a job joining the next launch on an idle lane as soon as its previous one has
- * completed (continuous batching without a global round), the other the NeuralCE jobs on a few streams, so the
- * two kinds overlap on the device.  A job's chunks depend only on its own parameters,
+ * completed (continuous batching without a global round), the other each NeuralCE job's next chunk as soon as its
+ * previous one has completed (a few streams), so the two kinds overlap on the device.  A job's chunks depend only on its own parameters,
  * so its result is the same alone and in any mix.  No call below waits for the device.
  * The reference has no serving mode; these entry points are new (they replace running neuralce-mc per job). */
 typedef struct nce_server *nce_server_handle;
@@ -401,7 +401,7 @@ typedef struct {
 typedef struct {
     int64_t queued, running, done, cancelled, failed;
     int64_t bytes_used, hbm_budget;
-    int64_t rounds_ce, rounds_nce;     /* CE batch launches completed; NeuralCE rounds (one chunk per running job) */
+    int64_t rounds_ce, rounds_nce;     /* CE batch launches completed; NeuralCE chunks completed */
     int64_t attempts;      /* swap attempts completed (replicas x steps) */
     double now;            /* server clock */
 } nce_server_stats;

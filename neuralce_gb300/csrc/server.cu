@@ -1,5 +1,5 @@
 // Job server of libnce_gb300 (serving form): admission by a device-memory budget, continuous batching of CE
-// jobs into persistent batch launches on a few lanes, NeuralCE jobs on side streams, all state resident on the
+// jobs into persistent batch launches on a few lanes, NeuralCE jobs chunk by chunk on side streams, all state resident on the
 // device while a job runs.  Host code only; the device work is the engines' own entry points.
 //
 // Threads: the caller's threads only touch host structures under `mu` (submit, poll, cancel, query never wait
@@ -7,7 +7,8 @@
 // copied to the caller's host buffers, device memory returned with cudaFreeAsync) on its own stream, so neither
 // stalls the device work; the CE thread keeps eight lanes (streams) of persistent batch launches busy with the
 // running CE jobs (up to max_batch jobs per launch; a job joins the next launch as soon as its previous one has
-// completed), the NeuralCE thread one chunk per running NeuralCE job per round on `nce_streams` streams.
+// completed), the NeuralCE thread each running NeuralCE job's next chunk as soon as its previous one has completed
+// (jobs spread over `nce_streams` streams, jobs of one model on one stream).
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -45,7 +46,10 @@ struct SJob {
     nce_pt_state st{};
     nce_nce_state nst{};
     int32_t chunks = 0, anchor = 1;
-    bool inflight = false;            // CE: part of a launch that has not completed (CE thread only)
+    bool inflight = false;            // part of a launch that has not completed (its worker thread only)
+    int64_t pending_steps = 0;        // NeuralCE: steps of the chunk in flight
+    cudaEvent_t ev = nullptr;         // NeuralCE: completion of the job's chunk in flight
+    ~SJob() { if (ev) cudaEventDestroy(ev); }
     cudaStream_t stream = nullptr;
 };
 
@@ -104,7 +108,7 @@ struct nce_server {
     int64_t n_done = 0, n_cancelled = 0, n_failed = 0, rounds[2] = {0, 0};
     std::atomic<int64_t> attempts{0};
     std::atomic<bool> stop{false};
-    std::thread worker[4];                           // CE rounds, NeuralCE rounds, CE io, NeuralCE io
+    std::thread worker[4];                           // CE launches, NeuralCE chunks, CE io, NeuralCE io
     std::chrono::steady_clock::time_point t0;
     cudaStream_t io_streams[2] = {nullptr, nullptr};
     std::vector<cudaStream_t> ce_streams, nce_streams;
@@ -356,21 +360,6 @@ void io_worker(nce_server *S, int kind) {
     }
 }
 
-// running jobs of `kind` for the next round (cancelled ones go to the io thread); false when the server stops
-bool take_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &run) {
-    std::unique_lock<std::mutex> lk(S->mu);
-    for (;;) {
-        if (S->stop) return false;
-        auto &a = S->active[kind];
-        for (auto it = a.begin(); it != a.end();) {
-            if ((*it)->cancel) { S->retiring[kind].push_back(*it); it = a.erase(it); }
-            else ++it;
-        }
-        if (!a.empty()) { run = a; return true; }
-        S->wake.wait_for(lk, std::chrono::milliseconds(2));
-    }
-}
-
 void end_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &run) {
     std::lock_guard<std::mutex> lk(S->mu);
     ++S->rounds[kind];
@@ -506,33 +495,75 @@ void ce_worker(nce_server *S) {
     }
 }
 
-// NeuralCE thread: every running job advances one chunk per round on its stream
+// NeuralCE thread: every running job's next chunk (and its periodic full-cache rebuild) is launched on the job's
+// stream as soon as its previous chunk has completed (event query), so jobs of different sizes never wait for one
+// another; jobs on one model share a stream, which orders their use of the model's step scratch.
 void nce_worker(nce_server *S) {
     cudaSetDevice(S->device);
-    std::vector<std::shared_ptr<SJob>> run;
-    while (take_round(S, 1, run)) {
-        int rc = NCE_OK;
-        for (auto &p : run) {
+    std::vector<std::shared_ptr<SJob>> mine, idle;     // jobs with a chunk in flight; jobs ready for the next one
+    for (;;) {
+        bool moved = false;
+        // 1. completed chunks
+        for (size_t i = 0; i < mine.size();) {
+            auto p = mine[i];
+            const cudaError_t e = cudaEventQuery(p->ev);
+            if (e == cudaErrorNotReady) { ++i; continue; }
+            moved = true;
+            p->inflight = false;
+            std::vector<std::shared_ptr<SJob>> one{p};
+            if (e != cudaSuccess) {
+                fail_round(S, 1, one, fail(NCE_ERR_CUDA, "NeuralCE chunk: %s", cudaGetErrorString(e)));
+            } else {
+                p->done += p->pending_steps;
+                S->attempts += p->pending_steps * p->d.R;
+                end_round(S, 1, one);
+            }
+            mine[i] = mine.back(); mine.pop_back();
+        }
+        // 2. running jobs without a chunk in flight (cancelled ones leave for the io thread)
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            if (S->stop && mine.empty()) break;
+            auto &a = S->active[1];
+            idle.clear();
+            for (auto it = a.begin(); it != a.end();) {
+                auto &p = *it;
+                if (p->inflight) { ++it; continue; }
+                if (p->cancel) { S->retiring[1].push_back(p); it = a.erase(it); S->wake.notify_all(); continue; }
+                if (!S->stop) idle.push_back(p);
+                ++it;
+            }
+            if (idle.empty() && mine.empty() && !moved) {
+                S->wake.wait_for(lk, std::chrono::milliseconds(2));
+                continue;
+            }
+        }
+        // 3. the next chunk of each of them
+        bool launched = false;
+        for (auto &p : idle) {
             SJob &j = *p;
+            int rc = NCE_OK;
+            if (!j.ev && cudaEventCreateWithFlags(&j.ev, cudaEventDisableTiming) != cudaSuccess)
+                rc = fail(NCE_ERR_CUDA, "NeuralCE chunk: event creation");
             nce_nce_chunk c; std::memset(&c, 0, sizeof(c));
             c.n_steps = chunk_len(j); c.step0 = j.done; c.seed = j.d.seed; c.sample_interval = 1;
             c.exchange_rounds = ((j.done + c.n_steps) % j.d.exchange_every) == 0 ? 1 : 0;
             c.cluster = S->cfg.nce_cluster;
-            rc = nce_nce_run_chunk((nce_nce_handle)j.d.model, &j.nst, &c, j.stream);
-            if (rc) break;
-            ++j.chunks;
-            if (j.chunks % j.anchor == 0) { rc = nce_nce_full_cache((nce_nce_handle)j.d.model, &j.nst, j.stream); if (rc) break; }
-            j.done += c.n_steps;
-            S->attempts += c.n_steps * j.d.R;
-        }
-        if (rc == NCE_OK)
-            for (cudaStream_t s : S->nce_streams) {
-                const cudaError_t e = cudaStreamSynchronize(s);
-                if (e != cudaSuccess) { rc = fail(NCE_ERR_CUDA, "NeuralCE round: %s", cudaGetErrorString(e)); break; }
+            if (!rc) rc = nce_nce_run_chunk((nce_nce_handle)j.d.model, &j.nst, &c, j.stream);
+            if (!rc && ++j.chunks % j.anchor == 0) rc = nce_nce_full_cache((nce_nce_handle)j.d.model, &j.nst, j.stream);
+            if (!rc && cudaEventRecord(j.ev, j.stream) != cudaSuccess) rc = fail(NCE_ERR_CUDA, "NeuralCE chunk: event record");
+            if (rc) {
+                cudaStreamSynchronize(j.stream);           // what was enqueued may still run
+                std::vector<std::shared_ptr<SJob>> one{p};
+                fail_round(S, 1, one, rc);
+                continue;
             }
-        if (rc) { fail_round(S, 1, run, rc); continue; }
-        end_round(S, 1, run);
+            j.pending_steps = c.n_steps; j.inflight = true;
+            mine.push_back(p); launched = true;
+        }
+        if (!launched && !moved) std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
+    for (auto &p : mine) cudaEventSynchronize(p->ev);
 }
 
 }  // namespace

@@ -4,8 +4,8 @@ libnce_gb300).
 Jobs of different cells, replica counts, compositions and models (CE or NeuralCE) are submitted while others run;
 the server admits them in submission order as device memory within its budget frees up, keeps their state on
 the device, advances the running CE jobs with persistent batch launches on eight lanes (a job joins the next
-launch on an idle lane as soon as its previous one has completed: continuous batching) and the NeuralCE jobs on
-side streams, and copies each job's final state into host arrays when it finishes.  A job's
+launch on an idle lane as soon as its previous one has completed: continuous batching) and each NeuralCE job chunk
+by chunk on side streams, and copies each job's final state into host arrays when it finishes.  A job's
 chunks (exchange interval, Philox key and global step of every chunk) depend only on its own parameters, so its
 result is the same alone and in any mix.  The reference has no serving mode: a job here is one
 ``run_pt_mcmc`` call (``neuralce/ce/pt_mcmc_ce.py:587-601``) or NeuralCE ``_run_replicas``
