@@ -451,15 +451,16 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     __shared__ BinProp prop[64];                      // ring of two batches of 32 proposals
     __shared__ int32_t near_flag[2];                  // per evaluated-swap parity
     // CLUSTER: one replica per thread-block cluster; every CTA keeps its own copy of the replica's occupancy and draws
-    // the same proposals, and the row chunks are split over the CTAs.  Fixed point (float64): every warp adds its
-    // chunks' exact partial dE into the evaluated swap's accumulator of every CTA of the cluster (a local shared
-    // atomic without a cluster), and after the barrier every warp of every CTA reads the total and reaches the same
-    // decision; the accumulators alternate between evaluated swaps and each CTA clears its previous one after the
-    // next step's first barrier.  The accepted swap is written to the occupancy by one thread; until the next
-    // barrier every thread reads the two sites through the swap it holds in registers, so no barrier follows the
-    // decision.  float32: each CTA counts its chunks per column, after the barrier the decision warp reads all
-    // CTAs' counts (through distributed shared memory with a cluster) and sums the columns in a fixed order, and a
-    // barrier ends the step; a count buffer is cleared by its owner only after the next cluster barrier.
+    // the same proposals, and the row chunks are split over the CTAs.  With a cluster in fixed point (float64):
+    // every warp adds its chunks' exact partial dE into the evaluated swap's accumulator of every CTA of the
+    // cluster, and after the cluster barrier every warp of every CTA reads the total and reaches the same decision;
+    // the accumulators alternate between evaluated swaps and each CTA clears its previous one after the next step's
+    // first barrier.  The accepted swap is written to the occupancy by one thread; until the next barrier every
+    // thread reads the two sites through the swap it holds in registers, so no barrier follows the decision.
+    // Otherwise (one CTA per replica, or float32): each CTA counts its chunks per column, after the barrier the
+    // decision warp sums the columns in a fixed order (reading every CTA's counts through distributed shared memory
+    // with a cluster), and a barrier ends the evaluated step; a count buffer is cleared by its owner only after the
+    // next cluster barrier.
     int CL = 1, rank = 0;
     if (CLUSTER) { cg::cluster_group cl = cg::this_cluster(); CL = (int)cl.num_blocks(); rank = (int)cl.block_rank(); }
     const int rep_idx = blockIdx.x / CL;
