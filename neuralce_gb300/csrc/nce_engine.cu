@@ -534,6 +534,7 @@ __device__ void layer_tiles(const NceJob &jb, int lvl, const LayerW &LW, const f
             }
             umma::fence_before();
             __syncthreads();
+#pragma unroll 8
             for (int i = 0; i < MS; ++i) {
                 const int mm = sg + i * SG;
                 const float4 y = *reinterpret_cast<const float4 *>(Y + (size_t)mm * YS + cg * 4);
@@ -1008,18 +1009,22 @@ __device__ void nce_step(const NceJob &jb, int r, int t, int64_t s_idx, NceCtl &
                         }, rank, CL, tc);
             csync<CLUSTER>();
         } else {
+            // the sink's reads and writes do not alias (caches, the step's new rows, the new site energies): the
+            // loads of one tile site may run ahead of the stores of the previous one
+            const float *__restrict__ e_r = e, *__restrict__ h0_r = h0, *__restrict__ nb0_r = nb0;
+            float *__restrict__ en_r = en;
             layer_tiles(jb, lvl, LWs[lvl], cache, newl, slot, ctl.nl[lvl], list, 0, nout, nullptr, X, src,
                         [&](int64_t pos, int c0, const float *v, int32_t site, int32_t p0) {
                             // the tile passes the site and its slot value (read while building the tile)
                             const float *hr = nullptr;
                             const int64_t st = site;
-                            if (pos >= 0) hr = (p0 >= 0 && p0 < n0) ? nb0 + (size_t)p0 * m.C0 : h0 + (size_t)st * m.C0;
+                            if (pos >= 0) hr = (p0 >= 0 && p0 < n0) ? nb0_r + (size_t)p0 * m.C0 : h0_r + (size_t)st * m.C0;
                             const float tot = site_energy(v, c0, hw, hr, lin, m.C0, ncg);
                             if (pos >= 0 && c0 == 0) {
-                                const bool active = m.Mb[st % m.nB] > 1;
+                                const bool active = m.Mb[site % m.nB] > 1;
                                 const float ev = active ? tot : 0.f;
-                                en[pos] = ev;
-                                dloc += (unsigned long long)llrint(((double)ev - (double)e[st]) * kFix);
+                                en_r[pos] = ev;
+                                dloc += (unsigned long long)llrint(((double)ev - (double)e_r[st]) * kFix);
                             }
                         }, rank, CL, tc);
         }
