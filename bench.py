@@ -43,6 +43,7 @@ B_GATHER = 14_996                     # bytes of member occupancy per attempt, c
 # keyed by (path, L, R, steps per chunk): profiles/ holds the capture (a 1000-step chunk; the tables and occupancy
 # are read once per launch, so the figure does not grow with the steps)
 TRAFFIC = {(2, 8, 32, 5000): 166_400}
+SMEM_PIPE = {(2, 8, 32, 5000): 0.150}       # the same capture's shared-memory wavefronts, fraction of the pipe's peak
 
 
 def parse():
@@ -760,13 +761,15 @@ def main():
     ms_chunk = float(np.mean(per_ms))
     achieved = R * T * B_GATHER / (ms_chunk / 1e3) / 1e9
     # DRAM bytes per launch from one ncu capture of this workload (dram__bytes_read.sum + dram__bytes_write.sum of
-    # ce_bin_chunk_kernel, 2,048 sites, R = 32, 5,000 steps, 16 warps x 8 CTAs): the tables and occupancies live in
-    # shared memory
+    # ce_bin_chunk_kernel, 2,048 sites, R = 32, 16 warps x 4 CTAs): the tables and occupancies live in shared memory;
+    # the same capture's shared-memory pipe use (l1tex__data_pipe_lsu_wavefronts_mem_shared.sum.pct_of_peak_sustained
+    # _elapsed), the on-chip roofline that the gathered bytes actually meet
     traffic = TRAFFIC.get((args.path, args.L, args.R, T))
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
             "kernel": {1: "ce_pt_chunk_kernel", 3: "ce_lf_chunk_kernel"}.get(args.path, "ce_bin_chunk_kernel"),
             "peak_source": src,
-            "algorithmic_bytes_per_launch": R * T * B_GATHER}
+            "algorithmic_bytes_per_launch": R * T * B_GATHER,
+            "shared_pipe_frac_ncu": SMEM_PIPE.get((args.path, args.L, args.R, T))}
     nce_line = nce_tc_line = nce_bf16_line = nce_shipped_line = None
     if rank == 0 and args.nce_steps > 0:
         nce_line = bench_nce(steps=args.nce_steps)
