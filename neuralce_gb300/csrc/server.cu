@@ -282,12 +282,15 @@ void io_worker(nce_server *S, int kind) {
     cudaStream_t ios = S->io_streams[kind];
     for (;;) {
         std::vector<std::shared_ptr<SJob>> fresh, out;
+        std::vector<char> cx;                        // cancelled when taken: a later cancel no longer applies
         {
             std::unique_lock<std::mutex> lk(S->mu);
             for (;;) {
                 if (S->stop) return;
                 out.assign(S->retiring[kind].begin(), S->retiring[kind].end());
                 S->retiring[kind].clear();
+                cx.clear();
+                for (auto &p : out) cx.push_back(p->cancel ? 1 : 0);
                 fresh = admit_locked(S, kind);
                 if (!out.empty() || !fresh.empty()) break;
                 S->wake.wait_for(lk, std::chrono::milliseconds(2));
@@ -296,20 +299,20 @@ void io_worker(nce_server *S, int kind) {
         // retire: every finished job's outputs queued on the io stream, one synchronisation, then each job's flags
         std::vector<int> frc(out.size(), NCE_OK);
         for (size_t k = 0; k < out.size(); ++k)
-            if (!out[k]->cancel) frc[k] = finish(*out[k], ios);
+            if (!cx[k]) frc[k] = finish(*out[k], ios);
         if (!out.empty()) {
             const cudaError_t e = cudaStreamSynchronize(ios);
             for (size_t k = 0; k < out.size(); ++k)
-                if (!out[k]->cancel && frc[k] == NCE_OK)
+                if (!cx[k] && frc[k] == NCE_OK)
                     frc[k] = e != cudaSuccess ? fail(NCE_ERR_CUDA, "retiring a job: %s", cudaGetErrorString(e)) : finish_check(*out[k]);
         }
         for (size_t k = 0; k < out.size(); ++k) {
             SJob &j = *out[k];
             int rc = frc[k];
-            if (j.cancel) drop(j, ios);
+            if (cx[k]) drop(j, ios);
             std::lock_guard<std::mutex> lk(S->mu);
             j.dev = reinterpret_cast<char *>(1);
-            if (j.cancel) {
+            if (cx[k]) {
                 release_locked(S, j, NCE_JOB_CANCELLED);
             } else if (rc) {
                 j.error = rc; j.msg = last_error();
@@ -360,10 +363,15 @@ void io_worker(nce_server *S, int kind) {
     }
 }
 
-void end_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &run) {
+// a completed launch: its jobs advance by `steps` (under the lock, where polls read them); finished jobs retire
+void end_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &run, const std::vector<int64_t> &steps) {
     std::lock_guard<std::mutex> lk(S->mu);
     ++S->rounds[kind];
     auto &a = S->active[kind];
+    for (size_t i = 0; i < run.size(); ++i) {
+        run[i]->done += steps[i];
+        S->attempts += steps[i] * run[i]->d.R;
+    }
     for (auto &p : run)
         if (p->done >= p->d.n_steps) {
             a.erase(std::remove(a.begin(), a.end(), p), a.end());
@@ -372,7 +380,10 @@ void end_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &run)
     S->wake.notify_all();
 }
 
-void fail_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &jobs, int rc) {
+// fail the jobs of a launch that could not be made or did not complete; `s` (the launch's stream) has nothing of
+// theirs left in flight.  Their device memory is given back on it (after a device fault that call fails too, and
+// the memory stays with the broken context).
+void fail_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &jobs, int rc, cudaStream_t s) {
     std::string m = last_error();
     std::lock_guard<std::mutex> lk(S->mu);
     auto &a = S->active[kind];
@@ -380,7 +391,8 @@ void fail_round(nce_server *S, int kind, std::vector<std::shared_ptr<SJob>> &job
         if (p->status != NCE_JOB_RUNNING) continue;
         p->error = rc; p->msg = m;
         a.erase(std::remove(a.begin(), a.end(), p), a.end());
-        release_locked(S, *p, NCE_JOB_FAILED);        // device memory stays with the failed context
+        if (p->dev && p->dev != reinterpret_cast<char *>(1)) cudaFreeAsync(p->dev, s);
+        release_locked(S, *p, NCE_JOB_FAILED);
     }
 }
 
@@ -417,13 +429,9 @@ void ce_worker(nce_server *S) {
             ln.busy = false; moved = true;
             for (auto &p : ln.jobs) p->inflight = false;
             if (e != cudaSuccess) {
-                fail_round(S, 0, ln.jobs, fail(NCE_ERR_CUDA, "CE launch: %s", cudaGetErrorString(e)));
+                fail_round(S, 0, ln.jobs, fail(NCE_ERR_CUDA, "CE launch: %s", cudaGetErrorString(e)), ln.s);
             } else {
-                for (size_t i = 0; i < ln.jobs.size(); ++i) {
-                    ln.jobs[i]->done += ln.steps[i];
-                    S->attempts += ln.steps[i] * ln.jobs[i]->d.R;
-                }
-                end_round(S, 0, ln.jobs);
+                end_round(S, 0, ln.jobs, ln.steps);
             }
             ln.jobs.clear(); ln.steps.clear();
         }
@@ -479,7 +487,7 @@ void ce_worker(nce_server *S) {
                 if (rc) {
                     // what was enqueued may still run: wait for the lane before the jobs' memory is given back
                     cudaStreamSynchronize(ln->s);
-                    fail_round(S, 0, js, rc);
+                    fail_round(S, 0, js, rc, ln->s);
                     continue;
                 }
                 ln->busy = true; launched = true;
@@ -512,11 +520,9 @@ void nce_worker(nce_server *S) {
             p->inflight = false;
             std::vector<std::shared_ptr<SJob>> one{p};
             if (e != cudaSuccess) {
-                fail_round(S, 1, one, fail(NCE_ERR_CUDA, "NeuralCE chunk: %s", cudaGetErrorString(e)));
+                fail_round(S, 1, one, fail(NCE_ERR_CUDA, "NeuralCE chunk: %s", cudaGetErrorString(e)), p->stream);
             } else {
-                p->done += p->pending_steps;
-                S->attempts += p->pending_steps * p->d.R;
-                end_round(S, 1, one);
+                end_round(S, 1, one, {p->pending_steps});
             }
             mine[i] = mine.back(); mine.pop_back();
         }
@@ -555,7 +561,7 @@ void nce_worker(nce_server *S) {
             if (rc) {
                 cudaStreamSynchronize(j.stream);           // what was enqueued may still run
                 std::vector<std::shared_ptr<SJob>> one{p};
-                fail_round(S, 1, one, rc);
+                fail_round(S, 1, one, rc, j.stream);
                 continue;
             }
             j.pending_steps = c.n_steps; j.inflight = true;
