@@ -385,6 +385,7 @@ struct BinProp {
     int32_t ka[3], kb[3], ba, bb;
 };
 
+constexpr int kBinNchTab = 64;                          // bases up to which the chunk counts are kept on chip
 struct BinLayout {
     size_t bix, chunk, nb, ecol, sig, bits, cnt, dcv, total;
     __host__ __device__ static BinLayout make(int nB, int J, int mo, int n_nbr, int n_pfc, int n_cols, int max_chunks, size_t acc_bytes,
@@ -492,6 +493,9 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
     }
     uint32_t *chunks = reinterpret_cast<uint32_t *>(smem + L.chunk);        // [basis][k]: col | start << 8 | len << 24
     for (int i = tid; i < jb.nB * jb.max_chunks; i += nt) chunks[i] = __ldg(jb.chunks + i);
+    // chunks per basis site, read by every evaluated swap: from shared memory, not a global load on the step's path
+    __shared__ uint16_t nch[kBinNchTab];
+    for (int i = tid; i < jb.nB && i < kBinNchTab; i += nt) nch[i] = (uint16_t)__ldg(jb.n_chunks + i);
     int4 *nbt = reinterpret_cast<int4 *>(smem + L.nb);                          // [basis][n]: (uo0, uo1, uo2, basis)
     for (int i = tid; i < jb.nB * n_nbr; i += nt) nbt[i] = make_int4(__ldg(jb.nb_uo + 3 * i), __ldg(jb.nb_uo + 3 * i + 1),
                                                                       __ldg(jb.nb_uo + 3 * i + 2), __ldg(jb.nb_b + i));
@@ -606,7 +610,8 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                 // per-side bases held in registers for the loop (shared-memory atomics below could alias the
                 // descriptor and proposal, which would otherwise be re-read every chunk)
                 const int ba = P.ba, bb = P.bb;
-                const int nca = __ldg(jb.n_chunks + ba), ncb = __ldg(jb.n_chunks + bb);
+                const int nca = jb.nB <= kBinNchTab ? (int)nch[ba] : __ldg(jb.n_chunks + ba);
+                const int ncb = jb.nB <= kBinNchTab ? (int)nch[bb] : __ldg(jb.n_chunks + bb);
                 const bool near = near_flag[par] != 0;
                 const int cw = nw > 1 ? warp : 0;
                 const int maxc = jb.max_chunks, J = jb.J;
@@ -661,7 +666,9 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
                         }
                     };
                     if (gstr >= 2) {
-                        const int wa = min(gstr - 1, max(1, (gstr * nca + (nca + ncb) / 2) / max(1, nca + ncb)));
+                        // (equal sides, as in every swap of a one-site basis: half the warps, without a division)
+                        const int wa = nca == ncb ? (gstr + 1) >> 1
+                                                  : min(gstr - 1, max(1, (gstr * nca + (nca + ncb) / 2) / max(1, nca + ncb)));
                         if (gw < wa) side_loop(std::false_type{}, nca, gw, wa);
                         else side_loop(std::true_type{}, ncb, gw - wa, gstr - wa);
                     } else {
