@@ -564,10 +564,11 @@ __global__ void __launch_bounds__(1024) ce_bin_chunk_kernel(const __grid_constan
         int32_t *cntp = cnt + par * n_cols;
         const uint32_t ia = (uint32_t)P.ia, ib = (uint32_t)P.ib;        // sites are below 2^32
         const int64_t thr = P.thr;
-        if (!sig_smem && s + 1 < n_steps) {
+        if (!sig_smem && s + 1 < n_steps && ((s + 1) & 31) != 0) {
             // occupancy in global memory (cells beyond the shared-memory budget): the next step's two
             // neighbourhoods are fetched into L2 while this step runs, one site a consumer thread (a step's first
-            // reads would otherwise wait on DRAM); the slot of step s + 1 is not refilled before step s + 33
+            // reads would otherwise wait on DRAM).  Only within a batch of 32 steps: the next batch's slots are
+            // visible after the barrier that opens it, and the slot of step s + 1 is not refilled before step s + 33
             const BinProp &Q = prop[(s + 1) & 63];
             for (int q = tid; q < 2 * n_nbr && tid < ncons * 32; q += ncons * 32) {
                 const int side = q >= n_nbr, n = side ? q - n_nbr : q;
