@@ -42,8 +42,8 @@ B_GATHER = 14_996                     # bytes of member occupancy per attempt, c
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of the headline kernel,
 # keyed by (path, L, R, steps per chunk): profiles/ holds the capture (a 1000-step chunk; the tables and occupancy
 # are read once per launch, so the figure does not grow with the steps)
-TRAFFIC = {(2, 8, 32, 5000): 166_400}
-SMEM_PIPE = {(2, 8, 32, 5000): 0.150}       # the same capture's shared-memory wavefronts, fraction of the pipe's peak
+TRAFFIC = {(2, 8, 32, 5000): 166_912}
+SMEM_PIPE = {(2, 8, 32, 5000): 0.178}       # the same capture's shared-memory wavefronts, fraction of the pipe's peak
 
 
 def parse():
